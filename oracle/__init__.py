@@ -1,0 +1,353 @@
+"""Oracle test infrastructure for the collision path. NOT part of the product.
+
+Two CPU implementations behind one Python interface:
+
+* ``port`` — ``oracle/port/imr_port.cpp``, a C++ restatement of the reference
+  engine's collision path (OBB fit, OBB-tree build, SAT traversal, Moller
+  narrow phase, contacts and uncollide rays), bit-identical in operation order.
+  It builds anywhere (``make -C oracle port``).
+* ``ref`` — the reference's own sources (inMyRoom_vulkan/src/Geometry/*.cpp,
+  src/CollisionDetection/*.cpp, eig3/eig3.cpp) compiled in place against the glm
+  shim by ``make -C oracle ref`` into ``oracle/_ref/``. Only available where the
+  reference checkout is.
+
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+may use this package, and only as the checker / baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT_DEFAULT = "/root/reference"
+
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+
+def build_port() -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+
+
+def build_ref(ref_root: str = REF_ROOT_DEFAULT) -> bool:
+    """Compiles the reference's own sources, if present. Returns availability."""
+    if not os.path.isdir(os.path.join(ref_root, "inMyRoom_vulkan", "src", "Geometry")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    return True
+
+
+def _declare(lib: C.CDLL, prefix: str) -> None:
+    vp = C.c_void_p
+    sz = C.c_size_t
+    f = lambda name: getattr(lib, prefix + name)  # noqa: E731
+    f("tree_build").restype = vp
+    f("tree_build").argtypes = [_f32p, sz, vp, _u32p, sz]
+    f("tree_free").argtypes = [vp]
+    f("tree_sizes").argtypes = [vp, C.POINTER(sz), C.POINTER(sz)]
+    f("tree_export").argtypes = [vp, _f32p, _f32p, _u32p, _u32p, _f32p, _f32p, _u32p]
+    f("relative_matrix").argtypes = [_f32p, _f32p, _f32p]
+    f("mid_phase").restype = vp
+    f("mid_phase").argtypes = [vp, vp, _f32p, _f32p]
+    f("mid_free").argtypes = [vp]
+    f("mid_count").restype = sz
+    f("mid_count").argtypes = [vp]
+    f("mid_get").argtypes = [vp, _u32p]
+    f("tri_tri").restype = C.c_int
+    f("tri_tri").argtypes = [_f32p, _f32p, C.POINTER(C.c_int), _f32p, _f32p]
+    f("transform_tri").argtypes = [_f32p, _f32p, _f32p]
+    f("sat").restype = C.c_int
+    f("sat").argtypes = [_f32p, _f32p]
+    f("surface").restype = C.c_float
+    f("surface").argtypes = [_f32p]
+    f("transform_box").argtypes = [_f32p, _f32p, _f32p]
+    f("obb_from_points").argtypes = [_f32p, sz, _f32p]
+    f("eig3").argtypes = [_f64p, _f64p, _f64p]
+    f("rays").argtypes = [vp, _f32p, _f32p, sz, sz, C.POINTER(sz), _f32p]
+    if prefix == "ref_":
+        f("narrow").restype = sz
+        f("narrow").argtypes = [vp, _u32p, _f32p, sz, C.POINTER(C.c_uint64)]
+        f("collide_batch").restype = C.c_uint64
+        f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int, C.POINTER(C.c_uint64)]
+    else:
+        f("narrow").restype = sz
+        f("narrow").argtypes = [vp, _u32p, _f32p, sz, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        f("tree_import").restype = vp
+        f("tree_import").argtypes = [_f32p, sz, _f32p, _u32p, _u32p, sz, _f32p, vp, vp]
+        f("tri_tri_ex").restype = C.c_int
+        f("tri_tri_ex").argtypes = [_f32p, _f32p, C.POINTER(C.c_int), C.POINTER(C.c_int), _f32p, _f32p]
+        f("contacts").restype = sz
+        f("contacts").argtypes = [vp, C.c_int, _u32p, _u32p, _f32p, sz]
+        f("collide_batch").restype = C.c_uint64
+        f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int,
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        f("collide_pairs").restype = sz
+        f("collide_pairs").argtypes = [vp, vp, _f32p, _f32p, sz, _u32p, _f32p, sz,
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+
+
+class FlatTree:
+    """A flattened OBB tree in the reference's node layout (OBBtree.h:61-75)."""
+
+    def __init__(self, root, node_obbs, node_ref, node_cnt, tri_pos, tri_nrm, tri_idx):
+        self.root = np.ascontiguousarray(root, np.float32).reshape(12)
+        self.node_obbs = np.ascontiguousarray(node_obbs, np.float32).reshape(-1, 2, 12)
+        self.node_ref = np.ascontiguousarray(node_ref, np.uint32).reshape(-1, 2)
+        self.node_cnt = np.ascontiguousarray(node_cnt, np.uint32).reshape(-1, 2)
+        self.tri_pos = np.ascontiguousarray(tri_pos, np.float32).reshape(-1, 9)
+        self.tri_nrm = np.ascontiguousarray(tri_nrm, np.float32).reshape(-1, 9)
+        self.tri_idx = np.ascontiguousarray(tri_idx, np.uint32).reshape(-1, 3)
+
+    @property
+    def n_nodes(self) -> int:
+        return self.node_obbs.shape[0]
+
+    @property
+    def n_tris(self) -> int:
+        return self.tri_pos.shape[0]
+
+    def arrays(self) -> dict:
+        return dict(root=self.root, node_obbs=self.node_obbs, node_ref=self.node_ref,
+                    node_cnt=self.node_cnt, tri_pos=self.tri_pos, tri_nrm=self.tri_nrm,
+                    tri_idx=self.tri_idx)
+
+    def equal(self, other: "FlatTree") -> bool:
+        a, b = self.arrays(), other.arrays()
+        return all(a[k].shape == b[k].shape and np.array_equal(a[k].view(np.uint32) if a[k].dtype == np.float32 else a[k],
+                                                            b[k].view(np.uint32) if b[k].dtype == np.float32 else b[k])
+                   for k in a)
+
+
+class Tree:
+    def __init__(self, impl: "Impl", handle: int):
+        self.impl, self.h = impl, handle
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.impl.fn("tree_free")(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def sizes(self):
+        n, t = C.c_size_t(), C.c_size_t()
+        self.impl.fn("tree_sizes")(self.h, C.byref(n), C.byref(t))
+        return n.value, t.value
+
+    def export(self) -> FlatTree:
+        n, t = self.sizes()
+        root = np.zeros(12, np.float32)
+        obbs = np.zeros((max(n, 1), 2, 12), np.float32)
+        ref = np.zeros((max(n, 1), 2), np.uint32)
+        cnt = np.zeros((max(n, 1), 2), np.uint32)
+        pos = np.zeros((max(t, 1), 9), np.float32)
+        nrm = np.zeros((max(t, 1), 9), np.float32)
+        idx = np.zeros((max(t, 1), 3), np.uint32)
+        self.impl.fn("tree_export")(self.h, root, obbs, ref, cnt, pos, nrm, idx)
+        return FlatTree(root, obbs[:n], ref[:n], cnt[:n], pos[:t], nrm[:t], idx[:t])
+
+
+class Mid:
+    def __init__(self, impl: "Impl", handle: int):
+        self.impl, self.h = impl, handle
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.impl.fn("mid_free")(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def leaf_pairs(self) -> np.ndarray:
+        n = self.impl.fn("mid_count")(self.h)
+        out = np.zeros((max(n, 1), 4), np.uint32)
+        self.impl.fn("mid_get")(self.h, out)
+        return out[:n]
+
+    def narrow(self):
+        """Colliding pairs (n,2) [tree-order indices], segments (n,6), tests, fragile."""
+        t = C.c_uint64()
+        fr = C.c_uint64()
+        dummy_p = np.zeros((1, 2), np.uint32)
+        dummy_s = np.zeros((1, 6), np.float32)
+        args = (C.byref(t),) if self.impl.prefix == "ref_" else (C.byref(t), C.byref(fr))
+        n = self.impl.fn("narrow")(self.h, dummy_p, dummy_s, 0, *args)
+        pairs = np.zeros((max(n, 1), 2), np.uint32)
+        segs = np.zeros((max(n, 1), 6), np.float32)
+        self.impl.fn("narrow")(self.h, pairs, segs, n, *args)
+        return pairs[:n], segs[:n], t.value, fr.value
+
+    def rays(self):
+        counts = (C.c_size_t * 2)()
+        avg = np.zeros(6, np.float32)
+        z = np.zeros((1, 6), np.float32)
+        self.impl.fn("rays")(self.h, z, z, 0, 0, counts, avg)
+        na, nb = counts[0], counts[1]
+        ra = np.zeros((max(na, 1), 6), np.float32)
+        rb = np.zeros((max(nb, 1), 6), np.float32)
+        self.impl.fn("rays")(self.h, ra, rb, na, nb, counts, avg)
+        return ra[:na], rb[:nb], avg
+
+    def contacts(self, side: int):
+        """(port only) per-triangle (index, mask, wsum xyz + weight), sorted by index."""
+        z32 = np.zeros(1, np.uint32)
+        zf = np.zeros((1, 4), np.float32)
+        n = self.impl.fn("contacts")(self.h, side, z32, z32, zf, 0)
+        idx = np.zeros(max(n, 1), np.uint32)
+        mask = np.zeros(max(n, 1), np.uint32)
+        f = np.zeros((max(n, 1), 4), np.float32)
+        self.impl.fn("contacts")(self.h, side, idx, mask, f, n)
+        return idx[:n], mask[:n], f[:n]
+
+
+def _f32(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a.reshape(-1) if n is None else a.reshape(n)
+
+
+class Impl:
+    def __init__(self, path: str, prefix: str):
+        self.lib = C.CDLL(path)
+        self.prefix = prefix
+        self.path = path
+        _declare(self.lib, prefix)
+
+    def fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    # --- trees
+    def tree_build(self, points, indices, normals=None) -> Tree:
+        pts = _f32(points)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        nrm = None if normals is None else _f32(normals)
+        h = self.fn("tree_build")(pts, pts.size // 3, None if nrm is None else nrm.ctypes.data, idx, idx.size)
+        t = Tree(self, h)
+        t._keep = nrm
+        return t
+
+    def tree_import(self, ft: FlatTree) -> Tree:
+        assert self.prefix == "port_"
+        h = self.fn("tree_import")(ft.root, ft.n_nodes, ft.node_obbs if ft.n_nodes else np.zeros(24, np.float32),
+                                   ft.node_ref if ft.n_nodes else np.zeros(2, np.uint32),
+                                   ft.node_cnt if ft.n_nodes else np.zeros(2, np.uint32),
+                                   ft.n_tris, ft.tri_pos, ft.tri_nrm.ctypes.data, ft.tri_idx.ctypes.data)
+        t = Tree(self, h)
+        t._keep = ft
+        return t
+
+    # --- queries
+    def relative_matrix(self, ma, mb) -> np.ndarray:
+        out = np.zeros(16, np.float32)
+        self.fn("relative_matrix")(_f32(ma, 16), _f32(mb, 16), out)
+        return out
+
+    def mid_phase(self, ta: Tree, tb: Tree, ma, mb) -> Mid:
+        return Mid(self, self.fn("mid_phase")(ta.h, tb.h, _f32(ma, 16), _f32(mb, 16)))
+
+    # --- primitives
+    def tri_tri(self, a, b):
+        cop = C.c_int()
+        s = np.zeros(3, np.float32)
+        t = np.zeros(3, np.float32)
+        hit = self.fn("tri_tri")(_f32(a, 9), _f32(b, 9), C.byref(cop), s, t)
+        return hit, cop.value, s, t
+
+    def transform_tri(self, m, a):
+        out = np.zeros(9, np.float32)
+        self.fn("transform_tri")(_f32(m, 16), _f32(a, 9), out)
+        return out
+
+    def sat(self, a, b) -> int:
+        return self.fn("sat")(_f32(a, 12), _f32(b, 12))
+
+    def surface(self, a) -> float:
+        return self.fn("surface")(_f32(a, 12))
+
+    def transform_box(self, m, a):
+        out = np.zeros(12, np.float32)
+        self.fn("transform_box")(_f32(m, 16), _f32(a, 12), out)
+        return out
+
+    def obb_from_points(self, pts):
+        p = _f32(pts)
+        out = np.zeros(12, np.float32)
+        self.fn("obb_from_points")(p, p.size // 3, out)
+        return out
+
+    def eig3(self, a):
+        a = np.ascontiguousarray(a, np.float64).reshape(9)
+        v = np.zeros(9, np.float64)
+        d = np.zeros(3, np.float64)
+        self.fn("eig3")(a, v, d)
+        return v.reshape(3, 3), d
+
+    def collide_batch(self, trees_a, trees_b, mats_a, mats_b, threads=1):
+        n = len(trees_a)
+        ha = (C.c_void_p * n)(*[t.h for t in trees_a])
+        hb = (C.c_void_p * n)(*[t.h for t in trees_b])
+        ma = _f32(mats_a)
+        mb = _f32(mats_b)
+        rays = C.c_uint64()
+        if self.prefix == "ref_":
+            tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(rays))
+            return dict(tests=tests, rays=rays.value)
+        hits = C.c_uint64()
+        tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(hits), C.byref(rays))
+        return dict(tests=tests, hits=hits.value, rays=rays.value)
+
+    def collide_pairs(self, trees_a, trees_b, mats_a, mats_b):
+        """(port) all colliding pairs of a batch: (n,3) [query, ia, ib], (n,6) segs, tests, leaf pairs."""
+        n = len(trees_a)
+        ha = (C.c_void_p * n)(*[t.h for t in trees_a])
+        hb = (C.c_void_p * n)(*[t.h for t in trees_b])
+        ma = _f32(mats_a)
+        mb = _f32(mats_b)
+        t = C.c_uint64()
+        lp = C.c_uint64()
+        z = np.zeros((1, 3), np.uint32)
+        zs = np.zeros((1, 6), np.float32)
+        cnt = self.fn("collide_pairs")(ha, hb, ma, mb, n, z, zs, 0, C.byref(t), C.byref(lp))
+        pairs = np.zeros((max(cnt, 1), 3), np.uint32)
+        segs = np.zeros((max(cnt, 1), 6), np.float32)
+        self.fn("collide_pairs")(ha, hb, ma, mb, n, pairs, segs, cnt, C.byref(t), C.byref(lp))
+        return pairs[:cnt], segs[:cnt], t.value, lp.value
+
+
+_cache: dict = {}
+
+
+def port(fast: bool = False) -> Impl:
+    key = ("port", fast)
+    if key not in _cache:
+        name = "liboracle_port_fast.so" if fast else "liboracle_port.so"
+        path = os.path.join(HERE, "_build", name)
+        if not os.path.exists(path):
+            build_port()
+        _cache[key] = Impl(path, "port_")
+    return _cache[key]
+
+
+def ref(fast: bool = False, ref_root: str = REF_ROOT_DEFAULT):
+    """The reference's own code compiled here, or None when the reference is absent."""
+    key = ("ref", fast)
+    if key not in _cache:
+        name = "libimr_ref_fast.so" if fast else "libimr_ref_strict.so"
+        path = os.path.join(HERE, "_ref", name)
+        if not os.path.exists(path):
+            try:
+                if not build_ref(ref_root):
+                    return None
+            except subprocess.CalledProcessError:
+                return None
+        try:
+            _cache[key] = Impl(path, "ref_")
+        except OSError:
+            return None
+    return _cache[key]
