@@ -1,0 +1,330 @@
+"""Benchmark of the GB300 collision path on the 256-entity scene.
+
+One step = one batched collide launch (CUDA graph: counter reset, query
+packing, persistent traversal with the fused triangle-pair narrow phase) over
+every entity pair of the scene whose world AABBs overlap. The metric is
+triangle-pair tests per second (Moller calls on candidate leaf pairs), with
+collision queries per second beside it.
+
+  python bench.py [--gpus N --steps K --warmup W]      # GPU arm
+  python bench.py --impl reference [...]                # the reference's CPU path
+
+value: device-resident inputs, each step timed with CUDA events on the
+launching stream, L2 flushed (a 512 MB write) between steps.
+e2e: the public host API (cg_collide with host queries + read-back of the
+colliding pairs), host-timed around the synchronous calls.
+roofline: the traversal kernel, algorithmic bytes (node pairs x 96 B of box
+data + triangle tests x 72 B of triangle data) per launch over its event-timed
+duration, against the measured copy bandwidth; the FP32 view beside it.
+cpu_baseline: the oracle restatement of the reference's CPU path (release
+flags) on all host cores over a bounded number of scene steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tri-pair tests/s & collision queries/s, 1 GB300 (batched vs plain), bwd ms"
+UNIT = "tri-pair tests/s"
+WORKLOAD = "scene: 256 rigid entities (500-20,000 tris, log-uniform), AABB-overlap pairs, batched launch"
+# per-unit algorithmic figures (source-level op counts of the reference path)
+NODE_PAIR_BYTES = 2 * 48   # two boxes
+TRI_TEST_BYTES = 2 * 36    # two triangles
+NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
+TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "sm_max_mhz": d.get("sm_max_mhz", 2070.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 9 for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def build_scene(seed: int):
+    import oracle
+    from inmyroom_vulkan_gb300 import scenes
+
+    sc = scenes.scene(seed=seed)
+    port = oracle.port()
+    trees = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    return sc, trees
+
+
+def cpu_baseline(sc, seconds: float = 10.0) -> dict:
+    """The oracle restatement (release flags) on all host cores over whole scene steps."""
+    import oracle
+
+    fast = oracle.port(fast=True)
+    trees = [fast.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+    ta, tb = [trees[i] for i in qa], [trees[j] for j in qb]
+    ma, mb = sc.mats[qa], sc.mats[qb]
+    cores = os.cpu_count() or 1
+    fast.collide_batch(ta, tb, ma, mb, threads=cores)  # warm
+    steps, tests, t0 = 0, 0, time.perf_counter()
+    while True:
+        r = fast.collide_batch(ta, tb, ma, mb, threads=cores)
+        steps += 1
+        tests += r["tests"]
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 200:
+            break
+    t1 = time.perf_counter()
+    r1 = fast.collide_batch(ta, tb, ma, mb, threads=1)
+    single = time.perf_counter() - t1
+    return {"value": tests / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} whole scene steps ({len(qa)} queries each), {el:.1f} s, release flags",
+            "single_thread_value": r1["tests"] / single, "steps": steps}
+
+
+def run_reference(args) -> dict:
+    """`--impl reference`: the reference's CPU path on the host cores. The
+    reference compiled from its own sources (oracle/_ref) where it exists,
+    else the oracle restatement of it."""
+    import oracle
+    from inmyroom_vulkan_gb300 import scenes
+
+    sc = scenes.scene(seed=1002)
+    impl, kind = oracle.ref(fast=True), "reference"
+    if impl is None:
+        impl, kind = oracle.port(fast=True), "port"
+    trees = [impl.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+    ta, tb = [trees[i] for i in qa], [trees[j] for j in qb]
+    ma, mb = sc.mats[qa], sc.mats[qb]
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        impl.collide_batch(ta, tb, ma, mb, threads=cores)
+    tests, t0 = 0, time.perf_counter()
+    for _ in range(args.steps):
+        tests += impl.collide_batch(ta, tb, ma, mb, threads=cores)["tests"]
+    el = time.perf_counter() - t0
+    v = tests / el
+    return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded PCG64, seed 1002)",
+            "config": {"workload": WORKLOAD, "queries": int(len(qa)), "cache": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{args.steps} whole scene steps, release flags"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_gpu(args) -> dict:
+    import torch
+
+    from inmyroom_vulkan_gb300 import capi, scenes
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    # each rank collides its own scene replica (weak scaling, no data exchange)
+    sc, trees = build_scene(seed=1002 + 1000 * rank)
+    ctx = capi.Context(device=local, max_queries=max(4096, len(sc.pairs)), max_tri_pairs=1 << 22)
+    ids = np.array([ctx.upload_flat(t.export()) for t in trees], np.uint32)
+    qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+    rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
+    q = capi.make_queries(ids[qa], ids[qb], rel)
+    n = len(q)
+
+    d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
+    torch.cuda.synchronize()
+    ctx.graph_capture(d_q.data_ptr(), n)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    st = None
+    for _ in range(max(args.warmup, 3)):
+        ctx.graph_launch(stream.cuda_stream)
+    st = ctx.sync_stats()
+    tests_per_step, pairs_per_step = st["tri_tests"], st["tri_pairs"]
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kernel_ms = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            starts[k].record(stream)
+            ctx.graph_launch(stream.cuda_stream)
+            ends[k].record(stream)
+            kernel_ms.append(ctx.traversal_ms())
+        torch.cuda.synchronize()
+        step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        st = ctx.sync_stats()
+        assert st["tri_tests"] == tests_per_step and st["status"] == 0
+
+        # end to end through the public host API: host queries in, pairs out
+        e2e_times = []
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.collide(q)
+            pairs = ctx.tri_pairs()
+            e2e_times.append(time.perf_counter() - t0)
+        assert len(pairs) == pairs_per_step
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * tests_per_step * args.steps / (total_ms / 1e3)
+    e2e_s = float(np.sum(e2e_times))
+    e2e_value = world * tests_per_step * args.steps / e2e_s
+
+    peaks = measured_peaks()
+    kms = float(np.mean(kernel_ms))
+    alg_bytes = st["node_pairs"] * NODE_PAIR_BYTES + st["tri_tests"] * TRI_TEST_BYTES
+    alg_flops = st["node_pairs"] * NODE_PAIR_FLOPS + st["tri_tests"] * TRI_TEST_FLOPS
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * peaks["sm_max_mhz"] * 1e6 / 1e12
+
+    # plain path: the rigid pair, one query per launch (the reference's unit of work)
+    rp = scenes.rigid_pair(n_poses=200)
+    import oracle
+
+    port = oracle.port()
+    pt = [port.tree_build(m.points, m.indices, m.normals) for m in (rp.mesh_a, rp.mesh_b)]
+    pid = [ctx.upload_flat(t.export()) for t in pt]
+    prel = np.stack([capi.relative_matrix(a, b) for a, b in zip(rp.mats_a, rp.mats_b)])
+    pq = capi.make_queries(np.full(200, pid[0]), np.full(200, pid[1]), prel)
+    d_pq = torch.from_numpy(pq.view(np.uint8).copy()).to(dev)
+    qsz = capi.QUERY_DTYPE.itemsize
+    for i in range(5):
+        ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, 0, stream.cuda_stream)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    ptests = 0
+    for i in range(200):
+        ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, 0, stream.cuda_stream)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = s0.elapsed_time(s1)
+    ctx.collide(pq)
+    ptests = ctx.sync_stats()["tri_tests"]
+
+    cpu = cpu_baseline(sc, seconds=args.cpu_seconds) if rank == 0 and args.cpu_seconds > 0 else None
+    clk = clocks.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG64, seed 1002 + 1000*rank)",
+        "config": {"workload": WORKLOAD, "queries_per_step": n, "triangles": int(sum(m.n_tris for m in sc.meshes)),
+                   "tri_tests_per_step": int(tests_per_step), "colliding_pairs_per_step": int(pairs_per_step),
+                   "node_pairs_per_step": int(st["node_pairs"]), "cache": "L2 flushed (512 MB write) between steps",
+                   "launch": "CUDA graph: init + flag reset + pack + persistent traversal"},
+        "queries_per_s": world * n * args.steps / (total_ms / 1e3),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * capi.QUERY_DTYPE.itemsize),
+                "d2h_bytes_per_step": int(64 + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize),
+                "ms_per_step": 1e3 * e2e_s / args.steps, "timing": "host perf_counter around synchronous calls"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "traverse_kernel",
+                     "kernel_ms": kms, "peak_source": peaks["source"],
+                     "fp32": {"achieved_tflops": alg_flops / (kms / 1e3) / 1e12, "peak_tflops": fp32_peak,
+                              "frac": alg_flops / (kms / 1e3) / 1e12 / fp32_peak}},
+        "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch",
+                  "queries_per_s": 200 / (plain_ms / 1e3), "tri_tests_per_s": ptests / (plain_ms / 1e3),
+                  "ms_per_query": plain_ms / 200},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+    }
+    if cpu:
+        out["cpu_baseline"] = cpu
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    res = run_gpu(args)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

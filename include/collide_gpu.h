@@ -1,0 +1,186 @@
+/*
+ * collide_gpu.h — C ABI of the GB300 (sm_103a) collision-detection library.
+ *
+ * Drop-in boundary for the CPU collision path of the inMyRoom_vulkan engine.
+ * The reference runs, per pair of CollisionDetectionEntry, a mid phase
+ *   OBBtreesCollision::ExecuteOBBtreesCollision
+ *     (inMyRoom_vulkan/include/CollisionDetection/OBBtreesCollision.h:14-20,
+ *      src/CollisionDetection/OBBtreesCollision.cpp:7-18)
+ * and a narrow phase
+ *   CreateUncollideRays::ExecuteCreateUncollideRays
+ *     (include/CollisionDetection/CreateUncollideRays.h:16-23,
+ *      src/CollisionDetection/CreateUncollideRays.cpp:60-201)
+ * on OBB trees built by OBBtree::OBBtree (src/Geometry/OBBtree.cpp:321-358).
+ * This ABI replaces those calls for a whole batch of pairs at once: trees are
+ * uploaded once (cg_tree_upload), a batch of queries is resolved in one
+ * persistent launch (cg_collide / cg_collide_async / cg_graph_launch), and the
+ * candidate leaf pairs, colliding triangle pairs, per-triangle contacts and
+ * uncollide rays are read back.
+ *
+ * Conventions: every function returns CG_OK (0) or a negative CG_ERR_* code;
+ * matrices are 4x4 column-major float[16] (glm::mat4 memory layout); triangle
+ * indices are positions in the tree's leaf (DFS) order, exactly the indices
+ * OBBtree::GetTrianglePosition takes. One context is used by one host thread
+ * at a time. There is no CPU fallback: without a usable CUDA device every call
+ * that needs one fails with CG_ERR_CUDA.
+ */
+#ifndef COLLIDE_GPU_H
+#define COLLIDE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum cg_status {
+    CG_OK = 0,
+    CG_ERR_INVALID_ARGUMENT = -1,
+    CG_ERR_CUDA = -2,
+    CG_ERR_OUT_OF_MEMORY = -3,
+    CG_ERR_QUEUE_OVERFLOW = -4,  /* the node-pair work queue filled up: raise cg_config.queue_capacity */
+    CG_ERR_OUTPUT_OVERFLOW = -5, /* more results than capacity; counts are exact, raise the capacity */
+    CG_ERR_TIMEOUT = -6,         /* a bounded device-side wait ran out (cg_config.wait_limit_ms) */
+    CG_ERR_BAD_TREE = -7,        /* tree view fails validation (index out of range, non-forward child) */
+    CG_ERR_NOT_FOUND = -8,       /* unknown tree id */
+};
+
+typedef struct cg_ctx cg_ctx;
+
+/* Launch and capacity settings. cg_config_default fills every field. */
+typedef struct cg_config {
+    int32_t device;            /* CUDA device ordinal */
+    uint32_t max_queries;      /* queries per launch */
+    uint64_t max_tri_pairs;    /* colliding triangle pairs kept per launch */
+    uint64_t max_leaf_pairs;   /* candidate leaf pairs kept per launch (only with CG_KEEP_LEAF_PAIRS) */
+    uint32_t queue_capacity;   /* node-pair tasks the global work queue can hold */
+    uint32_t warps_per_block;  /* persistent traversal kernel shape; 0 = tuned default */
+    uint32_t blocks_per_sm;    /* 0 = as many as fit */
+    uint32_t stack_entries;    /* per-warp shared-memory node-pair stack, power of two (256..4096) */
+    uint32_t donate_min;       /* a warp donates work to idle warps only above this stack size */
+    uint32_t leaf_flush;       /* buffered leaf pairs that trigger a warp's triangle-pair pass (1..64) */
+    uint32_t wait_limit_ms;    /* limit of every device-side wait */
+} cg_config;
+
+void cg_config_default(cg_config* cfg);
+
+int cg_create(const cg_config* cfg, cg_ctx** out);
+int cg_destroy(cg_ctx* ctx);
+int cg_reconfigure(cg_ctx* ctx, const cg_config* cfg); /* resizes buffers / launch shape */
+int cg_get_config(const cg_ctx* ctx, cg_config* out);
+const char* cg_status_string(int status);
+/* Copies the last error message of the context (NUL-terminated). */
+int cg_last_error(const cg_ctx* ctx, char* buf, size_t len);
+
+/* ---- trees ------------------------------------------------------------ */
+
+/* Paralgram / OBB: center and three half-extent vectors
+ * (include/Geometry/Paralgram.h:28-35), 48 bytes. */
+typedef struct cg_obb {
+    float center[3];
+    float u[3];
+    float v[3];
+    float w[3];
+} cg_obb;
+
+/* A flat OBB tree in the reference's layout (include/Geometry/OBBtree.h:61-75,
+ * 129-134): inner node k holds both child boxes and, per child, either an inner
+ * node index (count 0) or a triangle offset and count; node 0 is the root's
+ * node; the root box is separate; triangles are in leaf (DFS) order. A tree
+ * whose root is a leaf has node_count 0. Export it from an OBBtree through the
+ * public OBBtree::OBBtreeTraveler walk (inner nodes in pre-order). */
+typedef struct cg_tree_view {
+    cg_obb root_obb;
+    uint32_t node_count;
+    const cg_obb* node_obbs;          /* [node_count][2] left, right */
+    const uint32_t* node_ref;         /* [node_count][2] child node index or triangle offset */
+    const uint32_t* node_tri_count;   /* [node_count][2] triangle count, 0 = inner child */
+    uint32_t triangle_count;
+    const float* triangles_position;  /* [triangle_count][3][3] */
+    const float* triangles_normal;    /* [triangle_count][3][3], may be NULL (rays then unavailable) */
+    const uint32_t* triangles_indices;/* [triangle_count][3] vertex indices, may be NULL */
+} cg_tree_view;
+
+/* Replaces building/holding OBBtree objects for the GPU: copies the tree to
+ * device memory and returns its id. */
+int cg_tree_upload(cg_ctx* ctx, const cg_tree_view* view, uint32_t* tree_id);
+int cg_tree_free(cg_ctx* ctx, uint32_t tree_id);
+
+/* ---- queries ---------------------------------------------------------- */
+
+/* One entity pair, the unit of OBBtreesCollision::ExecuteOBBtreesCollision.
+ * relative = inverse(first.currentGlobalMatrix) * second.currentGlobalMatrix
+ * (OBBtreesCollision.cpp:15), computed on the host by the caller's math
+ * library so that it is bit-identical to the reference. 72 bytes. */
+typedef struct cg_query {
+    uint32_t tree_a;
+    uint32_t tree_b;
+    float relative[16];
+} cg_query;
+
+/* inverse(a) * b with the operation order of the glm-compatible convention
+ * this library is validated against (for callers without glm). */
+int cg_relative_matrix(const float a[16], const float b[16], float out[16]);
+
+/* One candidate leaf pair: OBBtreesIntersectInfo::CandidateTriangleRangeCombination
+ * (include/Geometry/OBBtree.h:8-19) tagged with its query. 16 bytes. */
+typedef struct cg_leaf_pair {
+    uint32_t query;
+    uint32_t offset_a;
+    uint32_t offset_b;
+    uint16_t count_a;
+    uint16_t count_b;
+} cg_leaf_pair;
+
+/* One colliding triangle pair (TrianglesIntersectionInfo with doIntersept &&
+ * !areCoplanar, include/Geometry/Triangle.h:12-18): tree-order triangle indices
+ * and the intersection segment in the first tree's model space. 36 bytes. */
+typedef struct cg_tri_pair {
+    uint32_t query;
+    uint32_t tri_a;
+    uint32_t tri_b;
+    float source[3];
+    float target[3];
+} cg_tri_pair;
+
+typedef struct cg_stats {
+    uint64_t node_pairs;  /* box pairs tested (SAT) */
+    uint64_t leaf_pairs;  /* candidate leaf pairs */
+    uint64_t tri_tests;   /* triangle-pair tests (Moller calls) */
+    uint64_t tri_pairs;   /* colliding triangle pairs (may exceed max_tri_pairs) */
+    uint64_t fragile;     /* pairs whose second interval degenerated (see docs) */
+    uint64_t donations;   /* node-pair tasks moved between warps */
+    int32_t status;       /* CG_OK or the error the launch raised */
+    int32_t pad;
+} cg_stats;
+
+#define CG_KEEP_LEAF_PAIRS 1u /* also write the candidate leaf pairs */
+#define CG_NO_TRI_PAIRS 2u    /* count triangle tests and hits but do not write pairs */
+
+/* Host queries in, stats out; synchronous. Results stay on the device until read. */
+int cg_collide(cg_ctx* ctx, const cg_query* queries, uint32_t n, uint32_t flags, cg_stats* stats);
+/* Queries already in device memory; enqueued on `stream` (cudaStream_t, NULL =
+ * the context's stream); no host synchronisation. */
+int cg_collide_async(cg_ctx* ctx, const cg_query* d_queries, uint32_t n, uint32_t flags, void* stream);
+/* Waits for the last launch and reads its statistics. */
+int cg_sync_stats(cg_ctx* ctx, cg_stats* stats);
+int cg_read_tri_pairs(cg_ctx* ctx, cg_tri_pair* out, uint64_t cap, uint64_t* n);
+int cg_read_leaf_pairs(cg_ctx* ctx, cg_leaf_pair* out, uint64_t cap, uint64_t* n);
+/* Device pointers to the last launch's results (valid until the next launch). */
+int cg_device_results(cg_ctx* ctx, const cg_tri_pair** pairs, const unsigned long long** pair_count);
+
+/* Device time of the last traversal kernel (the dominant kernel of a collide
+ * step), from CUDA events recorded around its launch; waits for it. */
+int cg_traversal_time_ms(cg_ctx* ctx, float* ms);
+
+/* CUDA graph of one whole collide step over device-resident queries
+ * (counter reset, query packing, persistent traversal + narrow phase). */
+int cg_graph_capture(cg_ctx* ctx, const cg_query* d_queries, uint32_t n, uint32_t flags);
+int cg_graph_launch(cg_ctx* ctx, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COLLIDE_GPU_H */

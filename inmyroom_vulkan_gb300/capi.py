@@ -1,0 +1,268 @@
+"""ctypes binding of the C ABI in include/collide_gpu.h (libcollide_gpu.so).
+
+This is plumbing for Python callers (tests, bench, the autograd wrapper): every
+call goes straight to the CUDA library. There is no CPU fallback; if the
+library cannot be built or loaded, or no CUDA device is usable, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+CG_OK = 0
+STATUS = {0: "CG_OK", -1: "CG_ERR_INVALID_ARGUMENT", -2: "CG_ERR_CUDA", -3: "CG_ERR_OUT_OF_MEMORY",
+          -4: "CG_ERR_QUEUE_OVERFLOW", -5: "CG_ERR_OUTPUT_OVERFLOW", -6: "CG_ERR_TIMEOUT", -7: "CG_ERR_BAD_TREE",
+          -8: "CG_ERR_NOT_FOUND"}
+CG_KEEP_LEAF_PAIRS = 1
+CG_NO_TRI_PAIRS = 2
+
+# Every function the header declares (checked by the CPU tests).
+EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",
+           "cg_last_error", "cg_tree_upload", "cg_tree_free", "cg_relative_matrix", "cg_collide", "cg_collide_async",
+           "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results",
+           "cg_traversal_time_ms", "cg_graph_capture", "cg_graph_launch"]
+
+
+class CgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class cg_config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_queries", C.c_uint32), ("max_tri_pairs", C.c_uint64),
+                ("max_leaf_pairs", C.c_uint64), ("queue_capacity", C.c_uint32), ("warps_per_block", C.c_uint32),
+                ("blocks_per_sm", C.c_uint32), ("stack_entries", C.c_uint32), ("donate_min", C.c_uint32),
+                ("leaf_flush", C.c_uint32), ("wait_limit_ms", C.c_uint32)]
+
+
+class cg_obb(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("u", C.c_float * 3), ("v", C.c_float * 3), ("w", C.c_float * 3)]
+
+
+class cg_tree_view(C.Structure):
+    _fields_ = [("root_obb", cg_obb), ("node_count", C.c_uint32), ("node_obbs", C.c_void_p),
+                ("node_ref", C.c_void_p), ("node_tri_count", C.c_void_p), ("triangle_count", C.c_uint32),
+                ("triangles_position", C.c_void_p), ("triangles_normal", C.c_void_p),
+                ("triangles_indices", C.c_void_p)]
+
+
+class cg_stats(C.Structure):
+    _fields_ = [("node_pairs", C.c_uint64), ("leaf_pairs", C.c_uint64), ("tri_tests", C.c_uint64),
+                ("tri_pairs", C.c_uint64), ("fragile", C.c_uint64), ("donations", C.c_uint64),
+                ("status", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+QUERY_DTYPE = np.dtype([("tree_a", "<u4"), ("tree_b", "<u4"), ("relative", "<f4", (16,))])
+TRI_PAIR_DTYPE = np.dtype([("query", "<u4"), ("tri_a", "<u4"), ("tri_b", "<u4"), ("source", "<f4", (3,)),
+                           ("target", "<f4", (3,))])
+LEAF_PAIR_DTYPE = np.dtype([("query", "<u4"), ("offset_a", "<u4"), ("offset_b", "<u4"), ("count_a", "<u2"),
+                            ("count_b", "<u2")])
+assert QUERY_DTYPE.itemsize == 72 and TRI_PAIR_DTYPE.itemsize == 36 and LEAF_PAIR_DTYPE.itemsize == 16
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads (building first if needed) libcollide_gpu.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or _build.build()
+    lib = C.CDLL(path)
+    vp, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
+    lib.cg_config_default.argtypes = [C.POINTER(cg_config)]
+    lib.cg_config_default.restype = None
+    lib.cg_create.argtypes = [C.POINTER(cg_config), C.POINTER(vp)]
+    lib.cg_destroy.argtypes = [vp]
+    lib.cg_reconfigure.argtypes = [vp, C.POINTER(cg_config)]
+    lib.cg_get_config.argtypes = [vp, C.POINTER(cg_config)]
+    lib.cg_status_string.argtypes = [C.c_int]
+    lib.cg_status_string.restype = C.c_char_p
+    lib.cg_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    lib.cg_tree_upload.argtypes = [vp, C.POINTER(cg_tree_view), C.POINTER(u32)]
+    lib.cg_tree_free.argtypes = [vp, u32]
+    lib.cg_relative_matrix.argtypes = [vp, vp, vp]
+    lib.cg_collide.argtypes = [vp, vp, u32, u32, C.POINTER(cg_stats)]
+    lib.cg_collide_async.argtypes = [vp, vp, u32, u32, vp]
+    lib.cg_sync_stats.argtypes = [vp, C.POINTER(cg_stats)]
+    lib.cg_read_tri_pairs.argtypes = [vp, vp, u64, C.POINTER(u64)]
+    lib.cg_read_leaf_pairs.argtypes = [vp, vp, u64, C.POINTER(u64)]
+    lib.cg_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
+    lib.cg_traversal_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    lib.cg_graph_capture.argtypes = [vp, vp, u32, u32]
+    lib.cg_graph_launch.argtypes = [vp, vp]
+    _lib = lib
+    return lib
+
+
+def default_config(**over) -> cg_config:
+    cfg = cg_config()
+    load_library().cg_config_default(C.byref(cfg))
+    for k, v in over.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def relative_matrix(a16, b16) -> np.ndarray:
+    a = np.ascontiguousarray(a16, np.float32).reshape(16)
+    b = np.ascontiguousarray(b16, np.float32).reshape(16)
+    out = np.zeros(16, np.float32)
+    rc = load_library().cg_relative_matrix(a.ctypes.data, b.ctypes.data, out.ctypes.data)
+    if rc != CG_OK:
+        raise CgError(rc, "cg_relative_matrix")
+    return out
+
+
+def make_queries(tree_a, tree_b, relative) -> np.ndarray:
+    tree_a = np.asarray(tree_a, np.uint32).reshape(-1)
+    q = np.zeros(tree_a.size, QUERY_DTYPE)
+    q["tree_a"] = tree_a
+    q["tree_b"] = np.asarray(tree_b, np.uint32).reshape(-1)
+    q["relative"] = np.asarray(relative, np.float32).reshape(-1, 16)
+    return q
+
+
+class Context:
+    """One cg_ctx: trees, launch buffers and a CUDA stream on one device."""
+
+    def __init__(self, config: cg_config | None = None, **over):
+        self.lib = load_library()
+        cfg = config if config is not None else default_config(**over)
+        h = C.c_void_p()
+        rc = self.lib.cg_create(C.byref(cfg), C.byref(h))
+        if rc != CG_OK:
+            raise CgError(rc, "cg_create (is a CUDA device available?)")
+        self.h = h
+        self._trees: dict[int, tuple] = {}
+
+    # -- housekeeping
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(512)
+        self.lib.cg_last_error(self.h, buf, 512)
+        return buf.value.decode()
+
+    def _check(self, rc: int, what: str):
+        if rc != CG_OK:
+            raise CgError(rc, f"{what}: {self.last_error()}")
+
+    def config(self) -> cg_config:
+        cfg = cg_config()
+        self._check(self.lib.cg_get_config(self.h, C.byref(cfg)), "cg_get_config")
+        return cfg
+
+    def reconfigure(self, **over):
+        cfg = self.config()
+        for k, v in over.items():
+            setattr(cfg, k, v)
+        self._check(self.lib.cg_reconfigure(self.h, C.byref(cfg)), "cg_reconfigure")
+
+    # -- trees
+    def upload_tree(self, root, node_obbs, node_ref, node_cnt, tri_pos, tri_nrm=None, tri_idx=None) -> int:
+        root = np.ascontiguousarray(root, np.float32).reshape(12)
+        node_obbs = np.ascontiguousarray(node_obbs, np.float32).reshape(-1, 2, 12)
+        node_ref = np.ascontiguousarray(node_ref, np.uint32).reshape(-1, 2)
+        node_cnt = np.ascontiguousarray(node_cnt, np.uint32).reshape(-1, 2)
+        tri_pos = np.ascontiguousarray(tri_pos, np.float32).reshape(-1, 9)
+        tri_nrm = None if tri_nrm is None else np.ascontiguousarray(tri_nrm, np.float32).reshape(-1, 9)
+        tri_idx = None if tri_idx is None else np.ascontiguousarray(tri_idx, np.uint32).reshape(-1, 3)
+        v = cg_tree_view()
+        for k, name in enumerate(("center", "u", "v", "w")):
+            getattr(v.root_obb, name)[:] = root[3 * k:3 * k + 3]
+        v.node_count = node_obbs.shape[0]
+        v.node_obbs = node_obbs.ctypes.data if node_obbs.size else None
+        v.node_ref = node_ref.ctypes.data if node_ref.size else None
+        v.node_tri_count = node_cnt.ctypes.data if node_cnt.size else None
+        v.triangle_count = tri_pos.shape[0]
+        v.triangles_position = tri_pos.ctypes.data if tri_pos.size else None
+        v.triangles_normal = None if tri_nrm is None else tri_nrm.ctypes.data
+        v.triangles_indices = None if tri_idx is None else tri_idx.ctypes.data
+        tid = C.c_uint32()
+        self._check(self.lib.cg_tree_upload(self.h, C.byref(v), C.byref(tid)), "cg_tree_upload")
+        return tid.value
+
+    def upload_flat(self, ft) -> int:
+        """Uploads an oracle-style flat tree (attributes root, node_obbs, ...)."""
+        return self.upload_tree(ft.root, ft.node_obbs, ft.node_ref, ft.node_cnt, ft.tri_pos, ft.tri_nrm, ft.tri_idx)
+
+    def free_tree(self, tid: int):
+        self._check(self.lib.cg_tree_free(self.h, tid), "cg_tree_free")
+
+    # -- collide
+    def collide(self, queries: np.ndarray, flags: int = 0, check: bool = True) -> dict:
+        q = np.ascontiguousarray(queries, QUERY_DTYPE)
+        st = cg_stats()
+        rc = self.lib.cg_collide(self.h, q.ctypes.data if q.size else None, q.size, flags, C.byref(st))
+        if check:
+            self._check(rc, "cg_collide")
+        d = st.as_dict()
+        d["rc"] = rc
+        return d
+
+    def collide_async(self, d_queries_ptr: int, n: int, flags: int = 0, stream: int | None = None):
+        self._check(self.lib.cg_collide_async(self.h, d_queries_ptr, n, flags, stream), "cg_collide_async")
+
+    def sync_stats(self, check: bool = True) -> dict:
+        st = cg_stats()
+        rc = self.lib.cg_sync_stats(self.h, C.byref(st))
+        if check:
+            self._check(rc, "cg_sync_stats")
+        d = st.as_dict()
+        d["rc"] = rc
+        return d
+
+    def tri_pairs(self) -> np.ndarray:
+        n = C.c_uint64()
+        self.lib.cg_read_tri_pairs(self.h, None, 0, C.byref(n))
+        out = np.zeros(n.value, TRI_PAIR_DTYPE)
+        rc = self.lib.cg_read_tri_pairs(self.h, out.ctypes.data if n.value else None, n.value, C.byref(n))
+        self._check(rc, "cg_read_tri_pairs")
+        return out
+
+    def leaf_pairs(self) -> np.ndarray:
+        n = C.c_uint64()
+        self.lib.cg_read_leaf_pairs(self.h, None, 0, C.byref(n))
+        out = np.zeros(n.value, LEAF_PAIR_DTYPE)
+        rc = self.lib.cg_read_leaf_pairs(self.h, out.ctypes.data if n.value else None, n.value, C.byref(n))
+        self._check(rc, "cg_read_leaf_pairs")
+        return out
+
+    def device_results(self) -> tuple[int, int]:
+        p, n = C.c_void_p(), C.c_void_p()
+        self._check(self.lib.cg_device_results(self.h, C.byref(p), C.byref(n)), "cg_device_results")
+        return p.value or 0, n.value or 0
+
+    def traversal_ms(self) -> float:
+        ms = C.c_float()
+        self._check(self.lib.cg_traversal_time_ms(self.h, C.byref(ms)), "cg_traversal_time_ms")
+        return ms.value
+
+    def graph_capture(self, d_queries_ptr: int, n: int, flags: int = 0):
+        self._check(self.lib.cg_graph_capture(self.h, d_queries_ptr, n, flags), "cg_graph_capture")
+
+    def graph_launch(self, stream: int | None = None):
+        self._check(self.lib.cg_graph_launch(self.h, stream), "cg_graph_launch")

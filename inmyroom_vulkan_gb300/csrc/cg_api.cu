@@ -1,0 +1,628 @@
+// Host side of the C ABI declared in include/collide_gpu.h: context and
+// buffers, tree upload with validation, launches, result read-back and the
+// CUDA graph of one collide step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cg_internal.h"
+#include "collide_gpu.h"
+
+using namespace cg;
+
+struct cg_ctx {
+    cg_config cfg{};
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = true;
+    uint32_t blocks = 0;  // persistent grid
+
+    // trees
+    struct Slot {
+        DevTree t{};
+        float4* recs = nullptr;
+        float4* tris = nullptr;
+        float* nrm = nullptr;
+        bool live = false;
+    };
+    std::vector<Slot> trees;
+    DevTree* d_trees = nullptr;
+    uint32_t d_trees_cap = 0;
+
+    // per-launch buffers
+    cg_query* d_queries = nullptr;  // staging for host queries
+    PackedQuery* d_packed = nullptr;
+    Counters* d_ctr = nullptr;
+    uint4* d_tasks = nullptr;
+    unsigned int* d_ready = nullptr;
+    uint32_t task_cap = 0;    // donors may publish this many
+    uint32_t task_slots = 0;  // allocated (donor cap + slack for waiting warps)
+    cg_tri_pair* d_pairs = nullptr;
+    cg_leaf_pair* d_leafs = nullptr;
+
+    cg_query* h_queries = nullptr;  // pinned
+    Counters* h_ctr = nullptr;      // pinned
+
+    uint32_t last_flags = 0;
+    bool launched = false;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    bool capturing = false;
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // around the traversal kernel
+
+    std::string err;
+};
+
+namespace {
+
+int fail(cg_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(cg_ctx* c, cudaError_t e, const char* what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA;
+    return fail(c, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CG_CUDA(call, what)                                 \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)
+
+bool pow2(uint32_t x) { return x && !(x & (x - 1)); }
+
+void free_buffers(cg_ctx* c) {
+    cudaFree(c->d_queries);
+    cudaFree(c->d_packed);
+    cudaFree(c->d_ctr);
+    cudaFree(c->d_tasks);
+    cudaFree(c->d_ready);
+    cudaFree(c->d_pairs);
+    cudaFree(c->d_leafs);
+    cudaFreeHost(c->h_queries);
+    cudaFreeHost(c->h_ctr);
+    c->d_queries = nullptr;
+    c->d_packed = nullptr;
+    c->d_ctr = nullptr;
+    c->d_tasks = nullptr;
+    c->d_ready = nullptr;
+    c->d_pairs = nullptr;
+    c->d_leafs = nullptr;
+    c->h_queries = nullptr;
+    c->h_ctr = nullptr;
+}
+
+void drop_graph(cg_ctx* c) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->graph_exec = nullptr;
+    c->graph = nullptr;
+}
+
+int check_config(cg_ctx* c, const cg_config* cfg) {
+    if (cfg->max_queries == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_queries must be > 0");
+    if (!pow2(cfg->stack_entries) || cfg->stack_entries < 256 || cfg->stack_entries > 4096)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "stack_entries must be a power of two in [256, 4096]");
+    if (cfg->warps_per_block == 0 || cfg->warps_per_block > 16)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "warps_per_block must be in [1, 16]");
+    if (cfg->leaf_flush == 0 || cfg->leaf_flush > uint32_t(kLeafCap - 32 + 1))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "leaf_flush must be in [1, %d]", kLeafCap - 32 + 1);
+    if (cfg->queue_capacity < 1024) return fail(c, CG_ERR_INVALID_ARGUMENT, "queue_capacity must be >= 1024");
+    if (cfg->wait_limit_ms == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "wait_limit_ms must be > 0");
+    return CG_OK;
+}
+
+int alloc_buffers(cg_ctx* c) {
+    const cg_config& g = c->cfg;
+    int occ = 0;
+    CG_CUDA(traverse_occupancy(g.warps_per_block, g.stack_entries, &occ), "occupancy");
+    if (occ < 1) return fail(c, CG_ERR_INVALID_ARGUMENT, "traversal kernel does not fit: %u warps x %u stack entries",
+                             g.warps_per_block, g.stack_entries);
+    const int per_sm = g.blocks_per_sm ? std::min<int>(occ, int(g.blocks_per_sm)) : occ;
+    c->blocks = uint32_t(per_sm * c->sm_count);
+    const uint32_t warps = c->blocks * g.warps_per_block;
+    c->task_cap = g.queue_capacity;
+    c->task_slots = g.queue_capacity + 33u * warps + 64u;
+
+    CG_CUDA(cudaMalloc(&c->d_queries, sizeof(cg_query) * g.max_queries), "alloc queries");
+    CG_CUDA(cudaMalloc(&c->d_packed, sizeof(PackedQuery) * g.max_queries), "alloc packed queries");
+    CG_CUDA(cudaMalloc(&c->d_ctr, sizeof(Counters)), "alloc counters");
+    CG_CUDA(cudaMemset(c->d_ctr, 0, sizeof(Counters)), "zero counters");
+    CG_CUDA(cudaMalloc(&c->d_tasks, sizeof(uint4) * c->task_slots), "alloc task queue");
+    CG_CUDA(cudaMalloc(&c->d_ready, sizeof(unsigned int) * c->task_slots), "alloc task flags");
+    CG_CUDA(cudaMemset(c->d_ready, 0, sizeof(unsigned int) * c->task_slots), "zero task flags");
+    if (g.max_tri_pairs) CG_CUDA(cudaMalloc(&c->d_pairs, sizeof(cg_tri_pair) * g.max_tri_pairs), "alloc pair output");
+    if (g.max_leaf_pairs)
+        CG_CUDA(cudaMalloc(&c->d_leafs, sizeof(cg_leaf_pair) * g.max_leaf_pairs), "alloc leaf-pair output");
+    CG_CUDA(cudaMallocHost(&c->h_queries, sizeof(cg_query) * g.max_queries), "alloc pinned queries");
+    CG_CUDA(cudaMallocHost(&c->h_ctr, sizeof(Counters)), "alloc pinned counters");
+    std::memset(c->h_ctr, 0, sizeof(Counters));
+    return CG_OK;
+}
+
+int sync_tree_table(cg_ctx* c) {
+    const uint32_t n = uint32_t(c->trees.size());
+    if (n > c->d_trees_cap) {
+        cudaFree(c->d_trees);
+        c->d_trees = nullptr;
+        const uint32_t cap = std::max<uint32_t>(64, n * 2);
+        CG_CUDA(cudaMalloc(&c->d_trees, sizeof(DevTree) * cap), "alloc tree table");
+        c->d_trees_cap = cap;
+    }
+    std::vector<DevTree> host(n);
+    for (uint32_t i = 0; i < n; ++i) host[i] = c->trees[i].live ? c->trees[i].t : DevTree{};
+    if (n) CG_CUDA(cudaMemcpy(c->d_trees, host.data(), sizeof(DevTree) * n, cudaMemcpyHostToDevice), "upload tree table");
+    return CG_OK;
+}
+
+void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
+    rec[0] = make_float4(b.center[0], b.center[1], b.center[2], b.u[0]);
+    rec[1] = make_float4(b.u[1], b.u[2], b.v[0], b.v[1]);
+    rec[2] = make_float4(b.v[2], b.w[0], b.w[1], b.w[2]);
+    float r, m;
+    std::memcpy(&r, &ref, 4);
+    std::memcpy(&m, &meta, 4);
+    rec[3] = make_float4(r, m, 0.f, 0.f);
+}
+
+// Enqueues counter reset, flag reset, packing and the traversal on `s`.
+int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s) {
+    CG_CUDA(launch_init(c->d_ctr, n, s), "init kernel");
+    CG_CUDA(cudaMemsetAsync(c->d_ready, 0, sizeof(unsigned int) * c->task_slots, s), "reset task flags");
+    CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->d_packed, c->d_ctr, s), "pack kernel");
+    TraverseParams p{};
+    p.q = c->d_packed;
+    p.n_queries = n;
+    p.tasks = c->d_tasks;
+    p.ready = c->d_ready;
+    p.task_cap = c->task_cap;
+    p.task_slots = c->task_slots;
+    p.ctr = c->d_ctr;
+    p.pairs = c->d_pairs;
+    p.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
+    p.leafs = c->d_leafs;
+    p.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
+    p.flags = flags;
+    p.stack_cap = c->cfg.stack_entries;
+    p.donate_min = std::min(std::max(c->cfg.donate_min, 64u), c->cfg.stack_entries - 63u);
+    p.leaf_flush = c->cfg.leaf_flush;
+    p.wait_ns = (unsigned long long)c->cfg.wait_limit_ms * 1000000ull;
+    const unsigned rec_flags = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    CG_CUDA(cudaEventRecordWithFlags(c->ev_t0, s, rec_flags), "timing event");
+    if (n) CG_CUDA(launch_traverse(p, c->blocks, c->cfg.warps_per_block, s), "traversal kernel");
+    CG_CUDA(cudaEventRecordWithFlags(c->ev_t1, s, rec_flags), "timing event");
+    return CG_OK;
+}
+
+int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
+    cg_stats s{};
+    s.node_pairs = k.node_pairs;
+    s.leaf_pairs = k.n_leafs;
+    s.tri_tests = k.tri_tests;
+    s.tri_pairs = k.n_pairs;
+    s.fragile = k.fragile;
+    s.donations = k.donations;
+    int status = CG_OK;
+    if (k.error & ERR_TIMEOUT)
+        status = fail(c, CG_ERR_TIMEOUT, "a device-side wait exceeded %u ms", c->cfg.wait_limit_ms);
+    else if (k.error & ERR_QUEUE)
+        status = fail(c, CG_ERR_QUEUE_OVERFLOW, "node-pair queue full (queue_capacity %u)", c->cfg.queue_capacity);
+    else if (k.error & ERR_BAD_QUERY)
+        status = fail(c, CG_ERR_INVALID_ARGUMENT, "a query names an unknown tree");
+    else if (!(c->last_flags & CG_NO_TRI_PAIRS) && k.n_pairs > (c->d_pairs ? c->cfg.max_tri_pairs : 0))
+        status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu colliding pairs, capacity %llu", (unsigned long long)k.n_pairs,
+                      (unsigned long long)c->cfg.max_tri_pairs);
+    else if ((c->last_flags & CG_KEEP_LEAF_PAIRS) && k.n_leafs > (c->d_leafs ? c->cfg.max_leaf_pairs : 0))
+        status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu leaf pairs, capacity %llu", (unsigned long long)k.n_leafs,
+                      (unsigned long long)c->cfg.max_leaf_pairs);
+    s.status = status;
+    if (st) *st = s;
+    return status;
+}
+
+// glm-convention 4x4 product and inverse (column-major); see cg_relative_matrix.
+void mat_mul(const float* A, const float* B, float* R) {
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 4; ++k) {
+            float acc = A[0 + k] * B[4 * j + 0];
+            acc = acc + A[4 + k] * B[4 * j + 1];
+            acc = acc + A[8 + k] * B[4 * j + 2];
+            acc = acc + A[12 + k] * B[4 * j + 3];
+            R[4 * j + k] = acc;
+        }
+}
+
+void mat_inverse(const float* M, float* R) {
+    auto a = [&](int r, int c) { return M[4 * c + r]; };
+    const float s01 = a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1);
+    const float s02 = a(0, 0) * a(1, 2) - a(1, 0) * a(0, 2);
+    const float s03 = a(0, 0) * a(1, 3) - a(1, 0) * a(0, 3);
+    const float s12 = a(0, 1) * a(1, 2) - a(1, 1) * a(0, 2);
+    const float s13 = a(0, 1) * a(1, 3) - a(1, 1) * a(0, 3);
+    const float s23 = a(0, 2) * a(1, 3) - a(1, 2) * a(0, 3);
+    const float q01 = a(2, 0) * a(3, 1) - a(3, 0) * a(2, 1);
+    const float q02 = a(2, 0) * a(3, 2) - a(3, 0) * a(2, 2);
+    const float q03 = a(2, 0) * a(3, 3) - a(3, 0) * a(2, 3);
+    const float q12 = a(2, 1) * a(3, 2) - a(3, 1) * a(2, 2);
+    const float q13 = a(2, 1) * a(3, 3) - a(3, 1) * a(2, 3);
+    const float q23 = a(2, 2) * a(3, 3) - a(3, 2) * a(2, 3);
+    const float det = s01 * q23 - s02 * q13 + s03 * q12 + s12 * q03 - s13 * q02 + s23 * q01;
+    const float inv = 1.0f / det;
+    float b[4][4];
+    b[0][0] = (a(1, 1) * q23 - a(1, 2) * q13 + a(1, 3) * q12) * inv;
+    b[0][1] = (-a(0, 1) * q23 + a(0, 2) * q13 - a(0, 3) * q12) * inv;
+    b[0][2] = (a(3, 1) * s23 - a(3, 2) * s13 + a(3, 3) * s12) * inv;
+    b[0][3] = (-a(2, 1) * s23 + a(2, 2) * s13 - a(2, 3) * s12) * inv;
+    b[1][0] = (-a(1, 0) * q23 + a(1, 2) * q03 - a(1, 3) * q02) * inv;
+    b[1][1] = (a(0, 0) * q23 - a(0, 2) * q03 + a(0, 3) * q02) * inv;
+    b[1][2] = (-a(3, 0) * s23 + a(3, 2) * s03 - a(3, 3) * s02) * inv;
+    b[1][3] = (a(2, 0) * s23 - a(2, 2) * s03 + a(2, 3) * s02) * inv;
+    b[2][0] = (a(1, 0) * q13 - a(1, 1) * q03 + a(1, 3) * q01) * inv;
+    b[2][1] = (-a(0, 0) * q13 + a(0, 1) * q03 - a(0, 3) * q01) * inv;
+    b[2][2] = (a(3, 0) * s13 - a(3, 1) * s03 + a(3, 3) * s01) * inv;
+    b[2][3] = (-a(2, 0) * s13 + a(2, 1) * s03 - a(2, 3) * s01) * inv;
+    b[3][0] = (-a(1, 0) * q12 + a(1, 1) * q02 - a(1, 2) * q01) * inv;
+    b[3][1] = (a(0, 0) * q12 - a(0, 1) * q02 + a(0, 2) * q01) * inv;
+    b[3][2] = (-a(3, 0) * s12 + a(3, 1) * s02 - a(3, 2) * s01) * inv;
+    b[3][3] = (a(2, 0) * s12 - a(2, 1) * s02 + a(2, 2) * s01) * inv;
+    for (int col = 0; col < 4; ++col)
+        for (int r = 0; r < 4; ++r) R[4 * col + r] = b[r][col];
+}
+
+}  // namespace
+
+extern "C" {
+
+void cg_config_default(cg_config* cfg) {
+    if (!cfg) return;
+    cfg->device = 0;
+    cfg->max_queries = 1u << 16;
+    cfg->max_tri_pairs = 1ull << 23;
+    cfg->max_leaf_pairs = 1ull << 22;
+    cfg->queue_capacity = 1u << 20;
+    cfg->warps_per_block = 8;
+    cfg->blocks_per_sm = 0;
+    cfg->stack_entries = 512;
+    cfg->donate_min = 64;
+    cfg->leaf_flush = 32;
+    cfg->wait_limit_ms = 2000;
+}
+
+const char* cg_status_string(int s) {
+    switch (s) {
+        case CG_OK: return "ok";
+        case CG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case CG_ERR_CUDA: return "CUDA error";
+        case CG_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case CG_ERR_QUEUE_OVERFLOW: return "work queue overflow";
+        case CG_ERR_OUTPUT_OVERFLOW: return "output overflow";
+        case CG_ERR_TIMEOUT: return "device wait timed out";
+        case CG_ERR_BAD_TREE: return "malformed tree";
+        case CG_ERR_NOT_FOUND: return "unknown tree id";
+        default: return "unknown status";
+    }
+}
+
+int cg_last_error(const cg_ctx* c, char* buf, size_t len) {
+    if (!c || !buf || len == 0) return CG_ERR_INVALID_ARGUMENT;
+    std::snprintf(buf, len, "%s", c->err.c_str());
+    return CG_OK;
+}
+
+int cg_create(const cg_config* cfg_in, cg_ctx** out) {
+    if (!out) return CG_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cg_config cfg;
+    if (cfg_in)
+        cfg = *cfg_in;
+    else
+        cg_config_default(&cfg);
+    auto* c = new cg_ctx;
+    c->cfg = cfg;
+    int rc = check_config(c, &cfg);
+    if (rc != CG_OK) {
+        delete c;
+        return rc;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0 || cfg.device < 0 || cfg.device >= ndev) {
+        delete c;
+        return CG_ERR_CUDA;
+    }
+    c->device = cfg.device;
+    if (cudaSetDevice(c->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess) {
+        delete c;
+        return CG_ERR_CUDA;
+    }
+    rc = alloc_buffers(c);
+    if (rc != CG_OK) {
+        free_buffers(c);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return CG_OK;
+}
+
+int cg_destroy(cg_ctx* c) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    for (auto& s : c->trees) {
+        cudaFree(s.recs);
+        cudaFree(s.tris);
+        cudaFree(s.nrm);
+    }
+    cudaFree(c->d_trees);
+    free_buffers(c);
+    cudaEventDestroy(c->ev_t0);
+    cudaEventDestroy(c->ev_t1);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return CG_OK;
+}
+
+int cg_get_config(const cg_ctx* c, cg_config* out) {
+    if (!c || !out) return CG_ERR_INVALID_ARGUMENT;
+    *out = c->cfg;
+    return CG_OK;
+}
+
+int cg_reconfigure(cg_ctx* c, const cg_config* cfg) {
+    if (!c || !cfg) return CG_ERR_INVALID_ARGUMENT;
+    if (cfg->device != c->device) return fail(c, CG_ERR_INVALID_ARGUMENT, "cannot change device");
+    int rc = check_config(c, cfg);
+    if (rc != CG_OK) return rc;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    free_buffers(c);
+    c->cfg = *cfg;
+    c->launched = false;
+    return alloc_buffers(c);
+}
+
+int cg_relative_matrix(const float a[16], const float b[16], float out[16]) {
+    if (!a || !b || !out) return CG_ERR_INVALID_ARGUMENT;
+    float inv[16];
+    mat_inverse(a, inv);
+    mat_mul(inv, b, out);
+    return CG_OK;
+}
+
+int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
+    if (!c || !v || !tree_id) return CG_ERR_INVALID_ARGUMENT;
+    const uint32_t N = v->node_count, T = v->triangle_count;
+    if ((N && (!v->node_obbs || !v->node_ref || !v->node_tri_count)) || (T && !v->triangles_position))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "tree view has null arrays");
+    if (N > (0x7fffffffu - 4u) / 2u) return fail(c, CG_ERR_BAD_TREE, "too many nodes");
+    // Validation: children of node k are nodes > k (pre-order) and < N; leaf
+    // ranges lie inside the triangle array; counts fit 16 bits.
+    for (uint32_t k = 0; k < N; ++k)
+        for (int s = 0; s < 2; ++s) {
+            const uint32_t ref = v->node_ref[2 * k + s], cnt = v->node_tri_count[2 * k + s];
+            if (cnt == 0) {
+                if (ref <= k || ref >= N) return fail(c, CG_ERR_BAD_TREE, "node %u child %d -> %u", k, s, ref);
+            } else {
+                if (cnt > 0xffffu || uint64_t(ref) + cnt > T)
+                    return fail(c, CG_ERR_BAD_TREE, "node %u leaf %d range [%u, +%u) outside %u triangles", k, s, ref,
+                                cnt, T);
+            }
+        }
+    if (N == 0 && T > 0xffffu) return fail(c, CG_ERR_BAD_TREE, "leaf root with %u triangles", T);
+    cudaSetDevice(c->device);
+
+    const uint32_t n_recs = 2 * N + 2;
+    std::vector<float4> recs(4ull * n_recs, make_float4(0, 0, 0, 0));
+    put_box(&recs[4], v->root_obb, 0, N ? 0u : (kLeafFlag | T));
+    for (uint32_t k = 0; k < N; ++k)
+        for (int s = 0; s < 2; ++s) {
+            const uint32_t r = 2 * k + 2 + s;
+            const uint32_t cnt = v->node_tri_count[2 * k + s];
+            put_box(&recs[4ull * r], v->node_obbs[2 * k + s], v->node_ref[2 * k + s], cnt ? (kLeafFlag | cnt) : 0u);
+        }
+    std::vector<float4> tris(3ull * std::max<uint32_t>(T, 1));
+    for (uint32_t t = 0; t < T; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const float* p = v->triangles_position + 9ull * t + 3 * k;
+            const uint32_t vi = v->triangles_indices ? v->triangles_indices[3ull * t + k] : 3u * t + k;
+            float w;
+            std::memcpy(&w, &vi, 4);
+            tris[3ull * t + k] = make_float4(p[0], p[1], p[2], w);
+        }
+
+    cg_ctx::Slot slot;
+    CG_CUDA(cudaMalloc(&slot.recs, sizeof(float4) * recs.size()), "alloc tree records");
+    CG_CUDA(cudaMalloc(&slot.tris, sizeof(float4) * tris.size()), "alloc tree triangles");
+    CG_CUDA(cudaMemcpy(slot.recs, recs.data(), sizeof(float4) * recs.size(), cudaMemcpyHostToDevice), "upload records");
+    CG_CUDA(cudaMemcpy(slot.tris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice), "upload triangles");
+    if (v->triangles_normal && T) {
+        CG_CUDA(cudaMalloc(&slot.nrm, sizeof(float) * 9ull * T), "alloc normals");
+        CG_CUDA(cudaMemcpy(slot.nrm, v->triangles_normal, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice),
+                "upload normals");
+    }
+    CG_CUDA(launch_surfaces(slot.recs, n_recs, c->stream), "surface kernel");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "surface kernel");
+    slot.t = DevTree{slot.recs, slot.tris, slot.nrm, n_recs, T};
+    slot.live = true;
+
+    uint32_t id = uint32_t(c->trees.size());
+    for (uint32_t i = 0; i < c->trees.size(); ++i)
+        if (!c->trees[i].live) {
+            id = i;
+            break;
+        }
+    if (id == c->trees.size())
+        c->trees.push_back(slot);
+    else
+        c->trees[id] = slot;
+    int rc = sync_tree_table(c);
+    if (rc != CG_OK) return rc;
+    *tree_id = id;
+    return CG_OK;
+}
+
+int cg_tree_free(cg_ctx* c, uint32_t id) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    auto& s = c->trees[id];
+    cudaFree(s.recs);
+    cudaFree(s.tris);
+    cudaFree(s.nrm);
+    s = cg_ctx::Slot{};
+    return sync_tree_table(c);
+}
+
+int cg_collide_async(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, void* stream) {
+    if (!c || (n && !d_queries)) return CG_ERR_INVALID_ARGUMENT;
+    if (n > c->cfg.max_queries) return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    c->last_flags = flags;
+    int rc = enqueue_step(c, d_queries, n, flags, s);
+    if (rc != CG_OK) return rc;
+    c->launched = true;
+    if (s != c->stream) {
+        // make later reads on the context stream wait for this launch
+        cudaEvent_t ev;
+        CG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+        CG_CUDA(cudaEventRecord(ev, s), "event record");
+        CG_CUDA(cudaStreamWaitEvent(c->stream, ev, 0), "stream wait");
+        cudaEventDestroy(ev);
+    }
+    return CG_OK;
+}
+
+int cg_sync_stats(cg_ctx* c, cg_stats* st) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "read counters");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "collide");
+    return stats_from(c, *c->h_ctr, st);
+}
+
+int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, cg_stats* st) {
+    if (!c || (n && !queries)) return CG_ERR_INVALID_ARGUMENT;
+    if (n > c->cfg.max_queries) return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t a = queries[i].tree_a, b = queries[i].tree_b;
+        if (a >= c->trees.size() || !c->trees[a].live || b >= c->trees.size() || !c->trees[b].live)
+            return fail(c, CG_ERR_NOT_FOUND, "query %u names tree %u / %u", i, a, b);
+    }
+    cudaSetDevice(c->device);
+    if (n) {
+        std::memcpy(c->h_queries, queries, sizeof(cg_query) * n);
+        CG_CUDA(cudaMemcpyAsync(c->d_queries, c->h_queries, sizeof(cg_query) * n, cudaMemcpyHostToDevice, c->stream),
+                "upload queries");
+    }
+    c->last_flags = flags;
+    int rc = enqueue_step(c, c->d_queries, n, flags, c->stream);
+    if (rc != CG_OK) return rc;
+    c->launched = true;
+    return cg_sync_stats(c, st);
+}
+
+int cg_read_tri_pairs(cg_ctx* c, cg_tri_pair* out, uint64_t cap, uint64_t* n) {
+    if (!c || !n || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "read counters");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "read counters");
+    const uint64_t avail = std::min<uint64_t>(c->h_ctr->n_pairs, c->d_pairs ? c->cfg.max_tri_pairs : 0);
+    *n = c->h_ctr->n_pairs;
+    const uint64_t m = std::min(avail, cap);
+    if (m) CG_CUDA(cudaMemcpy(out, c->d_pairs, sizeof(cg_tri_pair) * m, cudaMemcpyDeviceToHost), "read pairs");
+    return c->h_ctr->n_pairs > avail ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
+int cg_read_leaf_pairs(cg_ctx* c, cg_leaf_pair* out, uint64_t cap, uint64_t* n) {
+    if (!c || !n || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "read counters");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "read counters");
+    const uint64_t avail = std::min<uint64_t>(c->h_ctr->n_leafs, c->d_leafs ? c->cfg.max_leaf_pairs : 0);
+    *n = c->h_ctr->n_leafs;
+    const uint64_t m = std::min(avail, cap);
+    if (m) CG_CUDA(cudaMemcpy(out, c->d_leafs, sizeof(cg_leaf_pair) * m, cudaMemcpyDeviceToHost), "read leaf pairs");
+    return c->h_ctr->n_leafs > avail ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
+int cg_device_results(cg_ctx* c, const cg_tri_pair** pairs, const unsigned long long** pair_count) {
+    if (!c || !pairs || !pair_count) return CG_ERR_INVALID_ARGUMENT;
+    *pairs = c->d_pairs;
+    *pair_count = &c->d_ctr->n_pairs;
+    return CG_OK;
+}
+
+int cg_traversal_time_ms(cg_ctx* c, float* ms) {
+    if (!c || !ms) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaEventSynchronize(c->ev_t1), "timing event");
+    CG_CUDA(cudaEventElapsedTime(ms, c->ev_t0, c->ev_t1), "timing");
+    return CG_OK;
+}
+
+int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags) {
+    if (!c || (n && !d_queries)) return CG_ERR_INVALID_ARGUMENT;
+    if (n > c->cfg.max_queries) return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaStreamSynchronize(c->stream), "sync before capture");
+    drop_graph(c);
+    CG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    c->capturing = true;
+    const int rc = enqueue_step(c, d_queries, n, flags, c->stream);
+    c->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc != CG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+    c->graph = g;
+    CG_CUDA(cudaGraphInstantiate(&c->graph_exec, g, 0), "instantiate graph");
+    c->last_flags = flags;
+    return CG_OK;
+}
+
+int cg_graph_launch(cg_ctx* c, void* stream) {
+    if (!c || !c->graph_exec) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    CG_CUDA(cudaGraphLaunch(c->graph_exec, s), "graph launch");
+    c->launched = true;
+    if (s != c->stream) {
+        cudaEvent_t ev;
+        CG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+        CG_CUDA(cudaEventRecord(ev, s), "event record");
+        CG_CUDA(cudaStreamWaitEvent(c->stream, ev, 0), "stream wait");
+        cudaEventDestroy(ev);
+    }
+    return CG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,89 @@
+// Shared between the host side of the C ABI and the collision kernels.
+//
+// Device layout of one tree (HBM):
+//   recs : float4[4 * n_recs], one 64-byte record per box. Record 1 is the
+//          root; the two child boxes of inner node k are records 2k+2 (left)
+//          and 2k+3 (right), so one node's children share a 128-byte line.
+//          q0 = (c.x, c.y, c.z, u.x)  q1 = (u.y, u.z, v.x, v.y)
+//          q2 = (v.z, w.x, w.y, w.z)  q3 = (ref, meta, surface, 0)
+//          ref  = child inner-node index, or the leaf's first triangle
+//          meta = triangle count | 0x80000000 for a leaf
+//          surface = Paralgram::GetSurface of the box, precomputed
+//   tris : float4[3 * n_tris], 48 bytes per triangle in leaf (DFS) order,
+//          (p_k.xyz, vertex index k as bits) for k = 0, 1, 2.
+//   nrm  : float[9 * n_tris] vertex normals (uncollide rays), optional.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "collide_gpu.h"
+
+namespace cg {
+
+constexpr uint32_t kLeafFlag = 0x80000000u;
+constexpr int kLeafCap = 64;  // buffered leaf pairs per warp
+
+struct DevTree {
+    const float4* recs;
+    const float4* tris;
+    const float* nrm;
+    uint32_t n_recs;
+    uint32_t n_tris;
+};
+
+// A query as the kernels read it: relative matrix columns and tree pointers.
+struct alignas(16) PackedQuery {
+    float4 m[4];
+    const float4* recs_a;
+    const float4* recs_b;
+    const float4* tris_a;
+    const float4* tris_b;
+};
+
+struct Counters {
+    unsigned int head;  // next queue slot to claim (slots < n_queries are root tasks)
+    unsigned int tail;  // one past the last published slot
+    unsigned int work;  // tasks published and not yet finished
+    unsigned int error; // ERR_* bits
+    unsigned long long n_pairs;
+    unsigned long long n_leafs;
+    unsigned long long node_pairs;
+    unsigned long long tri_tests;
+    unsigned long long fragile;
+    unsigned long long donations;
+};
+
+enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
+
+struct TraverseParams {
+    const PackedQuery* q;
+    uint32_t n_queries;
+    uint4* tasks;         // donated tasks: slot s >= n_queries lives at index s - n_queries
+    unsigned int* ready;  // per donated slot: 1 once published
+    uint32_t task_cap;    // donated slots that donors may publish
+    uint32_t task_slots;  // allocated slots (task_cap plus room for warps waiting past it)
+    Counters* ctr;
+    cg_tri_pair* pairs;
+    unsigned long long pairs_cap;
+    cg_leaf_pair* leafs;
+    unsigned long long leafs_cap;
+    uint32_t flags;
+    uint32_t stack_cap;   // power of two
+    uint32_t donate_min;
+    uint32_t leaf_flush;
+    unsigned long long wait_ns;
+};
+
+__host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return 3u * stack_cap + 5u * kLeafCap + 1u; }
+
+// Kernel launchers (cg_kernels.cu).
+cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
+                        Counters* ctr, cudaStream_t s);
+cudaError_t launch_init(Counters* ctr, uint32_t n_queries, cudaStream_t s);
+cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s);
+cudaError_t traverse_occupancy(uint32_t warps_per_block, uint32_t stack_cap, int* blocks_per_sm);
+cudaError_t launch_surfaces(float4* recs, uint32_t n_recs, cudaStream_t s);
+
+}  // namespace cg
