@@ -195,7 +195,10 @@ def run_gpu(args) -> dict:
     d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
     torch.cuda.synchronize()
     ctx.graph_capture(d_q.data_ptr(), n)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: its handle is never 0, which the C ABI reads as
+    # "the context's own stream"
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
     st = None

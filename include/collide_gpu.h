@@ -150,7 +150,8 @@ typedef struct cg_stats {
     uint64_t tri_tests;   /* triangle-pair tests (Moller calls) */
     uint64_t tri_pairs;   /* colliding triangle pairs (may exceed max_tri_pairs) */
     uint64_t fragile;     /* pairs whose second interval degenerated (see docs) */
-    uint64_t donations;   /* node-pair tasks moved between warps */
+    uint64_t donations;   /* node pairs handed from busy to waiting warps */
+    uint64_t warp_steps;  /* traversal steps; node_pairs / warp_steps = busy lanes per step */
     int32_t status;       /* CG_OK or the error the launch raised */
     int32_t pad;
 } cg_stats;

@@ -53,7 +53,7 @@ class cg_tree_view(C.Structure):
 
 class cg_stats(C.Structure):
     _fields_ = [("node_pairs", C.c_uint64), ("leaf_pairs", C.c_uint64), ("tri_tests", C.c_uint64),
-                ("tri_pairs", C.c_uint64), ("fragile", C.c_uint64), ("donations", C.c_uint64),
+                ("tri_pairs", C.c_uint64), ("fragile", C.c_uint64), ("donations", C.c_uint64), ("warp_steps", C.c_uint64),
                 ("status", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self) -> dict:

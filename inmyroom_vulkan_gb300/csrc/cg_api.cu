@@ -40,10 +40,13 @@ struct cg_ctx {
     cg_query* d_queries = nullptr;  // staging for host queries
     PackedQuery* d_packed = nullptr;
     Counters* d_ctr = nullptr;
-    uint4* d_tasks = nullptr;
+    uint4* d_pool = nullptr;        // donated node-pair entries
+    uint2* d_slots = nullptr;       // chunk of each donated slot
     unsigned int* d_ready = nullptr;
-    uint32_t task_cap = 0;    // donors may publish this many
-    uint32_t task_slots = 0;  // allocated (donor cap + slack for waiting warps)
+    uint32_t pool_cap = 0;          // entries donors may reserve
+    uint32_t slot_cap = 0;          // slots donors may reserve
+    uint32_t pool_alloc = 0, slot_alloc = 0;  // allocated, with slack for concurrent reservations
+    cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
     cg_tri_pair* d_pairs = nullptr;
     cg_leaf_pair* d_leafs = nullptr;
 
@@ -92,7 +95,8 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_queries);
     cudaFree(c->d_packed);
     cudaFree(c->d_ctr);
-    cudaFree(c->d_tasks);
+    cudaFree(c->d_pool);
+    cudaFree(c->d_slots);
     cudaFree(c->d_ready);
     cudaFree(c->d_pairs);
     cudaFree(c->d_leafs);
@@ -101,7 +105,8 @@ void free_buffers(cg_ctx* c) {
     c->d_queries = nullptr;
     c->d_packed = nullptr;
     c->d_ctr = nullptr;
-    c->d_tasks = nullptr;
+    c->d_pool = nullptr;
+    c->d_slots = nullptr;
     c->d_ready = nullptr;
     c->d_pairs = nullptr;
     c->d_leafs = nullptr;
@@ -138,16 +143,19 @@ int alloc_buffers(cg_ctx* c) {
     const int per_sm = g.blocks_per_sm ? std::min<int>(occ, int(g.blocks_per_sm)) : occ;
     c->blocks = uint32_t(per_sm * c->sm_count);
     const uint32_t warps = c->blocks * g.warps_per_block;
-    c->task_cap = g.queue_capacity;
-    c->task_slots = g.queue_capacity + 33u * warps + 64u;
+    c->pool_cap = g.queue_capacity;
+    c->slot_cap = g.queue_capacity;
+    c->pool_alloc = g.queue_capacity + 32u * warps + 64u;
+    c->slot_alloc = g.queue_capacity + 2u * warps + 64u;
 
     CG_CUDA(cudaMalloc(&c->d_queries, sizeof(cg_query) * g.max_queries), "alloc queries");
     CG_CUDA(cudaMalloc(&c->d_packed, sizeof(PackedQuery) * g.max_queries), "alloc packed queries");
     CG_CUDA(cudaMalloc(&c->d_ctr, sizeof(Counters)), "alloc counters");
     CG_CUDA(cudaMemset(c->d_ctr, 0, sizeof(Counters)), "zero counters");
-    CG_CUDA(cudaMalloc(&c->d_tasks, sizeof(uint4) * c->task_slots), "alloc task queue");
-    CG_CUDA(cudaMalloc(&c->d_ready, sizeof(unsigned int) * c->task_slots), "alloc task flags");
-    CG_CUDA(cudaMemset(c->d_ready, 0, sizeof(unsigned int) * c->task_slots), "zero task flags");
+    CG_CUDA(cudaMalloc(&c->d_pool, sizeof(uint4) * c->pool_alloc), "alloc task pool");
+    CG_CUDA(cudaMalloc(&c->d_slots, sizeof(uint2) * c->slot_alloc), "alloc task slots");
+    CG_CUDA(cudaMalloc(&c->d_ready, sizeof(unsigned int) * c->slot_alloc), "alloc task flags");
+    CG_CUDA(cudaMemset(c->d_ready, 0, sizeof(unsigned int) * c->slot_alloc), "zero task flags");
     if (g.max_tri_pairs) CG_CUDA(cudaMalloc(&c->d_pairs, sizeof(cg_tri_pair) * g.max_tri_pairs), "alloc pair output");
     if (g.max_leaf_pairs)
         CG_CUDA(cudaMalloc(&c->d_leafs, sizeof(cg_leaf_pair) * g.max_leaf_pairs), "alloc leaf-pair output");
@@ -184,16 +192,17 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
 
 // Enqueues counter reset, flag reset, packing and the traversal on `s`.
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s) {
-    CG_CUDA(launch_init(c->d_ctr, n, s), "init kernel");
-    CG_CUDA(cudaMemsetAsync(c->d_ready, 0, sizeof(unsigned int) * c->task_slots, s), "reset task flags");
+    CG_CUDA(launch_init(c->d_ctr, c->d_ready, c->slot_alloc, n, s), "init kernel");
     CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->d_packed, c->d_ctr, s), "pack kernel");
     TraverseParams p{};
     p.q = c->d_packed;
     p.n_queries = n;
-    p.tasks = c->d_tasks;
+    p.pool = c->d_pool;
+    p.slots = c->d_slots;
     p.ready = c->d_ready;
-    p.task_cap = c->task_cap;
-    p.task_slots = c->task_slots;
+    p.pool_cap = c->pool_cap;
+    p.slot_cap = c->slot_cap;
+    p.slot_alloc = c->slot_alloc;
     p.ctr = c->d_ctr;
     p.pairs = c->d_pairs;
     p.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
@@ -201,7 +210,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     p.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
     p.flags = flags;
     p.stack_cap = c->cfg.stack_entries;
-    p.donate_min = std::min(std::max(c->cfg.donate_min, 64u), c->cfg.stack_entries - 63u);
+    p.donate_min = std::min(std::max(c->cfg.donate_min, 2u), c->cfg.stack_entries - 63u);
     p.leaf_flush = c->cfg.leaf_flush;
     p.wait_ns = (unsigned long long)c->cfg.wait_limit_ms * 1000000ull;
     const unsigned rec_flags = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -219,6 +228,7 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
     s.tri_pairs = k.n_pairs;
     s.fragile = k.fragile;
     s.donations = k.donations;
+    s.warp_steps = k.warp_steps;
     int status = CG_OK;
     if (k.error & ERR_TIMEOUT)
         status = fail(c, CG_ERR_TIMEOUT, "a device-side wait exceeded %u ms", c->cfg.wait_limit_ms);
@@ -300,7 +310,7 @@ void cg_config_default(cg_config* cfg) {
     cfg->warps_per_block = 8;
     cfg->blocks_per_sm = 0;
     cfg->stack_entries = 512;
-    cfg->donate_min = 64;
+    cfg->donate_min = 16;
     cfg->leaf_flush = 32;
     cfg->wait_limit_ms = 2000;
 }
@@ -351,7 +361,8 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
     if (cudaSetDevice(c->device) != cudaSuccess ||
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess) {
+        cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         delete c;
         return CG_ERR_CUDA;
     }
@@ -380,6 +391,7 @@ int cg_destroy(cg_ctx* c) {
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
+    cudaEventDestroy(c->ev_join);
     cudaStreamDestroy(c->stream);
     delete c;
     return CG_OK;
@@ -508,12 +520,9 @@ int cg_collide_async(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t 
     if (rc != CG_OK) return rc;
     c->launched = true;
     if (s != c->stream) {
-        // make later reads on the context stream wait for this launch
-        cudaEvent_t ev;
-        CG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
-        CG_CUDA(cudaEventRecord(ev, s), "event record");
-        CG_CUDA(cudaStreamWaitEvent(c->stream, ev, 0), "stream wait");
-        cudaEventDestroy(ev);
+        // later reads on the context stream wait for this launch
+        CG_CUDA(cudaEventRecord(c->ev_join, s), "event record");
+        CG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "stream wait");
     }
     return CG_OK;
 }
@@ -616,11 +625,8 @@ int cg_graph_launch(cg_ctx* c, void* stream) {
     CG_CUDA(cudaGraphLaunch(c->graph_exec, s), "graph launch");
     c->launched = true;
     if (s != c->stream) {
-        cudaEvent_t ev;
-        CG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
-        CG_CUDA(cudaEventRecord(ev, s), "event record");
-        CG_CUDA(cudaStreamWaitEvent(c->stream, ev, 0), "stream wait");
-        cudaEventDestroy(ev);
+        CG_CUDA(cudaEventRecord(c->ev_join, s), "event record");
+        CG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "stream wait");
     }
     return CG_OK;
 }

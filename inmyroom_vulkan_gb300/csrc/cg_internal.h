@@ -43,27 +43,36 @@ struct alignas(16) PackedQuery {
 };
 
 struct Counters {
-    unsigned int head;  // next queue slot to claim (slots < n_queries are root tasks)
-    unsigned int tail;  // one past the last published slot
-    unsigned int work;  // tasks published and not yet finished
-    unsigned int error; // ERR_* bits
+    unsigned int head;      // next task slot to claim (slots < n_queries are the root tasks)
+    unsigned int tail;      // one past the last reserved task slot
+    unsigned int work;      // tasks published and not yet finished
+    unsigned int error;     // ERR_* bits
+    unsigned int pool_tail; // node-pair entries reserved in the task pool
+    unsigned int n_queries; // queries of the launch (the next launch clears the slots it published)
     unsigned long long n_pairs;
     unsigned long long n_leafs;
     unsigned long long node_pairs;
     unsigned long long tri_tests;
     unsigned long long fragile;
-    unsigned long long donations;
+    unsigned long long donations;  // node pairs handed to other warps
+    unsigned long long warp_steps; // traversal steps (node_pairs / warp_steps = lanes busy per step)
 };
 
 enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
 
+// Work queue. A task is a chunk of up to 32 node pairs: slot s >= n_queries
+// describes chunk slots[s - n_queries] = (first pool entry, count) and is
+// readable once ready[s - n_queries] is 1. Slot s < n_queries is the root pair
+// of query s.
 struct TraverseParams {
     const PackedQuery* q;
     uint32_t n_queries;
-    uint4* tasks;         // donated tasks: slot s >= n_queries lives at index s - n_queries
+    uint4* pool;          // node-pair entries (query, record a, record b, 0)
+    uint2* slots;         // chunk of each donated slot
     unsigned int* ready;  // per donated slot: 1 once published
-    uint32_t task_cap;    // donated slots that donors may publish
-    uint32_t task_slots;  // allocated slots (task_cap plus room for warps waiting past it)
+    uint32_t pool_cap;    // entries donors may reserve
+    uint32_t slot_cap;    // donated slots donors may reserve
+    uint32_t slot_alloc;  // allocated slots (slot_cap plus room for warps waiting past it)
     Counters* ctr;
     cg_tri_pair* pairs;
     unsigned long long pairs_cap;
@@ -81,7 +90,7 @@ __host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
                         Counters* ctr, cudaStream_t s);
-cudaError_t launch_init(Counters* ctr, uint32_t n_queries, cudaStream_t s);
+cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries, cudaStream_t s);
 cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s);
 cudaError_t traverse_occupancy(uint32_t warps_per_block, uint32_t stack_cap, int* blocks_per_sm);
 cudaError_t launch_surfaces(float4* recs, uint32_t n_recs, cudaStream_t s);

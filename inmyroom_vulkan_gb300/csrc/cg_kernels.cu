@@ -3,18 +3,22 @@
 // triangle-pair (Moller) narrow phase.
 //
 // Traversal design. Each warp owns a node-pair deque in shared memory and
-// advances up to 32 node pairs per step, one per lane: load both child-box
-// records (four 16-byte loads each), move B's box into A's space, run the
-// 15-axis SAT, and apply the reference's descent rule
-// (OBBtree::IntersectOBBtreesRecursive, src/Geometry/OBBtree.cpp:414-476):
-// two inner nodes -> split the one with the larger surface, ties to the first
-// tree; one leaf -> split the other; two leaves -> a candidate leaf pair.
-// Surviving child pairs are pushed with __ballot_sync/__popc compaction, and
-// leaf pairs are buffered per warp; once leaf_flush of them are buffered the
-// warp runs their triangle pairs, one pair per lane. Load balance across warps
-// uses a global task queue: root pairs of all queries are the first slots, and
-// a warp with surplus work gives the bottom (shallowest) entries of its deque
-// to warps that are waiting. Every wait is bounded by wait_ns (globaltimer),
+// advances up to 32 node pairs per step, one per lane: load both box records
+// (four 16-byte loads each), move B's box into A's space, run the 15-axis SAT,
+// and apply the reference's descent rule (OBBtree::IntersectOBBtreesRecursive,
+// src/Geometry/OBBtree.cpp:414-476): two inner nodes -> split the one with the
+// larger surface, ties to the first tree; one leaf -> split the other; two
+// leaves -> a candidate leaf pair. Surviving child pairs are pushed with
+// __ballot_sync/__popc compaction; leaf pairs are buffered per warp, and once
+// leaf_flush of them are buffered the warp runs their triangle pairs, one pair
+// per lane.
+//
+// Load balance uses a global task queue. Tasks are chunks of up to 32 node
+// pairs in a pool; the root pairs of all queries are the first slots. A warp
+// whose deque runs dry claims the next slot and waits for it; a warp with
+// fewer than 32 node pairs tops up with already published slots without
+// waiting; a warp with surplus gives half of the bottom (shallowest) part of
+// its deque to waiting warps. Every wait is bounded by wait_ns (globaltimer),
 // after which the kernel records ERR_TIMEOUT and returns.
 #include <cuda_runtime.h>
 
@@ -42,6 +46,11 @@ __device__ __forceinline__ unsigned ld_relaxed(const unsigned* p) {
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -53,11 +62,23 @@ __device__ __forceinline__ uint4 ld_relaxed4(const uint4* p) {
                  : "memory");
     return v;
 }
+__device__ __forceinline__ uint2 ld_relaxed2(const uint2* p) {
+    uint2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
 }
+
+// head in the low 32 bits, tail in the high 32 bits of Counters::ht.
+__device__ __forceinline__ unsigned long long* ht_of(Counters* c) {
+    return reinterpret_cast<unsigned long long*>(&c->head);
+}
+__device__ __forceinline__ uint32_t ht_head(unsigned long long v) { return uint32_t(v); }
+__device__ __forceinline__ uint32_t ht_tail(unsigned long long v) { return uint32_t(v >> 32); }
 
 struct Rec {
     Box box;
@@ -89,6 +110,10 @@ __device__ __forceinline__ Mat4 load_mat(const PackedQuery* Q) {
     return M;
 }
 
+__device__ __forceinline__ const float4* load_ptr(const float4* const* p) {
+    return reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(p)));
+}
+
 __device__ __forceinline__ void load_tri(const float4* tris, uint32_t i, float3& p0, float3& p1, float3& p2) {
     const float4* p = tris + 3ull * i;
     const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
@@ -97,22 +122,84 @@ __device__ __forceinline__ void load_tri(const float4* tris, uint32_t i, float3&
     p2 = make_float3(c.x, c.y, c.z);
 }
 
-// Claims the next queue slot (lane 0 only). Root slots are immediate; a
-// donated slot is waited for until it is published, all work is finished, an
-// error is raised, or the wait limit passes.
-__device__ int acquire(const TraverseParams& P, uint32_t& q, uint32_t& a, uint32_t& b) {
-    const unsigned slot = atomicAdd(&P.ctr->head, 1u);
-    if (slot < P.n_queries) {
-        q = slot;
-        a = 1;
-        b = 1;
-        return 1;
+// The same 15 axes in the same order as cg::sat, as loops (a's then b's face
+// normals, then a_i x b_j) to keep the traversal kernel's code small.
+__device__ __forceinline__ bool sat_rolled(const Box& a, const Box& b) {
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+        const float3 u = s ? b.u : a.u;
+        const float3 v = s ? b.v : a.v;
+        const float3 w = s ? b.w : a.w;
+        if (!overlap_on(a, b, cross3(v, w))) return false;
+        if (!overlap_on(a, b, cross3(u, w))) return false;
+        if (!overlap_on(a, b, cross3(u, v))) return false;
     }
-    const unsigned idx = slot - P.n_queries;
-    if (idx >= P.task_slots) {
-        // Only reachable if more warps wait than the slack allows; nothing
-        // can ever be published there, so wait for the end of all work.
-        const unsigned long long t0 = gtimer();
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+        const float3 e = i == 0 ? a.u : (i == 1 ? a.v : a.w);
+        if (!overlap_on(a, b, cross3(e, b.u))) return false;
+        if (!overlap_on(a, b, cross3(e, b.v))) return false;
+        if (!overlap_on(a, b, cross3(e, b.w))) return false;
+    }
+    return true;
+}
+
+struct Deque {
+    uint32_t* q;
+    uint32_t* a;
+    uint32_t* b;
+    uint32_t mask;
+};
+
+struct LeafBuf {
+    uint32_t* q;
+    uint32_t* oa;
+    uint32_t* ob;
+    uint32_t* cn;  // count_a | count_b << 16
+    uint32_t* pre; // kLeafCap + 1 exclusive prefix sums of count_a * count_b
+};
+
+// Reads the chunk of slot `slot` (already published) into the deque at `top`;
+// returns its size (uniform over the warp).
+__device__ uint32_t take_chunk(const TraverseParams& P, uint32_t slot, const Deque& D, uint32_t top, int lane) {
+    uint32_t off = 0, cnt = 1;
+    // Lane 0 observed the slot's release (wait_ready); the barrier orders the
+    // other lanes' pool reads after that acquire.
+    __syncwarp();
+    if (slot >= P.n_queries) {
+        if (lane == 0) {
+            const uint2 c = ld_relaxed2(P.slots + (slot - P.n_queries));
+            off = c.x;
+            cnt = c.y;
+        }
+        off = __shfl_sync(kFull, off, 0);
+        cnt = __shfl_sync(kFull, cnt, 0);
+        if (uint32_t(lane) < cnt) {
+            const uint4 e = ld_relaxed4(P.pool + off + lane);
+            const uint32_t pos = (top + lane) & D.mask;
+            D.q[pos] = e.x;
+            D.a[pos] = e.y;
+            D.b[pos] = e.z;
+        }
+    } else if (lane == 0) {
+        const uint32_t pos = top & D.mask;
+        D.q[pos] = slot;
+        D.a[pos] = 1;
+        D.b[pos] = 1;
+    }
+    __syncwarp();
+    return cnt;
+}
+
+// Lane 0: waits until donated slot `slot` is published. Returns 0 when all
+// work finished, an error was raised, or the wait limit passed.
+__device__ int wait_ready(const TraverseParams& P, uint32_t slot) {
+    if (slot < P.n_queries) return 1;
+    const uint32_t idx = slot - P.n_queries;
+    const unsigned long long t0 = gtimer();
+    if (idx >= P.slot_alloc) {
+        // Past every slot a donor could publish: only the end of the work or
+        // an error can release this warp.
         while (ld_relaxed(&P.ctr->work) != 0 && ld_relaxed(&P.ctr->error) == 0) {
             if (gtimer() - t0 > P.wait_ns) {
                 atomicOr(&P.ctr->error, ERR_TIMEOUT);
@@ -122,16 +209,9 @@ __device__ int acquire(const TraverseParams& P, uint32_t& q, uint32_t& a, uint32
         }
         return 0;
     }
-    const unsigned long long t0 = gtimer();
     unsigned ns = 32;
     for (;;) {
-        if (ld_acquire(P.ready + idx)) {
-            const uint4 t = ld_relaxed4(P.tasks + idx);
-            q = t.x;
-            a = t.y;
-            b = t.z;
-            return 1;
-        }
+        if (ld_acquire(P.ready + idx)) return 1;
         if (ld_relaxed(&P.ctr->work) == 0) return 0;
         if (ld_relaxed(&P.ctr->error) != 0) return 0;
         if (gtimer() - t0 > P.wait_ns) {
@@ -143,13 +223,21 @@ __device__ int acquire(const TraverseParams& P, uint32_t& q, uint32_t& a, uint32
     }
 }
 
-struct LeafBuf {
-    uint32_t* q;
-    uint32_t* oa;
-    uint32_t* ob;
-    uint32_t* cn;  // count_a | count_b << 16
-    uint32_t* pre; // kLeafCap + 1 exclusive prefix sums of count_a * count_b
-};
+// Lane 0: claims a slot below the tail without waiting for new donations.
+// A claimed slot below the tail is published promptly by its donor.
+__device__ int try_claim(const TraverseParams& P, unsigned long long ht, uint32_t& slot) {
+    unsigned long long* w = ht_of(P.ctr);
+    for (int tries = 0; tries < 4; ++tries) {
+        if (int(ht_tail(ht) - ht_head(ht)) <= 0) return 0;
+        const unsigned long long prev = atomicCAS(w, ht, ht + 1ull);
+        if (prev == ht) {
+            slot = ht_head(ht);
+            return 1;
+        }
+        ht = prev;
+    }
+    return 0;
+}
 
 // Runs every triangle pair of the buffered leaf pairs, one pair per lane, in
 // the order of the reference's pair loop per leaf pair
@@ -182,23 +270,21 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
     L.pre[lane + 32] = tot0 + s1 - c1;
     if (lane == 0) L.pre[kLeafCap] = total;
 
+    unsigned long long lbase = 0;
+    if (lane == 0) lbase = atomicAdd(&P.ctr->n_leafs, (unsigned long long)nl);
     if (P.flags & CG_KEEP_LEAF_PAIRS) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&P.ctr->n_leafs, (unsigned long long)nl);
-        base = __shfl_sync(kFull, base, 0);
+        lbase = __shfl_sync(kFull, lbase, 0);
         for (uint32_t e = lane; e < nl; e += 32) {
-            if (base + e < P.leafs_cap) {
+            if (lbase + e < P.leafs_cap) {
                 cg_leaf_pair lp;
                 lp.query = L.q[e];
                 lp.offset_a = L.oa[e];
                 lp.offset_b = L.ob[e];
                 lp.count_a = uint16_t(L.cn[e] & 0xffffu);
                 lp.count_b = uint16_t(L.cn[e] >> 16);
-                P.leafs[base + e] = lp;
+                P.leafs[lbase + e] = lp;
             }
         }
-    } else {
-        if (lane == 0) atomicAdd(&P.ctr->n_leafs, (unsigned long long)nl);
     }
     __syncwarp();
 
@@ -226,11 +312,9 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
             ib = L.ob[lo] + j;
             const PackedQuery* Q = P.q + q;
             const Mat4 M = load_mat(Q);
-            const float4* tris_a = reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(&Q->tris_a)));
-            const float4* tris_b = reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(&Q->tris_b)));
             float3 a0, a1, a2, b0, b1, b2;
-            load_tri(tris_a, ia, a0, a1, a2);
-            load_tri(tris_b, ib, b0, b1, b2);
+            load_tri(load_ptr(&Q->tris_a), ia, a0, a1, a2);
+            load_tri(load_ptr(&Q->tris_b), ib, b0, b1, b2);
             b0 = xform(M, b0, 1.0f);
             b1 = xform(M, b1, 1.0f);
             b2 = xform(M, b2, 1.0f);
@@ -272,38 +356,41 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const uint32_t S = P.stack_cap;
-    const uint32_t MASK = S - 1u;
-    uint32_t* sq = smem + size_t(warp) * warp_smem_words(S);
-    uint32_t* sa = sq + S;
-    uint32_t* sb = sa + S;
+    Deque D;
+    D.q = smem + size_t(warp) * warp_smem_words(S);
+    D.a = D.q + S;
+    D.b = D.a + S;
+    D.mask = S - 1u;
     LeafBuf L;
-    L.q = sb + S;
+    L.q = D.b + S;
     L.oa = L.q + kLeafCap;
     L.ob = L.oa + kLeafCap;
     L.cn = L.ob + kLeafCap;
     L.pre = L.cn + kLeafCap;
+    unsigned long long* ht = ht_of(P.ctr);
 
-    uint32_t top = 0, bot = 0, nl = 0;
-    unsigned long long st_nodes = 0, st_tests = 0, st_frag = 0, st_don = 0;
+    uint32_t top = 0, bot = 0, nl = 0, held_tasks = 0;
+    unsigned long long st_nodes = 0, st_tests = 0, st_frag = 0, st_don = 0, st_steps = 0;
 
     for (;;) {
         if (top == bot) {
-            uint32_t tq = 0, ta = 0, tb = 0;
+            // Out of work: claim the next slot and wait for it.
+            uint32_t slot = 0;
             int got = 0;
-            if (lane == 0) got = acquire(P, tq, ta, tb);
+            if (lane == 0) {
+                slot = ht_head(atomicAdd(ht, 1ull));
+                got = wait_ready(P, slot);
+            }
             got = __shfl_sync(kFull, got, 0);
             if (!got) break;
-            tq = __shfl_sync(kFull, tq, 0);
-            ta = __shfl_sync(kFull, ta, 0);
-            tb = __shfl_sync(kFull, tb, 0);
-            if (lane == 0) {
-                sq[top & MASK] = tq;
-                sa[top & MASK] = ta;
-                sb[top & MASK] = tb;
-            }
-            ++top;
-            __syncwarp();
+            slot = __shfl_sync(kFull, slot, 0);
+            top += take_chunk(P, slot, D, top, lane);
+            held_tasks = 1;
         }
+
+        // Queue state, read early so its latency overlaps the step's loads.
+        unsigned long long qs = 0;
+        if (lane == 0) qs = ld_relaxed64(ht);
 
         // ---- one step over up to 32 node pairs from the top of the deque
         const uint32_t size = top - bot;
@@ -311,10 +398,10 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
         const bool active = uint32_t(lane) < n;
         uint32_t q = 0, ra = 0, rb = 0;
         if (active) {
-            const uint32_t pos = (top - n + lane) & MASK;
-            q = sq[pos];
-            ra = sa[pos];
-            rb = sb[pos];
+            const uint32_t pos = (top - n + lane) & D.mask;
+            q = D.q[pos];
+            ra = D.a[pos];
+            rb = D.b[pos];
         }
         top -= n;
         __syncwarp();
@@ -323,14 +410,14 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
         uint32_t child = 0, offA = 0, offB = 0, cnt = 0;
         if (active) {
             const PackedQuery* Q = P.q + q;
-            const float4* recs_a = reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(&Q->recs_a)));
-            const float4* recs_b = reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(&Q->recs_b)));
+            const float4* recs_a = load_ptr(&Q->recs_a);
+            const float4* recs_b = load_ptr(&Q->recs_b);
             if (recs_a != nullptr && recs_b != nullptr) {
                 const Mat4 M = load_mat(Q);
                 const Rec A = load_rec(recs_a, ra);
                 const Rec B = load_rec(recs_b, rb);
                 const Box bb = xform_box(M, B.box);
-                if (sat(A.box, bb)) {
+                if (sat_rolled(A.box, bb)) {
                     const bool la = (A.meta & kLeafFlag) != 0;
                     const bool lb = (B.meta & kLeafFlag) != 0;
                     if (!la && !lb)
@@ -352,21 +439,21 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
         const unsigned pushmask = __ballot_sync(kFull, act == 1 || act == 2);
         if (act == 1 || act == 2) {
             const uint32_t r = __popc(pushmask & lanemask_lt());
-            const uint32_t p0 = (top + 2u * r) & MASK;
-            const uint32_t p1 = (top + 2u * r + 1u) & MASK;
+            const uint32_t p0 = (top + 2u * r) & D.mask;
+            const uint32_t p1 = (top + 2u * r + 1u) & D.mask;
             const uint32_t c_left = 2u * child + 2u, c_right = 2u * child + 3u;
-            sq[p0] = q;
-            sq[p1] = q;
+            D.q[p0] = q;
+            D.q[p1] = q;
             if (act == 1) {
-                sa[p0] = c_right;
-                sb[p0] = rb;
-                sa[p1] = c_left;
-                sb[p1] = rb;
+                D.a[p0] = c_right;
+                D.b[p0] = rb;
+                D.a[p1] = c_left;
+                D.b[p1] = rb;
             } else {
-                sa[p0] = ra;
-                sb[p0] = c_right;
-                sa[p1] = ra;
-                sb[p1] = c_left;
+                D.a[p0] = ra;
+                D.b[p0] = c_right;
+                D.a[p1] = ra;
+                D.b[p1] = c_left;
             }
         }
         top += 2u * __popc(pushmask);
@@ -380,7 +467,10 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
             L.cn[slot] = cnt;
         }
         nl += __popc(leafmask);
-        if (lane == 0) st_nodes += n;
+        if (lane == 0) {
+            st_nodes += n;
+            ++st_steps;
+        }
         __syncwarp();
 
         if (nl >= P.leaf_flush || (top == bot && nl > 0)) {
@@ -388,42 +478,60 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
             nl = 0;
         }
 
-        // ---- give the bottom of the deque away: when it is nearly full
-        // (forced), or when other warps wait for work.
+        // ---- balance: give half of the bottom of the deque to waiting warps
+        // (all of a chunk when the deque is nearly full), or top up from
+        // published chunks when fewer than 32 node pairs are left.
         const uint32_t held = top - bot;
-        if (held >= P.donate_min) {
-            const bool forced = held + 64u > S;
-            int give = 0;
-            if (lane == 0) {
-                const unsigned tail = ld_relaxed(&P.ctr->tail);
-                const unsigned head = ld_relaxed(&P.ctr->head);
-                const bool waiting = int(tail - head) < 0;
-                const uint32_t k = min(32u, held - 32u);
-                if ((forced || waiting) && tail - P.n_queries + k <= P.task_cap) {
-                    atomicAdd(&P.ctr->work, k);
-                    give = int(atomicAdd(&P.ctr->tail, k) - P.n_queries);
-                    give = give + 1;  // 0 means "no donation"
+        const bool forced = held + 64u > S;
+        int mode = 0;  // 1: donate k, 2: top up from slot
+        uint32_t k = 0, base = 0, slot = 0;
+        if (lane == 0) {
+            const bool waiting = int(ht_tail(qs) - ht_head(qs)) < 0;
+            if (forced || (waiting && held >= P.donate_min)) {
+                k = forced ? 32u : min(32u, held >> 1);
+                const unsigned pt = ld_relaxed(&P.ctr->pool_tail);
+                if (pt + k <= P.pool_cap && ht_tail(qs) - P.n_queries < P.slot_cap) {
+                    atomicAdd(&P.ctr->work, 1u);
+                    base = atomicAdd(&P.ctr->pool_tail, k);
+                    slot = ht_tail(atomicAdd(ht, 1ull << 32));
+                    mode = 1;
+                } else if (forced) {
+                    atomicOr(&P.ctr->error, ERR_QUEUE);
+                    mode = -1;
                 }
-            }
-            give = __shfl_sync(kFull, give, 0);
-            const uint32_t k = min(32u, held - 32u);
-            if (give > 0) {
-                const uint32_t idx = uint32_t(give - 1) + lane;
-                if (uint32_t(lane) < k) {
-                    const uint32_t pos = (bot + lane) & MASK;
-                    P.tasks[idx] = make_uint4(sq[pos], sa[pos], sb[pos], 0u);
-                    st_release(P.ready + idx, 1u);
-                }
-                bot += k;
-                if (lane == 0) st_don += k;
-                __syncwarp();
-            } else if (forced) {
-                if (lane == 0) atomicOr(&P.ctr->error, ERR_QUEUE);
-                break;
+            } else if (held < 32u && held > 0u && !waiting) {
+                if (try_claim(P, qs, slot)) mode = wait_ready(P, slot) ? 2 : -1;
             }
         }
+        mode = __shfl_sync(kFull, mode, 0);
+        if (mode == -1) break;
+        if (mode == 1) {
+            k = __shfl_sync(kFull, k, 0);
+            base = __shfl_sync(kFull, base, 0);
+            slot = __shfl_sync(kFull, slot, 0);
+            if (uint32_t(lane) < k) {
+                const uint32_t pos = (bot + lane) & D.mask;
+                P.pool[base + lane] = make_uint4(D.q[pos], D.a[pos], D.b[pos], 0u);
+            }
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) {
+                P.slots[slot - P.n_queries] = make_uint2(base, k);
+                st_release(P.ready + (slot - P.n_queries), 1u);
+                st_don += k;
+            }
+            bot += k;
+            __syncwarp();
+        } else if (mode == 2) {
+            slot = __shfl_sync(kFull, slot, 0);
+            top += take_chunk(P, slot, D, top, lane);
+            ++held_tasks;
+        }
 
-        if (top == bot && lane == 0) atomicSub(&P.ctr->work, 1u);
+        if (top == bot) {
+            if (lane == 0) atomicSub(&P.ctr->work, held_tasks);
+            held_tasks = 0;
+        }
     }
 
     if (lane == 0) {
@@ -431,6 +539,7 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
         atomicAdd(&P.ctr->tri_tests, st_tests);
         atomicAdd(&P.ctr->fragile, st_frag);
         atomicAdd(&P.ctr->donations, st_don);
+        atomicAdd(&P.ctr->warp_steps, st_steps);
     }
 }
 
@@ -458,11 +567,27 @@ __global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees
     out[i] = p;
 }
 
-__global__ void init_kernel(Counters* ctr, uint32_t n_queries) {
-    Counters c = {};
-    c.tail = n_queries;
-    c.work = n_queries;
-    *ctr = c;
+// Resets the counters for a launch over n_queries and clears the ready flags
+// of the slots the previous launch published (their count is still in the
+// counters).
+__global__ void init_kernel(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries) {
+    __shared__ uint32_t used;
+    if (threadIdx.x == 0) {
+        const unsigned long long ht = *reinterpret_cast<unsigned long long*>(&ctr->head);
+        const uint32_t tail = uint32_t(ht >> 32);
+        const uint32_t prev_n = ctr->n_queries;
+        used = tail > prev_n ? min(tail - prev_n, slot_alloc) : 0u;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < used; i += blockDim.x) ready[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Counters c = {};
+        c.tail = n_queries;
+        c.work = n_queries;
+        c.n_queries = n_queries;
+        *ctr = c;
+    }
 }
 
 // Paralgram::GetSurface of every record, written into q3.z.
@@ -486,8 +611,8 @@ cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, ui
     return cudaGetLastError();
 }
 
-cudaError_t launch_init(Counters* ctr, uint32_t n_queries, cudaStream_t s) {
-    init_kernel<<<1, 1, 0, s>>>(ctr, n_queries);
+cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries, cudaStream_t s) {
+    init_kernel<<<1, 1024, 0, s>>>(ctr, ready, slot_alloc, n_queries);
     return cudaGetLastError();
 }
 
