@@ -158,6 +158,7 @@ typedef struct cg_stats {
 
 #define CG_KEEP_LEAF_PAIRS 1u /* also write the candidate leaf pairs */
 #define CG_NO_TRI_PAIRS 2u    /* count triangle tests and hits but do not write pairs */
+#define CG_TRACE 4u           /* record a utilisation timeline (see cg_read_trace) */
 
 /* Host queries in, stats out; synchronous. Results stay on the device until read. */
 int cg_collide(cg_ctx* ctx, const cg_query* queries, uint32_t n, uint32_t flags, cg_stats* stats);
@@ -174,6 +175,13 @@ int cg_device_results(cg_ctx* ctx, const cg_tri_pair** pairs, const unsigned lon
 /* Device time of the last traversal kernel (the dominant kernel of a collide
  * step), from CUDA events recorded around its launch; waits for it. */
 int cg_traversal_time_ms(cg_ctx* ctx, float* ms);
+
+/* Utilisation timeline of the last launch made with CG_TRACE: per time bucket
+ * of bucket_ns nanoseconds since the traversal started, four counters (busy
+ * lanes summed over traversal steps, traversal steps, triangle tests, triangle
+ * passes). bucket_ns (if non-zero) sets the width for later launches; out
+ * receives n_buckets x 4 values (at most 512 buckets). */
+int cg_read_trace(cg_ctx* ctx, uint32_t bucket_ns, uint32_t* out, uint32_t n_buckets);
 
 /* CUDA graph of one whole collide step over device-resident queries
  * (counter reset, query packing, persistent traversal + narrow phase). */

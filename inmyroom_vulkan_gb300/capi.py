@@ -19,12 +19,13 @@ STATUS = {0: "CG_OK", -1: "CG_ERR_INVALID_ARGUMENT", -2: "CG_ERR_CUDA", -3: "CG_
           -8: "CG_ERR_NOT_FOUND"}
 CG_KEEP_LEAF_PAIRS = 1
 CG_NO_TRI_PAIRS = 2
+CG_TRACE = 4
 
 # Every function the header declares (checked by the CPU tests).
 EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",
            "cg_last_error", "cg_tree_upload", "cg_tree_free", "cg_relative_matrix", "cg_collide", "cg_collide_async",
            "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results",
-           "cg_traversal_time_ms", "cg_graph_capture", "cg_graph_launch"]
+           "cg_traversal_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch"]
 
 
 class CgError(RuntimeError):
@@ -97,6 +98,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_read_leaf_pairs.argtypes = [vp, vp, u64, C.POINTER(u64)]
     lib.cg_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
     lib.cg_traversal_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    lib.cg_read_trace.argtypes = [vp, u32, vp, u32]
     lib.cg_graph_capture.argtypes = [vp, vp, u32, u32]
     lib.cg_graph_launch.argtypes = [vp, vp]
     _lib = lib
@@ -260,6 +262,15 @@ class Context:
         ms = C.c_float()
         self._check(self.lib.cg_traversal_time_ms(self.h, C.byref(ms)), "cg_traversal_time_ms")
         return ms.value
+
+    def set_trace_bucket(self, bucket_ns: int):
+        self._check(self.lib.cg_read_trace(self.h, bucket_ns, None, 0), "cg_read_trace")
+
+    def trace(self, n_buckets: int = 512) -> np.ndarray:
+        """(n_buckets, 4): busy lanes, traversal steps, triangle tests, triangle passes."""
+        out = np.zeros((n_buckets, 4), np.uint32)
+        self._check(self.lib.cg_read_trace(self.h, 0, out.ctypes.data, n_buckets), "cg_read_trace")
+        return out
 
     def graph_capture(self, d_queries_ptr: int, n: int, flags: int = 0):
         self._check(self.lib.cg_graph_capture(self.h, d_queries_ptr, n, flags), "cg_graph_capture")

@@ -1,14 +1,14 @@
 // Host side of the C ABI declared in include/collide_gpu.h: context and
-// buffers, tree upload with validation, launches, result read-back and the
-// CUDA graph of one collide step.
+// buffers, tree arenas with upload validation, launches, result read-back and
+// the CUDA graph of one collide step.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "cg_internal.h"
@@ -16,23 +16,99 @@
 
 using namespace cg;
 
+namespace {
+
+// A growable device array of fixed-size units (a unit is `width` float4s)
+// with first-fit reuse of released ranges. Growth copies the contents to a
+// larger allocation at the same offsets, so indices stay valid; the base
+// pointer changes and `gen` counts those changes.
+struct Arena {
+    float4* ptr = nullptr;
+    uint32_t width = 1;
+    uint64_t cap = 0;
+    uint64_t used = 0;
+    uint64_t gen = 0;
+    std::vector<std::pair<uint64_t, uint64_t>> free_list;  // (offset, units), sorted by offset
+
+    cudaError_t alloc(uint64_t n, uint64_t* off, cudaStream_t s) {
+        for (size_t i = 0; i < free_list.size(); ++i) {
+            if (free_list[i].second >= n) {
+                *off = free_list[i].first;
+                free_list[i].first += n;
+                free_list[i].second -= n;
+                if (free_list[i].second == 0) free_list.erase(free_list.begin() + long(i));
+                return cudaSuccess;
+            }
+        }
+        if (used + n > cap) {
+            uint64_t ncap = std::max<uint64_t>(std::max<uint64_t>(cap * 2, used + n), 1u << 14);
+            float4* np = nullptr;
+            cudaError_t e = cudaMalloc(&np, sizeof(float4) * width * ncap);
+            if (e != cudaSuccess) return e;
+            if (used) {
+                e = cudaStreamSynchronize(s);
+                if (e == cudaSuccess)
+                    e = cudaMemcpy(np, ptr, sizeof(float4) * width * used, cudaMemcpyDeviceToDevice);
+                if (e != cudaSuccess) {
+                    cudaFree(np);
+                    return e;
+                }
+            }
+            cudaFree(ptr);
+            ptr = np;
+            cap = ncap;
+            ++gen;
+        }
+        *off = used;
+        used += n;
+        return cudaSuccess;
+    }
+
+    void release(uint64_t off, uint64_t n) {
+        if (n == 0) return;
+        auto it = std::lower_bound(free_list.begin(), free_list.end(), std::make_pair(off, uint64_t(0)));
+        it = free_list.insert(it, {off, n});
+        size_t i = size_t(it - free_list.begin());
+        if (i + 1 < free_list.size() && free_list[i].first + free_list[i].second == free_list[i + 1].first) {
+            free_list[i].second += free_list[i + 1].second;
+            free_list.erase(free_list.begin() + long(i + 1));
+        }
+        if (i > 0 && free_list[i - 1].first + free_list[i - 1].second == free_list[i].first) {
+            free_list[i - 1].second += free_list[i].second;
+            free_list.erase(free_list.begin() + long(i));
+            --i;
+        }
+        if (free_list[i].first + free_list[i].second == used) {
+            used = free_list[i].first;
+            free_list.erase(free_list.begin() + long(i));
+        }
+    }
+
+    void destroy() {
+        cudaFree(ptr);
+        ptr = nullptr;
+        cap = used = 0;
+        free_list.clear();
+    }
+};
+
+}  // namespace
+
 struct cg_ctx {
     cg_config cfg{};
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
-    bool own_stream = true;
     uint32_t blocks = 0;  // persistent grid
 
     // trees
     struct Slot {
-        DevTree t{};
-        float4* recs = nullptr;
-        float4* tris = nullptr;
+        uint64_t rec_base = 0, n_recs = 0, tri_base = 0, n_tris = 0;
         float* nrm = nullptr;
         bool live = false;
     };
     std::vector<Slot> trees;
+    Arena recs, tris;
     DevTree* d_trees = nullptr;
     uint32_t d_trees_cap = 0;
 
@@ -46,20 +122,22 @@ struct cg_ctx {
     uint32_t pool_cap = 0;          // entries donors may reserve
     uint32_t slot_cap = 0;          // slots donors may reserve
     uint32_t pool_alloc = 0, slot_alloc = 0;  // allocated, with slack for concurrent reservations
-    cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
     cg_tri_pair* d_pairs = nullptr;
     cg_leaf_pair* d_leafs = nullptr;
+    unsigned int* d_trace = nullptr;
+    uint32_t trace_ns = 0;
 
     cg_query* h_queries = nullptr;  // pinned
     Counters* h_ctr = nullptr;      // pinned
 
     uint32_t last_flags = 0;
-    bool launched = false;
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_gen = 0;         // arena generations the graph was captured with
     bool capturing = false;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // around the traversal kernel
+    cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
 
     std::string err;
 };
@@ -83,13 +161,15 @@ int cuda_fail(cg_ctx* c, cudaError_t e, const char* what) {
     return fail(c, code, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CG_CUDA(call, what)                                 \
-    do {                                                    \
-        cudaError_t e_ = (call);                            \
+#define CG_CUDA(call, what)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
         if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
     } while (0)
 
 bool pow2(uint32_t x) { return x && !(x & (x - 1)); }
+
+uint64_t arena_gen(const cg_ctx* c) { return c->recs.gen * 1000003ull + c->tris.gen; }
 
 void free_buffers(cg_ctx* c) {
     cudaFree(c->d_queries);
@@ -100,6 +180,7 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_ready);
     cudaFree(c->d_pairs);
     cudaFree(c->d_leafs);
+    cudaFree(c->d_trace);
     cudaFreeHost(c->h_queries);
     cudaFreeHost(c->h_ctr);
     c->d_queries = nullptr;
@@ -110,6 +191,7 @@ void free_buffers(cg_ctx* c) {
     c->d_ready = nullptr;
     c->d_pairs = nullptr;
     c->d_leafs = nullptr;
+    c->d_trace = nullptr;
     c->h_queries = nullptr;
     c->h_ctr = nullptr;
 }
@@ -125,8 +207,8 @@ int check_config(cg_ctx* c, const cg_config* cfg) {
     if (cfg->max_queries == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_queries must be > 0");
     if (!pow2(cfg->stack_entries) || cfg->stack_entries < 256 || cfg->stack_entries > 4096)
         return fail(c, CG_ERR_INVALID_ARGUMENT, "stack_entries must be a power of two in [256, 4096]");
-    if (cfg->warps_per_block == 0 || cfg->warps_per_block > 16)
-        return fail(c, CG_ERR_INVALID_ARGUMENT, "warps_per_block must be in [1, 16]");
+    if (cfg->warps_per_block == 0 || cfg->warps_per_block > 8)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "warps_per_block must be in [1, 8]");
     if (cfg->leaf_flush == 0 || cfg->leaf_flush > uint32_t(kLeafCap - 32 + 1))
         return fail(c, CG_ERR_INVALID_ARGUMENT, "leaf_flush must be in [1, %d]", kLeafCap - 32 + 1);
     if (cfg->queue_capacity < 1024) return fail(c, CG_ERR_INVALID_ARGUMENT, "queue_capacity must be >= 1024");
@@ -138,8 +220,9 @@ int alloc_buffers(cg_ctx* c) {
     const cg_config& g = c->cfg;
     int occ = 0;
     CG_CUDA(traverse_occupancy(g.warps_per_block, g.stack_entries, &occ), "occupancy");
-    if (occ < 1) return fail(c, CG_ERR_INVALID_ARGUMENT, "traversal kernel does not fit: %u warps x %u stack entries",
-                             g.warps_per_block, g.stack_entries);
+    if (occ < 1)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "traversal kernel does not fit: %u warps x %u stack entries",
+                    g.warps_per_block, g.stack_entries);
     const int per_sm = g.blocks_per_sm ? std::min<int>(occ, int(g.blocks_per_sm)) : occ;
     c->blocks = uint32_t(per_sm * c->sm_count);
     const uint32_t warps = c->blocks * g.warps_per_block;
@@ -175,7 +258,11 @@ int sync_tree_table(cg_ctx* c) {
         c->d_trees_cap = cap;
     }
     std::vector<DevTree> host(n);
-    for (uint32_t i = 0; i < n; ++i) host[i] = c->trees[i].live ? c->trees[i].t : DevTree{};
+    for (uint32_t i = 0; i < n; ++i) {
+        const auto& s = c->trees[i];
+        host[i] = DevTree{uint32_t(s.rec_base), uint32_t(s.tri_base), uint32_t(s.n_recs), uint32_t(s.n_tris),
+                          s.live ? 1u : 0u, 0u, s.nrm};
+    }
     if (n) CG_CUDA(cudaMemcpy(c->d_trees, host.data(), sizeof(DevTree) * n, cudaMemcpyHostToDevice), "upload tree table");
     return CG_OK;
 }
@@ -190,13 +277,16 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
     rec[3] = make_float4(r, m, 0.f, 0.f);
 }
 
-// Enqueues counter reset, flag reset, packing and the traversal on `s`.
+// Enqueues counter reset, packing and the traversal on `s`.
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s) {
-    CG_CUDA(launch_init(c->d_ctr, c->d_ready, c->slot_alloc, n, s), "init kernel");
+    unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
+    CG_CUDA(launch_init(c->d_ctr, c->d_ready, c->slot_alloc, n, trace, s), "init kernel");
     CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->d_packed, c->d_ctr, s), "pack kernel");
     TraverseParams p{};
     p.q = c->d_packed;
     p.n_queries = n;
+    p.recs = c->recs.ptr;
+    p.tris = c->tris.ptr;
     p.pool = c->d_pool;
     p.slots = c->d_slots;
     p.ready = c->d_ready;
@@ -208,6 +298,8 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     p.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
     p.leafs = c->d_leafs;
     p.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
+    p.trace = trace;
+    p.trace_ns = c->trace_ns ? c->trace_ns : 1000u;
     p.flags = flags;
     p.stack_cap = c->cfg.stack_entries;
     p.donate_min = std::min(std::max(c->cfg.donate_min, 2u), c->cfg.stack_entries - 63u);
@@ -245,6 +337,14 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
     s.status = status;
     if (st) *st = s;
     return status;
+}
+
+int join_stream(cg_ctx* c, cudaStream_t s) {
+    if (s == c->stream) return CG_OK;
+    // later reads on the context stream wait for work enqueued on s
+    CG_CUDA(cudaEventRecord(c->ev_join, s), "event record");
+    CG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "stream wait");
+    return CG_OK;
 }
 
 // glm-convention 4x4 product and inverse (column-major); see cg_relative_matrix.
@@ -346,6 +446,8 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         cg_config_default(&cfg);
     auto* c = new cg_ctx;
     c->cfg = cfg;
+    c->recs.width = 4;
+    c->tris.width = 3;
     int rc = check_config(c, &cfg);
     if (rc != CG_OK) {
         delete c;
@@ -362,7 +464,8 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&c->d_trace, sizeof(unsigned int) * 4 * kTraceBuckets) != cudaSuccess) {
         delete c;
         return CG_ERR_CUDA;
     }
@@ -382,11 +485,9 @@ int cg_destroy(cg_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graph(c);
-    for (auto& s : c->trees) {
-        cudaFree(s.recs);
-        cudaFree(s.tris);
-        cudaFree(s.nrm);
-    }
+    for (auto& s : c->trees) cudaFree(s.nrm);
+    c->recs.destroy();
+    c->tris.destroy();
     cudaFree(c->d_trees);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
@@ -413,7 +514,7 @@ int cg_reconfigure(cg_ctx* c, const cg_config* cfg) {
     drop_graph(c);
     free_buffers(c);
     c->cfg = *cfg;
-    c->launched = false;
+    CG_CUDA(cudaMalloc(&c->d_trace, sizeof(unsigned int) * 4 * kTraceBuckets), "alloc trace");
     return alloc_buffers(c);
 }
 
@@ -447,16 +548,32 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
     if (N == 0 && T > 0xffffu) return fail(c, CG_ERR_BAD_TREE, "leaf root with %u triangles", T);
     cudaSetDevice(c->device);
 
-    const uint32_t n_recs = 2 * N + 2;
+    const uint64_t n_recs = 2ull * N + 2ull;
+    const uint64_t n_tris = std::max<uint64_t>(T, 1);
+    uint64_t rb = 0, tb = 0;
+    CG_CUDA(c->recs.alloc(n_recs, &rb, c->stream), "record arena");
+    cudaError_t e = c->tris.alloc(n_tris, &tb, c->stream);
+    if (e != cudaSuccess) {
+        c->recs.release(rb, n_recs);
+        return cuda_fail(c, e, "triangle arena");
+    }
+    if (rb + n_recs > 0xffffffffull || tb + n_tris > 0x7fffffffull) {
+        c->recs.release(rb, n_recs);
+        c->tris.release(tb, n_tris);
+        return fail(c, CG_ERR_OUT_OF_MEMORY, "arena index space exhausted");
+    }
+
     std::vector<float4> recs(4ull * n_recs, make_float4(0, 0, 0, 0));
-    put_box(&recs[4], v->root_obb, 0, N ? 0u : (kLeafFlag | T));
+    put_box(&recs[4], v->root_obb, N ? uint32_t(rb + 2) : uint32_t(tb), N ? 0u : (kLeafFlag | T));
     for (uint32_t k = 0; k < N; ++k)
         for (int s = 0; s < 2; ++s) {
-            const uint32_t r = 2 * k + 2 + s;
+            const uint64_t r = 2ull * k + 2 + s;
+            const uint32_t ref = v->node_ref[2 * k + s];
             const uint32_t cnt = v->node_tri_count[2 * k + s];
-            put_box(&recs[4ull * r], v->node_obbs[2 * k + s], v->node_ref[2 * k + s], cnt ? (kLeafFlag | cnt) : 0u);
+            const uint32_t abs_ref = cnt ? uint32_t(tb + ref) : uint32_t(rb + 2ull * ref + 2);
+            put_box(&recs[4 * r], v->node_obbs[2 * k + s], abs_ref, cnt ? (kLeafFlag | cnt) : 0u);
         }
-    std::vector<float4> tris(3ull * std::max<uint32_t>(T, 1));
+    std::vector<float4> tris(3ull * n_tris, make_float4(0, 0, 0, 0));
     for (uint32_t t = 0; t < T; ++t)
         for (int k = 0; k < 3; ++k) {
             const float* p = v->triangles_position + 9ull * t + 3 * k;
@@ -467,18 +584,24 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
         }
 
     cg_ctx::Slot slot;
-    CG_CUDA(cudaMalloc(&slot.recs, sizeof(float4) * recs.size()), "alloc tree records");
-    CG_CUDA(cudaMalloc(&slot.tris, sizeof(float4) * tris.size()), "alloc tree triangles");
-    CG_CUDA(cudaMemcpy(slot.recs, recs.data(), sizeof(float4) * recs.size(), cudaMemcpyHostToDevice), "upload records");
-    CG_CUDA(cudaMemcpy(slot.tris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice), "upload triangles");
+    slot.rec_base = rb;
+    slot.n_recs = n_recs;
+    slot.tri_base = tb;
+    slot.n_tris = n_tris;
+    CG_CUDA(cudaMemcpyAsync(c->recs.ptr + 4 * rb, recs.data(), sizeof(float4) * recs.size(), cudaMemcpyHostToDevice,
+                            c->stream),
+            "upload records");
+    CG_CUDA(cudaMemcpyAsync(c->tris.ptr + 3 * tb, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice,
+                            c->stream),
+            "upload triangles");
     if (v->triangles_normal && T) {
         CG_CUDA(cudaMalloc(&slot.nrm, sizeof(float) * 9ull * T), "alloc normals");
-        CG_CUDA(cudaMemcpy(slot.nrm, v->triangles_normal, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice),
+        CG_CUDA(cudaMemcpyAsync(slot.nrm, v->triangles_normal, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice,
+                                c->stream),
                 "upload normals");
     }
-    CG_CUDA(launch_surfaces(slot.recs, n_recs, c->stream), "surface kernel");
-    CG_CUDA(cudaStreamSynchronize(c->stream), "surface kernel");
-    slot.t = DevTree{slot.recs, slot.tris, slot.nrm, n_recs, T};
+    CG_CUDA(launch_surfaces(c->recs.ptr, uint32_t(rb), uint32_t(n_recs), c->stream), "surface kernel");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "tree upload");
     slot.live = true;
 
     uint32_t id = uint32_t(c->trees.size());
@@ -503,8 +626,8 @@ int cg_tree_free(cg_ctx* c, uint32_t id) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     auto& s = c->trees[id];
-    cudaFree(s.recs);
-    cudaFree(s.tris);
+    c->recs.release(s.rec_base, s.n_recs);
+    c->tris.release(s.tri_base, s.n_tris);
     cudaFree(s.nrm);
     s = cg_ctx::Slot{};
     return sync_tree_table(c);
@@ -512,19 +635,14 @@ int cg_tree_free(cg_ctx* c, uint32_t id) {
 
 int cg_collide_async(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, void* stream) {
     if (!c || (n && !d_queries)) return CG_ERR_INVALID_ARGUMENT;
-    if (n > c->cfg.max_queries) return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    if (n > c->cfg.max_queries)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     c->last_flags = flags;
     int rc = enqueue_step(c, d_queries, n, flags, s);
     if (rc != CG_OK) return rc;
-    c->launched = true;
-    if (s != c->stream) {
-        // later reads on the context stream wait for this launch
-        CG_CUDA(cudaEventRecord(c->ev_join, s), "event record");
-        CG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "stream wait");
-    }
-    return CG_OK;
+    return join_stream(c, s);
 }
 
 int cg_sync_stats(cg_ctx* c, cg_stats* st) {
@@ -537,7 +655,8 @@ int cg_sync_stats(cg_ctx* c, cg_stats* st) {
 
 int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, cg_stats* st) {
     if (!c || (n && !queries)) return CG_ERR_INVALID_ARGUMENT;
-    if (n > c->cfg.max_queries) return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    if (n > c->cfg.max_queries)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t a = queries[i].tree_a, b = queries[i].tree_b;
         if (a >= c->trees.size() || !c->trees[a].live || b >= c->trees.size() || !c->trees[b].live)
@@ -552,7 +671,6 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
     c->last_flags = flags;
     int rc = enqueue_step(c, c->d_queries, n, flags, c->stream);
     if (rc != CG_OK) return rc;
-    c->launched = true;
     return cg_sync_stats(c, st);
 }
 
@@ -595,9 +713,21 @@ int cg_traversal_time_ms(cg_ctx* c, float* ms) {
     return CG_OK;
 }
 
+int cg_read_trace(cg_ctx* c, uint32_t bucket_ns, uint32_t* out, uint32_t n_buckets) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (bucket_ns) c->trace_ns = bucket_ns;
+    if (!out || !n_buckets) return CG_OK;
+    const uint32_t m = std::min<uint32_t>(n_buckets, kTraceBuckets);
+    CG_CUDA(cudaStreamSynchronize(c->stream), "trace");
+    CG_CUDA(cudaMemcpy(out, c->d_trace, sizeof(uint32_t) * 4 * m, cudaMemcpyDeviceToHost), "read trace");
+    return CG_OK;
+}
+
 int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags) {
     if (!c || (n && !d_queries)) return CG_ERR_INVALID_ARGUMENT;
-    if (n > c->cfg.max_queries) return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    if (n > c->cfg.max_queries)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
     cudaSetDevice(c->device);
     CG_CUDA(cudaStreamSynchronize(c->stream), "sync before capture");
     drop_graph(c);
@@ -614,21 +744,19 @@ int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t 
     if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
     c->graph = g;
     CG_CUDA(cudaGraphInstantiate(&c->graph_exec, g, 0), "instantiate graph");
+    c->graph_gen = arena_gen(c);
     c->last_flags = flags;
     return CG_OK;
 }
 
 int cg_graph_launch(cg_ctx* c, void* stream) {
-    if (!c || !c->graph_exec) return CG_ERR_INVALID_ARGUMENT;
+    if (!c || !c->graph_exec) return fail(c, CG_ERR_INVALID_ARGUMENT, "no captured graph");
+    if (c->graph_gen != arena_gen(c))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "tree storage moved since the capture: capture the graph again");
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     CG_CUDA(cudaGraphLaunch(c->graph_exec, s), "graph launch");
-    c->launched = true;
-    if (s != c->stream) {
-        CG_CUDA(cudaEventRecord(c->ev_join, s), "event record");
-        CG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "stream wait");
-    }
-    return CG_OK;
+    return join_stream(c, s);
 }
 
 }  // extern "C"

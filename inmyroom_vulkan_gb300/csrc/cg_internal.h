@@ -1,17 +1,22 @@
 // Shared between the host side of the C ABI and the collision kernels.
 //
-// Device layout of one tree (HBM):
-//   recs : float4[4 * n_recs], one 64-byte record per box. Record 1 is the
-//          root; the two child boxes of inner node k are records 2k+2 (left)
-//          and 2k+3 (right), so one node's children share a 128-byte line.
-//          q0 = (c.x, c.y, c.z, u.x)  q1 = (u.y, u.z, v.x, v.y)
-//          q2 = (v.z, w.x, w.y, w.z)  q3 = (ref, meta, surface, 0)
-//          ref  = child inner-node index, or the leaf's first triangle
-//          meta = triangle count | 0x80000000 for a leaf
-//          surface = Paralgram::GetSurface of the box, precomputed
-//   tris : float4[3 * n_tris], 48 bytes per triangle in leaf (DFS) order,
-//          (p_k.xyz, vertex index k as bits) for k = 0, 1, 2.
-//   nrm  : float[9 * n_tris] vertex normals (uncollide rays), optional.
+// Device layout (HBM). All trees of a context live in two arenas, addressed by
+// absolute indices so that a traversal step needs no per-tree pointer:
+//   records  : float4[4 * n], one 64-byte record per box. A tree occupies a
+//              block of 2*node_count + 2 records starting at rec_base: record
+//              rec_base + 1 is the root, and the two child boxes of inner node
+//              k are records rec_base + 2k + 2 (left) and + 2k + 3 (right), so
+//              one node's children share a 128-byte line.
+//              q0 = (c.x, c.y, c.z, u.x)  q1 = (u.y, u.z, v.x, v.y)
+//              q2 = (v.z, w.x, w.y, w.z)  q3 = (ref, meta, surface, 0)
+//              ref  = absolute record index of the left child (inner box), or
+//                     absolute index of the leaf's first triangle
+//              meta = triangle count | 0x80000000 for a leaf
+//              surface = Paralgram::GetSurface of the box, precomputed
+//   triangles: float4[3 * n], 48 bytes per triangle in leaf (DFS) order,
+//              (p_k.xyz, vertex index k as bits) for k = 0, 1, 2; a tree's
+//              triangles start at tri_base.
+//   normals  : float[9 * n_tris] per tree (uncollide rays), optional.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,23 +28,25 @@
 namespace cg {
 
 constexpr uint32_t kLeafFlag = 0x80000000u;
-constexpr int kLeafCap = 64;  // buffered leaf pairs per warp
+constexpr int kLeafCap = 64;        // buffered leaf pairs per warp
+constexpr int kTraceBuckets = 512;  // utilisation trace: busy lanes per time bucket
 
 struct DevTree {
-    const float4* recs;
-    const float4* tris;
-    const float* nrm;
+    uint32_t rec_base;  // first record of the tree (its root is rec_base + 1)
+    uint32_t tri_base;  // first triangle of the tree
     uint32_t n_recs;
     uint32_t n_tris;
+    uint32_t live;
+    uint32_t pad;
+    const float* nrm;
 };
 
-// A query as the kernels read it: relative matrix columns and tree pointers.
+// A query as the kernels read it: relative matrix columns, the two roots and
+// triangle bases (to report tree-local triangle indices). root_a == 0 marks an
+// invalid query.
 struct alignas(16) PackedQuery {
     float4 m[4];
-    const float4* recs_a;
-    const float4* recs_b;
-    const float4* tris_a;
-    const float4* tris_b;
+    uint32_t root_a, root_b, tri_base_a, tri_base_b;
 };
 
 struct Counters {
@@ -56,6 +63,7 @@ struct Counters {
     unsigned long long fragile;
     unsigned long long donations;  // node pairs handed to other warps
     unsigned long long warp_steps; // traversal steps (node_pairs / warp_steps = lanes busy per step)
+    unsigned long long t_start;    // globaltimer at the first warp's start (trace only)
 };
 
 enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
@@ -67,6 +75,8 @@ enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
 struct TraverseParams {
     const PackedQuery* q;
     uint32_t n_queries;
+    const float4* recs;   // record arena
+    const float4* tris;   // triangle arena
     uint4* pool;          // node-pair entries (query, record a, record b, 0)
     uint2* slots;         // chunk of each donated slot
     unsigned int* ready;  // per donated slot: 1 once published
@@ -78,6 +88,8 @@ struct TraverseParams {
     unsigned long long pairs_cap;
     cg_leaf_pair* leafs;
     unsigned long long leafs_cap;
+    unsigned int* trace;  // kTraceBuckets x 2 (busy lanes, steps) or null
+    uint32_t trace_ns;    // trace bucket width
     uint32_t flags;
     uint32_t stack_cap;   // power of two
     uint32_t donate_min;
@@ -90,9 +102,10 @@ __host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
                         Counters* ctr, cudaStream_t s);
-cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries, cudaStream_t s);
+cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries,
+                        unsigned int* trace, cudaStream_t s);
 cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s);
 cudaError_t traverse_occupancy(uint32_t warps_per_block, uint32_t stack_cap, int* blocks_per_sm);
-cudaError_t launch_surfaces(float4* recs, uint32_t n_recs, cudaStream_t s);
+cudaError_t launch_surfaces(float4* recs, uint32_t first, uint32_t n_recs, cudaStream_t s);
 
 }  // namespace cg

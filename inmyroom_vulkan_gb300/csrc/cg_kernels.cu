@@ -110,10 +110,6 @@ __device__ __forceinline__ Mat4 load_mat(const PackedQuery* Q) {
     return M;
 }
 
-__device__ __forceinline__ const float4* load_ptr(const float4* const* p) {
-    return reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(p)));
-}
-
 __device__ __forceinline__ void load_tri(const float4* tris, uint32_t i, float3& p0, float3& p1, float3& p2) {
     const float4* p = tris + 3ull * i;
     const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
@@ -181,11 +177,21 @@ __device__ uint32_t take_chunk(const TraverseParams& P, uint32_t slot, const Deq
             D.a[pos] = e.y;
             D.b[pos] = e.z;
         }
-    } else if (lane == 0) {
-        const uint32_t pos = top & D.mask;
-        D.q[pos] = slot;
-        D.a[pos] = 1;
-        D.b[pos] = 1;
+    } else {
+        // root pair of query `slot`; an invalid query (root 0) has no work
+        uint32_t ra = 0, rb = 0;
+        if (lane == 0) {
+            const PackedQuery* Q = P.q + slot;
+            ra = __ldg(&Q->root_a);
+            rb = __ldg(&Q->root_b);
+            if (ra != 0u) {
+                const uint32_t pos = top & D.mask;
+                D.q[pos] = slot;
+                D.a[pos] = ra;
+                D.b[pos] = rb;
+            }
+        }
+        cnt = __shfl_sync(kFull, ra != 0u ? 1u : 0u, 0);
     }
     __syncwarp();
     return cnt;
@@ -244,7 +250,7 @@ __device__ int try_claim(const TraverseParams& P, unsigned long long ht, uint32_
 // (CreateUncollideRays.cpp:139-148): B's triangle is moved into A's space with
 // TrianglePosition::MultiplyBy4x4Matrix arithmetic, then tested.
 __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t nl, int lane,
-                            unsigned long long& tests, unsigned long long& fragile) {
+                            unsigned long long& tests, unsigned long long& fragile, unsigned long long t_base) {
     uint32_t c0 = 0, c1 = 0;
     if (uint32_t(lane) < nl) {
         const uint32_t cn = L.cn[lane];
@@ -276,10 +282,11 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
         lbase = __shfl_sync(kFull, lbase, 0);
         for (uint32_t e = lane; e < nl; e += 32) {
             if (lbase + e < P.leafs_cap) {
+                const PackedQuery* Q = P.q + L.q[e];
                 cg_leaf_pair lp;
                 lp.query = L.q[e];
-                lp.offset_a = L.oa[e];
-                lp.offset_b = L.ob[e];
+                lp.offset_a = L.oa[e] - __ldg(&Q->tri_base_a);
+                lp.offset_b = L.ob[e] - __ldg(&Q->tri_base_b);
                 lp.count_a = uint16_t(L.cn[e] & 0xffffu);
                 lp.count_b = uint16_t(L.cn[e] >> 16);
                 P.leafs[lbase + e] = lp;
@@ -313,8 +320,8 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
             const PackedQuery* Q = P.q + q;
             const Mat4 M = load_mat(Q);
             float3 a0, a1, a2, b0, b1, b2;
-            load_tri(load_ptr(&Q->tris_a), ia, a0, a1, a2);
-            load_tri(load_ptr(&Q->tris_b), ib, b0, b1, b2);
+            load_tri(P.tris, ia, a0, a1, a2);
+            load_tri(P.tris, ib, b0, b1, b2);
             b0 = xform(M, b0, 1.0f);
             b1 = xform(M, b1, 1.0f);
             b2 = xform(M, b2, 1.0f);
@@ -329,10 +336,11 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
             if (res == TT_HIT && !(P.flags & CG_NO_TRI_PAIRS)) {
                 const unsigned long long o = obase + __popc(hitmask & lanemask_lt());
                 if (o < P.pairs_cap) {
+                    const PackedQuery* Q = P.q + q;
                     cg_tri_pair r;
                     r.query = q;
-                    r.tri_a = ia;
-                    r.tri_b = ib;
+                    r.tri_a = ia - __ldg(&Q->tri_base_a);
+                    r.tri_b = ib - __ldg(&Q->tri_base_b);
                     r.source[0] = src.x;
                     r.source[1] = src.y;
                     r.source[2] = src.z;
@@ -343,7 +351,16 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
                 }
             }
         }
-        if (lane == 0) fragile += __popc(fragmask);
+        if (lane == 0) {
+            fragile += __popc(fragmask);
+            if (P.trace) {
+                const unsigned long long b = (gtimer() - t_base) / P.trace_ns;
+                if (b < kTraceBuckets) {
+                    atomicAdd(P.trace + 4 * b + 2, min(32u, total - base));
+                    atomicAdd(P.trace + 4 * b + 3, 1u);
+                }
+            }
+        }
     }
     if (lane == 0) tests += total;
     __syncwarp();
@@ -351,7 +368,7 @@ __device__ void flush_leafs(const TraverseParams& P, const LeafBuf& L, uint32_t 
 
 }  // namespace
 
-__global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
+__global__ void __launch_bounds__(256, 3) traverse_kernel(const TraverseParams P) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -371,6 +388,12 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
 
     uint32_t top = 0, bot = 0, nl = 0, held_tasks = 0;
     unsigned long long st_nodes = 0, st_tests = 0, st_frag = 0, st_don = 0, st_steps = 0;
+    unsigned long long t_base = 0;
+    if (P.trace && lane == 0) {
+        const unsigned long long now = gtimer();
+        const unsigned long long old = atomicCAS(&P.ctr->t_start, 0ull, now);
+        t_base = old ? old : now;
+    }
 
     for (;;) {
         if (top == bot) {
@@ -409,13 +432,10 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
         int act = 0;  // 1: split A, 2: split B, 3: leaf pair
         uint32_t child = 0, offA = 0, offB = 0, cnt = 0;
         if (active) {
-            const PackedQuery* Q = P.q + q;
-            const float4* recs_a = load_ptr(&Q->recs_a);
-            const float4* recs_b = load_ptr(&Q->recs_b);
-            if (recs_a != nullptr && recs_b != nullptr) {
-                const Mat4 M = load_mat(Q);
-                const Rec A = load_rec(recs_a, ra);
-                const Rec B = load_rec(recs_b, rb);
+            const Mat4 M = load_mat(P.q + q);
+            const Rec A = load_rec(P.recs, ra);
+            const Rec B = load_rec(P.recs, rb);
+            {
                 const Box bb = xform_box(M, B.box);
                 if (sat_rolled(A.box, bb)) {
                     const bool la = (A.meta & kLeafFlag) != 0;
@@ -441,7 +461,7 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
             const uint32_t r = __popc(pushmask & lanemask_lt());
             const uint32_t p0 = (top + 2u * r) & D.mask;
             const uint32_t p1 = (top + 2u * r + 1u) & D.mask;
-            const uint32_t c_left = 2u * child + 2u, c_right = 2u * child + 3u;
+            const uint32_t c_left = child, c_right = child + 1u;
             D.q[p0] = q;
             D.q[p1] = q;
             if (act == 1) {
@@ -470,11 +490,18 @@ __global__ void __launch_bounds__(512) traverse_kernel(const TraverseParams P) {
         if (lane == 0) {
             st_nodes += n;
             ++st_steps;
+            if (P.trace) {
+                const unsigned long long b = (gtimer() - t_base) / P.trace_ns;
+                if (b < kTraceBuckets) {
+                    atomicAdd(P.trace + 4 * b, n);
+                    atomicAdd(P.trace + 4 * b + 1, 1u);
+                }
+            }
         }
         __syncwarp();
 
         if (nl >= P.leaf_flush || (top == bot && nl > 0)) {
-            flush_leafs(P, L, nl, lane, st_tests, st_frag);
+            flush_leafs(P, L, nl, lane, st_tests, st_frag, t_base);
             nl = 0;
         }
 
@@ -553,15 +580,14 @@ __global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees
     p.m[1] = make_float4(Q.relative[4], Q.relative[5], Q.relative[6], Q.relative[7]);
     p.m[2] = make_float4(Q.relative[8], Q.relative[9], Q.relative[10], Q.relative[11]);
     p.m[3] = make_float4(Q.relative[12], Q.relative[13], Q.relative[14], Q.relative[15]);
-    const bool ok = Q.tree_a < n_trees && Q.tree_b < n_trees && trees[Q.tree_a].recs != nullptr &&
-                    trees[Q.tree_b].recs != nullptr;
+    const bool ok = Q.tree_a < n_trees && Q.tree_b < n_trees && trees[Q.tree_a].live && trees[Q.tree_b].live;
     if (ok) {
-        p.recs_a = trees[Q.tree_a].recs;
-        p.recs_b = trees[Q.tree_b].recs;
-        p.tris_a = trees[Q.tree_a].tris;
-        p.tris_b = trees[Q.tree_b].tris;
+        p.root_a = trees[Q.tree_a].rec_base + 1u;
+        p.root_b = trees[Q.tree_b].rec_base + 1u;
+        p.tri_base_a = trees[Q.tree_a].tri_base;
+        p.tri_base_b = trees[Q.tree_b].tri_base;
     } else {
-        p.recs_a = p.recs_b = p.tris_a = p.tris_b = nullptr;
+        p.root_a = p.root_b = p.tri_base_a = p.tri_base_b = 0u;
         atomicOr(&ctr->error, ERR_BAD_QUERY);
     }
     out[i] = p;
@@ -570,7 +596,8 @@ __global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees
 // Resets the counters for a launch over n_queries and clears the ready flags
 // of the slots the previous launch published (their count is still in the
 // counters).
-__global__ void init_kernel(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries) {
+__global__ void init_kernel(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries,
+                            unsigned int* trace) {
     __shared__ uint32_t used;
     if (threadIdx.x == 0) {
         const unsigned long long ht = *reinterpret_cast<unsigned long long*>(&ctr->head);
@@ -580,6 +607,8 @@ __global__ void init_kernel(Counters* ctr, unsigned int* ready, uint32_t slot_al
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < used; i += blockDim.x) ready[i] = 0u;
+    if (trace)
+        for (uint32_t i = threadIdx.x; i < 4u * kTraceBuckets; i += blockDim.x) trace[i] = 0u;
     __syncthreads();
     if (threadIdx.x == 0) {
         Counters c = {};
@@ -590,10 +619,11 @@ __global__ void init_kernel(Counters* ctr, unsigned int* ready, uint32_t slot_al
     }
 }
 
-// Paralgram::GetSurface of every record, written into q3.z.
-__global__ void surfaces_kernel(float4* recs, uint32_t n_recs) {
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n_recs) return;
+// Paralgram::GetSurface of records [first, first + n_recs), written into q3.z.
+__global__ void surfaces_kernel(float4* recs, uint32_t first, uint32_t n_recs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_recs) return;
+    const uint32_t r = first + i;
     float4* p = recs + 4ull * r;
     const float4 a = p[0], b = p[1], c = p[2];
     Box box;
@@ -611,14 +641,15 @@ cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, ui
     return cudaGetLastError();
 }
 
-cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries, cudaStream_t s) {
-    init_kernel<<<1, 1024, 0, s>>>(ctr, ready, slot_alloc, n_queries);
+cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries,
+                        unsigned int* trace, cudaStream_t s) {
+    init_kernel<<<1, 1024, 0, s>>>(ctr, ready, slot_alloc, n_queries, trace);
     return cudaGetLastError();
 }
 
-cudaError_t launch_surfaces(float4* recs, uint32_t n_recs, cudaStream_t s) {
+cudaError_t launch_surfaces(float4* recs, uint32_t first, uint32_t n_recs, cudaStream_t s) {
     if (n_recs == 0) return cudaSuccess;
-    surfaces_kernel<<<(n_recs + 255) / 256, 256, 0, s>>>(recs, n_recs);
+    surfaces_kernel<<<(n_recs + 255) / 256, 256, 0, s>>>(recs, first, n_recs);
     return cudaGetLastError();
 }
 

@@ -196,7 +196,7 @@ def test_malformed_tree_is_rejected(gpu_ctx):
 
 
 @pytest.mark.parametrize("shape", [dict(warps_per_block=4, stack_entries=256, donate_min=64, leaf_flush=1),
-                                   dict(warps_per_block=16, stack_entries=1024, donate_min=900, leaf_flush=33),
+                                   dict(warps_per_block=6, stack_entries=1024, donate_min=900, leaf_flush=33),
                                    dict(warps_per_block=8, stack_entries=512, blocks_per_sm=1, leaf_flush=16)])
 def test_launch_shapes_give_identical_sets(port, scene_setup, shape):
     sc, tp = scene_setup
