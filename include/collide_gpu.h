@@ -53,13 +53,13 @@ typedef struct cg_config {
     int32_t device;            /* CUDA device ordinal */
     uint32_t max_queries;      /* queries per launch */
     uint64_t max_tri_pairs;    /* colliding triangle pairs kept per launch */
-    uint64_t max_leaf_pairs;   /* candidate leaf pairs kept per launch (only with CG_KEEP_LEAF_PAIRS) */
-    uint32_t queue_capacity;   /* node-pair tasks the global work queue can hold */
+    uint64_t max_leaf_pairs;   /* candidate leaf pairs per launch (the list between traversal and narrow phase) */
+    uint32_t queue_capacity;   /* node pairs the global work queue can hold (in chunks of 32) */
     uint32_t warps_per_block;  /* persistent traversal kernel shape; 0 = tuned default */
     uint32_t blocks_per_sm;    /* 0 = as many as fit */
     uint32_t stack_entries;    /* per-warp shared-memory node-pair stack, power of two (256..4096) */
     uint32_t donate_min;       /* a warp donates work to idle warps only above this stack size */
-    uint32_t leaf_flush;       /* buffered leaf pairs that trigger a warp's triangle-pair pass (1..64) */
+    uint32_t leaf_flush;       /* leaf pairs a traversal warp buffers before appending them to the list (1..33) */
     uint32_t wait_limit_ms;    /* limit of every device-side wait */
 } cg_config;
 
@@ -172,9 +172,11 @@ int cg_read_leaf_pairs(cg_ctx* ctx, cg_leaf_pair* out, uint64_t cap, uint64_t* n
 /* Device pointers to the last launch's results (valid until the next launch). */
 int cg_device_results(cg_ctx* ctx, const cg_tri_pair** pairs, const unsigned long long** pair_count);
 
-/* Device time of the last traversal kernel (the dominant kernel of a collide
- * step), from CUDA events recorded around its launch; waits for it. */
+/* Device times of the last step's two main kernels, the OBB-tree traversal
+ * (emits candidate leaf pairs) and the narrow phase (triangle-pair tests),
+ * from CUDA events recorded around their launches; each waits for its kernel. */
 int cg_traversal_time_ms(cg_ctx* ctx, float* ms);
+int cg_narrow_time_ms(cg_ctx* ctx, float* ms);
 
 /* Utilisation timeline of the last launch made with CG_TRACE: per time bucket
  * of bucket_ns nanoseconds since the traversal started, four counters (busy

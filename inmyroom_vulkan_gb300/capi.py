@@ -25,7 +25,7 @@ CG_TRACE = 4
 EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",
            "cg_last_error", "cg_tree_upload", "cg_tree_free", "cg_relative_matrix", "cg_collide", "cg_collide_async",
            "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results",
-           "cg_traversal_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch"]
+           "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch"]
 
 
 class CgError(RuntimeError):
@@ -99,6 +99,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
     lib.cg_traversal_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
     lib.cg_read_trace.argtypes = [vp, u32, vp, u32]
+    lib.cg_narrow_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
     lib.cg_graph_capture.argtypes = [vp, vp, u32, u32]
     lib.cg_graph_launch.argtypes = [vp, vp]
     _lib = lib
@@ -261,6 +262,11 @@ class Context:
     def traversal_ms(self) -> float:
         ms = C.c_float()
         self._check(self.lib.cg_traversal_time_ms(self.h, C.byref(ms)), "cg_traversal_time_ms")
+        return ms.value
+
+    def narrow_ms(self) -> float:
+        ms = C.c_float()
+        self._check(self.lib.cg_narrow_time_ms(self.h, C.byref(ms)), "cg_narrow_time_ms")
         return ms.value
 
     def set_trace_bucket(self, bucket_ns: int):

@@ -99,7 +99,8 @@ struct cg_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
-    uint32_t blocks = 0;  // persistent grid
+    uint32_t blocks = 0;         // persistent traversal grid
+    uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
 
     // trees
     struct Slot {
@@ -117,11 +118,10 @@ struct cg_ctx {
     PackedQuery* d_packed = nullptr;
     Counters* d_ctr = nullptr;
     uint4* d_pool = nullptr;        // donated node-pair entries
-    uint2* d_slots = nullptr;       // chunk of each donated slot
     unsigned int* d_ready = nullptr;
-    uint32_t pool_cap = 0;          // entries donors may reserve
-    uint32_t slot_cap = 0;          // slots donors may reserve
-    uint32_t pool_alloc = 0, slot_alloc = 0;  // allocated, with slack for concurrent reservations
+    uint32_t slot_cap = 0;          // chunk slots donors may reserve
+    uint32_t slot_alloc = 0;        // allocated, with slack for concurrent reservations and waiters
+    uint4* d_leaf_list = nullptr;   // candidate leaf pairs between the two kernels
     cg_tri_pair* d_pairs = nullptr;
     cg_leaf_pair* d_leafs = nullptr;
     unsigned int* d_trace = nullptr;
@@ -136,7 +136,7 @@ struct cg_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_gen = 0;         // arena generations the graph was captured with
     bool capturing = false;
-    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // around the traversal kernel
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_t2 = nullptr;  // traversal start, end; narrow end
     cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
 
     std::string err;
@@ -176,7 +176,7 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_packed);
     cudaFree(c->d_ctr);
     cudaFree(c->d_pool);
-    cudaFree(c->d_slots);
+    cudaFree(c->d_leaf_list);
     cudaFree(c->d_ready);
     cudaFree(c->d_pairs);
     cudaFree(c->d_leafs);
@@ -187,7 +187,7 @@ void free_buffers(cg_ctx* c) {
     c->d_packed = nullptr;
     c->d_ctr = nullptr;
     c->d_pool = nullptr;
-    c->d_slots = nullptr;
+    c->d_leaf_list = nullptr;
     c->d_ready = nullptr;
     c->d_pairs = nullptr;
     c->d_leafs = nullptr;
@@ -226,17 +226,18 @@ int alloc_buffers(cg_ctx* c) {
     const int per_sm = g.blocks_per_sm ? std::min<int>(occ, int(g.blocks_per_sm)) : occ;
     c->blocks = uint32_t(per_sm * c->sm_count);
     const uint32_t warps = c->blocks * g.warps_per_block;
-    c->pool_cap = g.queue_capacity;
-    c->slot_cap = g.queue_capacity;
-    c->pool_alloc = g.queue_capacity + 32u * warps + 64u;
-    c->slot_alloc = g.queue_capacity + 2u * warps + 64u;
+    c->slot_cap = std::max<uint32_t>(g.queue_capacity / uint32_t(kChunk), 64u);
+    c->slot_alloc = c->slot_cap + 2u * warps + 64u;
+    int nocc = 0;
+    CG_CUDA(narrow_occupancy(8, &nocc), "occupancy");
+    c->narrow_blocks = uint32_t(std::max(nocc, 1) * c->sm_count);
 
     CG_CUDA(cudaMalloc(&c->d_queries, sizeof(cg_query) * g.max_queries), "alloc queries");
     CG_CUDA(cudaMalloc(&c->d_packed, sizeof(PackedQuery) * g.max_queries), "alloc packed queries");
     CG_CUDA(cudaMalloc(&c->d_ctr, sizeof(Counters)), "alloc counters");
     CG_CUDA(cudaMemset(c->d_ctr, 0, sizeof(Counters)), "zero counters");
-    CG_CUDA(cudaMalloc(&c->d_pool, sizeof(uint4) * c->pool_alloc), "alloc task pool");
-    CG_CUDA(cudaMalloc(&c->d_slots, sizeof(uint2) * c->slot_alloc), "alloc task slots");
+    CG_CUDA(cudaMalloc(&c->d_pool, sizeof(uint4) * size_t(kChunk) * c->slot_alloc), "alloc task pool");
+    CG_CUDA(cudaMalloc(&c->d_leaf_list, sizeof(uint4) * std::max<uint64_t>(g.max_leaf_pairs, 1)), "alloc leaf-pair list");
     CG_CUDA(cudaMalloc(&c->d_ready, sizeof(unsigned int) * c->slot_alloc), "alloc task flags");
     CG_CUDA(cudaMemset(c->d_ready, 0, sizeof(unsigned int) * c->slot_alloc), "zero task flags");
     if (g.max_tri_pairs) CG_CUDA(cudaMalloc(&c->d_pairs, sizeof(cg_tri_pair) * g.max_tri_pairs), "alloc pair output");
@@ -277,38 +278,48 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
     rec[3] = make_float4(r, m, 0.f, 0.f);
 }
 
-// Enqueues counter reset, packing and the traversal on `s`.
+// Enqueues counter reset, packing, the traversal and the narrow phase on `s`.
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s) {
     unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
+    const uint32_t trace_ns = c->trace_ns ? c->trace_ns : 1000u;
     CG_CUDA(launch_init(c->d_ctr, c->d_ready, c->slot_alloc, n, trace, s), "init kernel");
     CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->d_packed, c->d_ctr, s), "pack kernel");
     TraverseParams p{};
     p.q = c->d_packed;
     p.n_queries = n;
     p.recs = c->recs.ptr;
-    p.tris = c->tris.ptr;
     p.pool = c->d_pool;
-    p.slots = c->d_slots;
     p.ready = c->d_ready;
-    p.pool_cap = c->pool_cap;
     p.slot_cap = c->slot_cap;
     p.slot_alloc = c->slot_alloc;
     p.ctr = c->d_ctr;
-    p.pairs = c->d_pairs;
-    p.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
-    p.leafs = c->d_leafs;
-    p.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
+    p.leaf_list = c->d_leaf_list;
+    p.leaf_cap = uint32_t(std::min<uint64_t>(c->cfg.max_leaf_pairs, 0xffffffffull));
     p.trace = trace;
-    p.trace_ns = c->trace_ns ? c->trace_ns : 1000u;
-    p.flags = flags;
+    p.trace_ns = trace_ns;
     p.stack_cap = c->cfg.stack_entries;
     p.donate_min = std::min(std::max(c->cfg.donate_min, 2u), c->cfg.stack_entries - 63u);
     p.leaf_flush = c->cfg.leaf_flush;
     p.wait_ns = (unsigned long long)c->cfg.wait_limit_ms * 1000000ull;
+    NarrowParams np{};
+    np.q = c->d_packed;
+    np.tris = c->tris.ptr;
+    np.leaf_list = c->d_leaf_list;
+    np.leaf_cap = p.leaf_cap;
+    np.ctr = c->d_ctr;
+    np.pairs = c->d_pairs;
+    np.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
+    np.leafs = c->d_leafs;
+    np.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
+    np.flags = flags;
+    np.trace = trace;
+    np.trace_ns = trace_ns;
     const unsigned rec_flags = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t0, s, rec_flags), "timing event");
     if (n) CG_CUDA(launch_traverse(p, c->blocks, c->cfg.warps_per_block, s), "traversal kernel");
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t1, s, rec_flags), "timing event");
+    if (n) CG_CUDA(launch_narrow(np, c->narrow_blocks, 8, s), "narrow-phase kernel");
+    CG_CUDA(cudaEventRecordWithFlags(c->ev_t2, s, rec_flags), "timing event");
     return CG_OK;
 }
 
@@ -328,6 +339,9 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
         status = fail(c, CG_ERR_QUEUE_OVERFLOW, "node-pair queue full (queue_capacity %u)", c->cfg.queue_capacity);
     else if (k.error & ERR_BAD_QUERY)
         status = fail(c, CG_ERR_INVALID_ARGUMENT, "a query names an unknown tree");
+    else if (k.n_leafs > c->cfg.max_leaf_pairs)
+        status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu candidate leaf pairs, max_leaf_pairs %llu: triangle tests "
+                      "incomplete", (unsigned long long)k.n_leafs, (unsigned long long)c->cfg.max_leaf_pairs);
     else if (!(c->last_flags & CG_NO_TRI_PAIRS) && k.n_pairs > (c->d_pairs ? c->cfg.max_tri_pairs : 0))
         status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu colliding pairs, capacity %llu", (unsigned long long)k.n_pairs,
                       (unsigned long long)c->cfg.max_tri_pairs);
@@ -464,6 +478,7 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess ||
+        cudaEventCreate(&c->ev_t2) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&c->d_trace, sizeof(unsigned int) * 4 * kTraceBuckets) != cudaSuccess) {
         delete c;
@@ -492,6 +507,7 @@ int cg_destroy(cg_ctx* c) {
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
+    cudaEventDestroy(c->ev_t2);
     cudaEventDestroy(c->ev_join);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -710,6 +726,14 @@ int cg_traversal_time_ms(cg_ctx* c, float* ms) {
     cudaSetDevice(c->device);
     CG_CUDA(cudaEventSynchronize(c->ev_t1), "timing event");
     CG_CUDA(cudaEventElapsedTime(ms, c->ev_t0, c->ev_t1), "timing");
+    return CG_OK;
+}
+
+int cg_narrow_time_ms(cg_ctx* c, float* ms) {
+    if (!c || !ms) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaEventSynchronize(c->ev_t2), "timing event");
+    CG_CUDA(cudaEventElapsedTime(ms, c->ev_t1, c->ev_t2), "timing");
     return CG_OK;
 }
 

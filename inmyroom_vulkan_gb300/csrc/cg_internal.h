@@ -17,6 +17,10 @@
 //              (p_k.xyz, vertex index k as bits) for k = 0, 1, 2; a tree's
 //              triangles start at tri_base.
 //   normals  : float[9 * n_tris] per tree (uncollide rays), optional.
+//
+// A collide step runs two persistent kernels: the traversal writes candidate
+// leaf pairs to a list, and the narrow phase runs the triangle pairs of that
+// list, 32 leaf pairs per warp.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,8 +32,9 @@
 namespace cg {
 
 constexpr uint32_t kLeafFlag = 0x80000000u;
-constexpr int kLeafCap = 64;        // buffered leaf pairs per warp
-constexpr int kTraceBuckets = 512;  // utilisation trace: busy lanes per time bucket
+constexpr int kLeafCap = 64;        // buffered leaf pairs per traversal warp
+constexpr int kChunk = 32;          // node pairs per donated task slot
+constexpr int kTraceBuckets = 512;  // utilisation trace: counters per time bucket
 
 struct DevTree {
     uint32_t rec_base;  // first record of the tree (its root is rec_base + 1)
@@ -50,12 +55,12 @@ struct alignas(16) PackedQuery {
 };
 
 struct Counters {
-    unsigned int head;      // next task slot to claim (slots < n_queries are the root tasks)
-    unsigned int tail;      // one past the last reserved task slot
-    unsigned int work;      // tasks published and not yet finished
-    unsigned int error;     // ERR_* bits
-    unsigned int pool_tail; // node-pair entries reserved in the task pool
-    unsigned int n_queries; // queries of the launch (the next launch clears the slots it published)
+    unsigned int head;        // next task slot to claim (slots < n_queries are the root tasks)
+    unsigned int tail;        // one past the last reserved task slot
+    unsigned int done;        // finished tasks; all work is done when done == tail
+    unsigned int error;       // ERR_* bits
+    unsigned int n_queries;   // queries of the launch (the next launch clears the slots it published)
+    unsigned int narrow_next; // next block of 32 leaf pairs for the narrow phase
     unsigned long long n_pairs;
     unsigned long long n_leafs;
     unsigned long long node_pairs;
@@ -68,36 +73,46 @@ struct Counters {
 
 enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
 
-// Work queue. A task is a chunk of up to 32 node pairs: slot s >= n_queries
-// describes chunk slots[s - n_queries] = (first pool entry, count) and is
-// readable once ready[s - n_queries] is 1. Slot s < n_queries is the root pair
-// of query s.
+// Work queue. A task is a chunk of up to kChunk node pairs: donated slot
+// s >= n_queries holds its chunk at pool[kChunk * (s - n_queries)], and
+// ready[s - n_queries] becomes count + 1 when it is published. Slot
+// s < n_queries is the root pair of query s.
 struct TraverseParams {
     const PackedQuery* q;
     uint32_t n_queries;
     const float4* recs;   // record arena
-    const float4* tris;   // triangle arena
     uint4* pool;          // node-pair entries (query, record a, record b, 0)
-    uint2* slots;         // chunk of each donated slot
-    unsigned int* ready;  // per donated slot: 1 once published
-    uint32_t pool_cap;    // entries donors may reserve
+    unsigned int* ready;  // per donated slot
     uint32_t slot_cap;    // donated slots donors may reserve
     uint32_t slot_alloc;  // allocated slots (slot_cap plus room for warps waiting past it)
     Counters* ctr;
-    cg_tri_pair* pairs;
-    unsigned long long pairs_cap;
-    cg_leaf_pair* leafs;
-    unsigned long long leafs_cap;
-    unsigned int* trace;  // kTraceBuckets x 2 (busy lanes, steps) or null
+    uint4* leaf_list;     // (query, first triangle a, first triangle b, count_a | count_b << 16)
+    uint32_t leaf_cap;
+    unsigned int* trace;  // kTraceBuckets x 4 or null
     uint32_t trace_ns;    // trace bucket width
-    uint32_t flags;
     uint32_t stack_cap;   // power of two
     uint32_t donate_min;
-    uint32_t leaf_flush;
+    uint32_t leaf_flush;  // leaf pairs buffered before they are appended to the list
     unsigned long long wait_ns;
 };
 
-__host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return 3u * stack_cap + 5u * kLeafCap + 1u; }
+struct NarrowParams {
+    const PackedQuery* q;
+    const float4* tris;   // triangle arena
+    const uint4* leaf_list;
+    uint32_t leaf_cap;
+    Counters* ctr;
+    cg_tri_pair* pairs;
+    unsigned long long pairs_cap;
+    cg_leaf_pair* leafs;  // the public copy of the leaf pairs (CG_KEEP_LEAF_PAIRS)
+    unsigned long long leafs_cap;
+    uint32_t flags;
+    unsigned int* trace;
+    uint32_t trace_ns;
+};
+
+__host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return 3u * stack_cap + 4u * kLeafCap; }
+constexpr uint32_t kNarrowWarpWords = 5u * 32u + 1u;
 
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
@@ -105,7 +120,9 @@ cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, ui
 cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries,
                         unsigned int* trace, cudaStream_t s);
 cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s);
+cudaError_t launch_narrow(const NarrowParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s);
 cudaError_t traverse_occupancy(uint32_t warps_per_block, uint32_t stack_cap, int* blocks_per_sm);
+cudaError_t narrow_occupancy(uint32_t warps_per_block, int* blocks_per_sm);
 cudaError_t launch_surfaces(float4* recs, uint32_t first, uint32_t n_recs, cudaStream_t s);
 
 }  // namespace cg
