@@ -227,7 +227,7 @@ int alloc_buffers(cg_ctx* c) {
     c->blocks = uint32_t(per_sm * c->sm_count);
     const uint32_t warps = c->blocks * g.warps_per_block;
     c->slot_cap = std::max<uint32_t>(g.queue_capacity / uint32_t(kChunk), 64u);
-    c->slot_alloc = c->slot_cap + 2u * warps + 64u;
+    c->slot_alloc = c->slot_cap + 9u * warps + 64u;
     int nocc = 0;
     CG_CUDA(narrow_occupancy(8, &nocc), "occupancy");
     c->narrow_blocks = uint32_t(std::max(nocc, 1) * c->sm_count);
@@ -421,10 +421,10 @@ void cg_config_default(cg_config* cfg) {
     cfg->max_tri_pairs = 1ull << 23;
     cfg->max_leaf_pairs = 1ull << 22;
     cfg->queue_capacity = 1u << 20;
-    cfg->warps_per_block = 8;
-    cfg->blocks_per_sm = 0;
+    cfg->warps_per_block = 4;
+    cfg->blocks_per_sm = 3;
     cfg->stack_entries = 512;
-    cfg->donate_min = 16;
+    cfg->donate_min = 32;
     cfg->leaf_flush = 32;
     cfg->wait_limit_ms = 2000;
 }
@@ -460,7 +460,7 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         cg_config_default(&cfg);
     auto* c = new cg_ctx;
     c->cfg = cfg;
-    c->recs.width = 4;
+    c->recs.width = 8;  // units of two records: every tree starts on a 128-byte line
     c->tris.width = 3;
     int rc = check_config(c, &cfg);
     if (rc != CG_OK) {
@@ -564,17 +564,18 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
     if (N == 0 && T > 0xffffu) return fail(c, CG_ERR_BAD_TREE, "leaf root with %u triangles", T);
     cudaSetDevice(c->device);
 
-    const uint64_t n_recs = 2ull * N + 2ull;
+    const uint64_t n_recs = 2ull * N + 2ull;  // even: whole 128-byte record pairs
     const uint64_t n_tris = std::max<uint64_t>(T, 1);
-    uint64_t rb = 0, tb = 0;
-    CG_CUDA(c->recs.alloc(n_recs, &rb, c->stream), "record arena");
+    uint64_t rpair = 0, tb = 0;
+    CG_CUDA(c->recs.alloc(n_recs / 2, &rpair, c->stream), "record arena");
+    const uint64_t rb = 2 * rpair;
     cudaError_t e = c->tris.alloc(n_tris, &tb, c->stream);
     if (e != cudaSuccess) {
-        c->recs.release(rb, n_recs);
+        c->recs.release(rpair, n_recs / 2);
         return cuda_fail(c, e, "triangle arena");
     }
     if (rb + n_recs > 0xffffffffull || tb + n_tris > 0x7fffffffull) {
-        c->recs.release(rb, n_recs);
+        c->recs.release(rpair, n_recs / 2);
         c->tris.release(tb, n_tris);
         return fail(c, CG_ERR_OUT_OF_MEMORY, "arena index space exhausted");
     }
@@ -642,7 +643,7 @@ int cg_tree_free(cg_ctx* c, uint32_t id) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     auto& s = c->trees[id];
-    c->recs.release(s.rec_base, s.n_recs);
+    c->recs.release(s.rec_base / 2, s.n_recs / 2);
     c->tris.release(s.tri_base, s.n_tris);
     cudaFree(s.nrm);
     s = cg_ctx::Slot{};

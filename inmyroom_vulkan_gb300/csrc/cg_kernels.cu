@@ -343,6 +343,10 @@ __global__ void __launch_bounds__(256, 3) traverse_kernel(const TraverseParams P
                 else
                     act = 3;
                 child = act == 1 ? A.ref : B.ref;
+                // the split node's two child records share one 128-byte line
+                // (records are allocated in aligned pairs): fetch it into L1
+                // for the next step
+                if (act < 3) asm volatile("prefetch.global.L1 [%0];" ::"l"(P.recs + 4ull * child));
                 offA = A.ref;
                 offB = B.ref;
                 cnt = (A.meta & 0xffffu) | ((B.meta & 0xffffu) << 16);
@@ -396,26 +400,29 @@ __global__ void __launch_bounds__(256, 3) traverse_kernel(const TraverseParams P
             __syncwarp();
         }
 
-        // ---- balance: give half of the bottom of the deque to waiting warps
-        // (a full chunk when the deque is nearly full), or top up from
+        // ---- balance: give chunks from the bottom of the deque to the warps
+        // that wait (one chunk per waiting warp, up to 8, keeping at least a
+        // chunk; a full chunk when the deque is nearly full), or top up from
         // reserved chunks when fewer than 32 node pairs are left.
         const uint32_t held = top - bot;
         const bool forced = held + 64u > S;
-        int mode = 0;  // 1: donate k, 2: top up from slot
-        uint32_t k = 0, slot = 0;
+        int mode = 0;  // 1: donate nch chunks of c, 2: top up from slot
+        uint32_t c = 0, nch = 0, slot = 0;
         unsigned rr = 0;
         if (lane == 0) {
-            const bool waiting = int(ht_tail(qs) - ht_head(qs)) < 0;
-            if (forced || (waiting && held >= P.donate_min)) {
-                k = forced ? uint32_t(kChunk) : min(uint32_t(kChunk), held >> 1);
-                if (ht_tail(qs) - P.n_queries < P.slot_cap) {
-                    slot = ht_tail(atomicAdd(ht, 1ull << 32));
+            const int waiting = int(ht_head(qs) - ht_tail(qs));
+            if (forced || (waiting > 0 && held >= P.donate_min)) {
+                c = held >= 2u * kChunk ? uint32_t(kChunk) : (held >> 1);
+                nch = min(uint32_t(waiting > 0 ? waiting : 1), min(held / c - 1u, 8u));
+                if (nch == 0) nch = 1;
+                if (ht_tail(qs) - P.n_queries + nch <= P.slot_cap) {
+                    slot = ht_tail(atomicAdd(ht, (unsigned long long)nch << 32));
                     mode = 1;
                 } else if (forced) {
                     atomicOr(&P.ctr->error, ERR_QUEUE);
                     mode = -1;
                 }
-            } else if (held < 32u && held > 0u && !waiting) {
+            } else if (held < 32u && held > 0u && waiting <= 0) {
                 if (try_claim(P, qs, slot)) {
                     rr = wait_ready(P, slot);
                     mode = rr ? 2 : -1;
@@ -425,20 +432,21 @@ __global__ void __launch_bounds__(256, 3) traverse_kernel(const TraverseParams P
         mode = __shfl_sync(kFull, mode, 0);
         if (mode == -1) break;
         if (mode == 1) {
-            k = __shfl_sync(kFull, k, 0);
+            c = __shfl_sync(kFull, c, 0);
+            nch = __shfl_sync(kFull, nch, 0);
             slot = __shfl_sync(kFull, slot, 0);
-            const uint32_t idx = slot - P.n_queries;
-            if (uint32_t(lane) < k) {
-                const uint32_t pos = (bot + lane) & D.mask;
-                P.pool[size_t(kChunk) * idx + lane] = make_uint4(D.q[pos], D.a[pos], D.b[pos], 0u);
+            const uint32_t idx0 = slot - P.n_queries;
+            for (uint32_t ch = 0; ch < nch; ++ch) {
+                if (uint32_t(lane) < c) {
+                    const uint32_t pos = (bot + ch * c + lane) & D.mask;
+                    P.pool[size_t(kChunk) * (idx0 + ch) + lane] = make_uint4(D.q[pos], D.a[pos], D.b[pos], 0u);
+                }
             }
             __threadfence();
             __syncwarp();
-            if (lane == 0) {
-                st_release(P.ready + idx, k + 1u);
-                st_don += k;
-            }
-            bot += k;
+            if (uint32_t(lane) < nch) st_release(P.ready + idx0 + lane, c + 1u);
+            if (lane == 0) st_don += c * nch;
+            bot += c * nch;
             __syncwarp();
         } else if (mode == 2) {
             rr = __shfl_sync(kFull, rr, 0);
