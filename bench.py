@@ -13,9 +13,10 @@ value: device-resident inputs, each step timed with CUDA events on the
 launching stream, L2 flushed (a 512 MB write) between steps.
 e2e: the public host API (cg_collide with host queries + read-back of the
 colliding pairs), host-timed around the synchronous calls.
-roofline: the traversal kernel, algorithmic bytes (node pairs x 96 B of box
-data + triangle tests x 72 B of triangle data) per launch over its event-timed
-duration, against the measured copy bandwidth; the FP32 view beside it.
+roofline: the traversal kernel (the dominant one), algorithmic bytes (node
+pairs x 96 B of box data) per launch over its event-timed duration, against the
+measured copy bandwidth, with the FP32 view beside it; roofline_narrow: the
+same for the narrow-phase kernel (triangle tests x 72 B of triangle data).
 cpu_baseline: the oracle restatement of the reference's CPU path (release
 flags) on all host cores over a bounded number of scene steps.
 """
@@ -209,7 +210,7 @@ def run_gpu(args) -> dict:
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kernel_ms = []
+    trav_ms, narrow_ms = [], []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -219,7 +220,8 @@ def run_gpu(args) -> dict:
             starts[k].record(stream)
             ctx.graph_launch(stream.cuda_stream)
             ends[k].record(stream)
-            kernel_ms.append(ctx.traversal_ms())
+            trav_ms.append(ctx.traversal_ms())
+            narrow_ms.append(ctx.narrow_ms())
         torch.cuda.synchronize()
         step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
         st = ctx.sync_stats()
@@ -245,12 +247,22 @@ def run_gpu(args) -> dict:
     e2e_value = world * tests_per_step * args.steps / e2e_s
 
     peaks = measured_peaks()
-    kms = float(np.mean(kernel_ms))
-    alg_bytes = st["node_pairs"] * NODE_PAIR_BYTES + st["tri_tests"] * TRI_TEST_BYTES
-    alg_flops = st["node_pairs"] * NODE_PAIR_FLOPS + st["tri_tests"] * TRI_TEST_FLOPS
-    achieved = alg_bytes / (kms / 1e3) / 1e9
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sm_count * 128 * 2 * peaks["sm_max_mhz"] * 1e6 / 1e12
+
+    def kernel_roofline(name, ms, units, unit_bytes, unit_flops):
+        by, fl = units * unit_bytes, units * unit_flops
+        ach = by / (ms / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"], "traffic": None, "kernel": name, "kernel_ms": ms,
+                "algorithmic_bytes": int(by), "peak_source": peaks["source"],
+                "fp32": {"achieved_tflops": fl / (ms / 1e3) / 1e12, "peak_tflops": fp32_peak,
+                         "frac": fl / (ms / 1e3) / 1e12 / fp32_peak}}
+
+    roof_trav = kernel_roofline("traverse_kernel", float(np.mean(trav_ms)), st["node_pairs"], NODE_PAIR_BYTES,
+                                NODE_PAIR_FLOPS)
+    roof_narrow = kernel_roofline("narrow_kernel", float(np.mean(narrow_ms)), st["tri_tests"], TRI_TEST_BYTES,
+                                  TRI_TEST_FLOPS)
 
     # plain path: the rigid pair, one query per launch (the reference's unit of work)
     rp = scenes.rigid_pair(n_poses=200)
@@ -287,20 +299,18 @@ def run_gpu(args) -> dict:
         "config": {"workload": WORKLOAD, "queries_per_step": n, "triangles": int(sum(m.n_tris for m in sc.meshes)),
                    "tri_tests_per_step": int(tests_per_step), "colliding_pairs_per_step": int(pairs_per_step),
                    "node_pairs_per_step": int(st["node_pairs"]), "cache": "L2 flushed (512 MB write) between steps",
-                   "launch": "CUDA graph: init + flag reset + pack + persistent traversal"},
+                   "launch": "CUDA graph: init + pack + persistent traversal + persistent narrow phase",
+                   "lanes_per_step": st["node_pairs"] / max(1, st["warp_steps"])},
         "queries_per_s": world * n * args.steps / (total_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * capi.QUERY_DTYPE.itemsize),
                 "d2h_bytes_per_step": int(64 + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize),
                 "ms_per_step": 1e3 * e2e_s / args.steps, "timing": "host perf_counter around synchronous calls"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "traverse_kernel",
-                     "kernel_ms": kms, "peak_source": peaks["source"],
-                     "fp32": {"achieved_tflops": alg_flops / (kms / 1e3) / 1e12, "peak_tflops": fp32_peak,
-                              "frac": alg_flops / (kms / 1e3) / 1e12 / fp32_peak}},
+        "roofline": roof_trav,
+        "roofline_narrow": roof_narrow,
         "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch",
                   "queries_per_s": 200 / (plain_ms / 1e3), "tri_tests_per_s": ptests / (plain_ms / 1e3),
                   "ms_per_query": plain_ms / 200},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 4 * args.steps,
         "clocks": clk,
     }
     if cpu:
