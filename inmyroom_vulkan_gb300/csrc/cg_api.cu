@@ -209,8 +209,9 @@ int check_config(cg_ctx* c, const cg_config* cfg) {
         return fail(c, CG_ERR_INVALID_ARGUMENT, "stack_entries must be a power of two in [256, 4096]");
     if (cfg->warps_per_block == 0 || cfg->warps_per_block > 8)
         return fail(c, CG_ERR_INVALID_ARGUMENT, "warps_per_block must be in [1, 8]");
-    if (cfg->leaf_flush == 0 || cfg->leaf_flush > uint32_t(kLeafCap - 32 + 1))
-        return fail(c, CG_ERR_INVALID_ARGUMENT, "leaf_flush must be in [1, %d]", kLeafCap - 32 + 1);
+    if (cfg->leaf_flush == 0 || cfg->leaf_flush > uint32_t(kLeafCap - 63))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "leaf_flush must be in [1, %d]", kLeafCap - 63);
+    if (cfg->max_queries >= kItemSideB) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_queries must be < 2^31");
     if (cfg->queue_capacity < 1024) return fail(c, CG_ERR_INVALID_ARGUMENT, "queue_capacity must be >= 1024");
     if (cfg->wait_limit_ms == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "wait_limit_ms must be > 0");
     return CG_OK;
@@ -283,7 +284,10 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
     const uint32_t trace_ns = c->trace_ns ? c->trace_ns : 1000u;
     CG_CUDA(launch_init(c->d_ctr, c->d_ready, c->slot_alloc, n, trace, s), "init kernel");
-    CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->d_packed, c->d_ctr, s), "pack kernel");
+    const uint32_t leaf_cap = uint32_t(std::min<uint64_t>(c->cfg.max_leaf_pairs, 0xffffffffull));
+    CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->recs.ptr, c->d_packed, c->d_ctr,
+                        c->d_leaf_list, leaf_cap, s),
+            "pack kernel");
     TraverseParams p{};
     p.q = c->d_packed;
     p.n_queries = n;

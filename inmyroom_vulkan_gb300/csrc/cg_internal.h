@@ -32,7 +32,7 @@
 namespace cg {
 
 constexpr uint32_t kLeafFlag = 0x80000000u;
-constexpr int kLeafCap = 64;        // buffered leaf pairs per traversal warp
+constexpr int kLeafCap = 96;        // buffered leaf pairs per traversal warp (a step adds up to 64)
 constexpr int kChunk = 32;          // node pairs per donated task slot
 constexpr int kTraceBuckets = 512;  // utilisation trace: counters per time bucket
 
@@ -46,12 +46,22 @@ struct DevTree {
     const float* nrm;
 };
 
-// A query as the kernels read it: relative matrix columns, the two roots and
-// triangle bases (to report tree-local triangle indices). root_a == 0 marks an
-// invalid query.
+// A query as the kernels read it: relative matrix columns, the first
+// traversal item (made by the pack kernel from the root pair) and the
+// triangle bases (to report tree-local triangle indices).
+//
+// Traversal item (query word, split record, other record): the node being
+// split has its two child boxes at records split and split + 1; `other` is
+// the box of the other tree they are tested against. kItemSideB in the query
+// word marks children of the second tree. A query word of kNoItem means the
+// query has no item (invalid query, roots disjoint, or roots both leaves).
+constexpr uint32_t kItemSideB = 0x80000000u;
+constexpr uint32_t kNoItem = 0xffffffffu;
+
 struct alignas(16) PackedQuery {
     float4 m[4];
-    uint32_t root_a, root_b, tri_base_a, tri_base_b;
+    uint32_t item_q, item_split, item_other, pad;
+    uint32_t tri_base_a, tri_base_b, pad2, pad3;
 };
 
 struct Counters {
@@ -115,8 +125,8 @@ __host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return
 constexpr uint32_t kNarrowWarpWords = 5u * 32u + 1u;
 
 // Kernel launchers (cg_kernels.cu).
-cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
-                        Counters* ctr, cudaStream_t s);
+cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,
+                        PackedQuery* out, Counters* ctr, uint4* leaf_list, uint32_t leaf_cap, cudaStream_t s);
 cudaError_t launch_init(Counters* ctr, unsigned int* ready, uint32_t slot_alloc, uint32_t n_queries,
                         unsigned int* trace, cudaStream_t s);
 cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s);

@@ -124,6 +124,52 @@ __device__ __forceinline__ void load_tri(const float4* tris, uint32_t i, float3&
     p2 = make_float3(c.x, c.y, c.z);
 }
 
+// Round g of the 15 axes of cg::sat (same axes, same order, same arithmetic):
+// g = 0 a's faces, 1 b's faces, 2..4 a_u|a_v|a_w x b_u, b_v, b_w.
+__device__ __forceinline__ bool sat_round(const Box& a, const Box& b, int g) {
+    float3 x0, y0, x1, y1, x2, y2;
+    if (g < 2) {
+        const float3 u = g ? b.u : a.u;
+        const float3 v = g ? b.v : a.v;
+        const float3 w = g ? b.w : a.w;
+        x0 = v;
+        y0 = w;
+        x1 = u;
+        y1 = w;
+        x2 = u;
+        y2 = v;
+    } else {
+        const float3 e = g == 2 ? a.u : (g == 3 ? a.v : a.w);
+        x0 = e;
+        y0 = b.u;
+        x1 = e;
+        y1 = b.v;
+        x2 = e;
+        y2 = b.w;
+    }
+    const bool ok0 = overlap_on(a, b, cross3(x0, y0));
+    const bool ok1 = overlap_on(a, b, cross3(x1, y1));
+    const bool ok2 = overlap_on(a, b, cross3(x2, y2));
+    return ok0 & ok1 & ok2;
+}
+
+// Two box-pair SATs side by side, round by round, for instruction-level
+// parallelism; each verdict is the conjunction of its 15 axes, identical to
+// cg::sat.
+__device__ __forceinline__ void sat_two(const Box& a0, const Box& b0, const Box& a1, const Box& b1, bool& ok0,
+                                        bool& ok1) {
+    bool al0 = ok0, al1 = ok1;
+#pragma unroll 1
+    for (int g = 0; g < 5 && (al0 | al1); ++g) {
+        const bool r0 = sat_round(a0, b0, g);
+        const bool r1 = sat_round(a1, b1, g);
+        al0 = al0 & r0;
+        al1 = al1 & r1;
+    }
+    ok0 = al0;
+    ok1 = al1;
+}
+
 // The 15 axes of cg::sat in the same order and with the same arithmetic, three
 // independent axes per round (a's faces, b's faces, a_u x b_*, a_v x b_*,
 // a_w x b_*); the verdict is the conjunction, so it is identical.
@@ -233,20 +279,19 @@ __device__ uint32_t take_chunk(const TraverseParams& P, uint32_t slot, unsigned 
             D.b[pos] = e.z;
         }
     } else {
-        // root pair of query `slot`; an invalid query (root 0) has no work
-        uint32_t ra = 0, rb = 0;
+        // the first item of query `slot`, made by the pack kernel
+        uint32_t iq = kNoItem;
         if (lane == 0) {
             const PackedQuery* Q = P.q + slot;
-            ra = __ldg(&Q->root_a);
-            rb = __ldg(&Q->root_b);
-            if (ra != 0u) {
+            iq = __ldg(&Q->item_q);
+            if (iq != kNoItem) {
                 const uint32_t pos = top & D.mask;
-                D.q[pos] = slot;
-                D.a[pos] = ra;
-                D.b[pos] = rb;
+                D.q[pos] = iq;
+                D.a[pos] = __ldg(&Q->item_split);
+                D.b[pos] = __ldg(&Q->item_other);
             }
         }
-        cnt = __shfl_sync(kFull, ra != 0u ? 1u : 0u, 0);
+        cnt = __shfl_sync(kFull, iq != kNoItem ? 1u : 0u, 0);
     }
     __syncwarp();
     return cnt;
@@ -269,7 +314,7 @@ __device__ __forceinline__ unsigned long long trace_base(Counters* ctr) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(256, 3) traverse_kernel(const TraverseParams P) {
+__global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -310,81 +355,126 @@ __global__ void __launch_bounds__(256, 3) traverse_kernel(const TraverseParams P
         unsigned long long qs = 0;
         if (lane == 0) qs = ld_relaxed64(ht);
 
-        // ---- one step over up to 32 node pairs from the top of the deque
+        // ---- one step over up to 32 items from the top of the deque. An item
+        // tests both children of a split node against the other box: the
+        // other record is loaded (and, for the second tree, transformed) once,
+        // the two child records come from one 128-byte line, and the two SATs
+        // run side by side.
         const uint32_t size = top - bot;
         const uint32_t n = size < 32u ? size : 32u;
         const bool active = uint32_t(lane) < n;
-        uint32_t q = 0, ra = 0, rb = 0;
+        uint32_t iq = 0, is = 0, io = 0;
         if (active) {
             const uint32_t pos = (top - n + lane) & D.mask;
-            q = D.q[pos];
-            ra = D.a[pos];
-            rb = D.b[pos];
+            iq = D.q[pos];
+            is = D.a[pos];
+            io = D.b[pos];
         }
         top -= n;
         __syncwarp();
 
-        int act = 0;  // 1: split A, 2: split B, 3: leaf pair
-        uint32_t child = 0, offA = 0, offB = 0, cnt = 0;
+        // Per lane, per child k: a new item (split node, other record, query
+        // word) or a candidate leaf pair (triangle offsets and counts).
+        bool item[2] = {false, false}, leaf[2] = {false, false};
+        uint32_t out_q[2] = {0, 0}, out_s[2] = {0, 0}, out_o[2] = {0, 0};
+        const uint32_t qi = iq & ~kItemSideB;
         if (active) {
-            const Mat4 M = load_mat(P.q + q);
-            const Rec A = load_rec(P.recs, ra);
-            const Rec B = load_rec(P.recs, rb);
-            const Box bb = xform_box(M, B.box);
-            if (sat_grouped(A.box, bb)) {
-                const bool la = (A.meta & kLeafFlag) != 0;
-                const bool lb = (B.meta & kLeafFlag) != 0;
+            const bool sideB = (iq & kItemSideB) != 0;
+            const Mat4 M = load_mat(P.q + qi);
+            const Rec O = load_rec(P.recs, io);
+            const Rec C0 = load_rec(P.recs, is);
+            const Rec C1 = load_rec(P.recs, is + 1u);
+            Box a0, a1, b0, b1;
+            if (sideB) {
+                a0 = O.box;
+                a1 = O.box;
+                b0 = xform_box(M, C0.box);
+                b1 = xform_box(M, C1.box);
+            } else {
+                a0 = C0.box;
+                a1 = C1.box;
+                b0 = xform_box(M, O.box);
+                b1 = b0;
+            }
+            bool ok[2] = {true, true};
+            sat_two(a0, b0, a1, b1, ok[0], ok[1]);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (!ok[k]) continue;
+                const Rec& C = k ? C1 : C0;
+                const uint32_t rc = is + uint32_t(k);
+                const uint32_t a_ref = sideB ? O.ref : C.ref;
+                const uint32_t a_meta = sideB ? O.meta : C.meta;
+                const float a_surf = sideB ? O.surf : C.surf;
+                const uint32_t b_ref = sideB ? C.ref : O.ref;
+                const uint32_t b_meta = sideB ? C.meta : O.meta;
+                const uint32_t ra = sideB ? io : rc;
+                const uint32_t rb = sideB ? rc : io;
+                const bool la = (a_meta & kLeafFlag) != 0;
+                const bool lb = (b_meta & kLeafFlag) != 0;
+                int act;  // 1: split A, 2: split B, 3: leaf pair
                 if (!la && !lb)
-                    act = (A.surf >= surface(bb)) ? 1 : 2;
+                    act = (a_surf >= surface(k ? b1 : b0)) ? 1 : 2;
                 else if (la && !lb)
                     act = 2;
                 else if (!la && lb)
                     act = 1;
                 else
                     act = 3;
-                child = act == 1 ? A.ref : B.ref;
-                // the split node's two child records share one 128-byte line
-                // (records are allocated in aligned pairs): fetch it into L1
-                // for the next step
-                if (act < 3) asm volatile("prefetch.global.L1 [%0];" ::"l"(P.recs + 4ull * child));
-                offA = A.ref;
-                offB = B.ref;
-                cnt = (A.meta & 0xffffu) | ((B.meta & 0xffffu) << 16);
+                if (act == 3) {
+                    // leaf pair: first triangles of both leaves, counts packed
+                    leaf[k] = true;
+                    out_s[k] = a_ref;
+                    out_o[k] = b_ref;
+                    out_q[k] = (a_meta & 0xffffu) | ((b_meta & 0xffffu) << 16);
+                } else {
+                    item[k] = true;
+                    const uint32_t split = act == 1 ? a_ref : b_ref;
+                    out_q[k] = act == 1 ? qi : (qi | kItemSideB);
+                    out_s[k] = split;
+                    out_o[k] = act == 1 ? rb : ra;
+                    // the split node's two child records share one 128-byte
+                    // line: fetch it into L1 for the step that tests them
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(P.recs + 4ull * split));
+                }
             }
         }
 
-        const unsigned pushmask = __ballot_sync(kFull, act == 1 || act == 2);
-        if (act == 1 || act == 2) {
-            const uint32_t r = __popc(pushmask & lanemask_lt());
-            const uint32_t p0 = (top + 2u * r) & D.mask;
-            const uint32_t p1 = (top + 2u * r + 1u) & D.mask;
-            D.q[p0] = q;
-            D.q[p1] = q;
-            if (act == 1) {
-                D.a[p0] = child + 1u;
-                D.b[p0] = rb;
-                D.a[p1] = child;
-                D.b[p1] = rb;
-            } else {
-                D.a[p0] = ra;
-                D.b[p0] = child + 1u;
-                D.a[p1] = ra;
-                D.b[p1] = child;
+        const unsigned i0 = __ballot_sync(kFull, item[0]), i1 = __ballot_sync(kFull, item[1]);
+        {
+            const unsigned lt = lanemask_lt();
+            uint32_t r = __popc(i0 & lt) + __popc(i1 & lt);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (item[k]) {
+                    const uint32_t p = (top + r) & D.mask;
+                    D.q[p] = out_q[k];
+                    D.a[p] = out_s[k];
+                    D.b[p] = out_o[k];
+                    ++r;
+                }
             }
         }
-        top += 2u * __popc(pushmask);
+        top += __popc(i0) + __popc(i1);
 
-        const unsigned leafmask = __ballot_sync(kFull, act == 3);
-        if (act == 3) {
-            const uint32_t slot = nl + __popc(leafmask & lanemask_lt());
-            lq[slot] = q;
-            loa[slot] = offA;
-            lob[slot] = offB;
-            lcn[slot] = cnt;
+        const unsigned l0 = __ballot_sync(kFull, leaf[0]), l1 = __ballot_sync(kFull, leaf[1]);
+        {
+            const unsigned lt = lanemask_lt();
+            uint32_t r = nl + __popc(l0 & lt) + __popc(l1 & lt);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (leaf[k]) {
+                    lq[r] = qi;
+                    loa[r] = out_s[k];
+                    lob[r] = out_o[k];
+                    lcn[r] = out_q[k];
+                    ++r;
+                }
+            }
         }
-        nl += __popc(leafmask);
+        nl += __popc(l0) + __popc(l1);
         if (lane == 0) {
-            st_nodes += n;
+            st_nodes += 2u * n;
             ++st_steps;
             if (P.trace) trace_add(P.trace, P.trace_ns, t_base, 0, n);
         }
@@ -603,8 +693,12 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
     }
 }
 
-__global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
-                            Counters* ctr) {
+// One thread per query: packs the relative matrix and runs the root pair the
+// way the traversal runs every pair (SAT, then the descent rule), so that the
+// query enters the work queue as its first item; a leaf-leaf root goes
+// straight to the leaf-pair list.
+__global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees,
+                            const float4* recs, PackedQuery* out, Counters* ctr, uint4* leaf_list, uint32_t leaf_cap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const cg_query Q = in[i];
@@ -613,15 +707,36 @@ __global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees
     p.m[1] = make_float4(Q.relative[4], Q.relative[5], Q.relative[6], Q.relative[7]);
     p.m[2] = make_float4(Q.relative[8], Q.relative[9], Q.relative[10], Q.relative[11]);
     p.m[3] = make_float4(Q.relative[12], Q.relative[13], Q.relative[14], Q.relative[15]);
+    p.item_q = kNoItem;
+    p.item_split = p.item_other = p.pad = 0u;
+    p.tri_base_a = p.tri_base_b = p.pad2 = p.pad3 = 0u;
     const bool ok = Q.tree_a < n_trees && Q.tree_b < n_trees && trees[Q.tree_a].live && trees[Q.tree_b].live;
-    if (ok) {
-        p.root_a = trees[Q.tree_a].rec_base + 1u;
-        p.root_b = trees[Q.tree_b].rec_base + 1u;
-        p.tri_base_a = trees[Q.tree_a].tri_base;
-        p.tri_base_b = trees[Q.tree_b].tri_base;
-    } else {
-        p.root_a = p.root_b = p.tri_base_a = p.tri_base_b = 0u;
+    if (!ok) {
         atomicOr(&ctr->error, ERR_BAD_QUERY);
+        out[i] = p;
+        return;
+    }
+    p.tri_base_a = trees[Q.tree_a].tri_base;
+    p.tri_base_b = trees[Q.tree_b].tri_base;
+    const uint32_t ra = trees[Q.tree_a].rec_base + 1u;
+    const uint32_t rb = trees[Q.tree_b].rec_base + 1u;
+    const Mat4 M{p.m[0], p.m[1], p.m[2], p.m[3]};
+    const Rec A = load_rec(recs, ra);
+    const Rec B = load_rec(recs, rb);
+    const Box bb = xform_box(M, B.box);
+    atomicAdd(&ctr->node_pairs, 1ull);
+    if (sat(A.box, bb)) {
+        const bool la = (A.meta & kLeafFlag) != 0;
+        const bool lb = (B.meta & kLeafFlag) != 0;
+        if (la && lb) {
+            const unsigned long long idx = atomicAdd(&ctr->n_leafs, 1ull);
+            if (idx < leaf_cap) leaf_list[idx] = make_uint4(i, A.ref, B.ref, (A.meta & 0xffffu) | ((B.meta & 0xffffu) << 16));
+        } else {
+            const bool split_a = (!la && !lb) ? (A.surf >= surface(bb)) : !la;
+            p.item_q = split_a ? i : (i | kItemSideB);
+            p.item_split = split_a ? A.ref : B.ref;
+            p.item_other = split_a ? rb : ra;
+        }
     }
     out[i] = p;
 }
@@ -664,10 +779,10 @@ __global__ void surfaces_kernel(float4* recs, uint32_t first, uint32_t n_recs) {
     p[3].z = surface(box);
 }
 
-cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, PackedQuery* out,
-                        Counters* ctr, cudaStream_t s) {
+cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,
+                        PackedQuery* out, Counters* ctr, uint4* leaf_list, uint32_t leaf_cap, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    pack_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, n, trees, n_trees, out, ctr);
+    pack_kernel<<<(n + 127) / 128, 128, 0, s>>>(in, n, trees, n_trees, recs, out, ctr, leaf_list, leaf_cap);
     return cudaGetLastError();
 }
 
