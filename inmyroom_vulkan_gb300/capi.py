@@ -238,13 +238,19 @@ class Context:
         d["rc"] = rc
         return d
 
-    def tri_pairs(self) -> np.ndarray:
+    def tri_pairs(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
+        """Colliding pairs of the last launch. With `out` (a TRI_PAIR_DTYPE array,
+        e.g. a view of pinned memory) and the pair `count` known from the stats,
+        the read is a single device-to-host copy into it."""
         n = C.c_uint64()
-        self.lib.cg_read_tri_pairs(self.h, None, 0, C.byref(n))
-        out = np.zeros(n.value, TRI_PAIR_DTYPE)
-        rc = self.lib.cg_read_tri_pairs(self.h, out.ctypes.data if n.value else None, n.value, C.byref(n))
+        if count is None:
+            self.lib.cg_read_tri_pairs(self.h, None, 0, C.byref(n))
+            count = n.value
+        if out is None or len(out) < count:
+            out = np.zeros(count, TRI_PAIR_DTYPE)
+        rc = self.lib.cg_read_tri_pairs(self.h, out.ctypes.data if count else None, count, C.byref(n))
         self._check(rc, "cg_read_tri_pairs")
-        return out
+        return out[:n.value]
 
     def leaf_pairs(self) -> np.ndarray:
         n = C.c_uint64()

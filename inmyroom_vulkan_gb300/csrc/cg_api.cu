@@ -135,6 +135,11 @@ struct cg_ctx {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_gen = 0;         // arena generations the graph was captured with
+    struct HostGraph {              // cg_collide's own graph of a whole step
+        cudaGraphExec_t exec = nullptr;
+        uint32_t n = 0, flags = 0;
+        uint64_t gen = 0;
+    } host_graph;
     bool capturing = false;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_t2 = nullptr;  // traversal start, end; narrow end
     cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
@@ -199,8 +204,10 @@ void free_buffers(cg_ctx* c) {
 void drop_graph(cg_ctx* c) {
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->graph) cudaGraphDestroy(c->graph);
+    if (c->host_graph.exec) cudaGraphExecDestroy(c->host_graph.exec);
     c->graph_exec = nullptr;
     c->graph = nullptr;
+    c->host_graph.exec = nullptr;
 }
 
 int check_config(cg_ctx* c, const cg_config* cfg) {
@@ -426,7 +433,7 @@ void cg_config_default(cg_config* cfg) {
     cfg->max_leaf_pairs = 1ull << 22;
     cfg->queue_capacity = 1u << 20;
     cfg->warps_per_block = 4;
-    cfg->blocks_per_sm = 3;
+    cfg->blocks_per_sm = 2;
     cfg->stack_entries = 512;
     cfg->donate_min = 32;
     cfg->leaf_flush = 32;
@@ -684,15 +691,41 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
             return fail(c, CG_ERR_NOT_FOUND, "query %u names tree %u / %u", i, a, b);
     }
     cudaSetDevice(c->device);
-    if (n) {
-        std::memcpy(c->h_queries, queries, sizeof(cg_query) * n);
-        CG_CUDA(cudaMemcpyAsync(c->d_queries, c->h_queries, sizeof(cg_query) * n, cudaMemcpyHostToDevice, c->stream),
-                "upload queries");
-    }
+    if (n) std::memcpy(c->h_queries, queries, sizeof(cg_query) * n);
     c->last_flags = flags;
-    int rc = enqueue_step(c, c->d_queries, n, flags, c->stream);
-    if (rc != CG_OK) return rc;
-    return cg_sync_stats(c, st);
+    // The whole step (query upload from the pinned staging buffer, kernels,
+    // counter read-back) is one CUDA graph, captured once per (n, flags) and
+    // tree-storage generation and replayed.
+    auto& G = c->host_graph;
+    if (!G.exec || G.n != n || G.flags != flags || G.gen != arena_gen(c)) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        G.exec = nullptr;
+        CG_CUDA(cudaStreamSynchronize(c->stream), "sync before capture");
+        CG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        c->capturing = true;
+        cudaError_t e = cudaSuccess;
+        if (n)
+            e = cudaMemcpyAsync(c->d_queries, c->h_queries, sizeof(cg_query) * n, cudaMemcpyHostToDevice, c->stream);
+        int rc = e == cudaSuccess ? enqueue_step(c, c->d_queries, n, flags, c->stream) : CG_ERR_CUDA;
+        if (rc == CG_OK)
+            e = cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream);
+        c->capturing = false;
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+        if (rc != CG_OK || e != cudaSuccess || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return rc != CG_OK ? rc : cuda_fail(c, e != cudaSuccess ? e : ee, "capture collide step");
+        }
+        e = cudaGraphInstantiate(&G.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(c, e, "instantiate collide step");
+        G.n = n;
+        G.flags = flags;
+        G.gen = arena_gen(c);
+    }
+    CG_CUDA(cudaGraphLaunch(G.exec, c->stream), "collide step");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "collide");
+    return stats_from(c, *c->h_ctr, st);
 }
 
 int cg_read_tri_pairs(cg_ctx* c, cg_tri_pair* out, uint64_t cap, uint64_t* n) {
