@@ -159,6 +159,7 @@ typedef struct cg_stats {
 #define CG_KEEP_LEAF_PAIRS 1u /* also write the candidate leaf pairs */
 #define CG_NO_TRI_PAIRS 2u    /* count triangle tests and hits but do not write pairs */
 #define CG_TRACE 4u           /* record a utilisation timeline (see cg_read_trace) */
+#define CG_MID_ONLY 8u        /* mid phase only: candidate leaf pairs, no triangle tests */
 
 /* Host queries in, stats out; synchronous. Results stay on the device until read. */
 int cg_collide(cg_ctx* ctx, const cg_query* queries, uint32_t n, uint32_t flags, cg_stats* stats);

@@ -20,6 +20,7 @@ STATUS = {0: "CG_OK", -1: "CG_ERR_INVALID_ARGUMENT", -2: "CG_ERR_CUDA", -3: "CG_
 CG_KEEP_LEAF_PAIRS = 1
 CG_NO_TRI_PAIRS = 2
 CG_TRACE = 4
+CG_MID_ONLY = 8
 
 # Every function the header declares (checked by the CPU tests).
 EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",

@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
             const uint32_t t0 = __shfl_up_sync(kFull, s0, o);
             if (lane >= o) s0 += t0;
         }
-        const uint32_t total = __shfl_sync(kFull, s0, 31);
+        const uint32_t total = (P.flags & CG_MID_ONLY) ? 0u : __shfl_sync(kFull, s0, 31);
         pre[lane] = s0 - c0;
         if (lane == 0) pre[32] = total;
         __syncwarp();
