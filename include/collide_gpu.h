@@ -61,6 +61,8 @@ typedef struct cg_config {
     uint32_t donate_min;       /* a warp donates work to idle warps only above this stack size */
     uint32_t leaf_flush;       /* leaf pairs a traversal warp buffers before appending them to the list (1..33) */
     uint32_t wait_limit_ms;    /* limit of every device-side wait */
+    uint32_t pad;
+    uint64_t max_contacts;     /* triangles with contacts per launch (CG_CONTACTS); rays <= 3x this */
 } cg_config;
 
 void cg_config_default(cg_config* cfg);
@@ -160,6 +162,43 @@ typedef struct cg_stats {
 #define CG_NO_TRI_PAIRS 2u    /* count triangle tests and hits but do not write pairs */
 #define CG_TRACE 4u           /* record a utilisation timeline (see cg_read_trace) */
 #define CG_MID_ONLY 8u        /* mid phase only: candidate leaf pairs, no triangle tests */
+#define CG_CONTACTS 16u       /* also per-triangle contacts, uncollide rays and their averages */
+
+/* Per-triangle contact record, the TriangleCandidateRays of
+ * CreateUncollideRays.cpp:14-58 after the merge: bit k of mask set = vertex k
+ * of the triangle is not outside the other triangles' planes; weighted_avg =
+ * length-weighted mean of the intersection-segment midpoints (the first
+ * tree's model space); weight = total segment length. side 0 = first tree,
+ * 1 = second tree; tri is the tree-order index. 32 bytes. */
+typedef struct cg_contact {
+    uint32_t query;
+    uint32_t side;
+    uint32_t tri;
+    uint32_t mask;
+    float weighted_avg[3];
+    float weight;
+} cg_contact;
+
+/* One uncollide ray (CreateUncollideRays.cpp:131-178) in the first tree's
+ * model space: from a "not outside" vertex (once per vertex index) along the
+ * negated vertex normal, or from the weighted contact average along the
+ * negated interpolated normal. side as in cg_contact. 32 bytes. */
+typedef struct cg_ray {
+    uint32_t query;
+    uint32_t side;
+    float origin[3];
+    float direction[3];
+} cg_ray;
+
+/* Per query: average_point_first_modelspace and
+ * average_point_second_modelspace of CDentriesUncollideRays
+ * (CreateUncollideRays.cpp:240-258) and the ray counts. 32 bytes. */
+typedef struct cg_ray_average {
+    float first[3];
+    float second[3];
+    uint32_t rays_first;
+    uint32_t rays_second;
+} cg_ray_average;
 
 /* Host queries in, stats out; synchronous. Results stay on the device until read. */
 int cg_collide(cg_ctx* ctx, const cg_query* queries, uint32_t n, uint32_t flags, cg_stats* stats);
@@ -172,6 +211,12 @@ int cg_read_tri_pairs(cg_ctx* ctx, cg_tri_pair* out, uint64_t cap, uint64_t* n);
 int cg_read_leaf_pairs(cg_ctx* ctx, cg_leaf_pair* out, uint64_t cap, uint64_t* n);
 /* Device pointers to the last launch's results (valid until the next launch). */
 int cg_device_results(cg_ctx* ctx, const cg_tri_pair** pairs, const unsigned long long** pair_count);
+
+/* Results of a launch made with CG_CONTACTS (record order is unspecified;
+ * read the averages with cap >= the launch's query count). */
+int cg_read_contacts(cg_ctx* ctx, cg_contact* out, uint64_t cap, uint64_t* n);
+int cg_read_rays(cg_ctx* ctx, cg_ray* out, uint64_t cap, uint64_t* n);
+int cg_read_ray_averages(cg_ctx* ctx, cg_ray_average* out, uint64_t cap, uint64_t* n);
 
 /* Device times of the last step's two main kernels, the OBB-tree traversal
  * (emits candidate leaf pairs) and the narrow phase (triangle-pair tests),

@@ -21,11 +21,13 @@ CG_KEEP_LEAF_PAIRS = 1
 CG_NO_TRI_PAIRS = 2
 CG_TRACE = 4
 CG_MID_ONLY = 8
+CG_CONTACTS = 16
 
 # Every function the header declares (checked by the CPU tests).
 EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",
            "cg_last_error", "cg_tree_upload", "cg_tree_free", "cg_relative_matrix", "cg_collide", "cg_collide_async",
-           "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results",
+           "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results", "cg_read_contacts",
+           "cg_read_rays", "cg_read_ray_averages",
            "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch"]
 
 
@@ -39,7 +41,8 @@ class cg_config(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_queries", C.c_uint32), ("max_tri_pairs", C.c_uint64),
                 ("max_leaf_pairs", C.c_uint64), ("queue_capacity", C.c_uint32), ("warps_per_block", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("stack_entries", C.c_uint32), ("donate_min", C.c_uint32),
-                ("leaf_flush", C.c_uint32), ("wait_limit_ms", C.c_uint32)]
+                ("leaf_flush", C.c_uint32), ("wait_limit_ms", C.c_uint32), ("pad", C.c_uint32),
+                ("max_contacts", C.c_uint64)]
 
 
 class cg_obb(C.Structure):
@@ -67,7 +70,13 @@ TRI_PAIR_DTYPE = np.dtype([("query", "<u4"), ("tri_a", "<u4"), ("tri_b", "<u4"),
                            ("target", "<f4", (3,))])
 LEAF_PAIR_DTYPE = np.dtype([("query", "<u4"), ("offset_a", "<u4"), ("offset_b", "<u4"), ("count_a", "<u2"),
                             ("count_b", "<u2")])
+CONTACT_DTYPE = np.dtype([("query", "<u4"), ("side", "<u4"), ("tri", "<u4"), ("mask", "<u4"),
+                          ("weighted_avg", "<f4", (3,)), ("weight", "<f4")])
+RAY_DTYPE = np.dtype([("query", "<u4"), ("side", "<u4"), ("origin", "<f4", (3,)), ("direction", "<f4", (3,))])
+RAY_AVERAGE_DTYPE = np.dtype([("first", "<f4", (3,)), ("second", "<f4", (3,)), ("rays_first", "<u4"),
+                              ("rays_second", "<u4")])
 assert QUERY_DTYPE.itemsize == 72 and TRI_PAIR_DTYPE.itemsize == 36 and LEAF_PAIR_DTYPE.itemsize == 16
+assert CONTACT_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32 and RAY_AVERAGE_DTYPE.itemsize == 32
 
 _lib = None
 
@@ -98,6 +107,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_read_tri_pairs.argtypes = [vp, vp, u64, C.POINTER(u64)]
     lib.cg_read_leaf_pairs.argtypes = [vp, vp, u64, C.POINTER(u64)]
     lib.cg_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
+    lib.cg_read_contacts.argtypes = [vp, vp, u64, C.POINTER(u64)]
+    lib.cg_read_rays.argtypes = [vp, vp, u64, C.POINTER(u64)]
+    lib.cg_read_ray_averages.argtypes = [vp, vp, u64, C.POINTER(u64)]
     lib.cg_traversal_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
     lib.cg_read_trace.argtypes = [vp, u32, vp, u32]
     lib.cg_narrow_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
@@ -260,6 +272,26 @@ class Context:
         rc = self.lib.cg_read_leaf_pairs(self.h, out.ctypes.data if n.value else None, n.value, C.byref(n))
         self._check(rc, "cg_read_leaf_pairs")
         return out
+
+    def _read(self, fn, dtype) -> np.ndarray:
+        n = C.c_uint64()
+        self._check(getattr(self.lib, fn)(self.h, None, 0, C.byref(n)), fn)
+        out = np.zeros(n.value, dtype)
+        rc = getattr(self.lib, fn)(self.h, out.ctypes.data if n.value else None, n.value, C.byref(n))
+        self._check(rc, fn)
+        return out
+
+    def contacts(self) -> np.ndarray:
+        """Per-triangle contacts of the last CG_CONTACTS launch (CONTACT_DTYPE, unordered)."""
+        return self._read("cg_read_contacts", CONTACT_DTYPE)
+
+    def rays(self) -> np.ndarray:
+        """Uncollide rays of the last CG_CONTACTS launch (RAY_DTYPE, unordered)."""
+        return self._read("cg_read_rays", RAY_DTYPE)
+
+    def ray_averages(self) -> np.ndarray:
+        """Per query: mean ray origins of both sides (RAY_AVERAGE_DTYPE)."""
+        return self._read("cg_read_ray_averages", RAY_AVERAGE_DTYPE)
 
     def device_results(self) -> tuple[int, int]:
         p, n = C.c_void_p(), C.c_void_p()

@@ -112,6 +112,7 @@ struct cg_ctx {
     Arena recs, tris;
     DevTree* d_trees = nullptr;
     uint32_t d_trees_cap = 0;
+    uint64_t table_gen = 0;         // reallocations of d_trees
 
     // per-launch buffers
     cg_query* d_queries = nullptr;  // staging for host queries
@@ -126,6 +127,28 @@ struct cg_ctx {
     cg_leaf_pair* d_leafs = nullptr;
     unsigned int* d_trace = nullptr;
     uint32_t trace_ns = 0;
+
+    // contacts and rays (CG_CONTACTS), allocated when max_contacts > 0
+    struct Contacts {
+        uint32_t* pair_leaf = nullptr;
+        ContactSlot* table = nullptr;
+        uint32_t table_slots = 0;
+        uint32_t* occupied = nullptr;
+        unsigned long long* vkeys = nullptr;
+        uint32_t vslots = 0;
+        uint32_t* vocc = nullptr;
+        uint32_t* zero = nullptr;
+        uint32_t zero_cap = 0;
+        unsigned long long* gkeys = nullptr;
+        unsigned int* gflag = nullptr;
+        uint32_t gslots = 0;
+        uint32_t* gocc = nullptr;
+        cg_contact* contacts = nullptr;
+        cg_ray* rays = nullptr;
+        uint32_t max_rays = 0;
+        double* sums = nullptr;
+        cg_ray_average* averages = nullptr;
+    } ct;
 
     cg_query* h_queries = nullptr;  // pinned
     Counters* h_ctr = nullptr;      // pinned
@@ -174,7 +197,8 @@ int cuda_fail(cg_ctx* c, cudaError_t e, const char* what) {
 
 bool pow2(uint32_t x) { return x && !(x & (x - 1)); }
 
-uint64_t arena_gen(const cg_ctx* c) { return c->recs.gen * 1000003ull + c->tris.gen; }
+// Changes whenever a device address that a captured graph holds changes.
+uint64_t arena_gen(const cg_ctx* c) { return (c->recs.gen * 1000003ull + c->tris.gen) * 1000003ull + c->table_gen; }
 
 void free_buffers(cg_ctx* c) {
     cudaFree(c->d_queries);
@@ -186,6 +210,21 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_pairs);
     cudaFree(c->d_leafs);
     cudaFree(c->d_trace);
+    auto& t = c->ct;
+    cudaFree(t.pair_leaf);
+    cudaFree(t.table);
+    cudaFree(t.occupied);
+    cudaFree(t.vkeys);
+    cudaFree(t.vocc);
+    cudaFree(t.zero);
+    cudaFree(t.gkeys);
+    cudaFree(t.gflag);
+    cudaFree(t.gocc);
+    cudaFree(t.contacts);
+    cudaFree(t.rays);
+    cudaFree(t.sums);
+    cudaFree(t.averages);
+    t = cg_ctx::Contacts{};
     cudaFreeHost(c->h_queries);
     cudaFreeHost(c->h_ctr);
     c->d_queries = nullptr;
@@ -221,6 +260,10 @@ int check_config(cg_ctx* c, const cg_config* cfg) {
     if (cfg->max_queries >= kItemSideB) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_queries must be < 2^31");
     if (cfg->queue_capacity < 1024) return fail(c, CG_ERR_INVALID_ARGUMENT, "queue_capacity must be >= 1024");
     if (cfg->wait_limit_ms == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "wait_limit_ms must be > 0");
+    if (cfg->max_leaf_pairs >= (1ull << 31)) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_leaf_pairs must be < 2^31");
+    if (cfg->max_contacts > (1ull << 28)) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_contacts must be <= 2^28");
+    if (cfg->max_contacts && (cfg->max_tri_pairs == 0 || cfg->max_tri_pairs >= (1ull << 32)))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "contacts need 0 < max_tri_pairs < 2^32");
     return CG_OK;
 }
 
@@ -251,6 +294,37 @@ int alloc_buffers(cg_ctx* c) {
     if (g.max_tri_pairs) CG_CUDA(cudaMalloc(&c->d_pairs, sizeof(cg_tri_pair) * g.max_tri_pairs), "alloc pair output");
     if (g.max_leaf_pairs)
         CG_CUDA(cudaMalloc(&c->d_leafs, sizeof(cg_leaf_pair) * g.max_leaf_pairs), "alloc leaf-pair output");
+    if (g.max_contacts) {
+        // Hash tables at most half full: contacts (2 keys per colliding pair
+        // at most), vertices with a ray (3 per contact), zero-length groups.
+        auto pow2_at_least = [](uint64_t x) {
+            uint64_t p = 1024;
+            while (p < x) p <<= 1;
+            return uint32_t(p);
+        };
+        auto& t = c->ct;
+        t.table_slots = pow2_at_least(2 * g.max_contacts);
+        t.vslots = pow2_at_least(6 * g.max_contacts);
+        t.zero_cap = uint32_t(g.max_contacts);
+        t.gslots = pow2_at_least(4 * g.max_contacts);
+        t.max_rays = uint32_t(3 * g.max_contacts);
+        CG_CUDA(cudaMalloc(&t.pair_leaf, sizeof(uint32_t) * g.max_tri_pairs), "alloc pair leaf indices");
+        CG_CUDA(cudaMalloc(&t.table, sizeof(ContactSlot) * t.table_slots), "alloc contact table");
+        CG_CUDA(cudaMalloc(&t.occupied, sizeof(uint32_t) * t.table_slots), "alloc contact list");
+        CG_CUDA(cudaMalloc(&t.vkeys, sizeof(unsigned long long) * t.vslots), "alloc vertex set");
+        CG_CUDA(cudaMalloc(&t.vocc, sizeof(uint32_t) * t.vslots), "alloc vertex list");
+        CG_CUDA(cudaMalloc(&t.zero, sizeof(uint32_t) * t.zero_cap), "alloc zero-length list");
+        CG_CUDA(cudaMalloc(&t.gkeys, sizeof(unsigned long long) * t.gslots), "alloc group table");
+        CG_CUDA(cudaMalloc(&t.gflag, sizeof(unsigned int) * t.gslots), "alloc group flags");
+        CG_CUDA(cudaMalloc(&t.gocc, sizeof(uint32_t) * t.gslots), "alloc group list");
+        CG_CUDA(cudaMalloc(&t.contacts, sizeof(cg_contact) * g.max_contacts), "alloc contacts");
+        CG_CUDA(cudaMalloc(&t.rays, sizeof(cg_ray) * t.max_rays), "alloc rays");
+        CG_CUDA(cudaMalloc(&t.sums, sizeof(double) * 8 * g.max_queries), "alloc ray sums");
+        CG_CUDA(cudaMalloc(&t.averages, sizeof(cg_ray_average) * g.max_queries), "alloc ray averages");
+        CG_CUDA(init_contact_tables(t.table, t.table_slots, t.vkeys, t.vslots, t.gkeys, t.gflag, t.gslots, c->stream),
+                "init contact tables");
+        CG_CUDA(cudaStreamSynchronize(c->stream), "init contact tables");
+    }
     CG_CUDA(cudaMallocHost(&c->h_queries, sizeof(cg_query) * g.max_queries), "alloc pinned queries");
     CG_CUDA(cudaMallocHost(&c->h_ctr, sizeof(Counters)), "alloc pinned counters");
     std::memset(c->h_ctr, 0, sizeof(Counters));
@@ -265,6 +339,7 @@ int sync_tree_table(cg_ctx* c) {
         const uint32_t cap = std::max<uint32_t>(64, n * 2);
         CG_CUDA(cudaMalloc(&c->d_trees, sizeof(DevTree) * cap), "alloc tree table");
         c->d_trees_cap = cap;
+        ++c->table_gen;
     }
     std::vector<DevTree> host(n);
     for (uint32_t i = 0; i < n; ++i) {
@@ -319,6 +394,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     np.leaf_cap = p.leaf_cap;
     np.ctr = c->d_ctr;
     np.pairs = c->d_pairs;
+    np.pair_leaf = (flags & CG_CONTACTS) ? c->ct.pair_leaf : nullptr;
     np.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
     np.leafs = c->d_leafs;
     np.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
@@ -331,6 +407,37 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t1, s, rec_flags), "timing event");
     if (n) CG_CUDA(launch_narrow(np, c->narrow_blocks, 8, s), "narrow-phase kernel");
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t2, s, rec_flags), "timing event");
+    if ((flags & CG_CONTACTS) && n) {
+        const auto& t = c->ct;
+        ContactParams cp{};
+        cp.q = c->d_packed;
+        cp.n_queries = n;
+        cp.tris = c->tris.ptr;
+        cp.trees = c->d_trees;
+        cp.pairs = c->d_pairs;
+        cp.pair_leaf = t.pair_leaf;
+        cp.pairs_cap = c->cfg.max_tri_pairs;
+        cp.table = t.table;
+        cp.table_mask = t.table_slots - 1u;
+        cp.occupied = t.occupied;
+        cp.vkeys = t.vkeys;
+        cp.vtable_mask = t.vslots - 1u;
+        cp.vocc = t.vocc;
+        cp.zero = t.zero;
+        cp.zero_cap = t.zero_cap;
+        cp.gkeys = t.gkeys;
+        cp.gflag = t.gflag;
+        cp.gtable_mask = t.gslots - 1u;
+        cp.gocc = t.gocc;
+        cp.max_contacts = uint32_t(c->cfg.max_contacts);
+        cp.contacts = t.contacts;
+        cp.rays = t.rays;
+        cp.max_rays = t.max_rays;
+        cp.sums = t.sums;
+        cp.averages = t.averages;
+        cp.ctr = c->d_ctr;
+        CG_CUDA(launch_contacts(cp, c->narrow_blocks, s), "contact kernels");
+    }
     return CG_OK;
 }
 
@@ -359,9 +466,21 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
     else if ((c->last_flags & CG_KEEP_LEAF_PAIRS) && k.n_leafs > (c->d_leafs ? c->cfg.max_leaf_pairs : 0))
         status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu leaf pairs, capacity %llu", (unsigned long long)k.n_leafs,
                       (unsigned long long)c->cfg.max_leaf_pairs);
+    else if ((c->last_flags & CG_CONTACTS) &&
+             (k.c_overflow || k.n_contacts > c->cfg.max_contacts || k.n_rays > c->ct.max_rays))
+        status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%u contacts, %u rays (max_contacts %llu, flags %u): raise max_contacts",
+                      k.n_contacts, k.n_rays, (unsigned long long)c->cfg.max_contacts, k.c_overflow);
     s.status = status;
     if (st) *st = s;
     return status;
+}
+
+int check_flags(cg_ctx* c, uint32_t flags) {
+    if (!(flags & CG_CONTACTS)) return CG_OK;
+    if (!c->cfg.max_contacts) return fail(c, CG_ERR_INVALID_ARGUMENT, "CG_CONTACTS needs max_contacts > 0");
+    if (flags & (CG_NO_TRI_PAIRS | CG_MID_ONLY))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "CG_CONTACTS needs the colliding pairs (no CG_NO_TRI_PAIRS, CG_MID_ONLY)");
+    return CG_OK;
 }
 
 int join_stream(cg_ctx* c, cudaStream_t s) {
@@ -438,6 +557,8 @@ void cg_config_default(cg_config* cfg) {
     cfg->donate_min = 32;
     cfg->leaf_flush = 32;
     cfg->wait_limit_ms = 2000;
+    cfg->pad = 0;
+    cfg->max_contacts = 1ull << 18;
 }
 
 const char* cg_status_string(int s) {
@@ -665,6 +786,8 @@ int cg_collide_async(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t 
     if (!c || (n && !d_queries)) return CG_ERR_INVALID_ARGUMENT;
     if (n > c->cfg.max_queries)
         return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    int frc = check_flags(c, flags);
+    if (frc != CG_OK) return frc;
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     c->last_flags = flags;
@@ -690,6 +813,8 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
         if (a >= c->trees.size() || !c->trees[a].live || b >= c->trees.size() || !c->trees[b].live)
             return fail(c, CG_ERR_NOT_FOUND, "query %u names tree %u / %u", i, a, b);
     }
+    int frc = check_flags(c, flags);
+    if (frc != CG_OK) return frc;
     cudaSetDevice(c->device);
     if (n) std::memcpy(c->h_queries, queries, sizeof(cg_query) * n);
     c->last_flags = flags;
@@ -752,6 +877,53 @@ int cg_read_leaf_pairs(cg_ctx* c, cg_leaf_pair* out, uint64_t cap, uint64_t* n) 
     return c->h_ctr->n_leafs > avail ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
 }
 
+namespace {
+// Counters of the last launch, which must have been made with CG_CONTACTS.
+int contact_counters(cg_ctx* c) {
+    if (!(c->last_flags & CG_CONTACTS)) return fail(c, CG_ERR_INVALID_ARGUMENT, "the last launch had no CG_CONTACTS");
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "read counters");
+    CG_CUDA(cudaStreamSynchronize(c->stream), "read counters");
+    return CG_OK;
+}
+}  // namespace
+
+int cg_read_contacts(cg_ctx* c, cg_contact* out, uint64_t cap, uint64_t* n) {
+    if (!c || !n || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
+    int rc = contact_counters(c);
+    if (rc != CG_OK) return rc;
+    const uint64_t total = c->h_ctr->n_contacts;
+    const uint64_t avail = std::min<uint64_t>(total, c->cfg.max_contacts);
+    *n = total;
+    const uint64_t m = std::min(avail, cap);
+    if (m) CG_CUDA(cudaMemcpy(out, c->ct.contacts, sizeof(cg_contact) * m, cudaMemcpyDeviceToHost), "read contacts");
+    return (total > avail || (c->h_ctr->c_overflow & CONTACT_TABLE)) ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
+int cg_read_rays(cg_ctx* c, cg_ray* out, uint64_t cap, uint64_t* n) {
+    if (!c || !n || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
+    int rc = contact_counters(c);
+    if (rc != CG_OK) return rc;
+    const uint64_t total = c->h_ctr->n_rays;
+    const uint64_t avail = std::min<uint64_t>(total, c->ct.max_rays);
+    *n = total;
+    const uint64_t m = std::min(avail, cap);
+    if (m) CG_CUDA(cudaMemcpy(out, c->ct.rays, sizeof(cg_ray) * m, cudaMemcpyDeviceToHost), "read rays");
+    return (total > avail || c->h_ctr->c_overflow) ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
+int cg_read_ray_averages(cg_ctx* c, cg_ray_average* out, uint64_t cap, uint64_t* n) {
+    if (!c || !n || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
+    int rc = contact_counters(c);
+    if (rc != CG_OK) return rc;
+    const uint64_t total = c->h_ctr->n_queries;
+    *n = total;
+    const uint64_t m = std::min(total, cap);
+    if (m)
+        CG_CUDA(cudaMemcpy(out, c->ct.averages, sizeof(cg_ray_average) * m, cudaMemcpyDeviceToHost), "read averages");
+    return c->h_ctr->c_overflow ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
 int cg_device_results(cg_ctx* c, const cg_tri_pair** pairs, const unsigned long long** pair_count) {
     if (!c || !pairs || !pair_count) return CG_ERR_INVALID_ARGUMENT;
     *pairs = c->d_pairs;
@@ -790,6 +962,8 @@ int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t 
     if (!c || (n && !d_queries)) return CG_ERR_INVALID_ARGUMENT;
     if (n > c->cfg.max_queries)
         return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > max_queries %u", n, c->cfg.max_queries);
+    int frc = check_flags(c, flags);
+    if (frc != CG_OK) return frc;
     cudaSetDevice(c->device);
     CG_CUDA(cudaStreamSynchronize(c->stream), "sync before capture");
     drop_graph(c);

@@ -61,7 +61,7 @@ constexpr uint32_t kNoItem = 0xffffffffu;
 struct alignas(16) PackedQuery {
     float4 m[4];
     uint32_t item_q, item_split, item_other, pad;
-    uint32_t tri_base_a, tri_base_b, pad2, pad3;
+    uint32_t tri_base_a, tri_base_b, tree_a, tree_b;
 };
 
 struct Counters {
@@ -79,9 +79,64 @@ struct Counters {
     unsigned long long donations;  // node pairs handed to other warps
     unsigned long long warp_steps; // traversal steps (node_pairs / warp_steps = lanes busy per step)
     unsigned long long t_start;    // globaltimer at the first warp's start (trace only)
+    // contacts (CG_CONTACTS)
+    unsigned int n_contacts;  // contact slots taken
+    unsigned int n_vertices;  // vertex-set slots taken
+    unsigned int n_rays;
+    unsigned int n_zero;      // colliding pairs of zero segment length
+    unsigned int c_overflow;  // CONTACT_* bits
+    unsigned int n_groups;    // group-table slots taken
 };
 
+enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ZERO = 8u };
+
 enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
+
+// Contacts and rays (cg_contacts.cu). A contact slot holds one triangle's
+// merged TriangleCandidateRays: the sums are kept in double and rounded to
+// float once, so the order in which threads add changes them by at most the
+// last bit of the double.
+constexpr unsigned long long kEmptyKey = ~0ull;
+
+struct ContactSlot {
+    unsigned long long key;  // side << 63 | query << 32 | tree-local triangle, or kEmptyKey
+    double sx, sy, sz, sw;   // sums of weight * midpoint and of weight
+    unsigned int mask;       // AND of the "vertex not outside" bits
+    unsigned int pad;
+};
+
+struct ContactParams {
+    const PackedQuery* q;
+    uint32_t n_queries;
+    const float4* tris;
+    const DevTree* trees;
+    const cg_tri_pair* pairs;
+    const uint32_t* pair_leaf;  // leaf-list index of each pair
+    unsigned long long pairs_cap;
+    ContactSlot* table;
+    uint32_t table_mask;
+    uint32_t* occupied;         // slots taken this launch
+    unsigned long long* vkeys;  // set of (side, query, vertex index) that already have a ray
+    uint32_t vtable_mask;
+    uint32_t* vocc;
+    uint32_t* zero;             // pairs whose segment has zero length
+    uint32_t zero_cap;
+    unsigned long long* gkeys;  // (side, leaf pair, triangle) groups of those pairs
+    unsigned int* gflag;        // 1 = the group also has a pair of non-zero length
+    uint32_t gtable_mask;
+    uint32_t* gocc;
+    uint32_t max_contacts;
+    cg_contact* contacts;
+    cg_ray* rays;
+    uint32_t max_rays;
+    double* sums;               // per query: 2 sides x (x, y, z, count)
+    cg_ray_average* averages;
+    Counters* ctr;
+};
+
+cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s);
+cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
+                                unsigned long long* gkeys, unsigned int* gflag, uint32_t n_gslots, cudaStream_t s);
 
 // Work queue. A task is a chunk of up to kChunk node pairs: donated slot
 // s >= n_queries holds its chunk at pool[kChunk * (s - n_queries)], and
@@ -113,6 +168,7 @@ struct NarrowParams {
     uint32_t leaf_cap;
     Counters* ctr;
     cg_tri_pair* pairs;
+    uint32_t* pair_leaf;  // leaf-list index of each written pair (contacts) or null
     unsigned long long pairs_cap;
     cg_leaf_pair* leafs;  // the public copy of the leaf pairs (CG_KEEP_LEAF_PAIRS)
     unsigned long long leafs_cap;

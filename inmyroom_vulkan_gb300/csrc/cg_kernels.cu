@@ -627,7 +627,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
         for (uint32_t base = 0; base < total; base += 32) {
             const uint32_t t = base + lane;
             int res = TT_MISS;
-            uint32_t q = 0, ia = 0, ib = 0;
+            uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
             float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
             if (t < total) {
                 int lo = 0, hi = int(nl) - 1;
@@ -644,6 +644,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
                 const uint32_t i = local / cb;
                 const uint32_t j = local - i * cb;
                 q = lq[lo];
+                leaf_i = uint32_t(first) + uint32_t(lo);
                 ia = loa[lo] + i;
                 ib = lob[lo] + j;
                 const Mat4 M = load_mat(P.q + q);
@@ -676,6 +677,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
                         r.target[1] = tgt.y;
                         r.target[2] = tgt.z;
                         P.pairs[o] = r;
+                        if (P.pair_leaf) P.pair_leaf[o] = leaf_i;
                     }
                 }
             }
@@ -709,7 +711,9 @@ __global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees
     p.m[3] = make_float4(Q.relative[12], Q.relative[13], Q.relative[14], Q.relative[15]);
     p.item_q = kNoItem;
     p.item_split = p.item_other = p.pad = 0u;
-    p.tri_base_a = p.tri_base_b = p.pad2 = p.pad3 = 0u;
+    p.tri_base_a = p.tri_base_b = 0u;
+    p.tree_a = Q.tree_a;
+    p.tree_b = Q.tree_b;
     const bool ok = Q.tree_a < n_trees && Q.tree_b < n_trees && trees[Q.tree_a].live && trees[Q.tree_b].live;
     if (!ok) {
         atomicOr(&ctr->error, ERR_BAD_QUERY);

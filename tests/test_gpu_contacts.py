@@ -1,0 +1,179 @@
+"""GPU contacts and uncollide rays (CG_CONTACTS) against the oracle's
+restatement of CreateUncollideRays::ExecuteCreateUncollideRays
+(src/CollisionDetection/CreateUncollideRays.cpp:60-258).
+
+Bit for bit: the set of contact triangles per (query, side), their "vertex
+not outside" masks, the ray counts and every ray that starts at a vertex.
+Within tolerance: weights, weighted averages and the rays that start at a
+weighted average (the GPU sums in double, the CPU in float in its hash-map
+order) and the per-query mean origins. Tolerances: RTOL relative, plus
+RTOL x the largest magnitude of the compared quantity for sums that cancel.
+"""
+import numpy as np
+import pytest
+
+from inmyroom_vulkan_gb300 import capi, scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+RAY_TOL = 1e-4  # rays from a weighted average: relative to the origin scale (origin) and absolute (unit direction)
+
+
+def bits(x):
+    return np.ascontiguousarray(x, np.float32).view(np.uint32)
+
+
+def close(got, want, rtol=RTOL):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    scale = np.abs(want).max() if want.size else 0.0
+    np.testing.assert_allclose(got, want, rtol=rtol, atol=rtol * scale)
+
+
+def match_rays(got, want, n_avg_rays):
+    """got, want: (n, 6) origin + direction. Rays present in both bit for bit
+    are paired first; the remaining ones (at most one per contact that fell
+    back to its weighted average) are paired by nearest neighbour."""
+    assert len(got) == len(want)
+    if not len(want):
+        return
+    g = [tuple(r) for r in bits(got)]
+    w = [tuple(r) for r in bits(want)]
+    from collections import Counter
+
+    cg, cw = Counter(g), Counter(w)
+    exact = sum((cg & cw).values())
+    assert exact >= len(want) - n_avg_rays, (exact, len(want), n_avg_rays)
+    rest_g = np.array([r for r in (cg - cw).elements()], np.uint32).view(np.float32).reshape(-1, 6)
+    rest_w = np.array([r for r in (cw - cg).elements()], np.uint32).view(np.float32).reshape(-1, 6)
+    assert len(rest_g) == len(rest_w)
+    if not len(rest_w):
+        return
+    scale = max(float(np.abs(want[:, :3]).max()), 1e-30)
+    used = np.zeros(len(rest_g), bool)
+    for r in rest_w:
+        d = np.maximum(np.abs(rest_g[:, :3] - r[:3]).max(1) / scale, np.abs(rest_g[:, 3:] - r[3:]).max(1))
+        d[used] = np.inf
+        k = int(np.argmin(d))
+        assert d[k] < RAY_TOL, (r, rest_g[k], d[k])
+        used[k] = True
+
+
+def check_query(port, m, q, contacts, rays, averages):
+    ra, rb, avg = m.rays()
+    for side, want_rays in ((0, ra), (1, rb)):
+        idx, mask, f = m.contacts(side)
+        c = contacts[(contacts["query"] == q) & (contacts["side"] == side)]
+        c = c[np.argsort(c["tri"], kind="stable")]
+        assert np.array_equal(c["tri"], idx), (q, side)
+        assert np.array_equal(c["mask"], mask), (q, side)
+        close(c["weight"], f[:, 3])
+        with np.errstate(invalid="ignore", divide="ignore"):
+            want_avg = (f[:, :3] / f[:, 3:4]).astype(np.float32)
+        close(c["weighted_avg"], want_avg)
+        r = rays[(rays["query"] == q) & (rays["side"] == side)]
+        got_rays = np.concatenate([r["origin"], r["direction"]], 1)
+        match_rays(got_rays, want_rays, int((mask == 0).sum()))
+    a = averages[q]
+    assert a["rays_first"] == len(ra) and a["rays_second"] == len(rb)
+    if len(ra):
+        close(a["first"], avg[:3])
+    if len(rb):
+        close(a["second"], avg[3:])
+
+
+def run_contacts(ctx, port, tp, ids, qa, qb, mats_a, mats_b, flags=capi.CG_CONTACTS):
+    rel = np.stack([port.relative_matrix(a, b) for a, b in zip(mats_a, mats_b)])
+    q = capi.make_queries(np.asarray(ids)[qa], np.asarray(ids)[qb], rel)
+    st = ctx.collide(q, flags=flags)
+    return st, ctx.contacts(), ctx.rays(), ctx.ray_averages()
+
+
+def test_rigid_pair_contacts_and_rays(gpu_ctx, port):
+    rp = scenes.rigid_pair(n_poses=200)
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in (rp.mesh_a, rp.mesh_b)]
+    ids = [gpu_ctx.upload_flat(t.export()) for t in tp]
+    n = len(rp.mats_a)
+    st, contacts, rays, averages = run_contacts(gpu_ctx, port, tp, ids, np.zeros(n, int), np.ones(n, int),
+                                                rp.mats_a, rp.mats_b)
+    assert st["status"] == 0 and len(averages) == n
+    assert len(contacts) > 10000 and len(rays) > 10000
+    hit = 0
+    for k in range(n):
+        m = port.mid_phase(tp[0], tp[1], rp.mats_a[k], rp.mats_b[k])
+        check_query(port, m, k, contacts, rays, averages)
+        hit += int(averages[k]["rays_first"] > 0)
+    assert hit > 50
+    for i in ids:
+        gpu_ctx.free_tree(i)
+
+
+def test_scene_contacts_and_rays_repeatable(gpu_ctx, port):
+    sc = scenes.scene()
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    ids = [gpu_ctx.upload_flat(t.export()) for t in tp]
+    qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+    st, contacts, rays, averages = run_contacts(gpu_ctx, port, tp, ids, qa, qb, sc.mats[qa], sc.mats[qb])
+    assert st["status"] == 0
+    for k in range(len(qa)):
+        m = port.mid_phase(tp[qa[k]], tp[qb[k]], sc.mats[qa[k]], sc.mats[qb[k]])
+        check_query(port, m, k, contacts, rays, averages)
+    # a launch without contacts in between, then the same launch again: the
+    # tables were emptied, the results are the same sets
+    gpu_ctx.collide(capi.make_queries(np.asarray(ids)[qa], np.asarray(ids)[qb],
+                                      np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])))
+    st2, c2, r2, a2 = run_contacts(gpu_ctx, port, tp, ids, qa, qb, sc.mats[qa], sc.mats[qb])
+    assert st2["status"] == 0 and len(c2) == len(contacts) and len(r2) == len(rays)
+    key = lambda c: np.lexsort((c["tri"], c["side"], c["query"]))
+    assert np.array_equal(c2[key(c2)][["query", "side", "tri", "mask"]], contacts[key(contacts)][["query", "side", "tri", "mask"]])
+    assert np.array_equal(a2["rays_first"], averages["rays_first"])
+    for i in ids:
+        gpu_ctx.free_tree(i)
+
+
+def test_zero_length_segment_keeps_its_mask_bits(gpu_ctx, port):
+    """One leaf pair: the second tree's first triangle touches the first's
+    plane in a single point (a colliding pair of zero length), the second
+    crosses it. The touching pair adds no weight, but its plane test still
+    clears a vertex bit of the first triangle, as in the reference."""
+    pa = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    pb = np.array([[0.25, 0.25, 0], [1, 1, 1], [-1, 1, 1], [0.5, -0.5, -1], [0.5, 1.5, -1], [0.25, 0.5, 1]],
+                  np.float32)
+    ta = port.tree_build(pa, np.arange(3, dtype=np.uint32))
+    tb = port.tree_build(pb, np.arange(6, dtype=np.uint32))
+    eye = np.eye(4, dtype=np.float32).reshape(-1)
+    pairs, segs, _, _ = port.collide_pairs([ta], [tb], [eye], [eye])
+    w = np.linalg.norm(segs[:, :3] - segs[:, 3:], axis=1)
+    assert (w == 0).sum() == 1 and (w > 0).sum() == 1
+    fa, fb = ta.export(), tb.export()
+    # the first tree goes up without vertex normals: the face normal is used, as the oracle's build does
+    ida = gpu_ctx.upload_tree(fa.root, fa.node_obbs, fa.node_ref, fa.node_cnt, fa.tri_pos, None, fa.tri_idx)
+    idb = gpu_ctx.upload_flat(fb)
+    st, contacts, rays, averages = run_contacts(gpu_ctx, port, [ta, tb], [ida, idb], [0], [1], [eye], [eye])
+    assert st["status"] == 0
+    m = port.mid_phase(ta, tb, eye, eye)
+    assert m.contacts(0)[1].tolist() == [4]  # bit 0 cleared by the zero-length pair alone
+    check_query(port, m, 0, contacts, rays, averages)
+    gpu_ctx.free_tree(ida)
+    gpu_ctx.free_tree(idb)
+
+
+def test_contacts_flag_combinations_and_overflow(port):
+    sc = scenes.scene()
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes[:64]]
+    keep = (sc.pairs[:, 0] < 64) & (sc.pairs[:, 1] < 64)
+    qa, qb = sc.pairs[keep, 0], sc.pairs[keep, 1]
+    with capi.Context(max_contacts=16) as ctx:
+        ids = [ctx.upload_flat(t.export()) for t in tp]
+        rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
+        q = capi.make_queries(np.asarray(ids)[qa], np.asarray(ids)[qb], rel)
+        for bad in (capi.CG_CONTACTS | capi.CG_MID_ONLY, capi.CG_CONTACTS | capi.CG_NO_TRI_PAIRS):
+            with pytest.raises(capi.CgError) as e:
+                ctx.collide(q, flags=bad)
+            assert e.value.code == -1
+        st = ctx.collide(q, flags=capi.CG_CONTACTS, check=False)
+        assert st["rc"] == -5  # more contacts than max_contacts
+        ctx.reconfigure(max_contacts=1 << 18)
+        st = ctx.collide(q, flags=capi.CG_CONTACTS)
+        assert st["status"] == 0 and len(ctx.contacts()) > 16
