@@ -236,6 +236,46 @@ int cg_read_trace(cg_ctx* ctx, uint32_t bucket_ns, uint32_t* out, uint32_t n_buc
 int cg_graph_capture(cg_ctx* ctx, const cg_query* d_queries, uint32_t n, uint32_t flags);
 int cg_graph_launch(cg_ctx* ctx, void* stream);
 
+/* ---- No-allocation collide step (no reference counterpart) ----
+ *
+ * The collide step of cg_collide_async (same kernels, same colliding pairs)
+ * for callers that must not allocate device memory on the call's path: a
+ * frame loop that is being captured into a CUDA graph in global capture mode
+ * (where cudaMalloc is refused and cudaFree would synchronise the device), or
+ * an engine whose device memory comes from its own fixed budget. The call
+ * makes no cudaMalloc, cudaFree or other allocating call: its per-launch
+ * scratch (counters, work queue, candidate leaf pairs, packed queries) is one
+ * static device array of CG_STATIC_SCRATCH_BYTES inside the library, and the
+ * results go to caller-owned device memory. Trees come from `ctx`
+ * (cg_tree_upload, done beforehand).
+ *
+ * The first call on a device sets the scratch up (looks up its address and
+ * clears the counters and work-queue flags, then waits for that clear): make
+ * it before any stream capture. The scratch is one per device and process,
+ * so calls whose work overlaps on the device (any context, any stream) race:
+ * order them on one stream or wait for one before launching the next.
+ *
+ * Limits: n <= CG_STATIC_MAX_QUERIES (else CG_ERR_INVALID_ARGUMENT, nothing
+ * launched); at most CG_STATIC_MAX_LEAF_PAIRS candidate leaf pairs per call
+ * (else counts->status = CG_ERR_OUTPUT_OVERFLOW). Enqueued on `stream` (NULL =
+ * the context's stream), no host synchronisation: *d_counts (device memory)
+ * is valid once the stream reaches that point. Pairs beyond pairs_cap are
+ * counted, not written. */
+#define CG_STATIC_MAX_QUERIES 1024u
+#define CG_STATIC_MAX_LEAF_PAIRS 131072u
+#define CG_STATIC_SCRATCH_BYTES 10649856u /* about 10.2 MiB */
+
+typedef struct cg_static_counts {
+    uint64_t tri_pairs;  /* colliding triangle pairs found */
+    uint64_t tri_tests;  /* triangle-pair tests */
+    uint64_t leaf_pairs; /* candidate leaf pairs */
+    int32_t status;      /* CG_OK or the CG_ERR_* of the launch */
+    int32_t pad;
+} cg_static_counts;
+
+int cg_collide_static(cg_ctx* ctx, const cg_query* d_queries, uint32_t n, cg_tri_pair* d_pairs, uint64_t pairs_cap,
+                      cg_static_counts* d_counts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

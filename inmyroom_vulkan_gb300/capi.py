@@ -28,7 +28,10 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_last_error", "cg_tree_upload", "cg_tree_free", "cg_relative_matrix", "cg_collide", "cg_collide_async",
            "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results", "cg_read_contacts",
            "cg_read_rays", "cg_read_ray_averages",
-           "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch"]
+           "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch",
+           "cg_collide_static"]
+CG_STATIC_MAX_QUERIES = 1024
+CG_STATIC_MAX_LEAF_PAIRS = 131072
 
 
 class CgError(RuntimeError):
@@ -54,6 +57,11 @@ class cg_tree_view(C.Structure):
                 ("node_ref", C.c_void_p), ("node_tri_count", C.c_void_p), ("triangle_count", C.c_uint32),
                 ("triangles_position", C.c_void_p), ("triangles_normal", C.c_void_p),
                 ("triangles_indices", C.c_void_p)]
+
+
+class cg_static_counts(C.Structure):
+    _fields_ = [("tri_pairs", C.c_uint64), ("tri_tests", C.c_uint64), ("leaf_pairs", C.c_uint64),
+                ("status", C.c_int32), ("pad", C.c_int32)]
 
 
 class cg_stats(C.Structure):
@@ -115,6 +123,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_narrow_time_ms.argtypes = [vp, C.POINTER(C.c_float)]
     lib.cg_graph_capture.argtypes = [vp, vp, u32, u32]
     lib.cg_graph_launch.argtypes = [vp, vp]
+    lib.cg_collide_static.argtypes = [vp, vp, u32, vp, u64, vp, vp]
     _lib = lib
     return lib
 
@@ -292,6 +301,14 @@ class Context:
     def ray_averages(self) -> np.ndarray:
         """Per query: mean ray origins of both sides (RAY_AVERAGE_DTYPE)."""
         return self._read("cg_read_ray_averages", RAY_AVERAGE_DTYPE)
+
+    def collide_static(self, d_queries_ptr: int, n: int, d_pairs_ptr: int, pairs_cap: int, d_counts_ptr: int,
+                       stream: int | None = None):
+        """cg_collide_static: device queries in, pairs and a cg_static_counts
+        written to caller-owned device memory on `stream`; nothing allocated."""
+        rc = self.lib.cg_collide_static(self.h, d_queries_ptr or None, n, d_pairs_ptr or None, pairs_cap,
+                                        d_counts_ptr, stream)
+        self._check(rc, "cg_collide_static")
 
     def device_results(self) -> tuple[int, int]:
         p, n = C.c_void_p(), C.c_void_p()

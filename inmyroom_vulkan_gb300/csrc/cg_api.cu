@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -996,3 +997,127 @@ int cg_graph_launch(cg_ctx* c, void* stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// cg_collide_static: the collide step with its per-launch scratch in one
+// static device array (no allocation on the call's path).
+namespace {
+
+constexpr uint32_t kStaticSlots = 16384;     // work-queue chunk slots (ready flags + pool)
+constexpr uint32_t kStaticMinChunks = 1024;  // donated chunks a launch may always reserve
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kOffReady = align256(sizeof(Counters));
+constexpr size_t kOffPool = kOffReady + align256(sizeof(unsigned int) * kStaticSlots);
+constexpr size_t kOffLeaf = kOffPool + align256(sizeof(uint4) * kChunk * kStaticSlots);
+constexpr size_t kOffPacked = kOffLeaf + align256(sizeof(uint4) * CG_STATIC_MAX_LEAF_PAIRS);
+constexpr size_t kStaticBytes = kOffPacked + align256(sizeof(PackedQuery) * CG_STATIC_MAX_QUERIES);
+static_assert(kStaticBytes == CG_STATIC_SCRATCH_BYTES, "CG_STATIC_SCRATCH_BYTES is the static scratch size");
+
+// Counters | ready flags | node-pair pool | leaf-pair list | packed queries
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+constexpr int kStaticMaxDevices = 64;
+unsigned char* g_static_base[kStaticMaxDevices];  // device address of the scratch, per device once set up
+std::mutex g_static_mu;
+
+// Once per device, with that device current: the scratch's address, and the
+// counters and ready flags (which must start at zero) cleared.
+int static_scratch(cg_ctx* c, cudaStream_t s, unsigned char** out) {
+    if (c->device < 0 || c->device >= kStaticMaxDevices)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "device %d beyond the static scratch table", c->device);
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_base[c->device]) {
+        void* p = nullptr;
+        CG_CUDA(cudaGetSymbolAddress(&p, g_static_scratch), "static scratch address");
+        CG_CUDA(cudaMemsetAsync(p, 0, kOffPool, s), "clear static scratch");
+        CG_CUDA(cudaStreamSynchronize(s), "clear static scratch");
+        g_static_base[c->device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_static_base[c->device];
+    return CG_OK;
+}
+
+__global__ void static_counts_kernel(const Counters* k, uint64_t pairs_cap, cg_static_counts* out) {
+    cg_static_counts r;
+    r.tri_pairs = k->n_pairs;
+    r.tri_tests = k->tri_tests;
+    r.leaf_pairs = k->n_leafs;
+    r.pad = 0;
+    if (k->error & ERR_TIMEOUT)
+        r.status = CG_ERR_TIMEOUT;
+    else if (k->error & ERR_QUEUE)
+        r.status = CG_ERR_QUEUE_OVERFLOW;
+    else if (k->error & ERR_BAD_QUERY)
+        r.status = CG_ERR_INVALID_ARGUMENT;
+    else if (k->n_leafs > CG_STATIC_MAX_LEAF_PAIRS || k->n_pairs > pairs_cap)
+        r.status = CG_ERR_OUTPUT_OVERFLOW;
+    else
+        r.status = CG_OK;
+    *out = r;
+}
+
+}  // namespace
+
+extern "C" int cg_collide_static(cg_ctx* c, const cg_query* d_queries, uint32_t n, cg_tri_pair* d_pairs,
+                                 uint64_t pairs_cap, cg_static_counts* d_counts, void* stream) {
+    if (!c || (n && !d_queries) || (pairs_cap && !d_pairs) || !d_counts) return CG_ERR_INVALID_ARGUMENT;
+    if (n > CG_STATIC_MAX_QUERIES)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "%u queries > CG_STATIC_MAX_QUERIES (%u)", n, CG_STATIC_MAX_QUERIES);
+    CG_CUDA(cudaSetDevice(c->device), "set device");
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    unsigned char* base = nullptr;
+    int rc = static_scratch(c, s, &base);
+    if (rc != CG_OK) return rc;
+    auto* ctr = reinterpret_cast<Counters*>(base);
+    auto* ready = reinterpret_cast<unsigned int*>(base + kOffReady);
+    auto* pool = reinterpret_cast<uint4*>(base + kOffPool);
+    auto* leaf_list = reinterpret_cast<uint4*>(base + kOffLeaf);
+    auto* packed = reinterpret_cast<PackedQuery*>(base + kOffPacked);
+
+    // The traversal grid is the context's, made smaller if its waiting warps
+    // would leave fewer than kStaticMinChunks slots for donations.
+    const uint32_t wpb = c->cfg.warps_per_block;
+    const uint32_t max_blocks = (kStaticSlots - kStaticMinChunks - 64u) / (9u * wpb);
+    const uint32_t blocks = std::min(c->blocks, max_blocks);
+
+    CG_CUDA(launch_init(ctr, ready, kStaticSlots, n, nullptr, s), "init kernel");
+    CG_CUDA(launch_pack(d_queries, n, c->d_trees, uint32_t(c->trees.size()), c->recs.ptr, packed, ctr, leaf_list,
+                        CG_STATIC_MAX_LEAF_PAIRS, s),
+            "pack kernel");
+    TraverseParams p{};
+    p.q = packed;
+    p.n_queries = n;
+    p.recs = c->recs.ptr;
+    p.pool = pool;
+    p.ready = ready;
+    p.slot_cap = kStaticSlots - 9u * blocks * wpb - 64u;
+    p.slot_alloc = kStaticSlots;
+    p.ctr = ctr;
+    p.leaf_list = leaf_list;
+    p.leaf_cap = CG_STATIC_MAX_LEAF_PAIRS;
+    p.trace = nullptr;
+    p.trace_ns = 1000u;
+    p.stack_cap = c->cfg.stack_entries;
+    p.donate_min = std::min(std::max(c->cfg.donate_min, 2u), c->cfg.stack_entries - 63u);
+    p.leaf_flush = c->cfg.leaf_flush;
+    p.wait_ns = (unsigned long long)c->cfg.wait_limit_ms * 1000000ull;
+    NarrowParams np{};
+    np.q = packed;
+    np.tris = c->tris.ptr;
+    np.leaf_list = leaf_list;
+    np.leaf_cap = CG_STATIC_MAX_LEAF_PAIRS;
+    np.ctr = ctr;
+    np.pairs = d_pairs;
+    np.pair_leaf = nullptr;
+    np.pairs_cap = d_pairs ? pairs_cap : 0;
+    np.leafs = nullptr;
+    np.leafs_cap = 0;
+    np.flags = 0;
+    np.trace = nullptr;
+    np.trace_ns = 1000u;
+    if (n) CG_CUDA(launch_traverse(p, blocks, wpb, s), "traversal kernel");
+    if (n) CG_CUDA(launch_narrow(np, c->narrow_blocks, 8, s), "narrow-phase kernel");
+    static_counts_kernel<<<1, 1, 0, s>>>(ctr, np.pairs_cap, d_counts);
+    CG_CUDA(cudaGetLastError(), "counts kernel");
+    return CG_OK;
+}
