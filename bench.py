@@ -1,10 +1,12 @@
 """Benchmark of the GB300 collision path on the 256-entity scene.
 
 One step = one batched collide launch (CUDA graph: counter reset, query
-packing, persistent traversal with the fused triangle-pair narrow phase) over
-every entity pair of the scene whose world AABBs overlap. The metric is
-triangle-pair tests per second (Moller calls on candidate leaf pairs), with
-collision queries per second beside it.
+packing, persistent traversal, persistent triangle-pair narrow phase, then
+per-triangle contacts, uncollide rays and their mean origins) over every
+entity pair of the scene whose world AABBs overlap, the work the reference's
+mid phase + CreateUncollideRays does per pair. The metric is triangle-pair
+tests per second (Moller calls on candidate leaf pairs), with collision
+queries per second beside it.
 
   python bench.py [--gpus N --steps K --warmup W]      # GPU arm
   python bench.py --impl reference [...]                # the reference's CPU path
@@ -12,7 +14,8 @@ collision queries per second beside it.
 value: device-resident inputs, each step timed with CUDA events on the
 launching stream, L2 flushed (a 512 MB write) between steps.
 e2e: the public host API (cg_collide with host queries + read-back of the
-colliding pairs), host-timed around the synchronous calls.
+colliding pairs, the rays and the per-query mean origins into pinned memory),
+host-timed around the synchronous calls.
 roofline: the traversal kernel (the dominant one), algorithmic bytes (node
 pairs x 96 B of box data) per launch over its event-timed duration, against the
 measured copy bandwidth, with the FP32 view beside it; roofline_narrow: the
@@ -43,6 +46,7 @@ NODE_PAIR_BYTES = 2 * 48   # two boxes
 TRI_TEST_BYTES = 2 * 36    # two triangles
 NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
 TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
+COUNTERS_BYTES = 112       # the launch counters, read back by cg_collide and by each result read
 
 
 def measured_peaks() -> dict:
@@ -195,7 +199,8 @@ def run_gpu(args) -> dict:
 
     d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
     torch.cuda.synchronize()
-    ctx.graph_capture(d_q.data_ptr(), n)
+    flags = capi.CG_CONTACTS
+    ctx.graph_capture(d_q.data_ptr(), n, flags)
     # a dedicated stream: its handle is never 0, which the C ABI reads as
     # "the context's own stream"
     stream = torch.cuda.Stream(dev)
@@ -206,7 +211,7 @@ def run_gpu(args) -> dict:
     for _ in range(max(args.warmup, 3)):
         ctx.graph_launch(stream.cuda_stream)
     st = ctx.sync_stats()
-    tests_per_step, pairs_per_step = st["tri_tests"], st["tri_pairs"]
+    tests_per_step, pairs_per_step, rays_per_step = st["tri_tests"], st["tri_pairs"], st["rays"]
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -225,22 +230,28 @@ def run_gpu(args) -> dict:
         torch.cuda.synchronize()
         step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
         st = ctx.sync_stats()
-        assert st["tri_tests"] == tests_per_step and st["status"] == 0
+        assert st["tri_tests"] == tests_per_step and st["status"] == 0 and st["rays"] == rays_per_step
 
-        # end to end through the public host API: host queries in, pairs out
-        # results land in pinned host memory (one device-to-host copy)
-        out_pinned = torch.empty(pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
-        out_view = out_pinned.numpy().view(capi.TRI_PAIR_DTYPE)
-        ctx.collide(q)  # captures cg_collide's step graph outside the timed region
+        # end to end through the public host API: host queries in; pairs, rays
+        # and mean origins out, into pinned host memory (one copy each)
+        def pinned(count, dtype):
+            return torch.empty(count * dtype.itemsize, dtype=torch.uint8).pin_memory().numpy().view(dtype)
+
+        out_pairs = pinned(pairs_per_step, capi.TRI_PAIR_DTYPE)
+        out_rays = pinned(rays_per_step, capi.RAY_DTYPE)
+        out_avg = pinned(n, capi.RAY_AVERAGE_DTYPE)
+        ctx.collide(q, flags=flags)  # captures cg_collide's step graph outside the timed region
         e2e_times = []
         for k in range(args.steps):
             flush.fill_(k & 0xff)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            st_e = ctx.collide(q)
-            pairs = ctx.tri_pairs(out=out_view, count=st_e["tri_pairs"])
+            st_e = ctx.collide(q, flags=flags)
+            pairs = ctx.tri_pairs(out=out_pairs, count=st_e["tri_pairs"])
+            rays = ctx.rays(out=out_rays, count=st_e["rays"])
+            avgs = ctx.ray_averages(out=out_avg, count=n)
             e2e_times.append(time.perf_counter() - t0)
-        assert len(pairs) == pairs_per_step
+        assert len(pairs) == pairs_per_step and len(rays) == rays_per_step and len(avgs) == n
     total_ms = float(np.sum(step_ms))
     if dist:
         t = torch.tensor([total_ms], device=dev)
@@ -280,17 +291,17 @@ def run_gpu(args) -> dict:
     d_pq = torch.from_numpy(pq.view(np.uint8).copy()).to(dev)
     qsz = capi.QUERY_DTYPE.itemsize
     for i in range(5):
-        ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, 0, stream.cuda_stream)
+        ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, flags, stream.cuda_stream)
     torch.cuda.synchronize()
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s0.record(stream)
     ptests = 0
     for i in range(200):
-        ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, 0, stream.cuda_stream)
+        ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, flags, stream.cuda_stream)
     s1.record(stream)
     torch.cuda.synchronize()
     plain_ms = s0.elapsed_time(s1)
-    ctx.collide(pq)
+    ctx.collide(pq, flags=flags)
     ptests = ctx.sync_stats()["tri_tests"]
 
     cpu = cpu_baseline(sc, seconds=args.cpu_seconds) if rank == 0 and args.cpu_seconds > 0 else None
@@ -302,19 +313,23 @@ def run_gpu(args) -> dict:
         "data": "synthetic (seeded PCG64, seed 1002 + 1000*rank)",
         "config": {"workload": WORKLOAD, "queries_per_step": n, "triangles": int(sum(m.n_tris for m in sc.meshes)),
                    "tri_tests_per_step": int(tests_per_step), "colliding_pairs_per_step": int(pairs_per_step),
+                   "contacts_per_step": int(st["contacts"]), "rays_per_step": int(rays_per_step),
                    "node_pairs_per_step": int(st["node_pairs"]), "cache": "L2 flushed (512 MB write) between steps",
-                   "launch": "CUDA graph: init + pack + persistent traversal + persistent narrow phase",
+                   "launch": "CUDA graph: init + pack + persistent traversal + persistent narrow phase + "
+                             "5 contact/ray kernels",
                    "lanes_per_step": st["node_pairs"] / max(1, st["warp_steps"])},
         "queries_per_s": world * n * args.steps / (total_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * capi.QUERY_DTYPE.itemsize),
-                "d2h_bytes_per_step": int(64 + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize),
+                "d2h_bytes_per_step": int(4 * COUNTERS_BYTES + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize
+                                          + rays_per_step * capi.RAY_DTYPE.itemsize
+                                          + n * capi.RAY_AVERAGE_DTYPE.itemsize),
                 "ms_per_step": 1e3 * e2e_s / args.steps, "timing": "host perf_counter around synchronous calls"},
         "roofline": roof_trav,
         "roofline_narrow": roof_narrow,
-        "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch",
+        "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch (with contacts and rays)",
                   "queries_per_s": 200 / (plain_ms / 1e3), "tri_tests_per_s": ptests / (plain_ms / 1e3),
                   "ms_per_query": plain_ms / 200},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 9 * args.steps,
         "clocks": clk,
     }
     if cpu:

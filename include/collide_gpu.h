@@ -100,7 +100,7 @@ typedef struct cg_tree_view {
     const uint32_t* node_tri_count;   /* [node_count][2] triangle count, 0 = inner child */
     uint32_t triangle_count;
     const float* triangles_position;  /* [triangle_count][3][3] */
-    const float* triangles_normal;    /* [triangle_count][3][3], may be NULL (rays then unavailable) */
+    const float* triangles_normal;    /* [triangle_count][3][3], may be NULL (rays then use the face normal) */
     const uint32_t* triangles_indices;/* [triangle_count][3] vertex indices, may be NULL */
 } cg_tree_view;
 
@@ -154,6 +154,8 @@ typedef struct cg_stats {
     uint64_t fragile;     /* pairs whose second interval degenerated (see docs) */
     uint64_t donations;   /* node pairs handed from busy to waiting warps */
     uint64_t warp_steps;  /* traversal steps; node_pairs / warp_steps = busy lanes per step */
+    uint64_t contacts;    /* triangles with contacts (CG_CONTACTS) */
+    uint64_t rays;        /* uncollide rays (CG_CONTACTS) */
     int32_t status;       /* CG_OK or the error the launch raised */
     int32_t pad;
 } cg_stats;

@@ -67,7 +67,7 @@ class cg_static_counts(C.Structure):
 class cg_stats(C.Structure):
     _fields_ = [("node_pairs", C.c_uint64), ("leaf_pairs", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("tri_pairs", C.c_uint64), ("fragile", C.c_uint64), ("donations", C.c_uint64), ("warp_steps", C.c_uint64),
-                ("status", C.c_int32), ("pad", C.c_int32)]
+                ("contacts", C.c_uint64), ("rays", C.c_uint64), ("status", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
@@ -282,25 +282,28 @@ class Context:
         self._check(rc, "cg_read_leaf_pairs")
         return out
 
-    def _read(self, fn, dtype) -> np.ndarray:
+    def _read(self, fn, dtype, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
         n = C.c_uint64()
-        self._check(getattr(self.lib, fn)(self.h, None, 0, C.byref(n)), fn)
-        out = np.zeros(n.value, dtype)
-        rc = getattr(self.lib, fn)(self.h, out.ctypes.data if n.value else None, n.value, C.byref(n))
+        if count is None:
+            self._check(getattr(self.lib, fn)(self.h, None, 0, C.byref(n)), fn)
+            count = n.value
+        if out is None or len(out) < count:
+            out = np.zeros(count, dtype)
+        rc = getattr(self.lib, fn)(self.h, out.ctypes.data if count else None, count, C.byref(n))
         self._check(rc, fn)
-        return out
+        return out[:n.value]
 
-    def contacts(self) -> np.ndarray:
+    def contacts(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
         """Per-triangle contacts of the last CG_CONTACTS launch (CONTACT_DTYPE, unordered)."""
-        return self._read("cg_read_contacts", CONTACT_DTYPE)
+        return self._read("cg_read_contacts", CONTACT_DTYPE, out, count)
 
-    def rays(self) -> np.ndarray:
+    def rays(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
         """Uncollide rays of the last CG_CONTACTS launch (RAY_DTYPE, unordered)."""
-        return self._read("cg_read_rays", RAY_DTYPE)
+        return self._read("cg_read_rays", RAY_DTYPE, out, count)
 
-    def ray_averages(self) -> np.ndarray:
+    def ray_averages(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
         """Per query: mean ray origins of both sides (RAY_AVERAGE_DTYPE)."""
-        return self._read("cg_read_ray_averages", RAY_AVERAGE_DTYPE)
+        return self._read("cg_read_ray_averages", RAY_AVERAGE_DTYPE, out, count)
 
     def collide_static(self, d_queries_ptr: int, n: int, d_pairs_ptr: int, pairs_cap: int, d_counts_ptr: int,
                        stream: int | None = None):

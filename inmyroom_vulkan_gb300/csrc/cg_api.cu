@@ -138,12 +138,6 @@ struct cg_ctx {
         unsigned long long* vkeys = nullptr;
         uint32_t vslots = 0;
         uint32_t* vocc = nullptr;
-        uint32_t* zero = nullptr;
-        uint32_t zero_cap = 0;
-        unsigned long long* gkeys = nullptr;
-        unsigned int* gflag = nullptr;
-        uint32_t gslots = 0;
-        uint32_t* gocc = nullptr;
         cg_contact* contacts = nullptr;
         cg_ray* rays = nullptr;
         uint32_t max_rays = 0;
@@ -217,10 +211,6 @@ void free_buffers(cg_ctx* c) {
     cudaFree(t.occupied);
     cudaFree(t.vkeys);
     cudaFree(t.vocc);
-    cudaFree(t.zero);
-    cudaFree(t.gkeys);
-    cudaFree(t.gflag);
-    cudaFree(t.gocc);
     cudaFree(t.contacts);
     cudaFree(t.rays);
     cudaFree(t.sums);
@@ -296,8 +286,8 @@ int alloc_buffers(cg_ctx* c) {
     if (g.max_leaf_pairs)
         CG_CUDA(cudaMalloc(&c->d_leafs, sizeof(cg_leaf_pair) * g.max_leaf_pairs), "alloc leaf-pair output");
     if (g.max_contacts) {
-        // Hash tables at most half full: contacts (2 keys per colliding pair
-        // at most), vertices with a ray (3 per contact), zero-length groups.
+        // Hash tables at most half full: contacts, vertices with a ray (3 per
+        // contact at most).
         auto pow2_at_least = [](uint64_t x) {
             uint64_t p = 1024;
             while (p < x) p <<= 1;
@@ -306,24 +296,17 @@ int alloc_buffers(cg_ctx* c) {
         auto& t = c->ct;
         t.table_slots = pow2_at_least(2 * g.max_contacts);
         t.vslots = pow2_at_least(6 * g.max_contacts);
-        t.zero_cap = uint32_t(g.max_contacts);
-        t.gslots = pow2_at_least(4 * g.max_contacts);
         t.max_rays = uint32_t(3 * g.max_contacts);
         CG_CUDA(cudaMalloc(&t.pair_leaf, sizeof(uint32_t) * g.max_tri_pairs), "alloc pair leaf indices");
         CG_CUDA(cudaMalloc(&t.table, sizeof(ContactSlot) * t.table_slots), "alloc contact table");
         CG_CUDA(cudaMalloc(&t.occupied, sizeof(uint32_t) * t.table_slots), "alloc contact list");
         CG_CUDA(cudaMalloc(&t.vkeys, sizeof(unsigned long long) * t.vslots), "alloc vertex set");
         CG_CUDA(cudaMalloc(&t.vocc, sizeof(uint32_t) * t.vslots), "alloc vertex list");
-        CG_CUDA(cudaMalloc(&t.zero, sizeof(uint32_t) * t.zero_cap), "alloc zero-length list");
-        CG_CUDA(cudaMalloc(&t.gkeys, sizeof(unsigned long long) * t.gslots), "alloc group table");
-        CG_CUDA(cudaMalloc(&t.gflag, sizeof(unsigned int) * t.gslots), "alloc group flags");
-        CG_CUDA(cudaMalloc(&t.gocc, sizeof(uint32_t) * t.gslots), "alloc group list");
         CG_CUDA(cudaMalloc(&t.contacts, sizeof(cg_contact) * g.max_contacts), "alloc contacts");
         CG_CUDA(cudaMalloc(&t.rays, sizeof(cg_ray) * t.max_rays), "alloc rays");
         CG_CUDA(cudaMalloc(&t.sums, sizeof(double) * 8 * g.max_queries), "alloc ray sums");
         CG_CUDA(cudaMalloc(&t.averages, sizeof(cg_ray_average) * g.max_queries), "alloc ray averages");
-        CG_CUDA(init_contact_tables(t.table, t.table_slots, t.vkeys, t.vslots, t.gkeys, t.gflag, t.gslots, c->stream),
-                "init contact tables");
+        CG_CUDA(init_contact_tables(t.table, t.table_slots, t.vkeys, t.vslots, c->stream), "init contact tables");
         CG_CUDA(cudaStreamSynchronize(c->stream), "init contact tables");
     }
     CG_CUDA(cudaMallocHost(&c->h_queries, sizeof(cg_query) * g.max_queries), "alloc pinned queries");
@@ -417,6 +400,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.trees = c->d_trees;
         cp.pairs = c->d_pairs;
         cp.pair_leaf = t.pair_leaf;
+        cp.leaf_list = c->d_leaf_list;
         cp.pairs_cap = c->cfg.max_tri_pairs;
         cp.table = t.table;
         cp.table_mask = t.table_slots - 1u;
@@ -424,12 +408,6 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.vkeys = t.vkeys;
         cp.vtable_mask = t.vslots - 1u;
         cp.vocc = t.vocc;
-        cp.zero = t.zero;
-        cp.zero_cap = t.zero_cap;
-        cp.gkeys = t.gkeys;
-        cp.gflag = t.gflag;
-        cp.gtable_mask = t.gslots - 1u;
-        cp.gocc = t.gocc;
         cp.max_contacts = uint32_t(c->cfg.max_contacts);
         cp.contacts = t.contacts;
         cp.rays = t.rays;
@@ -451,6 +429,8 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
     s.fragile = k.fragile;
     s.donations = k.donations;
     s.warp_steps = k.warp_steps;
+    s.contacts = k.n_contacts;
+    s.rays = k.n_rays;
     int status = CG_OK;
     if (k.error & ERR_TIMEOUT)
         status = fail(c, CG_ERR_TIMEOUT, "a device-side wait exceeded %u ms", c->cfg.wait_limit_ms);

@@ -8,26 +8,23 @@
 // of non-zero weight into a per-triangle map. Here every colliding pair adds
 // directly into a hash table keyed by (side, query, triangle). A pair whose
 // segment has zero length adds no weight and no midpoint, so it only matters
-// for its "not outside" bits, and only when its leaf pair gave the same
-// triangle some weight; such pairs are rare and take a side path:
+// for its "not outside" bits, and only when its leaf pair gives the same
+// triangle some weight: such a pair (rare) re-runs the triangle tests of its
+// leaf pair for that triangle (at most a leaf's four triangles) to find out.
 //
-//   contacts_accumulate  pairs of non-zero length: planes (Plane.cpp:5-28),
-//                        weight, weighted midpoint, vertex bits -> table;
-//                        pairs of zero length: listed, and their (side, leaf
-//                        pair, triangle) groups entered into a group table
-//   contacts_mark        (only when some pair had zero length) pairs of
-//                        non-zero length flag their groups in that table
-//   contacts_apply       zero-length pairs of flagged groups AND their vertex
-//                        bits into the triangle's contact
+//   contacts_accumulate  one thread per colliding pair: planes (Plane.cpp:
+//                        5-28), weight, weighted midpoint, vertex bits ->
+//                        table; also empties the vertex set of the previous
+//                        contacts launch and the per-query origin sums
 //   contacts_emit        one thread per contact: the cg_contact record and its
 //                        rays (find_rays_lambda, CreateUncollideRays.cpp:
 //                        131-178), vertex rays deduplicated per (side, query,
-//                        vertex index) through a set; the slot is emptied
-//   ray_averages         per query: the mean ray origins
-//                        (CreateUncollideRays.cpp:240-258); the vertex set and
-//                        group table are emptied
+//                        vertex index) through a set; the slot is emptied.
+//                        The last block to finish computes the per-query mean
+//                        origins (CreateUncollideRays.cpp:240-258).
 //
-// Geometry uses the reference's arithmetic (no contraction, IEEE division and
+// Appends to the shared lists (contacts, vertices, rays) take one atomic per
+// warp. Geometry uses the reference's arithmetic (no contraction, IEEE division and
 // square root), so masks, weights of single pairs and ray directions are the
 // CPU's bits. Sums are kept in double: the weighted averages and mean origins
 // agree with the CPU's float sums to float rounding, not bit for bit (the
@@ -146,9 +143,34 @@ __device__ __forceinline__ void tri_at(const float4* tris, uint32_t i, float3 p[
     }
 }
 
-// (side, query or leaf pair, index) in one word; queries and leaf pairs are < 2^31.
+// (side, query, index) in one word; queries are < 2^31.
 __device__ __forceinline__ unsigned long long make_key(uint32_t side, uint32_t hi, uint32_t lo) {
     return ((unsigned long long)side << 63) | ((unsigned long long)hi << 32) | lo;
+}
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lanes_below() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// One atomic per warp: lane l gets base + (number of its lanes below l that
+// take a slot) when `take` is set. All 32 lanes must call it together.
+__device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned take) {
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned incl = take;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= unsigned(o)) incl += t;
+    }
+    const unsigned total = __shfl_sync(kFullMask, incl, 31);
+    unsigned base = 0;
+    if (lane == 31 && total) base = atomicAdd(counter, total);
+    base = __shfl_sync(kFullMask, base, 31);
+    return base + incl - take;
 }
 
 // Everything the contact step needs of one colliding pair.
@@ -162,7 +184,7 @@ struct PairGeom {
 // CreateUncollideRays.cpp:148-172 for pair i: the second triangle is moved
 // into the first tree's space, each triangle's vertices are tested against
 // the other's plane, w = |source - target| and mid = w * (source + target) / 2.
-__device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i, bool need_masks) {
+__device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i) {
     const cg_tri_pair r = P.pairs[i];
     PairGeom g;
     g.q = r.query;
@@ -173,8 +195,6 @@ __device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i, bool
     const float3 t = make_float3(r.target[0], r.target[1], r.target[2]);
     g.w = length3(sub3(s, t));
     g.mid = divs3(scale3(g.w, add3(s, t)), 2.0f);
-    g.mask_a = g.mask_b = 7u;
-    if (!need_masks) return g;
     const PackedQuery* Q = P.q + r.query;
     const Mat4 M = query_mat(Q);
     float3 pa[3], pb[3];
@@ -185,6 +205,7 @@ __device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i, bool
     for (int k = 0; k < 3; ++k) pb[k] = xform(M, pb[k], 1.0f);
     const Plane plane_a = plane_of(pa[0], pa[1], pa[2]);
     const Plane plane_b = plane_of(pb[0], pb[1], pb[2]);
+    g.mask_a = g.mask_b = 7u;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         if (outside(plane_b, pa[k])) g.mask_a &= ~(1u << k);
@@ -193,9 +214,35 @@ __device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i, bool
     return g;
 }
 
+// True when the leaf pair of a zero-length pair gives its triangle on `side`
+// some weight: the triangle tests of that triangle against the other leaf's
+// triangles (the narrow phase's own tests, re-run) have a colliding pair of
+// non-zero length.
+__device__ bool group_has_weight(const ContactParams& P, const PairGeom& g, uint32_t side) {
+    const uint4 lp = P.leaf_list[g.leaf];  // (query, first triangle a, first triangle b, counts)
+    const PackedQuery* Q = P.q + g.q;
+    const Mat4 M = query_mat(Q);
+    const uint32_t cnt_a = lp.w & 0xffffu, cnt_b = lp.w >> 16;
+    const uint32_t n = side ? cnt_a : cnt_b;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t ia = side ? lp.y + k : __ldg(&Q->tri_base_a) + g.tri_a;
+        const uint32_t ib = side ? __ldg(&Q->tri_base_b) + g.tri_b : lp.z + k;
+        float3 a[3], b[3];
+        uint32_t vi[3];
+        tri_at(P.tris, ia, a, vi);
+        tri_at(P.tris, ib, b, vi);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) b[j] = xform(M, b[j], 1.0f);
+        float3 src, tgt;
+        if (tri_tri(a[0], a[1], a[2], b[0], b[1], b[2], src, tgt) == TT_HIT && length3(sub3(src, tgt)) != 0.0f)
+            return true;
+    }
+    return false;
+}
+
 // Hash sets with open addressing and linear probing over 64-bit keys stored
-// `stride` words apart. No key is removed while a table is in use: each
-// launch empties the slots it took once it is done with them.
+// `stride` words apart. No key is removed while a set is in use: each launch
+// empties the slots it took once it is done with them.
 __device__ int table_insert(unsigned long long* keys, uint32_t stride, uint32_t mask, unsigned long long key,
                             uint32_t* slot_out) {
     uint32_t slot = hash64(key) & mask;
@@ -212,70 +259,23 @@ __device__ int table_insert(unsigned long long* keys, uint32_t stride, uint32_t 
     return -1;  // full
 }
 
-__device__ bool table_find(const unsigned long long* keys, uint32_t stride, uint32_t mask, unsigned long long key,
-                           uint32_t* slot_out) {
-    uint32_t slot = hash64(key) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        const unsigned long long cur = keys[size_t(stride) * slot];
-        if (cur == key) {
-            *slot_out = slot;
-            return true;
-        }
-        if (cur == kEmptyKey) return false;
-        slot = (slot + 1u) & mask;
-    }
-    return false;
-}
-
 constexpr uint32_t kSlotWords = sizeof(ContactSlot) / sizeof(unsigned long long);
 static_assert(sizeof(ContactSlot) % sizeof(unsigned long long) == 0, "contact slots hold whole key words");
 
-__device__ void add_contact(const ContactParams& P, unsigned long long key, float3 mid, float w, unsigned mask) {
-    uint32_t slot = 0;
-    const int r = table_insert(&P.table->key, kSlotWords, P.table_mask, key, &slot);
-    if (r < 0) {
-        atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
-        return;
-    }
-    if (r == 1) P.occupied[atomicAdd(&P.ctr->n_contacts, 1u)] = slot;  // once per slot: fits the list
+// Inserts (or finds) the contact of `key`; -1 when the table is full.
+__device__ int contact_slot(const ContactParams& P, unsigned long long key, uint32_t* slot) {
+    const int r = table_insert(&P.table->key, kSlotWords, P.table_mask, key, slot);
+    if (r < 0) atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
+    return r;
+}
+
+__device__ __forceinline__ void add_to_slot(const ContactParams& P, uint32_t slot, float3 mid, float w, unsigned mask) {
     ContactSlot* s = P.table + slot;
     atomicAdd(&s->sx, double(mid.x));
     atomicAdd(&s->sy, double(mid.y));
     atomicAdd(&s->sz, double(mid.z));
     atomicAdd(&s->sw, double(w));
     if (mask != 7u) atomicAnd(&s->mask, mask);
-}
-
-__device__ void group_insert(const ContactParams& P, unsigned long long key) {
-    uint32_t slot = 0;
-    const int r = table_insert(P.gkeys, 1u, P.gtable_mask, key, &slot);
-    if (r < 0)
-        atomicOr(&P.ctr->c_overflow, CONTACT_ZERO);
-    else if (r == 1)
-        P.gocc[atomicAdd(&P.ctr->n_groups, 1u)] = slot;
-}
-
-__device__ void emit_ray(const ContactParams& P, uint32_t q, uint32_t side, float3 o, float3 d) {
-    const unsigned idx = atomicAdd(&P.ctr->n_rays, 1u);
-    if (idx < P.max_rays) {
-        cg_ray r;
-        r.query = q;
-        r.side = side;
-        r.origin[0] = o.x;
-        r.origin[1] = o.y;
-        r.origin[2] = o.z;
-        r.direction[0] = d.x;
-        r.direction[1] = d.y;
-        r.direction[2] = d.z;
-        P.rays[idx] = r;
-    } else {
-        atomicOr(&P.ctr->c_overflow, CONTACT_RAYS);
-    }
-    double* s = P.sums + 8ull * q + 4ull * side;
-    atomicAdd(s + 0, double(o.x));
-    atomicAdd(s + 1, double(o.y));
-    atomicAdd(s + 2, double(o.z));
-    atomicAdd(s + 3, 1.0);
 }
 
 __device__ __forceinline__ unsigned long long n_written_pairs(const ContactParams& P) {
@@ -285,167 +285,209 @@ __device__ __forceinline__ unsigned long long n_written_pairs(const ContactParam
 
 }  // namespace
 
-__global__ void contacts_accumulate_kernel(const ContactParams P) {
+__global__ void __launch_bounds__(256) contacts_accumulate_kernel(const ContactParams P) {
     const unsigned long long tid = blockIdx.x * 1ull * blockDim.x + threadIdx.x;
     const unsigned long long stride = 1ull * gridDim.x * blockDim.x;
+    // vertex set of the previous contacts launch, and this launch's origin sums
+    const uint32_t nv = P.ctr->prev_vertices;
+    for (unsigned long long j = tid; j < nv; j += stride) P.vkeys[P.vocc[j]] = kEmptyKey;
     for (unsigned long long j = tid; j < 8ull * P.n_queries; j += stride) P.sums[j] = 0.0;
+
     const unsigned long long n = n_written_pairs(P);
-    for (unsigned long long i = tid; i < n; i += stride) {
-        const PairGeom g = pair_geom(P, i, true);
-        if (g.w != 0.0f) {
-            add_contact(P, make_key(0u, g.q, g.tri_a), g.mid, g.w, g.mask_a);
-            add_contact(P, make_key(1u, g.q, g.tri_b), g.mid, g.w, g.mask_b);
-        } else {
-            const unsigned z = atomicAdd(&P.ctr->n_zero, 1u);
-            if (z < P.zero_cap) {
-                P.zero[z] = uint32_t(i);
-                group_insert(P, make_key(0u, g.leaf, g.tri_a));
-                group_insert(P, make_key(1u, g.leaf, g.tri_b));
+    const unsigned long long warp0 = tid & ~31ull;  // warp-uniform loop: warp_append needs all lanes
+    for (unsigned long long base = warp0; base < n; base += stride) {
+        const unsigned long long i = base + (threadIdx.x & 31u);
+        int ra = -2, rb = -2;  // -2: no slot wanted, else contact_slot's result
+        uint32_t sa = 0, sb = 0;
+        if (i < n) {
+            const PairGeom g = pair_geom(P, i);
+            if (g.w != 0.0f) {
+                ra = contact_slot(P, make_key(0u, g.q, g.tri_a), &sa);
+                if (ra >= 0) add_to_slot(P, sa, g.mid, g.w, g.mask_a);
+                rb = contact_slot(P, make_key(1u, g.q, g.tri_b), &sb);
+                if (rb >= 0) add_to_slot(P, sb, g.mid, g.w, g.mask_b);
             } else {
-                atomicOr(&P.ctr->c_overflow, CONTACT_ZERO);
+                // no weight: only the vertex bits count, and only in a leaf pair
+                // that gives the triangle weight (then its contact exists anyway)
+                if (group_has_weight(P, g, 0u)) {
+                    ra = contact_slot(P, make_key(0u, g.q, g.tri_a), &sa);
+                    if (ra >= 0) atomicAnd(&P.table[sa].mask, g.mask_a);
+                }
+                if (group_has_weight(P, g, 1u)) {
+                    rb = contact_slot(P, make_key(1u, g.q, g.tri_b), &sb);
+                    if (rb >= 0) atomicAnd(&P.table[sb].mask, g.mask_b);
+                }
             }
         }
+        __syncwarp();
+        const unsigned new_a = ra == 1, new_b = rb == 1;
+        const unsigned o = warp_append(&P.ctr->n_contacts, new_a + new_b);
+        if (new_a) P.occupied[o] = sa;  // one entry per slot: the list never outgrows the table
+        if (new_b) P.occupied[o + new_a] = sb;
     }
 }
 
-__global__ void contacts_mark_kernel(const ContactParams P) {
-    if (P.ctr->n_zero == 0u) return;
-    const unsigned long long n = n_written_pairs(P);
-    for (unsigned long long i = blockIdx.x * 1ull * blockDim.x + threadIdx.x; i < n;
-         i += 1ull * gridDim.x * blockDim.x) {
-        const PairGeom g = pair_geom(P, i, false);
-        if (g.w == 0.0f) continue;
-        uint32_t slot = 0;
-        if (table_find(P.gkeys, 1u, P.gtable_mask, make_key(0u, g.leaf, g.tri_a), &slot)) P.gflag[slot] = 1u;
-        if (table_find(P.gkeys, 1u, P.gtable_mask, make_key(1u, g.leaf, g.tri_b), &slot)) P.gflag[slot] = 1u;
-    }
-}
+// Rays of one contact, made in registers before they are appended.
+struct LaneRays {
+    float3 o[3], d[3];
+    uint32_t vs[3];  // vertex-set slots taken for them
+    unsigned n, nv;
+};
 
-__global__ void contacts_apply_kernel(const ContactParams P) {
-    const uint32_t nz = min(P.ctr->n_zero, P.zero_cap);
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nz; j += gridDim.x * blockDim.x) {
-        const PairGeom g = pair_geom(P, P.zero[j], true);
-        uint32_t gs = 0, cs = 0;
-        if (table_find(P.gkeys, 1u, P.gtable_mask, make_key(0u, g.leaf, g.tri_a), &gs) && P.gflag[gs] &&
-            table_find(&P.table->key, kSlotWords, P.table_mask, make_key(0u, g.q, g.tri_a), &cs))
-            atomicAnd(&P.table[cs].mask, g.mask_a);
-        if (table_find(P.gkeys, 1u, P.gtable_mask, make_key(1u, g.leaf, g.tri_b), &gs) && P.gflag[gs] &&
-            table_find(&P.table->key, kSlotWords, P.table_mask, make_key(1u, g.q, g.tri_b), &cs))
-            atomicAnd(&P.table[cs].mask, g.mask_b);
-    }
-}
-
-__global__ void contacts_emit_kernel(const ContactParams P) {
+__global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams P) {
+    __shared__ bool last_block;
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr->prev_vertices = 0u;  // the accumulate kernel emptied them
     const uint32_t n = P.ctr->n_contacts;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        ContactSlot* s = P.table + P.occupied[j];
-        const unsigned long long key = s->key;
-        const uint32_t side = uint32_t(key >> 63);
-        const uint32_t q = uint32_t(key >> 32) & 0x7fffffffu;
-        const uint32_t tri = uint32_t(key);
-        const float3 wsum = make_float3(float(s->sx), float(s->sy), float(s->sz));
-        const float weight = float(s->sw);
-        const unsigned mask = s->mask;
-        s->sx = s->sy = s->sz = s->sw = 0.0;  // the slot is empty again for the next launch
-        s->mask = 7u;
-        s->key = kEmptyKey;
-        // TriangleCandidateRays::GetWeightedAvg
-        const float3 avg = divs3(wsum, weight);
-        if (j < P.max_contacts) {
-            cg_contact c;
-            c.query = q;
-            c.side = side;
-            c.tri = tri;
-            c.mask = mask;
-            c.weighted_avg[0] = avg.x;
-            c.weighted_avg[1] = avg.y;
-            c.weighted_avg[2] = avg.z;
-            c.weight = weight;
-            P.contacts[j] = c;
-        }
-
-        const PackedQuery* Q = P.q + q;
-        const float* nrm = P.trees[side ? __ldg(&Q->tree_b) : __ldg(&Q->tree_a)].nrm;
-        const Mat4 M = query_mat(Q);
-        float3 p[3], n3[3];
-        uint32_t vi[3];
-        tri_at(P.tris, (side ? __ldg(&Q->tri_base_b) : __ldg(&Q->tri_base_a)) + tri, p, vi);
-        if (nrm) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float* np = nrm + 9ull * tri + 3 * k;
-                n3[k] = make_float3(__ldg(np), __ldg(np + 1), __ldg(np + 2));
-            }
-        } else {  // a tree without vertex normals carries the face normal on all corners
-            n3[0] = n3[1] = n3[2] = face_normal(p[0], p[1], p[2]);
-        }
-        if (side) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) p[k] = xform(M, p[k], 1.0f);
-        }
-        const Mat3 N = cofactor3(M);
-        if (mask != 0u) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                if (!(mask & (1u << k))) continue;
-                uint32_t vs = 0;
-                const int r = table_insert(P.vkeys, 1u, P.vtable_mask, make_key(side, q, vi[k]), &vs);
-                if (r < 0) atomicOr(&P.ctr->c_overflow, CONTACT_VERTICES);
-                if (r != 1) continue;  // this vertex already has its ray
-                P.vocc[atomicAdd(&P.ctr->n_vertices, 1u)] = vs;
-                // TriangleNormal::GetNormal(index[, corrected_matrix]) (Triangle.cpp:180-195)
-                const float3 nn = side ? normalize3(mul3(N, n3[k])) : normalize3(n3[k]);
-                emit_ray(P, q, side, p[k], neg3(nn));
-            }
-        } else {
-            // TrianglePosition::GetBarycentricOfPoint (Triangle.cpp:148-163) and
-            // TriangleNormal::GetNormal(bary[, corrected_matrix]) (Triangle.cpp:197-212)
-            const float3 v0 = sub3(p[1], p[0]), v1 = sub3(p[2], p[0]), v2 = sub3(avg, p[0]);
-            const float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
-            const float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
-            const float den = d00 * d11 - d01 * d01;
-            const float bx = (d11 * d20 - d01 * d21) / den;
-            const float by = (d00 * d21 - d01 * d20) / den;
-            const float b0 = 1.f - bx - by;
-            const float3 in = add3(add3(scale3(b0, n3[0]), scale3(bx, n3[1])), scale3(by, n3[2]));
-            const float3 nn = side ? normalize3(mul3(N, in)) : normalize3(in);
-            emit_ray(P, q, side, avg, neg3(nn));
-        }
-    }
-}
-
-__global__ void ray_averages_kernel(const ContactParams P) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t nv = P.ctr->n_vertices;
-    for (uint32_t j = i; j < nv; j += stride) P.vkeys[P.vocc[j]] = kEmptyKey;
-    const uint32_t ng = P.ctr->n_groups;
-    for (uint32_t j = i; j < ng; j += stride) {
-        P.gkeys[P.gocc[j]] = kEmptyKey;
-        P.gflag[P.gocc[j]] = 0u;
+    for (uint32_t base = tid & ~31u; base < n; base += stride) {
+        const uint32_t j = base + (threadIdx.x & 31u);
+        LaneRays R;
+        R.n = R.nv = 0;
+        uint32_t q = 0, side = 0;
+        if (j < n) {
+            ContactSlot* s = P.table + P.occupied[j];
+            const unsigned long long key = s->key;
+            side = uint32_t(key >> 63);
+            q = uint32_t(key >> 32) & 0x7fffffffu;
+            const uint32_t tri = uint32_t(key);
+            const float3 wsum = make_float3(float(s->sx), float(s->sy), float(s->sz));
+            const float weight = float(s->sw);
+            const unsigned mask = s->mask;
+            s->sx = s->sy = s->sz = s->sw = 0.0;  // the slot is empty again for the next launch
+            s->mask = 7u;
+            s->key = kEmptyKey;
+            // TriangleCandidateRays::GetWeightedAvg
+            const float3 avg = divs3(wsum, weight);
+            if (j < P.max_contacts) {
+                cg_contact c;
+                c.query = q;
+                c.side = side;
+                c.tri = tri;
+                c.mask = mask;
+                c.weighted_avg[0] = avg.x;
+                c.weighted_avg[1] = avg.y;
+                c.weighted_avg[2] = avg.z;
+                c.weight = weight;
+                P.contacts[j] = c;
+            }
+
+            const PackedQuery* Q = P.q + q;
+            const float* nrm = P.trees[side ? __ldg(&Q->tree_b) : __ldg(&Q->tree_a)].nrm;
+            const Mat4 M = query_mat(Q);
+            float3 p[3], n3[3];
+            uint32_t vi[3];
+            tri_at(P.tris, (side ? __ldg(&Q->tri_base_b) : __ldg(&Q->tri_base_a)) + tri, p, vi);
+            if (nrm) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float* np = nrm + 9ull * tri + 3 * k;
+                    n3[k] = make_float3(__ldg(np), __ldg(np + 1), __ldg(np + 2));
+                }
+            } else {  // a tree without vertex normals carries the face normal on all corners
+                n3[0] = n3[1] = n3[2] = face_normal(p[0], p[1], p[2]);
+            }
+            if (side) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) p[k] = xform(M, p[k], 1.0f);
+            }
+            const Mat3 N = cofactor3(M);
+            if (mask != 0u) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!(mask & (1u << k))) continue;
+                    uint32_t vs = 0;
+                    const int r = table_insert(P.vkeys, 1u, P.vtable_mask, make_key(side, q, vi[k]), &vs);
+                    if (r < 0) atomicOr(&P.ctr->c_overflow, CONTACT_VERTICES);
+                    if (r != 1) continue;  // this vertex already has its ray
+                    // TriangleNormal::GetNormal(index[, corrected_matrix]) (Triangle.cpp:180-195)
+                    const float3 nn = side ? normalize3(mul3(N, n3[k])) : normalize3(n3[k]);
+                    R.o[R.n] = p[k];
+                    R.d[R.n] = neg3(nn);
+                    R.vs[R.n] = vs;
+                    ++R.n;
+                }
+                R.nv = R.n;
+            } else {
+                // TrianglePosition::GetBarycentricOfPoint (Triangle.cpp:148-163) and
+                // TriangleNormal::GetNormal(bary[, corrected_matrix]) (Triangle.cpp:197-212)
+                const float3 v0 = sub3(p[1], p[0]), v1 = sub3(p[2], p[0]), v2 = sub3(avg, p[0]);
+                const float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
+                const float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
+                const float den = d00 * d11 - d01 * d01;
+                const float bx = (d11 * d20 - d01 * d21) / den;
+                const float by = (d00 * d21 - d01 * d20) / den;
+                const float b0 = 1.f - bx - by;
+                const float3 in = add3(add3(scale3(b0, n3[0]), scale3(bx, n3[1])), scale3(by, n3[2]));
+                const float3 nn = side ? normalize3(mul3(N, in)) : normalize3(in);
+                R.o[0] = avg;
+                R.d[0] = neg3(nn);
+                R.n = 1;
+            }
+        }
+        __syncwarp();
+        const unsigned vo = warp_append(&P.ctr->n_vertices, R.nv);
+        const unsigned ro = warp_append(&P.ctr->n_rays, R.n);
+        for (unsigned k = 0; k < R.nv; ++k) P.vocc[vo + k] = R.vs[k];  // never more than the set's slots
+        double* sum = P.sums + 8ull * q + 4ull * side;
+        for (unsigned k = 0; k < R.n; ++k) {
+            if (ro + k < P.max_rays) {
+                cg_ray r;
+                r.query = q;
+                r.side = side;
+                r.origin[0] = R.o[k].x;
+                r.origin[1] = R.o[k].y;
+                r.origin[2] = R.o[k].z;
+                r.direction[0] = R.d[k].x;
+                r.direction[1] = R.d[k].y;
+                r.direction[2] = R.d[k].z;
+                P.rays[ro + k] = r;
+            } else {
+                atomicOr(&P.ctr->c_overflow, CONTACT_RAYS);
+            }
+            atomicAdd(sum + 0, double(R.o[k].x));
+            atomicAdd(sum + 1, double(R.o[k].y));
+            atomicAdd(sum + 2, double(R.o[k].z));
+            atomicAdd(sum + 3, 1.0);
+        }
     }
-    if (i >= P.n_queries) return;
-    const double* s = P.sums + 8ull * i;
-    float3 avg[2];
-    for (int side = 0; side < 2; ++side) {
-        const float3 sum = make_float3(float(s[4 * side]), float(s[4 * side + 1]), float(s[4 * side + 2]));
-        avg[side] = divs3(sum, float(s[4 * side + 3]));
+
+    // The last block to finish: per-query mean origins, from the sums every
+    // block has completed (each block publishes its atomics before it counts
+    // itself done).
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last_block = atomicAdd(&P.ctr->emit_done, 1u) == gridDim.x - 1u;
     }
-    const float3 back = xform(inverse4(query_mat(P.q + i)), avg[1], 1.0f);
-    cg_ray_average a;
-    a.first[0] = avg[0].x;
-    a.first[1] = avg[0].y;
-    a.first[2] = avg[0].z;
-    a.second[0] = back.x;
-    a.second[1] = back.y;
-    a.second[2] = back.z;
-    a.rays_first = uint32_t(s[3]);
-    a.rays_second = uint32_t(s[7]);
-    P.averages[i] = a;
+    __syncthreads();
+    if (!last_block) return;
+    __threadfence();
+    for (uint32_t i = threadIdx.x; i < P.n_queries; i += blockDim.x) {
+        const double* s = P.sums + 8ull * i;
+        float3 avg[2];
+        float cnt[2];
+        for (int side = 0; side < 2; ++side) {
+            const float3 sum = make_float3(float(__ldcg(s + 4 * side)), float(__ldcg(s + 4 * side + 1)),
+                                           float(__ldcg(s + 4 * side + 2)));
+            cnt[side] = float(__ldcg(s + 4 * side + 3));
+            avg[side] = divs3(sum, cnt[side]);
+        }
+        const float3 back = xform(inverse4(query_mat(P.q + i)), avg[1], 1.0f);
+        cg_ray_average a;
+        a.first[0] = avg[0].x;
+        a.first[1] = avg[0].y;
+        a.first[2] = avg[0].z;
+        a.second[0] = back.x;
+        a.second[1] = back.y;
+        a.second[2] = back.z;
+        a.rays_first = uint32_t(cnt[0]);
+        a.rays_second = uint32_t(cnt[1]);
+        P.averages[i] = a;
+    }
 }
 
-__global__ void init_tables_kernel(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
-                                   unsigned long long* gkeys, unsigned int* gflag, uint32_t n_gslots) {
+__global__ void init_tables_kernel(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots) {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (uint32_t i = i0; i < n_slots; i += stride) {
@@ -457,25 +499,17 @@ __global__ void init_tables_kernel(ContactSlot* table, uint32_t n_slots, unsigne
         table[i] = s;
     }
     for (uint32_t i = i0; i < n_vslots; i += stride) vkeys[i] = kEmptyKey;
-    for (uint32_t i = i0; i < n_gslots; i += stride) {
-        gkeys[i] = kEmptyKey;
-        gflag[i] = 0u;
-    }
 }
 
 cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
-                                unsigned long long* gkeys, unsigned int* gflag, uint32_t n_gslots, cudaStream_t s) {
-    init_tables_kernel<<<1024, 256, 0, s>>>(table, n_slots, vkeys, n_vslots, gkeys, gflag, n_gslots);
+                                cudaStream_t s) {
+    init_tables_kernel<<<1024, 256, 0, s>>>(table, n_slots, vkeys, n_vslots);
     return cudaGetLastError();
 }
 
 cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s) {
     contacts_accumulate_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_mark_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_apply_kernel<<<grid, 256, 0, s>>>(p);
     contacts_emit_kernel<<<grid, 256, 0, s>>>(p);
-    const uint32_t qgrid = (p.n_queries + 255u) / 256u;
-    ray_averages_kernel<<<qgrid > grid ? qgrid : grid, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

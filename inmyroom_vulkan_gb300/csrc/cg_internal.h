@@ -83,12 +83,12 @@ struct Counters {
     unsigned int n_contacts;  // contact slots taken
     unsigned int n_vertices;  // vertex-set slots taken
     unsigned int n_rays;
-    unsigned int n_zero;      // colliding pairs of zero segment length
-    unsigned int c_overflow;  // CONTACT_* bits
-    unsigned int n_groups;    // group-table slots taken
+    unsigned int c_overflow;     // CONTACT_* bits
+    unsigned int emit_done;      // blocks of the emit kernel that finished
+    unsigned int prev_vertices;  // vertex-set slots earlier launches took and no launch emptied yet
 };
 
-enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ZERO = 8u };
+enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u };
 
 enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
 
@@ -112,19 +112,14 @@ struct ContactParams {
     const DevTree* trees;
     const cg_tri_pair* pairs;
     const uint32_t* pair_leaf;  // leaf-list index of each pair
+    const uint4* leaf_list;     // the launch's candidate leaf pairs
     unsigned long long pairs_cap;
     ContactSlot* table;
     uint32_t table_mask;
     uint32_t* occupied;         // slots taken this launch
     unsigned long long* vkeys;  // set of (side, query, vertex index) that already have a ray
     uint32_t vtable_mask;
-    uint32_t* vocc;
-    uint32_t* zero;             // pairs whose segment has zero length
-    uint32_t zero_cap;
-    unsigned long long* gkeys;  // (side, leaf pair, triangle) groups of those pairs
-    unsigned int* gflag;        // 1 = the group also has a pair of non-zero length
-    uint32_t gtable_mask;
-    uint32_t* gocc;
+    uint32_t* vocc;             // vertex-set slots taken, in order
     uint32_t max_contacts;
     cg_contact* contacts;
     cg_ray* rays;
@@ -136,7 +131,7 @@ struct ContactParams {
 
 cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s);
 cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
-                                unsigned long long* gkeys, unsigned int* gflag, uint32_t n_gslots, cudaStream_t s);
+                                cudaStream_t s);
 
 // Work queue. A task is a chunk of up to kChunk node pairs: donated slot
 // s >= n_queries holds its chunk at pool[kChunk * (s - n_queries)], and

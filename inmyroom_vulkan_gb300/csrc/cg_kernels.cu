@@ -765,6 +765,8 @@ __global__ void init_kernel(Counters* ctr, unsigned int* ready, uint32_t slot_al
         Counters c = {};
         c.tail = n_queries;
         c.n_queries = n_queries;
+        // vertex-set slots stay taken until a contacts launch empties them
+        c.prev_vertices = ctr->prev_vertices + ctr->n_vertices;
         *ctr = c;
     }
 }
