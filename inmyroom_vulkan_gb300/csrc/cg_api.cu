@@ -131,7 +131,7 @@ struct cg_ctx {
 
     // contacts and rays (CG_CONTACTS), allocated when max_contacts > 0
     struct Contacts {
-        uint32_t* pair_leaf = nullptr;
+        uint4* pair_aux = nullptr;
         ContactSlot* table = nullptr;
         uint32_t table_slots = 0;
         uint32_t* occupied = nullptr;
@@ -206,7 +206,7 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_leafs);
     cudaFree(c->d_trace);
     auto& t = c->ct;
-    cudaFree(t.pair_leaf);
+    cudaFree(t.pair_aux);
     cudaFree(t.table);
     cudaFree(t.occupied);
     cudaFree(t.vkeys);
@@ -297,7 +297,7 @@ int alloc_buffers(cg_ctx* c) {
         t.table_slots = pow2_at_least(2 * g.max_contacts);
         t.vslots = pow2_at_least(6 * g.max_contacts);
         t.max_rays = uint32_t(3 * g.max_contacts);
-        CG_CUDA(cudaMalloc(&t.pair_leaf, sizeof(uint32_t) * g.max_tri_pairs), "alloc pair leaf indices");
+        CG_CUDA(cudaMalloc(&t.pair_aux, sizeof(uint4) * g.max_tri_pairs), "alloc pair side records");
         CG_CUDA(cudaMalloc(&t.table, sizeof(ContactSlot) * t.table_slots), "alloc contact table");
         CG_CUDA(cudaMalloc(&t.occupied, sizeof(uint32_t) * t.table_slots), "alloc contact list");
         CG_CUDA(cudaMalloc(&t.vkeys, sizeof(unsigned long long) * t.vslots), "alloc vertex set");
@@ -378,7 +378,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     np.leaf_cap = p.leaf_cap;
     np.ctr = c->d_ctr;
     np.pairs = c->d_pairs;
-    np.pair_leaf = (flags & CG_CONTACTS) ? c->ct.pair_leaf : nullptr;
+    np.pair_aux = (flags & CG_CONTACTS) ? c->ct.pair_aux : nullptr;
     np.pairs_cap = c->d_pairs ? c->cfg.max_tri_pairs : 0;
     np.leafs = c->d_leafs;
     np.leafs_cap = c->d_leafs ? c->cfg.max_leaf_pairs : 0;
@@ -399,7 +399,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.tris = c->tris.ptr;
         cp.trees = c->d_trees;
         cp.pairs = c->d_pairs;
-        cp.pair_leaf = t.pair_leaf;
+        cp.pair_aux = t.pair_aux;
         cp.leaf_list = c->d_leaf_list;
         cp.pairs_cap = c->cfg.max_tri_pairs;
         cp.table = t.table;
@@ -1088,7 +1088,7 @@ extern "C" int cg_collide_static(cg_ctx* c, const cg_query* d_queries, uint32_t 
     np.leaf_cap = CG_STATIC_MAX_LEAF_PAIRS;
     np.ctr = ctr;
     np.pairs = d_pairs;
-    np.pair_leaf = nullptr;
+    np.pair_aux = nullptr;
     np.pairs_cap = d_pairs ? pairs_cap : 0;
     np.leafs = nullptr;
     np.leafs_cap = 0;

@@ -173,9 +173,35 @@ __device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned take
     return base + incl - take;
 }
 
+// warp_append for two adjacent counters (lo, and hi at lo + 1, an 8-byte
+// aligned pair) with one 64-bit atomic.
+__device__ __forceinline__ void warp_append2(unsigned* lo, unsigned take_lo, unsigned take_hi, unsigned* base_lo,
+                                             unsigned* base_hi) {
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned a = take_lo, b = take_hi;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned ta = __shfl_up_sync(kFullMask, a, o);
+        const unsigned tb = __shfl_up_sync(kFullMask, b, o);
+        if (lane >= unsigned(o)) {
+            a += ta;
+            b += tb;
+        }
+    }
+    const unsigned total_a = __shfl_sync(kFullMask, a, 31), total_b = __shfl_sync(kFullMask, b, 31);
+    unsigned long long old = 0;
+    if (lane == 31 && (total_a | total_b))
+        old = atomicAdd(reinterpret_cast<unsigned long long*>(lo),
+                        (unsigned long long)total_a | ((unsigned long long)total_b << 32));
+    old = __shfl_sync(kFullMask, old, 31);
+    *base_lo = unsigned(old) + a - take_lo;
+    *base_hi = unsigned(old >> 32) + b - take_hi;
+}
+
 // Everything the contact step needs of one colliding pair.
 struct PairGeom {
-    uint32_t q, tri_a, tri_b, leaf;
+    uint32_t q, tri_a, tri_b, leaf;  // query, tree-local triangles, leaf-list index
+    uint32_t ia, ib;                 // arena triangles
     float w;
     float3 mid;
     unsigned mask_a, mask_b;
@@ -184,23 +210,27 @@ struct PairGeom {
 // CreateUncollideRays.cpp:148-172 for pair i: the second triangle is moved
 // into the first tree's space, each triangle's vertices are tested against
 // the other's plane, w = |source - target| and mid = w * (source + target) / 2.
+// The pair record and its side record load together, then the matrix and
+// both triangles.
 __device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i) {
     const cg_tri_pair r = P.pairs[i];
+    const uint4 x = P.pair_aux[i];
     PairGeom g;
-    g.q = r.query;
+    g.q = x.w;
     g.tri_a = r.tri_a;
     g.tri_b = r.tri_b;
-    g.leaf = P.pair_leaf[i];
+    g.leaf = x.z;
+    g.ia = x.x;
+    g.ib = x.y;
     const float3 s = make_float3(r.source[0], r.source[1], r.source[2]);
     const float3 t = make_float3(r.target[0], r.target[1], r.target[2]);
     g.w = length3(sub3(s, t));
     g.mid = divs3(scale3(g.w, add3(s, t)), 2.0f);
-    const PackedQuery* Q = P.q + r.query;
-    const Mat4 M = query_mat(Q);
+    const Mat4 M = query_mat(P.q + x.w);
     float3 pa[3], pb[3];
     uint32_t vi[3];
-    tri_at(P.tris, __ldg(&Q->tri_base_a) + r.tri_a, pa, vi);
-    tri_at(P.tris, __ldg(&Q->tri_base_b) + r.tri_b, pb, vi);
+    tri_at(P.tris, x.x, pa, vi);
+    tri_at(P.tris, x.y, pb, vi);
 #pragma unroll
     for (int k = 0; k < 3; ++k) pb[k] = xform(M, pb[k], 1.0f);
     const Plane plane_a = plane_of(pa[0], pa[1], pa[2]);
@@ -220,13 +250,12 @@ __device__ PairGeom pair_geom(const ContactParams& P, unsigned long long i) {
 // non-zero length.
 __device__ bool group_has_weight(const ContactParams& P, const PairGeom& g, uint32_t side) {
     const uint4 lp = P.leaf_list[g.leaf];  // (query, first triangle a, first triangle b, counts)
-    const PackedQuery* Q = P.q + g.q;
-    const Mat4 M = query_mat(Q);
+    const Mat4 M = query_mat(P.q + g.q);
     const uint32_t cnt_a = lp.w & 0xffffu, cnt_b = lp.w >> 16;
     const uint32_t n = side ? cnt_a : cnt_b;
     for (uint32_t k = 0; k < n; ++k) {
-        const uint32_t ia = side ? lp.y + k : __ldg(&Q->tri_base_a) + g.tri_a;
-        const uint32_t ib = side ? __ldg(&Q->tri_base_b) + g.tri_b : lp.z + k;
+        const uint32_t ia = side ? lp.y + k : g.ia;
+        const uint32_t ib = side ? g.ib : lp.z + k;
         float3 a[3], b[3];
         uint32_t vi[3];
         tri_at(P.tris, ia, a, vi);
@@ -242,31 +271,37 @@ __device__ bool group_has_weight(const ContactParams& P, const PairGeom& g, uint
 
 // Hash sets with open addressing and linear probing over 64-bit keys stored
 // `stride` words apart. No key is removed while a set is in use: each launch
-// empties the slots it took once it is done with them.
-__device__ int table_insert(unsigned long long* keys, uint32_t stride, uint32_t mask, unsigned long long key,
-                            uint32_t* slot_out) {
-    uint32_t slot = hash64(key) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        unsigned long long* k = keys + size_t(stride) * slot;
-        unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(k);
-        if (cur == kEmptyKey) cur = atomicCAS(k, kEmptyKey, key);
+// empties the slots it took once it is done with them. An insert is a CAS at
+// the key's home slot (issued by the caller, so that a thread's inserts are
+// in flight together) and, after a collision, at the following slots.
+struct Probe {
+    unsigned long long* keys;
+    uint32_t stride, mask;
+    __device__ unsigned long long* at(uint32_t slot) const { return keys + size_t(stride) * slot; }
+    __device__ uint32_t home(unsigned long long key) const { return hash64(key) & mask; }
+};
+
+// Result of an insert whose home-slot CAS returned `cur`: 1 inserted, 0
+// already present (*slot set either way), -1 the table is full.
+__device__ int finish_insert(const Probe& T, unsigned long long key, unsigned long long cur, uint32_t home,
+                             uint32_t* slot) {
+    uint32_t s = home;
+    for (uint32_t probe = 0;; ++probe) {
         if (cur == kEmptyKey || cur == key) {
-            *slot_out = slot;
-            return cur == kEmptyKey ? 1 : 0;  // 1: inserted now, 0: present
+            *slot = s;
+            return cur == kEmptyKey ? 1 : 0;
         }
-        slot = (slot + 1u) & mask;
+        if (probe == T.mask) return -1;
+        s = (s + 1u) & T.mask;
+        cur = atomicCAS(T.at(s), kEmptyKey, key);
     }
-    return -1;  // full
 }
 
 constexpr uint32_t kSlotWords = sizeof(ContactSlot) / sizeof(unsigned long long);
 static_assert(sizeof(ContactSlot) % sizeof(unsigned long long) == 0, "contact slots hold whole key words");
 
-// Inserts (or finds) the contact of `key`; -1 when the table is full.
-__device__ int contact_slot(const ContactParams& P, unsigned long long key, uint32_t* slot) {
-    const int r = table_insert(&P.table->key, kSlotWords, P.table_mask, key, slot);
-    if (r < 0) atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
-    return r;
+__device__ __forceinline__ Probe contact_table(const ContactParams& P) {
+    return Probe{&P.table->key, kSlotWords, P.table_mask};
 }
 
 __device__ __forceinline__ void add_to_slot(const ContactParams& P, uint32_t slot, float3 mid, float w, unsigned mask) {
@@ -297,26 +332,29 @@ __global__ void __launch_bounds__(256) contacts_accumulate_kernel(const ContactP
     const unsigned long long warp0 = tid & ~31ull;  // warp-uniform loop: warp_append needs all lanes
     for (unsigned long long base = warp0; base < n; base += stride) {
         const unsigned long long i = base + (threadIdx.x & 31u);
-        int ra = -2, rb = -2;  // -2: no slot wanted, else contact_slot's result
+        int ra = -2, rb = -2;  // -2: no slot wanted, else the insert's result
         uint32_t sa = 0, sb = 0;
         if (i < n) {
             const PairGeom g = pair_geom(P, i);
-            if (g.w != 0.0f) {
-                ra = contact_slot(P, make_key(0u, g.q, g.tri_a), &sa);
-                if (ra >= 0) add_to_slot(P, sa, g.mid, g.w, g.mask_a);
-                rb = contact_slot(P, make_key(1u, g.q, g.tri_b), &sb);
-                if (rb >= 0) add_to_slot(P, sb, g.mid, g.w, g.mask_b);
-            } else {
-                // no weight: only the vertex bits count, and only in a leaf pair
-                // that gives the triangle weight (then its contact exists anyway)
-                if (group_has_weight(P, g, 0u)) {
-                    ra = contact_slot(P, make_key(0u, g.q, g.tri_a), &sa);
-                    if (ra >= 0) atomicAnd(&P.table[sa].mask, g.mask_a);
-                }
-                if (group_has_weight(P, g, 1u)) {
-                    rb = contact_slot(P, make_key(1u, g.q, g.tri_b), &sb);
-                    if (rb >= 0) atomicAnd(&P.table[sb].mask, g.mask_b);
-                }
+            const Probe T = contact_table(P);
+            const unsigned long long ka = make_key(0u, g.q, g.tri_a), kb = make_key(1u, g.q, g.tri_b);
+            // a pair of zero length only ANDs its vertex bits, and only where
+            // its leaf pair gives the triangle weight
+            const bool want_a = g.w != 0.0f || group_has_weight(P, g, 0u);
+            const bool want_b = g.w != 0.0f || group_has_weight(P, g, 1u);
+            const uint32_t ha = T.home(ka), hb = T.home(kb);
+            const unsigned long long ca = want_a ? atomicCAS(T.at(ha), kEmptyKey, ka) : 0ull;
+            const unsigned long long cb = want_b ? atomicCAS(T.at(hb), kEmptyKey, kb) : 0ull;
+            if (want_a) ra = finish_insert(T, ka, ca, ha, &sa);
+            if (want_b) rb = finish_insert(T, kb, cb, hb, &sb);
+            if (ra == -1 || rb == -1) atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
+            if (ra >= 0) {
+                if (g.w != 0.0f) add_to_slot(P, sa, g.mid, g.w, g.mask_a);
+                else atomicAnd(&P.table[sa].mask, g.mask_a);
+            }
+            if (rb >= 0) {
+                if (g.w != 0.0f) add_to_slot(P, sb, g.mid, g.w, g.mask_b);
+                else atomicAnd(&P.table[sb].mask, g.mask_b);
             }
         }
         __syncwarp();
@@ -328,10 +366,13 @@ __global__ void __launch_bounds__(256) contacts_accumulate_kernel(const ContactP
 }
 
 // Rays of one contact, made in registers before they are appended.
+// Ray k of a contact sits in entry k (a vertex ray) or 0 (the weighted
+// average's ray); `live` has bit k set for each ray made.
 struct LaneRays {
     float3 o[3], d[3];
-    uint32_t vs[3];  // vertex-set slots taken for them
-    unsigned n, nv;
+    uint32_t vs[3];   // vertex-set slots taken for vertex rays
+    unsigned live;
+    bool vertex;      // rays from vertices (they take vertex-set entries)
 };
 
 __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams P) {
@@ -343,7 +384,8 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
     for (uint32_t base = tid & ~31u; base < n; base += stride) {
         const uint32_t j = base + (threadIdx.x & 31u);
         LaneRays R;
-        R.n = R.nv = 0;
+        R.live = 0u;
+        R.vertex = false;
         uint32_t q = 0, side = 0;
         if (j < n) {
             ContactSlot* s = P.table + P.occupied[j];
@@ -393,21 +435,31 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
             }
             const Mat3 N = cofactor3(M);
             if (mask != 0u) {
+                // the home-slot inserts of the (up to) three vertices go out together
+                const Probe V{P.vkeys, 1u, P.vtable_mask};
+                unsigned long long vk[3], cur[3];
+                uint32_t home[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    vk[k] = make_key(side, q, vi[k]);
+                    home[k] = V.home(vk[k]);
+                    cur[k] = (mask & (1u << k)) ? atomicCAS(V.at(home[k]), kEmptyKey, vk[k]) : 0ull;
+                }
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     if (!(mask & (1u << k))) continue;
                     uint32_t vs = 0;
-                    const int r = table_insert(P.vkeys, 1u, P.vtable_mask, make_key(side, q, vi[k]), &vs);
+                    const int r = finish_insert(V, vk[k], cur[k], home[k], &vs);
                     if (r < 0) atomicOr(&P.ctr->c_overflow, CONTACT_VERTICES);
                     if (r != 1) continue;  // this vertex already has its ray
                     // TriangleNormal::GetNormal(index[, corrected_matrix]) (Triangle.cpp:180-195)
                     const float3 nn = side ? normalize3(mul3(N, n3[k])) : normalize3(n3[k]);
-                    R.o[R.n] = p[k];
-                    R.d[R.n] = neg3(nn);
-                    R.vs[R.n] = vs;
-                    ++R.n;
+                    R.o[k] = p[k];
+                    R.d[k] = neg3(nn);
+                    R.vs[k] = vs;
+                    R.live |= 1u << k;
                 }
-                R.nv = R.n;
+                R.vertex = true;
             } else {
                 // TrianglePosition::GetBarycentricOfPoint (Triangle.cpp:148-163) and
                 // TriangleNormal::GetNormal(bary[, corrected_matrix]) (Triangle.cpp:197-212)
@@ -422,16 +474,20 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
                 const float3 nn = side ? normalize3(mul3(N, in)) : normalize3(in);
                 R.o[0] = avg;
                 R.d[0] = neg3(nn);
-                R.n = 1;
+                R.live = 1u;
             }
         }
         __syncwarp();
-        const unsigned vo = warp_append(&P.ctr->n_vertices, R.nv);
-        const unsigned ro = warp_append(&P.ctr->n_rays, R.n);
-        for (unsigned k = 0; k < R.nv; ++k) P.vocc[vo + k] = R.vs[k];  // never more than the set's slots
+        const unsigned n_rays = __popc(R.live);
+        unsigned vo, ro;
+        warp_append2(&P.ctr->n_vertices, R.vertex ? n_rays : 0u, n_rays, &vo, &ro);
         double* sum = P.sums + 8ull * q + 4ull * side;
-        for (unsigned k = 0; k < R.n; ++k) {
-            if (ro + k < P.max_rays) {
+#pragma unroll
+        for (unsigned k = 0; k < 3; ++k) {
+            if (!(R.live & (1u << k))) continue;
+            const unsigned below = __popc(R.live & ((1u << k) - 1u));
+            if (R.vertex) P.vocc[vo + below] = R.vs[k];  // never more entries than the set's slots
+            if (ro + below < P.max_rays) {
                 cg_ray r;
                 r.query = q;
                 r.side = side;
@@ -441,7 +497,7 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
                 r.direction[0] = R.d[k].x;
                 r.direction[1] = R.d[k].y;
                 r.direction[2] = R.d[k].z;
-                P.rays[ro + k] = r;
+                P.rays[ro + below] = r;
             } else {
                 atomicOr(&P.ctr->c_overflow, CONTACT_RAYS);
             }

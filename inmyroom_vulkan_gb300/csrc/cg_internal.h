@@ -25,6 +25,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 
 #include "collide_gpu.h"
@@ -80,13 +81,16 @@ struct Counters {
     unsigned long long warp_steps; // traversal steps (node_pairs / warp_steps = lanes busy per step)
     unsigned long long t_start;    // globaltimer at the first warp's start (trace only)
     // contacts (CG_CONTACTS)
+    unsigned int n_vertices;  // vertex-set slots taken  } one 64-bit word: the emit kernel
+    unsigned int n_rays;      // rays                    } appends to both with one atomic
     unsigned int n_contacts;  // contact slots taken
-    unsigned int n_vertices;  // vertex-set slots taken
-    unsigned int n_rays;
     unsigned int c_overflow;     // CONTACT_* bits
     unsigned int emit_done;      // blocks of the emit kernel that finished
     unsigned int prev_vertices;  // vertex-set slots earlier launches took and no launch emptied yet
 };
+
+static_assert(offsetof(Counters, n_vertices) % 8 == 0 && offsetof(Counters, n_rays) == offsetof(Counters, n_vertices) + 4,
+              "n_vertices and n_rays form one 64-bit word");
 
 enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u };
 
@@ -111,7 +115,7 @@ struct ContactParams {
     const float4* tris;
     const DevTree* trees;
     const cg_tri_pair* pairs;
-    const uint32_t* pair_leaf;  // leaf-list index of each pair
+    const uint4* pair_aux;      // per pair: (first triangle, second triangle, leaf-list index, query), arena indices
     const uint4* leaf_list;     // the launch's candidate leaf pairs
     unsigned long long pairs_cap;
     ContactSlot* table;
@@ -163,7 +167,7 @@ struct NarrowParams {
     uint32_t leaf_cap;
     Counters* ctr;
     cg_tri_pair* pairs;
-    uint32_t* pair_leaf;  // leaf-list index of each written pair (contacts) or null
+    uint4* pair_aux;      // per written pair (contacts): arena triangles, leaf-list index, query; or null
     unsigned long long pairs_cap;
     cg_leaf_pair* leafs;  // the public copy of the leaf pairs (CG_KEEP_LEAF_PAIRS)
     unsigned long long leafs_cap;

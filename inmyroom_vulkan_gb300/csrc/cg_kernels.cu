@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
                         r.target[1] = tgt.y;
                         r.target[2] = tgt.z;
                         P.pairs[o] = r;
-                        if (P.pair_leaf) P.pair_leaf[o] = leaf_i;
+                        if (P.pair_aux) P.pair_aux[o] = make_uint4(ia, ib, leaf_i, q);
                     }
                 }
             }
