@@ -71,7 +71,7 @@ struct Counters {
     unsigned int done;        // finished tasks; all work is done when done == tail
     unsigned int error;       // ERR_* bits
     unsigned int n_queries;   // queries of the launch (the next launch clears the slots it published)
-    unsigned int narrow_next; // next block of 32 leaf pairs for the narrow phase
+    unsigned int narrow_lp;   // next leaf pair for the narrow phase
     unsigned long long n_pairs;
     unsigned long long n_leafs;
     unsigned long long node_pairs;
@@ -137,6 +137,22 @@ cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t 
 cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
                                 cudaStream_t s);
 
+struct NarrowParams {
+    const PackedQuery* q;
+    const float4* tris;   // triangle arena
+    const uint4* leaf_list;
+    uint32_t leaf_cap;
+    Counters* ctr;
+    cg_tri_pair* pairs;
+    uint4* pair_aux;      // per written pair (contacts): arena triangles, leaf-list index, query; or null
+    unsigned long long pairs_cap;
+    cg_leaf_pair* leafs;  // the public copy of the leaf pairs (CG_KEEP_LEAF_PAIRS)
+    unsigned long long leafs_cap;
+    uint32_t flags;
+    unsigned int* trace;
+    uint32_t trace_ns;
+};
+
 // Work queue. A task is a chunk of up to kChunk node pairs: donated slot
 // s >= n_queries holds its chunk at pool[kChunk * (s - n_queries)], and
 // ready[s - n_queries] becomes count + 1 when it is published. Slot
@@ -160,24 +176,9 @@ struct TraverseParams {
     unsigned long long wait_ns;
 };
 
-struct NarrowParams {
-    const PackedQuery* q;
-    const float4* tris;   // triangle arena
-    const uint4* leaf_list;
-    uint32_t leaf_cap;
-    Counters* ctr;
-    cg_tri_pair* pairs;
-    uint4* pair_aux;      // per written pair (contacts): arena triangles, leaf-list index, query; or null
-    unsigned long long pairs_cap;
-    cg_leaf_pair* leafs;  // the public copy of the leaf pairs (CG_KEEP_LEAF_PAIRS)
-    unsigned long long leafs_cap;
-    uint32_t flags;
-    unsigned int* trace;
-    uint32_t trace_ns;
-};
 
 __host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return 3u * stack_cap + 4u * kLeafCap; }
-constexpr uint32_t kNarrowWarpWords = 5u * 32u + 1u;
+constexpr uint32_t kNarrowWarpWords = 5u * 32u + 1u;  // a narrow block: 32 leaf pairs + prefix sums
 
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,

@@ -245,6 +245,31 @@ __device__ unsigned wait_ready(const TraverseParams& P, uint32_t slot) {
     }
 }
 
+// Lane 0: one look at slot `slot` (wait_ready without the wait): 1 with r =
+// its chunk size + 1 (2 for a root slot) when it can be read, 0 with r = 0
+// when all work finished, an error was raised or the wait limit (counted
+// from t0) passed, -1 when it is not ready yet.
+__device__ int poll_ready(const TraverseParams& P, uint32_t slot, unsigned long long t0, unsigned& r) {
+    r = 0;
+    if (slot < P.n_queries) {
+        r = 2u;
+        return 1;
+    }
+    const uint32_t idx = slot - P.n_queries;
+    if (idx < P.slot_alloc) {
+        r = ld_acquire(P.ready + idx);
+        if (r) return 1;
+    }
+    // past every slot a donor could publish, only the end of the work or an
+    // error releases the warp
+    if (all_done(P.ctr) || ld_relaxed(&P.ctr->error) != 0) return 0;
+    if (gtimer() - t0 > P.wait_ns) {
+        atomicOr(&P.ctr->error, ERR_TIMEOUT);
+        return 0;
+    }
+    return -1;
+}
+
 // Lane 0: claims a slot below the tail without waiting for new donations; a
 // slot below the tail is reserved, and its donor publishes it promptly.
 __device__ int try_claim(const TraverseParams& P, unsigned long long ht, uint32_t& slot) {
@@ -312,6 +337,124 @@ __device__ __forceinline__ unsigned long long trace_base(Counters* ctr) {
     return old ? old : now;
 }
 
+// The narrow phase of leaf pairs [first, first + nl) of the list (nl <= 32),
+// staged in `stage` (kNarrowWarpWords words); all 32 lanes call it. The
+// entries must be visible to the calling warp.
+__device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* stage, uint32_t first, uint32_t nl,
+                                             int lane, unsigned long long& tests, unsigned long long& fragile,
+                                             unsigned long long t_base) {
+    uint32_t* lq = stage;
+    uint32_t* loa = lq + 32;
+    uint32_t* lob = loa + 32;
+    uint32_t* lcn = lob + 32;
+    uint32_t* pre = lcn + 32;  // 33 entries
+    uint32_t c0 = 0;
+    if (uint32_t(lane) < nl) {
+        const uint4 e = P.leaf_list[first + lane];
+        lq[lane] = e.x;
+        loa[lane] = e.y;
+        lob[lane] = e.z;
+        lcn[lane] = e.w;
+        c0 = (e.w & 0xffffu) * (e.w >> 16);
+        if ((P.flags & CG_KEEP_LEAF_PAIRS) && first + lane < P.leafs_cap) {
+            const PackedQuery* Q = P.q + e.x;
+            cg_leaf_pair lp;
+            lp.query = e.x;
+            lp.offset_a = e.y - __ldg(&Q->tri_base_a);
+            lp.offset_b = e.z - __ldg(&Q->tri_base_b);
+            lp.count_a = uint16_t(e.w & 0xffffu);
+            lp.count_b = uint16_t(e.w >> 16);
+            P.leafs[first + lane] = lp;
+        }
+    }
+    uint32_t s0 = c0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t0 = __shfl_up_sync(kFull, s0, o);
+        if (lane >= o) s0 += t0;
+    }
+    const uint32_t total = (P.flags & CG_MID_ONLY) ? 0u : __shfl_sync(kFull, s0, 31);
+    pre[lane] = s0 - c0;
+    if (lane == 0) pre[32] = total;
+    __syncwarp();
+
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t t = base + lane;
+        int res = TT_MISS;
+        uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
+        float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
+        if (t < total) {
+            int lo = 0, hi = int(nl) - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (pre[mid] <= t)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const uint32_t local = t - pre[lo];
+            const uint32_t cn = lcn[lo];
+            const uint32_t cb = cn >> 16;
+            const uint32_t i = local / cb;
+            const uint32_t j = local - i * cb;
+            q = lq[lo];
+            leaf_i = first + uint32_t(lo);
+            ia = loa[lo] + i;
+            ib = lob[lo] + j;
+            const Mat4 M = load_mat(P.q + q);
+            float3 a0, a1, a2, b0, b1, b2;
+            load_tri(P.tris, ia, a0, a1, a2);
+            load_tri(P.tris, ib, b0, b1, b2);
+            b0 = xform(M, b0, 1.0f);
+            b1 = xform(M, b1, 1.0f);
+            b2 = xform(M, b2, 1.0f);
+            res = tri_tri(a0, a1, a2, b0, b1, b2, src, tgt);
+        }
+        const unsigned hitmask = __ballot_sync(kFull, res == TT_HIT);
+        const unsigned fragmask = __ballot_sync(kFull, res == TT_FRAGILE);
+        if (hitmask) {
+            unsigned long long obase = 0;
+            if (lane == 0) obase = atomicAdd(&P.ctr->n_pairs, (unsigned long long)__popc(hitmask));
+            obase = __shfl_sync(kFull, obase, 0);
+            if (res == TT_HIT && !(P.flags & CG_NO_TRI_PAIRS)) {
+                const unsigned long long o = obase + __popc(hitmask & lanemask_lt());
+                if (o < P.pairs_cap) {
+                    const PackedQuery* Q = P.q + q;
+                    cg_tri_pair r;
+                    r.query = q;
+                    r.tri_a = ia - __ldg(&Q->tri_base_a);
+                    r.tri_b = ib - __ldg(&Q->tri_base_b);
+                    r.source[0] = src.x;
+                    r.source[1] = src.y;
+                    r.source[2] = src.z;
+                    r.target[0] = tgt.x;
+                    r.target[1] = tgt.y;
+                    r.target[2] = tgt.z;
+                    P.pairs[o] = r;
+                    if (P.pair_aux) P.pair_aux[o] = make_uint4(ia, ib, leaf_i, q);
+                }
+            }
+        }
+        if (lane == 0) {
+            fragile += __popc(fragmask);
+            if (P.trace) trace_add(P.trace, P.trace_ns, t_base, 2, min(32u, total - base));
+        }
+    }
+    if (lane == 0) tests += total;
+    __syncwarp();
+}
+
+// Appends the warp's buffered leaf pairs to the list.
+__device__ __forceinline__ void flush_leafs(const TraverseParams& P, const uint32_t* lq, const uint32_t* loa,
+                                            const uint32_t* lob, const uint32_t* lcn, uint32_t nl, int lane) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&P.ctr->n_leafs, (unsigned long long)nl);
+    base = __shfl_sync(kFull, base, 0);
+    for (uint32_t e = lane; e < nl; e += 32)
+        if (base + e < P.leaf_cap) P.leaf_list[base + e] = make_uint4(lq[e], loa[e], lob[e], lcn[e]);
+    __syncwarp();
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P) {
@@ -337,16 +480,30 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
 
     for (;;) {
         if (top == bot) {
-            // Out of work: claim the next slot and wait for it.
+            // Out of work: claim the next slot and wait for it (the whole
+            // warp polls; lane 0 looks and sleeps between looks).
             uint32_t slot = 0;
+            if (lane == 0) slot = ht_head(atomicAdd(ht, 1ull));
+            slot = __shfl_sync(kFull, slot, 0);
             unsigned r = 0;
-            if (lane == 0) {
-                slot = ht_head(atomicAdd(ht, 1ull));
-                r = wait_ready(P, slot);
+            unsigned long long t0 = 0;
+            unsigned ns = 32;
+            for (;;) {
+                int st = 0;
+                if (lane == 0) {
+                    if (!t0) t0 = gtimer();
+                    st = poll_ready(P, slot, t0, r);
+                }
+                st = __shfl_sync(kFull, st, 0);
+                if (st >= 0) break;
+                if (lane == 0) {
+                    __nanosleep(ns);
+                    if (ns < 1024) ns <<= 1;
+                }
+                __syncwarp();
             }
             r = __shfl_sync(kFull, r, 0);
             if (!r) break;
-            slot = __shfl_sync(kFull, slot, 0);
             top += take_chunk(P, slot, r, D, top, lane);
             held_tasks = 1;
         }
@@ -481,13 +638,8 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
         __syncwarp();
 
         if (nl >= P.leaf_flush) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(&P.ctr->n_leafs, (unsigned long long)nl);
-            base = __shfl_sync(kFull, base, 0);
-            for (uint32_t e = lane; e < nl; e += 32)
-                if (base + e < P.leaf_cap) P.leaf_list[base + e] = make_uint4(lq[e], loa[e], lob[e], lcn[e]);
+            flush_leafs(P, lq, loa, lob, lcn, nl, lane);
             nl = 0;
-            __syncwarp();
         }
 
         // ---- balance: give chunks from the bottom of the deque to the warps
@@ -552,13 +704,7 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
     }
 
     // remaining buffered leaf pairs
-    if (nl) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&P.ctr->n_leafs, (unsigned long long)nl);
-        base = __shfl_sync(kFull, base, 0);
-        for (uint32_t e = lane; e < nl; e += 32)
-            if (base + e < P.leaf_cap) P.leaf_list[base + e] = make_uint4(lq[e], loa[e], lob[e], lcn[e]);
-    }
+    if (nl) flush_leafs(P, lq, loa, lob, lcn, nl, lane);
     if (lane == 0) {
         atomicAdd(&P.ctr->node_pairs, st_nodes);
         atomicAdd(&P.ctr->donations, st_don);
@@ -574,11 +720,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
     __shared__ uint32_t sm[8 * kNarrowWarpWords];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    uint32_t* lq = sm + warp * kNarrowWarpWords;
-    uint32_t* loa = lq + 32;
-    uint32_t* lob = loa + 32;
-    uint32_t* lcn = lob + 32;
-    uint32_t* pre = lcn + 32;  // 33 entries
+    uint32_t* stage = sm + warp * kNarrowWarpWords;
 
     const unsigned long long n_all = *reinterpret_cast<volatile unsigned long long*>(&P.ctr->n_leafs);
     const uint32_t n = uint32_t(n_all < P.leaf_cap ? n_all : P.leaf_cap);
@@ -587,107 +729,12 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
     if (P.trace && lane == 0) t_base = trace_base(P.ctr);
 
     for (;;) {
-        uint32_t blk = 0;
-        if (lane == 0) blk = atomicAdd(&P.ctr->narrow_next, 1u);
-        blk = __shfl_sync(kFull, blk, 0);
-        const uint64_t first = uint64_t(blk) * 32u;
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(&P.ctr->narrow_lp, 32u);
+        first = __shfl_sync(kFull, first, 0);
         if (first >= n) break;
-        const uint32_t nl = uint32_t(min(uint64_t(32), n - first));
-
-        uint32_t c0 = 0;
-        if (uint32_t(lane) < nl) {
-            const uint4 e = P.leaf_list[first + lane];
-            lq[lane] = e.x;
-            loa[lane] = e.y;
-            lob[lane] = e.z;
-            lcn[lane] = e.w;
-            c0 = (e.w & 0xffffu) * (e.w >> 16);
-            if ((P.flags & CG_KEEP_LEAF_PAIRS) && first + lane < P.leafs_cap) {
-                const PackedQuery* Q = P.q + e.x;
-                cg_leaf_pair lp;
-                lp.query = e.x;
-                lp.offset_a = e.y - __ldg(&Q->tri_base_a);
-                lp.offset_b = e.z - __ldg(&Q->tri_base_b);
-                lp.count_a = uint16_t(e.w & 0xffffu);
-                lp.count_b = uint16_t(e.w >> 16);
-                P.leafs[first + lane] = lp;
-            }
-        }
-        uint32_t s0 = c0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t0 = __shfl_up_sync(kFull, s0, o);
-            if (lane >= o) s0 += t0;
-        }
-        const uint32_t total = (P.flags & CG_MID_ONLY) ? 0u : __shfl_sync(kFull, s0, 31);
-        pre[lane] = s0 - c0;
-        if (lane == 0) pre[32] = total;
-        __syncwarp();
-
-        for (uint32_t base = 0; base < total; base += 32) {
-            const uint32_t t = base + lane;
-            int res = TT_MISS;
-            uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
-            float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
-            if (t < total) {
-                int lo = 0, hi = int(nl) - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (pre[mid] <= t)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                const uint32_t local = t - pre[lo];
-                const uint32_t cn = lcn[lo];
-                const uint32_t cb = cn >> 16;
-                const uint32_t i = local / cb;
-                const uint32_t j = local - i * cb;
-                q = lq[lo];
-                leaf_i = uint32_t(first) + uint32_t(lo);
-                ia = loa[lo] + i;
-                ib = lob[lo] + j;
-                const Mat4 M = load_mat(P.q + q);
-                float3 a0, a1, a2, b0, b1, b2;
-                load_tri(P.tris, ia, a0, a1, a2);
-                load_tri(P.tris, ib, b0, b1, b2);
-                b0 = xform(M, b0, 1.0f);
-                b1 = xform(M, b1, 1.0f);
-                b2 = xform(M, b2, 1.0f);
-                res = tri_tri(a0, a1, a2, b0, b1, b2, src, tgt);
-            }
-            const unsigned hitmask = __ballot_sync(kFull, res == TT_HIT);
-            const unsigned fragmask = __ballot_sync(kFull, res == TT_FRAGILE);
-            if (hitmask) {
-                unsigned long long obase = 0;
-                if (lane == 0) obase = atomicAdd(&P.ctr->n_pairs, (unsigned long long)__popc(hitmask));
-                obase = __shfl_sync(kFull, obase, 0);
-                if (res == TT_HIT && !(P.flags & CG_NO_TRI_PAIRS)) {
-                    const unsigned long long o = obase + __popc(hitmask & lanemask_lt());
-                    if (o < P.pairs_cap) {
-                        const PackedQuery* Q = P.q + q;
-                        cg_tri_pair r;
-                        r.query = q;
-                        r.tri_a = ia - __ldg(&Q->tri_base_a);
-                        r.tri_b = ib - __ldg(&Q->tri_base_b);
-                        r.source[0] = src.x;
-                        r.source[1] = src.y;
-                        r.source[2] = src.z;
-                        r.target[0] = tgt.x;
-                        r.target[1] = tgt.y;
-                        r.target[2] = tgt.z;
-                        P.pairs[o] = r;
-                        if (P.pair_aux) P.pair_aux[o] = make_uint4(ia, ib, leaf_i, q);
-                    }
-                }
-            }
-            if (lane == 0) {
-                fragile += __popc(fragmask);
-                if (P.trace) trace_add(P.trace, P.trace_ns, t_base, 2, min(32u, total - base));
-            }
-        }
-        if (lane == 0) tests += total;
-        __syncwarp();
+        const uint32_t nl = min(32u, n - first);
+        narrow_block(P, stage, first, nl, lane, tests, fragile, t_base);
     }
     if (lane == 0) {
         atomicAdd(&P.ctr->tri_tests, tests);
