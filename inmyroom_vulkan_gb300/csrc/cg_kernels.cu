@@ -33,6 +33,7 @@ namespace cg {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr unsigned kPollSleepMaxNs = 256;  // longest sleep of a waiting warp between two looks at its slot
 
 __device__ __forceinline__ unsigned long long gtimer() {
     unsigned long long t;
@@ -498,7 +499,7 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
                 if (st >= 0) break;
                 if (lane == 0) {
                     __nanosleep(ns);
-                    if (ns < 1024) ns <<= 1;
+                    if (ns < kPollSleepMaxNs) ns <<= 1;
                 }
                 __syncwarp();
             }
