@@ -47,6 +47,7 @@ TRI_TEST_BYTES = 2 * 36    # two triangles
 NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
 TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
 COUNTERS_BYTES = 112       # the launch counters, read back by cg_collide and by each result read
+STEP_KERNELS = 6           # init, pack, traverse, narrow, contacts_accumulate, contacts_emit
 
 
 def measured_peaks() -> dict:
@@ -56,6 +57,21 @@ def measured_peaks() -> dict:
             d = json.load(f)
         return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "sm_max_mhz": d.get("sm_max_mhz", 2070.0), "source": "measured"}
     return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary
+    (profiles/<kernel>_scene256.md, the row marked 'traffic per launch'), or
+    None when there is none."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_scene256.md")
+    if not os.path.exists(path):
+        return None
+    scale = {"B": 1, "KB": 1e3, "MB": 1e6, "GB": 1e9}
+    for line in open(path):
+        if "traffic per launch" in line:
+            cell = line.split("|")[2].split()
+            return int(float(cell[0]) * scale[cell[1]])
+    return None
 
 
 class ClockSampler:
@@ -129,7 +145,7 @@ def cpu_baseline(sc, seconds: float = 10.0) -> dict:
         steps += 1
         tests += r["tests"]
         el = time.perf_counter() - t0
-        if el >= seconds or steps >= 200:
+        if el >= seconds or steps >= 5000:
             break
     t1 = time.perf_counter()
     r1 = fast.collide_batch(ta, tb, ma, mb, threads=1)
@@ -269,7 +285,7 @@ def run_gpu(args) -> dict:
         by, fl = units * unit_bytes, units * unit_flops
         ach = by / (ms / 1e3) / 1e9
         return {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": ach / peaks["hbm_gbs"], "traffic": None, "kernel": name, "kernel_ms": ms,
+                "frac": ach / peaks["hbm_gbs"], "traffic": profiled_traffic(name), "kernel": name, "kernel_ms": ms,
                 "algorithmic_bytes": int(by), "peak_source": peaks["source"],
                 "fp32": {"achieved_tflops": fl / (ms / 1e3) / 1e12, "peak_tflops": fp32_peak,
                          "frac": fl / (ms / 1e3) / 1e12 / fp32_peak}}
@@ -316,7 +332,7 @@ def run_gpu(args) -> dict:
                    "contacts_per_step": int(st["contacts"]), "rays_per_step": int(rays_per_step),
                    "node_pairs_per_step": int(st["node_pairs"]), "cache": "L2 flushed (512 MB write) between steps",
                    "launch": "CUDA graph: init + pack + persistent traversal + persistent narrow phase + "
-                             "5 contact/ray kernels",
+                             "contact accumulate + contact/ray emit",
                    "lanes_per_step": st["node_pairs"] / max(1, st["warp_steps"])},
         "queries_per_s": world * n * args.steps / (total_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * capi.QUERY_DTYPE.itemsize),
@@ -329,7 +345,7 @@ def run_gpu(args) -> dict:
         "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch (with contacts and rays)",
                   "queries_per_s": 200 / (plain_ms / 1e3), "tri_tests_per_s": ptests / (plain_ms / 1e3),
                   "ms_per_query": plain_ms / 200},
-        "gpu_launches": 9 * args.steps,
+        "gpu_launches": STEP_KERNELS * args.steps,
         "clocks": clk,
     }
     if cpu:

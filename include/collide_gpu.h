@@ -194,7 +194,7 @@ typedef struct cg_ray {
 
 /* Per query: average_point_first_modelspace and
  * average_point_second_modelspace of CDentriesUncollideRays
- * (CreateUncollideRays.cpp:240-258) and the ray counts. 32 bytes. */
+ * (CreateUncollideRays.cpp:183-198) and the ray counts. 32 bytes. */
 typedef struct cg_ray_average {
     float first[3];
     float second[3];

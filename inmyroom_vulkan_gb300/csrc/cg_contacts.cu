@@ -1,6 +1,6 @@
 // Contacts and uncollide rays on the device: the part of
 // CreateUncollideRays::ExecuteCreateUncollideRays
-// (src/CollisionDetection/CreateUncollideRays.cpp:60-258) that follows the
+// (src/CollisionDetection/CreateUncollideRays.cpp:60-201) that follows the
 // triangle-pair tests, for every query of a launch at once.
 //
 // The reference keeps one TriangleCandidateRays per triangle of a leaf pair,
@@ -21,7 +21,7 @@
 //                        131-178), vertex rays deduplicated per (side, query,
 //                        vertex index) through a set; the slot is emptied.
 //                        The last block to finish computes the per-query mean
-//                        origins (CreateUncollideRays.cpp:240-258).
+//                        origins (CreateUncollideRays.cpp:183-198).
 //
 // Appends to the shared lists (contacts, vertices, rays) take one atomic per
 // warp. Geometry uses the reference's arithmetic (no contraction, IEEE division and
@@ -207,7 +207,7 @@ struct PairGeom {
     unsigned mask_a, mask_b;
 };
 
-// CreateUncollideRays.cpp:148-172 for pair i: the second triangle is moved
+// CreateUncollideRays.cpp:87-112 for pair i: the second triangle is moved
 // into the first tree's space, each triangle's vertices are tested against
 // the other's plane, w = |source - target| and mid = w * (source + target) / 2.
 // The pair record and its side record load together, then the matrix and

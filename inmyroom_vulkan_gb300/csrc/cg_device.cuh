@@ -147,7 +147,7 @@ __device__ __forceinline__ bool interval(float3 x0, float3 x1, float3 x2, float 
 enum : int { TT_MISS = 0, TT_HIT = 1, TT_COPLANAR = 2, TT_FRAGILE = 3 };
 
 // tri_tri_intersect_with_isectline (Triangle.cpp:866-1003). TT_HIT means
-// doIntersept && !areCoplanar (the pairs CreateUncollideRays.cpp:148 keeps);
+// doIntersept && !areCoplanar (the pairs CreateUncollideRays.cpp:88 keeps);
 // TT_COPLANAR covers every coplanar outcome (never kept); TT_FRAGILE is the
 // case where the second interval degenerates (U's distances all zero while V's
 // are not), in which the reference reads uninitialised values: it is defined

@@ -715,7 +715,7 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
 
 // Runs the triangle pairs of the leaf-pair list, 32 leaf pairs per warp and
 // one triangle pair per lane, in the order of the reference's pair loop per
-// leaf pair (CreateUncollideRays.cpp:139-148): B's triangle is moved into A's
+// leaf pair (CreateUncollideRays.cpp:78-86): B's triangle is moved into A's
 // space with TrianglePosition::MultiplyBy4x4Matrix arithmetic, then tested.
 __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
     __shared__ uint32_t sm[8 * kNarrowWarpWords];

@@ -636,7 +636,7 @@ struct Narrow {
 };
 
 // The pair loop of CreateUncollideRays::ExecuteCreateUncollideRays
-// (CreateUncollideRays.cpp:134-188): every (i, j) of every candidate leaf
+// (CreateUncollideRays.cpp:74-127): every (i, j) of every candidate leaf
 // pair, B's triangle re-transformed per pair; colliding = hit and not
 // coplanar; contacts accumulated per leaf pair, then merged per triangle in
 // leaf-pair order.

@@ -194,7 +194,7 @@ void ref_mid_get(void* rp, uint32_t* out) {
     }
 }
 
-// The narrow-phase pair loop of CreateUncollideRays.cpp:134-148, calling the
+// The narrow-phase pair loop of CreateUncollideRays.cpp:74-115, calling the
 // reference's own transform and Moller test per pair, collecting the pairs
 // that count as colliding (doIntersept && !areCoplanar) with their segment.
 // Returns the number of colliding pairs (writes at most cap); *tests receives

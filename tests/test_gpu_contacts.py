@@ -1,6 +1,6 @@
 """GPU contacts and uncollide rays (CG_CONTACTS) against the oracle's
 restatement of CreateUncollideRays::ExecuteCreateUncollideRays
-(src/CollisionDetection/CreateUncollideRays.cpp:60-258).
+(src/CollisionDetection/CreateUncollideRays.cpp:60-201).
 
 Bit for bit: the set of contact triangles per (query, side), their "vertex
 not outside" masks, the ray counts and every ray that starts at a vertex.
