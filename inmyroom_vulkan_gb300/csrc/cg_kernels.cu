@@ -171,40 +171,6 @@ __device__ __forceinline__ void sat_two(const Box& a0, const Box& b0, const Box&
     ok1 = al1;
 }
 
-// The 15 axes of cg::sat in the same order and with the same arithmetic, three
-// independent axes per round (a's faces, b's faces, a_u x b_*, a_v x b_*,
-// a_w x b_*); the verdict is the conjunction, so it is identical.
-__device__ __forceinline__ bool sat_grouped(const Box& a, const Box& b) {
-#pragma unroll 1
-    for (int g = 0; g < 5; ++g) {
-        float3 x0, y0, x1, y1, x2, y2;
-        if (g < 2) {
-            const float3 u = g ? b.u : a.u;
-            const float3 v = g ? b.v : a.v;
-            const float3 w = g ? b.w : a.w;
-            x0 = v;
-            y0 = w;
-            x1 = u;
-            y1 = w;
-            x2 = u;
-            y2 = v;
-        } else {
-            const float3 e = g == 2 ? a.u : (g == 3 ? a.v : a.w);
-            x0 = e;
-            y0 = b.u;
-            x1 = e;
-            y1 = b.v;
-            x2 = e;
-            y2 = b.w;
-        }
-        const bool ok0 = overlap_on(a, b, cross3(x0, y0));
-        const bool ok1 = overlap_on(a, b, cross3(x1, y1));
-        const bool ok2 = overlap_on(a, b, cross3(x2, y2));
-        if (!(ok0 & ok1 & ok2)) return false;
-    }
-    return true;
-}
-
 struct Deque {
     uint32_t* q;
     uint32_t* a;
