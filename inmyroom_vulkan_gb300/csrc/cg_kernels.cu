@@ -171,6 +171,58 @@ __device__ __forceinline__ void sat_two(const Box& a0, const Box& b0, const Box&
     ok1 = al1;
 }
 
+// Rounds [g0, g1) of one SAT, stopping at the first separating round.
+__device__ __forceinline__ bool sat_rounds(const Box& a, const Box& b, int g0, int g1) {
+    bool ok = true;
+#pragma unroll 1
+    for (int g = g0; g < g1 && ok; ++g) ok = sat_round(a, b, g);
+    return ok;
+}
+
+// The reference descent rule (OBBtree.cpp:414-476) for a child pair whose
+// boxes overlap: split the inner node with the larger box surface (the first
+// tree's on ties), else the inner one, or report a leaf pair. C is the child
+// record (record rc) of the split node, O the other box (record io), bx the
+// child pair's box of the second tree as transformed for the SAT.
+__device__ __forceinline__ void descend(const TraverseParams& P, bool sideB, const Rec& O, const Rec& C, uint32_t rc,
+                                        uint32_t io, uint32_t qi, const Box& bx, bool& item, bool& leaf,
+                                        uint32_t& out_q, uint32_t& out_s, uint32_t& out_o) {
+    const uint32_t a_ref = sideB ? O.ref : C.ref;
+    const uint32_t a_meta = sideB ? O.meta : C.meta;
+    const float a_surf = sideB ? O.surf : C.surf;
+    const uint32_t b_ref = sideB ? C.ref : O.ref;
+    const uint32_t b_meta = sideB ? C.meta : O.meta;
+    const uint32_t ra = sideB ? io : rc;
+    const uint32_t rb = sideB ? rc : io;
+    const bool la = (a_meta & kLeafFlag) != 0;
+    const bool lb = (b_meta & kLeafFlag) != 0;
+    int act;  // 1: split A, 2: split B, 3: leaf pair
+    if (!la && !lb)
+        act = (a_surf >= surface(bx)) ? 1 : 2;
+    else if (la && !lb)
+        act = 2;
+    else if (!la && lb)
+        act = 1;
+    else
+        act = 3;
+    if (act == 3) {
+        // leaf pair: first triangles of both leaves, counts packed
+        leaf = true;
+        out_s = a_ref;
+        out_o = b_ref;
+        out_q = (a_meta & 0xffffu) | ((b_meta & 0xffffu) << 16);
+    } else {
+        item = true;
+        const uint32_t split = act == 1 ? a_ref : b_ref;
+        out_q = act == 1 ? qi : (qi | kItemSideB);
+        out_s = split;
+        out_o = act == 1 ? rb : ra;
+        // the split node's two child records share one 128-byte line: fetch
+        // it into L1 for the step that tests them
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(P.recs + 4ull * split));
+    }
+}
+
 struct Deque {
     uint32_t* q;
     uint32_t* a;
@@ -482,14 +534,20 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
         // ---- one step over up to 32 items from the top of the deque. An item
         // tests both children of a split node against the other box: the
         // other record is loaded (and, for the second tree, transformed) once,
-        // the two child records come from one 128-byte line, and the two SATs
-        // run side by side.
+        // the two child records come from one 128-byte line. With more than
+        // 16 items a lane runs an item's two SATs side by side; with 9..16 two
+        // lanes share an item (one child each), with up to 8 four lanes (each
+        // a part of one child's 15 axes), so that a step with few items takes
+        // less time. Every verdict is the conjunction of the same 15 axes.
         const uint32_t size = top - bot;
         const uint32_t n = size < 32u ? size : 32u;
-        const bool active = uint32_t(lane) < n;
+        const uint32_t lg = n <= 8u ? 2u : (n <= 16u ? 1u : 0u);  // log2 of lanes per item
+        const uint32_t slot_i = uint32_t(lane) >> lg;
+        const uint32_t sub = uint32_t(lane) & ((1u << lg) - 1u);
+        const bool active = slot_i < n;
         uint32_t iq = 0, is = 0, io = 0;
         if (active) {
-            const uint32_t pos = (top - n + lane) & D.mask;
+            const uint32_t pos = (top - n + slot_i) & D.mask;
             iq = D.q[pos];
             is = D.a[pos];
             io = D.b[pos];
@@ -502,66 +560,47 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
         bool item[2] = {false, false}, leaf[2] = {false, false};
         uint32_t out_q[2] = {0, 0}, out_s[2] = {0, 0}, out_o[2] = {0, 0};
         const uint32_t qi = iq & ~kItemSideB;
-        if (active) {
-            const bool sideB = (iq & kItemSideB) != 0;
-            const Mat4 M = load_mat(P.q + qi);
-            const Rec O = load_rec(P.recs, io);
-            const Rec C0 = load_rec(P.recs, is);
-            const Rec C1 = load_rec(P.recs, is + 1u);
-            Box a0, a1, b0, b1;
-            if (sideB) {
-                a0 = O.box;
-                a1 = O.box;
-                b0 = xform_box(M, C0.box);
-                b1 = xform_box(M, C1.box);
-            } else {
-                a0 = C0.box;
-                a1 = C1.box;
-                b0 = xform_box(M, O.box);
-                b1 = b0;
-            }
-            bool ok[2] = {true, true};
-            sat_two(a0, b0, a1, b1, ok[0], ok[1]);
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                if (!ok[k]) continue;
-                const Rec& C = k ? C1 : C0;
-                const uint32_t rc = is + uint32_t(k);
-                const uint32_t a_ref = sideB ? O.ref : C.ref;
-                const uint32_t a_meta = sideB ? O.meta : C.meta;
-                const float a_surf = sideB ? O.surf : C.surf;
-                const uint32_t b_ref = sideB ? C.ref : O.ref;
-                const uint32_t b_meta = sideB ? C.meta : O.meta;
-                const uint32_t ra = sideB ? io : rc;
-                const uint32_t rb = sideB ? rc : io;
-                const bool la = (a_meta & kLeafFlag) != 0;
-                const bool lb = (b_meta & kLeafFlag) != 0;
-                int act;  // 1: split A, 2: split B, 3: leaf pair
-                if (!la && !lb)
-                    act = (a_surf >= surface(k ? b1 : b0)) ? 1 : 2;
-                else if (la && !lb)
-                    act = 2;
-                else if (!la && lb)
-                    act = 1;
-                else
-                    act = 3;
-                if (act == 3) {
-                    // leaf pair: first triangles of both leaves, counts packed
-                    leaf[k] = true;
-                    out_s[k] = a_ref;
-                    out_o[k] = b_ref;
-                    out_q[k] = (a_meta & 0xffffu) | ((b_meta & 0xffffu) << 16);
+        const bool sideB = (iq & kItemSideB) != 0;
+        if (lg == 0u) {
+            if (active) {
+                const Mat4 M = load_mat(P.q + qi);
+                const Rec O = load_rec(P.recs, io);
+                const Rec C0 = load_rec(P.recs, is);
+                const Rec C1 = load_rec(P.recs, is + 1u);
+                Box a0, a1, b0, b1;
+                if (sideB) {
+                    a0 = O.box;
+                    a1 = O.box;
+                    b0 = xform_box(M, C0.box);
+                    b1 = xform_box(M, C1.box);
                 } else {
-                    item[k] = true;
-                    const uint32_t split = act == 1 ? a_ref : b_ref;
-                    out_q[k] = act == 1 ? qi : (qi | kItemSideB);
-                    out_s[k] = split;
-                    out_o[k] = act == 1 ? rb : ra;
-                    // the split node's two child records share one 128-byte
-                    // line: fetch it into L1 for the step that tests them
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(P.recs + 4ull * split));
+                    a0 = C0.box;
+                    a1 = C1.box;
+                    b0 = xform_box(M, O.box);
+                    b1 = b0;
                 }
+                bool ok[2] = {true, true};
+                sat_two(a0, b0, a1, b1, ok[0], ok[1]);
+                if (ok[0]) descend(P, sideB, O, C0, is, io, qi, b0, item[0], leaf[0], out_q[0], out_s[0], out_o[0]);
+                if (ok[1]) descend(P, sideB, O, C1, is + 1u, io, qi, b1, item[1], leaf[1], out_q[1], out_s[1], out_o[1]);
             }
+        } else {
+            const uint32_t kc = sub & 1u;    // the child this lane tests
+            const uint32_t part = sub >> 1;  // with four lanes: rounds 0..2 or 3..4 of its SAT
+            bool ok = false;
+            Rec O, C;
+            Box bx;
+            if (active) {
+                const Mat4 M = load_mat(P.q + qi);
+                O = load_rec(P.recs, io);
+                C = load_rec(P.recs, is + kc);
+                const Box ax = sideB ? O.box : C.box;
+                bx = xform_box(M, sideB ? C.box : O.box);
+                ok = lg == 1u ? sat_rounds(ax, bx, 0, 5) : sat_rounds(ax, bx, part ? 3 : 0, part ? 5 : 3);
+            }
+            if (lg == 2u) ok = ok & (__shfl_xor_sync(kFull, ok ? 1 : 0, 2) != 0);
+            if (active && ok && part == 0u)
+                descend(P, sideB, O, C, is + kc, io, qi, bx, item[0], leaf[0], out_q[0], out_s[0], out_o[0]);
         }
 
         const unsigned i0 = __ballot_sync(kFull, item[0]), i1 = __ballot_sync(kFull, item[1]);
