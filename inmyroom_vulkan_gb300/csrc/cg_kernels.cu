@@ -230,42 +230,8 @@ struct Deque {
     uint32_t mask;
 };
 
-// Lane 0: waits until slot `slot` can be read. Returns its chunk size + 1 for
-// a donated slot, 2 for a root slot (one pair), 0 when all work finished, an
-// error was raised, or the wait limit passed.
-__device__ unsigned wait_ready(const TraverseParams& P, uint32_t slot) {
-    if (slot < P.n_queries) return 2u;
-    const uint32_t idx = slot - P.n_queries;
-    const unsigned long long t0 = gtimer();
-    if (idx >= P.slot_alloc) {
-        // Past every slot a donor could publish: only the end of the work or
-        // an error can release this warp.
-        while (!all_done(P.ctr) && ld_relaxed(&P.ctr->error) == 0) {
-            if (gtimer() - t0 > P.wait_ns) {
-                atomicOr(&P.ctr->error, ERR_TIMEOUT);
-                break;
-            }
-            __nanosleep(1024);
-        }
-        return 0u;
-    }
-    unsigned ns = 32;
-    for (;;) {
-        const unsigned r = ld_acquire(P.ready + idx);
-        if (r) return r;
-        if (all_done(P.ctr)) return 0u;
-        if (ld_relaxed(&P.ctr->error) != 0) return 0u;
-        if (gtimer() - t0 > P.wait_ns) {
-            atomicOr(&P.ctr->error, ERR_TIMEOUT);
-            return 0u;
-        }
-        __nanosleep(ns);
-        if (ns < 1024) ns <<= 1;
-    }
-}
-
-// Lane 0: one look at slot `slot` (wait_ready without the wait): 1 with r =
-// its chunk size + 1 (2 for a root slot) when it can be read, 0 with r = 0
+// Lane 0: one look at slot `slot`: 1 with r = its chunk size + 1 (2 for a
+// root slot) when it can be read, 0 with r = 0
 // when all work finished, an error was raised or the wait limit (counted
 // from t0) passed, -1 when it is not ready yet.
 __device__ int poll_ready(const TraverseParams& P, uint32_t slot, unsigned long long t0, unsigned& r) {
@@ -289,24 +255,8 @@ __device__ int poll_ready(const TraverseParams& P, uint32_t slot, unsigned long 
     return -1;
 }
 
-// Lane 0: claims a slot below the tail without waiting for new donations; a
-// slot below the tail is reserved, and its donor publishes it promptly.
-__device__ int try_claim(const TraverseParams& P, unsigned long long ht, uint32_t& slot) {
-    unsigned long long* w = ht_of(P.ctr);
-    for (int tries = 0; tries < 4; ++tries) {
-        if (int(ht_tail(ht) - ht_head(ht)) <= 0) return 0;
-        const unsigned long long prev = atomicCAS(w, ht, ht + 1ull);
-        if (prev == ht) {
-            slot = ht_head(ht);
-            return 1;
-        }
-        ht = prev;
-    }
-    return 0;
-}
-
 // Copies the chunk of slot `slot` into the deque at `top` (all lanes); `r` is
-// wait_ready's value. Returns the number of node pairs added.
+// poll_ready's value. Returns the number of node pairs added.
 __device__ uint32_t take_chunk(const TraverseParams& P, uint32_t slot, unsigned r, const Deque& D, uint32_t top,
                                int lane) {
     // Lane 0 observed the slot's release; the barrier orders the other lanes'
@@ -650,13 +600,13 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
 
         // ---- balance: give chunks from the bottom of the deque to the warps
         // that wait (one chunk per waiting warp, up to 8, keeping at least a
-        // chunk; a full chunk when the deque is nearly full), or top up from
-        // reserved chunks when fewer than 32 node pairs are left.
+        // chunk; a full chunk when the deque is nearly full). A warp does not
+        // take queued chunks while it has work: that costs a contended atomic
+        // per step and measured slower.
         const uint32_t held = top - bot;
         const bool forced = held + 64u > S;
-        int mode = 0;  // 1: donate nch chunks of c, 2: top up from slot
+        int mode = 0;  // 1: donate nch chunks of c
         uint32_t c = 0, nch = 0, slot = 0;
-        unsigned rr = 0;
         if (lane == 0) {
             const int waiting = int(ht_head(qs) - ht_tail(qs));
             if (forced || (waiting > 0 && held >= P.donate_min)) {
@@ -669,11 +619,6 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
                 } else if (forced) {
                     atomicOr(&P.ctr->error, ERR_QUEUE);
                     mode = -1;
-                }
-            } else if (held < 32u && held > 0u && waiting <= 0) {
-                if (try_claim(P, qs, slot)) {
-                    rr = wait_ready(P, slot);
-                    mode = rr ? 2 : -1;
                 }
             }
         }
@@ -696,11 +641,6 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
             if (lane == 0) st_don += c * nch;
             bot += c * nch;
             __syncwarp();
-        } else if (mode == 2) {
-            rr = __shfl_sync(kFull, rr, 0);
-            slot = __shfl_sync(kFull, slot, 0);
-            top += take_chunk(P, slot, rr, D, top, lane);
-            ++held_tasks;
         }
 
         if (top == bot) {
