@@ -102,6 +102,7 @@ struct cg_ctx {
     cudaStream_t stream = nullptr;
     uint32_t blocks = 0;         // persistent traversal grid
     uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
+    uint32_t accumulate_blocks = 0, emit_blocks = 0;  // contact kernels: one resident wave
 
     // trees
     struct Slot {
@@ -273,6 +274,10 @@ int alloc_buffers(cg_ctx* c) {
     int nocc = 0;
     CG_CUDA(narrow_occupancy(8, &nocc), "occupancy");
     c->narrow_blocks = uint32_t(std::max(nocc, 1) * c->sm_count);
+    int aocc = 0, eocc = 0;
+    CG_CUDA(contacts_occupancy(&aocc, &eocc), "occupancy");
+    c->accumulate_blocks = uint32_t(std::max(aocc, 1) * c->sm_count);
+    c->emit_blocks = uint32_t(std::max(eocc, 1) * c->sm_count);
 
     CG_CUDA(cudaMalloc(&c->d_queries, sizeof(cg_query) * g.max_queries), "alloc queries");
     CG_CUDA(cudaMalloc(&c->d_packed, sizeof(PackedQuery) * g.max_queries), "alloc packed queries");
@@ -415,7 +420,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.sums = t.sums;
         cp.averages = t.averages;
         cp.ctr = c->d_ctr;
-        CG_CUDA(launch_contacts(cp, c->narrow_blocks, s), "contact kernels");
+        CG_CUDA(launch_contacts(cp, c->accumulate_blocks, c->emit_blocks, s), "contact kernels");
     }
     return CG_OK;
 }

@@ -365,145 +365,141 @@ __global__ void __launch_bounds__(256) contacts_accumulate_kernel(const ContactP
     }
 }
 
-// Rays of one contact, made in registers before they are appended.
-// Ray k of a contact sits in entry k (a vertex ray) or 0 (the weighted
-// average's ray); `live` has bit k set for each ray made.
-struct LaneRays {
-    float3 o[3], d[3];
-    uint32_t vs[3];   // vertex-set slots taken for vertex rays
-    unsigned live;
-    bool vertex;      // rays from vertices (they take vertex-set entries)
-};
+// Three lanes per contact (lanes 0..29 of a warp, ten contacts per warp and
+// turn): lane k of a contact makes the ray of the contact's vertex k, and
+// lane 0 also writes the contact record and, when no vertex is "not outside",
+// the ray from the weighted average.
+constexpr uint32_t kContactsPerWarp = 10;
 
-__global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams P) {
+__global__ void __launch_bounds__(256, 3) contacts_emit_kernel(const ContactParams P) {
     __shared__ bool last_block;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr->prev_vertices = 0u;  // the accumulate kernel emptied them
     const uint32_t n = P.ctr->n_contacts;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = tid & ~31u; base < n; base += stride) {
-        const uint32_t j = base + (threadIdx.x & 31u);
-        LaneRays R;
-        R.live = 0u;
-        R.vertex = false;
-        uint32_t q = 0, side = 0;
-        if (j < n) {
-            ContactSlot* s = P.table + P.occupied[j];
-            const unsigned long long key = s->key;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t k = lane % 3u;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t cb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kContactsPerWarp; cb < n;
+         cb += n_warps * kContactsPerWarp) {
+        const uint32_t j = cb + lane / 3u;
+        const bool valid = lane < 3u * kContactsPerWarp && j < n;
+        ContactSlot* s = nullptr;
+        unsigned long long key = 0;
+        double sx = 0, sy = 0, sz = 0, sw = 0;
+        unsigned mask = 0;
+        if (valid) {
+            s = P.table + P.occupied[j];
+            key = s->key;
+            sx = s->sx;
+            sy = s->sy;
+            sz = s->sz;
+            sw = s->sw;
+            mask = s->mask;
+        }
+        __syncwarp();  // the contact's three lanes have read the slot
+        bool ray = false, vertex = false;
+        float3 ro_ = make_float3(0.f, 0.f, 0.f), rd = ro_;
+        uint32_t vs = 0, q = 0, side = 0;
+        if (valid) {
             side = uint32_t(key >> 63);
             q = uint32_t(key >> 32) & 0x7fffffffu;
             const uint32_t tri = uint32_t(key);
-            const float3 wsum = make_float3(float(s->sx), float(s->sy), float(s->sz));
-            const float weight = float(s->sw);
-            const unsigned mask = s->mask;
-            s->sx = s->sy = s->sz = s->sw = 0.0;  // the slot is empty again for the next launch
-            s->mask = 7u;
-            s->key = kEmptyKey;
             // TriangleCandidateRays::GetWeightedAvg
-            const float3 avg = divs3(wsum, weight);
-            if (j < P.max_contacts) {
-                cg_contact c;
-                c.query = q;
-                c.side = side;
-                c.tri = tri;
-                c.mask = mask;
-                c.weighted_avg[0] = avg.x;
-                c.weighted_avg[1] = avg.y;
-                c.weighted_avg[2] = avg.z;
-                c.weight = weight;
-                P.contacts[j] = c;
-            }
-
-            const PackedQuery* Q = P.q + q;
-            const float* nrm = P.trees[side ? __ldg(&Q->tree_b) : __ldg(&Q->tree_a)].nrm;
-            const Mat4 M = query_mat(Q);
-            float3 p[3], n3[3];
-            uint32_t vi[3];
-            tri_at(P.tris, (side ? __ldg(&Q->tri_base_b) : __ldg(&Q->tri_base_a)) + tri, p, vi);
-            if (nrm) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const float* np = nrm + 9ull * tri + 3 * k;
-                    n3[k] = make_float3(__ldg(np), __ldg(np + 1), __ldg(np + 2));
+            const float3 avg = divs3(make_float3(float(sx), float(sy), float(sz)), float(sw));
+            if (k == 0) {
+                s->sx = s->sy = s->sz = s->sw = 0.0;  // the slot is empty again for the next launch
+                s->mask = 7u;
+                s->key = kEmptyKey;
+                if (j < P.max_contacts) {
+                    cg_contact c;
+                    c.query = q;
+                    c.side = side;
+                    c.tri = tri;
+                    c.mask = mask;
+                    c.weighted_avg[0] = avg.x;
+                    c.weighted_avg[1] = avg.y;
+                    c.weighted_avg[2] = avg.z;
+                    c.weight = float(sw);
+                    P.contacts[j] = c;
                 }
-            } else {  // a tree without vertex normals carries the face normal on all corners
-                n3[0] = n3[1] = n3[2] = face_normal(p[0], p[1], p[2]);
             }
-            if (side) {
+            const bool mine = mask != 0u ? (mask >> k) & 1u : k == 0;
+            if (mine) {
+                const PackedQuery* Q = P.q + q;
+                const float* nrm = P.trees[side ? __ldg(&Q->tree_b) : __ldg(&Q->tree_a)].nrm;
+                const Mat4 M = query_mat(Q);
+                float3 p[3], n3[3];
+                uint32_t vi[3];
+                tri_at(P.tris, (side ? __ldg(&Q->tri_base_b) : __ldg(&Q->tri_base_a)) + tri, p, vi);
+                if (nrm) {
 #pragma unroll
-                for (int k = 0; k < 3; ++k) p[k] = xform(M, p[k], 1.0f);
-            }
-            const Mat3 N = cofactor3(M);
-            if (mask != 0u) {
-                // the home-slot inserts of the (up to) three vertices go out together
-                const Probe V{P.vkeys, 1u, P.vtable_mask};
-                unsigned long long vk[3], cur[3];
-                uint32_t home[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    vk[k] = make_key(side, q, vi[k]);
-                    home[k] = V.home(vk[k]);
-                    cur[k] = (mask & (1u << k)) ? atomicCAS(V.at(home[k]), kEmptyKey, vk[k]) : 0ull;
+                    for (int c = 0; c < 3; ++c) {
+                        const float* np = nrm + 9ull * tri + 3 * c;
+                        n3[c] = make_float3(__ldg(np), __ldg(np + 1), __ldg(np + 2));
+                    }
+                } else {  // a tree without vertex normals carries the face normal on all corners
+                    n3[0] = n3[1] = n3[2] = face_normal(p[0], p[1], p[2]);
                 }
+                if (side) {
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (!(mask & (1u << k))) continue;
-                    uint32_t vs = 0;
-                    const int r = finish_insert(V, vk[k], cur[k], home[k], &vs);
+                    for (int c = 0; c < 3; ++c) p[c] = xform(M, p[c], 1.0f);
+                }
+                const Mat3 N = cofactor3(M);
+                if (mask != 0u) {
+                    // one ray per vertex index and side of the query
+                    const Probe V{P.vkeys, 1u, P.vtable_mask};
+                    const unsigned long long vk = make_key(side, q, k == 0 ? vi[0] : (k == 1 ? vi[1] : vi[2]));
+                    const uint32_t home = V.home(vk);
+                    const int r = finish_insert(V, vk, atomicCAS(V.at(home), kEmptyKey, vk), home, &vs);
                     if (r < 0) atomicOr(&P.ctr->c_overflow, CONTACT_VERTICES);
-                    if (r != 1) continue;  // this vertex already has its ray
-                    // TriangleNormal::GetNormal(index[, corrected_matrix]) (Triangle.cpp:180-195)
-                    const float3 nn = side ? normalize3(mul3(N, n3[k])) : normalize3(n3[k]);
-                    R.o[k] = p[k];
-                    R.d[k] = neg3(nn);
-                    R.vs[k] = vs;
-                    R.live |= 1u << k;
+                    if (r == 1) {
+                        // TriangleNormal::GetNormal(index[, corrected_matrix]) (Triangle.cpp:180-195)
+                        const float3 nk = k == 0 ? n3[0] : (k == 1 ? n3[1] : n3[2]);
+                        const float3 nn = side ? normalize3(mul3(N, nk)) : normalize3(nk);
+                        ro_ = k == 0 ? p[0] : (k == 1 ? p[1] : p[2]);
+                        rd = neg3(nn);
+                        ray = vertex = true;
+                    }
+                } else {
+                    // TrianglePosition::GetBarycentricOfPoint (Triangle.cpp:148-163) and
+                    // TriangleNormal::GetNormal(bary[, corrected_matrix]) (Triangle.cpp:197-212)
+                    const float3 v0 = sub3(p[1], p[0]), v1 = sub3(p[2], p[0]), v2 = sub3(avg, p[0]);
+                    const float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
+                    const float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
+                    const float den = d00 * d11 - d01 * d01;
+                    const float bx = (d11 * d20 - d01 * d21) / den;
+                    const float by = (d00 * d21 - d01 * d20) / den;
+                    const float b0 = 1.f - bx - by;
+                    const float3 in = add3(add3(scale3(b0, n3[0]), scale3(bx, n3[1])), scale3(by, n3[2]));
+                    const float3 nn = side ? normalize3(mul3(N, in)) : normalize3(in);
+                    ro_ = avg;
+                    rd = neg3(nn);
+                    ray = true;
                 }
-                R.vertex = true;
-            } else {
-                // TrianglePosition::GetBarycentricOfPoint (Triangle.cpp:148-163) and
-                // TriangleNormal::GetNormal(bary[, corrected_matrix]) (Triangle.cpp:197-212)
-                const float3 v0 = sub3(p[1], p[0]), v1 = sub3(p[2], p[0]), v2 = sub3(avg, p[0]);
-                const float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
-                const float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
-                const float den = d00 * d11 - d01 * d01;
-                const float bx = (d11 * d20 - d01 * d21) / den;
-                const float by = (d00 * d21 - d01 * d20) / den;
-                const float b0 = 1.f - bx - by;
-                const float3 in = add3(add3(scale3(b0, n3[0]), scale3(bx, n3[1])), scale3(by, n3[2]));
-                const float3 nn = side ? normalize3(mul3(N, in)) : normalize3(in);
-                R.o[0] = avg;
-                R.d[0] = neg3(nn);
-                R.live = 1u;
             }
         }
         __syncwarp();
-        const unsigned n_rays = __popc(R.live);
         unsigned vo, ro;
-        warp_append2(&P.ctr->n_vertices, R.vertex ? n_rays : 0u, n_rays, &vo, &ro);
-        double* sum = P.sums + 8ull * q + 4ull * side;
-#pragma unroll
-        for (unsigned k = 0; k < 3; ++k) {
-            if (!(R.live & (1u << k))) continue;
-            const unsigned below = __popc(R.live & ((1u << k) - 1u));
-            if (R.vertex) P.vocc[vo + below] = R.vs[k];  // never more entries than the set's slots
-            if (ro + below < P.max_rays) {
+        warp_append2(&P.ctr->n_vertices, vertex ? 1u : 0u, ray ? 1u : 0u, &vo, &ro);
+        if (ray) {
+            if (vertex) P.vocc[vo] = vs;  // never more entries than the set's slots
+            if (ro < P.max_rays) {
                 cg_ray r;
                 r.query = q;
                 r.side = side;
-                r.origin[0] = R.o[k].x;
-                r.origin[1] = R.o[k].y;
-                r.origin[2] = R.o[k].z;
-                r.direction[0] = R.d[k].x;
-                r.direction[1] = R.d[k].y;
-                r.direction[2] = R.d[k].z;
-                P.rays[ro + below] = r;
+                r.origin[0] = ro_.x;
+                r.origin[1] = ro_.y;
+                r.origin[2] = ro_.z;
+                r.direction[0] = rd.x;
+                r.direction[1] = rd.y;
+                r.direction[2] = rd.z;
+                P.rays[ro] = r;
             } else {
                 atomicOr(&P.ctr->c_overflow, CONTACT_RAYS);
             }
-            atomicAdd(sum + 0, double(R.o[k].x));
-            atomicAdd(sum + 1, double(R.o[k].y));
-            atomicAdd(sum + 2, double(R.o[k].z));
+            double* sum = P.sums + 8ull * q + 4ull * side;
+            atomicAdd(sum + 0, double(ro_.x));
+            atomicAdd(sum + 1, double(ro_.y));
+            atomicAdd(sum + 2, double(ro_.z));
             atomicAdd(sum + 3, 1.0);
         }
     }
@@ -563,9 +559,16 @@ cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned l
     return cudaGetLastError();
 }
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s) {
-    contacts_accumulate_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_emit_kernel<<<grid, 256, 0, s>>>(p);
+cudaError_t contacts_occupancy(int* accumulate_blocks_per_sm, int* emit_blocks_per_sm) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(accumulate_blocks_per_sm, contacts_accumulate_kernel,
+                                                                  256, 0);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(emit_blocks_per_sm, contacts_emit_kernel, 256, 0);
+}
+
+cudaError_t launch_contacts(const ContactParams& p, uint32_t accumulate_grid, uint32_t emit_grid, cudaStream_t s) {
+    contacts_accumulate_kernel<<<accumulate_grid, 256, 0, s>>>(p);
+    contacts_emit_kernel<<<emit_grid, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -133,7 +133,8 @@ struct ContactParams {
     Counters* ctr;
 };
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s);
+cudaError_t launch_contacts(const ContactParams& p, uint32_t accumulate_grid, uint32_t emit_grid, cudaStream_t s);
+cudaError_t contacts_occupancy(int* accumulate_blocks_per_sm, int* emit_blocks_per_sm);
 cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
                                 cudaStream_t s);
 
