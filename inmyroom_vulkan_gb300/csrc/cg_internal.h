@@ -179,7 +179,7 @@ struct TraverseParams {
 
 
 __host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return 3u * stack_cap + 4u * kLeafCap; }
-constexpr uint32_t kNarrowWarpWords = 5u * 32u + 1u;  // a narrow block: 32 leaf pairs + prefix sums
+constexpr uint32_t kNarrowWarpWords = 6u * 32u + 1u;  // a narrow block: 32 leaf pairs + prefix sums
 
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,

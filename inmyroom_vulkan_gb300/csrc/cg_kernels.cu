@@ -316,7 +316,8 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
     uint32_t* loa = lq + 32;
     uint32_t* lob = loa + 32;
     uint32_t* lcn = lob + 32;
-    uint32_t* pre = lcn + 32;  // 33 entries
+    uint32_t* lrc = lcn + 32;  // ceil(2^16 / count_b), or 0 where the division is done in full
+    uint32_t* pre = lrc + 32;  // 33 entries
     uint32_t c0 = 0;
     if (uint32_t(lane) < nl) {
         const uint4 e = P.leaf_list[first + lane];
@@ -324,7 +325,10 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
         loa[lane] = e.y;
         lob[lane] = e.z;
         lcn[lane] = e.w;
-        c0 = (e.w & 0xffffu) * (e.w >> 16);
+        const uint32_t cb = e.w >> 16;
+        c0 = (e.w & 0xffffu) * cb;
+        // local / cb == (local * ceil(2^16 / cb)) >> 16 for local < 256, cb <= 16
+        lrc[lane] = (cb <= 16u && c0 < 256u) ? (65536u + cb - 1u) / cb : 0u;
         if ((P.flags & CG_KEEP_LEAF_PAIRS) && first + lane < P.leafs_cap) {
             const PackedQuery* Q = P.q + e.x;
             cg_leaf_pair lp;
@@ -343,28 +347,46 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
         if (lane >= o) s0 += t0;
     }
     const uint32_t total = (P.flags & CG_MID_ONLY) ? 0u : __shfl_sync(kFull, s0, 31);
-    pre[lane] = s0 - c0;
+    const uint32_t my_pre = s0 - c0;  // first test of this lane's leaf pair
+    pre[lane] = my_pre;
     if (lane == 0) pre[32] = total;
     __syncwarp();
 
+    // The leaf pair of test t: each round, the leaf pairs that start inside
+    // the round's 32 tests set their bit, and a lane counts the starts at or
+    // below it from the leaf pair that holds the round's first test. A leaf
+    // pair without tests (an empty leaf) starts where the next one does; a
+    // block with one looks the leaf pair up by binary search instead.
+    const bool counted = __all_sync(kFull, uint32_t(lane) >= nl || c0 != 0u);
+    uint32_t own0 = 0;
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t t = base + lane;
+        const int d = int(my_pre) - int(base);
+        const bool mine = uint32_t(lane) < nl;
+        const unsigned starts = __reduce_or_sync(kFull, (mine && d >= 1 && d <= 31) ? (1u << d) : 0u);
+        const bool next_at_32 = __any_sync(kFull, mine && d == 32);
+        uint32_t lo = own0 + __popc(starts & ((2u << lane) - 1u));
+        own0 += __popc(starts) + (next_at_32 ? 1u : 0u);
         int res = TT_MISS;
         uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
         float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
         if (t < total) {
-            int lo = 0, hi = int(nl) - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (pre[mid] <= t)
-                    lo = mid;
-                else
-                    hi = mid - 1;
+            if (!counted) {
+                int l = 0, h = int(nl) - 1;
+                while (l < h) {
+                    const int mid = (l + h + 1) >> 1;
+                    if (pre[mid] <= t)
+                        l = mid;
+                    else
+                        h = mid - 1;
+                }
+                lo = uint32_t(l);
             }
             const uint32_t local = t - pre[lo];
             const uint32_t cn = lcn[lo];
             const uint32_t cb = cn >> 16;
-            const uint32_t i = local / cb;
+            const uint32_t rc = lrc[lo];
+            const uint32_t i = rc ? (local * rc) >> 16 : local / cb;
             const uint32_t j = local - i * cb;
             q = lq[lo];
             leaf_i = first + uint32_t(lo);
@@ -721,7 +743,11 @@ __global__ void pack_kernel(const cg_query* in, uint32_t n, const DevTree* trees
     const Rec A = load_rec(recs, ra);
     const Rec B = load_rec(recs, rb);
     const Box bb = xform_box(M, B.box);
-    atomicAdd(&ctr->node_pairs, 1ull);
+    {
+        // one atomic per group of converged lanes
+        const unsigned m = __activemask();
+        if ((threadIdx.x & 31u) == unsigned(__ffs(m) - 1)) atomicAdd(&ctr->node_pairs, (unsigned long long)__popc(m));
+    }
     if (sat(A.box, bb)) {
         const bool la = (A.meta & kLeafFlag) != 0;
         const bool lb = (B.meta & kLeafFlag) != 0;

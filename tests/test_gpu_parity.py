@@ -207,3 +207,39 @@ def test_launch_shapes_give_identical_sets(port, scene_setup, shape):
         st, pairs, segs, tests, nleaf = run_both(ctx, port, tp, ids, qa, qb, sc.mats[qa], sc.mats[qb])
         assert st["status"] == 0 and st["tri_tests"] == tests
         assert np.array_equal(gpu_pair_table(ctx.tri_pairs()), pair_table(pairs[:, 0], pairs[:, 1], pairs[:, 2], segs))
+
+
+def test_large_leaves_bit_exact(gpu_ctx, port):
+    """Leaves far above the builder's four triangles (a tree that is one leaf
+    of 40 or 18 triangles, and one of 3): the narrow phase's long and
+    multi-round leaf pairs, with the full integer division, against the
+    oracle on the same flat trees."""
+    rng = np.random.Generator(np.random.PCG64(7))
+    big = 10.0
+    root = np.array([0, 0, 0, big, 0, 0, 0, big, 0, 0, 0, big], np.float32)
+
+    def leaf_tree(n_tris):
+        pos = (rng.normal(size=(n_tris, 9)) * 0.4).astype(np.float32)
+        nrm = np.tile(np.array([0, 0, 1], np.float32), (n_tris, 3))
+        idx = np.arange(3 * n_tris, dtype=np.uint32).reshape(-1, 3)
+        return oracle.FlatTree(root, np.zeros((0, 2, 12), np.float32), np.zeros((0, 2), np.uint32),
+                               np.zeros((0, 2), np.uint32), pos, nrm, idx)
+
+    flats = [leaf_tree(40), leaf_tree(18), leaf_tree(3)]
+    tp = [port.tree_import(f) for f in flats]
+    ids = [gpu_ctx.upload_flat(f) for f in flats]
+    qa, qb, ma, mb = [], [], [], []
+    for i in range(3):
+        for j in range(3):
+            for _ in range(4):
+                qa.append(i)
+                qb.append(j)
+                ma.append(scenes.pose(scenes.random_rotation(rng), rng.normal(size=3) * 0.1))
+                mb.append(scenes.pose(scenes.random_rotation(rng), rng.normal(size=3) * 0.1))
+    st, pairs, segs, tests, nleaf = run_both(gpu_ctx, port, tp, ids, np.array(qa), np.array(qb), np.array(ma),
+                                             np.array(mb))
+    assert st["status"] == 0 and st["tri_tests"] == tests and tests > 10000 and st["leaf_pairs"] == nleaf
+    assert len(pairs) > 100
+    assert np.array_equal(gpu_pair_table(gpu_ctx.tri_pairs()), pair_table(pairs[:, 0], pairs[:, 1], pairs[:, 2], segs))
+    for i in ids:
+        gpu_ctx.free_tree(i)
