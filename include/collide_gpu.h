@@ -238,6 +238,66 @@ int cg_read_trace(cg_ctx* ctx, uint32_t bucket_ns, uint32_t* out, uint32_t n_buc
 int cg_graph_capture(cg_ctx* ctx, const cg_query* d_queries, uint32_t n, uint32_t flags);
 int cg_graph_launch(cg_ctx* ctx, void* stream);
 
+/* ---- deforming meshes ------------------------------------------------- */
+
+/* Morph targets, then linear-blend skinning, of a vertex array: the position
+ * path of the engine's skinning compute shader
+ * (shaders/dynamicMeshShader_glsl.comp:78-145, which replaces vertex data the
+ * engine's CPU collision path then uses). All arrays are device memory:
+ *   vertices       n_vertices x (1 + n_targets) x float4: per vertex the base
+ *                  position (w = 1) then the morph target offsets (w = 0), the
+ *                  shader's interleaved layout; 16-byte aligned
+ *   morph_weights  n_targets floats
+ *   joints         n_vertices x n_groups x 4 uint16 (8-byte aligned); a joint
+ *                  index >= n_joints makes that vertex NaN
+ *   weights        n_vertices x n_groups x float4 (16-byte aligned)
+ *   joint_matrices n_joints x 16 floats, column-major: the shader's
+ *                  modelMatrices[matrixOffset + 1 + j]
+ *   inverse_bind   n_joints x 16 floats: inverseModelMatrices[inverseMatricesOffset + j]
+ * out receives n_vertices x float4 (16-byte aligned). n_groups = 0 skips the
+ * skin. n_joints <= 2048. Enqueued on `stream` (NULL = the context's). */
+typedef struct cg_deform_view {
+    uint32_t n_vertices;
+    uint32_t n_targets;
+    uint32_t n_groups;
+    uint32_t n_joints;
+    const float* vertices;
+    const float* morph_weights;
+    const uint16_t* joints;
+    const float* weights;
+    const float* joint_matrices;
+    const float* inverse_bind;
+} cg_deform_view;
+
+int cg_deform(cg_ctx* ctx, const cg_deform_view* view, float* out, void* stream);
+/* n meshes in one launch: views[i] into outs[i]. The table of views goes to
+ * device memory when it differs from the previous call's (that upload waits
+ * for the stream, so make the first call of a new table outside stream
+ * capture); repeating the same batch costs one kernel launch. */
+int cg_deform_batch(cg_ctx* ctx, const cg_deform_view* views, float* const* outs, uint32_t n, void* stream);
+
+/* Refits an uploaded tree to new vertex positions (device, n_positions x
+ * float4, 16-byte aligned, indexed by the triangles' vertex indices given at
+ * upload, e.g. cg_deform's output): the topology stays; every box is fitted
+ * again with OBB::CreateOBBfromPoints (src/Geometry/OBB.cpp:33-89) to the
+ * corners of its subtree's triangles, taken in the tree's leaf (DFS) order.
+ * A vertex index >= n_positions makes its corner NaN. Enqueued on `stream`
+ * (NULL = the context's); a collide launched after it on the same stream sees
+ * the new boxes. */
+int cg_tree_refit(cg_ctx* ctx, uint32_t tree_id, const float* positions, uint32_t n_positions, void* stream);
+/* n trees in one launch of each refit kernel (the table is handled as in
+ * cg_deform_batch). */
+int cg_tree_refit_batch(cg_ctx* ctx, const uint32_t* tree_ids, const float* const* positions,
+                        const uint32_t* n_positions, uint32_t n, void* stream);
+
+/* Copies an uploaded (or refitted) tree's boxes and triangle positions back:
+ * root box, node_obbs[node_count][2] (left, right) and
+ * triangles_position[triangle_count][3][3], in the layout of cg_tree_view; any
+ * pointer may be NULL. node_count and triangle_count must be the tree's (or
+ * 0 for an array not wanted). Waits for the context's stream. */
+int cg_tree_download(cg_ctx* ctx, uint32_t tree_id, cg_obb* root, cg_obb* node_obbs, uint32_t node_count,
+                     float* triangles_position, uint32_t triangle_count);
+
 /* ---- No-allocation collide step (no reference counterpart) ----
  *
  * The collide step of cg_collide_async (same kernels, same colliding pairs)

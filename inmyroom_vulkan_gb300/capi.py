@@ -29,7 +29,8 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_sync_stats", "cg_read_tri_pairs", "cg_read_leaf_pairs", "cg_device_results", "cg_read_contacts",
            "cg_read_rays", "cg_read_ray_averages",
            "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch",
-           "cg_collide_static"]
+           "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
+           "cg_tree_download"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -57,6 +58,13 @@ class cg_tree_view(C.Structure):
                 ("node_ref", C.c_void_p), ("node_tri_count", C.c_void_p), ("triangle_count", C.c_uint32),
                 ("triangles_position", C.c_void_p), ("triangles_normal", C.c_void_p),
                 ("triangles_indices", C.c_void_p)]
+
+
+class cg_deform_view(C.Structure):
+    _fields_ = [("n_vertices", C.c_uint32), ("n_targets", C.c_uint32), ("n_groups", C.c_uint32),
+                ("n_joints", C.c_uint32), ("vertices", C.c_void_p), ("morph_weights", C.c_void_p),
+                ("joints", C.c_void_p), ("weights", C.c_void_p), ("joint_matrices", C.c_void_p),
+                ("inverse_bind", C.c_void_p)]
 
 
 class cg_static_counts(C.Structure):
@@ -124,6 +132,11 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_graph_capture.argtypes = [vp, vp, u32, u32]
     lib.cg_graph_launch.argtypes = [vp, vp]
     lib.cg_collide_static.argtypes = [vp, vp, u32, vp, u64, vp, vp]
+    lib.cg_deform.argtypes = [vp, C.POINTER(cg_deform_view), vp, vp]
+    lib.cg_tree_refit.argtypes = [vp, u32, vp, u32, vp]
+    lib.cg_deform_batch.argtypes = [vp, vp, vp, u32, vp]
+    lib.cg_tree_refit_batch.argtypes = [vp, vp, vp, vp, u32, vp]
+    lib.cg_tree_download.argtypes = [vp, u32, vp, vp, u32, vp, u32]
     _lib = lib
     return lib
 
@@ -312,6 +325,41 @@ class Context:
         rc = self.lib.cg_collide_static(self.h, d_queries_ptr or None, n, d_pairs_ptr or None, pairs_cap,
                                         d_counts_ptr, stream)
         self._check(rc, "cg_collide_static")
+
+    def deform(self, n_vertices: int, n_targets: int, n_groups: int, n_joints: int, vertices: int,
+               morph_weights: int, joints: int, weights: int, joint_matrices: int, inverse_bind: int, out: int,
+               stream: int | None = None):
+        """cg_deform on device pointers (see cg_deform_view)."""
+        v = cg_deform_view(n_vertices, n_targets, n_groups, n_joints, vertices, morph_weights, joints, weights,
+                           joint_matrices, inverse_bind)
+        self._check(self.lib.cg_deform(self.h, C.byref(v), out, stream), "cg_deform")
+
+    def tree_refit(self, tree_id: int, positions: int, n_positions: int, stream: int | None = None):
+        """cg_tree_refit: positions is a device pointer to n_positions float4."""
+        self._check(self.lib.cg_tree_refit(self.h, tree_id, positions, n_positions, stream), "cg_tree_refit")
+
+    def deform_batch(self, views: list, outs: list, stream: int | None = None):
+        """cg_deform_batch: views are cg_deform_view, outs device pointers."""
+        arr = (cg_deform_view * len(views))(*views)
+        optr = (C.c_void_p * len(outs))(*outs)
+        self._check(self.lib.cg_deform_batch(self.h, arr, optr, len(views), stream), "cg_deform_batch")
+
+    def tree_refit_batch(self, tree_ids, positions, n_positions, stream: int | None = None):
+        n = len(tree_ids)
+        ids = (C.c_uint32 * n)(*tree_ids)
+        pos = (C.c_void_p * n)(*positions)
+        cnt = (C.c_uint32 * n)(*n_positions)
+        self._check(self.lib.cg_tree_refit_batch(self.h, ids, pos, cnt, n, stream), "cg_tree_refit_batch")
+
+    def tree_download(self, tree_id: int, node_count: int, triangle_count: int):
+        """(root (12,), node_obbs (node_count, 2, 12), triangle positions (triangle_count, 9))."""
+        root = np.zeros(12, np.float32)
+        obbs = np.zeros((max(node_count, 1), 2, 12), np.float32)
+        tri = np.zeros((max(triangle_count, 1), 9), np.float32)
+        rc = self.lib.cg_tree_download(self.h, tree_id, root.ctypes.data, obbs.ctypes.data if node_count else None,
+                                       node_count, tri.ctypes.data if triangle_count else None, triangle_count)
+        self._check(rc, "cg_tree_download")
+        return root, obbs[:node_count], tri[:triangle_count]
 
     def device_results(self) -> tuple[int, int]:
         p, n = C.c_void_p(), C.c_void_p()

@@ -107,7 +107,9 @@ struct cg_ctx {
     // trees
     struct Slot {
         uint64_t rec_base = 0, n_recs = 0, tri_base = 0, n_tris = 0;
+        uint32_t n_tri_used = 0;  // the tree's triangle count (n_tris is at least 1)
         float* nrm = nullptr;
+        uint2* ranges = nullptr;  // per record: first triangle and count of its subtree (refit)
         bool live = false;
     };
     std::vector<Slot> trees;
@@ -162,6 +164,14 @@ struct cg_ctx {
     bool capturing = false;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_t2 = nullptr;  // traversal start, end; narrow end
     cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
+
+    // batch tables of cg_deform_batch / cg_tree_refit_batch in device memory,
+    // uploaded when their contents change
+    struct Table {
+        std::vector<char> host;
+        void* dev = nullptr;
+        size_t cap = 0;
+    } deform_table, refit_table;
 
     std::string err;
 };
@@ -232,6 +242,27 @@ void free_buffers(cg_ctx* c) {
     c->h_ctr = nullptr;
 }
 
+// Device copy of a batch table; uploaded (after the stream's earlier work,
+// which may still read the old one) only when its contents changed.
+int stage_table(cg_ctx* c, cg_ctx::Table& t, const void* data, size_t bytes, cudaStream_t s, const void** dev) {
+    if (bytes == t.host.size() && std::memcmp(t.host.data(), data, bytes) == 0) {
+        *dev = t.dev;
+        return CG_OK;
+    }
+    CG_CUDA(cudaStreamSynchronize(s), "batch table");
+    if (bytes > t.cap) {
+        cudaFree(t.dev);
+        t.dev = nullptr;
+        t.cap = 0;
+        CG_CUDA(cudaMalloc(&t.dev, bytes), "alloc batch table");
+        t.cap = bytes;
+    }
+    CG_CUDA(cudaMemcpy(t.dev, data, bytes, cudaMemcpyHostToDevice), "upload batch table");
+    t.host.assign(static_cast<const char*>(data), static_cast<const char*>(data) + bytes);
+    *dev = t.dev;
+    return CG_OK;
+}
+
 void drop_graph(cg_ctx* c) {
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->graph) cudaGraphDestroy(c->graph);
@@ -278,6 +309,7 @@ int alloc_buffers(cg_ctx* c) {
     CG_CUDA(contacts_occupancy(&aocc, &eocc), "occupancy");
     c->accumulate_blocks = uint32_t(std::max(aocc, 1) * c->sm_count);
     c->emit_blocks = uint32_t(std::max(eocc, 1) * c->sm_count);
+    CG_CUDA(deform_smem_limit(), "deform kernel shared memory");
 
     CG_CUDA(cudaMalloc(&c->d_queries, sizeof(cg_query) * g.max_queries), "alloc queries");
     CG_CUDA(cudaMalloc(&c->d_packed, sizeof(PackedQuery) * g.max_queries), "alloc packed queries");
@@ -618,10 +650,15 @@ int cg_destroy(cg_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graph(c);
-    for (auto& s : c->trees) cudaFree(s.nrm);
+    for (auto& s : c->trees) {
+        cudaFree(s.nrm);
+        cudaFree(s.ranges);
+    }
     c->recs.destroy();
     c->tris.destroy();
     cudaFree(c->d_trees);
+    cudaFree(c->deform_table.dev);
+    cudaFree(c->refit_table.dev);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
@@ -735,6 +772,32 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
                                 c->stream),
                 "upload normals");
     }
+    // subtree triangle range of every record (the root, then both children of
+    // each node; children come after their parent, so a backward pass over
+    // the nodes sees each inner child's range before its parent needs it)
+    {
+        std::vector<uint2> rg(n_recs, make_uint2(0u, ~0u));
+        std::vector<uint2> node_rg(N);
+        for (uint32_t k = N; k-- > 0;) {
+            uint32_t lo = 0xffffffffu, hi = 0;
+            for (int s2 = 0; s2 < 2; ++s2) {
+                const uint32_t ref = v->node_ref[2 * k + s2], cnt = v->node_tri_count[2 * k + s2];
+                const uint2 crg = cnt ? make_uint2(ref, cnt) : node_rg[ref];
+                rg[2ull * k + 2 + s2] = crg;
+                if (crg.y) {
+                    lo = std::min(lo, crg.x);
+                    hi = std::max(hi, crg.x + crg.y);
+                }
+            }
+            node_rg[k] = lo <= hi ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
+        }
+        rg[1] = N ? node_rg[0] : make_uint2(0u, T);
+        CG_CUDA(cudaMalloc(&slot.ranges, sizeof(uint2) * n_recs), "alloc record ranges");
+        CG_CUDA(cudaMemcpyAsync(slot.ranges, rg.data(), sizeof(uint2) * n_recs, cudaMemcpyHostToDevice, c->stream),
+                "upload record ranges");
+        CG_CUDA(cudaStreamSynchronize(c->stream), "upload record ranges");
+    }
+    slot.n_tri_used = T;
     CG_CUDA(launch_surfaces(c->recs.ptr, uint32_t(rb), uint32_t(n_recs), c->stream), "surface kernel");
     CG_CUDA(cudaStreamSynchronize(c->stream), "tree upload");
     slot.live = true;
@@ -764,6 +827,7 @@ int cg_tree_free(cg_ctx* c, uint32_t id) {
     c->recs.release(s.rec_base / 2, s.n_recs / 2);
     c->tris.release(s.tri_base, s.n_tris);
     cudaFree(s.nrm);
+    cudaFree(s.ranges);
     s = cg_ctx::Slot{};
     return sync_tree_table(c);
 }
@@ -942,6 +1006,120 @@ int cg_read_trace(cg_ctx* c, uint32_t bucket_ns, uint32_t* out, uint32_t n_bucke
     CG_CUDA(cudaStreamSynchronize(c->stream), "trace");
     CG_CUDA(cudaMemcpy(out, c->d_trace, sizeof(uint32_t) * 4 * m, cudaMemcpyDeviceToHost), "read trace");
     return CG_OK;
+}
+
+int cg_tree_download(cg_ctx* c, uint32_t id, cg_obb* root, cg_obb* node_obbs, uint32_t node_count,
+                     float* triangles_position, uint32_t triangle_count) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
+    const auto& t = c->trees[id];
+    const uint32_t N = uint32_t((t.n_recs - 2) / 2);
+    if ((node_count && node_count != N) || (triangle_count && triangle_count != t.n_tri_used))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "tree %u has %u nodes and %u triangles", id, N, t.n_tri_used);
+    cudaSetDevice(c->device);
+    CG_CUDA(cudaStreamSynchronize(c->stream), "download tree");
+    auto unbox = [](const float4* r, cg_obb* b) {
+        b->center[0] = r[0].x, b->center[1] = r[0].y, b->center[2] = r[0].z;
+        b->u[0] = r[0].w, b->u[1] = r[1].x, b->u[2] = r[1].y;
+        b->v[0] = r[1].z, b->v[1] = r[1].w, b->v[2] = r[2].x;
+        b->w[0] = r[2].y, b->w[1] = r[2].z, b->w[2] = r[2].w;
+    };
+    if (root || (node_obbs && node_count)) {
+        std::vector<float4> recs(4ull * t.n_recs);
+        CG_CUDA(cudaMemcpy(recs.data(), c->recs.ptr + 4 * t.rec_base, sizeof(float4) * recs.size(),
+                           cudaMemcpyDeviceToHost),
+                "download records");
+        if (root) unbox(&recs[4], root);
+        if (node_obbs)
+            for (uint32_t r = 2; r < t.n_recs; ++r) unbox(&recs[4ull * r], node_obbs + (r - 2));
+    }
+    if (triangles_position && triangle_count) {
+        std::vector<float4> tris(3ull * triangle_count);
+        CG_CUDA(cudaMemcpy(tris.data(), c->tris.ptr + 3 * t.tri_base, sizeof(float4) * tris.size(),
+                           cudaMemcpyDeviceToHost),
+                "download triangles");
+        for (size_t k = 0; k < tris.size(); ++k) {
+            triangles_position[3 * k] = tris[k].x;
+            triangles_position[3 * k + 1] = tris[k].y;
+            triangles_position[3 * k + 2] = tris[k].z;
+        }
+    }
+    return CG_OK;
+}
+
+int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const* positions,
+                        const uint32_t* n_positions, uint32_t n, void* stream) {
+    if (!c || (n && (!tree_ids || !positions || !n_positions))) return CG_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CG_OK;
+    std::vector<RefitTree> table(n);
+    uint32_t max_tris = 0, max_recs = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t id = tree_ids[i];
+        if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
+        if ((!positions[i] && n_positions[i]) || (reinterpret_cast<uintptr_t>(positions[i]) & 15u))
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "positions %u must be 16-byte aligned device memory", i);
+        const auto& t = c->trees[id];
+        table[i] = RefitTree{uint32_t(t.rec_base), uint32_t(t.n_recs), uint32_t(t.tri_base), t.n_tri_used, t.ranges,
+                             reinterpret_cast<const float4*>(positions[i]), n_positions[i], 0u};
+        max_tris = std::max(max_tris, t.n_tri_used);
+        max_recs = std::max(max_recs, uint32_t(t.n_recs));
+    }
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    const void* d_table = nullptr;
+    int rc = stage_table(c, c->refit_table, table.data(), sizeof(RefitTree) * n, s, &d_table);
+    if (rc != CG_OK) return rc;
+    CG_CUDA(launch_refit(c->recs.ptr, c->tris.ptr, static_cast<const RefitTree*>(d_table), n, max_tris, max_recs, s),
+            "refit kernels");
+    return CG_OK;
+}
+
+int cg_tree_refit(cg_ctx* c, uint32_t id, const float* positions, uint32_t n_positions, void* stream) {
+    return cg_tree_refit_batch(c, &id, &positions, &n_positions, 1, stream);
+}
+
+int cg_deform_batch(cg_ctx* c, const cg_deform_view* views, float* const* outs, uint32_t n, void* stream) {
+    if (!c || (n && (!views || !outs))) return CG_ERR_INVALID_ARGUMENT;
+    auto aligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; };
+    std::vector<DeformParams> table(n);
+    uint32_t max_vertices = 0, max_joints = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const cg_deform_view* v = views + i;
+        float* out = outs[i];
+        if (v->n_vertices && (!v->vertices || !out || (v->n_targets && !v->morph_weights) ||
+                              (v->n_groups && (!v->joints || !v->weights || !v->joint_matrices || !v->inverse_bind))))
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "deform view %u has null arrays", i);
+        if (!aligned(v->vertices, 16) || !aligned(out, 16) ||
+            (v->n_groups && (!aligned(v->weights, 16) || !aligned(v->joints, 8))))
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "deform view %u: arrays must be 16-byte (joints 8-byte) aligned", i);
+        if (v->n_joints > kMaxJoints) return fail(c, CG_ERR_INVALID_ARGUMENT, "n_joints %u > %u", v->n_joints, kMaxJoints);
+        DeformParams& p = table[i];
+        p.n_vertices = v->n_vertices;
+        p.n_targets = v->n_targets;
+        p.n_groups = v->n_groups;
+        p.n_joints = v->n_groups ? v->n_joints : 0u;
+        p.vertices = v->vertices;
+        p.morph_weights = v->morph_weights;
+        p.joints = v->joints;
+        p.weights = v->weights;
+        p.joint_matrices = v->joint_matrices;
+        p.inverse_bind = v->inverse_bind;
+        p.out = out;
+        max_vertices = std::max(max_vertices, p.n_vertices);
+        max_joints = std::max(max_joints, p.n_joints);
+    }
+    if (n == 0 || max_vertices == 0) return CG_OK;
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    const void* d_table = nullptr;
+    int rc = stage_table(c, c->deform_table, table.data(), sizeof(DeformParams) * n, s, &d_table);
+    if (rc != CG_OK) return rc;
+    CG_CUDA(launch_deform(static_cast<const DeformParams*>(d_table), n, max_vertices, max_joints, s), "deform kernel");
+    return CG_OK;
+}
+
+int cg_deform(cg_ctx* c, const cg_deform_view* v, float* out, void* stream) {
+    return cg_deform_batch(c, v, &out, 1, stream);
 }
 
 int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags) {

@@ -181,6 +181,37 @@ struct TraverseParams {
 __host__ __device__ inline uint32_t warp_smem_words(uint32_t stack_cap) { return 3u * stack_cap + 4u * kLeafCap; }
 constexpr uint32_t kNarrowWarpWords = 6u * 32u + 1u;  // a narrow block: 32 leaf pairs + prefix sums
 
+// Morph and skinning (cg_deform.cu); the arrays are those of cg_deform_view.
+struct DeformParams {
+    uint32_t n_vertices, n_targets, n_groups, n_joints;
+    const float* vertices;
+    const float* morph_weights;
+    const uint16_t* joints;
+    const float* weights;
+    const float* joint_matrices;
+    const float* inverse_bind;
+    float* out;
+};
+constexpr uint32_t kMaxJoints = 2048;  // joint products staged in shared memory (128 KB)
+// One launch for a batch of meshes (grid.y = mesh); the parameters are in
+// device memory.
+cudaError_t launch_deform(const DeformParams* d_meshes, uint32_t n_meshes, uint32_t max_vertices, uint32_t max_joints,
+                          cudaStream_t s);
+cudaError_t deform_smem_limit();
+
+// Refit (cg_refit.cu): new corner positions of a tree's triangles from a
+// vertex array, then every record's box from its triangle range (x first, y
+// count; y = ~0 marks the unused record). One launch per kernel for a batch
+// of trees (grid.y = tree); the table is in device memory.
+struct RefitTree {
+    uint32_t rec_base, n_recs, tri_base, n_tris;
+    const uint2* ranges;
+    const float4* positions;
+    uint32_t n_positions, pad;
+};
+cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
+                         uint32_t max_recs, cudaStream_t s);
+
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,
                         PackedQuery* out, Counters* ctr, uint4* leaf_list, uint32_t leaf_cap, cudaStream_t s);

@@ -246,3 +246,138 @@ def batch_sweep(n_queries: int = 10000, pool: int = 48, seed: int = SEED_BASE + 
     ma = np.stack([pose(random_rotation(rng), np.zeros(3)) for _ in range(n_queries)])
     mb = np.stack([pose(random_rotation(rng), ball_point(rng, 2.52)) for _ in range(n_queries)])
     return BatchSweep(meshes, qa, qb, ma, mb)
+
+
+# ---------------------------------------------------------------- deforming --
+# Skinned, morphed tubes against a static heightfield (the deforming and
+# differentiable workloads). Choices of the builder, recorded here: each mesh
+# is an open tube along +y, `rings` x `around` quads (two triangles each),
+# radius 0.12 m, length 2 m, skinned to a chain of `n_bones` bones of equal
+# length along the tube; a vertex's four joints are the bones nearest to its
+# height, with Dirichlet(1) weights; 8 morph targets of N(0, 0.02) offsets;
+# per mesh, bone rotations as axis-angle vectors N(0, 0.3 rad) per component
+# and morph weights U[0, 1]. The heightfield is a `grid` x `grid` vertex grid
+# over [0, 20] m x [0, 20] m with fBm heights of amplitude 0.5 m.
+
+
+def axis_angle_matrix(aa: np.ndarray) -> np.ndarray:
+    """3x3 rotation of an axis-angle vector (Rodrigues), float64."""
+    th = float(np.linalg.norm(aa))
+    if th < 1e-12:
+        return np.eye(3)
+    k = aa / th
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + math.sin(th) * K + (1 - math.cos(th)) * (K @ K)
+
+
+def translate(t) -> np.ndarray:
+    M = np.eye(4)
+    M[:3, 3] = t
+    return M
+
+
+def chain_matrices(aa: np.ndarray, bone_len: float) -> np.ndarray:
+    """World matrices (n_bones, 4, 4) of a bone chain along +y: bone 0 at the
+    origin rotated by aa[0]; bone j = bone j-1 * T(0, bone_len, 0) * R(aa[j])."""
+    out = np.zeros((len(aa), 4, 4))
+    G = np.eye(4)
+    for j, a in enumerate(aa):
+        R = np.eye(4)
+        R[:3, :3] = axis_angle_matrix(a)
+        G = (G @ translate([0, bone_len, 0]) @ R) if j else R
+        out[j] = G
+    return out
+
+
+def col_major(M: np.ndarray) -> np.ndarray:
+    """(..., 4, 4) row-major math -> (..., 16) column-major float32."""
+    return np.ascontiguousarray(np.swapaxes(M, -1, -2).reshape(M.shape[:-2] + (16,)), np.float32)
+
+
+def tube(rings: int, around: int, radius: float, length: float) -> Mesh:
+    ys = np.linspace(0.0, length, rings + 1)
+    ang = np.linspace(0.0, 2 * math.pi, around, endpoint=False)
+    pts = np.stack([np.stack([radius * np.cos(ang), np.full(around, y), radius * np.sin(ang)], 1) for y in ys])
+    pts = pts.reshape(-1, 3).astype(np.float32)
+    idx = []
+    for r in range(rings):
+        for a in range(around):
+            i0, i1 = r * around + a, r * around + (a + 1) % around
+            j0, j1 = i0 + around, i1 + around
+            idx += [i0, j0, i1, i1, j0, j1]
+    idx = np.array(idx, np.uint32)
+    return Mesh(pts, vertex_normals(pts, idx), idx)
+
+
+def fbm_heightfield(grid: int, size: float, amplitude: float, rng: np.random.Generator) -> Mesh:
+    from scipy.ndimage import zoom
+
+    h = np.zeros((grid, grid))
+    total = 0.0
+    for o in range(5):
+        res = 4 * 2 ** o
+        noise = rng.uniform(-1, 1, size=(res + 1, res + 1))
+        up = zoom(noise, grid / (res + 1), order=3)[:grid, :grid]
+        h += up * 0.5 ** o
+        total += 0.5 ** o
+    h *= amplitude / total
+    xs = np.linspace(0.0, size, grid)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    pts = np.stack([X, h, Z], -1).reshape(-1, 3).astype(np.float32)
+    idx = []
+    for i in range(grid - 1):
+        for j in range(grid - 1):
+            a, b, c, d = i * grid + j, i * grid + j + 1, (i + 1) * grid + j, (i + 1) * grid + j + 1
+            idx += [a, b, c, b, d, c]
+    idx = np.array(idx, np.uint32)
+    return Mesh(pts, vertex_normals(pts, idx), idx), h
+
+
+@dataclass
+class DeformingScene:
+    mesh: Mesh                  # rest tube (shared topology)
+    vertices: np.ndarray        # (n_meshes, V, 1 + targets, 4): base (w = 1) then target offsets (w = 0)
+    morph_weights: np.ndarray   # (n_meshes, targets)
+    joints: np.ndarray          # (V, 1, 4) uint16
+    weights: np.ndarray         # (V, 1, 4) float32
+    axis_angles: np.ndarray     # (n_meshes, n_bones, 3)
+    joint_matrices: np.ndarray  # (n_meshes, n_bones, 16) posed chain
+    inverse_bind: np.ndarray    # (n_bones, 16) inverse rest chain
+    models: np.ndarray          # (n_meshes, 16) tube placement in the world
+    field: Mesh                 # heightfield (identity placement)
+    bone_len: float
+
+
+def deforming(n_meshes: int = 64, seed: int = SEED_BASE + 3, rings: int = 100, around: int = 60, n_bones: int = 50,
+              n_targets: int = 8, grid: int = 316) -> DeformingScene:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    length = 2.0
+    mesh = tube(rings, around, 0.12, length)
+    V = len(mesh.points)
+    bone_len = length / n_bones
+    # four nearest bones by height, Dirichlet(1) weights
+    centre = (np.arange(n_bones) + 0.5) * bone_len
+    near = np.argsort(np.abs(mesh.points[:, 1:2] - centre[None, :]), axis=1)[:, :4]
+    joints = near.astype(np.uint16).reshape(V, 1, 4)
+    weights = rng.dirichlet(np.ones(4), size=V).astype(np.float32).reshape(V, 1, 4)
+    rest = np.stack([translate([0, j * bone_len, 0]) for j in range(n_bones)])
+    inverse_bind = col_major(np.linalg.inv(rest))
+    verts = np.zeros((n_meshes, V, 1 + n_targets, 4), np.float32)
+    verts[:, :, 0, :3] = mesh.points
+    verts[:, :, 0, 3] = 1.0
+    verts[:, :, 1:, :3] = rng.normal(0.0, 0.02, size=(n_meshes, V, n_targets, 3))
+    morph_w = rng.uniform(0.0, 1.0, size=(n_meshes, n_targets)).astype(np.float32)
+    aa = rng.normal(0.0, 0.3, size=(n_meshes, n_bones, 3))
+    jm = np.stack([col_major(chain_matrices(aa[m], bone_len)) for m in range(n_meshes)])
+    field, h = fbm_heightfield(grid, 20.0, 0.5, rng)
+    models = []
+    for m in range(n_meshes):
+        gx, gz = rng.uniform(2.0, 18.0, size=2)
+        gi = min(grid - 1, int(round(gx / 20.0 * (grid - 1))))
+        gj = min(grid - 1, int(round(gz / 20.0 * (grid - 1))))
+        # the tube's root at the ground, its axis tilted into the ground by a random angle
+        R = axis_angle_matrix(np.array([0.0, rng.uniform(0, 2 * math.pi), 0.0])) @ \
+            axis_angle_matrix(np.array([0.0, 0.0, math.pi / 2 + rng.uniform(-0.4, 0.4)]))
+        models.append(pose(R, [gx, h[gi, gj] + 0.05, gz]))
+    return DeformingScene(mesh, verts, morph_w, joints, weights, aa, jm, inverse_bind, np.stack(models), field,
+                          bone_len)

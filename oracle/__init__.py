@@ -86,6 +86,8 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
         f("collide_batch").restype = C.c_uint64
         f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int,
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        f("deform").argtypes = [sz, sz, sz, sz, _f32p, _f32p, vp, _f32p, _f32p, _f32p, _f32p]
+        f("tree_refit").argtypes = [sz, _u32p, _u32p, sz, _u32p, _f32p, sz, _f32p, _f32p, _f32p]
         f("collide_pairs").restype = sz
         f("collide_pairs").argtypes = [vp, vp, _f32p, _f32p, sz, _u32p, _f32p, sz,
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
@@ -258,6 +260,35 @@ class Impl:
         t = np.zeros(3, np.float32)
         hit = self.fn("tri_tri")(_f32(a, 9), _f32(b, 9), C.byref(cop), s, t)
         return hit, cop.value, s, t
+
+    def deform(self, vertices, morph_weights, joints, weights, joint_matrices, inverse_bind):
+        """(port) morph then linear-blend skinning: vertices (n, 1 + targets, 4),
+        joints/weights (n, groups, 4), matrices (joints, 16) -> (n, 4)."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        n, t1 = v.shape[0], v.shape[1]
+        jn = np.ascontiguousarray(joints, np.uint16)
+        w = np.ascontiguousarray(weights, np.float32)
+        groups = jn.shape[1] if jn.ndim == 3 else 0
+        jm = np.ascontiguousarray(joint_matrices, np.float32).reshape(-1, 16)
+        ib = np.ascontiguousarray(inverse_bind, np.float32).reshape(-1, 16)
+        out = np.zeros((n, 4), np.float32)
+        self.fn("deform")(n, t1 - 1, groups, jm.shape[0], v.reshape(-1), _f32(morph_weights),
+                          jn.ctypes.data, w.reshape(-1), jm.reshape(-1), ib.reshape(-1), out)
+        return out
+
+    def tree_refit(self, ft: "FlatTree", positions) -> "FlatTree":
+        """(port) the flat tree refitted to positions (n, 4): new corner positions
+        and every box fitted again to its subtree's corners in leaf order."""
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+        n, t = ft.n_nodes, ft.n_tris
+        root = np.zeros(12, np.float32)
+        obbs = np.zeros((max(n, 1), 2, 12), np.float32)
+        tri = np.zeros((max(t, 1), 9), np.float32)
+        self.fn("tree_refit")(n, ft.node_ref.reshape(-1) if n else np.zeros(2, np.uint32),
+                              ft.node_cnt.reshape(-1) if n else np.zeros(2, np.uint32), t,
+                              ft.tri_idx.reshape(-1), pos.reshape(-1), pos.shape[0], root, obbs.reshape(-1),
+                              tri.reshape(-1))
+        return FlatTree(root, obbs[:n], ft.node_ref[:n], ft.node_cnt[:n], tri[:t], ft.tri_nrm[:t], ft.tri_idx[:t])
 
     def transform_tri(self, m, a):
         out = np.zeros(9, np.float32)

@@ -1091,4 +1091,87 @@ size_t port_collide_pairs(void* const* trees_a, void* const* trees_b, const floa
     return total;
 }
 
+// Morph targets, then linear-blend skinning, of dynamicMeshShader_glsl.comp
+// (shaders/dynamicMeshShader_glsl.comp:78-145; position path: no NORMALIZE,
+// no ZERO_W), restated in C++ because the shader cannot run here.
+// vertices: per vertex the base then n_targets target offsets, vec4 each (the
+// shader's interleaved buffer); joints/weights: n_groups groups of four per
+// vertex; joint_matrices[j] is the shader's modelMatrices[matrixOffset + 1 + j],
+// inverse_bind[j] its inverseModelMatrices[inverseMatricesOffset + j].
+// Operation order: morphed += w_i * target_i per component; each joint's
+// matrix is joint_matrix * inverse_bind (glm convention), applied to the vec4
+// as (c0 x + c1 y) + (c2 z + c3 w); result += weight * that, joints x, y, z, w
+// in turn.
+void port_deform(size_t n_vertices, size_t n_targets, size_t n_groups, size_t n_joints, const float* vertices,
+                 const float* morph_weights, const uint16_t* joints, const float* weights, const float* joint_matrices,
+                 const float* inverse_bind, float* out) {
+    std::vector<M4> mats(n_joints);
+    for (size_t j = 0; j < n_joints; ++j) {
+        M4 g, ib;
+        std::memcpy(g.m, joint_matrices + 16 * j, sizeof(g.m));
+        std::memcpy(ib.m, inverse_bind + 16 * j, sizeof(ib.m));
+        mats[j] = mul(g, ib);
+    }
+    for (size_t x = 0; x < n_vertices; ++x) {
+        const float* vx = vertices + 4 * (n_targets + 1) * x;
+        float v[4] = {vx[0], vx[1], vx[2], vx[3]};
+        for (size_t i = 0; i < n_targets; ++i)
+            for (int c = 0; c < 4; ++c) v[c] = v[c] + morph_weights[i] * vx[4 * (i + 1) + c];
+        float r[4] = {0.f, 0.f, 0.f, 0.f};
+        if (n_groups == 0)
+            for (int c = 0; c < 4; ++c) r[c] = v[c];
+        for (size_t g = 0; g < n_groups; ++g) {
+            const float* w = weights + 4 * (n_groups * x + g);
+            const uint16_t* jn = joints + 4 * (n_groups * x + g);
+            for (int e = 0; e < 4; ++e) {
+                const float* m = mats[jn[e]].m;
+                for (int c = 0; c < 4; ++c) {
+                    const float t = (m[0 + c] * v[0] + m[4 + c] * v[1]) + (m[8 + c] * v[2] + m[12 + c] * v[3]);
+                    r[c] = r[c] + w[e] * t;
+                }
+            }
+        }
+        for (int c = 0; c < 4; ++c) out[4 * x + c] = r[c];
+    }
+}
+
+// Refit of a flat tree to new vertex positions (n_positions x 4 floats,
+// indexed by tri_idx): corner positions replaced, then every box fitted again
+// with fit_box (OBB::CreateOBBfromPoints) to the corners of its subtree's
+// triangles in leaf (DFS) order. Writes the new root box, node boxes and
+// triangle positions.
+void port_tree_refit(size_t n_nodes, const uint32_t* node_ref, const uint32_t* node_cnt, size_t n_tris,
+                     const uint32_t* tri_idx, const float* positions, size_t n_positions, float* out_root12,
+                     float* out_node_obbs, float* out_tri_pos) {
+    std::vector<V3> pos(3 * n_tris);
+    const float nan = std::numeric_limits<float>::quiet_NaN();
+    for (size_t t = 0; t < n_tris; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t vi = tri_idx[3 * t + k];
+            pos[3 * t + k] = vi < n_positions ? V3{positions[4 * vi], positions[4 * vi + 1], positions[4 * vi + 2]}
+                                              : V3{nan, nan, nan};
+            st3(pos[3 * t + k], out_tri_pos + 9 * t + 3 * k);
+        }
+    auto fit_range = [&](uint32_t first, uint32_t count) {
+        std::vector<V3> pts(pos.begin() + 3 * size_t(first), pos.begin() + 3 * size_t(first + count));
+        return fit_box(pts);
+    };
+    std::vector<std::pair<uint32_t, uint32_t>> rg(n_nodes);
+    for (size_t k = n_nodes; k-- > 0;) {
+        uint32_t lo = 0xffffffffu, hi = 0;
+        for (int s = 0; s < 2; ++s) {
+            const uint32_t ref = node_ref[2 * k + s], cnt = node_cnt[2 * k + s];
+            const std::pair<uint32_t, uint32_t> c = cnt ? std::make_pair(ref, cnt) : rg[ref];
+            stbox(fit_range(c.first, c.second), out_node_obbs + 24 * k + 12 * s);
+            if (c.second) {
+                lo = std::min(lo, c.first);
+                hi = std::max(hi, c.first + c.second);
+            }
+        }
+        rg[k] = lo <= hi ? std::make_pair(lo, hi - lo) : std::make_pair(0u, 0u);
+    }
+    const std::pair<uint32_t, uint32_t> root = n_nodes ? rg[0] : std::make_pair(0u, uint32_t(n_tris));
+    stbox(fit_range(root.first, root.second), out_root12);
+}
+
 }  // extern "C"
