@@ -188,6 +188,99 @@ def run_reference(args) -> dict:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_deforming(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
+    """Deforming workload: per frame, morph + skin all tubes (one batched
+    launch), refit their trees (one batched launch of each refit kernel), and
+    collide every tube with the static heightfield with contacts and rays.
+    Event-timed per phase on `stream`, L2 flushed between frames; beside it the
+    oracle restatement of the same frame on the host cores."""
+    import torch
+
+    import oracle
+    from inmyroom_vulkan_gb300 import capi, scenes
+
+    sc = scenes.deforming()
+    n = sc.vertices.shape[0]
+    V = sc.vertices.shape[1]
+    port = oracle.port(fast=True)
+    rest = port.tree_build(sc.mesh.points, sc.mesh.indices, sc.mesh.normals)
+    field = port.tree_build(sc.field.points, sc.field.indices, sc.field.normals)
+    rest_flat = rest.export()
+    ctx = ctx_factory()
+    ids = [ctx.upload_flat(rest_flat) for _ in range(n)]
+    fid = ctx.upload_flat(field.export())
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    j, w, ib = dev(sc.joints.view(np.int16)), dev(sc.weights), dev(sc.inverse_bind)
+    keep, views, outs = [j, w, ib], [], []
+    for m in range(n):
+        v, mw, jm = dev(sc.vertices[m]), dev(sc.morph_weights[m]), dev(sc.joint_matrices[m])
+        out = torch.zeros((V, 4), dtype=torch.float32, device="cuda")
+        keep += [v, mw, jm]
+        outs.append(out)
+        views.append(capi.cg_deform_view(V, sc.vertices.shape[2] - 1, 1, sc.joint_matrices.shape[1], v.data_ptr(),
+                                         mw.data_ptr(), j.data_ptr(), w.data_ptr(), jm.data_ptr(), ib.data_ptr()))
+    out_ptrs = [o.data_ptr() for o in outs]
+    eye = np.eye(4, dtype=np.float32).reshape(16)
+    q = capi.make_queries(ids, [fid] * n, np.stack([capi.relative_matrix(sc.models[m], eye) for m in range(n)]))
+    d_q = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    flags = capi.CG_CONTACTS
+    sp = stream.cuda_stream
+
+    def frame():
+        ctx.deform_batch(views, out_ptrs, sp)
+        e1.record(stream)
+        ctx.tree_refit_batch(ids, out_ptrs, [V] * n, sp)
+        e2.record(stream)
+        ctx.collide_async(d_q.data_ptr(), n, flags, sp)
+
+    e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    for _ in range(max(args.warmup, 3)):
+        frame()
+    st = ctx.sync_stats()
+    ms, parts = [], []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        e0.record(stream)
+        frame()
+        e3.record(stream)
+        e3.synchronize()
+        ms.append(e0.elapsed_time(e3))
+        parts.append((e0.elapsed_time(e1), e1.elapsed_time(e2), e2.elapsed_time(e3)))
+    st = ctx.sync_stats()
+    assert st["status"] == 0
+    frame_ms = float(np.mean(ms))
+    tests = st["tri_tests"]
+    res = {"workload": f"{n} skinned + morphed tubes ({sc.mesh.n_tris} tris, 50 bones, 8 targets) vs a "
+                       f"{sc.field.n_tris}-triangle heightfield; per frame deform + refit + collide with contacts",
+           "ms_per_frame": frame_ms, "deform_ms": float(np.mean([p[0] for p in parts])),
+           "refit_ms": float(np.mean([p[1] for p in parts])), "collide_ms": float(np.mean([p[2] for p in parts])),
+           "tri_tests_per_frame": int(tests), "tri_pairs_per_frame": int(st["tri_pairs"]),
+           "tri_tests_per_s": tests / (frame_ms / 1e3), "frames": args.steps}
+    ctx.close()
+    if cpu_seconds > 0:
+        from concurrent.futures import ThreadPoolExecutor
+
+        cores = os.cpu_count() or 1
+        pool = ThreadPoolExecutor(cores)
+
+        def cpu_mesh(m):
+            pos = port.deform(sc.vertices[m], sc.morph_weights[m], sc.joints, sc.weights, sc.joint_matrices[m],
+                              sc.inverse_bind)
+            return port.tree_import(port.tree_refit(rest_flat, pos))
+
+        frames, t0 = 0, time.perf_counter()
+        while True:
+            trees = list(pool.map(cpu_mesh, range(n)))
+            port.collide_batch(trees, [field] * n, sc.models, [eye] * n, threads=cores)
+            frames += 1
+            if time.perf_counter() - t0 >= cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"ms_per_frame": 1e3 * el / frames, "cores": cores, "kind": "port",
+                               "sample": f"{frames} whole frames, {el:.1f} s (deform, refit, collide with rays)"}
+    return res
+
+
 def run_gpu(args) -> dict:
     import torch
 
@@ -321,6 +414,10 @@ def run_gpu(args) -> dict:
     ptests = ctx.sync_stats()["tri_tests"]
 
     cpu = cpu_baseline(sc, seconds=args.cpu_seconds) if rank == 0 and args.cpu_seconds > 0 else None
+    deforming = None
+    if rank == 0 and not args.skip_deforming:
+        deforming = run_deforming(args, lambda: capi.Context(device=local, max_queries=4096, max_tri_pairs=1 << 22),
+                                  flush, stream, min(args.cpu_seconds, 5.0))
     clk = clocks.summary()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -350,6 +447,8 @@ def run_gpu(args) -> dict:
     }
     if cpu:
         out["cpu_baseline"] = cpu
+    if deforming:
+        out["deforming"] = deforming
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -363,6 +462,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--skip-deforming", action="store_true", help="leave out the deforming-meshes line")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

@@ -172,6 +172,8 @@ struct cg_ctx {
         void* dev = nullptr;
         size_t cap = 0;
     } deform_table, refit_table;
+    RefitScratch* refit_scratch = nullptr;  // one entry per record of a refit batch
+    uint32_t refit_scratch_cap = 0;
 
     std::string err;
 };
@@ -659,6 +661,7 @@ int cg_destroy(cg_ctx* c) {
     cudaFree(c->d_trees);
     cudaFree(c->deform_table.dev);
     cudaFree(c->refit_table.dev);
+    cudaFree(c->refit_scratch);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
@@ -1052,7 +1055,7 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
     if (!c || (n && (!tree_ids || !positions || !n_positions))) return CG_ERR_INVALID_ARGUMENT;
     if (n == 0) return CG_OK;
     std::vector<RefitTree> table(n);
-    uint32_t max_tris = 0, max_recs = 0;
+    uint32_t max_tris = 0, max_recs = 0, total_recs = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t id = tree_ids[i];
         if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
@@ -1060,7 +1063,8 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
             return fail(c, CG_ERR_INVALID_ARGUMENT, "positions %u must be 16-byte aligned device memory", i);
         const auto& t = c->trees[id];
         table[i] = RefitTree{uint32_t(t.rec_base), uint32_t(t.n_recs), uint32_t(t.tri_base), t.n_tri_used, t.ranges,
-                             reinterpret_cast<const float4*>(positions[i]), n_positions[i], 0u};
+                             reinterpret_cast<const float4*>(positions[i]), n_positions[i], total_recs};
+        total_recs += uint32_t(t.n_recs);
         max_tris = std::max(max_tris, t.n_tri_used);
         max_recs = std::max(max_recs, uint32_t(t.n_recs));
     }
@@ -1069,7 +1073,16 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
     const void* d_table = nullptr;
     int rc = stage_table(c, c->refit_table, table.data(), sizeof(RefitTree) * n, s, &d_table);
     if (rc != CG_OK) return rc;
-    CG_CUDA(launch_refit(c->recs.ptr, c->tris.ptr, static_cast<const RefitTree*>(d_table), n, max_tris, max_recs, s),
+    if (total_recs > c->refit_scratch_cap) {
+        CG_CUDA(cudaStreamSynchronize(s), "refit scratch");
+        cudaFree(c->refit_scratch);
+        c->refit_scratch = nullptr;
+        c->refit_scratch_cap = 0;
+        CG_CUDA(cudaMalloc(&c->refit_scratch, sizeof(RefitScratch) * total_recs), "alloc refit scratch");
+        c->refit_scratch_cap = total_recs;
+    }
+    CG_CUDA(launch_refit(c->recs.ptr, c->tris.ptr, static_cast<const RefitTree*>(d_table), n, max_tris, max_recs,
+                         c->refit_scratch, s),
             "refit kernels");
     return CG_OK;
 }

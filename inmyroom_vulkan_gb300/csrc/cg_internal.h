@@ -202,15 +202,24 @@ cudaError_t deform_smem_limit();
 // Refit (cg_refit.cu): new corner positions of a tree's triangles from a
 // vertex array, then every record's box from its triangle range (x first, y
 // count; y = ~0 marks the unused record). One launch per kernel for a batch
-// of trees (grid.y = tree); the table is in device memory.
+// of trees (grid.y = tree); the table is in device memory, the scratch holds
+// one entry per record of the batch (tree i's from scratch_base).
 struct RefitTree {
     uint32_t rec_base, n_recs, tri_base, n_tris;
     const uint2* ranges;
     const float4* positions;
-    uint32_t n_positions, pad;
+    uint32_t n_positions, scratch_base;
+};
+enum : uint32_t { kRefitSkip = 0, kRefitEmpty = 1, kRefitPoint = 2, kRefitBox = 3 };
+struct RefitScratch {
+    float cov[6];   // xx, yy, zz, xy, xz, yz
+    float axes[9];  // rows: the box axes
+    float p0[3];    // the point of a point box
+    float maxabs;   // largest |x| + |y| + |z| of the points
+    uint32_t kind;
 };
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, cudaStream_t s);
+                         uint32_t max_recs, RefitScratch* scratch, cudaStream_t s);
 
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,

@@ -1,16 +1,26 @@
 // Refit of an uploaded tree to deformed vertices: the topology stays, every
-// box is fitted again to the points of its subtree with
-// OBB::CreateOBBfromPoints (src/Geometry/OBB.cpp:33-89) -- FP64 mean and
-// covariance accumulated point by point, the eig3 eigensystem
-// (eig3/eig3.cpp:21-265: Householder reduction, implicit-shift QL, ascending
-// sort; eigenvectors of the covariance as the box axes), FP64 min/max
-// projections padded by 2 FLT_EPSILON, float cast.
+// box is fitted again to the points of its subtree (the corners of its
+// triangles) the way OBB::CreateOBBfromPoints (src/Geometry/OBB.cpp:33-89)
+// fits a box: mean and covariance of the points, the eig3 eigensystem of the
+// covariance (eig3/eig3.cpp:21-265: Householder reduction, implicit-shift QL,
+// ascending sort) with the rows of its eigenvector matrix as the box axes,
+// min/max projections on the axes padded by 2 FLT_EPSILON.
 //
-// A box's points are the corners of its subtree's triangles in the tree's leaf
-// (DFS) order, corner 0, 1, 2 of each. The sums run in that order, one lane per
-// sum, so every box is the same bits as the host restatement on the same
-// order; the min/max projections are order-free and run over all lanes. One
-// warp per box; the points pass through shared memory 32 triangles at a time.
+// The reference builds trees on the CPU and has no refit; this one is shaped
+// for a part whose FP64 pipe is narrow (a sequential FP64 fit of a
+// 12k-triangle tube's root takes tens of milliseconds here):
+//   refit_moments  compensated FP32 sums of the points and of their centred
+//                  products: a thread per box of up to kSmallPoints points, a
+//                  warp per larger box (lane sums combined with error-free
+//                  FP32 sums)
+//   refit_axes     a thread per box: the eig3 procedure in FP32
+//   refit_box      FP32 projections (thread or warp per box as above); the box
+//                  is padded by 2 FLT_EPSILON plus a bound on the FP32
+//                  rounding of the projections, the axes' departure from
+//                  orthonormal and the box's assembly, so it contains every
+//                  point of its subtree
+// The boxes are conservative like the reference's but not its bits; the
+// colliding triangle pairs found with them are the same.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -23,48 +33,42 @@ namespace cg {
 namespace {
 
 constexpr unsigned kAll = 0xffffffffu;
-constexpr int kRefitWarps = 4;  // warps per block
+constexpr int kRefitWarps = 4;           // warps per block of the warp-per-box kernels
+constexpr uint32_t kSmallPoints = 48;    // boxes up to this many points take one thread
 
-struct D3 {
-    double x, y, z;
-};
-
-__device__ __forceinline__ double dotd(D3 a, D3 b) {
-    double s = a.x * b.x;
-    s = s + a.y * b.y;
-    s = s + a.z * b.z;
-    return s;
+template <typename R>
+__device__ __forceinline__ R hyp(R x, R y) {
+    return sqrt(x * x + y * y);
 }
-
-__device__ __forceinline__ double hyp(double x, double y) { return sqrt(x * x + y * y); }
 
 // Householder reduction of the symmetric 3x3 in v to tridiagonal form
 // (eig3.cpp:21-134): v becomes the accumulated transform, d the diagonal,
 // e[1..2] the sub-diagonal.
-__device__ void tridiagonalize(double v[3][3], double d[3], double e[3]) {
+template <typename R>
+__device__ void tridiagonalize(R v[3][3], R d[3], R e[3]) {
     for (int c = 0; c < 3; ++c) d[c] = v[2][c];
     for (int i = 2; i >= 1; --i) {
-        double scale = 0.0, h = 0.0;
+        R scale = R(0), h = R(0);
         for (int k = 0; k < i; ++k) scale = scale + fabs(d[k]);
-        if (scale == 0.0) {
+        if (scale == R(0)) {
             e[i] = d[i - 1];
             for (int c = 0; c < i; ++c) {
                 d[c] = v[i - 1][c];
-                v[i][c] = 0.0;
-                v[c][i] = 0.0;
+                v[i][c] = R(0);
+                v[c][i] = R(0);
             }
         } else {
             for (int k = 0; k < i; ++k) {
                 d[k] = d[k] / scale;
                 h = h + d[k] * d[k];
             }
-            double f = d[i - 1];
-            double g = sqrt(h);
+            R f = d[i - 1];
+            R g = sqrt(h);
             if (f > 0) g = -g;
             e[i] = scale * g;
             h = h - f * g;
             d[i - 1] = f - g;
-            for (int c = 0; c < i; ++c) e[c] = 0.0;
+            for (int c = 0; c < i; ++c) e[c] = R(0);
             for (int c = 0; c < i; ++c) {
                 f = d[c];
                 v[c][i] = f;
@@ -75,55 +79,55 @@ __device__ void tridiagonalize(double v[3][3], double d[3], double e[3]) {
                 }
                 e[c] = g;
             }
-            f = 0.0;
+            f = R(0);
             for (int c = 0; c < i; ++c) {
                 e[c] = e[c] / h;
                 f = f + e[c] * d[c];
             }
-            const double hh = f / (h + h);
+            const R hh = f / (h + h);
             for (int c = 0; c < i; ++c) e[c] = e[c] - hh * d[c];
             for (int c = 0; c < i; ++c) {
                 f = d[c];
                 g = e[c];
                 for (int k = c; k <= i - 1; ++k) v[k][c] = v[k][c] - (f * e[k] + g * d[k]);
                 d[c] = v[i - 1][c];
-                v[i][c] = 0.0;
+                v[i][c] = R(0);
             }
         }
         d[i] = h;
     }
     for (int i = 0; i < 2; ++i) {
         v[2][i] = v[i][i];
-        v[i][i] = 1.0;
-        const double h = d[i + 1];
-        if (h != 0.0) {
+        v[i][i] = R(1);
+        const R h = d[i + 1];
+        if (h != R(0)) {
             for (int k = 0; k <= i; ++k) d[k] = v[k][i + 1] / h;
             for (int c = 0; c <= i; ++c) {
-                double g = 0.0;
+                R g = R(0);
                 for (int k = 0; k <= i; ++k) g = g + v[k][i + 1] * v[k][c];
                 for (int k = 0; k <= i; ++k) v[k][c] = v[k][c] - g * d[k];
             }
         }
-        for (int k = 0; k <= i; ++k) v[k][i + 1] = 0.0;
+        for (int k = 0; k <= i; ++k) v[k][i + 1] = R(0);
     }
     for (int c = 0; c < 3; ++c) {
         d[c] = v[2][c];
-        v[2][c] = 0.0;
+        v[2][c] = R(0);
     }
-    v[2][2] = 1.0;
-    e[0] = 0.0;
+    v[2][2] = R(1);
+    e[0] = R(0);
 }
 
 // Implicit-shift QL on the tridiagonal form, then the ascending sort of the
 // eigenvalues with their eigenvector columns (eig3.cpp:138-254). A sweep
 // count limit stops what only a non-finite input could run forever.
-__device__ void ql_sort(double v[3][3], double d[3], double e[3]) {
+template <typename R>
+__device__ void ql_sort(R v[3][3], R d[3], R e[3], R eps) {
     for (int i = 1; i < 3; ++i) e[i - 1] = e[i];
-    e[2] = 0.0;
-    double f = 0.0, tst1 = 0.0;
-    const double eps = 2.220446049250313e-16;  // 2^-52
+    e[2] = R(0);
+    R f = 0, tst1 = 0;
     for (int l = 0; l < 3; ++l) {
-        const double t = fabs(d[l]) + fabs(e[l]);
+        const R t = fabs(d[l]) + fabs(e[l]);
         tst1 = (tst1 > t) ? tst1 : t;
         int m = l;
         while (m < 3) {
@@ -134,20 +138,20 @@ __device__ void ql_sort(double v[3][3], double d[3], double e[3]) {
             int sweeps = 0;
             do {
                 ++sweeps;
-                double g = d[l];
-                double p = (d[l + 1] - g) / (2.0 * e[l]);
-                double r = hyp(p, 1.0);
+                R g = d[l];
+                R p = (d[l + 1] - g) / (R(2) * e[l]);
+                R r = hyp(p, R(1));
                 if (p < 0) r = -r;
                 d[l] = e[l] / (p + r);
                 d[l + 1] = e[l] * (p + r);
-                const double dl1 = d[l + 1];
-                double h = g - d[l];
+                const R dl1 = d[l + 1];
+                R h = g - d[l];
                 for (int i = l + 2; i < 3; ++i) d[i] = d[i] - h;
                 f = f + h;
                 p = d[m];
-                double c = 1.0, c2 = c, c3 = c;
-                const double el1 = e[l + 1];
-                double s = 0.0, s2 = 0.0;
+                R c = R(1), c2 = c, c3 = c;
+                const R el1 = e[l + 1];
+                R s = R(0), s2 = R(0);
                 for (int i = m - 1; i >= l; --i) {
                     c3 = c2;
                     c2 = c;
@@ -172,11 +176,11 @@ __device__ void ql_sort(double v[3][3], double d[3], double e[3]) {
             } while (fabs(e[l]) > eps * tst1 && sweeps < 10000);
         }
         d[l] = d[l] + f;
-        e[l] = 0.0;
+        e[l] = R(0);
     }
     for (int i = 0; i < 2; ++i) {
         int k = i;
-        double p = d[i];
+        R p = d[i];
         for (int j = i + 1; j < 3; ++j)
             if (d[j] < p) {
                 k = j;
@@ -186,7 +190,7 @@ __device__ void ql_sort(double v[3][3], double d[3], double e[3]) {
             d[k] = d[i];
             d[i] = p;
             for (int r = 0; r < 3; ++r) {
-                const double tmp = v[r][i];
+                const R tmp = v[r][i];
                 v[r][i] = v[r][k];
                 v[r][k] = tmp;
             }
@@ -194,25 +198,44 @@ __device__ void ql_sort(double v[3][3], double d[3], double e[3]) {
     }
 }
 
-__device__ __forceinline__ float3 corner(const float4* tris, uint32_t tri, int k) {
-    const float4 q = tris[3ull * tri + k];
-    return make_float3(q.x, q.y, q.z);
+// Compensated running sum (Kahan): s - c carries the sum of the added values.
+struct KSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// Error-free sum of two floats (Knuth's two-sum): a + b = hi + lo exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& hi, float& lo) {
+    hi = a + b;
+    const float bb = hi - a;
+    lo = (a - (hi - bb)) + (b - bb);
 }
 
-__device__ __forceinline__ double warp_min(double v) {
+// Sum over the warp of the lanes' (hi, lo) pairs, kept as a float pair.
+__device__ __forceinline__ void warp_sum2(float& hi, float& lo) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double w = __shfl_xor_sync(kAll, v, o);
-        v = w < v ? w : v;
+        const float oh = __shfl_xor_sync(kAll, hi, o), ol = __shfl_xor_sync(kAll, lo, o);
+        float h, l;
+        two_sum(hi, oh, h, l);
+        hi = h;
+        lo = (lo + ol) + l;
     }
+}
+
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kAll, v, o));
     return v;
 }
-__device__ __forceinline__ double warp_max(double v) {
+__device__ __forceinline__ float warp_minf(float v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double w = __shfl_xor_sync(kAll, v, o);
-        v = w > v ? w : v;
-    }
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kAll, v, o));
     return v;
 }
 
@@ -222,157 +245,276 @@ __global__ void refit_tris_kernel(float4* tris, const RefitTree* trees) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 3u * T.n_tris) return;
     float4* q = tris + 3ull * T.tri_base + i;
-    const float4* positions = T.positions;
-    const uint32_t n_positions = T.n_positions;
     const uint32_t vi = __float_as_uint(q->w);
     const float nan = __int_as_float(0x7fc00000);
-    const float4 p = vi < n_positions ? positions[vi] : make_float4(nan, nan, nan, 0.f);
+    const float4 p = vi < T.n_positions ? T.positions[vi] : make_float4(nan, nan, nan, 0.f);
     q->x = p.x;
     q->y = p.y;
     q->z = p.z;
 }
 
-// One warp per record of the tree; record r covers tree-local triangles
-// [range.x, range.x + range.y).
-__global__ void __launch_bounds__(32 * kRefitWarps) refit_boxes_kernel(float4* recs, const float4* tris,
-                                                                        const RefitTree* trees) {
-    __shared__ float stage[kRefitWarps][3][96];
+// The moments of one box's points, by one lane (lanes = 1) or a whole warp.
+struct Moments {
+    KSum s[3];    // x, y, z
+    KSum c[6];    // xx, yy, zz, xy, xz, yz of the centred points
+    float mabs = 0.f;
+    bool differ = false;
+};
+
+__device__ __forceinline__ void record_out(RefitScratch& out, float4 p0, bool differ, float mabs, const float* cov) {
+    if (!differ) {
+        out.kind = kRefitPoint;
+        out.p0[0] = p0.x;
+        out.p0[1] = p0.y;
+        out.p0[2] = p0.z;
+        return;
+    }
+    out.kind = kRefitBox;
+    out.maxabs = mabs;
+    for (int i = 0; i < 6; ++i) out.cov[i] = cov[i];
+}
+
+// Thread per small box: the count, whether two points differ, the largest
+// |x| + |y| + |z| and the covariance.
+__global__ void refit_moments_small_kernel(const float4* tris, const RefitTree* trees, RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= T.n_recs) return;
+    const uint2 rg = T.ranges[r];
+    RefitScratch& out = scratch[T.scratch_base + r];
+    if (rg.y == ~0u || rg.y == 0u) {
+        out.kind = rg.y == ~0u ? kRefitSkip : kRefitEmpty;
+        return;
+    }
+    const uint32_t n_pts = 3u * rg.y;
+    if (n_pts > kSmallPoints) return;  // the warp kernel's
+    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
+    const float4 p0 = pt[0];
+    KSum sx, sy, sz;
+    float mabs = 0.f;
+    bool differ = false;
+    for (uint32_t k = 0; k < n_pts; ++k) {
+        const float4 p = pt[k];
+        sx.add(p.x);
+        sy.add(p.y);
+        sz.add(p.z);
+        mabs = fmaxf(mabs, (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z));
+        differ |= p.x != p0.x || p.y != p0.y || p.z != p0.z;
+    }
+    const float fn = float(n_pts);
+    const float mx = (sx.s - sx.c) / fn, my = (sy.s - sy.c) / fn, mz = (sz.s - sz.c) / fn;
+    KSum c[6];
+    for (uint32_t k = 0; k < n_pts && differ; ++k) {
+        const float4 p = pt[k];
+        const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
+        c[0].add(dx * dx);
+        c[1].add(dy * dy);
+        c[2].add(dz * dz);
+        c[3].add(dx * dy);
+        c[4].add(dx * dz);
+        c[5].add(dy * dz);
+    }
+    float cov[6];
+    for (int i = 0; i < 6; ++i) cov[i] = (c[i].s - c[i].c) / fn;
+    record_out(out, p0, differ, mabs, cov);
+}
+
+// Warp per large box: the same over all lanes, combined with error-free sums.
+__global__ void __launch_bounds__(32 * kRefitWarps) refit_moments_kernel(const float4* tris, const RefitTree* trees,
+                                                                          RefitScratch* scratch) {
     const RefitTree T = trees[blockIdx.y];
     const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const uint32_t r = blockIdx.x * kRefitWarps + uint32_t(w);
+    const uint32_t r = blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
     if (r >= T.n_recs) return;  // whole warps
-    const uint32_t rec_base = T.rec_base, tri_base = T.tri_base;
-    const uint2* ranges = T.ranges;
-    const uint2 rg = ranges[r];
-    if (rg.y == ~0u) return;  // the unused record of the tree's first pair
-    float* sx = stage[w][0];
-    float* sy = stage[w][1];
-    float* sz = stage[w][2];
-    const uint32_t t0 = tri_base + rg.x;
+    const uint2 rg = T.ranges[r];
+    if (rg.y == ~0u || 3ull * rg.y <= kSmallPoints) return;  // the small kernel's
+    RefitScratch& out = scratch[T.scratch_base + r];
     const uint32_t n_pts = 3u * rg.y;
-    float4* out = recs + 4ull * (rec_base + r);
-
-    Box b;
-    if (n_pts == 0) {
-        b.c = make_float3(0.f, 0.f, 0.f);
-        b.u = make_float3(FLT_EPSILON, 0.f, 0.f);
-        b.v = make_float3(0.f, FLT_EPSILON, 0.f);
-        b.w = make_float3(0.f, 0.f, FLT_EPSILON);
-    } else {
-        // fewer than two distinct points: the point box (OBB.cpp:36-44)
-        const float3 p0 = corner(tris, t0, 0);
-        bool differ = false;
-        for (uint32_t k = lane; k < n_pts; k += 32) {
-            const float3 p = corner(tris, t0 + k / 3u, int(k % 3u));
-            differ |= p.x != p0.x || p.y != p0.y || p.z != p0.z;
-        }
-        if (!__any_sync(kAll, differ)) {
-            b.c = p0;
-            b.u = make_float3(FLT_EPSILON, 0.f, 0.f);
-            b.v = make_float3(0.f, FLT_EPSILON, 0.f);
-            b.w = make_float3(0.f, 0.f, FLT_EPSILON);
-        } else {
-            const double n = double(n_pts);
-            // pass 1: sums of x, y, z (lanes 0, 1, 2), point by point
-            double acc = 0.0;
-            double mx = 0.0, my = 0.0, mz = 0.0;
-            for (int pass = 0; pass < 2; ++pass) {
-                acc = 0.0;
-                for (uint32_t c0 = 0; c0 < rg.y; c0 += 32) {
-                    const uint32_t nt = min(32u, rg.y - c0);
-                    __syncwarp();
-                    if (uint32_t(lane) < nt)
-                        for (int k = 0; k < 3; ++k) {
-                            const float3 p = corner(tris, t0 + c0 + lane, k);
-                            sx[3 * lane + k] = p.x;
-                            sy[3 * lane + k] = p.y;
-                            sz[3 * lane + k] = p.z;
-                        }
-                    __syncwarp();
-                    const uint32_t np = 3u * nt;
-                    if (pass == 0) {
-                        if (lane < 3) {
-                            const float* s = lane == 0 ? sx : (lane == 1 ? sy : sz);
-                            for (uint32_t k = 0; k < np; ++k) acc = acc + double(s[k]);
-                        }
-                    } else if (lane < 6) {
-                        // cxx, cyy, czz, cxy, cxz, cyz
-                        const float* s1 = (lane == 0 || lane == 3 || lane == 4) ? sx : (lane == 1 || lane == 5 ? sy : sz);
-                        const float* s2 = (lane == 0) ? sx : (lane == 1 || lane == 3) ? sy : sz;
-                        const double m1 = (lane == 0 || lane == 3 || lane == 4) ? mx : (lane == 1 || lane == 5 ? my : mz);
-                        const double m2 = (lane == 0) ? mx : (lane == 1 || lane == 3) ? my : mz;
-                        for (uint32_t k = 0; k < np; ++k) acc = acc + (double(s1[k]) - m1) * (double(s2[k]) - m2);
-                    }
-                }
-                if (pass == 0) {
-                    mx = __shfl_sync(kAll, acc, 0) / n;
-                    my = __shfl_sync(kAll, acc, 1) / n;
-                    mz = __shfl_sync(kAll, acc, 2) / n;
-                }
-            }
-            const double cxx = __shfl_sync(kAll, acc, 0), cyy = __shfl_sync(kAll, acc, 1);
-            const double czz = __shfl_sync(kAll, acc, 2), cxy = __shfl_sync(kAll, acc, 3);
-            const double cxz = __shfl_sync(kAll, acc, 4), cyz = __shfl_sync(kAll, acc, 5);
-            double ax[9];
-            if (lane == 0) {
-                double v[3][3] = {{cxx / n, cxy / n, cxz / n}, {cxy / n, cyy / n, cyz / n}, {cxz / n, cyz / n, czz / n}};
-                double d[3], e[3];
-                tridiagonalize(v, d, e);
-                ql_sort(v, d, e);
-                // the box axes are the rows of the eigenvector matrix
-                for (int i = 0; i < 3; ++i)
-                    for (int j = 0; j < 3; ++j) ax[3 * i + j] = v[i][j];
-            }
+    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
+    const float4 p0 = pt[0];
+    KSum sx, sy, sz;
+    float mabs = 0.f;
+    bool differ = false;
+    for (uint32_t k = lane; k < n_pts; k += 32) {
+        const float4 p = pt[k];
+        sx.add(p.x);
+        sy.add(p.y);
+        sz.add(p.z);
+        mabs = fmaxf(mabs, (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z));
+        differ |= p.x != p0.x || p.y != p0.y || p.z != p0.z;
+    }
+    differ = __any_sync(kAll, differ);
+    mabs = warp_maxf(mabs);
+    if (!differ) {
+        if (lane == 0) record_out(out, p0, false, mabs, nullptr);
+        return;
+    }
+    float hx = sx.s, lx = -sx.c, hy = sy.s, ly = -sy.c, hz = sz.s, lz = -sz.c;
+    warp_sum2(hx, lx);
+    warp_sum2(hy, ly);
+    warp_sum2(hz, lz);
+    const float fn = float(n_pts);
+    const float mx = (hx + lx) / fn, my = (hy + ly) / fn, mz = (hz + lz) / fn;
+    KSum c[6];
+    for (uint32_t k = lane; k < n_pts; k += 32) {
+        const float4 p = pt[k];
+        const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
+        c[0].add(dx * dx);
+        c[1].add(dy * dy);
+        c[2].add(dz * dz);
+        c[3].add(dx * dy);
+        c[4].add(dx * dz);
+        c[5].add(dy * dz);
+    }
+    float cov[6];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) ax[i] = __shfl_sync(kAll, ax[i], 0);
-            // OBB::CreateAABBfromPoints on those axes (OBB.cpp:105-166)
-            const double pad = 2.0 * double(FLT_EPSILON);
-            double cx = 0.0, cy = 0.0, cz = 0.0;
-            float3 half[3];
-            for (int a = 0; a < 3; ++a) {
-                const D3 axis{ax[3 * a], ax[3 * a + 1], ax[3 * a + 2]};
-                double lo = __longlong_as_double(0x7ff0000000000000ll), hi = -lo;
-                for (uint32_t k = lane; k < n_pts; k += 32) {
-                    const float3 p = corner(tris, t0 + k / 3u, int(k % 3u));
-                    const double pr = dotd(axis, D3{double(p.x), double(p.y), double(p.z)});
-                    lo = (lo < pr) ? lo : pr;
-                    hi = (pr < hi) ? hi : pr;
-                }
-                lo = warp_min(lo);
-                hi = warp_max(hi);
-                const double delta = (hi - lo) + pad;
-                const double mid = (hi + lo) / 2.0;
-                cx = cx + mid * axis.x;
-                cy = cy + mid * axis.y;
-                cz = cz + mid * axis.z;
-                const double h = delta / 2.0;
-                half[a] = make_float3(float(h * axis.x), float(h * axis.y), float(h * axis.z));
-            }
-            b.c = make_float3(float(cx), float(cy), float(cz));
-            b.u = half[0];
-            b.v = half[1];
-            b.w = half[2];
+    for (int i = 0; i < 6; ++i) {
+        float h = c[i].s, l = -c[i].c;
+        warp_sum2(h, l);
+        cov[i] = (h + l) / fn;
+    }
+    if (lane == 0) record_out(out, p0, true, mabs, cov);
+}
+
+// One thread per record: the eigensystem of the covariance by the eig3
+// procedure in FP32 (the covariance carries FP32 accuracy); the box axes are
+// the rows of the eigenvector matrix, as the reference takes them.
+__global__ void refit_axes_kernel(const RefitTree* trees, RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= T.n_recs) return;
+    RefitScratch& sc = scratch[T.scratch_base + r];
+    if (sc.kind != kRefitBox) return;
+    const float* c = sc.cov;  // xx, yy, zz, xy, xz, yz
+    float v[3][3] = {{c[0], c[3], c[4]}, {c[3], c[1], c[5]}, {c[4], c[5], c[2]}};
+    float d[3], e[3];
+    tridiagonalize(v, d, e);
+    ql_sort(v, d, e, FLT_EPSILON);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) sc.axes[3 * i + j] = v[i][j];
+}
+
+// The box from its axes and the projections' min and max per axis. The pad
+// adds to the reference's 2 FLT_EPSILON a bound, 2^-20 * (M + extent) with M
+// the largest |x| + |y| + |z|, on the FP32 rounding of a projection
+// (3 * 2^-24 * M), of the axes' departure from orthonormal and of the box's
+// FP32 assembly, so every point stays inside.
+__device__ __forceinline__ Box assemble(const float ax[9], const float lo[3], const float hi[3], float maxabs) {
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    float3 half[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ext = hi[a] - lo[a];
+        const float pad = 2.f * FLT_EPSILON + 8.f * FLT_EPSILON * (maxabs + ext);
+        const float mid = 0.5f * (hi[a] + lo[a]);
+        const float h2 = 0.5f * ext + pad;
+        cx = cx + mid * ax[3 * a];
+        cy = cy + mid * ax[3 * a + 1];
+        cz = cz + mid * ax[3 * a + 2];
+        half[a] = make_float3(h2 * ax[3 * a], h2 * ax[3 * a + 1], h2 * ax[3 * a + 2]);
+    }
+    return Box{make_float3(cx, cy, cz), half[0], half[1], half[2]};
+}
+
+__device__ __forceinline__ Box special_box(const RefitScratch& sc) {
+    Box b;
+    b.c = sc.kind == kRefitPoint ? make_float3(sc.p0[0], sc.p0[1], sc.p0[2]) : make_float3(0.f, 0.f, 0.f);
+    b.u = make_float3(FLT_EPSILON, 0.f, 0.f);
+    b.v = make_float3(0.f, FLT_EPSILON, 0.f);
+    b.w = make_float3(0.f, 0.f, FLT_EPSILON);
+    return b;
+}
+
+__device__ __forceinline__ void write_box(float4* recs, uint32_t rec, const Box& b) {
+    float4* out = recs + 4ull * rec;
+    const float4 q3 = out[3];
+    out[0] = make_float4(b.c.x, b.c.y, b.c.z, b.u.x);
+    out[1] = make_float4(b.u.y, b.u.z, b.v.x, b.v.y);
+    out[2] = make_float4(b.v.z, b.w.x, b.w.y, b.w.z);
+    out[3] = make_float4(q3.x, q3.y, surface(b), q3.w);
+}
+
+// Thread per small box (and every empty or point box).
+__global__ void refit_box_small_kernel(float4* recs, const float4* tris, const RefitTree* trees,
+                                       const RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= T.n_recs) return;
+    const RefitScratch& sc = scratch[T.scratch_base + r];
+    if (sc.kind == kRefitSkip) return;
+    const uint2 rg = T.ranges[r];
+    const uint32_t n_pts = 3u * rg.y;
+    if (sc.kind != kRefitBox) {
+        write_box(recs, T.rec_base + r, special_box(sc));
+        return;
+    }
+    if (n_pts > kSmallPoints) return;  // the warp kernel's
+    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
+    float ax[9];
+    for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
+    const float inf = __int_as_float(0x7f800000);
+    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+    for (uint32_t k = 0; k < n_pts; ++k) {
+        const float4 p = pt[k];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float pr = (ax[3 * a] * p.x + ax[3 * a + 1] * p.y) + ax[3 * a + 2] * p.z;
+            lo[a] = fminf(lo[a], pr);
+            hi[a] = fmaxf(hi[a], pr);
         }
     }
-    if (lane == 0) {
-        const float4 q3 = out[3];
-        out[0] = make_float4(b.c.x, b.c.y, b.c.z, b.u.x);
-        out[1] = make_float4(b.u.y, b.u.z, b.v.x, b.v.y);
-        out[2] = make_float4(b.v.z, b.w.x, b.w.y, b.w.z);
-        out[3] = make_float4(q3.x, q3.y, surface(b), q3.w);
+    write_box(recs, T.rec_base + r, assemble(ax, lo, hi, sc.maxabs));
+}
+
+// Warp per large box.
+__global__ void __launch_bounds__(32 * kRefitWarps) refit_box_kernel(float4* recs, const float4* tris,
+                                                                      const RefitTree* trees,
+                                                                      const RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const uint32_t r = blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
+    if (r >= T.n_recs) return;  // whole warps
+    const uint2 rg = T.ranges[r];
+    if (rg.y == ~0u || 3ull * rg.y <= kSmallPoints) return;  // the small kernel's
+    const RefitScratch& sc = scratch[T.scratch_base + r];
+    if (sc.kind != kRefitBox) return;  // written by the small kernel
+    const uint32_t n_pts = 3u * rg.y;
+    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
+    float ax[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
+    const float inf = __int_as_float(0x7f800000);
+    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+    for (uint32_t k = lane; k < n_pts; k += 32) {
+        const float4 p = pt[k];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float pr = (ax[3 * a] * p.x + ax[3 * a + 1] * p.y) + ax[3 * a + 2] * p.z;
+            lo[a] = fminf(lo[a], pr);
+            hi[a] = fmaxf(hi[a], pr);
+        }
     }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = warp_minf(lo[a]);
+        hi[a] = warp_maxf(hi[a]);
+    }
+    if (lane == 0) write_box(recs, T.rec_base + r, assemble(ax, lo, hi, sc.maxabs));
 }
 
 }  // namespace
 
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, cudaStream_t s) {
+                         uint32_t max_recs, RefitScratch* scratch, cudaStream_t s) {
     if (n_trees == 0) return cudaSuccess;
-    if (max_tris)
-        refit_tris_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees);
-    refit_boxes_kernel<<<dim3((max_recs + kRefitWarps - 1) / kRefitWarps, n_trees), 32 * kRefitWarps, 0, s>>>(
-        recs, tris, d_trees);
+    if (max_tris) refit_tris_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees);
+    const dim3 threads((max_recs + 127u) / 128u, n_trees);
+    const dim3 warps((max_recs + kRefitWarps - 1) / kRefitWarps, n_trees);
+    refit_moments_small_kernel<<<threads, 128, 0, s>>>(tris, d_trees, scratch);
+    refit_moments_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(tris, d_trees, scratch);
+    refit_axes_kernel<<<threads, 128, 0, s>>>(d_trees, scratch);
+    refit_box_small_kernel<<<threads, 128, 0, s>>>(recs, tris, d_trees, scratch);
+    refit_box_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(recs, tris, d_trees, scratch);
     return cudaGetLastError();
 }
 

@@ -1,7 +1,9 @@
 """Deforming meshes on the GPU against the oracle: morph + linear-blend
-skinning (the engine's skinning shader, restated), the tree refit to the
-deformed vertices, and the triangle pairs of refitted trees against a
-heightfield -- all bit for bit."""
+skinning (the engine's skinning shader, restated) bit for bit; the tree refit
+to the deformed vertices (boxes that contain their subtrees, with axes from the same eigen procedure; where the covariance is nearly
+degenerate, as across a tube, any axes fit, so boxes are not compared
+directly); the colliding triangle pairs of refitted trees against a
+heightfield, which do not depend on the boxes, bit for bit."""
 import numpy as np
 import pytest
 
@@ -51,11 +53,41 @@ def test_deform_bit_exact(port):
             assert np.abs(got[:, :3] - sc.vertices[m][:, 0, :3]).max() > 0.05  # it did deform
 
 
-def test_refit_and_collide_bit_exact(port):
+def record_ranges(ft):
+    """(first, count) of the subtree triangles of the root and every child box."""
+    n = ft.n_nodes
+    node_rg = [None] * n
+    boxes = []
+    for k in range(n - 1, -1, -1):
+        rs = []
+        for s2 in range(2):
+            ref, cnt = int(ft.node_ref[k, s2]), int(ft.node_cnt[k, s2])
+            rs.append((ref, cnt) if cnt else node_rg[ref])
+        lo = min(r[0] for r in rs if r[1])
+        hi = max(r[0] + r[1] for r in rs if r[1])
+        node_rg[k] = (lo, hi - lo)
+        boxes.append((k, rs))
+    root = node_rg[0] if n else (0, ft.n_tris)
+    return root, dict(boxes)
+
+
+def contains(box, pts):
+    """max |t| over points p = c + t_u u + t_v v + t_w w (FP64)."""
+    c = box[0:3].astype(np.float64)
+    H = np.stack([box[3:6], box[6:9], box[9:12]], 1).astype(np.float64)
+    t = np.linalg.solve(H, (pts.astype(np.float64) - c).T)
+    return np.abs(t).max()
+
+
+def test_refit_contains_and_collides_like_oracle(port):
+    """The refit boxes contain every corner of their subtree; the colliding
+    triangle pairs (and segments) against a heightfield equal the oracle's on
+    its own FP64 refit of the same deformed vertices."""
     torch = pytest.importorskip("torch")
     sc = scenes.deforming(n_meshes=4, rings=40, around=24, grid=96)
     rest = port.tree_build(sc.mesh.points, sc.mesh.indices, sc.mesh.normals).export()
     field = port.tree_build(sc.field.points, sc.field.indices, sc.field.normals)
+    root_rg, node_rgs = record_ranges(rest)
     with capi.Context() as ctx:
         outs, _ = deform_on_gpu(torch, ctx, sc)
         ids = [ctx.upload_flat(rest) for _ in range(4)]
@@ -68,16 +100,19 @@ def test_refit_and_collide_bit_exact(port):
             want = port.tree_refit(rest, pos)
             root, obbs, tri = ctx.tree_download(ids[m], rest.n_nodes, rest.n_tris)
             assert np.array_equal(tri.view(np.uint32), want.tri_pos.view(np.uint32)), m
-            assert np.array_equal(root.view(np.uint32), want.root.view(np.uint32)), m
-            assert np.array_equal(obbs.view(np.uint32), want.node_obbs.view(np.uint32)), m
-            assert not np.array_equal(obbs, rest.node_obbs)
+            corners = tri.reshape(-1, 3, 3)
+            pts = lambda rg: corners[rg[0]:rg[0] + rg[1]].reshape(-1, 3)  # noqa: E731
+            worst = contains(root, pts(root_rg))
+            for k, rs in node_rgs.items():
+                for s2 in range(2):
+                    worst = max(worst, contains(obbs[k, s2], pts(rs[s2])))
+            assert worst <= 1.0, (m, worst)
             refit_port.append(port.tree_import(want))
-        # the refitted tubes against the heightfield
         eye = np.eye(4, dtype=np.float32).reshape(16)
         rel = np.stack([capi.relative_matrix(sc.models[m], eye) for m in range(4)])
         st = ctx.collide(capi.make_queries(ids, [fid] * 4, rel))
         pairs, segs, tests, nleaf = port.collide_pairs(refit_port, [field] * 4, sc.models, [eye] * 4)
-        assert st["status"] == 0 and st["tri_tests"] == tests and st["tri_pairs"] == len(pairs) > 0
+        assert st["status"] == 0 and st["tri_pairs"] == len(pairs) > 0
         got = ctx.tri_pairs()
         key = lambda q, a, b, s: np.lexsort(np.c_[q, a, b, np.ascontiguousarray(s, np.float32).view(np.uint32)].T[::-1])
         gs = np.concatenate([got["source"], got["target"]], 1)
