@@ -188,6 +188,84 @@ def run_reference(args) -> dict:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_differentiable(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
+    """Differentiable workload on the deforming scene: forward = pose the 64
+    skeletons from axis angles, morph + skin, refit, collide, penetration
+    energy; backward = the energy's adjoint to the axis angles and morph
+    weights (recomputing deformed vertices). Both event-timed on `stream`, L2
+    flushed before each forward. Beside it, the FP64 reference gradient of the
+    same pair set on the host (torch autograd on the CPU)."""
+    import torch
+
+    import oracle
+    from inmyroom_vulkan_gb300 import capi, scenes
+    from inmyroom_vulkan_gb300.energy import DeformingCollider, penetration_energy
+
+    sc = scenes.deforming()
+    n = sc.vertices.shape[0]
+    parent, offsets = scenes.chain_skeleton(sc)
+    port = oracle.port(fast=True)
+    rest = port.tree_build(sc.mesh.points, sc.mesh.indices, sc.mesh.normals)
+    field = port.tree_build(sc.field.points, sc.field.indices, sc.field.normals)
+    rf, ff = rest.export(), field.export()
+    ctx = ctx_factory()
+    fid = ctx.upload_flat(ff)
+    eye = np.eye(4, dtype=np.float32).reshape(16)
+    rel = np.stack([capi.relative_matrix(m, eye) for m in sc.models])
+    col = DeformingCollider(ctx, rf, capi.Skeleton(parent, offsets), sc.vertices, sc.joints, sc.weights,
+                            sc.inverse_bind, fid, rel)
+    aa = torch.tensor(sc.axis_angles, dtype=torch.float32, device="cuda", requires_grad=True)
+    mw = torch.tensor(sc.morph_weights, dtype=torch.float32, device="cuda", requires_grad=True)
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            aa.grad = mw.grad = None
+            penetration_energy(aa, mw, col).backward()
+        fwd, bwd = [], []
+        for k in range(args.steps):
+            aa.grad = mw.grad = None
+            flush.fill_(k & 0xff)
+            e0.record(stream)
+            E = penetration_energy(aa, mw, col)
+            e1.record(stream)
+            E.backward()
+            e2.record(stream)
+            e2.synchronize()
+            fwd.append(e0.elapsed_time(e1))
+            bwd.append(e1.elapsed_time(e2))
+    st = ctx.sync_stats()
+    assert st["status"] == 0
+    pairs = col.tri_pairs()
+    f_ms, b_ms = float(np.mean(fwd)), float(np.mean(bwd))
+    res = {"workload": f"{n} tubes ({sc.mesh.n_tris} tris, 50 bones, 8 targets) vs a {sc.field.n_tris}-triangle "
+                       "heightfield; E = sum of squared plane-penetration depths over colliding pairs; "
+                       "gradients to 64x50x3 axis angles and 64x8 morph weights",
+           "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+           "energy": float(E.item()), "colliding_pairs": int(len(pairs)), "steps": args.steps,
+           "forward": "pose + deform + refit + collide + energy kernels", "backward":
+           "vertex-gradient + skin-adjoint + pose-adjoint kernels (deformed vertices recomputed)"}
+    col.close()
+    ctx.free_tree(fid)
+    ctx.close()
+    if cpu_seconds > 0:
+        from oracle import energy as oe
+
+        arr = np.stack([pairs["query"], pairs["tri_a"], pairs["tri_b"]], 1).astype(np.int64)
+        pr = oe.Problem(parent, offsets.astype(np.float64), sc.inverse_bind, sc.vertices, sc.joints, sc.weights,
+                        rf.tri_idx, ff.tri_pos, rel, arr)
+        runs, t0 = 0, time.perf_counter()
+        while True:
+            pr.value_and_grad(sc.axis_angles, sc.morph_weights.astype(np.float64))
+            runs += 1
+            if time.perf_counter() - t0 >= cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"ms_forward_backward": 1e3 * el / runs, "cores": torch.get_num_threads(),
+                               "kind": "port", "sample": f"{runs} FP64 torch-autograd energy + gradient evaluations "
+                                                         "on the host (same pair set, no collide)"}
+    return res
+
+
 def run_deforming(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
     """Deforming workload: per frame, morph + skin all tubes (one batched
     launch), refit their trees (one batched launch of each refit kernel), and
@@ -418,6 +496,11 @@ def run_gpu(args) -> dict:
     if rank == 0 and not args.skip_deforming:
         deforming = run_deforming(args, lambda: capi.Context(device=local, max_queries=4096, max_tri_pairs=1 << 22),
                                   flush, stream, min(args.cpu_seconds, 5.0))
+    differentiable = None
+    if rank == 0 and not args.skip_deforming:
+        differentiable = run_differentiable(
+            args, lambda: capi.Context(device=local, max_queries=4096, max_tri_pairs=1 << 22), flush, stream,
+            min(args.cpu_seconds, 5.0))
     clk = clocks.summary()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -449,6 +532,8 @@ def run_gpu(args) -> dict:
         out["cpu_baseline"] = cpu
     if deforming:
         out["deforming"] = deforming
+    if differentiable:
+        out["differentiable"] = differentiable
     ctx.close()
     if dist:
         dist.destroy_process_group()

@@ -298,6 +298,68 @@ int cg_tree_refit_batch(cg_ctx* ctx, const uint32_t* tree_ids, const float* cons
 int cg_tree_download(cg_ctx* ctx, uint32_t tree_id, cg_obb* root, cg_obb* node_obbs, uint32_t node_count,
                      float* triangles_position, uint32_t triangle_count);
 
+/* ---- Differentiable penetration energy (no reference counterpart: the
+ * engine does not differentiate its collision response) ----
+ *
+ * Skeleton posing from per-bone axis-angle rotations: bone j's world matrix is
+ * G_j = G_parent(j) * T(offset_j) * R(a_j) (G of a root = T(offset_j) * R(a_j)),
+ * R(a) the rotation by |a| about a / |a|. The matrices feed
+ * cg_deform_view.joint_matrices, as the skin's joint nodes' world matrices
+ * do in the engine (shaders/dynamicMeshShader_glsl.comp:41-44, 78-83). */
+typedef struct cg_skeleton_view {
+    uint32_t n_bones;       /* 1 .. CG_MAX_JOINTS */
+    const int32_t* parent;  /* host [n_bones]: parent(j) < j, or -1 */
+    const float* offsets;   /* host [n_bones][3]: translation from the parent */
+} cg_skeleton_view;
+#define CG_MAX_JOINTS 2048u
+
+/* d_axis_angles [n_poses][n_bones][3] -> d_joint_matrices
+ * [n_poses][n_bones][16] (column-major), device memory, on `stream`. */
+int cg_pose(cg_ctx* ctx, const cg_skeleton_view* skeleton, const float* d_axis_angles, uint32_t n_poses,
+            float* d_joint_matrices, void* stream);
+/* Adjoint of cg_pose: d_grad_joint_matrices (dE/dG, same layout as the
+ * matrices) -> d_grad_axis_angles (dE/da, overwritten). d_joint_matrices is
+ * cg_pose's output for the same angles. */
+int cg_pose_backward(cg_ctx* ctx, const cg_skeleton_view* skeleton, const float* d_axis_angles,
+                     const float* d_joint_matrices, const float* d_grad_joint_matrices, uint32_t n_poses,
+                     float* d_grad_axis_angles, void* stream);
+
+/* Penetration energy of the colliding triangle pairs of the context's last
+ * collide step (cg_collide, cg_collide_async or cg_graph_launch, with the
+ * pairs stored: no CG_NO_TRI_PAIRS / CG_MID_ONLY), into *d_energy (device):
+ *   E = sum over pairs, both directions of the vertex-vs-plane test of
+ *       src/CollisionDetection/CreateUncollideRays.cpp:102-112, of min(0, s)^2,
+ *       s = n . (p - p0): the depth of the vertex p below the other triangle's
+ *       plane (unit face normal n through its first vertex p0, Plane.cpp:14-20),
+ * in the first tree's space. FP32 terms, FP64 sum. Pairs beyond max_tri_pairs
+ * (reported by the collide's stats) are not in the sum. Enqueue it on the
+ * collide's stream. */
+int cg_energy(cg_ctx* ctx, double* d_energy, void* stream);
+
+/* One side (first or second tree) of every query of that collide step, for
+ * the adjoint. views[q] describes how tree q's vertices were made (the
+ * cg_deform view its refit positions came from, read again now: deformed
+ * vertices are recomputed, not kept); a view with n_vertices = 0, or
+ * views = NULL, marks a static side. Gradients are written (overwritten) to
+ *   grad_joint_matrices [n_queries][joint_stride][16] dE/d joint_matrices
+ *                       (column-major; row 3 is zero),
+ *   grad_morph_weights  [n_queries][target_stride]   dE/d morph_weights,
+ * device memory. n_targets <= 256 per view. */
+typedef struct cg_energy_side {
+    const cg_deform_view* views;
+    uint32_t joint_stride;
+    uint32_t target_stride;
+    float* grad_joint_matrices;
+    float* grad_morph_weights;
+} cg_energy_side;
+
+/* Adjoint of cg_energy for the same collide step: *d_grad_energy (device,
+ * dL/dE) -> dL/d joint_matrices and dL/d morph_weights of both sides (either
+ * may be NULL: static). Joint matrices and morph weights must still hold the
+ * forward's values. */
+int cg_energy_backward(cg_ctx* ctx, const double* d_grad_energy, const cg_energy_side* side_a,
+                       const cg_energy_side* side_b, void* stream);
+
 /* ---- No-allocation collide step (no reference counterpart) ----
  *
  * The collide step of cg_collide_async (same kernels, same colliding pairs)

@@ -30,7 +30,7 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_read_rays", "cg_read_ray_averages",
            "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch",
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
-           "cg_tree_download"]
+           "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -65,6 +65,15 @@ class cg_deform_view(C.Structure):
                 ("n_joints", C.c_uint32), ("vertices", C.c_void_p), ("morph_weights", C.c_void_p),
                 ("joints", C.c_void_p), ("weights", C.c_void_p), ("joint_matrices", C.c_void_p),
                 ("inverse_bind", C.c_void_p)]
+
+
+class cg_skeleton_view(C.Structure):
+    _fields_ = [("n_bones", C.c_uint32), ("parent", C.c_void_p), ("offsets", C.c_void_p)]
+
+
+class cg_energy_side(C.Structure):
+    _fields_ = [("views", C.c_void_p), ("joint_stride", C.c_uint32), ("target_stride", C.c_uint32),
+                ("grad_joint_matrices", C.c_void_p), ("grad_morph_weights", C.c_void_p)]
 
 
 class cg_static_counts(C.Structure):
@@ -137,6 +146,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_deform_batch.argtypes = [vp, vp, vp, u32, vp]
     lib.cg_tree_refit_batch.argtypes = [vp, vp, vp, vp, u32, vp]
     lib.cg_tree_download.argtypes = [vp, u32, vp, vp, u32, vp, u32]
+    lib.cg_pose.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, u32, vp, vp]
+    lib.cg_pose_backward.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, vp, vp, u32, vp, vp]
+    lib.cg_energy.argtypes = [vp, vp, vp]
+    lib.cg_energy_backward.argtypes = [vp, vp, C.POINTER(cg_energy_side), C.POINTER(cg_energy_side), vp]
     _lib = lib
     return lib
 
@@ -361,6 +374,28 @@ class Context:
         self._check(rc, "cg_tree_download")
         return root, obbs[:node_count], tri[:triangle_count]
 
+    def pose(self, skeleton: "Skeleton", axis_angles: int, n_poses: int, joint_matrices: int,
+             stream: int | None = None):
+        """cg_pose on device pointers ([n_poses][n_bones][3] -> [n_poses][n_bones][16])."""
+        self._check(self.lib.cg_pose(self.h, C.byref(skeleton.view), axis_angles, n_poses, joint_matrices, stream),
+                    "cg_pose")
+
+    def pose_backward(self, skeleton: "Skeleton", axis_angles: int, joint_matrices: int, grad_joint_matrices: int,
+                      n_poses: int, grad_axis_angles: int, stream: int | None = None):
+        self._check(self.lib.cg_pose_backward(self.h, C.byref(skeleton.view), axis_angles, joint_matrices,
+                                              grad_joint_matrices, n_poses, grad_axis_angles, stream),
+                    "cg_pose_backward")
+
+    def energy(self, d_energy: int, stream: int | None = None):
+        """cg_energy into a device double."""
+        self._check(self.lib.cg_energy(self.h, d_energy, stream), "cg_energy")
+
+    def energy_backward(self, d_grad_energy: int, side_a: "EnergySide | None", side_b: "EnergySide | None" = None,
+                        stream: int | None = None):
+        a = C.byref(side_a.side) if side_a is not None else None
+        b = C.byref(side_b.side) if side_b is not None else None
+        self._check(self.lib.cg_energy_backward(self.h, d_grad_energy, a, b, stream), "cg_energy_backward")
+
     def device_results(self) -> tuple[int, int]:
         p, n = C.c_void_p(), C.c_void_p()
         self._check(self.lib.cg_device_results(self.h, C.byref(p), C.byref(n)), "cg_device_results")
@@ -390,3 +425,29 @@ class Context:
 
     def graph_launch(self, stream: int | None = None):
         self._check(self.lib.cg_graph_launch(self.h, stream), "cg_graph_launch")
+
+
+class Skeleton:
+    """cg_skeleton_view with its host arrays kept alive: parent[j] (< j or -1)
+    and offsets[j] (translation from the parent)."""
+
+    def __init__(self, parent, offsets):
+        self.parent = np.ascontiguousarray(parent, np.int32)
+        self.offsets = np.ascontiguousarray(offsets, np.float32).reshape(-1, 3)
+        assert len(self.parent) == len(self.offsets)
+        self.view = cg_skeleton_view(len(self.parent), self.parent.ctypes.data, self.offsets.ctypes.data)
+
+    @property
+    def n_bones(self) -> int:
+        return len(self.parent)
+
+
+class EnergySide:
+    """cg_energy_side with its view table kept alive (views: list of
+    cg_deform_view, one per query; None entries are static)."""
+
+    def __init__(self, views, joint_stride: int, target_stride: int, grad_joint_matrices: int,
+                 grad_morph_weights: int | None):
+        self.views = (cg_deform_view * len(views))(*[v if v is not None else cg_deform_view() for v in views])
+        self.side = cg_energy_side(C.cast(self.views, C.c_void_p), joint_stride, target_stride, grad_joint_matrices,
+                                   grad_morph_weights)

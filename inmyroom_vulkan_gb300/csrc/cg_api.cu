@@ -103,6 +103,7 @@ struct cg_ctx {
     uint32_t blocks = 0;         // persistent traversal grid
     uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
     uint32_t accumulate_blocks = 0, emit_blocks = 0;  // contact kernels: one resident wave
+    uint32_t energy_blocks = 0;                        // energy kernels: one resident wave
 
     // trees
     struct Slot {
@@ -152,10 +153,12 @@ struct cg_ctx {
     Counters* h_ctr = nullptr;      // pinned
 
     uint32_t last_flags = 0;
+    uint32_t last_n = 0;            // queries of the last collide step enqueued
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_gen = 0;         // arena generations the graph was captured with
+    uint32_t graph_n = 0, graph_flags = 0;
     struct HostGraph {              // cg_collide's own graph of a whole step
         cudaGraphExec_t exec = nullptr;
         uint32_t n = 0, flags = 0;
@@ -171,9 +174,13 @@ struct cg_ctx {
         std::vector<char> host;
         void* dev = nullptr;
         size_t cap = 0;
-    } deform_table, refit_table;
+    } deform_table, refit_table, skeleton_table, energy_table;
     RefitScratch* refit_scratch = nullptr;  // one entry per record of a refit batch
     uint32_t refit_scratch_cap = 0;
+    float* pose_scratch = nullptr;          // pose adjoint: dE/dG accumulated per bone
+    uint64_t pose_scratch_cap = 0;
+    float* vgrad = nullptr;                 // energy adjoint: per-vertex gradient, zero between calls
+    uint64_t vgrad_cap = 0;
 
     std::string err;
 };
@@ -265,6 +272,75 @@ int stage_table(cg_ctx* c, cg_ctx::Table& t, const void* data, size_t bytes, cud
     return CG_OK;
 }
 
+bool aligned_to(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+// A cg_deform_view checked and turned into the kernels' form; `out` is
+// required when want_out is set.
+int deform_params(cg_ctx* c, const cg_deform_view* v, float* out, bool want_out, uint32_t i, DeformParams* p) {
+    if (v->n_vertices && (!v->vertices || (want_out && !out) || (v->n_targets && !v->morph_weights) ||
+                          (v->n_groups && (!v->joints || !v->weights || !v->joint_matrices || !v->inverse_bind))))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "deform view %u has null arrays", i);
+    if (!aligned_to(v->vertices, 16) || !aligned_to(out, 16) ||
+        (v->n_groups && (!aligned_to(v->weights, 16) || !aligned_to(v->joints, 8))))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "deform view %u: arrays must be 16-byte (joints 8-byte) aligned", i);
+    if (v->n_joints > kMaxJoints) return fail(c, CG_ERR_INVALID_ARGUMENT, "n_joints %u > %u", v->n_joints, kMaxJoints);
+    p->n_vertices = v->n_vertices;
+    p->n_targets = v->n_targets;
+    p->n_groups = v->n_groups;
+    p->n_joints = v->n_groups ? v->n_joints : 0u;
+    p->vertices = v->vertices;
+    p->morph_weights = v->morph_weights;
+    p->joints = v->joints;
+    p->weights = v->weights;
+    p->joint_matrices = v->joint_matrices;
+    p->inverse_bind = v->inverse_bind;
+    p->out = out;
+    return CG_OK;
+}
+
+// The skeleton of cg_pose / cg_pose_backward checked and staged in device
+// memory: parents (int32), then offsets (3 floats) from a 16-byte boundary.
+int pose_params(cg_ctx* c, const cg_skeleton_view* sk, uint32_t n_poses, cudaStream_t s, PoseParams* p) {
+    const uint32_t nb = sk->n_bones;
+    if (nb == 0 || nb > kMaxJoints || !sk->parent || !sk->offsets)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "skeleton: n_bones %u (1..%u) and both arrays are required", nb,
+                    kMaxJoints);
+    for (uint32_t j = 0; j < nb; ++j)
+        if (sk->parent[j] < -1 || sk->parent[j] >= int32_t(j))
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "skeleton: parent of bone %u is %d (must be -1 or < %u)", j,
+                        sk->parent[j], j);
+    const size_t off = (sizeof(int32_t) * nb + 15u) & ~size_t(15);
+    std::vector<char> blob(off + sizeof(float) * 3u * nb, 0);
+    std::memcpy(blob.data(), sk->parent, sizeof(int32_t) * nb);
+    std::memcpy(blob.data() + off, sk->offsets, sizeof(float) * 3u * nb);
+    const void* d = nullptr;
+    const int rc = stage_table(c, c->skeleton_table, blob.data(), blob.size(), s, &d);
+    if (rc != CG_OK) return rc;
+    p->n_poses = n_poses;
+    p->n_bones = nb;
+    p->parent = static_cast<const int32_t*>(d);
+    p->offsets = reinterpret_cast<const float*>(static_cast<const char*>(d) + off);
+    return CG_OK;
+}
+
+// The last collide step stored its colliding pairs.
+int energy_ready(cg_ctx* c) {
+    if (!c->cfg.max_tri_pairs || (c->last_flags & (CG_NO_TRI_PAIRS | CG_MID_ONLY)))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "the energy needs the colliding pairs of the last collide step");
+    return CG_OK;
+}
+
+EnergyParams energy_params(cg_ctx* c) {
+    EnergyParams p{};
+    p.q = c->d_packed;
+    p.n_queries = c->last_n;
+    p.tris = c->tris.ptr;
+    p.pairs = c->d_pairs;
+    p.ctr = c->d_ctr;
+    p.pairs_cap = c->cfg.max_tri_pairs;
+    return p;
+}
+
 void drop_graph(cg_ctx* c) {
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->graph) cudaGraphDestroy(c->graph);
@@ -312,6 +388,9 @@ int alloc_buffers(cg_ctx* c) {
     c->accumulate_blocks = uint32_t(std::max(aocc, 1) * c->sm_count);
     c->emit_blocks = uint32_t(std::max(eocc, 1) * c->sm_count);
     CG_CUDA(deform_smem_limit(), "deform kernel shared memory");
+    int gocc = 0;
+    CG_CUDA(energy_occupancy(&gocc), "occupancy");
+    c->energy_blocks = uint32_t(std::max(gocc, 1) * c->sm_count);
 
     CG_CUDA(cudaMalloc(&c->d_queries, sizeof(cg_query) * g.max_queries), "alloc queries");
     CG_CUDA(cudaMalloc(&c->d_packed, sizeof(PackedQuery) * g.max_queries), "alloc packed queries");
@@ -386,6 +465,7 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
 
 // Enqueues counter reset, packing, the traversal and the narrow phase on `s`.
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s) {
+    c->last_n = n;
     unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
     const uint32_t trace_ns = c->trace_ns ? c->trace_ns : 1000u;
     CG_CUDA(launch_init(c->d_ctr, c->d_ready, c->slot_alloc, n, trace, s), "init kernel");
@@ -662,6 +742,10 @@ int cg_destroy(cg_ctx* c) {
     cudaFree(c->deform_table.dev);
     cudaFree(c->refit_table.dev);
     cudaFree(c->refit_scratch);
+    cudaFree(c->skeleton_table.dev);
+    cudaFree(c->energy_table.dev);
+    cudaFree(c->pose_scratch);
+    cudaFree(c->vgrad);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
@@ -844,6 +928,7 @@ int cg_collide_async(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t 
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     c->last_flags = flags;
+    c->last_n = n;
     int rc = enqueue_step(c, d_queries, n, flags, s);
     if (rc != CG_OK) return rc;
     return join_stream(c, s);
@@ -871,6 +956,7 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
     cudaSetDevice(c->device);
     if (n) std::memcpy(c->h_queries, queries, sizeof(cg_query) * n);
     c->last_flags = flags;
+    c->last_n = n;
     // The whole step (query upload from the pinned staging buffer, kernels,
     // counter read-back) is one CUDA graph, captured once per (n, flags) and
     // tree-storage generation and replayed.
@@ -1093,33 +1179,13 @@ int cg_tree_refit(cg_ctx* c, uint32_t id, const float* positions, uint32_t n_pos
 
 int cg_deform_batch(cg_ctx* c, const cg_deform_view* views, float* const* outs, uint32_t n, void* stream) {
     if (!c || (n && (!views || !outs))) return CG_ERR_INVALID_ARGUMENT;
-    auto aligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; };
     std::vector<DeformParams> table(n);
     uint32_t max_vertices = 0, max_joints = 0;
     for (uint32_t i = 0; i < n; ++i) {
-        const cg_deform_view* v = views + i;
-        float* out = outs[i];
-        if (v->n_vertices && (!v->vertices || !out || (v->n_targets && !v->morph_weights) ||
-                              (v->n_groups && (!v->joints || !v->weights || !v->joint_matrices || !v->inverse_bind))))
-            return fail(c, CG_ERR_INVALID_ARGUMENT, "deform view %u has null arrays", i);
-        if (!aligned(v->vertices, 16) || !aligned(out, 16) ||
-            (v->n_groups && (!aligned(v->weights, 16) || !aligned(v->joints, 8))))
-            return fail(c, CG_ERR_INVALID_ARGUMENT, "deform view %u: arrays must be 16-byte (joints 8-byte) aligned", i);
-        if (v->n_joints > kMaxJoints) return fail(c, CG_ERR_INVALID_ARGUMENT, "n_joints %u > %u", v->n_joints, kMaxJoints);
-        DeformParams& p = table[i];
-        p.n_vertices = v->n_vertices;
-        p.n_targets = v->n_targets;
-        p.n_groups = v->n_groups;
-        p.n_joints = v->n_groups ? v->n_joints : 0u;
-        p.vertices = v->vertices;
-        p.morph_weights = v->morph_weights;
-        p.joints = v->joints;
-        p.weights = v->weights;
-        p.joint_matrices = v->joint_matrices;
-        p.inverse_bind = v->inverse_bind;
-        p.out = out;
-        max_vertices = std::max(max_vertices, p.n_vertices);
-        max_joints = std::max(max_joints, p.n_joints);
+        const int rc = deform_params(c, views + i, outs[i], true, i, &table[i]);
+        if (rc != CG_OK) return rc;
+        max_vertices = std::max(max_vertices, table[i].n_vertices);
+        max_joints = std::max(max_joints, table[i].n_joints);
     }
     if (n == 0 || max_vertices == 0) return CG_OK;
     cudaSetDevice(c->device);
@@ -1133,6 +1199,138 @@ int cg_deform_batch(cg_ctx* c, const cg_deform_view* views, float* const* outs, 
 
 int cg_deform(cg_ctx* c, const cg_deform_view* v, float* out, void* stream) {
     return cg_deform_batch(c, v, &out, 1, stream);
+}
+
+int cg_pose(cg_ctx* c, const cg_skeleton_view* sk, const float* d_axis_angles, uint32_t n_poses,
+            float* d_joint_matrices, void* stream) {
+    if (!c || !sk || (n_poses && (!d_axis_angles || !d_joint_matrices))) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    PoseParams p{};
+    int rc = pose_params(c, sk, n_poses, s, &p);
+    if (rc != CG_OK) return rc;
+    p.axis_angles = d_axis_angles;
+    p.joint_matrices = d_joint_matrices;
+    CG_CUDA(launch_pose(p, s), "pose kernel");
+    return CG_OK;
+}
+
+int cg_pose_backward(cg_ctx* c, const cg_skeleton_view* sk, const float* d_axis_angles, const float* d_joint_matrices,
+                     const float* d_grad_joint_matrices, uint32_t n_poses, float* d_grad_axis_angles, void* stream) {
+    if (!c || !sk || (n_poses && (!d_axis_angles || !d_joint_matrices || !d_grad_joint_matrices || !d_grad_axis_angles)))
+        return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    PoseParams p{};
+    int rc = pose_params(c, sk, n_poses, s, &p);
+    if (rc != CG_OK) return rc;
+    const uint64_t need = uint64_t(n_poses) * p.n_bones * 16u;
+    if (need > c->pose_scratch_cap) {
+        CG_CUDA(cudaStreamSynchronize(s), "pose scratch");
+        cudaFree(c->pose_scratch);
+        c->pose_scratch = nullptr;
+        c->pose_scratch_cap = 0;
+        CG_CUDA(cudaMalloc(&c->pose_scratch, sizeof(float) * need), "alloc pose scratch");
+        c->pose_scratch_cap = need;
+    }
+    p.axis_angles = d_axis_angles;
+    p.joint_matrices = const_cast<float*>(d_joint_matrices);  // read only in the adjoint
+    p.grad_joint = d_grad_joint_matrices;
+    p.grad_acc = c->pose_scratch;
+    p.grad_axis_angles = d_grad_axis_angles;
+    CG_CUDA(launch_pose_backward(p, s), "pose adjoint kernel");
+    return CG_OK;
+}
+
+int cg_energy(cg_ctx* c, double* d_energy, void* stream) {
+    if (!c || !d_energy) return CG_ERR_INVALID_ARGUMENT;
+    int rc = energy_ready(c);
+    if (rc != CG_OK) return rc;
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    EnergyParams p = energy_params(c);
+    p.energy = d_energy;
+    CG_CUDA(cudaMemsetAsync(d_energy, 0, sizeof(double), s), "clear energy");
+    CG_CUDA(launch_energy(p, c->energy_blocks, s), "energy kernel");
+    return CG_OK;
+}
+
+int cg_energy_backward(cg_ctx* c, const double* d_grad_energy, const cg_energy_side* side_a,
+                       const cg_energy_side* side_b, void* stream) {
+    if (!c || !d_grad_energy) return CG_ERR_INVALID_ARGUMENT;
+    int rc = energy_ready(c);
+    if (rc != CG_OK) return rc;
+    const uint32_t n = c->last_n;
+    std::vector<EnergySide> sides(2ull * n);
+    std::vector<uint32_t> deforming;
+    uint64_t total = 0;
+    uint32_t max_vertices = 0, max_joints = 0, max_targets = 0;
+    const cg_energy_side* both[2] = {side_a, side_b};
+    for (uint32_t k = 0; k < 2; ++k) {
+        const cg_energy_side* sd = both[k];
+        if (!sd || !sd->views) continue;
+        for (uint32_t q = 0; q < n; ++q) {
+            const cg_deform_view* v = sd->views + q;
+            if (!v->n_vertices) continue;
+            if (!sd->grad_joint_matrices || (sd->target_stride && !sd->grad_morph_weights))
+                return fail(c, CG_ERR_INVALID_ARGUMENT, "energy side %u: null gradient arrays", k);
+            EnergySide& e = sides[size_t(k) * n + q];
+            rc = deform_params(c, v, nullptr, false, q, &e.d);
+            if (rc != CG_OK) return rc;
+            if (e.d.n_joints > sd->joint_stride || v->n_targets > sd->target_stride || v->n_targets > 256u)
+                return fail(c, CG_ERR_INVALID_ARGUMENT,
+                            "energy side %u view %u: %u joints / %u targets over the strides %u / %u (targets <= 256)",
+                            k, q, e.d.n_joints, v->n_targets, sd->joint_stride, sd->target_stride);
+            if (total + v->n_vertices > 0xffffffffull)
+                return fail(c, CG_ERR_INVALID_ARGUMENT, "more than 2^32 deforming vertices");
+            e.grad_base = uint32_t(total);
+            total += v->n_vertices;
+            e.grad_joint = sd->grad_joint_matrices + size_t(q) * sd->joint_stride * 16u;
+            e.grad_morph = sd->grad_morph_weights ? sd->grad_morph_weights + size_t(q) * sd->target_stride : nullptr;
+            deforming.push_back(k * n + q);
+            max_vertices = std::max(max_vertices, e.d.n_vertices);
+            max_joints = std::max(max_joints, e.d.n_joints);
+            max_targets = std::max(max_targets, e.d.n_targets);
+        }
+    }
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    for (uint32_t k = 0; k < 2; ++k) {
+        const cg_energy_side* sd = both[k];
+        if (!sd || !sd->views || !n) continue;
+        if (sd->grad_joint_matrices && sd->joint_stride)
+            CG_CUDA(cudaMemsetAsync(sd->grad_joint_matrices, 0, sizeof(float) * 16u * sd->joint_stride * n, s),
+                    "clear joint gradients");
+        if (sd->grad_morph_weights && sd->target_stride)
+            CG_CUDA(cudaMemsetAsync(sd->grad_morph_weights, 0, sizeof(float) * sd->target_stride * n, s),
+                    "clear morph-weight gradients");
+    }
+    if (deforming.empty()) return CG_OK;
+    if (3u * total > c->vgrad_cap) {
+        CG_CUDA(cudaStreamSynchronize(s), "vertex gradient buffer");
+        cudaFree(c->vgrad);
+        c->vgrad = nullptr;
+        c->vgrad_cap = 0;
+        CG_CUDA(cudaMalloc(&c->vgrad, sizeof(float) * 3u * total), "alloc vertex gradients");
+        CG_CUDA(cudaMemset(c->vgrad, 0, sizeof(float) * 3u * total), "zero vertex gradients");
+        c->vgrad_cap = 3u * total;
+    }
+    std::vector<char> blob(sizeof(EnergySide) * sides.size() + sizeof(uint32_t) * deforming.size());
+    std::memcpy(blob.data(), sides.data(), sizeof(EnergySide) * sides.size());
+    std::memcpy(blob.data() + sizeof(EnergySide) * sides.size(), deforming.data(), sizeof(uint32_t) * deforming.size());
+    const void* d_blob = nullptr;
+    rc = stage_table(c, c->energy_table, blob.data(), blob.size(), s, &d_blob);
+    if (rc != CG_OK) return rc;
+    EnergyParams p = energy_params(c);
+    p.grad_energy = d_grad_energy;
+    p.sides = static_cast<const EnergySide*>(d_blob);
+    p.deforming = reinterpret_cast<const uint32_t*>(static_cast<const char*>(d_blob) + sizeof(EnergySide) * sides.size());
+    p.n_deforming = uint32_t(deforming.size());
+    p.vgrad = c->vgrad;
+    p.max_joints = max_joints;
+    p.max_targets = max_targets;
+    CG_CUDA(launch_energy_backward(p, c->energy_blocks, max_vertices, s), "energy adjoint kernels");
+    return CG_OK;
 }
 
 int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags) {
@@ -1158,7 +1356,10 @@ int cg_graph_capture(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t 
     c->graph = g;
     CG_CUDA(cudaGraphInstantiate(&c->graph_exec, g, 0), "instantiate graph");
     c->graph_gen = arena_gen(c);
+    c->graph_n = n;
+    c->graph_flags = flags;
     c->last_flags = flags;
+    c->last_n = n;
     return CG_OK;
 }
 
@@ -1169,6 +1370,8 @@ int cg_graph_launch(cg_ctx* c, void* stream) {
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     CG_CUDA(cudaGraphLaunch(c->graph_exec, s), "graph launch");
+    c->last_flags = c->graph_flags;
+    c->last_n = c->graph_n;
     return join_stream(c, s);
 }
 

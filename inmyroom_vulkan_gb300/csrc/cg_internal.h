@@ -221,6 +221,51 @@ struct RefitScratch {
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
                          uint32_t max_recs, RefitScratch* scratch, cudaStream_t s);
 
+// Axis-angle posing of a skeleton and its adjoint (cg_energy.cu): bone j's
+// world matrix is G_parent(j) * T(offset_j) * R(axis_angle_j).
+struct PoseParams {
+    uint32_t n_poses, n_bones;
+    const int32_t* parent;          // [n_bones], < j or -1
+    const float* offsets;           // [n_bones][3]
+    const float* axis_angles;       // [n_poses][n_bones][3]
+    float* joint_matrices;          // forward out / backward in: [n_poses][n_bones][16]
+    const float* grad_joint;        // backward in: [n_poses][n_bones][16]
+    float* grad_acc;                // backward scratch: [n_poses][n_bones][16]
+    float* grad_axis_angles;        // backward out: [n_poses][n_bones][3]
+};
+cudaError_t launch_pose(const PoseParams& p, cudaStream_t s);
+cudaError_t launch_pose_backward(const PoseParams& p, cudaStream_t s);
+
+// Penetration energy over the colliding pairs of the last collide and its
+// adjoint (cg_energy.cu). One side of a query deforms when its view has
+// vertices; then its vertices are recomputed from the view (cg_skin.cuh) and
+// its gradient lands in grad_joint / grad_morph.
+struct EnergySide {
+    DeformParams d;      // d.n_vertices == 0: the side is static
+    uint32_t grad_base;  // first vertex of this side in the vertex-gradient buffer
+    uint32_t pad;
+    float* grad_joint;   // [joint_stride][16], rows 0-2 written
+    float* grad_morph;   // [n_targets]
+};
+struct EnergyParams {
+    const PackedQuery* q;
+    uint32_t n_queries;
+    uint32_t n_deforming;         // entries of `deforming`
+    const float4* tris;           // triangle arena
+    const cg_tri_pair* pairs;
+    const Counters* ctr;          // n_pairs of the collide
+    unsigned long long pairs_cap;
+    double* energy;               // forward out
+    const double* grad_energy;    // backward in (dL/dE)
+    const EnergySide* sides;      // [2 * n_queries]: side A of every query, then side B
+    const uint32_t* deforming;    // indices into sides of the deforming ones
+    float* vgrad;                 // [sum of deforming sides' n_vertices][3], zero between calls
+    uint32_t max_joints, max_targets;
+};
+cudaError_t launch_energy(const EnergyParams& p, uint32_t blocks, cudaStream_t s);
+cudaError_t launch_energy_backward(const EnergyParams& p, uint32_t blocks, uint32_t max_vertices, cudaStream_t s);
+cudaError_t energy_occupancy(int* blocks_per_sm);
+
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,
                         PackedQuery* out, Counters* ctr, uint4* leaf_list, uint32_t leaf_cap, cudaStream_t s);

@@ -381,3 +381,14 @@ def deforming(n_meshes: int = 64, seed: int = SEED_BASE + 3, rings: int = 100, a
         models.append(pose(R, [gx, h[gi, gj] + 0.05, gz]))
     return DeformingScene(mesh, verts, morph_w, joints, weights, aa, jm, inverse_bind, np.stack(models), field,
                           bone_len)
+
+
+def chain_skeleton(sc: DeformingScene) -> tuple[np.ndarray, np.ndarray]:
+    """(parent, offsets) of the tubes' bone chain in the axis-angle posing
+    form G_j = G_parent(j) * T(offset_j) * R(a_j): bone 0 at the origin, bone j
+    one bone length up +y from bone j - 1 (chain_matrices)."""
+    B = sc.axis_angles.shape[1]
+    parent = np.arange(-1, B - 1, dtype=np.int32)
+    offsets = np.zeros((B, 3), np.float32)
+    offsets[1:, 1] = sc.bone_len
+    return parent, offsets
