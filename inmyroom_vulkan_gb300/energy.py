@@ -17,6 +17,15 @@ import torch
 
 from . import capi
 
+# cudaStreamLegacy: torch reports its legacy default stream as handle 0, which
+# the C ABI reads as "the context's own stream"; this handle names the legacy
+# default stream itself, so the kernels stay ordered with torch's work on it.
+CUDA_STREAM_LEGACY = 1
+
+
+def current_stream() -> int:
+    return torch.cuda.current_stream().cuda_stream or CUDA_STREAM_LEGACY
+
 
 class DeformingCollider:
     """n meshes of one rest topology (one OBB tree each, refitted every
@@ -71,7 +80,7 @@ class DeformingCollider:
     # -- the two passes, on device buffers --
 
     def forward_pass(self, axis_angles: torch.Tensor, morph_weights: torch.Tensor) -> torch.Tensor:
-        s = torch.cuda.current_stream().cuda_stream
+        s = current_stream()
         self.axis_angles.copy_(axis_angles.detach().reshape(self.n, self.B, 3))
         if self.T:
             self.morph_weights.copy_(morph_weights.detach().reshape(self.n, self.T))
@@ -85,7 +94,7 @@ class DeformingCollider:
         return self.energy_out
 
     def backward_pass(self, grad_energy: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
-        s = torch.cuda.current_stream().cuda_stream
+        s = current_stream()
         g = grad_energy.detach().to(device=self.energy_out.device, dtype=torch.float64).reshape(()).contiguous()
         c = self.ctx
         c.energy_backward(g.data_ptr(), self.side, None, s)

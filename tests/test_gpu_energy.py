@@ -15,7 +15,7 @@ import pytest
 import torch
 
 from inmyroom_vulkan_gb300 import capi, scenes
-from inmyroom_vulkan_gb300.energy import DeformingCollider, penetration_energy
+from inmyroom_vulkan_gb300.energy import DeformingCollider, current_stream, penetration_energy
 from oracle import energy as oe
 
 pytestmark = pytest.mark.gpu
@@ -58,7 +58,7 @@ def test_pose_matches_fp64(gpu_ctx):
     aa[0, :5] = 0.0  # the series branch
     aa[1, :5] *= 1e-3
     jm = torch.zeros(8, aa.shape[1], 16, device="cuda")
-    gpu_ctx.pose(skel, aa.data_ptr(), 8, jm.data_ptr())
+    gpu_ctx.pose(skel, aa.data_ptr(), 8, jm.data_ptr(), current_stream())
     want = oe.col_major(oe.pose(aa.cpu().double(), parent, offsets.astype(np.float64))).numpy()
     np.testing.assert_allclose(jm.cpu().numpy(), want, rtol=0, atol=5e-6)
 
