@@ -188,6 +188,94 @@ def run_reference(args) -> dict:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_sweep(args, local: int, flush, stream, cpu_seconds: float) -> dict:
+    """Autotuned batch sweep: 10,000 uneven rigid mesh-pair queries (a pool of
+    48 meshes of 256..65,536 triangles, log-uniform; random SO(3) poses with
+    root-box overlap probability about 0.5) resolved in one launch. Timed with
+    the context's starting settings, then tuned (autotune.tune_collide) and
+    timed again as a captured CUDA graph; beside it the plain path (one query
+    per launch) over the first 1,000 queries and the CPU restatement on the
+    host cores. L2 flushed before every timed launch."""
+    import torch
+
+    import oracle
+    from inmyroom_vulkan_gb300 import autotune, capi, scenes
+
+    bs = scenes.batch_sweep()
+    port = oracle.port(fast=True)
+    trees = [port.tree_build(m.points, m.indices, m.normals) for m in bs.meshes]
+    ctx = capi.Context(device=local, max_queries=16384, max_tri_pairs=1 << 23, max_leaf_pairs=1 << 24)
+    ids = np.array([ctx.upload_flat(t.export()) for t in trees], np.uint32)
+    rel = np.stack([capi.relative_matrix(a, b) for a, b in zip(bs.mats_a, bs.mats_b)])
+    q = capi.make_queries(ids[bs.qa], ids[bs.qb], rel)
+    n = len(q)
+    d_q = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    flags = 0
+    sp = stream.cuda_stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(launch, reps):
+        ms = []
+        for k in range(reps):
+            flush.fill_(k & 0xff)
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    batched = lambda: ctx.collide_async(d_q.data_ptr(), n, flags, sp)  # noqa: E731
+    for _ in range(max(args.warmup, 3)):
+        batched()
+    st = ctx.sync_stats()
+    start_ms = timed(batched, max(args.steps, 5))
+    tune = autotune.tune_collide(ctx, d_q.data_ptr(), n, flags, flush=flush)
+    ctx.graph_capture(d_q.data_ptr(), n, flags)
+    graph = lambda: ctx.graph_launch(sp)  # noqa: E731
+    for _ in range(max(args.warmup, 3)):
+        graph()
+    tuned_ms = timed(graph, max(args.steps, 5))
+    st2 = ctx.sync_stats()
+    assert st2["status"] == 0 and st2["tri_tests"] == st["tri_tests"] and st2["tri_pairs"] == st["tri_pairs"]
+    tests, node_pairs = st["tri_tests"], st["node_pairs"]
+    # plain path: one query per launch
+    P = min(1000, n)
+    qsz = capi.QUERY_DTYPE.itemsize
+    plain = lambda: [ctx.collide_async(d_q.data_ptr() + i * qsz, 1, flags, sp) for i in range(P)]  # noqa: E731
+    plain()
+    plain_ms = timed(plain, 3)
+    ctx.collide(q[:P], flags=flags)
+    ptests = ctx.sync_stats()["tri_tests"]
+    res = {"workload": f"{n} rigid mesh-pair queries over a pool of {len(bs.meshes)} meshes "
+                       f"({min(m.n_tris for m in bs.meshes)}..{max(m.n_tris for m in bs.meshes)} triangles, "
+                       "log-uniform), root-box overlap ~0.5, one launch (colliding pairs out)",
+           "tri_tests_per_launch": int(tests), "tri_pairs_per_launch": int(st["tri_pairs"]),
+           "leaf_pairs_per_launch": int(st["leaf_pairs"]), "node_pairs_per_launch": int(node_pairs),
+           "start_ms": start_ms, "tuned_ms": tuned_ms, "tri_tests_per_s": tests / (tuned_ms / 1e3),
+           "queries_per_s": n / (tuned_ms / 1e3),
+           "operand_gbs": (node_pairs * NODE_PAIR_BYTES + tests * TRI_TEST_BYTES) / (tuned_ms / 1e3) / 1e9,
+           "autotune": tune.as_dict(),
+           "plain": {"queries": P, "ms_per_query": plain_ms / P, "queries_per_s": P / (plain_ms / 1e3),
+                     "tri_tests_per_s": ptests / (plain_ms / 1e3)},
+           "cache": "L2 flushed (512 MB write) before every timed launch", "launch": "CUDA graph after tuning"}
+    ctx.close()
+    if cpu_seconds > 0:
+        cores = os.cpu_count() or 1
+        ta = [trees[i] for i in bs.qa[:P]]
+        tb = [trees[i] for i in bs.qb[:P]]
+        runs, ctests, t0 = 0, 0, time.perf_counter()
+        while True:
+            ctests += port.collide_batch(ta, tb, bs.mats_a[:P], bs.mats_b[:P], threads=cores)["tests"]
+            runs += 1
+            if time.perf_counter() - t0 >= cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"tri_tests_per_s": ctests / el, "cores": cores, "kind": "port",
+                               "sample": f"the first {P} queries x {runs}, {el:.1f} s, release flags"}
+    return res
+
+
 def run_differentiable(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
     """Differentiable workload on the deforming scene: forward = pose the 64
     skeletons from axis angles, morph + skin, refit, collide, penetration
@@ -501,6 +589,9 @@ def run_gpu(args) -> dict:
         differentiable = run_differentiable(
             args, lambda: capi.Context(device=local, max_queries=4096, max_tri_pairs=1 << 22), flush, stream,
             min(args.cpu_seconds, 5.0))
+    sweep = None
+    if rank == 0 and not args.skip_sweep:
+        sweep = run_sweep(args, local, flush, stream, min(args.cpu_seconds, 5.0))
     clk = clocks.summary()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -534,6 +625,8 @@ def run_gpu(args) -> dict:
         out["deforming"] = deforming
     if differentiable:
         out["differentiable"] = differentiable
+    if sweep:
+        out["batch_sweep"] = sweep
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -547,7 +640,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--skip-deforming", action="store_true", help="leave out the deforming-meshes line")
+    ap.add_argument("--skip-deforming", action="store_true", help="leave out the deforming and differentiable lines")
+    ap.add_argument("--skip-sweep", action="store_true", help="leave out the autotuned batch-sweep line")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
