@@ -13,9 +13,9 @@ queries per second beside it.
 
 value: device-resident inputs, each step timed with CUDA events on the
 launching stream, L2 flushed (a 512 MB write) between steps.
-e2e: the public host API (cg_collide with host queries + read-back of the
-colliding pairs, the rays and the per-query mean origins into pinned memory),
-host-timed around the synchronous calls.
+e2e: the public host API: one cg_collide call with host queries, whose step
+also writes the colliding pairs, the rays and the per-query mean origins into
+pinned host buffers (cg_set_host_outputs); host-timed around the call.
 roofline: the traversal kernel (the dominant one), algorithmic bytes (node
 pairs x 96 B of box data) per launch over its event-timed duration, against the
 measured copy bandwidth, with the FP32 view beside it; roofline_narrow: the
@@ -475,12 +475,17 @@ def run_gpu(args) -> dict:
     d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
     torch.cuda.synchronize()
     flags = capi.CG_CONTACTS
-    ctx.graph_capture(d_q.data_ptr(), n, flags)
     # a dedicated stream: its handle is never 0, which the C ABI reads as
     # "the context's own stream"
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    tune = None
+    if not args.no_tune:
+        from inmyroom_vulkan_gb300 import autotune
+
+        tune = autotune.tune_collide(ctx, d_q.data_ptr(), n, flags, flush=flush).as_dict()
+    ctx.graph_capture(d_q.data_ptr(), n, flags)
 
     st = None
     for _ in range(max(args.warmup, 3)):
@@ -508,13 +513,15 @@ def run_gpu(args) -> dict:
         assert st["tri_tests"] == tests_per_step and st["status"] == 0 and st["rays"] == rays_per_step
 
         # end to end through the public host API: host queries in; pairs, rays
-        # and mean origins out, into pinned host memory (one copy each)
+        # and mean origins out, into pinned host memory, in one cg_collide call
         def pinned(count, dtype):
             return torch.empty(count * dtype.itemsize, dtype=torch.uint8).pin_memory().numpy().view(dtype)
 
         out_pairs = pinned(pairs_per_step, capi.TRI_PAIR_DTYPE)
         out_rays = pinned(rays_per_step, capi.RAY_DTYPE)
         out_avg = pinned(n, capi.RAY_AVERAGE_DTYPE)
+        # the step graph itself writes the results into these buffers
+        ctx.set_host_outputs(out_pairs, out_rays, out_avg)
         ctx.collide(q, flags=flags)  # captures cg_collide's step graph outside the timed region
         e2e_times = []
         for k in range(args.steps):
@@ -522,11 +529,12 @@ def run_gpu(args) -> dict:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             st_e = ctx.collide(q, flags=flags)
-            pairs = ctx.tri_pairs(out=out_pairs, count=st_e["tri_pairs"])
-            rays = ctx.rays(out=out_rays, count=st_e["rays"])
-            avgs = ctx.ray_averages(out=out_avg, count=n)
+            pairs = out_pairs[:st_e["tri_pairs"]]
+            rays = out_rays[:st_e["rays"]]
+            avgs = out_avg[:n]
             e2e_times.append(time.perf_counter() - t0)
         assert len(pairs) == pairs_per_step and len(rays) == rays_per_step and len(avgs) == n
+        assert np.array_equal(pairs.view(np.uint8), ctx.tri_pairs().view(np.uint8))
     total_ms = float(np.sum(step_ms))
     if dist:
         t = torch.tensor([total_ms], device=dev)
@@ -604,13 +612,16 @@ def run_gpu(args) -> dict:
                    "node_pairs_per_step": int(st["node_pairs"]), "cache": "L2 flushed (512 MB write) between steps",
                    "launch": "CUDA graph: init + pack + persistent traversal + persistent narrow phase + "
                              "contact accumulate + contact/ray emit",
-                   "lanes_per_step": st["node_pairs"] / max(1, st["warp_steps"])},
+                   "lanes_per_step": st["node_pairs"] / max(1, st["warp_steps"]),
+                   "autotune": tune},
         "queries_per_s": world * n * args.steps / (total_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * capi.QUERY_DTYPE.itemsize),
-                "d2h_bytes_per_step": int(4 * COUNTERS_BYTES + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize
+                "d2h_bytes_per_step": int(COUNTERS_BYTES + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize
                                           + rays_per_step * capi.RAY_DTYPE.itemsize
                                           + n * capi.RAY_AVERAGE_DTYPE.itemsize),
-                "ms_per_step": 1e3 * e2e_s / args.steps, "timing": "host perf_counter around synchronous calls"},
+                "ms_per_step": 1e3 * e2e_s / args.steps,
+                "timing": "host perf_counter around one synchronous cg_collide (results written to pinned "
+                          "host buffers by the step)"},
         "roofline": roof_trav,
         "roofline_narrow": roof_narrow,
         "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch (with contacts and rays)",
@@ -642,6 +653,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-deforming", action="store_true", help="leave out the deforming and differentiable lines")
     ap.add_argument("--skip-sweep", action="store_true", help="leave out the autotuned batch-sweep line")
+    ap.add_argument("--no-tune", action="store_true", help="time the scene step with the default launch settings")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

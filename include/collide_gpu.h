@@ -220,6 +220,21 @@ int cg_read_contacts(cg_ctx* ctx, cg_contact* out, uint64_t cap, uint64_t* n);
 int cg_read_rays(cg_ctx* ctx, cg_ray* out, uint64_t cap, uint64_t* n);
 int cg_read_ray_averages(cg_ctx* ctx, cg_ray_average* out, uint64_t cap, uint64_t* n);
 
+/* Host destinations of cg_collide's results, so that one cg_collide call
+ * returns them (no read calls, one synchronisation): with these set, every
+ * cg_collide step also writes its colliding pairs (the first pairs_cap), and
+ * for CG_CONTACTS steps its uncollide rays (the first rays_cap) and per-query
+ * ray averages (the first averages_cap), straight into these buffers, as part
+ * of the step's own launch sequence. The counts are the step's cg_stats
+ * (tri_pairs, rays; averages: one per query). The buffers must be page-locked
+ * host memory the device can write (cudaHostAlloc, cudaHostRegister), rays
+ * and averages 16-byte aligned, and stay valid until replaced; a NULL pointer
+ * or zero capacity leaves that result on the device only. Results are still
+ * readable with the cg_read_* calls. Does not apply to cg_collide_async and
+ * cg_graph_launch. */
+int cg_set_host_outputs(cg_ctx* ctx, cg_tri_pair* pairs, uint64_t pairs_cap, cg_ray* rays, uint64_t rays_cap,
+                        cg_ray_average* averages, uint64_t averages_cap);
+
 /* Device times of the last step's two main kernels, the OBB-tree traversal
  * (emits candidate leaf pairs) and the narrow phase (triangle-pair tests),
  * from CUDA events recorded around their launches; each waits for its kernel. */

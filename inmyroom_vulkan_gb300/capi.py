@@ -30,7 +30,8 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_read_rays", "cg_read_ray_averages",
            "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch",
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
-           "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward"]
+           "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
+           "cg_set_host_outputs"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -146,6 +147,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_deform_batch.argtypes = [vp, vp, vp, u32, vp]
     lib.cg_tree_refit_batch.argtypes = [vp, vp, vp, vp, u32, vp]
     lib.cg_tree_download.argtypes = [vp, u32, vp, vp, u32, vp, u32]
+    lib.cg_set_host_outputs.argtypes = [vp, vp, u64, vp, u64, vp, u64]
     lib.cg_pose.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, u32, vp, vp]
     lib.cg_pose_backward.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, vp, vp, u32, vp, vp]
     lib.cg_energy.argtypes = [vp, vp, vp]
@@ -373,6 +375,22 @@ class Context:
                                        node_count, tri.ctypes.data if triangle_count else None, triangle_count)
         self._check(rc, "cg_tree_download")
         return root, obbs[:node_count], tri[:triangle_count]
+
+    def set_host_outputs(self, pairs: np.ndarray | None = None, rays: np.ndarray | None = None,
+                         averages: np.ndarray | None = None):
+        """cg_set_host_outputs on page-locked numpy arrays (e.g. from
+        torch.empty(..., pin_memory=True).numpy()) of TRI_PAIR_DTYPE,
+        RAY_DTYPE and RAY_AVERAGE_DTYPE; None turns a destination off. The
+        arrays must stay alive while set."""
+        def arg(a, dt):
+            if a is None:
+                return None, 0
+            assert a.dtype == dt and a.flags.c_contiguous
+            return a.ctypes.data, len(a)
+
+        p, r, v = arg(pairs, TRI_PAIR_DTYPE), arg(rays, RAY_DTYPE), arg(averages, RAY_AVERAGE_DTYPE)
+        self._check(self.lib.cg_set_host_outputs(self.h, p[0], p[1], r[0], r[1], v[0], v[1]), "cg_set_host_outputs")
+        self._host_outputs = (pairs, rays, averages)
 
     def pose(self, skeleton: "Skeleton", axis_angles: int, n_poses: int, joint_matrices: int,
              stream: int | None = None):

@@ -162,9 +162,21 @@ struct cg_ctx {
     struct HostGraph {              // cg_collide's own graph of a whole step
         cudaGraphExec_t exec = nullptr;
         uint32_t n = 0, flags = 0;
-        uint64_t gen = 0;
+        uint64_t gen = 0, out_gen = 0;
     } host_graph;
     bool capturing = false;
+    // cg_set_host_outputs: page-locked host destinations of cg_collide's
+    // results (device aliases), written by the step graph itself
+    struct HostOut {
+        cg_tri_pair* pairs = nullptr;
+        uint64_t pairs_cap = 0;
+        cg_ray* rays = nullptr;
+        uint64_t rays_cap = 0;
+        cg_ray_average* averages = nullptr;
+        uint64_t averages_cap = 0;
+        uint64_t gen = 0;  // settings changes (the step graph is captured again)
+    } host_out;
+    uint32_t copy_blocks = 0;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_t2 = nullptr;  // traversal start, end; narrow end
     cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
 
@@ -388,6 +400,7 @@ int alloc_buffers(cg_ctx* c) {
     c->accumulate_blocks = uint32_t(std::max(aocc, 1) * c->sm_count);
     c->emit_blocks = uint32_t(std::max(eocc, 1) * c->sm_count);
     CG_CUDA(deform_smem_limit(), "deform kernel shared memory");
+    c->copy_blocks = uint32_t(4 * c->sm_count);
     int gocc = 0;
     CG_CUDA(energy_occupancy(&gocc), "occupancy");
     c->energy_blocks = uint32_t(std::max(gocc, 1) * c->sm_count);
@@ -961,7 +974,8 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
     // counter read-back) is one CUDA graph, captured once per (n, flags) and
     // tree-storage generation and replayed.
     auto& G = c->host_graph;
-    if (!G.exec || G.n != n || G.flags != flags || G.gen != arena_gen(c)) {
+    if (!G.exec || G.n != n || G.flags != flags || G.gen != arena_gen(c) ||
+        G.out_gen != c->host_out.gen) {
         if (G.exec) cudaGraphExecDestroy(G.exec);
         G.exec = nullptr;
         CG_CUDA(cudaStreamSynchronize(c->stream), "sync before capture");
@@ -971,7 +985,24 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
         if (n)
             e = cudaMemcpyAsync(c->d_queries, c->h_queries, sizeof(cg_query) * n, cudaMemcpyHostToDevice, c->stream);
         int rc = e == cudaSuccess ? enqueue_step(c, c->d_queries, n, flags, c->stream) : CG_ERR_CUDA;
-        if (rc == CG_OK)
+        if (rc == CG_OK && (c->host_out.pairs || c->host_out.rays || c->host_out.averages)) {
+            CopyOutParams cp{};
+            cp.ctr = c->d_ctr;
+            cp.pairs = c->d_pairs;
+            cp.pairs_avail = c->d_pairs ? c->cfg.max_tri_pairs : 0;
+            cp.host_pairs = (flags & (CG_NO_TRI_PAIRS | CG_MID_ONLY)) ? nullptr : c->host_out.pairs;
+            cp.host_pairs_cap = c->host_out.pairs_cap;
+            const bool contacts = (flags & CG_CONTACTS) != 0;
+            cp.rays = c->ct.rays;
+            cp.rays_avail = c->ct.max_rays;
+            cp.host_rays = contacts ? c->host_out.rays : nullptr;
+            cp.host_rays_cap = c->host_out.rays_cap;
+            cp.averages = c->ct.averages;
+            cp.host_averages = contacts ? c->host_out.averages : nullptr;
+            cp.host_averages_cap = c->host_out.averages_cap;
+            e = launch_copy_out(cp, c->copy_blocks, c->stream);
+        }
+        if (rc == CG_OK && e == cudaSuccess)
             e = cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream);
         c->capturing = false;
         cudaGraph_t g = nullptr;
@@ -986,6 +1017,7 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
         G.n = n;
         G.flags = flags;
         G.gen = arena_gen(c);
+        G.out_gen = c->host_out.gen;
     }
     CG_CUDA(cudaGraphLaunch(G.exec, c->stream), "collide step");
     CG_CUDA(cudaStreamSynchronize(c->stream), "collide");
@@ -1002,6 +1034,40 @@ int cg_read_tri_pairs(cg_ctx* c, cg_tri_pair* out, uint64_t cap, uint64_t* n) {
     const uint64_t m = std::min(avail, cap);
     if (m) CG_CUDA(cudaMemcpy(out, c->d_pairs, sizeof(cg_tri_pair) * m, cudaMemcpyDeviceToHost), "read pairs");
     return c->h_ctr->n_pairs > avail ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
+int cg_set_host_outputs(cg_ctx* c, cg_tri_pair* pairs, uint64_t pairs_cap, cg_ray* rays, uint64_t rays_cap,
+                        cg_ray_average* averages, uint64_t averages_cap) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    // the device's address of a page-locked host buffer (null: none)
+    auto alias = [&](void* h, uint64_t cap, uintptr_t align, const char* what, void** d) -> int {
+        *d = nullptr;
+        if (!h || !cap) return CG_OK;
+        if (!aligned_to(h, align))
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "host %s buffer must be %u-byte aligned", what, unsigned(align));
+        const cudaError_t e = cudaHostGetDevicePointer(d, h, 0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "host %s buffer is not page-locked host memory (%s)", what,
+                        cudaGetErrorString(e));
+        }
+        return CG_OK;
+    };
+    void *dp = nullptr, *dr = nullptr, *da = nullptr;
+    int rc = alias(pairs, pairs_cap, 4, "pair", &dp);
+    if (rc == CG_OK) rc = alias(rays, rays_cap, 16, "ray", &dr);
+    if (rc == CG_OK) rc = alias(averages, averages_cap, 16, "ray-average", &da);
+    if (rc != CG_OK) return rc;
+    auto& H = c->host_out;
+    H.pairs = static_cast<cg_tri_pair*>(dp);
+    H.pairs_cap = dp ? pairs_cap : 0;
+    H.rays = static_cast<cg_ray*>(dr);
+    H.rays_cap = dr ? rays_cap : 0;
+    H.averages = static_cast<cg_ray_average*>(da);
+    H.averages_cap = da ? averages_cap : 0;
+    ++H.gen;
+    return CG_OK;
 }
 
 int cg_read_leaf_pairs(cg_ctx* c, cg_leaf_pair* out, uint64_t cap, uint64_t* n) {

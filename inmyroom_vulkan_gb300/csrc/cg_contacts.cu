@@ -559,6 +559,39 @@ cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned l
     return cudaGetLastError();
 }
 
+// Copies the step's results to the caller's page-locked host buffers (written
+// through the device's mapping of them): colliding pairs as 4-byte words (36 B
+// records), rays and per-query averages as 16-byte words. Counts from the
+// step's counters, capped by what the device buffers and the host buffers hold.
+__global__ void __launch_bounds__(256) copy_out_kernel(const CopyOutParams P) {
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long i0 = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const Counters& C = *P.ctr;
+    if (P.host_pairs) {
+        const unsigned long long n = min(min(C.n_pairs, P.pairs_avail), P.host_pairs_cap);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(P.pairs);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(P.host_pairs);
+        for (unsigned long long w = i0; w < 9ull * n; w += stride) dst[w] = __ldg(src + w);
+    }
+    if (P.host_rays) {
+        const unsigned long long n = min(min((unsigned long long)C.n_rays, P.rays_avail), P.host_rays_cap);
+        const uint4* src = reinterpret_cast<const uint4*>(P.rays);
+        uint4* dst = reinterpret_cast<uint4*>(P.host_rays);
+        for (unsigned long long w = i0; w < 2ull * n; w += stride) dst[w] = __ldg(src + w);
+    }
+    if (P.host_averages) {
+        const unsigned long long n = min((unsigned long long)C.n_queries, P.host_averages_cap);
+        const uint4* src = reinterpret_cast<const uint4*>(P.averages);
+        uint4* dst = reinterpret_cast<uint4*>(P.host_averages);
+        for (unsigned long long w = i0; w < 2ull * n; w += stride) dst[w] = __ldg(src + w);
+    }
+}
+
+cudaError_t launch_copy_out(const CopyOutParams& p, uint32_t blocks, cudaStream_t s) {
+    copy_out_kernel<<<blocks, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
 cudaError_t contacts_occupancy(int* accumulate_blocks_per_sm, int* emit_blocks_per_sm) {
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(accumulate_blocks_per_sm, contacts_accumulate_kernel,
                                                                   256, 0);

@@ -134,6 +134,23 @@ struct ContactParams {
 };
 
 cudaError_t launch_contacts(const ContactParams& p, uint32_t accumulate_grid, uint32_t emit_grid, cudaStream_t s);
+
+// Results of a step written to host buffers (cg_set_host_outputs).
+struct CopyOutParams {
+    const Counters* ctr;
+    const cg_tri_pair* pairs;
+    unsigned long long pairs_avail;  // records the device buffer holds
+    cg_tri_pair* host_pairs;         // device alias of the host buffer, or null
+    unsigned long long host_pairs_cap;
+    const cg_ray* rays;
+    unsigned long long rays_avail;
+    cg_ray* host_rays;
+    unsigned long long host_rays_cap;
+    const cg_ray_average* averages;
+    cg_ray_average* host_averages;
+    unsigned long long host_averages_cap;
+};
+cudaError_t launch_copy_out(const CopyOutParams& p, uint32_t blocks, cudaStream_t s);
 cudaError_t contacts_occupancy(int* accumulate_blocks_per_sm, int* emit_blocks_per_sm);
 cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
                                 cudaStream_t s);

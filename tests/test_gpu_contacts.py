@@ -177,3 +177,42 @@ def test_contacts_flag_combinations_and_overflow(port):
         ctx.reconfigure(max_contacts=1 << 18)
         st = ctx.collide(q, flags=capi.CG_CONTACTS)
         assert st["status"] == 0 and len(ctx.contacts()) > 16
+
+
+def test_host_outputs_match_the_read_calls(port):
+    """cg_set_host_outputs: one cg_collide writes the pairs, rays and
+    averages into page-locked host arrays; they equal what the read calls
+    return. A smaller pair capacity takes the first records; pageable memory is
+    refused."""
+    import torch
+
+    sc = scenes.scene()
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes[:96]]
+    keep = (sc.pairs[:, 0] < 96) & (sc.pairs[:, 1] < 96)
+    qa, qb = sc.pairs[keep, 0], sc.pairs[keep, 1]
+
+    def pinned(count, dtype):
+        return torch.empty(count * dtype.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(dtype)
+
+    with capi.Context() as ctx:
+        ids = [ctx.upload_flat(t.export()) for t in tp]
+        rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
+        q = capi.make_queries(np.asarray(ids)[qa], np.asarray(ids)[qb], rel)
+        st = ctx.collide(q, flags=capi.CG_CONTACTS)
+        n_p, n_r = st["tri_pairs"], st["rays"]
+        assert n_p > 1000 and n_r > 1000
+        hp, hr, ha = pinned(n_p + 7, capi.TRI_PAIR_DTYPE), pinned(n_r, capi.RAY_DTYPE), pinned(len(q),
+                                                                                            capi.RAY_AVERAGE_DTYPE)
+        ctx.set_host_outputs(hp, hr, ha)
+        st2 = ctx.collide(q, flags=capi.CG_CONTACTS)
+        assert st2["tri_pairs"] == n_p and st2["rays"] == n_r
+        assert np.array_equal(hp[:n_p].view(np.uint8), ctx.tri_pairs().view(np.uint8))
+        assert np.array_equal(hr.view(np.uint8), ctx.rays().view(np.uint8))
+        assert np.array_equal(ha.view(np.uint8), ctx.ray_averages().view(np.uint8))
+        small = pinned(100, capi.TRI_PAIR_DTYPE)
+        ctx.set_host_outputs(small)
+        ctx.collide(q)
+        assert np.array_equal(small.view(np.uint8), ctx.tri_pairs()[:100].view(np.uint8))
+        with pytest.raises(capi.CgError):
+            ctx.set_host_outputs(np.zeros(10, capi.TRI_PAIR_DTYPE))
+        ctx.set_host_outputs()
