@@ -25,9 +25,10 @@
 //                 per-vertex buffer (side B's turned back into its model space
 //                 by the transposed matrix)
 //   skin_adjoint  one thread per vertex with a gradient g (and clears it):
-//                 recomputes the morphed vertex u; for each influence (w, j):
-//                 dE/dG_j += w g (IBM_j u)^T, dE/du += w IBM_j^T G_j^T g;
-//                 dE/dw_i = dE/du . target_i. Block sums in shared memory.
+//                 recomputes the morphed vertex u; for each influence (w, j)
+//                 of skin matrix S_j = G_j IBM_j: dE/dS_j += w g u^T,
+//                 dE/du += w S_j^T g; dE/dw_i = dE/du . target_i; block sums
+//                 in shared memory, dE/dG_j = dE/dS_j IBM_j^T per block.
 //   pose_backward a half-warp per pose (lane = matrix entry), bones in reverse
 //                 order: dE/dG_parent += dE/dG_j L_j^T, dE/dL_j = G_parent^T
 //                 dE/dG_j, then the axis-angle rotation's adjoint.
@@ -75,10 +76,13 @@ __device__ __forceinline__ RotCoef rot_coef(float t2) {
     return k;
 }
 
+// a[i] by selects (a run-time index would put a in local memory)
+__device__ __forceinline__ float pick3(const float a[3], uint32_t i) { return i == 0u ? a[0] : (i == 1u ? a[1] : a[2]); }
+
 // [a]x entry (r, c), r, c < 3.
 __device__ __forceinline__ float skew(const float a[3], uint32_t r, uint32_t c) {
     if (r == c) return 0.0f;
-    const float v = a[3u - r - c];
+    const float v = pick3(a, 3u - r - c);
     return ((r + 1u) % 3u == c) ? -v : v;
 }
 
@@ -88,78 +92,140 @@ __device__ __forceinline__ float local_entry(const float a[3], float t2, const R
     if (r == 3u) return c == 3u ? 1.0f : 0.0f;
     if (c == 3u) return off[r];
     const float diag = r == c ? 1.0f : 0.0f;
-    return diag + k.A * skew(a, r, c) + k.B * (a[r] * a[c] - diag * t2);
+    return diag + k.A * skew(a, r, c) + k.B * (pick3(a, r) * pick3(a, c) - diag * t2);
 }
 
 // ---- posing ----
 
 // A half-warp per pose; lane l holds entry l of the column-major 4x4 (row
-// l & 3, column l >> 2). Bones in order; a parent precedes its children.
-__global__ void __launch_bounds__(128) pose_kernel(const PoseParams P) {
-    const uint32_t l = threadIdx.x & 15u, r = l & 3u, c = l >> 2;
-    const uint32_t pose = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-    const bool live = pose < P.n_poses;
-    const float* aa = P.axis_angles + 3ull * P.n_bones * pose;
-    float* G = P.joint_matrices + 16ull * P.n_bones * pose;
+// l & 3, column l >> 2). Bones in order; a parent precedes its children. The
+// chain of bones is a dependent sequence, so everything it touches (parents,
+// offsets, the pose's angles and matrices, the adjoint's accumulators) is
+// staged in shared memory when it fits (P.staged): a step then costs
+// shared-memory latency instead of a round trip to L2.
+struct PoseStage {
+    const int32_t* parent;
+    const float* offsets;
+    const float* aa;
+    float* G;
+    float* acc;  // adjoint only
+};
+
+// Shared layout: parent[nb] (int), offsets[3 nb], then per pose slot
+// aa[3 nb], G[16 nb] and, for the adjoint, acc[16 nb].
+__device__ __forceinline__ PoseStage pose_stage(const PoseParams& P, uint32_t slot, uint32_t pose, bool live,
+                                                bool adjoint) {
+    extern __shared__ float sh[];
+    const uint32_t nb = P.n_bones;
+    PoseStage st;
+    if (!P.staged) {
+        st.parent = P.parent;
+        st.offsets = P.offsets;
+        st.aa = P.axis_angles + 3ull * nb * pose;
+        st.G = P.joint_matrices + 16ull * nb * pose;
+        st.acc = adjoint ? P.grad_acc + 16ull * nb * pose : nullptr;
+        return st;
+    }
+    int32_t* par = reinterpret_cast<int32_t*>(sh);
+    float* off = sh + nb;
+    float* mine = sh + 4u * nb + size_t(slot) * (adjoint ? 35u : 19u) * nb;
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) par[i] = P.parent[i];
+    for (uint32_t i = threadIdx.x; i < 3u * nb; i += blockDim.x) off[i] = P.offsets[i];
+    const uint32_t l = threadIdx.x & 15u;
+    if (live) {
+        const float* aa = P.axis_angles + 3ull * nb * pose;
+        for (uint32_t i = l; i < 3u * nb; i += 16u) mine[i] = aa[i];
+        if (adjoint) {
+            const float* G = P.joint_matrices + 16ull * nb * pose;
+            const float* gin = P.grad_joint + 16ull * nb * pose;
+            for (uint32_t i = l; i < 16u * nb; i += 16u) {
+                mine[3u * nb + i] = G[i];
+                mine[19u * nb + i] = gin[i];
+            }
+        }
+    }
+    __syncthreads();
+    st.parent = par;
+    st.offsets = off;
+    st.aa = mine;
+    st.G = mine + 3u * nb;
+    st.acc = adjoint ? mine + 19u * nb : nullptr;
+    return st;
+}
+
+__global__ void __launch_bounds__(256) pose_kernel(const PoseParams P) {
+    const uint32_t slot = threadIdx.x >> 4, l = threadIdx.x & 15u, r = l & 3u, c = l >> 2;
+    const uint32_t pose = blockIdx.x * P.per_block + slot;
+    const bool live = slot < P.per_block && pose < P.n_poses;
+    const PoseStage S = pose_stage(P, slot, pose, live, false);
     for (uint32_t j = 0; j < P.n_bones; ++j) {
         if (live) {
-            const float a[3] = {aa[3 * j], aa[3 * j + 1], aa[3 * j + 2]};
+            const float a[3] = {S.aa[3 * j], S.aa[3 * j + 1], S.aa[3 * j + 2]};
             const float t2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
             const RotCoef k = rot_coef(t2);
-            const float* off = P.offsets + 3ull * j;
+            const float* off = S.offsets + 3ull * j;
             float L[4];  // column c of the local matrix
 #pragma unroll
             for (uint32_t i = 0; i < 4; ++i) L[i] = local_entry(a, t2, k, off, i, c);
-            const int par = P.parent[j];
+            const int par = S.parent[j];
             float g;
             if (par < 0) {
-                g = L[r];
+                g = r == 0u ? L[0] : (r == 1u ? L[1] : (r == 2u ? L[2] : L[3]));
             } else {
-                const float* Gp = G + 16ull * par;
+                const float* Gp = S.G + 16ull * par;
                 g = (Gp[r] * L[0] + Gp[4 + r] * L[1]) + (Gp[8 + r] * L[2] + Gp[12 + r] * L[3]);
             }
-            G[16ull * j + l] = g;
+            S.G[16ull * j + l] = g;
         }
         __syncwarp();  // the bone's entries are visible to the half-warp before a child reads them
     }
+    if (P.staged && live) {
+        float* out = P.joint_matrices + 16ull * P.n_bones * pose;
+        for (uint32_t i = l; i < 16u * P.n_bones; i += 16u) out[i] = S.G[i];
+    }
 }
 
-__global__ void __launch_bounds__(128) pose_backward_kernel(const PoseParams P) {
+__global__ void __launch_bounds__(256) pose_backward_kernel(const PoseParams P) {
     const uint32_t lane = threadIdx.x & 31u, base = lane & 16u, l = lane & 15u, r = l & 3u, c = l >> 2;
-    const uint32_t pose_w = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-    const bool live = pose_w < P.n_poses;
-    const uint32_t pose = live ? pose_w : P.n_poses - 1u;  // a spare half reads a real pose and writes nothing
-    const float* aa = P.axis_angles + 3ull * P.n_bones * pose;
-    const float* G = P.joint_matrices + 16ull * P.n_bones * pose;
-    const float* gin = P.grad_joint + 16ull * P.n_bones * pose;
-    float* acc = P.grad_acc + 16ull * P.n_bones * pose;
+    const uint32_t slot = threadIdx.x >> 4;
+    const uint32_t pose_w = blockIdx.x * P.per_block + slot;
+    const bool live = slot < P.per_block && pose_w < P.n_poses;
+    // a spare half-warp follows a real pose's reads (its shuffles need the
+    // whole warp) and writes nothing
+    const uint32_t pose = live ? pose_w : P.n_poses - 1u;
+    const bool stage_live = live || !P.staged;
+    const PoseStage S = pose_stage(P, slot, pose, live, true);
     float* ga = P.grad_axis_angles + 3ull * P.n_bones * pose;
-    if (live)
-        for (uint32_t j = 0; j < P.n_bones; ++j) acc[16ull * j + l] = gin[16ull * j + l];
+    if (live && !P.staged) {
+        const float* gin = P.grad_joint + 16ull * P.n_bones * pose;
+        for (uint32_t j = 0; j < P.n_bones; ++j) S.acc[16ull * j + l] = gin[16ull * j + l];
+    }
     for (uint32_t jj = P.n_bones; jj-- > 0;) {
         // every lane reads and writes only its own entry of acc; the entries
-        // of other lanes come by shuffle
-        const float g = acc[16ull * jj + l];  // dE/dG_j, children's shares included
-        const float a[3] = {aa[3 * jj], aa[3 * jj + 1], aa[3 * jj + 2]};
+        // of other lanes come by shuffle (a spare half-warp of a staged launch
+        // has no shared slot: it shuffles zeros)
+        const float g = stage_live ? S.acc[16ull * jj + l] : 0.0f;  // dE/dG_j, children's shares included
+        float a[3] = {0.f, 0.f, 0.f};
+        if (stage_live) a[0] = S.aa[3 * jj], a[1] = S.aa[3 * jj + 1], a[2] = S.aa[3 * jj + 2];
         const float t2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
         const RotCoef k = rot_coef(t2);
-        const float* off = P.offsets + 3ull * jj;
+        const float* off = S.offsets + 3ull * jj;
         float grow[4], gcol[4];
 #pragma unroll
         for (uint32_t i = 0; i < 4; ++i) {
             grow[i] = __shfl_sync(0xffffffffu, g, base + 4u * i + r);  // g[r][i]
             gcol[i] = __shfl_sync(0xffffffffu, g, base + 4u * c + i);  // g[i][c]
         }
-        const int par = P.parent[jj];
+        const int par = S.parent[jj];
         float gL = g;
-        if (par >= 0) {
+        if (par >= 0 && stage_live) {
             // dE/dG_par[r][c] += sum_i g[r][i] L[c][i]
             float add = 0.0f;
 #pragma unroll
             for (uint32_t i = 0; i < 4; ++i) add = add + grow[i] * local_entry(a, t2, k, off, c, i);
-            if (live) acc[16ull * par + l] += add;
+            if (live) S.acc[16ull * par + l] += add;
             // dE/dL[r][c] = sum_i G_par[i][r] g[i][c]
-            const float* Gp = G + 16ull * par;
+            const float* Gp = S.G + 16ull * par;
             gL = (Gp[4 * r] * gcol[0] + Gp[4 * r + 1] * gcol[1]) + (Gp[4 * r + 2] * gcol[2] + Gp[4 * r + 3] * gcol[3]);
         }
         float gR[3][3];
@@ -346,92 +412,160 @@ __global__ void __launch_bounds__(256) vertex_grad_kernel(const EnergyParams P) 
     }
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// dE/dS_j (S_j = G_j * IBM_j, the skin matrix) is summed per block in shared
+// memory: when every vertex of a warp with a gradient has the same joint in an
+// influence slot (a tube's ring shares its joints), the warp sums its terms
+// with shuffles and one lane adds them; otherwise each lane adds its own. At
+// the end dE/dG_j = dE/dS_j IBM_j^T goes to the output once per block.
 __global__ void __launch_bounds__(256) skin_adjoint_kernel(const EnergyParams P) {
-    extern __shared__ float sh[];  // [n_joints][12] dE/dG (column-major rows 0-2), then [n_targets] dE/dw
+    extern __shared__ float sh[];  // [nj][12] dE/dS (column-major rows 0-2), [nt] dE/dw, [nj][16] S when staged
     __shared__ int busy;
-    const EnergySide& S = P.sides[P.deforming[blockIdx.y]];
-    const DeformParams& D = S.d;
+    const EnergySide& ES = P.sides[P.deforming[blockIdx.y]];
+    const DeformParams& D = ES.d;
     if (blockIdx.x * blockDim.x >= D.n_vertices) return;  // whole block
     const uint32_t nj = D.n_groups ? D.n_joints : 0u, nt = D.n_targets;
-    float* gG = sh;
+    float* gS = sh;
     float* gw = sh + 12u * nj;
+    float* Ms = P.skin_in_smem ? gw + nt : nullptr;
     for (uint32_t e = threadIdx.x; e < 12u * nj + nt; e += blockDim.x) sh[e] = 0.0f;
+    if (Ms)
+        for (uint32_t e = threadIdx.x; e < 16u * nj; e += blockDim.x)
+            Ms[e] = skin_entry(D.joint_matrices + 16ull * (e >> 4), D.inverse_bind + 16ull * (e >> 4), e & 15u);
     if (threadIdx.x == 0) busy = 0;
     __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x < D.n_vertices) {
-        float* gp = P.vgrad + 3ull * (S.grad_base + x);
-        const float gx = gp[0], gy = gp[1], gz = gp[2];
-        if (gx != 0.0f || gy != 0.0f || gz != 0.0f) {
-            gp[0] = gp[1] = gp[2] = 0.0f;  // the buffer is zero again for the next call
-            busy = 1;
-            const float4 u = morph_vertex(D, x);
-            float gu[4] = {0.f, 0.f, 0.f, 0.f};
-            if (D.n_groups == 0) {
-                gu[0] = gx, gu[1] = gy, gu[2] = gz;
-            }
-            for (uint32_t grp = 0; grp < D.n_groups; ++grp) {
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    float* gp = P.vgrad + 3ull * (ES.grad_base + x);
+    if (x < D.n_vertices) gx = gp[0], gy = gp[1], gz = gp[2];
+    const bool has = gx != 0.0f || gy != 0.0f || gz != 0.0f;
+    if (has) gp[0] = gp[1] = gp[2] = 0.0f;  // the buffer is zero again for the next call
+    const unsigned act = __ballot_sync(0xffffffffu, has);
+    if (act) {
+        if (lane == 0) busy = 1;
+        const uint32_t leader = __ffs(act) - 1u;
+        const float4 u = has ? morph_vertex(D, x) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float uc[4] = {u.x, u.y, u.z, u.w};
+        float gu[4] = {0.f, 0.f, 0.f, 0.f};
+        if (D.n_groups == 0) gu[0] = gx, gu[1] = gy, gu[2] = gz;
+        for (uint32_t grp = 0; grp < D.n_groups; ++grp) {
+            float4 w4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            ushort4 j4 = make_ushort4(0xffff, 0xffff, 0xffff, 0xffff);
+            if (has) {
                 const size_t kk = size_t(D.n_groups) * x + grp;
-                const float4 w4 = reinterpret_cast<const float4*>(D.weights)[kk];
-                const ushort4 j4 = reinterpret_cast<const ushort4*>(D.joints)[kk];
-                const float we[4] = {w4.x, w4.y, w4.z, w4.w};
-                const uint32_t je[4] = {j4.x, j4.y, j4.z, j4.w};
+                w4 = reinterpret_cast<const float4*>(D.weights)[kk];
+                j4 = reinterpret_cast<const ushort4*>(D.joints)[kk];
+            }
+            const float we[4] = {w4.x, w4.y, w4.z, w4.w};
+            const uint32_t je[4] = {j4.x, j4.y, j4.z, j4.w};
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    if (je[e] >= nj || we[e] == 0.0f) continue;
-                    const float* Gj = D.joint_matrices + 16ull * je[e];
-                    const float* Ij = D.inverse_bind + 16ull * je[e];
-                    float iu[4];
-#pragma unroll
-                    for (int rr = 0; rr < 4; ++rr)
-                        iu[rr] = (Ij[rr] * u.x + Ij[4 + rr] * u.y) + (Ij[8 + rr] * u.z + Ij[12 + rr] * u.w);
-                    const float wg[3] = {we[e] * gx, we[e] * gy, we[e] * gz};
-                    float* dst = gG + 12u * je[e];
+            for (int e = 0; e < 4; ++e) {
+                const uint32_t j = je[e];
+                const bool ok = has && j < nj && we[e] != 0.0f;
+                const float wg[3] = {ok ? we[e] * gx : 0.f, ok ? we[e] * gy : 0.f, ok ? we[e] * gz : 0.f};
+                const uint32_t jl = __shfl_sync(0xffffffffu, j, leader);
+                const bool uniform = __all_sync(0xffffffffu, !ok || j == jl) && jl < nj;
+                if (uniform) {
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
-                        for (int rr = 0; rr < 3; ++rr) atomicAdd(dst + 3 * cc + rr, wg[rr] * iu[cc]);
-                    float t[4];  // G_j^T (w g)
+                        for (int rr = 0; rr < 3; ++rr) {
+                            const float v = warp_sum(wg[rr] * uc[cc]);
+                            if (lane == leader && v != 0.0f) atomicAdd(gS + 12u * jl + 3 * cc + rr, v);
+                        }
+                } else if (ok) {
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc)
-                        t[cc] = (Gj[4 * cc] * wg[0] + Gj[4 * cc + 1] * wg[1]) + Gj[4 * cc + 2] * wg[2];
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc)
-                        gu[cc] = gu[cc] + ((Ij[4 * cc] * t[0] + Ij[4 * cc + 1] * t[1]) +
-                                           (Ij[4 * cc + 2] * t[2] + Ij[4 * cc + 3] * t[3]));
+                        for (int rr = 0; rr < 3; ++rr) atomicAdd(gS + 12u * j + 3 * cc + rr, wg[rr] * uc[cc]);
+                }
+                if (ok) {
+                    float m[16];
+                    if (Ms) {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) m[i] = Ms[16u * j + i];
+                    } else {
+#pragma unroll
+                        for (uint32_t i = 0; i < 16; ++i)
+                            m[i] = skin_entry(D.joint_matrices + 16ull * j, D.inverse_bind + 16ull * j, i);
+                    }
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc)  // S_j^T (w g)
+                        gu[cc] = gu[cc] + ((m[4 * cc] * wg[0] + m[4 * cc + 1] * wg[1]) + m[4 * cc + 2] * wg[2]);
                 }
             }
-            const float4* tg = reinterpret_cast<const float4*>(D.vertices) + size_t(nt + 1u) * x + 1;
-            for (uint32_t i = 0; i < nt; ++i) {
+        }
+        const float4* tg = reinterpret_cast<const float4*>(D.vertices) + size_t(nt + 1u) * x + 1;
+        for (uint32_t i = 0; i < nt; ++i) {
+            float v = 0.0f;
+            if (has) {
                 const float4 d = tg[i];
-                atomicAdd(gw + i, (gu[0] * d.x + gu[1] * d.y) + (gu[2] * d.z + gu[3] * d.w));
+                v = (gu[0] * d.x + gu[1] * d.y) + (gu[2] * d.z + gu[3] * d.w);
             }
+            v = warp_sum(v);
+            if (lane == leader && v != 0.0f) atomicAdd(gw + i, v);
         }
     }
     __syncthreads();
     if (!busy) return;
     for (uint32_t e = threadIdx.x; e < 12u * nj; e += blockDim.x) {
-        const float v = gG[e];
-        if (v != 0.0f) {
-            const uint32_t j = e / 12u, cc = (e % 12u) / 3u, rr = e % 3u;
-            atomicAdd(S.grad_joint + 16ull * j + 4u * cc + rr, v);
-        }
+        const uint32_t j = e / 12u, cc = (e % 12u) / 3u, rr = e % 3u;
+        const float* d = gS + 12u * j;
+        const float* I = D.inverse_bind + 16ull * j;  // dE/dG = dE/dS IBM^T: sum_k dS[rr][k] IBM[cc][k]
+        const float v = (d[rr] * I[cc] + d[3 + rr] * I[4 + cc]) + (d[6 + rr] * I[8 + cc] + d[9 + rr] * I[12 + cc]);
+        if (v != 0.0f) atomicAdd(ES.grad_joint + 16ull * j + 4u * cc + rr, v);
     }
     for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x)
-        if (gw[i] != 0.0f) atomicAdd(S.grad_morph + i, gw[i]);
+        if (gw[i] != 0.0f) atomicAdd(ES.grad_morph + i, gw[i]);
 }
 
 }  // namespace
 
-cudaError_t launch_pose(const PoseParams& p, cudaStream_t s) {
-    if (p.n_poses == 0 || p.n_bones == 0) return cudaSuccess;
-    pose_kernel<<<(p.n_poses + 7u) / 8u, 128, 0, s>>>(p);
+// Shared memory of the skin adjoint: dE/dS (12 floats per joint) and the skin
+// matrices (16 per joint, up to kSkinStagedJoints joints; more joints form
+// them on the spot), plus up to 256 morph weights.
+constexpr uint32_t kSkinStagedJoints = 1024u;
+constexpr uint32_t kSkinAdjointSmemFloats =
+    (28u * kSkinStagedJoints > 12u * kMaxJoints ? 28u * kSkinStagedJoints : 12u * kMaxJoints) + 256u;
+
+// Poses per block and whether the chain is staged in shared memory (at most
+// kPoseSmem bytes: the adjoint's 35 floats per bone and pose, plus 4 per bone
+// for the skeleton).
+constexpr uint32_t kPoseSmem = 96u * 1024u;
+
+void pose_shape(PoseParams& p, bool adjoint, uint32_t* threads, size_t* smem) {
+    const size_t per_pose = sizeof(float) * (adjoint ? 35u : 19u) * p.n_bones;
+    const size_t common = sizeof(float) * 4u * p.n_bones;
+    const size_t fit = common < kPoseSmem ? (kPoseSmem - common) / per_pose : 0;
+    p.staged = fit >= 1 ? 1u : 0u;
+    p.per_block = p.staged ? uint32_t(fit < 8 ? fit : 8) : 8u;
+    *threads = (16u * p.per_block + 31u) / 32u * 32u;
+    *smem = p.staged ? common + per_pose * p.per_block : 0;
+}
+
+cudaError_t launch_pose(const PoseParams& p_in, cudaStream_t s) {
+    if (p_in.n_poses == 0 || p_in.n_bones == 0) return cudaSuccess;
+    PoseParams p = p_in;
+    uint32_t threads;
+    size_t smem;
+    pose_shape(p, false, &threads, &smem);
+    pose_kernel<<<(p.n_poses + p.per_block - 1u) / p.per_block, threads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pose_backward(const PoseParams& p, cudaStream_t s) {
-    if (p.n_poses == 0 || p.n_bones == 0) return cudaSuccess;
-    pose_backward_kernel<<<(p.n_poses + 7u) / 8u, 128, 0, s>>>(p);
+cudaError_t launch_pose_backward(const PoseParams& p_in, cudaStream_t s) {
+    if (p_in.n_poses == 0 || p_in.n_bones == 0) return cudaSuccess;
+    PoseParams p = p_in;
+    uint32_t threads;
+    size_t smem;
+    pose_shape(p, true, &threads, &smem);
+    pose_backward_kernel<<<(p.n_poses + p.per_block - 1u) / p.per_block, threads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -442,8 +576,12 @@ cudaError_t energy_occupancy(int* blocks_per_sm) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, vertex_grad_kernel, 256, 0);
     if (b < *blocks_per_sm) *blocks_per_sm = b;
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(pose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPoseSmem));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(pose_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPoseSmem));
+    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(skin_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(sizeof(float) * (12u * kMaxJoints + 256u)));
+                                int(sizeof(float) * kSkinAdjointSmemFloats));
 }
 
 cudaError_t launch_energy(const EnergyParams& p, uint32_t blocks, cudaStream_t s) {
@@ -455,8 +593,11 @@ cudaError_t launch_energy_backward(const EnergyParams& p, uint32_t blocks, uint3
     vertex_grad_kernel<<<blocks, 256, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.n_deforming == 0 || max_vertices == 0) return e;
-    const size_t smem = sizeof(float) * (12u * p.max_joints + p.max_targets);
-    skin_adjoint_kernel<<<dim3((max_vertices + 255u) / 256u, p.n_deforming), 256, smem, s>>>(p);
+    EnergyParams q = p;
+    // skin matrices staged in shared memory up to kSkinStagedJoints joints
+    q.skin_in_smem = p.max_joints <= kSkinStagedJoints ? 1u : 0u;
+    const size_t smem = sizeof(float) * ((q.skin_in_smem ? 28u : 12u) * p.max_joints + p.max_targets);
+    skin_adjoint_kernel<<<dim3((max_vertices + 255u) / 256u, p.n_deforming), 256, smem, s>>>(q);
     return cudaGetLastError();
 }
 

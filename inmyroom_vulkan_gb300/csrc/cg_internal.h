@@ -242,6 +242,7 @@ cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, u
 // world matrix is G_parent(j) * T(offset_j) * R(axis_angle_j).
 struct PoseParams {
     uint32_t n_poses, n_bones;
+    uint32_t per_block, staged;     // set by the launchers
     const int32_t* parent;          // [n_bones], < j or -1
     const float* offsets;           // [n_bones][3]
     const float* axis_angles;       // [n_poses][n_bones][3]
@@ -278,6 +279,7 @@ struct EnergyParams {
     const uint32_t* deforming;    // indices into sides of the deforming ones
     float* vgrad;                 // [sum of deforming sides' n_vertices][3], zero between calls
     uint32_t max_joints, max_targets;
+    uint32_t skin_in_smem;        // set by the launcher
 };
 cudaError_t launch_energy(const EnergyParams& p, uint32_t blocks, cudaStream_t s);
 cudaError_t launch_energy_backward(const EnergyParams& p, uint32_t blocks, uint32_t max_vertices, cudaStream_t s);
