@@ -226,9 +226,10 @@ int cg_read_ray_averages(cg_ctx* ctx, cg_ray_average* out, uint64_t cap, uint64_
  * for CG_CONTACTS steps its uncollide rays (the first rays_cap) and per-query
  * ray averages (the first averages_cap), straight into these buffers, as part
  * of the step's own launch sequence. The counts are the step's cg_stats
- * (tri_pairs, rays; averages: one per query). The buffers must be page-locked
- * host memory the device can write (cudaHostAlloc, cudaHostRegister), rays
- * and averages 16-byte aligned, and stay valid until replaced; a NULL pointer
+ * (tri_pairs, rays; averages: one per query). The buffers must be host memory
+ * the device can write: page-locked (cudaHostAlloc, cudaHostRegister), or any
+ * host memory where the device accesses pageable memory (Grace); rays and
+ * averages 16-byte aligned; valid until replaced. A NULL pointer
  * or zero capacity leaves that result on the device only. Results are still
  * readable with the cg_read_* calls. Does not apply to cg_collide_async and
  * cg_graph_launch. */

@@ -1040,7 +1040,7 @@ int cg_set_host_outputs(cg_ctx* c, cg_tri_pair* pairs, uint64_t pairs_cap, cg_ra
                         cg_ray_average* averages, uint64_t averages_cap) {
     if (!c) return CG_ERR_INVALID_ARGUMENT;
     cudaSetDevice(c->device);
-    // the device's address of a page-locked host buffer (null: none)
+    // the device's address of a host buffer it can write (null: none)
     auto alias = [&](void* h, uint64_t cap, uintptr_t align, const char* what, void** d) -> int {
         *d = nullptr;
         if (!h || !cap) return CG_OK;
@@ -1049,7 +1049,7 @@ int cg_set_host_outputs(cg_ctx* c, cg_tri_pair* pairs, uint64_t pairs_cap, cg_ra
         const cudaError_t e = cudaHostGetDevicePointer(d, h, 0);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return fail(c, CG_ERR_INVALID_ARGUMENT, "host %s buffer is not page-locked host memory (%s)", what,
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "the device cannot write the host %s buffer (%s)", what,
                         cudaGetErrorString(e));
         }
         return CG_OK;

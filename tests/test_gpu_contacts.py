@@ -182,8 +182,7 @@ def test_contacts_flag_combinations_and_overflow(port):
 def test_host_outputs_match_the_read_calls(port):
     """cg_set_host_outputs: one cg_collide writes the pairs, rays and
     averages into page-locked host arrays; they equal what the read calls
-    return. A smaller pair capacity takes the first records; pageable memory is
-    refused."""
+    return. A smaller pair capacity takes the first records."""
     import torch
 
     sc = scenes.scene()
@@ -213,6 +212,14 @@ def test_host_outputs_match_the_read_calls(port):
         ctx.set_host_outputs(small)
         ctx.collide(q)
         assert np.array_equal(small.view(np.uint8), ctx.tri_pairs()[:100].view(np.uint8))
-        with pytest.raises(capi.CgError):
-            ctx.set_host_outputs(np.zeros(10, capi.TRI_PAIR_DTYPE))
+        # pageable memory: refused, unless the device writes pageable host
+        # memory directly (as on Grace), and then the results land there too
+        pageable = np.zeros(100, capi.TRI_PAIR_DTYPE)
+        try:
+            ctx.set_host_outputs(pageable)
+        except capi.CgError:
+            pass
+        else:
+            ctx.collide(q)
+            assert np.array_equal(pageable.view(np.uint8), ctx.tri_pairs()[:100].view(np.uint8))
         ctx.set_host_outputs()
