@@ -171,12 +171,23 @@ __device__ __forceinline__ void sat_two(const Box& a0, const Box& b0, const Box&
     ok1 = al1;
 }
 
-// Rounds [g0, g1) of one SAT, stopping at the first separating round.
-__device__ __forceinline__ bool sat_rounds(const Box& a, const Box& b, int g0, int g1) {
-    bool ok = true;
-#pragma unroll 1
-    for (int g = g0; g < g1 && ok; ++g) ok = sat_round(a, b, g);
-    return ok;
+// Axis k (0..14) of the SAT in the reference's order: a's face normals
+// (v x w, u x w, u x v), b's, then a_i x b_j; true when the boxes overlap on
+// it. The SAT verdict is the conjunction over k, whatever lanes compute it.
+__device__ __forceinline__ bool sat_axis(const Box& a, const Box& b, uint32_t k) {
+    float3 x, y;
+    if (k < 6u) {
+        const bool onA = k < 3u;
+        const uint32_t f = onA ? k : k - 3u;
+        const float3 u = onA ? a.u : b.u, v = onA ? a.v : b.v, w = onA ? a.w : b.w;
+        x = f == 0u ? v : u;
+        y = f == 2u ? v : w;
+    } else {
+        const uint32_t i = (k - 6u) / 3u, j = (k - 6u) % 3u;
+        x = i == 0u ? a.u : (i == 1u ? a.v : a.w);
+        y = j == 0u ? b.u : (j == 1u ? b.v : b.w);
+    }
+    return overlap_on(a, b, cross3(x, y));
 }
 
 // The reference descent rule (OBBtree.cpp:414-476) for a child pair whose
@@ -507,13 +518,17 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
         // tests both children of a split node against the other box: the
         // other record is loaded (and, for the second tree, transformed) once,
         // the two child records come from one 128-byte line. With more than
-        // 16 items a lane runs an item's two SATs side by side; with 9..16 two
-        // lanes share an item (one child each), with up to 8 four lanes (each
-        // a part of one child's 15 axes), so that a step with few items takes
-        // less time. Every verdict is the conjunction of the same 15 axes.
+        // 16 items a lane runs an item's two SATs side by side; with fewer,
+        // 2 L lanes share an item, L per child (L = 1, 2, 4, 8, 16 for 9-16,
+        // 5-8, 3-4, 2 and 1 items), each taking every L-th of the child's 15
+        // axes, so that a step with few items (the ramp and the tail of a
+        // launch, where the deepest queries' chains of dependent steps set
+        // the time) takes less time. Every verdict is the conjunction of the
+        // same 15 axes.
         const uint32_t size = top - bot;
         const uint32_t n = size < 32u ? size : 32u;
-        const uint32_t lg = n <= 8u ? 2u : (n <= 16u ? 1u : 0u);  // log2 of lanes per item
+        // log2 of lanes per item
+        const uint32_t lg = n <= 1u ? 5u : (n <= 2u ? 4u : (n <= 4u ? 3u : (n <= 8u ? 2u : (n <= 16u ? 1u : 0u))));
         const uint32_t slot_i = uint32_t(lane) >> lg;
         const uint32_t sub = uint32_t(lane) & ((1u << lg) - 1u);
         const bool active = slot_i < n;
@@ -557,9 +572,10 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
                 if (ok[1]) descend(P, sideB, O, C1, is + 1u, io, qi, b1, item[1], leaf[1], out_q[1], out_s[1], out_o[1]);
             }
         } else {
-            const uint32_t kc = sub & 1u;    // the child this lane tests
-            const uint32_t part = sub >> 1;  // with four lanes: rounds 0..2 or 3..4 of its SAT
-            bool ok = false;
+            const uint32_t lc = lg - 1u;               // log2 of lanes per child
+            const uint32_t kc = sub >> lc;             // the child this lane tests
+            const uint32_t ax0 = sub & ((1u << lc) - 1u);  // its first axis; it takes every (1 << lc)-th
+            bool ok = true;
             Rec O, C;
             Box bx;
             if (active) {
@@ -568,10 +584,14 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
                 C = load_rec(P.recs, is + kc);
                 const Box ax = sideB ? O.box : C.box;
                 bx = xform_box(M, sideB ? C.box : O.box);
-                ok = lg == 1u ? sat_rounds(ax, bx, 0, 5) : sat_rounds(ax, bx, part ? 3 : 0, part ? 5 : 3);
+#pragma unroll 1
+                for (uint32_t k = ax0; k < 15u && ok; k += 1u << lc) ok = sat_axis(ax, bx, k);
             }
-            if (lg == 2u) ok = ok & (__shfl_xor_sync(kFull, ok ? 1 : 0, 2) != 0);
-            if (active && ok && part == 0u)
+            // the child's verdict: no lane of its group found a separating axis
+            const unsigned fail = __ballot_sync(kFull, !ok);
+            const unsigned group = (lc == 4u ? 0xffffu : ((1u << (1u << lc)) - 1u)) << (uint32_t(lane) & ~((1u << lc) - 1u));
+            ok = (fail & group) == 0u;
+            if (active && ok && ax0 == 0u)
                 descend(P, sideB, O, C, is + kc, io, qi, bx, item[0], leaf[0], out_q[0], out_s[0], out_o[0]);
         }
 
