@@ -111,6 +111,8 @@ struct cg_ctx {
         uint32_t n_tri_used = 0;  // the tree's triangle count (n_tris is at least 1)
         float* nrm = nullptr;
         uint2* ranges = nullptr;  // per record: first triangle and count of its subtree (refit)
+        uint32_t* big = nullptr;  // refit: records with more than kSmallPoints points, largest first
+        uint32_t n_big = 0, n_block = 0;
         bool live = false;
     };
     std::vector<Slot> trees;
@@ -748,6 +750,7 @@ int cg_destroy(cg_ctx* c) {
     for (auto& s : c->trees) {
         cudaFree(s.nrm);
         cudaFree(s.ranges);
+        cudaFree(s.big);
     }
     c->recs.destroy();
     c->tris.destroy();
@@ -895,6 +898,20 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
         CG_CUDA(cudaMalloc(&slot.ranges, sizeof(uint2) * n_recs), "alloc record ranges");
         CG_CUDA(cudaMemcpyAsync(slot.ranges, rg.data(), sizeof(uint2) * n_recs, cudaMemcpyHostToDevice, c->stream),
                 "upload record ranges");
+        // the refit's large boxes, largest first
+        std::vector<uint32_t> big;
+        for (uint32_t r = 0; r < n_recs; ++r)
+            if (rg[r].y != ~0u && 3ull * rg[r].y > kSmallPoints) big.push_back(r);
+        std::stable_sort(big.begin(), big.end(), [&](uint32_t a, uint32_t b) { return rg[a].y > rg[b].y; });
+        slot.n_big = uint32_t(big.size());
+        slot.n_block = 0;
+        while (slot.n_block < slot.n_big && 3ull * rg[big[slot.n_block]].y > kBlockPoints) ++slot.n_block;
+        if (!big.empty()) {
+            CG_CUDA(cudaMalloc(&slot.big, sizeof(uint32_t) * big.size()), "alloc refit list");
+            CG_CUDA(cudaMemcpyAsync(slot.big, big.data(), sizeof(uint32_t) * big.size(), cudaMemcpyHostToDevice,
+                                    c->stream),
+                    "upload refit list");
+        }
         CG_CUDA(cudaStreamSynchronize(c->stream), "upload record ranges");
     }
     slot.n_tri_used = T;
@@ -928,6 +945,7 @@ int cg_tree_free(cg_ctx* c, uint32_t id) {
     c->tris.release(s.tri_base, s.n_tris);
     cudaFree(s.nrm);
     cudaFree(s.ranges);
+    cudaFree(s.big);
     s = cg_ctx::Slot{};
     return sync_tree_table(c);
 }
@@ -1207,7 +1225,7 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
     if (!c || (n && (!tree_ids || !positions || !n_positions))) return CG_ERR_INVALID_ARGUMENT;
     if (n == 0) return CG_OK;
     std::vector<RefitTree> table(n);
-    uint32_t max_tris = 0, max_recs = 0, total_recs = 0;
+    uint32_t max_tris = 0, max_recs = 0, total_recs = 0, max_block = 0, max_warp = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t id = tree_ids[i];
         if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
@@ -1215,7 +1233,10 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
             return fail(c, CG_ERR_INVALID_ARGUMENT, "positions %u must be 16-byte aligned device memory", i);
         const auto& t = c->trees[id];
         table[i] = RefitTree{uint32_t(t.rec_base), uint32_t(t.n_recs), uint32_t(t.tri_base), t.n_tri_used, t.ranges,
-                             reinterpret_cast<const float4*>(positions[i]), n_positions[i], total_recs};
+                             reinterpret_cast<const float4*>(positions[i]), n_positions[i], total_recs,
+                             t.big, t.n_big, t.n_block};
+        max_block = std::max(max_block, t.n_block);
+        max_warp = std::max(max_warp, t.n_big - t.n_block);
         total_recs += uint32_t(t.n_recs);
         max_tris = std::max(max_tris, t.n_tri_used);
         max_recs = std::max(max_recs, uint32_t(t.n_recs));
@@ -1234,7 +1255,7 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
         c->refit_scratch_cap = total_recs;
     }
     CG_CUDA(launch_refit(c->recs.ptr, c->tris.ptr, static_cast<const RefitTree*>(d_table), n, max_tris, max_recs,
-                         c->refit_scratch, s),
+                         max_block, max_warp, c->refit_scratch, s),
             "refit kernels");
     return CG_OK;
 }

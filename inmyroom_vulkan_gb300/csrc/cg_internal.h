@@ -226,7 +226,11 @@ struct RefitTree {
     const uint2* ranges;
     const float4* positions;
     uint32_t n_positions, scratch_base;
+    const uint32_t* big;      // records with more than kSmallPoints points, largest first
+    uint32_t n_big, n_block;  // list length; the first n_block have more than kBlockPoints
 };
+constexpr uint32_t kSmallPoints = 48;    // refit: boxes up to this many points take one thread
+constexpr uint32_t kBlockPoints = 1536;  // refit: boxes above this many points take a block
 enum : uint32_t { kRefitSkip = 0, kRefitEmpty = 1, kRefitPoint = 2, kRefitBox = 3 };
 struct RefitScratch {
     float cov[6];   // xx, yy, zz, xy, xz, yz
@@ -236,7 +240,8 @@ struct RefitScratch {
     uint32_t kind;
 };
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, RefitScratch* scratch, cudaStream_t s);
+                         uint32_t max_recs, uint32_t max_block, uint32_t max_warp, RefitScratch* scratch,
+                         cudaStream_t s);
 
 // Axis-angle posing of a skeleton and its adjoint (cg_energy.cu): bone j's
 // world matrix is G_parent(j) * T(offset_j) * R(axis_angle_j).

@@ -11,10 +11,12 @@
 // 12k-triangle tube's root takes tens of milliseconds here):
 //   refit_moments  compensated FP32 sums of the points and of their centred
 //                  products: a thread per box of up to kSmallPoints points, a
-//                  warp per larger box (lane sums combined with error-free
-//                  FP32 sums)
+//                  warp per larger box, a block per box of more than
+//                  kBlockPoints (lane sums combined with error-free FP32
+//                  sums); the larger boxes come from a per-tree list made at
+//                  upload, largest first
 //   refit_axes     a thread per box: the eig3 procedure in FP32
-//   refit_box      FP32 projections (thread or warp per box as above); the box
+//   refit_box      FP32 projections (thread, warp or block per box as above); the box
 //                  is padded by 2 FLT_EPSILON plus a bound on the FP32
 //                  rounding of the projections, the axes' departure from
 //                  orthonormal and the box's assembly, so it contains every
@@ -34,7 +36,6 @@ namespace {
 
 constexpr unsigned kAll = 0xffffffffu;
 constexpr int kRefitWarps = 4;           // warps per block of the warp-per-box kernels
-constexpr uint32_t kSmallPoints = 48;    // boxes up to this many points take one thread
 
 template <typename R>
 __device__ __forceinline__ R hyp(R x, R y) {
@@ -287,7 +288,7 @@ __global__ void refit_moments_small_kernel(const float4* tris, const RefitTree* 
         return;
     }
     const uint32_t n_pts = 3u * rg.y;
-    if (n_pts > kSmallPoints) return;  // the warp kernel's
+    if (n_pts > kSmallPoints) return;  // a warp or block kernel's
     const float4* pt = tris + 3ull * (T.tri_base + rg.x);
     const float4 p0 = pt[0];
     KSum sx, sy, sz;
@@ -319,23 +320,67 @@ __global__ void refit_moments_small_kernel(const float4* tris, const RefitTree* 
     record_out(out, p0, differ, mabs, cov);
 }
 
-// Warp per large box: the same over all lanes, combined with error-free sums.
-__global__ void __launch_bounds__(32 * kRefitWarps) refit_moments_kernel(const float4* tris, const RefitTree* trees,
-                                                                          RefitScratch* scratch) {
-    const RefitTree T = trees[blockIdx.y];
-    const int lane = threadIdx.x & 31;
-    const uint32_t r = blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
-    if (r >= T.n_recs) return;  // whole warps
-    const uint2 rg = T.ranges[r];
-    if (rg.y == ~0u || 3ull * rg.y <= kSmallPoints) return;  // the small kernel's
-    RefitScratch& out = scratch[T.scratch_base + r];
-    const uint32_t n_pts = 3u * rg.y;
-    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
+// Reductions over the points of one box by a warp (G = 32) or a whole block
+// (G = 256, `red` = 18 floats of shared memory); the result is the same on
+// every thread of the group.
+template <int G>
+struct Group;
+template <>
+struct Group<32> {
+    __device__ static void sum2(float& h, float& l, float*) { warp_sum2(h, l); }
+    __device__ static float maxf(float v, float*) { return warp_maxf(v); }
+    __device__ static float minf(float v, float*) { return warp_minf(v); }
+    __device__ static bool any(bool b, float*) { return __any_sync(kAll, b); }
+};
+template <>
+struct Group<256> {
+    __device__ static void sum2(float& h, float& l, float* red) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        warp_sum2(h, l);
+        if (lane == 0) red[2 * w] = h, red[2 * w + 1] = l;
+        __syncthreads();
+        if (w == 0) {
+            float hh = lane < 8 ? red[2 * lane] : 0.f, ll = lane < 8 ? red[2 * lane + 1] : 0.f;
+            warp_sum2(hh, ll);
+            if (lane == 0) red[16] = hh, red[17] = ll;
+        }
+        __syncthreads();
+        h = red[16];
+        l = red[17];
+        __syncthreads();
+    }
+    template <bool kMax>
+    __device__ static float ext(float v, float* red) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        v = kMax ? warp_maxf(v) : warp_minf(v);
+        if (lane == 0) red[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            float x = lane < 8 ? red[lane] : red[0];
+            x = kMax ? warp_maxf(x) : warp_minf(x);
+            if (lane == 0) red[16] = x;
+        }
+        __syncthreads();
+        v = red[16];
+        __syncthreads();
+        return v;
+    }
+    __device__ static float maxf(float v, float* red) { return ext<true>(v, red); }
+    __device__ static float minf(float v, float* red) { return ext<false>(v, red); }
+    __device__ static bool any(bool b, float*) { return __syncthreads_or(b) != 0; }
+};
+
+// The moments of a large box's points by a group of G threads (thread t),
+// lane sums combined with error-free sums.
+template <int G>
+__device__ __forceinline__ void group_moments(const float4* pt, uint32_t n_pts, uint32_t t, RefitScratch& out,
+                                              float* red) {
     const float4 p0 = pt[0];
     KSum sx, sy, sz;
     float mabs = 0.f;
     bool differ = false;
-    for (uint32_t k = lane; k < n_pts; k += 32) {
+#pragma unroll 4
+    for (uint32_t k = t; k < n_pts; k += G) {
         const float4 p = pt[k];
         sx.add(p.x);
         sy.add(p.y);
@@ -343,20 +388,21 @@ __global__ void __launch_bounds__(32 * kRefitWarps) refit_moments_kernel(const f
         mabs = fmaxf(mabs, (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z));
         differ |= p.x != p0.x || p.y != p0.y || p.z != p0.z;
     }
-    differ = __any_sync(kAll, differ);
-    mabs = warp_maxf(mabs);
+    differ = Group<G>::any(differ, red);
+    mabs = Group<G>::maxf(mabs, red);
     if (!differ) {
-        if (lane == 0) record_out(out, p0, false, mabs, nullptr);
+        if (t == 0) record_out(out, p0, false, mabs, nullptr);
         return;
     }
     float hx = sx.s, lx = -sx.c, hy = sy.s, ly = -sy.c, hz = sz.s, lz = -sz.c;
-    warp_sum2(hx, lx);
-    warp_sum2(hy, ly);
-    warp_sum2(hz, lz);
+    Group<G>::sum2(hx, lx, red);
+    Group<G>::sum2(hy, ly, red);
+    Group<G>::sum2(hz, lz, red);
     const float fn = float(n_pts);
     const float mx = (hx + lx) / fn, my = (hy + ly) / fn, mz = (hz + lz) / fn;
     KSum c[6];
-    for (uint32_t k = lane; k < n_pts; k += 32) {
+#pragma unroll 4
+    for (uint32_t k = t; k < n_pts; k += G) {
         const float4 p = pt[k];
         const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
         c[0].add(dx * dx);
@@ -370,10 +416,34 @@ __global__ void __launch_bounds__(32 * kRefitWarps) refit_moments_kernel(const f
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
         float h = c[i].s, l = -c[i].c;
-        warp_sum2(h, l);
+        Group<G>::sum2(h, l, red);
         cov[i] = (h + l) / fn;
     }
-    if (lane == 0) record_out(out, p0, true, mabs, cov);
+    if (t == 0) record_out(out, p0, true, mabs, cov);
+}
+
+// Large boxes come from the tree's list of records with more than
+// kSmallPoints points, largest first: the first n_block (more than
+// kBlockPoints points) take a block each, the rest a warp each.
+__global__ void __launch_bounds__(256) refit_moments_block_kernel(const float4* tris, const RefitTree* trees,
+                                                                  RefitScratch* scratch) {
+    __shared__ float red[32];
+    const RefitTree T = trees[blockIdx.y];
+    if (blockIdx.x >= T.n_block) return;
+    const uint32_t r = T.big[blockIdx.x];
+    const uint2 rg = T.ranges[r];
+    group_moments<256>(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x, scratch[T.scratch_base + r], red);
+}
+
+__global__ void __launch_bounds__(32 * kRefitWarps) refit_moments_kernel(const float4* tris, const RefitTree* trees,
+                                                                          RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t i = T.n_block + blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
+    if (i >= T.n_big) return;  // whole warps
+    const uint32_t r = T.big[i];
+    const uint2 rg = T.ranges[r];
+    group_moments<32>(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x & 31u, scratch[T.scratch_base + r],
+                      nullptr);
 }
 
 // One thread per record: the eigensystem of the covariance by the eig3
@@ -448,7 +518,7 @@ __global__ void refit_box_small_kernel(float4* recs, const float4* tris, const R
         write_box(recs, T.rec_base + r, special_box(sc));
         return;
     }
-    if (n_pts > kSmallPoints) return;  // the warp kernel's
+    if (n_pts > kSmallPoints) return;  // a warp or block kernel's
     const float4* pt = tris + 3ull * (T.tri_base + rg.x);
     float ax[9];
     for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
@@ -466,26 +536,17 @@ __global__ void refit_box_small_kernel(float4* recs, const float4* tris, const R
     write_box(recs, T.rec_base + r, assemble(ax, lo, hi, sc.maxabs));
 }
 
-// Warp per large box.
-__global__ void __launch_bounds__(32 * kRefitWarps) refit_box_kernel(float4* recs, const float4* tris,
-                                                                      const RefitTree* trees,
-                                                                      const RefitScratch* scratch) {
-    const RefitTree T = trees[blockIdx.y];
-    const int lane = threadIdx.x & 31;
-    const uint32_t r = blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
-    if (r >= T.n_recs) return;  // whole warps
-    const uint2 rg = T.ranges[r];
-    if (rg.y == ~0u || 3ull * rg.y <= kSmallPoints) return;  // the small kernel's
-    const RefitScratch& sc = scratch[T.scratch_base + r];
-    if (sc.kind != kRefitBox) return;  // written by the small kernel
-    const uint32_t n_pts = 3u * rg.y;
-    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
+// Extent of a large box's points on its axes by a group of G threads.
+template <int G>
+__device__ __forceinline__ void group_box(float4* recs, uint32_t rec, const float4* pt, uint32_t n_pts, uint32_t t,
+                                          const RefitScratch& sc, float* red) {
     float ax[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
     const float inf = __int_as_float(0x7f800000);
     float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-    for (uint32_t k = lane; k < n_pts; k += 32) {
+#pragma unroll 4
+    for (uint32_t k = t; k < n_pts; k += G) {
         const float4 p = pt[k];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -496,25 +557,55 @@ __global__ void __launch_bounds__(32 * kRefitWarps) refit_box_kernel(float4* rec
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        lo[a] = warp_minf(lo[a]);
-        hi[a] = warp_maxf(hi[a]);
+        lo[a] = Group<G>::minf(lo[a], red);
+        hi[a] = Group<G>::maxf(hi[a], red);
     }
-    if (lane == 0) write_box(recs, T.rec_base + r, assemble(ax, lo, hi, sc.maxabs));
+    if (t == 0) write_box(recs, rec, assemble(ax, lo, hi, sc.maxabs));
+}
+
+__global__ void __launch_bounds__(256) refit_box_block_kernel(float4* recs, const float4* tris, const RefitTree* trees,
+                                                              const RefitScratch* scratch) {
+    __shared__ float red[32];
+    const RefitTree T = trees[blockIdx.y];
+    if (blockIdx.x >= T.n_block) return;
+    const uint32_t r = T.big[blockIdx.x];
+    const RefitScratch& sc = scratch[T.scratch_base + r];
+    if (sc.kind != kRefitBox) return;  // written by the small kernel (whole block)
+    const uint2 rg = T.ranges[r];
+    group_box<256>(recs, T.rec_base + r, tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x, sc, red);
+}
+
+__global__ void __launch_bounds__(32 * kRefitWarps) refit_box_kernel(float4* recs, const float4* tris,
+                                                                      const RefitTree* trees,
+                                                                      const RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t i = T.n_block + blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
+    if (i >= T.n_big) return;  // whole warps
+    const uint32_t r = T.big[i];
+    const RefitScratch& sc = scratch[T.scratch_base + r];
+    if (sc.kind != kRefitBox) return;  // written by the small kernel
+    const uint2 rg = T.ranges[r];
+    group_box<32>(recs, T.rec_base + r, tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x & 31u, sc,
+                  nullptr);
 }
 
 }  // namespace
 
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, RefitScratch* scratch, cudaStream_t s) {
+                         uint32_t max_recs, uint32_t max_block, uint32_t max_warp, RefitScratch* scratch,
+                         cudaStream_t s) {
     if (n_trees == 0) return cudaSuccess;
     if (max_tris) refit_tris_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees);
     const dim3 threads((max_recs + 127u) / 128u, n_trees);
-    const dim3 warps((max_recs + kRefitWarps - 1) / kRefitWarps, n_trees);
+    const dim3 blocks(max_block, n_trees);
+    const dim3 warps((max_warp + kRefitWarps - 1) / kRefitWarps, n_trees);
     refit_moments_small_kernel<<<threads, 128, 0, s>>>(tris, d_trees, scratch);
-    refit_moments_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(tris, d_trees, scratch);
+    if (max_block) refit_moments_block_kernel<<<blocks, 256, 0, s>>>(tris, d_trees, scratch);
+    if (max_warp) refit_moments_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(tris, d_trees, scratch);
     refit_axes_kernel<<<threads, 128, 0, s>>>(d_trees, scratch);
     refit_box_small_kernel<<<threads, 128, 0, s>>>(recs, tris, d_trees, scratch);
-    refit_box_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(recs, tris, d_trees, scratch);
+    if (max_block) refit_box_block_kernel<<<blocks, 256, 0, s>>>(recs, tris, d_trees, scratch);
+    if (max_warp) refit_box_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(recs, tris, d_trees, scratch);
     return cudaGetLastError();
 }
 
