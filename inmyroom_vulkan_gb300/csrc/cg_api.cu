@@ -111,8 +111,8 @@ struct cg_ctx {
         uint32_t n_tri_used = 0;  // the tree's triangle count (n_tris is at least 1)
         float* nrm = nullptr;
         uint2* ranges = nullptr;  // per record: first triangle and count of its subtree (refit)
-        uint32_t* big = nullptr;  // refit: records with more than kSmallPoints points, largest first
-        uint32_t n_big = 0, n_block = 0;
+        uint32_t* topo = nullptr;  // refit: parent per record, leaf record per triangle, the leaf records
+        uint32_t n_leaves = 0;
         bool live = false;
     };
     std::vector<Slot> trees;
@@ -750,7 +750,7 @@ int cg_destroy(cg_ctx* c) {
     for (auto& s : c->trees) {
         cudaFree(s.nrm);
         cudaFree(s.ranges);
-        cudaFree(s.big);
+        cudaFree(s.topo);
     }
     c->recs.destroy();
     c->tris.destroy();
@@ -898,20 +898,35 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
         CG_CUDA(cudaMalloc(&slot.ranges, sizeof(uint2) * n_recs), "alloc record ranges");
         CG_CUDA(cudaMemcpyAsync(slot.ranges, rg.data(), sizeof(uint2) * n_recs, cudaMemcpyHostToDevice, c->stream),
                 "upload record ranges");
-        // the refit's large boxes, largest first
-        std::vector<uint32_t> big;
-        for (uint32_t r = 0; r < n_recs; ++r)
-            if (rg[r].y != ~0u && 3ull * rg[r].y > kSmallPoints) big.push_back(r);
-        std::stable_sort(big.begin(), big.end(), [&](uint32_t a, uint32_t b) { return rg[a].y > rg[b].y; });
-        slot.n_big = uint32_t(big.size());
-        slot.n_block = 0;
-        while (slot.n_block < slot.n_big && 3ull * rg[big[slot.n_block]].y > kBlockPoints) ++slot.n_block;
-        if (!big.empty()) {
-            CG_CUDA(cudaMalloc(&slot.big, sizeof(uint32_t) * big.size()), "alloc refit list");
-            CG_CUDA(cudaMemcpyAsync(slot.big, big.data(), sizeof(uint32_t) * big.size(), cudaMemcpyHostToDevice,
-                                    c->stream),
-                    "upload refit list");
+        // the refit's view of the topology: the parent box of every record,
+        // the leaf box of every triangle and the list of leaf boxes (a node's
+        // record is known before its children's: pre-order)
+        std::vector<uint32_t> topo(size_t(n_recs) + T, ~0u), rec_of_node(N, ~0u), leaves;
+        uint32_t* parent = topo.data();
+        uint32_t* leaf_of_tri = topo.data() + n_recs;
+        if (N) rec_of_node[0] = 1;
+        for (uint32_t k = 0; k < N; ++k)
+            for (int s2 = 0; s2 < 2; ++s2) {
+                const uint32_t r = 2u * k + 2u + uint32_t(s2);
+                const uint32_t ref = v->node_ref[2 * k + s2], cnt = v->node_tri_count[2 * k + s2];
+                parent[r] = rec_of_node[k];
+                if (!cnt) {
+                    rec_of_node[ref] = r;
+                } else {
+                    leaves.push_back(r);
+                    for (uint32_t t = ref; t < ref + cnt; ++t) leaf_of_tri[t] = r;
+                }
+            }
+        if (!N) {
+            leaves.push_back(1u);
+            for (uint32_t t = 0; t < T; ++t) leaf_of_tri[t] = 1u;
         }
+        topo.insert(topo.end(), leaves.begin(), leaves.end());
+        slot.n_leaves = uint32_t(leaves.size());
+        CG_CUDA(cudaMalloc(&slot.topo, sizeof(uint32_t) * topo.size()), "alloc refit topology");
+        CG_CUDA(cudaMemcpyAsync(slot.topo, topo.data(), sizeof(uint32_t) * topo.size(), cudaMemcpyHostToDevice,
+                                c->stream),
+                "upload refit topology");
         CG_CUDA(cudaStreamSynchronize(c->stream), "upload record ranges");
     }
     slot.n_tri_used = T;
@@ -945,7 +960,7 @@ int cg_tree_free(cg_ctx* c, uint32_t id) {
     c->tris.release(s.tri_base, s.n_tris);
     cudaFree(s.nrm);
     cudaFree(s.ranges);
-    cudaFree(s.big);
+    cudaFree(s.topo);
     s = cg_ctx::Slot{};
     return sync_tree_table(c);
 }
@@ -1225,7 +1240,7 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
     if (!c || (n && (!tree_ids || !positions || !n_positions))) return CG_ERR_INVALID_ARGUMENT;
     if (n == 0) return CG_OK;
     std::vector<RefitTree> table(n);
-    uint32_t max_tris = 0, max_recs = 0, total_recs = 0, max_block = 0, max_warp = 0;
+    uint32_t max_tris = 0, max_recs = 0, total_recs = 0, max_leaves = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t id = tree_ids[i];
         if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
@@ -1234,9 +1249,8 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
         const auto& t = c->trees[id];
         table[i] = RefitTree{uint32_t(t.rec_base), uint32_t(t.n_recs), uint32_t(t.tri_base), t.n_tri_used, t.ranges,
                              reinterpret_cast<const float4*>(positions[i]), n_positions[i], total_recs,
-                             t.big, t.n_big, t.n_block};
-        max_block = std::max(max_block, t.n_block);
-        max_warp = std::max(max_warp, t.n_big - t.n_block);
+                             t.topo, t.topo + t.n_recs, t.topo + t.n_recs + t.n_tri_used, t.n_leaves, 0u};
+        max_leaves = std::max(max_leaves, t.n_leaves);
         total_recs += uint32_t(t.n_recs);
         max_tris = std::max(max_tris, t.n_tri_used);
         max_recs = std::max(max_recs, uint32_t(t.n_recs));
@@ -1253,9 +1267,10 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
         c->refit_scratch_cap = 0;
         CG_CUDA(cudaMalloc(&c->refit_scratch, sizeof(RefitScratch) * total_recs), "alloc refit scratch");
         c->refit_scratch_cap = total_recs;
+        CG_CUDA(init_refit_scratch(c->refit_scratch, total_recs, s), "clear refit scratch");
     }
     CG_CUDA(launch_refit(c->recs.ptr, c->tris.ptr, static_cast<const RefitTree*>(d_table), n, max_tris, max_recs,
-                         max_block, max_warp, c->refit_scratch, s),
+                         max_leaves, c->refit_scratch, s),
             "refit kernels");
     return CG_OK;
 }

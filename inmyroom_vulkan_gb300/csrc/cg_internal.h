@@ -226,22 +226,28 @@ struct RefitTree {
     const uint2* ranges;
     const float4* positions;
     uint32_t n_positions, scratch_base;
-    const uint32_t* big;      // records with more than kSmallPoints points, largest first
-    uint32_t n_big, n_block;  // list length; the first n_block have more than kBlockPoints
+    const uint32_t* parent;       // per record: the record of its parent box, or ~0 (root, unused)
+    const uint32_t* leaf_of_tri;  // per triangle: the record of its leaf box
+    const uint32_t* leaves;       // the leaf records
+    uint32_t n_leaves, pad;
 };
-constexpr uint32_t kSmallPoints = 48;    // refit: boxes up to this many points take one thread
-constexpr uint32_t kBlockPoints = 1536;  // refit: boxes above this many points take a block
 enum : uint32_t { kRefitSkip = 0, kRefitEmpty = 1, kRefitPoint = 2, kRefitBox = 3 };
+constexpr int kExtLo = 0x7f800000;           // order key of +inf
+constexpr int kExtHi = int(0x807fffffu);     // order key of -inf
 struct RefitScratch {
-    float cov[6];   // xx, yy, zz, xy, xz, yz
-    float axes[9];  // rows: the box axes
-    float p0[3];    // the point of a point box
-    float maxabs;   // largest |x| + |y| + |z| of the points
+    uint32_t n;       // points
     uint32_t kind;
+    float mean[3];
+    float m2[6];      // centred second moments: xx, yy, zz, xy, xz, yz
+    float p0[3];      // first point (the point of a point box)
+    float maxabs;     // largest |x| + |y| + |z| of the points
+    float axes[9];    // rows: the box axes
+    int ext[6];       // order keys of the min (x3) and max (x3) projections; kExtLo / kExtHi between refits
+    uint32_t arrive;  // children that finished their moments; 0 between refits
 };
+cudaError_t init_refit_scratch(RefitScratch* scratch, uint32_t n, cudaStream_t s);
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, uint32_t max_block, uint32_t max_warp, RefitScratch* scratch,
-                         cudaStream_t s);
+                         uint32_t max_recs, uint32_t max_leaves, RefitScratch* scratch, cudaStream_t s);
 
 // Axis-angle posing of a skeleton and its adjoint (cg_energy.cu): bone j's
 // world matrix is G_parent(j) * T(offset_j) * R(axis_angle_j).

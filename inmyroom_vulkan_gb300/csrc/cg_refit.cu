@@ -8,19 +8,26 @@
 //
 // The reference builds trees on the CPU and has no refit; this one is shaped
 // for a part whose FP64 pipe is narrow (a sequential FP64 fit of a
-// 12k-triangle tube's root takes tens of milliseconds here):
-//   refit_moments  compensated FP32 sums of the points and of their centred
-//                  products: a thread per box of up to kSmallPoints points, a
-//                  warp per larger box, a block per box of more than
-//                  kBlockPoints (lane sums combined with error-free FP32
-//                  sums); the larger boxes come from a per-tree list made at
-//                  upload, largest first
-//   refit_axes     a thread per box: the eig3 procedure in FP32
-//   refit_box      FP32 projections (thread, warp or block per box as above); the box
-//                  is padded by 2 FLT_EPSILON plus a bound on the FP32
-//                  rounding of the projections, the axes' departure from
-//                  orthonormal and the box's assembly, so it contains every
-//                  point of its subtree
+// 12k-triangle tube's root takes tens of milliseconds here) and so that no
+// box reads its subtree's points itself (a root box would read them all):
+//   refit_tris     the triangles' corners from the new vertex positions
+//   refit_climb    a thread per leaf box: count, mean and centred second
+//                  moments of its points in FP32; then up the tree, the
+//                  second child to arrive at a parent (an arrival counter per
+//                  record, no waiting) merges the two children's moments
+//                  (Chan, Golub and LeVeque's pairwise update: mean += d nb/n,
+//                  M2 = M2a + M2b + d d^T na nb / n)
+//   refit_axes     a thread per box: the eig3 procedure in FP32 on M2 / n
+//   refit_extent   a thread per point: up its chain of boxes, the projection
+//                  on each box's axes; lanes of a warp on the same box take
+//                  a segmented min/max by shuffles, one lane per box and
+//                  warp adds it with an integer atomic min/max on the float's
+//                  order-preserving key
+//   refit_assemble a thread per box: the box from its axes and extents (and
+//                  resets the extents for the next refit). The box is padded
+//                  by 2 FLT_EPSILON plus a bound on the FP32 rounding of the
+//                  projections, the axes' departure from orthonormal and the
+//                  box's assembly, so it contains every point of its subtree
 // The boxes are conservative like the reference's but not its bits; the
 // colliding triangle pairs found with them are the same.
 #include <cuda_runtime.h>
@@ -35,7 +42,7 @@ namespace cg {
 namespace {
 
 constexpr unsigned kAll = 0xffffffffu;
-constexpr int kRefitWarps = 4;           // warps per block of the warp-per-box kernels
+constexpr uint32_t kNoRec = 0xffffffffu;
 
 template <typename R>
 __device__ __forceinline__ R hyp(R x, R y) {
@@ -199,47 +206,6 @@ __device__ void ql_sort(R v[3][3], R d[3], R e[3], R eps) {
     }
 }
 
-// Compensated running sum (Kahan): s - c carries the sum of the added values.
-struct KSum {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        const float y = x - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-};
-
-// Error-free sum of two floats (Knuth's two-sum): a + b = hi + lo exactly.
-__device__ __forceinline__ void two_sum(float a, float b, float& hi, float& lo) {
-    hi = a + b;
-    const float bb = hi - a;
-    lo = (a - (hi - bb)) + (b - bb);
-}
-
-// Sum over the warp of the lanes' (hi, lo) pairs, kept as a float pair.
-__device__ __forceinline__ void warp_sum2(float& hi, float& lo) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float oh = __shfl_xor_sync(kAll, hi, o), ol = __shfl_xor_sync(kAll, lo, o);
-        float h, l;
-        two_sum(hi, oh, h, l);
-        hi = h;
-        lo = (lo + ol) + l;
-    }
-}
-
-__device__ __forceinline__ float warp_maxf(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kAll, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_minf(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kAll, v, o));
-    return v;
-}
-
 // New corner positions: p_k = positions[vertex index k] for every triangle.
 __global__ void refit_tris_kernel(float4* tris, const RefitTree* trees) {
     const RefitTree T = trees[blockIdx.y];
@@ -254,214 +220,201 @@ __global__ void refit_tris_kernel(float4* tris, const RefitTree* trees) {
     q->z = p.z;
 }
 
-// The moments of one box's points, by one lane (lanes = 1) or a whole warp.
-struct Moments {
-    KSum s[3];    // x, y, z
-    KSum c[6];    // xx, yy, zz, xy, xz, yz of the centred points
-    float mabs = 0.f;
-    bool differ = false;
+// Count, mean, centred second moments (xx, yy, zz, xy, xz, yz), first point,
+// largest |x| + |y| + |z| and kind of a box's points.
+struct Mom {
+    uint32_t n;
+    uint32_t kind;
+    float mean[3];
+    float m2[6];
+    float p0[3];
+    float mabs;
 };
 
-__device__ __forceinline__ void record_out(RefitScratch& out, float4 p0, bool differ, float mabs, const float* cov) {
-    if (!differ) {
-        out.kind = kRefitPoint;
-        out.p0[0] = p0.x;
-        out.p0[1] = p0.y;
-        out.p0[2] = p0.z;
-        return;
-    }
-    out.kind = kRefitBox;
-    out.maxabs = mabs;
-    for (int i = 0; i < 6; ++i) out.cov[i] = cov[i];
+__device__ __forceinline__ void store_mom(RefitScratch& s, const Mom& m) {
+    s.n = m.n;
+    s.kind = m.kind;
+    for (int i = 0; i < 3; ++i) s.mean[i] = m.mean[i], s.p0[i] = m.p0[i];
+    for (int i = 0; i < 6; ++i) s.m2[i] = m.m2[i];
+    s.maxabs = m.mabs;
 }
 
-// Thread per small box: the count, whether two points differ, the largest
-// |x| + |y| + |z| and the covariance.
-__global__ void refit_moments_small_kernel(const float4* tris, const RefitTree* trees, RefitScratch* scratch) {
-    const RefitTree T = trees[blockIdx.y];
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= T.n_recs) return;
-    const uint2 rg = T.ranges[r];
-    RefitScratch& out = scratch[T.scratch_base + r];
-    if (rg.y == ~0u || rg.y == 0u) {
-        out.kind = rg.y == ~0u ? kRefitSkip : kRefitEmpty;
-        return;
+// Read through L2: another SM wrote these fields in this launch.
+__device__ __forceinline__ Mom load_mom(const RefitScratch& s) {
+    Mom m;
+    m.n = __ldcg(&s.n);
+    m.kind = __ldcg(&s.kind);
+    for (int i = 0; i < 3; ++i) m.mean[i] = __ldcg(&s.mean[i]), m.p0[i] = __ldcg(&s.p0[i]);
+    for (int i = 0; i < 6; ++i) m.m2[i] = __ldcg(&s.m2[i]);
+    m.mabs = __ldcg(&s.maxabs);
+    return m;
+}
+
+// The moments of a leaf's points, two passes over them.
+__device__ Mom leaf_mom(const float4* pt, uint32_t n_pts) {
+    Mom m{};
+    m.n = n_pts;
+    if (n_pts == 0) {
+        m.kind = kRefitEmpty;
+        return m;
     }
-    const uint32_t n_pts = 3u * rg.y;
-    if (n_pts > kSmallPoints) return;  // a warp or block kernel's
-    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
     const float4 p0 = pt[0];
-    KSum sx, sy, sz;
-    float mabs = 0.f;
+    m.p0[0] = p0.x, m.p0[1] = p0.y, m.p0[2] = p0.z;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
     bool differ = false;
     for (uint32_t k = 0; k < n_pts; ++k) {
         const float4 p = pt[k];
-        sx.add(p.x);
-        sy.add(p.y);
-        sz.add(p.z);
-        mabs = fmaxf(mabs, (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z));
+        sx = sx + p.x;
+        sy = sy + p.y;
+        sz = sz + p.z;
+        m.mabs = fmaxf(m.mabs, (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z));
         differ |= p.x != p0.x || p.y != p0.y || p.z != p0.z;
     }
     const float fn = float(n_pts);
-    const float mx = (sx.s - sx.c) / fn, my = (sy.s - sy.c) / fn, mz = (sz.s - sz.c) / fn;
-    KSum c[6];
+    m.mean[0] = sx / fn, m.mean[1] = sy / fn, m.mean[2] = sz / fn;
     for (uint32_t k = 0; k < n_pts && differ; ++k) {
         const float4 p = pt[k];
-        const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
-        c[0].add(dx * dx);
-        c[1].add(dy * dy);
-        c[2].add(dz * dz);
-        c[3].add(dx * dy);
-        c[4].add(dx * dz);
-        c[5].add(dy * dz);
+        const float dx = p.x - m.mean[0], dy = p.y - m.mean[1], dz = p.z - m.mean[2];
+        m.m2[0] = m.m2[0] + dx * dx;
+        m.m2[1] = m.m2[1] + dy * dy;
+        m.m2[2] = m.m2[2] + dz * dz;
+        m.m2[3] = m.m2[3] + dx * dy;
+        m.m2[4] = m.m2[4] + dx * dz;
+        m.m2[5] = m.m2[5] + dy * dz;
     }
-    float cov[6];
-    for (int i = 0; i < 6; ++i) cov[i] = (c[i].s - c[i].c) / fn;
-    record_out(out, p0, differ, mabs, cov);
+    m.kind = differ ? kRefitBox : kRefitPoint;
+    return m;
 }
 
-// Reductions over the points of one box by a warp (G = 32) or a whole block
-// (G = 256, `red` = 18 floats of shared memory); the result is the same on
-// every thread of the group.
-template <int G>
-struct Group;
-template <>
-struct Group<32> {
-    __device__ static void sum2(float& h, float& l, float*) { warp_sum2(h, l); }
-    __device__ static float maxf(float v, float*) { return warp_maxf(v); }
-    __device__ static float minf(float v, float*) { return warp_minf(v); }
-    __device__ static bool any(bool b, float*) { return __any_sync(kAll, b); }
-};
-template <>
-struct Group<256> {
-    __device__ static void sum2(float& h, float& l, float* red) {
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        warp_sum2(h, l);
-        if (lane == 0) red[2 * w] = h, red[2 * w + 1] = l;
-        __syncthreads();
-        if (w == 0) {
-            float hh = lane < 8 ? red[2 * lane] : 0.f, ll = lane < 8 ? red[2 * lane + 1] : 0.f;
-            warp_sum2(hh, ll);
-            if (lane == 0) red[16] = hh, red[17] = ll;
-        }
-        __syncthreads();
-        h = red[16];
-        l = red[17];
-        __syncthreads();
-    }
-    template <bool kMax>
-    __device__ static float ext(float v, float* red) {
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        v = kMax ? warp_maxf(v) : warp_minf(v);
-        if (lane == 0) red[w] = v;
-        __syncthreads();
-        if (w == 0) {
-            float x = lane < 8 ? red[lane] : red[0];
-            x = kMax ? warp_maxf(x) : warp_minf(x);
-            if (lane == 0) red[16] = x;
-        }
-        __syncthreads();
-        v = red[16];
-        __syncthreads();
-        return v;
-    }
-    __device__ static float maxf(float v, float* red) { return ext<true>(v, red); }
-    __device__ static float minf(float v, float* red) { return ext<false>(v, red); }
-    __device__ static bool any(bool b, float*) { return __syncthreads_or(b) != 0; }
-};
-
-// The moments of a large box's points by a group of G threads (thread t),
-// lane sums combined with error-free sums.
-template <int G>
-__device__ __forceinline__ void group_moments(const float4* pt, uint32_t n_pts, uint32_t t, RefitScratch& out,
-                                              float* red) {
-    const float4 p0 = pt[0];
-    KSum sx, sy, sz;
-    float mabs = 0.f;
-    bool differ = false;
-#pragma unroll 4
-    for (uint32_t k = t; k < n_pts; k += G) {
-        const float4 p = pt[k];
-        sx.add(p.x);
-        sy.add(p.y);
-        sz.add(p.z);
-        mabs = fmaxf(mabs, (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z));
-        differ |= p.x != p0.x || p.y != p0.y || p.z != p0.z;
-    }
-    differ = Group<G>::any(differ, red);
-    mabs = Group<G>::maxf(mabs, red);
-    if (!differ) {
-        if (t == 0) record_out(out, p0, false, mabs, nullptr);
-        return;
-    }
-    float hx = sx.s, lx = -sx.c, hy = sy.s, ly = -sy.c, hz = sz.s, lz = -sz.c;
-    Group<G>::sum2(hx, lx, red);
-    Group<G>::sum2(hy, ly, red);
-    Group<G>::sum2(hz, lz, red);
-    const float fn = float(n_pts);
-    const float mx = (hx + lx) / fn, my = (hy + ly) / fn, mz = (hz + lz) / fn;
-    KSum c[6];
-#pragma unroll 4
-    for (uint32_t k = t; k < n_pts; k += G) {
-        const float4 p = pt[k];
-        const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
-        c[0].add(dx * dx);
-        c[1].add(dy * dy);
-        c[2].add(dz * dz);
-        c[3].add(dx * dy);
-        c[4].add(dx * dz);
-        c[5].add(dy * dz);
-    }
-    float cov[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        float h = c[i].s, l = -c[i].c;
-        Group<G>::sum2(h, l, red);
-        cov[i] = (h + l) / fn;
-    }
-    if (t == 0) record_out(out, p0, true, mabs, cov);
+// The moments of the union of two disjoint point sets (a first in leaf
+// order).
+__device__ Mom merge_mom(const Mom& a, const Mom& b) {
+    if (b.n == 0) return a;
+    if (a.n == 0) return b;
+    Mom m;
+    m.n = a.n + b.n;
+    const float fa = float(a.n), fb = float(b.n), fn = float(m.n);
+    const float d[3] = {b.mean[0] - a.mean[0], b.mean[1] - a.mean[1], b.mean[2] - a.mean[2]};
+    const float f = fb / fn, w = (fa * fb) / fn;
+    for (int i = 0; i < 3; ++i) m.mean[i] = a.mean[i] + d[i] * f, m.p0[i] = a.p0[i];
+    const int r[6] = {0, 1, 2, 0, 0, 1}, c[6] = {0, 1, 2, 1, 2, 2};
+    for (int i = 0; i < 6; ++i) m.m2[i] = (a.m2[i] + b.m2[i]) + (d[r[i]] * d[c[i]]) * w;
+    m.mabs = fmaxf(a.mabs, b.mabs);
+    const bool same = a.kind == kRefitPoint && b.kind == kRefitPoint && a.p0[0] == b.p0[0] && a.p0[1] == b.p0[1] &&
+                      a.p0[2] == b.p0[2];
+    m.kind = same ? kRefitPoint : kRefitBox;
+    return m;
 }
 
-// Large boxes come from the tree's list of records with more than
-// kSmallPoints points, largest first: the first n_block (more than
-// kBlockPoints points) take a block each, the rest a warp each.
-__global__ void __launch_bounds__(256) refit_moments_block_kernel(const float4* tris, const RefitTree* trees,
-                                                                  RefitScratch* scratch) {
-    __shared__ float red[32];
+// A thread per leaf box; the second child to arrive at a parent merges and
+// climbs on. The arrival counter is reset by the thread that merges.
+__global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, const float4* tris,
+                                                          const RefitTree* trees, RefitScratch* scratch) {
     const RefitTree T = trees[blockIdx.y];
-    if (blockIdx.x >= T.n_block) return;
-    const uint32_t r = T.big[blockIdx.x];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T.n_leaves) return;
+    RefitScratch* S = scratch + T.scratch_base;
+    uint32_t r = T.leaves[i];
     const uint2 rg = T.ranges[r];
-    group_moments<256>(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x, scratch[T.scratch_base + r], red);
+    Mom m = leaf_mom(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y);
+    store_mom(S[r], m);
+    for (;;) {
+        const uint32_t p = T.parent[r];
+        if (p == kNoRec) break;
+        __threadfence();  // this box's moments before the arrival
+        if (atomicAdd(&S[p].arrive, 1u) == 0u) break;  // the sibling merges
+        S[p].arrive = 0u;
+        __threadfence();  // the sibling's moments after its arrival
+        const uint32_t c0 = __float_as_uint(__ldg(&recs[4ull * (T.rec_base + p) + 3].x)) - T.rec_base;
+        const Mom a = c0 == r ? m : load_mom(S[c0]);
+        const Mom b = c0 + 1u == r ? m : load_mom(S[c0 + 1u]);
+        m = merge_mom(a, b);
+        store_mom(S[p], m);
+        r = p;
+    }
 }
 
-__global__ void __launch_bounds__(32 * kRefitWarps) refit_moments_kernel(const float4* tris, const RefitTree* trees,
-                                                                          RefitScratch* scratch) {
-    const RefitTree T = trees[blockIdx.y];
-    const uint32_t i = T.n_block + blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
-    if (i >= T.n_big) return;  // whole warps
-    const uint32_t r = T.big[i];
-    const uint2 rg = T.ranges[r];
-    group_moments<32>(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x & 31u, scratch[T.scratch_base + r],
-                      nullptr);
-}
-
-// One thread per record: the eigensystem of the covariance by the eig3
-// procedure in FP32 (the covariance carries FP32 accuracy); the box axes are
-// the rows of the eigenvector matrix, as the reference takes them.
+// One thread per record: the eigensystem of M2 / n by the eig3 procedure in
+// FP32; the box axes are the rows of the eigenvector matrix, as the reference
+// takes them.
 __global__ void refit_axes_kernel(const RefitTree* trees, RefitScratch* scratch) {
     const RefitTree T = trees[blockIdx.y];
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= T.n_recs) return;
     RefitScratch& sc = scratch[T.scratch_base + r];
-    if (sc.kind != kRefitBox) return;
-    const float* c = sc.cov;  // xx, yy, zz, xy, xz, yz
+    if (T.ranges[r].y == ~0u || sc.kind != kRefitBox) return;
+    const float fn = float(sc.n);
+    float c[6];
+    for (int i = 0; i < 6; ++i) c[i] = sc.m2[i] / fn;  // xx, yy, zz, xy, xz, yz
     float v[3][3] = {{c[0], c[3], c[4]}, {c[3], c[1], c[5]}, {c[4], c[5], c[2]}};
     float d[3], e[3];
     tridiagonalize(v, d, e);
     ql_sort(v, d, e, FLT_EPSILON);
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) sc.axes[3 * i + j] = v[i][j];
+}
+
+// Order-preserving int key of a float (and its inverse): integer min/max of
+// keys is float min/max.
+__device__ __forceinline__ int fkey(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float unkey(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+
+// A thread per point: its projections on the axes of every box above it.
+__global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, const RefitTree* trees,
+                                                           RefitScratch* scratch) {
+    const RefitTree T = trees[blockIdx.y];
+    if (blockIdx.x * blockDim.x >= 3u * T.n_tris) return;  // whole block
+    RefitScratch* S = scratch + T.scratch_base;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool live = k < 3u * T.n_tris;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t r = kNoRec;
+    if (live) {
+        p = tris[3ull * T.tri_base + k];
+        r = T.leaf_of_tri[k / 3u];
+    }
+    const float inf = __int_as_float(0x7f800000);
+    while (__any_sync(kAll, r != kNoRec)) {
+        float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+        bool box = false;
+        if (r != kNoRec) {
+            const RefitScratch& sc = S[r];
+            box = sc.kind == kRefitBox;
+            if (box) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float pr = (sc.axes[3 * a] * p.x + sc.axes[3 * a + 1] * p.y) + sc.axes[3 * a + 2] * p.z;
+                    lo[a] = hi[a] = pr;
+                }
+            }
+        }
+        // segmented min/max over the lanes at the same box (suffix form: the
+        // first lane of each run holds its run's result)
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ro = __shfl_down_sync(kAll, r, o);
+            const bool take = lane + o < 32 && ro == r;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float l2 = __shfl_down_sync(kAll, lo[a], o), h2 = __shfl_down_sync(kAll, hi[a], o);
+                if (take) lo[a] = fminf(lo[a], l2), hi[a] = fmaxf(hi[a], h2);
+            }
+        }
+        const uint32_t rp = __shfl_up_sync(kAll, r, 1);
+        if (box && (lane == 0 || rp != r)) {
+            RefitScratch& sc = S[r];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                atomicMin(&sc.ext[a], fkey(lo[a]));
+                atomicMax(&sc.ext[3 + a], fkey(hi[a]));
+            }
+        }
+        if (r != kNoRec) r = T.parent[r];
+    }
 }
 
 // The box from its axes and the projections' min and max per axis. The pad
@@ -504,108 +457,52 @@ __device__ __forceinline__ void write_box(float4* recs, uint32_t rec, const Box&
     out[3] = make_float4(q3.x, q3.y, surface(b), q3.w);
 }
 
-// Thread per small box (and every empty or point box).
-__global__ void refit_box_small_kernel(float4* recs, const float4* tris, const RefitTree* trees,
-                                       const RefitScratch* scratch) {
+__global__ void refit_assemble_kernel(float4* recs, const RefitTree* trees, RefitScratch* scratch) {
     const RefitTree T = trees[blockIdx.y];
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= T.n_recs) return;
-    const RefitScratch& sc = scratch[T.scratch_base + r];
-    if (sc.kind == kRefitSkip) return;
-    const uint2 rg = T.ranges[r];
-    const uint32_t n_pts = 3u * rg.y;
+    if (r >= T.n_recs || T.ranges[r].y == ~0u) return;
+    RefitScratch& sc = scratch[T.scratch_base + r];
     if (sc.kind != kRefitBox) {
         write_box(recs, T.rec_base + r, special_box(sc));
         return;
     }
-    if (n_pts > kSmallPoints) return;  // a warp or block kernel's
-    const float4* pt = tris + 3ull * (T.tri_base + rg.x);
-    float ax[9];
+    float ax[9], lo[3], hi[3];
     for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
-    const float inf = __int_as_float(0x7f800000);
-    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-    for (uint32_t k = 0; k < n_pts; ++k) {
-        const float4 p = pt[k];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float pr = (ax[3 * a] * p.x + ax[3 * a + 1] * p.y) + ax[3 * a + 2] * p.z;
-            lo[a] = fminf(lo[a], pr);
-            hi[a] = fmaxf(hi[a], pr);
-        }
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = unkey(sc.ext[a]);
+        hi[a] = unkey(sc.ext[3 + a]);
+        sc.ext[a] = kExtLo;
+        sc.ext[3 + a] = kExtHi;
     }
     write_box(recs, T.rec_base + r, assemble(ax, lo, hi, sc.maxabs));
 }
 
-// Extent of a large box's points on its axes by a group of G threads.
-template <int G>
-__device__ __forceinline__ void group_box(float4* recs, uint32_t rec, const float4* pt, uint32_t n_pts, uint32_t t,
-                                          const RefitScratch& sc, float* red) {
-    float ax[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
-    const float inf = __int_as_float(0x7f800000);
-    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-#pragma unroll 4
-    for (uint32_t k = t; k < n_pts; k += G) {
-        const float4 p = pt[k];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float pr = (ax[3 * a] * p.x + ax[3 * a + 1] * p.y) + ax[3 * a + 2] * p.z;
-            lo[a] = fminf(lo[a], pr);
-            hi[a] = fmaxf(hi[a], pr);
-        }
+__global__ void refit_scratch_init_kernel(RefitScratch* scratch, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        RefitScratch& s = scratch[i];
+        s.arrive = 0u;
+        for (int a = 0; a < 3; ++a) s.ext[a] = kExtLo, s.ext[3 + a] = kExtHi;
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        lo[a] = Group<G>::minf(lo[a], red);
-        hi[a] = Group<G>::maxf(hi[a], red);
-    }
-    if (t == 0) write_box(recs, rec, assemble(ax, lo, hi, sc.maxabs));
-}
-
-__global__ void __launch_bounds__(256) refit_box_block_kernel(float4* recs, const float4* tris, const RefitTree* trees,
-                                                              const RefitScratch* scratch) {
-    __shared__ float red[32];
-    const RefitTree T = trees[blockIdx.y];
-    if (blockIdx.x >= T.n_block) return;
-    const uint32_t r = T.big[blockIdx.x];
-    const RefitScratch& sc = scratch[T.scratch_base + r];
-    if (sc.kind != kRefitBox) return;  // written by the small kernel (whole block)
-    const uint2 rg = T.ranges[r];
-    group_box<256>(recs, T.rec_base + r, tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x, sc, red);
-}
-
-__global__ void __launch_bounds__(32 * kRefitWarps) refit_box_kernel(float4* recs, const float4* tris,
-                                                                      const RefitTree* trees,
-                                                                      const RefitScratch* scratch) {
-    const RefitTree T = trees[blockIdx.y];
-    const uint32_t i = T.n_block + blockIdx.x * kRefitWarps + uint32_t(threadIdx.x >> 5);
-    if (i >= T.n_big) return;  // whole warps
-    const uint32_t r = T.big[i];
-    const RefitScratch& sc = scratch[T.scratch_base + r];
-    if (sc.kind != kRefitBox) return;  // written by the small kernel
-    const uint2 rg = T.ranges[r];
-    group_box<32>(recs, T.rec_base + r, tris + 3ull * (T.tri_base + rg.x), 3u * rg.y, threadIdx.x & 31u, sc,
-                  nullptr);
 }
 
 }  // namespace
 
+cudaError_t init_refit_scratch(RefitScratch* scratch, uint32_t n, cudaStream_t s) {
+    if (n) refit_scratch_init_kernel<<<(n + 255u) / 256u < 4096u ? (n + 255u) / 256u : 4096u, 256, 0, s>>>(scratch, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, uint32_t max_block, uint32_t max_warp, RefitScratch* scratch,
-                         cudaStream_t s) {
+                         uint32_t max_recs, uint32_t max_leaves, RefitScratch* scratch, cudaStream_t s) {
     if (n_trees == 0) return cudaSuccess;
     if (max_tris) refit_tris_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees);
-    const dim3 threads((max_recs + 127u) / 128u, n_trees);
-    const dim3 blocks(max_block, n_trees);
-    const dim3 warps((max_warp + kRefitWarps - 1) / kRefitWarps, n_trees);
-    refit_moments_small_kernel<<<threads, 128, 0, s>>>(tris, d_trees, scratch);
-    if (max_block) refit_moments_block_kernel<<<blocks, 256, 0, s>>>(tris, d_trees, scratch);
-    if (max_warp) refit_moments_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(tris, d_trees, scratch);
-    refit_axes_kernel<<<threads, 128, 0, s>>>(d_trees, scratch);
-    refit_box_small_kernel<<<threads, 128, 0, s>>>(recs, tris, d_trees, scratch);
-    if (max_block) refit_box_block_kernel<<<blocks, 256, 0, s>>>(recs, tris, d_trees, scratch);
-    if (max_warp) refit_box_kernel<<<warps, 32 * kRefitWarps, 0, s>>>(recs, tris, d_trees, scratch);
+    if (max_leaves)
+        refit_climb_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(recs, tris, d_trees, scratch);
+    const dim3 per_rec((max_recs + 127u) / 128u, n_trees);
+    refit_axes_kernel<<<per_rec, 128, 0, s>>>(d_trees, scratch);
+    if (max_tris)
+        refit_extent_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees, scratch);
+    refit_assemble_kernel<<<per_rec, 128, 0, s>>>(recs, d_trees, scratch);
     return cudaGetLastError();
 }
 
