@@ -644,6 +644,23 @@ def run_gpu(args) -> dict:
     return out if rank == 0 else None
 
 
+def run_only(args) -> dict:
+    """One secondary workload alone (for profiling it): its JSON object."""
+    import torch
+
+    from inmyroom_vulkan_gb300 import capi
+
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    factory = lambda: capi.Context(max_queries=4096, max_tri_pairs=1 << 22)  # noqa: E731
+    if args.only == "deforming":
+        return run_deforming(args, factory, flush, stream, 0.0)
+    if args.only == "differentiable":
+        return run_differentiable(args, factory, flush, stream, 0.0)
+    return run_sweep(args, 0, flush, stream, 0.0)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -654,11 +671,16 @@ def main():
     ap.add_argument("--skip-deforming", action="store_true", help="leave out the deforming and differentiable lines")
     ap.add_argument("--skip-sweep", action="store_true", help="leave out the autotuned batch-sweep line")
     ap.add_argument("--no-tune", action="store_true", help="time the scene step with the default launch settings")
+    ap.add_argument("--only", choices=["deforming", "differentiable", "sweep"],
+                    help="run one secondary workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
         print(json.dumps(run_reference(args)))
+        return
+    if args.only:
+        print(json.dumps(run_only(args)))
         return
     res = run_gpu(args)
     if res is not None:
