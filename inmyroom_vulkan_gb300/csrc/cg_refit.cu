@@ -19,10 +19,10 @@
 //                  M2 = M2a + M2b + d d^T na nb / n)
 //   refit_axes     a thread per box: the eig3 procedure in FP32 on M2 / n
 //   refit_extent   a thread per point: up its chain of boxes, the projection
-//                  on each box's axes; lanes of a warp on the same box take
-//                  a segmented min/max by shuffles, one lane per box and
-//                  warp adds it with an integer atomic min/max on the float's
-//                  order-preserving key
+//                  on each box's axes as the float's order-preserving integer
+//                  key; lanes of a warp at the same box reduce their keys with
+//                  one warp min/max each, and one lane per box and warp adds
+//                  the result with an integer atomic min/max
 //   refit_assemble a thread per box: the box from its axes and extents (and
 //                  resets the extents for the next refit). The box is padded
 //                  by 2 FLT_EPSILON plus a bound on the FP32 rounding of the
@@ -250,8 +250,49 @@ __device__ __forceinline__ Mom load_mom(const RefitScratch& s) {
     return m;
 }
 
-// The moments of a leaf's points, two passes over them.
+// The moments of a leaf's points, two passes over them (held in registers
+// for the usual leaf of up to 4 triangles).
+constexpr uint32_t kLeafRegPoints = 12;
+
 __device__ Mom leaf_mom(const float4* pt, uint32_t n_pts) {
+    if (n_pts > 0 && n_pts <= kLeafRegPoints) {
+        float4 q[kLeafRegPoints];
+        q[0] = pt[0];
+#pragma unroll
+        for (uint32_t k = 1; k < kLeafRegPoints; ++k) {
+            q[k] = q[0];
+            if (k < n_pts) q[k] = pt[k];
+        }
+        Mom m{};
+        m.n = n_pts;
+        m.p0[0] = q[0].x, m.p0[1] = q[0].y, m.p0[2] = q[0].z;
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        bool differ = false;
+#pragma unroll
+        for (uint32_t k = 0; k < kLeafRegPoints; ++k)
+            if (k < n_pts) {
+                sx = sx + q[k].x;
+                sy = sy + q[k].y;
+                sz = sz + q[k].z;
+                m.mabs = fmaxf(m.mabs, (fabsf(q[k].x) + fabsf(q[k].y)) + fabsf(q[k].z));
+                differ |= q[k].x != q[0].x || q[k].y != q[0].y || q[k].z != q[0].z;
+            }
+        const float fn = float(n_pts);
+        m.mean[0] = sx / fn, m.mean[1] = sy / fn, m.mean[2] = sz / fn;
+#pragma unroll
+        for (uint32_t k = 0; k < kLeafRegPoints; ++k)
+            if (k < n_pts && differ) {
+                const float dx = q[k].x - m.mean[0], dy = q[k].y - m.mean[1], dz = q[k].z - m.mean[2];
+                m.m2[0] = m.m2[0] + dx * dx;
+                m.m2[1] = m.m2[1] + dy * dy;
+                m.m2[2] = m.m2[2] + dz * dz;
+                m.m2[3] = m.m2[3] + dx * dy;
+                m.m2[4] = m.m2[4] + dx * dz;
+                m.m2[5] = m.m2[5] + dy * dz;
+            }
+        m.kind = differ ? kRefitBox : kRefitPoint;
+        return m;
+    }
     Mom m{};
     m.n = n_pts;
     if (n_pts == 0) {
@@ -306,6 +347,12 @@ __device__ Mom merge_mom(const Mom& a, const Mom& b) {
     return m;
 }
 
+__device__ __forceinline__ unsigned arrive_acq_rel(unsigned* p) {
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
 // A thread per leaf box; the second child to arrive at a parent merges and
 // climbs on. The arrival counter is reset by the thread that merges.
 __global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, const float4* tris,
@@ -321,10 +368,9 @@ __global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, co
     for (;;) {
         const uint32_t p = T.parent[r];
         if (p == kNoRec) break;
-        __threadfence();  // this box's moments before the arrival
-        if (atomicAdd(&S[p].arrive, 1u) == 0u) break;  // the sibling merges
+        // the arrival releases this box's moments and acquires the sibling's
+        if (arrive_acq_rel(&S[p].arrive) == 0u) break;  // the sibling merges
         S[p].arrive = 0u;
-        __threadfence();  // the sibling's moments after its arrival
         const uint32_t c0 = __float_as_uint(__ldg(&recs[4ull * (T.rec_base + p) + 3].x)) - T.rec_base;
         const Mom a = c0 == r ? m : load_mom(S[c0]);
         const Mom b = c0 + 1u == r ? m : load_mom(S[c0 + 1u]);
@@ -377,40 +423,31 @@ __global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, c
         p = tris[3ull * T.tri_base + k];
         r = T.leaf_of_tri[k / 3u];
     }
-    const float inf = __int_as_float(0x7f800000);
     while (__any_sync(kAll, r != kNoRec)) {
-        float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+        int lo[3] = {kExtLo, kExtLo, kExtLo}, hi[3] = {kExtHi, kExtHi, kExtHi};
         bool box = false;
         if (r != kNoRec) {
             const RefitScratch& sc = S[r];
             box = sc.kind == kRefitBox;
             if (box) {
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float pr = (sc.axes[3 * a] * p.x + sc.axes[3 * a + 1] * p.y) + sc.axes[3 * a + 2] * p.z;
-                    lo[a] = hi[a] = pr;
-                }
+                for (int a = 0; a < 3; ++a)
+                    lo[a] = hi[a] = fkey((sc.axes[3 * a] * p.x + sc.axes[3 * a + 1] * p.y) + sc.axes[3 * a + 2] * p.z);
             }
         }
-        // segmented min/max over the lanes at the same box (suffix form: the
-        // first lane of each run holds its run's result)
+        // lanes at the same box reduce together; the lowest one adds the result
+        const unsigned grp = __match_any_sync(kAll, r);
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t ro = __shfl_down_sync(kAll, r, o);
-            const bool take = lane + o < 32 && ro == r;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const float l2 = __shfl_down_sync(kAll, lo[a], o), h2 = __shfl_down_sync(kAll, hi[a], o);
-                if (take) lo[a] = fminf(lo[a], l2), hi[a] = fmaxf(hi[a], h2);
-            }
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = __reduce_min_sync(grp, lo[a]);
+            hi[a] = __reduce_max_sync(grp, hi[a]);
         }
-        const uint32_t rp = __shfl_up_sync(kAll, r, 1);
-        if (box && (lane == 0 || rp != r)) {
+        if (box && lane == __ffs(grp) - 1) {
             RefitScratch& sc = S[r];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                atomicMin(&sc.ext[a], fkey(lo[a]));
-                atomicMax(&sc.ext[3 + a], fkey(hi[a]));
+                atomicMin(&sc.ext[a], lo[a]);
+                atomicMax(&sc.ext[3 + a], hi[a]);
             }
         }
         if (r != kNoRec) r = T.parent[r];
