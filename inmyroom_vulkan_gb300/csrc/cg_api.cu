@@ -189,7 +189,7 @@ struct cg_ctx {
         void* dev = nullptr;
         size_t cap = 0;
     } deform_table, refit_table, skeleton_table, energy_table;
-    RefitScratch* refit_scratch = nullptr;  // one entry per record of a refit batch
+    void* refit_scratch = nullptr;          // RefitBufs for this many records of a refit batch
     uint32_t refit_scratch_cap = 0;
     float* pose_scratch = nullptr;          // pose adjoint: dE/dG accumulated per bone
     uint64_t pose_scratch_cap = 0;
@@ -1265,12 +1265,12 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
         cudaFree(c->refit_scratch);
         c->refit_scratch = nullptr;
         c->refit_scratch_cap = 0;
-        CG_CUDA(cudaMalloc(&c->refit_scratch, sizeof(RefitScratch) * total_recs), "alloc refit scratch");
+        CG_CUDA(cudaMalloc(&c->refit_scratch, kRefitBytesPerRecord * total_recs), "alloc refit scratch");
         c->refit_scratch_cap = total_recs;
-        CG_CUDA(init_refit_scratch(c->refit_scratch, total_recs, s), "clear refit scratch");
+        CG_CUDA(init_refit_scratch(refit_bufs(c->refit_scratch, total_recs), total_recs, s), "clear refit scratch");
     }
     CG_CUDA(launch_refit(c->recs.ptr, c->tris.ptr, static_cast<const RefitTree*>(d_table), n, max_tris, max_recs,
-                         max_leaves, c->refit_scratch, s),
+                         max_leaves, refit_bufs(c->refit_scratch, c->refit_scratch_cap), s),
             "refit kernels");
     return CG_OK;
 }

@@ -234,20 +234,37 @@ struct RefitTree {
 enum : uint32_t { kRefitSkip = 0, kRefitEmpty = 1, kRefitPoint = 2, kRefitBox = 3 };
 constexpr int kExtLo = 0x7f800000;           // order key of +inf
 constexpr int kExtHi = int(0x807fffffu);     // order key of -inf
-struct RefitScratch {
-    uint32_t n;       // points
-    uint32_t kind;
+struct RefitMom {  // count, mean, centred second moments, first point, largest |x| + |y| + |z|: 64 bytes
+    uint32_t n, kind;
     float mean[3];
-    float m2[6];      // centred second moments: xx, yy, zz, xy, xz, yz
-    float p0[3];      // first point (the point of a point box)
-    float maxabs;     // largest |x| + |y| + |z| of the points
-    float axes[9];    // rows: the box axes
-    int ext[6];       // order keys of the min (x3) and max (x3) projections; kExtLo / kExtHi between refits
-    uint32_t arrive;  // children that finished their moments; 0 between refits
+    float m2[6];  // xx, yy, zz, xy, xz, yz
+    float p0[3];
+    float mabs;
 };
-cudaError_t init_refit_scratch(RefitScratch* scratch, uint32_t n, cudaStream_t s);
+// Refit scratch, one entry per record of a batch (tree i's from scratch_base),
+// in separate arrays so that each kernel reads only what it needs.
+struct RefitBufs {
+    RefitMom* mom;
+    float4* axes;       // [3] per record: axis rows (xyz); w of the first is 1 for a box
+    int4* ext;          // [2] per record: order keys of the min and max projections (xyz); kExtLo / kExtHi between refits
+    uint32_t* arrive;   // children that finished their moments; 0 between refits
+};
+constexpr size_t kRefitBytesPerRecord = sizeof(RefitMom) + 3 * sizeof(float4) + 2 * sizeof(int4) + sizeof(uint32_t);
+inline RefitBufs refit_bufs(void* base, uint32_t cap) {
+    char* p = static_cast<char*>(base);
+    RefitBufs b;
+    b.mom = reinterpret_cast<RefitMom*>(p);
+    p += sizeof(RefitMom) * size_t(cap);
+    b.axes = reinterpret_cast<float4*>(p);
+    p += 3 * sizeof(float4) * size_t(cap);
+    b.ext = reinterpret_cast<int4*>(p);
+    p += 2 * sizeof(int4) * size_t(cap);
+    b.arrive = reinterpret_cast<uint32_t*>(p);
+    return b;
+}
+cudaError_t init_refit_scratch(const RefitBufs& b, uint32_t n, cudaStream_t s);
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, uint32_t max_leaves, RefitScratch* scratch, cudaStream_t s);
+                         uint32_t max_recs, uint32_t max_leaves, const RefitBufs& scratch, cudaStream_t s);
 
 // Axis-angle posing of a skeleton and its adjoint (cg_energy.cu): bone j's
 // world matrix is G_parent(j) * T(offset_j) * R(axis_angle_j).

@@ -220,33 +220,16 @@ __global__ void refit_tris_kernel(float4* tris, const RefitTree* trees) {
     q->z = p.z;
 }
 
-// Count, mean, centred second moments (xx, yy, zz, xy, xz, yz), first point,
-// largest |x| + |y| + |z| and kind of a box's points.
-struct Mom {
-    uint32_t n;
-    uint32_t kind;
-    float mean[3];
-    float m2[6];
-    float p0[3];
-    float mabs;
-};
+using Mom = RefitMom;
 
-__device__ __forceinline__ void store_mom(RefitScratch& s, const Mom& m) {
-    s.n = m.n;
-    s.kind = m.kind;
-    for (int i = 0; i < 3; ++i) s.mean[i] = m.mean[i], s.p0[i] = m.p0[i];
-    for (int i = 0; i < 6; ++i) s.m2[i] = m.m2[i];
-    s.maxabs = m.mabs;
-}
-
-// Read through L2: another SM wrote these fields in this launch.
-__device__ __forceinline__ Mom load_mom(const RefitScratch& s) {
+// Read through L2: another SM wrote it in this launch.
+__device__ __forceinline__ Mom load_mom(const Mom* s) {
     Mom m;
-    m.n = __ldcg(&s.n);
-    m.kind = __ldcg(&s.kind);
-    for (int i = 0; i < 3; ++i) m.mean[i] = __ldcg(&s.mean[i]), m.p0[i] = __ldcg(&s.p0[i]);
-    for (int i = 0; i < 6; ++i) m.m2[i] = __ldcg(&s.m2[i]);
-    m.mabs = __ldcg(&s.maxabs);
+    const uint4* q = reinterpret_cast<const uint4*>(s);
+    uint4 w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = __ldcg(q + i);
+    memcpy(&m, w, sizeof(Mom));
     return m;
 }
 
@@ -356,26 +339,27 @@ __device__ __forceinline__ unsigned arrive_acq_rel(unsigned* p) {
 // A thread per leaf box; the second child to arrive at a parent merges and
 // climbs on. The arrival counter is reset by the thread that merges.
 __global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, const float4* tris,
-                                                          const RefitTree* trees, RefitScratch* scratch) {
+                                                          const RefitTree* trees, const RefitBufs B) {
     const RefitTree T = trees[blockIdx.y];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= T.n_leaves) return;
-    RefitScratch* S = scratch + T.scratch_base;
+    Mom* M = B.mom + T.scratch_base;
+    uint32_t* arrive = B.arrive + T.scratch_base;
     uint32_t r = T.leaves[i];
     const uint2 rg = T.ranges[r];
     Mom m = leaf_mom(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y);
-    store_mom(S[r], m);
+    M[r] = m;
     for (;;) {
         const uint32_t p = T.parent[r];
         if (p == kNoRec) break;
         // the arrival releases this box's moments and acquires the sibling's
-        if (arrive_acq_rel(&S[p].arrive) == 0u) break;  // the sibling merges
-        S[p].arrive = 0u;
+        if (arrive_acq_rel(arrive + p) == 0u) break;  // the sibling merges
+        arrive[p] = 0u;
         const uint32_t c0 = __float_as_uint(__ldg(&recs[4ull * (T.rec_base + p) + 3].x)) - T.rec_base;
-        const Mom a = c0 == r ? m : load_mom(S[c0]);
-        const Mom b = c0 + 1u == r ? m : load_mom(S[c0 + 1u]);
+        const Mom a = c0 == r ? m : load_mom(M + c0);
+        const Mom b = c0 + 1u == r ? m : load_mom(M + c0 + 1u);
         m = merge_mom(a, b);
-        store_mom(S[p], m);
+        M[p] = m;
         r = p;
     }
 }
@@ -383,21 +367,26 @@ __global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, co
 // One thread per record: the eigensystem of M2 / n by the eig3 procedure in
 // FP32; the box axes are the rows of the eigenvector matrix, as the reference
 // takes them.
-__global__ void refit_axes_kernel(const RefitTree* trees, RefitScratch* scratch) {
+__global__ void refit_axes_kernel(const RefitTree* trees, const RefitBufs B) {
     const RefitTree T = trees[blockIdx.y];
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= T.n_recs) return;
-    RefitScratch& sc = scratch[T.scratch_base + r];
-    if (T.ranges[r].y == ~0u || sc.kind != kRefitBox) return;
-    const float fn = float(sc.n);
+    if (r >= T.n_recs || T.ranges[r].y == ~0u) return;
+    const Mom& m = B.mom[T.scratch_base + r];
+    float4* ax = B.axes + 3ull * (T.scratch_base + r);
+    if (m.kind != kRefitBox) {
+        ax[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float fn = float(m.n);
     float c[6];
-    for (int i = 0; i < 6; ++i) c[i] = sc.m2[i] / fn;  // xx, yy, zz, xy, xz, yz
+    for (int i = 0; i < 6; ++i) c[i] = m.m2[i] / fn;  // xx, yy, zz, xy, xz, yz
     float v[3][3] = {{c[0], c[3], c[4]}, {c[3], c[1], c[5]}, {c[4], c[5], c[2]}};
     float d[3], e[3];
     tridiagonalize(v, d, e);
     ql_sort(v, d, e, FLT_EPSILON);
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) sc.axes[3 * i + j] = v[i][j];
+    ax[0] = make_float4(v[0][0], v[0][1], v[0][2], 1.f);
+    ax[1] = make_float4(v[1][0], v[1][1], v[1][2], 0.f);
+    ax[2] = make_float4(v[2][0], v[2][1], v[2][2], 0.f);
 }
 
 // Order-preserving int key of a float (and its inverse): integer min/max of
@@ -410,10 +399,11 @@ __device__ __forceinline__ float unkey(int k) { return __int_as_float(k >= 0 ? k
 
 // A thread per point: its projections on the axes of every box above it.
 __global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, const RefitTree* trees,
-                                                           RefitScratch* scratch) {
+                                                           const RefitBufs B) {
     const RefitTree T = trees[blockIdx.y];
     if (blockIdx.x * blockDim.x >= 3u * T.n_tris) return;  // whole block
-    RefitScratch* S = scratch + T.scratch_base;
+    const float4* AX = B.axes + 3ull * T.scratch_base;
+    int4* EX = B.ext + 2ull * T.scratch_base;
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool live = k < 3u * T.n_tris;
@@ -426,31 +416,33 @@ __global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, c
     while (__any_sync(kAll, r != kNoRec)) {
         int lo[3] = {kExtLo, kExtLo, kExtLo}, hi[3] = {kExtHi, kExtHi, kExtHi};
         bool box = false;
+        uint32_t next = kNoRec;
         if (r != kNoRec) {
-            const RefitScratch& sc = S[r];
-            box = sc.kind == kRefitBox;
+            next = T.parent[r];  // issued with the axes' loads
+            const float4 a0 = AX[3ull * r], a1 = AX[3ull * r + 1], a2 = AX[3ull * r + 2];
+            box = a0.w != 0.f;
             if (box) {
+                const float4 a[3] = {a0, a1, a2};
 #pragma unroll
-                for (int a = 0; a < 3; ++a)
-                    lo[a] = hi[a] = fkey((sc.axes[3 * a] * p.x + sc.axes[3 * a + 1] * p.y) + sc.axes[3 * a + 2] * p.z);
+                for (int j = 0; j < 3; ++j) lo[j] = hi[j] = fkey((a[j].x * p.x + a[j].y * p.y) + a[j].z * p.z);
             }
         }
         // lanes at the same box reduce together; the lowest one adds the result
         const unsigned grp = __match_any_sync(kAll, r);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = __reduce_min_sync(grp, lo[a]);
-            hi[a] = __reduce_max_sync(grp, hi[a]);
+        for (int j = 0; j < 3; ++j) {
+            lo[j] = __reduce_min_sync(grp, lo[j]);
+            hi[j] = __reduce_max_sync(grp, hi[j]);
         }
         if (box && lane == __ffs(grp) - 1) {
-            RefitScratch& sc = S[r];
+            int* e = reinterpret_cast<int*>(EX + 2ull * r);
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                atomicMin(&sc.ext[a], lo[a]);
-                atomicMax(&sc.ext[3 + a], hi[a]);
+            for (int j = 0; j < 3; ++j) {
+                atomicMin(e + j, lo[j]);
+                atomicMax(e + 4 + j, hi[j]);
             }
         }
-        if (r != kNoRec) r = T.parent[r];
+        r = next;
     }
 }
 
@@ -476,9 +468,9 @@ __device__ __forceinline__ Box assemble(const float ax[9], const float lo[3], co
     return Box{make_float3(cx, cy, cz), half[0], half[1], half[2]};
 }
 
-__device__ __forceinline__ Box special_box(const RefitScratch& sc) {
+__device__ __forceinline__ Box special_box(const Mom& m) {
     Box b;
-    b.c = sc.kind == kRefitPoint ? make_float3(sc.p0[0], sc.p0[1], sc.p0[2]) : make_float3(0.f, 0.f, 0.f);
+    b.c = m.kind == kRefitPoint ? make_float3(m.p0[0], m.p0[1], m.p0[2]) : make_float3(0.f, 0.f, 0.f);
     b.u = make_float3(FLT_EPSILON, 0.f, 0.f);
     b.v = make_float3(0.f, FLT_EPSILON, 0.f);
     b.w = make_float3(0.f, 0.f, FLT_EPSILON);
@@ -494,52 +486,56 @@ __device__ __forceinline__ void write_box(float4* recs, uint32_t rec, const Box&
     out[3] = make_float4(q3.x, q3.y, surface(b), q3.w);
 }
 
-__global__ void refit_assemble_kernel(float4* recs, const RefitTree* trees, RefitScratch* scratch) {
+__global__ void refit_assemble_kernel(float4* recs, const RefitTree* trees, const RefitBufs B) {
     const RefitTree T = trees[blockIdx.y];
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= T.n_recs || T.ranges[r].y == ~0u) return;
-    RefitScratch& sc = scratch[T.scratch_base + r];
-    if (sc.kind != kRefitBox) {
-        write_box(recs, T.rec_base + r, special_box(sc));
+    const size_t q = size_t(T.scratch_base) + r;
+    const Mom& m = B.mom[q];
+    if (m.kind != kRefitBox) {
+        write_box(recs, T.rec_base + r, special_box(m));
         return;
     }
+    const float4* A = B.axes + 3 * q;
     float ax[9], lo[3], hi[3];
-    for (int i = 0; i < 9; ++i) ax[i] = sc.axes[i];
-    for (int a = 0; a < 3; ++a) {
-        lo[a] = unkey(sc.ext[a]);
-        hi[a] = unkey(sc.ext[3 + a]);
-        sc.ext[a] = kExtLo;
-        sc.ext[3 + a] = kExtHi;
+    for (int j = 0; j < 3; ++j) {
+        const float4 a = A[j];
+        ax[3 * j] = a.x, ax[3 * j + 1] = a.y, ax[3 * j + 2] = a.z;
     }
-    write_box(recs, T.rec_base + r, assemble(ax, lo, hi, sc.maxabs));
+    int4* E = B.ext + 2 * q;
+    const int4 el = E[0], eh = E[1];
+    lo[0] = unkey(el.x), lo[1] = unkey(el.y), lo[2] = unkey(el.z);
+    hi[0] = unkey(eh.x), hi[1] = unkey(eh.y), hi[2] = unkey(eh.z);
+    E[0] = make_int4(kExtLo, kExtLo, kExtLo, 0);
+    E[1] = make_int4(kExtHi, kExtHi, kExtHi, 0);
+    write_box(recs, T.rec_base + r, assemble(ax, lo, hi, m.mabs));
 }
 
-__global__ void refit_scratch_init_kernel(RefitScratch* scratch, uint32_t n) {
+__global__ void refit_scratch_init_kernel(const RefitBufs B, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        RefitScratch& s = scratch[i];
-        s.arrive = 0u;
-        for (int a = 0; a < 3; ++a) s.ext[a] = kExtLo, s.ext[3 + a] = kExtHi;
+        B.arrive[i] = 0u;
+        B.ext[2ull * i] = make_int4(kExtLo, kExtLo, kExtLo, 0);
+        B.ext[2ull * i + 1] = make_int4(kExtHi, kExtHi, kExtHi, 0);
     }
 }
 
 }  // namespace
 
-cudaError_t init_refit_scratch(RefitScratch* scratch, uint32_t n, cudaStream_t s) {
-    if (n) refit_scratch_init_kernel<<<(n + 255u) / 256u < 4096u ? (n + 255u) / 256u : 4096u, 256, 0, s>>>(scratch, n);
+cudaError_t init_refit_scratch(const RefitBufs& b, uint32_t n, cudaStream_t s) {
+    if (n) refit_scratch_init_kernel<<<(n + 255u) / 256u < 4096u ? (n + 255u) / 256u : 4096u, 256, 0, s>>>(b, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, uint32_t n_trees, uint32_t max_tris,
-                         uint32_t max_recs, uint32_t max_leaves, RefitScratch* scratch, cudaStream_t s) {
+                         uint32_t max_recs, uint32_t max_leaves, const RefitBufs& b, cudaStream_t s) {
     if (n_trees == 0) return cudaSuccess;
     if (max_tris) refit_tris_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees);
     if (max_leaves)
-        refit_climb_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(recs, tris, d_trees, scratch);
+        refit_climb_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(recs, tris, d_trees, b);
     const dim3 per_rec((max_recs + 127u) / 128u, n_trees);
-    refit_axes_kernel<<<per_rec, 128, 0, s>>>(d_trees, scratch);
-    if (max_tris)
-        refit_extent_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees, scratch);
-    refit_assemble_kernel<<<per_rec, 128, 0, s>>>(recs, d_trees, scratch);
+    refit_axes_kernel<<<per_rec, 128, 0, s>>>(d_trees, b);
+    if (max_tris) refit_extent_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees, b);
+    refit_assemble_kernel<<<per_rec, 128, 0, s>>>(recs, d_trees, b);
     return cudaGetLastError();
 }
 
