@@ -1265,7 +1265,7 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
         cudaFree(c->refit_scratch);
         c->refit_scratch = nullptr;
         c->refit_scratch_cap = 0;
-        CG_CUDA(cudaMalloc(&c->refit_scratch, kRefitBytesPerRecord * total_recs), "alloc refit scratch");
+        CG_CUDA(cudaMalloc(&c->refit_scratch, refit_bytes(total_recs)), "alloc refit scratch");
         c->refit_scratch_cap = total_recs;
         CG_CUDA(init_refit_scratch(refit_bufs(c->refit_scratch, total_recs), total_recs, s), "clear refit scratch");
     }

@@ -234,13 +234,15 @@ struct RefitTree {
 enum : uint32_t { kRefitSkip = 0, kRefitEmpty = 1, kRefitPoint = 2, kRefitBox = 3 };
 constexpr int kExtLo = 0x7f800000;           // order key of +inf
 constexpr int kExtHi = int(0x807fffffu);     // order key of -inf
-struct RefitMom {  // count, mean, centred second moments, first point, largest |x| + |y| + |z|: 64 bytes
+struct alignas(16) RefitMom {  // count, mean, centred second moments, first point, largest |x| + |y| + |z|
     uint32_t n, kind;
     float mean[3];
     float m2[6];  // xx, yy, zz, xy, xz, yz
     float p0[3];
     float mabs;
+    float pad;
 };
+static_assert(sizeof(RefitMom) == 64, "RefitMom is read as four 16-byte words");
 // Refit scratch, one entry per record of a batch (tree i's from scratch_base),
 // in separate arrays so that each kernel reads only what it needs.
 struct RefitBufs {
@@ -249,16 +251,22 @@ struct RefitBufs {
     int4* ext;          // [2] per record: order keys of the min and max projections (xyz); kExtLo / kExtHi between refits
     uint32_t* arrive;   // children that finished their moments; 0 between refits
 };
-constexpr size_t kRefitBytesPerRecord = sizeof(RefitMom) + 3 * sizeof(float4) + 2 * sizeof(int4) + sizeof(uint32_t);
+// bytes of the scratch for cap records: each array starts on a 256-byte boundary
+inline size_t refit_bytes(uint32_t cap) {
+    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
+    return up(sizeof(RefitMom) * size_t(cap)) + up(3 * sizeof(float4) * size_t(cap)) +
+           up(2 * sizeof(int4) * size_t(cap)) + up(sizeof(uint32_t) * size_t(cap));
+}
 inline RefitBufs refit_bufs(void* base, uint32_t cap) {
+    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
     char* p = static_cast<char*>(base);
     RefitBufs b;
     b.mom = reinterpret_cast<RefitMom*>(p);
-    p += sizeof(RefitMom) * size_t(cap);
+    p += up(sizeof(RefitMom) * size_t(cap));
     b.axes = reinterpret_cast<float4*>(p);
-    p += 3 * sizeof(float4) * size_t(cap);
+    p += up(3 * sizeof(float4) * size_t(cap));
     b.ext = reinterpret_cast<int4*>(p);
-    p += 2 * sizeof(int4) * size_t(cap);
+    p += up(2 * sizeof(int4) * size_t(cap));
     b.arrive = reinterpret_cast<uint32_t*>(p);
     return b;
 }
