@@ -22,7 +22,8 @@
 //                  on each box's axes as the float's order-preserving integer
 //                  key; lanes of a warp at the same box reduce their keys with
 //                  one warp min/max each, and one lane per box and warp adds
-//                  the result with an integer atomic min/max
+//                  the result with an integer atomic min/max where it moves
+//                  the box's current extent
 //   refit_assemble a thread per box: the box from its axes and extents (and
 //                  resets the extents for the next refit). The box is padded
 //                  by 2 FLT_EPSILON plus a bound on the FP32 rounding of the
@@ -417,8 +418,13 @@ __global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, c
         int lo[3] = {kExtLo, kExtLo, kExtLo}, hi[3] = {kExtHi, kExtHi, kExtHi};
         bool box = false;
         uint32_t next = kNoRec;
+        int4 cur_lo = make_int4(kExtHi, kExtHi, kExtHi, 0), cur_hi = make_int4(kExtLo, kExtLo, kExtLo, 0);
         if (r != kNoRec) {
             next = T.parent[r];  // issued with the axes' loads
+            // the box's extents so far (a stale value only makes an atomic
+            // that was not needed: the keys only move outwards)
+            cur_lo = __ldcg(EX + 2ull * r);
+            cur_hi = __ldcg(EX + 2ull * r + 1);
             const float4 a0 = AX[3ull * r], a1 = AX[3ull * r + 1], a2 = AX[3ull * r + 2];
             box = a0.w != 0.f;
             if (box) {
@@ -436,10 +442,11 @@ __global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, c
         }
         if (box && lane == __ffs(grp) - 1) {
             int* e = reinterpret_cast<int*>(EX + 2ull * r);
+            const int clo[3] = {cur_lo.x, cur_lo.y, cur_lo.z}, chi[3] = {cur_hi.x, cur_hi.y, cur_hi.z};
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                atomicMin(e + j, lo[j]);
-                atomicMax(e + 4 + j, hi[j]);
+                if (lo[j] < clo[j]) atomicMin(e + j, lo[j]);
+                if (hi[j] > chi[j]) atomicMax(e + 4 + j, hi[j]);
             }
         }
         r = next;
