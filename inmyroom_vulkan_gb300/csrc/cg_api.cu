@@ -111,7 +111,7 @@ struct cg_ctx {
         uint32_t n_tri_used = 0;  // the tree's triangle count (n_tris is at least 1)
         float* nrm = nullptr;
         uint2* ranges = nullptr;  // per record: first triangle and count of its subtree (refit)
-        uint32_t* topo = nullptr;  // refit: parent per record, leaf record per triangle, the leaf records
+        uint32_t* topo = nullptr;  // refit: parent per record, then the leaf records
         uint32_t n_leaves = 0;
         bool live = false;
     };
@@ -898,29 +898,23 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
         CG_CUDA(cudaMalloc(&slot.ranges, sizeof(uint2) * n_recs), "alloc record ranges");
         CG_CUDA(cudaMemcpyAsync(slot.ranges, rg.data(), sizeof(uint2) * n_recs, cudaMemcpyHostToDevice, c->stream),
                 "upload record ranges");
-        // the refit's view of the topology: the parent box of every record,
-        // the leaf box of every triangle and the list of leaf boxes (a node's
-        // record is known before its children's: pre-order)
-        std::vector<uint32_t> topo(size_t(n_recs) + T, ~0u), rec_of_node(N, ~0u), leaves;
+        // the refit's view of the topology: the parent box of every record and
+        // the list of leaf boxes in tree order (a node's record is known
+        // before its children's: pre-order)
+        std::vector<uint32_t> topo(n_recs, ~0u), rec_of_node(N, ~0u), leaves;
         uint32_t* parent = topo.data();
-        uint32_t* leaf_of_tri = topo.data() + n_recs;
         if (N) rec_of_node[0] = 1;
         for (uint32_t k = 0; k < N; ++k)
             for (int s2 = 0; s2 < 2; ++s2) {
                 const uint32_t r = 2u * k + 2u + uint32_t(s2);
                 const uint32_t ref = v->node_ref[2 * k + s2], cnt = v->node_tri_count[2 * k + s2];
                 parent[r] = rec_of_node[k];
-                if (!cnt) {
+                if (!cnt)
                     rec_of_node[ref] = r;
-                } else {
+                else
                     leaves.push_back(r);
-                    for (uint32_t t = ref; t < ref + cnt; ++t) leaf_of_tri[t] = r;
-                }
             }
-        if (!N) {
-            leaves.push_back(1u);
-            for (uint32_t t = 0; t < T; ++t) leaf_of_tri[t] = 1u;
-        }
+        if (!N) leaves.push_back(1u);
         topo.insert(topo.end(), leaves.begin(), leaves.end());
         slot.n_leaves = uint32_t(leaves.size());
         CG_CUDA(cudaMalloc(&slot.topo, sizeof(uint32_t) * topo.size()), "alloc refit topology");
@@ -1249,7 +1243,7 @@ int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const*
         const auto& t = c->trees[id];
         table[i] = RefitTree{uint32_t(t.rec_base), uint32_t(t.n_recs), uint32_t(t.tri_base), t.n_tri_used, t.ranges,
                              reinterpret_cast<const float4*>(positions[i]), n_positions[i], total_recs,
-                             t.topo, t.topo + t.n_recs, t.topo + t.n_recs + t.n_tri_used, t.n_leaves, 0u};
+                             t.topo, t.topo + t.n_recs, t.n_leaves, 0u};
         max_leaves = std::max(max_leaves, t.n_leaves);
         total_recs += uint32_t(t.n_recs);
         max_tris = std::max(max_tris, t.n_tri_used);

@@ -227,8 +227,7 @@ struct RefitTree {
     const float4* positions;
     uint32_t n_positions, scratch_base;
     const uint32_t* parent;       // per record: the record of its parent box, or ~0 (root, unused)
-    const uint32_t* leaf_of_tri;  // per triangle: the record of its leaf box
-    const uint32_t* leaves;       // the leaf records
+    const uint32_t* leaves;       // the leaf records, in tree order
     uint32_t n_leaves, pad;
 };
 enum : uint32_t { kRefitSkip = 0, kRefitEmpty = 1, kRefitPoint = 2, kRefitBox = 3 };

@@ -18,12 +18,12 @@
 //                  (Chan, Golub and LeVeque's pairwise update: mean += d nb/n,
 //                  M2 = M2a + M2b + d d^T na nb / n)
 //   refit_axes     a thread per box: the eig3 procedure in FP32 on M2 / n
-//   refit_extent   a thread per point: up its chain of boxes, the projection
-//                  on each box's axes as the float's order-preserving integer
-//                  key; lanes of a warp at the same box reduce their keys with
-//                  one warp min/max each, and one lane per box and warp adds
-//                  the result with an integer atomic min/max where it moves
-//                  the box's current extent
+//   refit_extent   a thread per leaf box: up its chain of boxes, the extent
+//                  of the leaf's points on each box's axes as the floats'
+//                  order-preserving integer keys; lanes of a warp at the same
+//                  box reduce their keys with one warp min/max each, and one
+//                  lane per box and warp adds the result with an integer
+//                  atomic min/max where it moves the box's current extent
 //   refit_assemble a thread per box: the box from its axes and extents (and
 //                  resets the extents for the next refit). The box is padded
 //                  by 2 FLT_EPSILON plus a bound on the FP32 rounding of the
@@ -398,21 +398,32 @@ __device__ __forceinline__ int fkey(float f) {
 }
 __device__ __forceinline__ float unkey(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
 
-// A thread per point: its projections on the axes of every box above it.
-__global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, const RefitTree* trees,
+// A thread per leaf box: the projections of its points (held in registers
+// for the usual leaf of up to 4 triangles) on the axes of the leaf and of
+// every box above it. Leaves are in tree order, so a warp's leaves share most
+// of their chains.
+__global__ void __launch_bounds__(128) refit_extent_kernel(const float4* tris, const RefitTree* trees,
                                                            const RefitBufs B) {
     const RefitTree T = trees[blockIdx.y];
-    if (blockIdx.x * blockDim.x >= 3u * T.n_tris) return;  // whole block
+    if (blockIdx.x * blockDim.x >= T.n_leaves) return;  // whole block
     const float4* AX = B.axes + 3ull * T.scratch_base;
     int4* EX = B.ext + 2ull * T.scratch_base;
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const bool live = k < 3u * T.n_tris;
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    uint32_t r = kNoRec;
-    if (live) {
-        p = tris[3ull * T.tri_base + k];
-        r = T.leaf_of_tri[k / 3u];
+    uint32_t r = kNoRec, n_pts = 0;
+    const float4* pt = nullptr;
+    float4 q[kLeafRegPoints];
+    if (i < T.n_leaves) {
+        r = T.leaves[i];
+        const uint2 rg = T.ranges[r];
+        n_pts = 3u * rg.y;
+        pt = tris + 3ull * (T.tri_base + rg.x);
+        if (n_pts) q[0] = pt[0];
+#pragma unroll
+        for (uint32_t k = 1; k < kLeafRegPoints; ++k) {
+            q[k] = q[0];
+            if (k < n_pts) q[k] = pt[k];
+        }
     }
     while (__any_sync(kAll, r != kNoRec)) {
         int lo[3] = {kExtLo, kExtLo, kExtLo}, hi[3] = {kExtHi, kExtHi, kExtHi};
@@ -426,11 +437,34 @@ __global__ void __launch_bounds__(256) refit_extent_kernel(const float4* tris, c
             cur_lo = __ldcg(EX + 2ull * r);
             cur_hi = __ldcg(EX + 2ull * r + 1);
             const float4 a0 = AX[3ull * r], a1 = AX[3ull * r + 1], a2 = AX[3ull * r + 2];
-            box = a0.w != 0.f;
+            box = a0.w != 0.f && n_pts != 0;
             if (box) {
                 const float4 a[3] = {a0, a1, a2};
+                float flo[3], fhi[3];
 #pragma unroll
-                for (int j = 0; j < 3; ++j) lo[j] = hi[j] = fkey((a[j].x * p.x + a[j].y * p.y) + a[j].z * p.z);
+                for (int j = 0; j < 3; ++j) flo[j] = fhi[j] = (a[j].x * q[0].x + a[j].y * q[0].y) + a[j].z * q[0].z;
+                if (n_pts <= kLeafRegPoints) {
+#pragma unroll
+                    for (uint32_t k = 1; k < kLeafRegPoints; ++k)
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) {
+                            const float pr = (a[j].x * q[k].x + a[j].y * q[k].y) + a[j].z * q[k].z;
+                            flo[j] = fminf(flo[j], pr);
+                            fhi[j] = fmaxf(fhi[j], pr);
+                        }
+                } else {
+                    for (uint32_t k = 1; k < n_pts; ++k) {
+                        const float4 p = pt[k];
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) {
+                            const float pr = (a[j].x * p.x + a[j].y * p.y) + a[j].z * p.z;
+                            flo[j] = fminf(flo[j], pr);
+                            fhi[j] = fmaxf(fhi[j], pr);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 3; ++j) lo[j] = fkey(flo[j]), hi[j] = fkey(fhi[j]);
             }
         }
         // lanes at the same box reduce together; the lowest one adds the result
@@ -541,7 +575,8 @@ cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, u
         refit_climb_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(recs, tris, d_trees, b);
     const dim3 per_rec((max_recs + 127u) / 128u, n_trees);
     refit_axes_kernel<<<per_rec, 128, 0, s>>>(d_trees, b);
-    if (max_tris) refit_extent_kernel<<<dim3((3u * max_tris + 255u) / 256u, n_trees), 256, 0, s>>>(tris, d_trees, b);
+    if (max_leaves)
+        refit_extent_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(tris, d_trees, b);
     refit_assemble_kernel<<<per_rec, 128, 0, s>>>(recs, d_trees, b);
     return cudaGetLastError();
 }
