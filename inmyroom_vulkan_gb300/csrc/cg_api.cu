@@ -1320,7 +1320,7 @@ int cg_pose_backward(cg_ctx* c, const cg_skeleton_view* sk, const float* d_axis_
     PoseParams p{};
     int rc = pose_params(c, sk, n_poses, s, &p);
     if (rc != CG_OK) return rc;
-    const uint64_t need = uint64_t(n_poses) * p.n_bones * 16u;
+    const uint64_t need = uint64_t(n_poses) * p.n_bones * 37u;  // dE/dG, local matrices, dE/dR per bone
     if (need > c->pose_scratch_cap) {
         CG_CUDA(cudaStreamSynchronize(s), "pose scratch");
         cudaFree(c->pose_scratch);

@@ -31,7 +31,7 @@
 //                 in shared memory, dE/dG_j = dE/dS_j IBM_j^T per block.
 //   pose_backward a half-warp per pose (lane = matrix entry), bones in reverse
 //                 order: dE/dG_parent += dE/dG_j L_j^T, dE/dL_j = G_parent^T
-//                 dE/dG_j, then the axis-angle rotation's adjoint.
+//                 dE/dG_j; then every axis-angle rotation's adjoint in parallel.
 //
 // Rotation of an axis-angle a (t = |a|, K = [a]x): R = I + A K + B K^2 with
 // A = sin t / t, B = (1 - cos t) / t^2 (Rodrigues), and
@@ -98,21 +98,28 @@ __device__ __forceinline__ float local_entry(const float a[3], float t2, const R
 // ---- posing ----
 
 // A half-warp per pose; lane l holds entry l of the column-major 4x4 (row
-// l & 3, column l >> 2). Bones in order; a parent precedes its children. The
-// chain of bones is a dependent sequence, so everything it touches (parents,
-// offsets, the pose's angles and matrices, the adjoint's accumulators) is
-// staged in shared memory when it fits (P.staged): a step then costs
-// shared-memory latency instead of a round trip to L2.
+// l & 3, column l >> 2). Three phases: every bone's local matrix
+// T(offset) R(a) (the rotation's sines and divisions) in parallel over the
+// bones, then the chain in bone order (a parent precedes its children), only
+// 4x4 products on it; the adjoint runs the chain in reverse and then every
+// rotation's adjoint in parallel again. What the chain touches (parents,
+// offsets, angles, matrices, accumulators) is staged in shared memory when it
+// fits (P.staged).
 struct PoseStage {
     const int32_t* parent;
     const float* offsets;
     const float* aa;
-    float* G;
-    float* acc;  // adjoint only
+    float* G;    // forward: local matrices, then the world matrices in place
+    float* acc;  // adjoint: dE/dG accumulated over children
+    float* L;    // adjoint: local matrices, rows 0-2 (12 per bone, column-major)
+    float* gR;   // adjoint: dE/dR (9 per bone, row-major)
 };
 
-// Shared layout: parent[nb] (int), offsets[3 nb], then per pose slot
-// aa[3 nb], G[16 nb] and, for the adjoint, acc[16 nb].
+// Shared layout: parent[nb] (int), offsets[3 nb], then per pose slot aa[3 nb]
+// and G[16 nb], and for the adjoint acc[16 nb], L[12 nb], gR[9 nb]. Unstaged,
+// the adjoint's acc, L and gR are in P.grad_acc (37 nb per pose).
+constexpr uint32_t kPoseFwdFloats = 19u, kPoseAdjFloats = 56u, kPoseAdjScratch = 37u;
+
 __device__ __forceinline__ PoseStage pose_stage(const PoseParams& P, uint32_t slot, uint32_t pose, bool live,
                                                 bool adjoint) {
     extern __shared__ float sh[];
@@ -123,12 +130,15 @@ __device__ __forceinline__ PoseStage pose_stage(const PoseParams& P, uint32_t sl
         st.offsets = P.offsets;
         st.aa = P.axis_angles + 3ull * nb * pose;
         st.G = P.joint_matrices + 16ull * nb * pose;
-        st.acc = adjoint ? P.grad_acc + 16ull * nb * pose : nullptr;
+        float* sc = adjoint ? P.grad_acc + size_t(kPoseAdjScratch) * nb * pose : nullptr;
+        st.acc = sc;
+        st.L = adjoint ? sc + 16u * nb : nullptr;
+        st.gR = adjoint ? sc + 28u * nb : nullptr;
         return st;
     }
     int32_t* par = reinterpret_cast<int32_t*>(sh);
     float* off = sh + nb;
-    float* mine = sh + 4u * nb + size_t(slot) * (adjoint ? 35u : 19u) * nb;
+    float* mine = sh + 4u * nb + size_t(slot) * (adjoint ? kPoseAdjFloats : kPoseFwdFloats) * nb;
     for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) par[i] = P.parent[i];
     for (uint32_t i = threadIdx.x; i < 3u * nb; i += blockDim.x) off[i] = P.offsets[i];
     const uint32_t l = threadIdx.x & 15u;
@@ -137,11 +147,7 @@ __device__ __forceinline__ PoseStage pose_stage(const PoseParams& P, uint32_t sl
         for (uint32_t i = l; i < 3u * nb; i += 16u) mine[i] = aa[i];
         if (adjoint) {
             const float* G = P.joint_matrices + 16ull * nb * pose;
-            const float* gin = P.grad_joint + 16ull * nb * pose;
-            for (uint32_t i = l; i < 16u * nb; i += 16u) {
-                mine[3u * nb + i] = G[i];
-                mine[19u * nb + i] = gin[i];
-            }
+            for (uint32_t i = l; i < 16u * nb; i += 16u) mine[3u * nb + i] = G[i];
         }
     }
     __syncthreads();
@@ -150,7 +156,23 @@ __device__ __forceinline__ PoseStage pose_stage(const PoseParams& P, uint32_t sl
     st.aa = mine;
     st.G = mine + 3u * nb;
     st.acc = adjoint ? mine + 19u * nb : nullptr;
+    st.L = adjoint ? mine + 35u * nb : nullptr;
+    st.gR = adjoint ? mine + 47u * nb : nullptr;
     return st;
+}
+
+// The local matrix of bone j: all 16 entries (column-major) into out[16], or
+// rows 0-2 into out[12] (column-major, 3 per column).
+template <int kRows>
+__device__ __forceinline__ void local_matrix(const PoseStage& S, uint32_t j, float* out) {
+    const float a[3] = {S.aa[3 * j], S.aa[3 * j + 1], S.aa[3 * j + 2]};
+    const float t2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
+    const RotCoef k = rot_coef(t2);
+    const float* off = S.offsets + 3ull * j;
+#pragma unroll
+    for (uint32_t c = 0; c < 4; ++c)
+#pragma unroll
+        for (uint32_t r = 0; r < uint32_t(kRows); ++r) out[kRows * c + r] = local_entry(a, t2, k, off, r, c);
 }
 
 __global__ void __launch_bounds__(256) pose_kernel(const PoseParams P) {
@@ -158,30 +180,31 @@ __global__ void __launch_bounds__(256) pose_kernel(const PoseParams P) {
     const uint32_t pose = blockIdx.x * P.per_block + slot;
     const bool live = slot < P.per_block && pose < P.n_poses;
     const PoseStage S = pose_stage(P, slot, pose, live, false);
-    for (uint32_t j = 0; j < P.n_bones; ++j) {
+    const uint32_t nb = P.n_bones;
+    // local matrices, bones spread over the half-warp
+    if (live)
+        for (uint32_t j = l; j < nb; j += 16u) local_matrix<4>(S, j, S.G + 16ull * j);
+    __syncwarp();
+    for (uint32_t j = 0; j < nb; ++j) {
+        float g = 0.0f;
         if (live) {
-            const float a[3] = {S.aa[3 * j], S.aa[3 * j + 1], S.aa[3 * j + 2]};
-            const float t2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
-            const RotCoef k = rot_coef(t2);
-            const float* off = S.offsets + 3ull * j;
-            float L[4];  // column c of the local matrix
-#pragma unroll
-            for (uint32_t i = 0; i < 4; ++i) L[i] = local_entry(a, t2, k, off, i, c);
+            const float* Lc = S.G + 16ull * j + 4u * c;  // column c of the local matrix
+            const float L0 = Lc[0], L1 = Lc[1], L2 = Lc[2], L3 = Lc[3];
             const int par = S.parent[j];
-            float g;
             if (par < 0) {
-                g = r == 0u ? L[0] : (r == 1u ? L[1] : (r == 2u ? L[2] : L[3]));
+                g = r == 0u ? L0 : (r == 1u ? L1 : (r == 2u ? L2 : L3));
             } else {
                 const float* Gp = S.G + 16ull * par;
-                g = (Gp[r] * L[0] + Gp[4 + r] * L[1]) + (Gp[8 + r] * L[2] + Gp[12 + r] * L[3]);
+                g = (Gp[r] * L0 + Gp[4 + r] * L1) + (Gp[8 + r] * L2 + Gp[12 + r] * L3);
             }
-            S.G[16ull * j + l] = g;
         }
+        __syncwarp();  // every lane has read the column it needs before any lane writes
+        if (live) S.G[16ull * j + l] = g;
         __syncwarp();  // the bone's entries are visible to the half-warp before a child reads them
     }
     if (P.staged && live) {
-        float* out = P.joint_matrices + 16ull * P.n_bones * pose;
-        for (uint32_t i = l; i < 16u * P.n_bones; i += 16u) out[i] = S.G[i];
+        float* out = P.joint_matrices + 16ull * nb * pose;
+        for (uint32_t i = l; i < 16u * nb; i += 16u) out[i] = S.G[i];
     }
 }
 
@@ -190,26 +213,23 @@ __global__ void __launch_bounds__(256) pose_backward_kernel(const PoseParams P) 
     const uint32_t slot = threadIdx.x >> 4;
     const uint32_t pose_w = blockIdx.x * P.per_block + slot;
     const bool live = slot < P.per_block && pose_w < P.n_poses;
-    // a spare half-warp follows a real pose's reads (its shuffles need the
-    // whole warp) and writes nothing
+    // a spare half-warp follows a real pose's chain (its shuffles need the
+    // whole warp) and writes nothing; staged, it has no shared slot and
+    // shuffles zeros
     const uint32_t pose = live ? pose_w : P.n_poses - 1u;
     const bool stage_live = live || !P.staged;
     const PoseStage S = pose_stage(P, slot, pose, live, true);
-    float* ga = P.grad_axis_angles + 3ull * P.n_bones * pose;
-    if (live && !P.staged) {
-        const float* gin = P.grad_joint + 16ull * P.n_bones * pose;
-        for (uint32_t j = 0; j < P.n_bones; ++j) S.acc[16ull * j + l] = gin[16ull * j + l];
+    const uint32_t nb = P.n_bones;
+    if (live) {
+        const float* gin = P.grad_joint + 16ull * nb * pose;
+        for (uint32_t i = l; i < 16u * nb; i += 16u) S.acc[i] = gin[i];
+        for (uint32_t j = l; j < nb; j += 16u) local_matrix<3>(S, j, S.L + 12ull * j);
     }
-    for (uint32_t jj = P.n_bones; jj-- > 0;) {
+    __syncwarp();
+    for (uint32_t jj = nb; jj-- > 0;) {
         // every lane reads and writes only its own entry of acc; the entries
-        // of other lanes come by shuffle (a spare half-warp of a staged launch
-        // has no shared slot: it shuffles zeros)
+        // of other lanes come by shuffle
         const float g = stage_live ? S.acc[16ull * jj + l] : 0.0f;  // dE/dG_j, children's shares included
-        float a[3] = {0.f, 0.f, 0.f};
-        if (stage_live) a[0] = S.aa[3 * jj], a[1] = S.aa[3 * jj + 1], a[2] = S.aa[3 * jj + 2];
-        const float t2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
-        const RotCoef k = rot_coef(t2);
-        const float* off = S.offsets + 3ull * jj;
         float grow[4], gcol[4];
 #pragma unroll
         for (uint32_t i = 0; i < 4; ++i) {
@@ -219,21 +239,28 @@ __global__ void __launch_bounds__(256) pose_backward_kernel(const PoseParams P) 
         const int par = S.parent[jj];
         float gL = g;
         if (par >= 0 && stage_live) {
-            // dE/dG_par[r][c] += sum_i g[r][i] L[c][i]
-            float add = 0.0f;
-#pragma unroll
-            for (uint32_t i = 0; i < 4; ++i) add = add + grow[i] * local_entry(a, t2, k, off, c, i);
+            // dE/dG_par[r][c] += sum_i g[r][i] L[c][i] (row 3 of L: 0 0 0 1)
+            const float* Lj = S.L + 12ull * jj;
+            float add = c == 3u ? grow[3] : 0.0f;
+            if (c < 3u)
+                add = ((grow[0] * Lj[c] + grow[1] * Lj[3 + c]) + grow[2] * Lj[6 + c]) + grow[3] * Lj[9 + c];
             if (live) S.acc[16ull * par + l] += add;
             // dE/dL[r][c] = sum_i G_par[i][r] g[i][c]
             const float* Gp = S.G + 16ull * par;
             gL = (Gp[4 * r] * gcol[0] + Gp[4 * r + 1] * gcol[1]) + (Gp[4 * r + 2] * gcol[2] + Gp[4 * r + 3] * gcol[3]);
         }
-        float gR[3][3];
-#pragma unroll
-        for (uint32_t i = 0; i < 3; ++i)
-#pragma unroll
-            for (uint32_t m = 0; m < 3; ++m) gR[i][m] = __shfl_sync(0xffffffffu, gL, base + 4u * m + i);
-        if (live && l == 0) {
+        if (live && r < 3u && c < 3u) S.gR[9ull * jj + 3u * r + c] = gL;
+        __syncwarp();
+    }
+    // the rotations' adjoints, bones spread over the half-warp
+    if (live) {
+        float* ga = P.grad_axis_angles + 3ull * nb * pose;
+        for (uint32_t j = l; j < nb; j += 16u) {
+            const float a[3] = {S.aa[3 * j], S.aa[3 * j + 1], S.aa[3 * j + 2]};
+            const float t2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
+            const RotCoef k = rot_coef(t2);
+            const float* R = S.gR + 9ull * j;
+            const float gR[3][3] = {{R[0], R[1], R[2]}, {R[3], R[4], R[5]}, {R[6], R[7], R[8]}};
             const float w[3] = {gR[2][1] - gR[1][2], gR[0][2] - gR[2][0], gR[1][0] - gR[0][1]};
             const float tr = (gR[0][0] + gR[1][1]) + gR[2][2];
             float Ra[3], Rta[3];
@@ -247,9 +274,8 @@ __global__ void __launch_bounds__(256) pose_backward_kernel(const PoseParams P) 
             const float radial = k.dA * aw + k.dB * (aRa - t2 * tr);
 #pragma unroll
             for (uint32_t i = 0; i < 3; ++i)
-                ga[3 * jj + i] = a[i] * radial + k.A * w[i] + k.B * ((Rta[i] + Ra[i]) - 2.0f * tr * a[i]);
+                ga[3 * j + i] = a[i] * radial + k.A * w[i] + k.B * ((Rta[i] + Ra[i]) - 2.0f * tr * a[i]);
         }
-        __syncwarp();
     }
 }
 
@@ -425,11 +451,18 @@ __device__ __forceinline__ float warp_sum(float v) {
 // the end dE/dG_j = dE/dS_j IBM_j^T goes to the output once per block.
 __global__ void __launch_bounds__(256) skin_adjoint_kernel(const EnergyParams P) {
     extern __shared__ float sh[];  // [nj][12] dE/dS (column-major rows 0-2), [nt] dE/dw, [nj][16] S when staged
-    __shared__ int busy;
     const EnergySide& ES = P.sides[P.deforming[blockIdx.y]];
     const DeformParams& D = ES.d;
     if (blockIdx.x * blockDim.x >= D.n_vertices) return;  // whole block
     const uint32_t nj = D.n_groups ? D.n_joints : 0u, nt = D.n_targets;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    float* gp = P.vgrad + 3ull * (ES.grad_base + x);
+    if (x < D.n_vertices) gx = gp[0], gy = gp[1], gz = gp[2];
+    const bool has = gx != 0.0f || gy != 0.0f || gz != 0.0f;
+    if (!__syncthreads_or(has)) return;  // most blocks: no vertex of theirs touches a colliding pair
+    if (has) gp[0] = gp[1] = gp[2] = 0.0f;  // the buffer is zero again for the next call
     float* gS = sh;
     float* gw = sh + 12u * nj;
     float* Ms = P.skin_in_smem ? gw + nt : nullptr;
@@ -437,18 +470,9 @@ __global__ void __launch_bounds__(256) skin_adjoint_kernel(const EnergyParams P)
     if (Ms)
         for (uint32_t e = threadIdx.x; e < 16u * nj; e += blockDim.x)
             Ms[e] = skin_entry(D.joint_matrices + 16ull * (e >> 4), D.inverse_bind + 16ull * (e >> 4), e & 15u);
-    if (threadIdx.x == 0) busy = 0;
     __syncthreads();
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-    float* gp = P.vgrad + 3ull * (ES.grad_base + x);
-    if (x < D.n_vertices) gx = gp[0], gy = gp[1], gz = gp[2];
-    const bool has = gx != 0.0f || gy != 0.0f || gz != 0.0f;
-    if (has) gp[0] = gp[1] = gp[2] = 0.0f;  // the buffer is zero again for the next call
     const unsigned act = __ballot_sync(0xffffffffu, has);
     if (act) {
-        if (lane == 0) busy = 1;
         const uint32_t leader = __ffs(act) - 1u;
         const float4 u = has ? morph_vertex(D, x) : make_float4(0.f, 0.f, 0.f, 0.f);
         const float uc[4] = {u.x, u.y, u.z, u.w};
@@ -513,7 +537,6 @@ __global__ void __launch_bounds__(256) skin_adjoint_kernel(const EnergyParams P)
         }
     }
     __syncthreads();
-    if (!busy) return;
     for (uint32_t e = threadIdx.x; e < 12u * nj; e += blockDim.x) {
         const uint32_t j = e / 12u, cc = (e % 12u) / 3u, rr = e % 3u;
         const float* d = gS + 12u * j;
@@ -535,12 +558,12 @@ constexpr uint32_t kSkinAdjointSmemFloats =
     (28u * kSkinStagedJoints > 12u * kMaxJoints ? 28u * kSkinStagedJoints : 12u * kMaxJoints) + 256u;
 
 // Poses per block and whether the chain is staged in shared memory (at most
-// kPoseSmem bytes: the adjoint's 35 floats per bone and pose, plus 4 per bone
+// kPoseSmem bytes: the adjoint's 56 floats per bone and pose, plus 4 per bone
 // for the skeleton).
 constexpr uint32_t kPoseSmem = 96u * 1024u;
 
 void pose_shape(PoseParams& p, bool adjoint, uint32_t* threads, size_t* smem) {
-    const size_t per_pose = sizeof(float) * (adjoint ? 35u : 19u) * p.n_bones;
+    const size_t per_pose = sizeof(float) * (adjoint ? kPoseAdjFloats : kPoseFwdFloats) * p.n_bones;
     const size_t common = sizeof(float) * 4u * p.n_bones;
     const size_t fit = common < kPoseSmem ? (kPoseSmem - common) / per_pose : 0;
     p.staged = fit >= 1 ? 1u : 0u;

@@ -283,7 +283,7 @@ struct PoseParams {
     const float* axis_angles;       // [n_poses][n_bones][3]
     float* joint_matrices;          // forward out / backward in: [n_poses][n_bones][16]
     const float* grad_joint;        // backward in: [n_poses][n_bones][16]
-    float* grad_acc;                // backward scratch: [n_poses][n_bones][16]
+    float* grad_acc;                // backward scratch: [n_poses][n_bones][37] (used when not staged)
     float* grad_axis_angles;        // backward out: [n_poses][n_bones][3]
 };
 cudaError_t launch_pose(const PoseParams& p, cudaStream_t s);
