@@ -181,6 +181,8 @@ struct cg_ctx {
     uint32_t copy_blocks = 0;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_t2 = nullptr;  // traversal start, end; narrow end
     cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
+    cudaStream_t side = nullptr;    // a branch of cg_collide's step graph (host copy of the pairs)
+    cudaEvent_t ev_fork = nullptr, ev_joined = nullptr;
 
     // batch tables of cg_deform_batch / cg_tree_refit_batch in device memory,
     // uploaded when their contents change
@@ -479,7 +481,10 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
 }
 
 // Enqueues counter reset, packing, the traversal and the narrow phase on `s`.
-int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s) {
+// pairs_copy: with the step's colliding pairs final (after the narrow phase),
+// copy them out on a branch that runs beside the contact kernels.
+int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s,
+                 const CopyOutParams* pairs_copy = nullptr) {
     c->last_n = n;
     unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
     const uint32_t trace_ns = c->trace_ns ? c->trace_ns : 1000u;
@@ -525,6 +530,12 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t1, s, rec_flags), "timing event");
     if (n) CG_CUDA(launch_narrow(np, c->narrow_blocks, 8, s), "narrow-phase kernel");
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t2, s, rec_flags), "timing event");
+    if (pairs_copy) {
+        CG_CUDA(cudaEventRecord(c->ev_fork, s), "fork event");
+        CG_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+        CG_CUDA(launch_copy_out(*pairs_copy, c->copy_blocks, c->side), "copy kernel");
+        CG_CUDA(cudaEventRecord(c->ev_joined, c->side), "join event");
+    }
     if ((flags & CG_CONTACTS) && n) {
         const auto& t = c->ct;
         ContactParams cp{};
@@ -551,6 +562,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.ctr = c->d_ctr;
         CG_CUDA(launch_contacts(cp, c->accumulate_blocks, c->emit_blocks, s), "contact kernels");
     }
+    if (pairs_copy) CG_CUDA(cudaStreamWaitEvent(s, c->ev_joined, 0), "join");
     return CG_OK;
 }
 
@@ -727,6 +739,9 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess ||
         cudaEventCreate(&c->ev_t2) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_joined, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&c->d_trace, sizeof(unsigned int) * 4 * kTraceBuckets) != cudaSuccess) {
         delete c;
         return CG_ERR_CUDA;
@@ -767,6 +782,9 @@ int cg_destroy(cg_ctx* c) {
     cudaEventDestroy(c->ev_t1);
     cudaEventDestroy(c->ev_t2);
     cudaEventDestroy(c->ev_join);
+    cudaEventDestroy(c->ev_fork);
+    cudaEventDestroy(c->ev_joined);
+    cudaStreamDestroy(c->side);
     cudaStreamDestroy(c->stream);
     delete c;
     return CG_OK;
@@ -1011,24 +1029,25 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
         cudaError_t e = cudaSuccess;
         if (n)
             e = cudaMemcpyAsync(c->d_queries, c->h_queries, sizeof(cg_query) * n, cudaMemcpyHostToDevice, c->stream);
-        int rc = e == cudaSuccess ? enqueue_step(c, c->d_queries, n, flags, c->stream) : CG_ERR_CUDA;
-        if (rc == CG_OK && (c->host_out.pairs || c->host_out.rays || c->host_out.averages)) {
-            CopyOutParams cp{};
-            cp.ctr = c->d_ctr;
-            cp.pairs = c->d_pairs;
-            cp.pairs_avail = c->d_pairs ? c->cfg.max_tri_pairs : 0;
-            cp.host_pairs = (flags & (CG_NO_TRI_PAIRS | CG_MID_ONLY)) ? nullptr : c->host_out.pairs;
-            cp.host_pairs_cap = c->host_out.pairs_cap;
-            const bool contacts = (flags & CG_CONTACTS) != 0;
-            cp.rays = c->ct.rays;
-            cp.rays_avail = c->ct.max_rays;
-            cp.host_rays = contacts ? c->host_out.rays : nullptr;
-            cp.host_rays_cap = c->host_out.rays_cap;
-            cp.averages = c->ct.averages;
-            cp.host_averages = contacts ? c->host_out.averages : nullptr;
-            cp.host_averages_cap = c->host_out.averages_cap;
-            e = launch_copy_out(cp, c->copy_blocks, c->stream);
-        }
+        // results to the host buffers: the pairs on a branch beside the
+        // contact kernels, the rays and averages after them
+        CopyOutParams pc{}, rc2{};
+        pc.ctr = rc2.ctr = c->d_ctr;
+        pc.pairs = c->d_pairs;
+        pc.pairs_avail = c->d_pairs ? c->cfg.max_tri_pairs : 0;
+        pc.host_pairs = (flags & (CG_NO_TRI_PAIRS | CG_MID_ONLY)) ? nullptr : c->host_out.pairs;
+        pc.host_pairs_cap = c->host_out.pairs_cap;
+        const bool contacts = (flags & CG_CONTACTS) != 0;
+        rc2.rays = c->ct.rays;
+        rc2.rays_avail = c->ct.max_rays;
+        rc2.host_rays = contacts ? c->host_out.rays : nullptr;
+        rc2.host_rays_cap = c->host_out.rays_cap;
+        rc2.averages = c->ct.averages;
+        rc2.host_averages = contacts ? c->host_out.averages : nullptr;
+        rc2.host_averages_cap = c->host_out.averages_cap;
+        int rc = e == cudaSuccess ? enqueue_step(c, c->d_queries, n, flags, c->stream, pc.host_pairs ? &pc : nullptr)
+                                  : CG_ERR_CUDA;
+        if (rc == CG_OK && (rc2.host_rays || rc2.host_averages)) e = launch_copy_out(rc2, c->copy_blocks, c->stream);
         if (rc == CG_OK && e == cudaSuccess)
             e = cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream);
         c->capturing = false;
@@ -1082,7 +1101,7 @@ int cg_set_host_outputs(cg_ctx* c, cg_tri_pair* pairs, uint64_t pairs_cap, cg_ra
         return CG_OK;
     };
     void *dp = nullptr, *dr = nullptr, *da = nullptr;
-    int rc = alias(pairs, pairs_cap, 4, "pair", &dp);
+    int rc = alias(pairs, pairs_cap, 16, "pair", &dp);
     if (rc == CG_OK) rc = alias(rays, rays_cap, 16, "ray", &dr);
     if (rc == CG_OK) rc = alias(averages, averages_cap, 16, "ray-average", &da);
     if (rc != CG_OK) return rc;

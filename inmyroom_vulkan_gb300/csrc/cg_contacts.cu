@@ -559,19 +559,25 @@ cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned l
     return cudaGetLastError();
 }
 
-// Copies the step's results to the caller's page-locked host buffers (written
-// through the device's mapping of them): colliding pairs as 4-byte words (36 B
-// records), rays and per-query averages as 16-byte words. Counts from the
+// Copies the step's results to the caller's host buffers (written through the
+// device's mapping of them) as 16-byte words: colliding pairs (36-byte
+// records; the last words of an odd count as 4-byte words), rays and
+// per-query averages. Counts from the
 // step's counters, capped by what the device buffers and the host buffers hold.
 __global__ void __launch_bounds__(256) copy_out_kernel(const CopyOutParams P) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     const unsigned long long i0 = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     const Counters& C = *P.ctr;
     if (P.host_pairs) {
+        // 36-byte records: whole 16-byte words, then the last 4-byte words
         const unsigned long long n = min(min(C.n_pairs, P.pairs_avail), P.host_pairs_cap);
+        const unsigned long long words = 9ull * n, quads = words >> 2;
+        const uint4* src4 = reinterpret_cast<const uint4*>(P.pairs);
+        uint4* dst4 = reinterpret_cast<uint4*>(P.host_pairs);
+        for (unsigned long long w = i0; w < quads; w += stride) dst4[w] = __ldg(src4 + w);
         const uint32_t* src = reinterpret_cast<const uint32_t*>(P.pairs);
         uint32_t* dst = reinterpret_cast<uint32_t*>(P.host_pairs);
-        for (unsigned long long w = i0; w < 9ull * n; w += stride) dst[w] = __ldg(src + w);
+        for (unsigned long long w = 4ull * quads + i0; w < words; w += stride) dst[w] = __ldg(src + w);
     }
     if (P.host_rays) {
         const unsigned long long n = min(min((unsigned long long)C.n_rays, P.rays_avail), P.host_rays_cap);
