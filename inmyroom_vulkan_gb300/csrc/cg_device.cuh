@@ -146,34 +146,29 @@ __device__ __forceinline__ bool interval(float3 x0, float3 x1, float3 x2, float 
 // Outcome of one triangle-pair test.
 enum : int { TT_MISS = 0, TT_HIT = 1, TT_COPLANAR = 2, TT_FRAGILE = 3 };
 
-// The first triangle's plane (its normal n1) and the signed distances of the
-// second triangle's vertices to it; true when they all lie strictly on one
-// side (no intersection). The first step of tri_tri, split out so that a
-// caller can run it on many pairs and the rest only on the survivors.
-__device__ __forceinline__ float3 tt_normal1(float3 V0, float3 V1, float3 V2) {
-    const float3 e1 = sub3(V1, V0), e2 = sub3(V2, V0);
-    return make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
-}
-__device__ __forceinline__ bool tt_stage1(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float& du0,
-                                          float& du1, float& du2) {
-    const float3 n1 = tt_normal1(V0, V1, V2);
+// tri_tri_intersect_with_isectline (Triangle.cpp:866-1003). TT_HIT means
+// doIntersept && !areCoplanar (the pairs CreateUncollideRays.cpp:88 keeps);
+// TT_COPLANAR covers every coplanar outcome (never kept); TT_FRAGILE is the
+// case where the second interval degenerates (U's distances all zero while V's
+// are not), in which the reference reads uninitialised values: it is defined
+// here, as in the oracle, as "not colliding" and counted.
+__device__ __forceinline__ int tri_tri(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float3& src,
+                                       float3& tgt) {
+    float3 e1 = sub3(V1, V0), e2 = sub3(V2, V0);
+    const float3 n1 = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
     const float d1 = -((n1.x * V0.x + n1.y * V0.y) + n1.z * V0.z);
-    du0 = ((n1.x * U0.x + n1.y * U0.y) + n1.z * U0.z) + d1;
-    du1 = ((n1.x * U1.x + n1.y * U1.y) + n1.z * U1.z) + d1;
-    du2 = ((n1.x * U2.x + n1.y * U2.y) + n1.z * U2.z) + d1;
+    float du0 = ((n1.x * U0.x + n1.y * U0.y) + n1.z * U0.z) + d1;
+    float du1 = ((n1.x * U1.x + n1.y * U1.y) + n1.z * U1.z) + d1;
+    float du2 = ((n1.x * U2.x + n1.y * U2.y) + n1.z * U2.z) + d1;
     if (tiny(du0)) du0 = 0.0f;
     if (tiny(du1)) du1 = 0.0f;
     if (tiny(du2)) du2 = 0.0f;
-    return du0 * du1 > 0.0f && du0 * du2 > 0.0f;
-}
-
-// The rest of tri_tri after tt_stage1 found no separation.
-__device__ __forceinline__ int tt_stage2(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float du0,
-                                         float du1, float du2, float3& src, float3& tgt) {
-    const float3 n1 = tt_normal1(V0, V1, V2);
     const float du0du1 = du0 * du1;
     const float du0du2 = du0 * du2;
-    float3 e1 = sub3(U1, U0), e2 = sub3(U2, U0);
+    if (du0du1 > 0.0f && du0du2 > 0.0f) return TT_MISS;
+
+    e1 = sub3(U1, U0);
+    e2 = sub3(U2, U0);
     const float3 n2 = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
     const float d2 = -((n2.x * U0.x + n2.y * U0.y) + n2.z * U0.z);
     float dv0 = ((n2.x * V0.x + n2.y * V0.y) + n2.z * V0.z) + d2;
@@ -237,19 +232,6 @@ __device__ __forceinline__ int tt_stage2(float3 V0, float3 V1, float3 V2, float3
             tgt = smallest2 == 0 ? pb2 : pb1;
     }
     return TT_HIT;
-}
-
-// tri_tri_intersect_with_isectline (Triangle.cpp:866-1003). TT_HIT means
-// doIntersept && !areCoplanar (the pairs CreateUncollideRays.cpp:88 keeps);
-// TT_COPLANAR covers every coplanar outcome (never kept); TT_FRAGILE is the
-// case where the second interval degenerates (U's distances all zero while V's
-// are not), in which the reference reads uninitialised values: it is defined
-// here, as in the oracle, as "not colliding" and counted.
-__device__ __forceinline__ int tri_tri(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float3& src,
-                                       float3& tgt) {
-    float du0, du1, du2;
-    if (tt_stage1(V0, V1, V2, U0, U1, U2, du0, du1, du2)) return TT_MISS;
-    return tt_stage2(V0, V1, V2, U0, U1, U2, du0, du1, du2, src, tgt);
 }
 
 }  // namespace cg

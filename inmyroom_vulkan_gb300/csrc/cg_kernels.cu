@@ -320,89 +320,9 @@ __device__ __forceinline__ unsigned long long trace_base(Counters* ctr) {
 // The narrow phase of leaf pairs [first, first + nl) of the list (nl <= 32),
 // staged in `stage` (kNarrowWarpWords words); all 32 lanes call it. The
 // entries must be visible to the calling warp.
-// Survivors of the first plane test wait in a per-warp queue in shared
-// memory (structure of arrays, kNarrowQueue slots): both triangles (the
-// second already moved into the first's space), the three plane distances and
-// (query, arena triangles, leaf-list index). The rest of the test runs on 32
-// of them at a time, so that its lanes are busy.
-constexpr uint32_t kNarrowQueue = 64;
-enum : uint32_t { QW_A = 0, QW_B = 9, QW_DU = 18, QW_Q = 21, QW_IA = 22, QW_IB = 23, QW_LEAF = 24, QW_WORDS = 25 };
-
-__device__ __forceinline__ void queue_put(uint32_t* qb, uint32_t slot, const float3 a[3], const float3 b[3],
-                                          float du0, float du1, float du2, uint32_t q, uint32_t ia, uint32_t ib,
-                                          uint32_t leaf_i) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        qb[(QW_A + 3 * k) * kNarrowQueue + slot] = __float_as_uint(a[k].x);
-        qb[(QW_A + 3 * k + 1) * kNarrowQueue + slot] = __float_as_uint(a[k].y);
-        qb[(QW_A + 3 * k + 2) * kNarrowQueue + slot] = __float_as_uint(a[k].z);
-        qb[(QW_B + 3 * k) * kNarrowQueue + slot] = __float_as_uint(b[k].x);
-        qb[(QW_B + 3 * k + 1) * kNarrowQueue + slot] = __float_as_uint(b[k].y);
-        qb[(QW_B + 3 * k + 2) * kNarrowQueue + slot] = __float_as_uint(b[k].z);
-    }
-    qb[QW_DU * kNarrowQueue + slot] = __float_as_uint(du0);
-    qb[(QW_DU + 1) * kNarrowQueue + slot] = __float_as_uint(du1);
-    qb[(QW_DU + 2) * kNarrowQueue + slot] = __float_as_uint(du2);
-    qb[QW_Q * kNarrowQueue + slot] = q;
-    qb[QW_IA * kNarrowQueue + slot] = ia;
-    qb[QW_IB * kNarrowQueue + slot] = ib;
-    qb[QW_LEAF * kNarrowQueue + slot] = leaf_i;
-}
-
-// The rest of the test on queue slots [first, first + count), one per lane,
-// and the colliding pairs out.
-__device__ __forceinline__ void narrow_stage2(const NarrowParams& P, const uint32_t* qb, uint32_t first,
-                                              uint32_t count, int lane, unsigned long long& fragile) {
-    int res = TT_MISS;
-    uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
-    float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
-    if (uint32_t(lane) < count) {
-        const uint32_t slot = first + uint32_t(lane);
-        auto f = [&](uint32_t w) { return __uint_as_float(qb[w * kNarrowQueue + slot]); };
-        float3 a[3], b[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            a[k] = make_float3(f(QW_A + 3 * k), f(QW_A + 3 * k + 1), f(QW_A + 3 * k + 2));
-            b[k] = make_float3(f(QW_B + 3 * k), f(QW_B + 3 * k + 1), f(QW_B + 3 * k + 2));
-        }
-        q = qb[QW_Q * kNarrowQueue + slot];
-        ia = qb[QW_IA * kNarrowQueue + slot];
-        ib = qb[QW_IB * kNarrowQueue + slot];
-        leaf_i = qb[QW_LEAF * kNarrowQueue + slot];
-        res = tt_stage2(a[0], a[1], a[2], b[0], b[1], b[2], f(QW_DU), f(QW_DU + 1), f(QW_DU + 2), src, tgt);
-    }
-    const unsigned hitmask = __ballot_sync(kFull, res == TT_HIT);
-    const unsigned fragmask = __ballot_sync(kFull, res == TT_FRAGILE);
-    if (hitmask) {
-        unsigned long long obase = 0;
-        if (lane == 0) obase = atomicAdd(&P.ctr->n_pairs, (unsigned long long)__popc(hitmask));
-        obase = __shfl_sync(kFull, obase, 0);
-        if (res == TT_HIT && !(P.flags & CG_NO_TRI_PAIRS)) {
-            const unsigned long long o = obase + __popc(hitmask & lanemask_lt());
-            if (o < P.pairs_cap) {
-                const PackedQuery* Q = P.q + q;
-                cg_tri_pair r;
-                r.query = q;
-                r.tri_a = ia - __ldg(&Q->tri_base_a);
-                r.tri_b = ib - __ldg(&Q->tri_base_b);
-                r.source[0] = src.x;
-                r.source[1] = src.y;
-                r.source[2] = src.z;
-                r.target[0] = tgt.x;
-                r.target[1] = tgt.y;
-                r.target[2] = tgt.z;
-                P.pairs[o] = r;
-                if (P.pair_aux) P.pair_aux[o] = make_uint4(ia, ib, leaf_i, q);
-            }
-        }
-    }
-    if (lane == 0) fragile += __popc(fragmask);
-    __syncwarp();
-}
-
-__device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* stage, uint32_t* qb, uint32_t& qn,
-                                             uint32_t first, uint32_t nl, int lane, unsigned long long& tests,
-                                             unsigned long long& fragile, unsigned long long t_base) {
+__device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* stage, uint32_t first, uint32_t nl,
+                                             int lane, unsigned long long& tests, unsigned long long& fragile,
+                                             unsigned long long t_base) {
     uint32_t* lq = stage;
     uint32_t* loa = lq + 32;
     uint32_t* lob = loa + 32;
@@ -458,10 +378,9 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
         const bool next_at_32 = __any_sync(kFull, mine && d == 32);
         uint32_t lo = own0 + __popc(starts & ((2u << lane) - 1u));
         own0 += __popc(starts) + (next_at_32 ? 1u : 0u);
-        bool surv = false;
+        int res = TT_MISS;
         uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
-        float3 a[3], b[3];
-        float du0 = 0.f, du1 = 0.f, du2 = 0.f;
+        float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
         if (t < total) {
             if (!counted) {
                 int l = 0, h = int(nl) - 1;
@@ -485,22 +404,43 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
             ia = loa[lo] + i;
             ib = lob[lo] + j;
             const Mat4 M = load_mat(P.q + q);
-            load_tri(P.tris, ia, a[0], a[1], a[2]);
-            load_tri(P.tris, ib, b[0], b[1], b[2]);
-            b[0] = xform(M, b[0], 1.0f);
-            b[1] = xform(M, b[1], 1.0f);
-            b[2] = xform(M, b[2], 1.0f);
-            surv = !tt_stage1(a[0], a[1], a[2], b[0], b[1], b[2], du0, du1, du2);
+            float3 a0, a1, a2, b0, b1, b2;
+            load_tri(P.tris, ia, a0, a1, a2);
+            load_tri(P.tris, ib, b0, b1, b2);
+            b0 = xform(M, b0, 1.0f);
+            b1 = xform(M, b1, 1.0f);
+            b2 = xform(M, b2, 1.0f);
+            res = tri_tri(a0, a1, a2, b0, b1, b2, src, tgt);
         }
-        const unsigned sv = __ballot_sync(kFull, surv);
-        if (surv) queue_put(qb, qn + __popc(sv & lanemask_lt()), a, b, du0, du1, du2, q, ia, ib, leaf_i);
-        qn += __popc(sv);
-        __syncwarp();
-        if (qn >= 32u) {
-            qn -= 32u;
-            narrow_stage2(P, qb, qn, 32u, lane, fragile);
+        const unsigned hitmask = __ballot_sync(kFull, res == TT_HIT);
+        const unsigned fragmask = __ballot_sync(kFull, res == TT_FRAGILE);
+        if (hitmask) {
+            unsigned long long obase = 0;
+            if (lane == 0) obase = atomicAdd(&P.ctr->n_pairs, (unsigned long long)__popc(hitmask));
+            obase = __shfl_sync(kFull, obase, 0);
+            if (res == TT_HIT && !(P.flags & CG_NO_TRI_PAIRS)) {
+                const unsigned long long o = obase + __popc(hitmask & lanemask_lt());
+                if (o < P.pairs_cap) {
+                    const PackedQuery* Q = P.q + q;
+                    cg_tri_pair r;
+                    r.query = q;
+                    r.tri_a = ia - __ldg(&Q->tri_base_a);
+                    r.tri_b = ib - __ldg(&Q->tri_base_b);
+                    r.source[0] = src.x;
+                    r.source[1] = src.y;
+                    r.source[2] = src.z;
+                    r.target[0] = tgt.x;
+                    r.target[1] = tgt.y;
+                    r.target[2] = tgt.z;
+                    P.pairs[o] = r;
+                    if (P.pair_aux) P.pair_aux[o] = make_uint4(ia, ib, leaf_i, q);
+                }
+            }
         }
-        if (lane == 0 && P.trace) trace_add(P.trace, P.trace_ns, t_base, 2, min(32u, total - base));
+        if (lane == 0) {
+            fragile += __popc(fragmask);
+            if (P.trace) trace_add(P.trace, P.trace_ns, t_base, 2, min(32u, total - base));
+        }
     }
     if (lane == 0) tests += total;
     __syncwarp();
@@ -764,15 +704,11 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
 // one triangle pair per lane, in the order of the reference's pair loop per
 // leaf pair (CreateUncollideRays.cpp:78-86): B's triangle is moved into A's
 // space with TrianglePosition::MultiplyBy4x4Matrix arithmetic, then tested.
-constexpr uint32_t kNarrowWarpSmemWords = kNarrowWarpWords + QW_WORDS * kNarrowQueue;
-
 __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
-    extern __shared__ uint32_t sm[];
+    __shared__ uint32_t sm[8 * kNarrowWarpWords];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    uint32_t* stage = sm + warp * kNarrowWarpSmemWords;
-    uint32_t* qb = stage + kNarrowWarpWords;
-    uint32_t qn = 0;
+    uint32_t* stage = sm + warp * kNarrowWarpWords;
 
     const unsigned long long n_all = *reinterpret_cast<volatile unsigned long long*>(&P.ctr->n_leafs);
     const uint32_t n = uint32_t(n_all < P.leaf_cap ? n_all : P.leaf_cap);
@@ -786,9 +722,8 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
         first = __shfl_sync(kFull, first, 0);
         if (first >= n) break;
         const uint32_t nl = min(32u, n - first);
-        narrow_block(P, stage, qb, qn, first, nl, lane, tests, fragile, t_base);
+        narrow_block(P, stage, first, nl, lane, tests, fragile, t_base);
     }
-    if (qn) narrow_stage2(P, qb, 0, qn, lane, fragile);
     if (lane == 0) {
         atomicAdd(&P.ctr->tri_tests, tests);
         atomicAdd(&P.ctr->fragile, fragile);
@@ -917,10 +852,7 @@ cudaError_t traverse_occupancy(uint32_t warps_per_block, uint32_t stack_cap, int
 }
 
 cudaError_t narrow_occupancy(uint32_t warps_per_block, int* blocks_per_sm) {
-    const size_t smem = sizeof(uint32_t) * kNarrowWarpSmemWords * warps_per_block;
-    cudaError_t e = cudaFuncSetAttribute(narrow_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, narrow_kernel, int(32 * warps_per_block), smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, narrow_kernel, int(32 * warps_per_block), 0);
 }
 
 cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s) {
@@ -930,7 +862,7 @@ cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t w
 }
 
 cudaError_t launch_narrow(const NarrowParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s) {
-    narrow_kernel<<<blocks, 32 * warps_per_block, sizeof(uint32_t) * kNarrowWarpSmemWords * warps_per_block, s>>>(p);
+    narrow_kernel<<<blocks, 32 * warps_per_block, 0, s>>>(p);
     return cudaGetLastError();
 }
 
