@@ -16,9 +16,8 @@
 //                  second child to arrive at a parent (an arrival counter per
 //                  record, no waiting) merges the two children's moments
 //                  (Chan, Golub and LeVeque's pairwise update: mean += d nb/n,
-//                  M2 = M2a + M2b + d d^T na nb / n); whoever finishes a box's
-//                  moments also takes its axes: the eig3 procedure in FP32 on
-//                  M2 / n
+//                  M2 = M2a + M2b + d d^T na nb / n)
+//   refit_axes     a thread per box: the eig3 procedure in FP32 on M2 / n
 //   refit_extent   a thread per leaf box: up its chain of boxes, the extent
 //                  of the leaf's points on each box's axes as the floats'
 //                  order-preserving integer keys; lanes of a warp at the same
@@ -338,10 +337,43 @@ __device__ __forceinline__ unsigned arrive_acq_rel(unsigned* p) {
     return old;
 }
 
-// The box axes of moments m: the eigensystem of M2 / n by the eig3 procedure
-// in FP32, the rows of its eigenvector matrix, as the reference takes them;
-// w of the first row is 1 for a box (0: an empty or point box).
-__device__ __forceinline__ void store_axes(float4* ax, const Mom& m) {
+// A thread per leaf box; the second child to arrive at a parent merges and
+// climbs on. The arrival counter is reset by the thread that merges.
+__global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, const float4* tris,
+                                                          const RefitTree* trees, const RefitBufs B) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T.n_leaves) return;
+    Mom* M = B.mom + T.scratch_base;
+    uint32_t* arrive = B.arrive + T.scratch_base;
+    uint32_t r = T.leaves[i];
+    const uint2 rg = T.ranges[r];
+    Mom m = leaf_mom(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y);
+    M[r] = m;
+    for (;;) {
+        const uint32_t p = T.parent[r];
+        if (p == kNoRec) break;
+        // the arrival releases this box's moments and acquires the sibling's
+        if (arrive_acq_rel(arrive + p) == 0u) break;  // the sibling merges
+        arrive[p] = 0u;
+        const uint32_t c0 = __float_as_uint(__ldg(&recs[4ull * (T.rec_base + p) + 3].x)) - T.rec_base;
+        const Mom a = c0 == r ? m : load_mom(M + c0);
+        const Mom b = c0 + 1u == r ? m : load_mom(M + c0 + 1u);
+        m = merge_mom(a, b);
+        M[p] = m;
+        r = p;
+    }
+}
+
+// One thread per record: the eigensystem of M2 / n by the eig3 procedure in
+// FP32; the box axes are the rows of the eigenvector matrix, as the reference
+// takes them.
+__global__ void refit_axes_kernel(const RefitTree* trees, const RefitBufs B) {
+    const RefitTree T = trees[blockIdx.y];
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= T.n_recs || T.ranges[r].y == ~0u) return;
+    const Mom& m = B.mom[T.scratch_base + r];
+    float4* ax = B.axes + 3ull * (T.scratch_base + r);
     if (m.kind != kRefitBox) {
         ax[0] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
@@ -356,37 +388,6 @@ __device__ __forceinline__ void store_axes(float4* ax, const Mom& m) {
     ax[0] = make_float4(v[0][0], v[0][1], v[0][2], 1.f);
     ax[1] = make_float4(v[1][0], v[1][1], v[1][2], 0.f);
     ax[2] = make_float4(v[2][0], v[2][1], v[2][2], 0.f);
-}
-
-// A thread per leaf box; the second child to arrive at a parent merges and
-// climbs on. The arrival counter is reset by the thread that merges.
-__global__ void __launch_bounds__(128) refit_climb_kernel(const float4* recs, const float4* tris,
-                                                          const RefitTree* trees, const RefitBufs B) {
-    const RefitTree T = trees[blockIdx.y];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= T.n_leaves) return;
-    Mom* M = B.mom + T.scratch_base;
-    uint32_t* arrive = B.arrive + T.scratch_base;
-    uint32_t r = T.leaves[i];
-    const uint2 rg = T.ranges[r];
-    float4* AX = B.axes + 3ull * T.scratch_base;
-    Mom m = leaf_mom(tris + 3ull * (T.tri_base + rg.x), 3u * rg.y);
-    M[r] = m;
-    store_axes(AX + 3ull * r, m);
-    for (;;) {
-        const uint32_t p = T.parent[r];
-        if (p == kNoRec) break;
-        // the arrival releases this box's moments and acquires the sibling's
-        if (arrive_acq_rel(arrive + p) == 0u) break;  // the sibling merges
-        arrive[p] = 0u;
-        const uint32_t c0 = __float_as_uint(__ldg(&recs[4ull * (T.rec_base + p) + 3].x)) - T.rec_base;
-        const Mom a = c0 == r ? m : load_mom(M + c0);
-        const Mom b = c0 + 1u == r ? m : load_mom(M + c0 + 1u);
-        m = merge_mom(a, b);
-        M[p] = m;
-        store_axes(AX + 3ull * p, m);
-        r = p;
-    }
 }
 
 // Order-preserving int key of a float (and its inverse): integer min/max of
@@ -573,6 +574,7 @@ cudaError_t launch_refit(float4* recs, float4* tris, const RefitTree* d_trees, u
     if (max_leaves)
         refit_climb_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(recs, tris, d_trees, b);
     const dim3 per_rec((max_recs + 127u) / 128u, n_trees);
+    refit_axes_kernel<<<per_rec, 128, 0, s>>>(d_trees, b);
     if (max_leaves)
         refit_extent_kernel<<<dim3((max_leaves + 127u) / 128u, n_trees), 128, 0, s>>>(tris, d_trees, b);
     refit_assemble_kernel<<<per_rec, 128, 0, s>>>(recs, d_trees, b);
