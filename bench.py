@@ -188,6 +188,65 @@ def run_reference(args) -> dict:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_shoot(args, ctx, sc, ids, q, cpu_seconds: float) -> dict:
+    """Uncollide-ray shooting of the scene step: ShootUncollideRays for every
+    AABB-overlap pair with the rays the step's contact kernels made (grouped
+    per pair and side). Host-timed around the synchronous cg_shoot_rays call
+    (rays and queries uploaded, deltas read back, inside the timing); beside
+    it the oracle restatement on all host cores over the same rays."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle
+    from inmyroom_vulkan_gb300 import capi
+
+    assert ctx.collide(q, flags=capi.CG_CONTACTS)["status"] == 0
+    rays = ctx.rays()
+    rays = rays[np.lexsort((rays["side"], rays["query"]))]
+    qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+    n = len(qa)
+    starts = np.searchsorted(rays["query"], np.arange(n + 1))
+    ra, rb = [], []
+    for k in range(n):
+        mine = rays[starts[k]:starts[k + 1]]
+        for side, out in ((0, ra), (1, rb)):
+            m = mine[mine["side"] == side]
+            out.append(np.concatenate([m["origin"], m["direction"]], 1))
+    ga, gb = sc.mats[qa], sc.mats[qb]
+    ta, tb = [int(ids[i]) for i in qa], [int(ids[j]) for j in qb]
+    for _ in range(max(args.warmup, 3)):
+        deltas = ctx.shoot_rays(ta, tb, ga, gb, ra, rb)
+    times = []
+    for _ in range(max(args.steps, 5)):
+        t0 = time.perf_counter()
+        deltas = ctx.shoot_rays(ta, tb, ga, gb, ra, rb)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.median(times))
+    res = {"workload": f"ShootUncollideRays for the scene step's {n} pairs with its {len(rays)} uncollide rays",
+           "rays": int(len(rays)), "pairs": int(n), "pairs_moved": int((np.abs(deltas).sum(1) > 0).sum()),
+           "ms_per_step": ms, "rays_per_s": len(rays) / (ms / 1e3),
+           "timing": "host perf_counter around the synchronous cg_shoot_rays (uploads and read-back included)"}
+    if cpu_seconds > 0:
+        fast = oracle.port(fast=True)
+        trees = [fast.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+        cores = os.cpu_count() or 1
+        pool = ThreadPoolExecutor(cores)
+        work = [k for k in range(n) if len(ra[k]) or len(rb[k])]
+
+        def one(k):
+            return fast.shoot_rays(trees[qa[k]], trees[qb[k]], ga[k], gb[k], ra[k], rb[k])
+
+        runs, t0 = 0, time.perf_counter()
+        while True:
+            list(pool.map(one, work))
+            runs += 1
+            if time.perf_counter() - t0 >= cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"ms_per_step": 1e3 * el / runs, "cores": cores, "kind": "port",
+                               "sample": f"{runs} whole steps of shooting, {el:.1f} s, release flags"}
+    return res
+
+
 def run_sweep(args, local: int, flush, stream, cpu_seconds: float) -> dict:
     """Autotuned batch sweep: 10,000 uneven rigid mesh-pair queries (a pool of
     48 meshes of 256..65,536 triangles, log-uniform; random SO(3) poses with
@@ -587,6 +646,9 @@ def run_gpu(args) -> dict:
     ctx.collide(pq, flags=flags)
     ptests = ctx.sync_stats()["tri_tests"]
 
+    shoot = None
+    if rank == 0 and not args.skip_shoot:
+        shoot = run_shoot(args, ctx, sc, ids, q, min(args.cpu_seconds, 5.0))
     cpu = cpu_baseline(sc, seconds=args.cpu_seconds) if rank == 0 and args.cpu_seconds > 0 else None
     deforming = None
     if rank == 0 and not args.skip_deforming:
@@ -638,6 +700,8 @@ def run_gpu(args) -> dict:
         out["differentiable"] = differentiable
     if sweep:
         out["batch_sweep"] = sweep
+    if shoot:
+        out["shoot"] = shoot
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -671,6 +735,7 @@ def main():
     ap.add_argument("--skip-deforming", action="store_true", help="leave out the deforming and differentiable lines")
     ap.add_argument("--skip-sweep", action="store_true", help="leave out the autotuned batch-sweep line")
     ap.add_argument("--no-tune", action="store_true", help="time the scene step with the default launch settings")
+    ap.add_argument("--skip-shoot", action="store_true", help="leave out the uncollide-ray shooting line")
     ap.add_argument("--only", choices=["deforming", "differentiable", "sweep"],
                     help="run one secondary workload alone and print its object (for profiling)")
     args = ap.parse_args()

@@ -377,6 +377,43 @@ typedef struct cg_energy_side {
 int cg_energy_backward(cg_ctx* ctx, const double* d_grad_energy, const cg_energy_side* side_a,
                        const cg_energy_side* side_b, void* stream);
 
+/* ---- Uncollide-ray shooting ----
+ *
+ * ShootUncollideRays::ExecuteShootUncollideRays
+ * (src/CollisionDetection/ShootUncollideRays.cpp:14-98) for a batch of entity
+ * pairs: each ray's Hermann pass (closest hit on the other entity's tree with
+ * Ray::IntersectOBBtree, Ray.cpp:135-237; a back face; nothing nearer on its
+ * own tree) and its reflection's, the force responses summed in the
+ * reference's order, FindResponse, and the first entity's world-space delta.
+ * Bit for bit the reference's result for the same rays in the same order; the
+ * ray/triangle test is Moller-Trumbore, two-sided, back face = negative
+ * determinant (the reference's glm fork is not public). */
+typedef struct cg_shoot_params {
+    float smoothstep_start;   /* radians; the engine: 40 degrees (CollisionDetection.cpp:22-24) */
+    float smoothstep_finish;  /* radians; the engine: 65 degrees */
+    float distance_bias;      /* the engine: 1.01 */
+} cg_shoot_params;
+void cg_shoot_params_default(cg_shoot_params* params);
+
+/* One entity pair. Its rays are consecutive in the ray array: n_first from
+ * the first entity (CDentriesUncollideRays::rays_from_first_to_second), then
+ * n_second from the second (rays_from_second_to_first), all in the first
+ * entity's model space, as CreateUncollideRays makes them (cg_read_rays gives
+ * them per query and side). 144 bytes. */
+typedef struct cg_shoot_query {
+    uint32_t tree_a, tree_b;
+    float first_global[16];   /* firstEntry.currentGlobalMatrix */
+    float second_global[16];  /* secondEntry.currentGlobalMatrix */
+    uint32_t n_first, n_second;
+} cg_shoot_query;
+
+/* n pairs, rays (host, [n_rays][6]: origin, direction; n_rays the sum of the
+ * queries' counts) -> deltas (host, [n][3]). params NULL: the engine's.
+ * Synchronous. CG_ERR_QUEUE_OVERFLOW if a tree is deeper than the traversal's
+ * stack (96 levels). */
+int cg_shoot_rays(cg_ctx* ctx, const cg_shoot_query* queries, uint32_t n, const float* rays, uint64_t n_rays,
+                  const cg_shoot_params* params, float* deltas);
+
 /* ---- No-allocation collide step (no reference counterpart) ----
  *
  * The collide step of cg_collide_async (same kernels, same colliding pairs)

@@ -31,7 +31,7 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch",
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
            "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
-           "cg_set_host_outputs"]
+           "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -75,6 +75,15 @@ class cg_skeleton_view(C.Structure):
 class cg_energy_side(C.Structure):
     _fields_ = [("views", C.c_void_p), ("joint_stride", C.c_uint32), ("target_stride", C.c_uint32),
                 ("grad_joint_matrices", C.c_void_p), ("grad_morph_weights", C.c_void_p)]
+
+
+class cg_shoot_params(C.Structure):
+    _fields_ = [("smoothstep_start", C.c_float), ("smoothstep_finish", C.c_float), ("distance_bias", C.c_float)]
+
+
+class cg_shoot_query(C.Structure):
+    _fields_ = [("tree_a", C.c_uint32), ("tree_b", C.c_uint32), ("first_global", C.c_float * 16),
+                ("second_global", C.c_float * 16), ("n_first", C.c_uint32), ("n_second", C.c_uint32)]
 
 
 class cg_static_counts(C.Structure):
@@ -148,6 +157,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_tree_refit_batch.argtypes = [vp, vp, vp, vp, u32, vp]
     lib.cg_tree_download.argtypes = [vp, u32, vp, vp, u32, vp, u32]
     lib.cg_set_host_outputs.argtypes = [vp, vp, u64, vp, u64, vp, u64]
+    lib.cg_shoot_params_default.argtypes = [C.POINTER(cg_shoot_params)]
+    lib.cg_shoot_params_default.restype = None
+    lib.cg_shoot_rays.argtypes = [vp, vp, u32, vp, u64, C.POINTER(cg_shoot_params), vp]
     lib.cg_pose.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, u32, vp, vp]
     lib.cg_pose_backward.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, vp, vp, u32, vp, vp]
     lib.cg_energy.argtypes = [vp, vp, vp]
@@ -391,6 +403,35 @@ class Context:
         p, r, v = arg(pairs, TRI_PAIR_DTYPE), arg(rays, RAY_DTYPE), arg(averages, RAY_AVERAGE_DTYPE)
         self._check(self.lib.cg_set_host_outputs(self.h, p[0], p[1], r[0], r[1], v[0], v[1]), "cg_set_host_outputs")
         self._host_outputs = (pairs, rays, averages)
+
+    def shoot_rays(self, tree_a, tree_b, first_globals, second_globals, rays_first, rays_second,
+                   params: tuple | None = None) -> np.ndarray:
+        """cg_shoot_rays for n pairs: tree ids (n,), world matrices (n, 16),
+        per pair its rays from the first and from the second entity ((k, 6)
+        arrays in the first entity's space); params (start, finish angle in
+        radians, bias) or the engine's. The deltas (n, 3)."""
+        n = len(tree_a)
+        q = (cg_shoot_query * max(n, 1))()
+        parts = []
+        ga = np.asarray(first_globals, np.float32).reshape(n, 16)
+        gb = np.asarray(second_globals, np.float32).reshape(n, 16)
+        for i in range(n):
+            ra = np.asarray(rays_first[i], np.float32).reshape(-1, 6)
+            rb = np.asarray(rays_second[i], np.float32).reshape(-1, 6)
+            q[i].tree_a, q[i].tree_b = int(tree_a[i]), int(tree_b[i])
+            q[i].first_global[:] = ga[i].tolist()
+            q[i].second_global[:] = gb[i].tolist()
+            q[i].n_first, q[i].n_second = len(ra), len(rb)
+            parts += [ra, rb]
+        rays = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros((0, 6), np.float32))
+        out = np.zeros((max(n, 1), 3), np.float32)
+        pp = None
+        if params is not None:
+            pp = cg_shoot_params(*[float(x) for x in params])
+        self._check(self.lib.cg_shoot_rays(self.h, q, n, rays.ctypes.data if len(rays) else None, len(rays),
+                                           C.byref(pp) if pp is not None else None, out.ctypes.data),
+                    "cg_shoot_rays")
+        return out[:n]
 
     def pose(self, skeleton: "Skeleton", axis_angles: int, n_poses: int, joint_matrices: int,
              stream: int | None = None):

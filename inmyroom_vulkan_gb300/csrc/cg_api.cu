@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -197,6 +198,8 @@ struct cg_ctx {
     uint64_t pose_scratch_cap = 0;
     float* vgrad = nullptr;                 // energy adjoint: per-vertex gradient, zero between calls
     uint64_t vgrad_cap = 0;
+    void* shoot = nullptr;                  // cg_shoot_rays: queries, rays, tags, per-ray results, deltas, flag
+    size_t shoot_cap = 0;
 
     std::string err;
 };
@@ -777,6 +780,7 @@ int cg_destroy(cg_ctx* c) {
     cudaFree(c->energy_table.dev);
     cudaFree(c->pose_scratch);
     cudaFree(c->vgrad);
+    cudaFree(c->shoot);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
@@ -1445,6 +1449,103 @@ int cg_energy_backward(cg_ctx* c, const double* d_grad_energy, const cg_energy_s
     p.max_joints = max_joints;
     p.max_targets = max_targets;
     CG_CUDA(launch_energy_backward(p, c->energy_blocks, max_vertices, s), "energy adjoint kernels");
+    return CG_OK;
+}
+
+void cg_shoot_params_default(cg_shoot_params* p) {
+    if (!p) return;
+    const float deg = 0.01745329251994329576923690768489f;  // glm::radians
+    p->smoothstep_start = 40.f * deg;
+    p->smoothstep_finish = 65.f * deg;
+    p->distance_bias = 1.01f;
+}
+
+int cg_shoot_rays(cg_ctx* c, const cg_shoot_query* queries, uint32_t n, const float* rays, uint64_t n_rays,
+                  const cg_shoot_params* params, float* deltas) {
+    if (!c || (n && (!queries || !deltas)) || (n_rays && !rays)) return CG_ERR_INVALID_ARGUMENT;
+    if (n_rays > 0x7fffffffull) return fail(c, CG_ERR_INVALID_ARGUMENT, "more than 2^31 rays");
+    if (n > 0x7fffffffu) return fail(c, CG_ERR_INVALID_ARGUMENT, "more than 2^31 queries");
+    cg_shoot_params pr;
+    cg_shoot_params_default(&pr);
+    if (params) pr = *params;
+    std::vector<ShootQuery> table(n);
+    std::vector<uint32_t> tags(n_rays);
+    uint64_t next = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const cg_shoot_query& q = queries[i];
+        if (q.tree_a >= c->trees.size() || !c->trees[q.tree_a].live || q.tree_b >= c->trees.size() ||
+            !c->trees[q.tree_b].live)
+            return fail(c, CG_ERR_NOT_FOUND, "shoot query %u names tree %u / %u", i, q.tree_a, q.tree_b);
+        const uint64_t cnt = uint64_t(q.n_first) + q.n_second;
+        if (next + cnt > n_rays)
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "the queries' ray counts exceed n_rays (%llu)",
+                        (unsigned long long)n_rays);
+        ShootQuery& t = table[i];
+        float inv[16];
+        mat_inverse(q.first_global, inv);
+        mat_mul(inv, q.second_global, t.relative);  // OBBtreesCollision.cpp:15 / ShootUncollideRays.cpp:16-17
+        std::memcpy(t.first_global, q.first_global, sizeof(t.first_global));
+        t.tree_a = q.tree_a;
+        t.tree_b = q.tree_b;
+        t.ray_first = uint32_t(next);
+        t.n_first = q.n_first;
+        t.n_second = q.n_second;
+        for (uint64_t k = 0; k < cnt; ++k) tags[next + k] = i | (k >= q.n_first ? 0x80000000u : 0u);
+        next += cnt;
+    }
+    if (next != n_rays)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "the queries' ray counts (%llu) differ from n_rays (%llu)",
+                    (unsigned long long)next, (unsigned long long)n_rays);
+    if (n == 0) return CG_OK;
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
+    const size_t b_q = up(sizeof(ShootQuery) * n), b_r = up(sizeof(float) * 6 * n_rays), b_t = up(sizeof(uint32_t) * n_rays),
+                 b_o = up(sizeof(ShootRayOut) * n_rays), b_d = up(sizeof(float) * 3 * n), b_e = 256;
+    const size_t need = b_q + b_r + b_t + b_o + b_d + b_e;
+    if (need > c->shoot_cap) {
+        CG_CUDA(cudaStreamSynchronize(s), "shoot buffers");
+        cudaFree(c->shoot);
+        c->shoot = nullptr;
+        c->shoot_cap = 0;
+        CG_CUDA(cudaMalloc(&c->shoot, need), "alloc shoot buffers");
+        c->shoot_cap = need;
+    }
+    char* base = static_cast<char*>(c->shoot);
+    ShootQuery* d_q = reinterpret_cast<ShootQuery*>(base);
+    float* d_rays = reinterpret_cast<float*>(base + b_q);
+    uint32_t* d_tags = reinterpret_cast<uint32_t*>(base + b_q + b_r);
+    ShootRayOut* d_out = reinterpret_cast<ShootRayOut*>(base + b_q + b_r + b_t);
+    float* d_deltas = reinterpret_cast<float*>(base + b_q + b_r + b_t + b_o);
+    unsigned* d_err = reinterpret_cast<unsigned*>(base + b_q + b_r + b_t + b_o + b_d);
+    CG_CUDA(cudaMemcpyAsync(d_q, table.data(), sizeof(ShootQuery) * n, cudaMemcpyHostToDevice, s), "upload queries");
+    if (n_rays) {
+        CG_CUDA(cudaMemcpyAsync(d_rays, rays, sizeof(float) * 6 * n_rays, cudaMemcpyHostToDevice, s), "upload rays");
+        CG_CUDA(cudaMemcpyAsync(d_tags, tags.data(), sizeof(uint32_t) * n_rays, cudaMemcpyHostToDevice, s),
+                "upload ray tags");
+    }
+    CG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s), "clear flag");
+    ShootParams p{};
+    p.q = d_q;
+    p.n_queries = n;
+    p.n_rays = uint32_t(n_rays);
+    p.trees = c->d_trees;
+    p.recs = c->recs.ptr;
+    p.tris = c->tris.ptr;
+    p.rays = d_rays;
+    p.ray_query = d_tags;
+    p.out = d_out;
+    p.cos_start = std::cos(pr.smoothstep_start);  // the constructor's cosines (ShootUncollideRays.cpp:4-11)
+    p.cos_finish = std::cos(pr.smoothstep_finish);
+    p.bias = pr.distance_bias;
+    p.deltas = d_deltas;
+    p.error = d_err;
+    CG_CUDA(launch_shoot(p, s), "shoot kernels");
+    unsigned err = 0;
+    CG_CUDA(cudaMemcpyAsync(deltas, d_deltas, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s), "read deltas");
+    CG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read flag");
+    CG_CUDA(cudaStreamSynchronize(s), "shoot");
+    if (err) return fail(c, CG_ERR_QUEUE_OVERFLOW, "a tree is deeper than the ray traversal's stack");
     return CG_OK;
 }
 

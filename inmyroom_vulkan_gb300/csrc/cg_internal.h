@@ -320,6 +320,33 @@ cudaError_t launch_energy(const EnergyParams& p, uint32_t blocks, cudaStream_t s
 cudaError_t launch_energy_backward(const EnergyParams& p, uint32_t blocks, uint32_t max_vertices, cudaStream_t s);
 cudaError_t energy_occupancy(int* blocks_per_sm);
 
+// Uncollide-ray shooting (cg_shoot.cu).
+struct ShootQuery {
+    float relative[16];      // second entity's model space to the first's
+    float first_global[16];  // the first entity's world matrix (the delta's frame)
+    uint32_t tree_a, tree_b;
+    uint32_t ray_first, n_first, n_second;  // rays [ray_first, + n_first) from the first, then n_second
+    uint32_t pad[3];
+};
+struct ShootRayOut {  // a ray's pass and its reflection's: signed force and ray responses
+    float f1[3], r1[3], f2[3], r2[3];
+    uint32_t ok1, ok2;
+};
+struct ShootParams {
+    const ShootQuery* q;
+    uint32_t n_queries, n_rays;
+    const DevTree* trees;
+    const float4* recs;
+    const float4* tris;
+    const float* rays;          // [n_rays][6] origin, direction (the first entity's space)
+    const uint32_t* ray_query;  // per ray: query | (from the second entity) << 31
+    ShootRayOut* out;
+    float cos_start, cos_finish, bias;
+    float* deltas;              // [n_queries][3]
+    unsigned* error;            // ERR_QUEUE when a tree is deeper than the traversal stack
+};
+cudaError_t launch_shoot(const ShootParams& p, cudaStream_t s);
+
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,
                         PackedQuery* out, Counters* ctr, uint4* leaf_list, uint32_t leaf_cap, cudaStream_t s);

@@ -1,0 +1,384 @@
+// Uncollide-ray shooting: ShootUncollideRays::ExecuteShootUncollideRays
+// (src/CollisionDetection/ShootUncollideRays.cpp:14-180) for a batch of entity
+// pairs, over Ray::IntersectOBBtree closest-hit traversals
+// (src/Geometry/Ray.cpp:36-237).
+//
+//   shoot_ray_kernel    a thread per ray: the Hermann pass of the ray (the
+//                       closest hit on the other tree, a back face, no nearer
+//                       hit on its own tree from the origin moved by 4 ulps),
+//                       and when it succeeds the pass of its reflection back;
+//                       each success as (signed force response, signed ray
+//                       response)
+//   shoot_query_kernel  a thread per pair: the force responses summed in the
+//                       reference's order (rays from the first entity, each
+//                       followed by its reflection, then those from the
+//                       second), FindResponse over the ray responses, the
+//                       delta in world space
+// Every step rounds where the reference rounds (built without contraction,
+// IEEE division and square root), so the deltas are the reference's bits for
+// the same rays in the same order. The ray/triangle test is the one the glm
+// shim states for the reference's glm fork (Moller-Trumbore, two-sided, back
+// face = negative determinant).
+//
+// The traversal keeps the recursion's order with an explicit stack: of two
+// children whose slabs the ray enters, the nearer entry first (ties: the
+// right child), each visited only if its entry is before the best hit so far
+// (checked when it is taken from the stack, as the recursion checks the
+// second child after the first's subtree) and its exit is not behind the ray.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+
+#include "cg_device.cuh"
+#include "cg_internal.h"
+
+namespace cg {
+
+namespace {
+
+constexpr uint32_t kShootStack = 96;  // deferred boxes per ray (a tree deeper than this reports ERR_QUEUE)
+
+struct Slab {
+    bool hit;
+    float tmin, tmax;
+};
+
+// Ray::IntersectParalgram (Ray.cpp:36-133) for a ray from the origin.
+__device__ __forceinline__ Slab ray_box(const Box& b, float3 dir) {
+    float mn = -__int_as_float(0x7f800000), mx = __int_as_float(0x7f800000);
+    const float3 ro = sub3(make_float3(0.f, 0.f, 0.f), b.c);
+    const float3 fa[3] = {b.v, b.w, b.u}, fb[3] = {b.w, b.u, b.v}, side[3] = {b.u, b.v, b.w};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float3 pd = normalize3(cross3(fa[k], fb[k]));
+        const float d = -fabsf(dot3(pd, side[k]));
+        const float pc = dot3(pd, ro);
+        const float n1 = pc + d;
+        const float n2 = -pc + d;
+        const float vd = dot3(pd, dir);
+        if (fabsf(vd) >= FLT_EPSILON) {
+            const float inv = 1.f / vd;
+            float t1 = -n1 * inv;
+            float t2 = n2 * inv;
+            if (t1 > t2) {
+                const float t = t1;
+                t1 = t2;
+                t2 = t;
+            }
+            mn = (t1 < mn) ? mn : t1;
+            mx = (mx < t2) ? mx : t2;
+            if (mn > mx || mx < 0.f) return Slab{false, 0.f, 0.f};
+        } else if (n1 > 0.f || n2 > 0.f) {
+            return Slab{false, 0.f, 0.f};
+        }
+    }
+    return Slab{true, mn, mx};
+}
+
+// The glm fork's intersectRayTriangle as the shim states it (Ray.cpp:22-33).
+__device__ __forceinline__ bool ray_tri(float3 orig, float3 dir, float3 v0, float3 v1, float3 v2, float& bx,
+                                        float& by, float& t, bool& back) {
+    const float3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
+    const float3 p = cross3(dir, e2);
+    const float det = dot3(e1, p);
+    back = det < 0.f;
+    if (fabsf(det) <= FLT_EPSILON) return false;
+    const float inv = 1.f / det;
+    const float3 s0 = sub3(orig, v0);
+    const float u = dot3(s0, p) * inv;
+    if (u < 0.f || u > 1.f) return false;
+    const float3 q = cross3(s0, e1);
+    const float v = dot3(dir, q) * inv;
+    if (v < 0.f || u + v > 1.f) return false;
+    const float tt = dot3(e2, q) * inv;
+    if (tt < 0.f) return false;
+    bx = u;
+    by = v;
+    t = tt;
+    return true;
+}
+
+struct TreeHit {
+    bool hit, back;
+    float dist;
+    uint32_t tri;  // arena index
+    float bx, by;
+};
+
+__device__ __forceinline__ void rec_box(const float4* recs, uint32_t r, Box& b, uint32_t& ref, uint32_t& meta) {
+    const float4* p = recs + 4ull * r;
+    const float4 a = __ldg(p), c1 = __ldg(p + 1), c2 = __ldg(p + 2), d = __ldg(p + 3);
+    b.c = make_float3(a.x, a.y, a.z);
+    b.u = make_float3(a.w, c1.x, c1.y);
+    b.v = make_float3(c1.z, c1.w, c2.x);
+    b.w = make_float3(c2.y, c2.z, c2.w);
+    ref = __float_as_uint(d.x);
+    meta = __float_as_uint(d.y);
+}
+
+// Ray::IntersectOBBtree (Ray.cpp:135-237) on the tree rooted at record root.
+__device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t root, const Mat4& matrix, float3 origin,
+                            float3 dir, unsigned* error) {
+    Mat4 cm = matrix;
+    if (!(origin.x == 0.f && origin.y == 0.f && origin.z == 0.f))
+        cm.c3 = make_float4(matrix.c3.x - origin.x, matrix.c3.y - origin.y, matrix.c3.z - origin.z, matrix.c3.w - 0.f);
+    TreeHit best{false, false, __int_as_float(0x7f800000), 0xffffffffu, 0.f, 0.f};
+    uint32_t st_rec[kShootStack];
+    float st_min[kShootStack];
+    uint32_t sp = 0;
+    {
+        Box b;
+        uint32_t ref, meta;
+        rec_box(recs, root, b, ref, meta);
+        const Slab h = ray_box(xform_box(cm, b), dir);
+        if (h.hit && h.tmax >= 0.f) {
+            st_rec[0] = root;
+            st_min[0] = -__int_as_float(0x7f800000);  // the root is entered without the distance check
+            sp = 1;
+        }
+    }
+    const float3 zero = make_float3(0.f, 0.f, 0.f);
+    while (sp) {
+        --sp;
+        const uint32_t r = st_rec[sp];
+        if (!(st_min[sp] < best.dist)) continue;
+        Box nb;
+        uint32_t ref, meta;
+        rec_box(recs, r, nb, ref, meta);
+        if (!(meta & kLeafFlag)) {
+            Box lb, rb;
+            uint32_t lref, lmeta, rref, rmeta;
+            rec_box(recs, ref, lb, lref, lmeta);
+            rec_box(recs, ref + 1u, rb, rref, rmeta);
+            const Slab hl = ray_box(xform_box(cm, lb), dir);
+            const Slab hr = ray_box(xform_box(cm, rb), dir);
+            auto push = [&](uint32_t rec, const Slab& h) {
+                if (h.tmax < 0.f) return;  // the box is behind the ray
+                if (sp < kShootStack) {
+                    st_rec[sp] = rec;
+                    st_min[sp] = h.tmin;
+                    ++sp;
+                } else {
+                    atomicOr(error, ERR_QUEUE);
+                }
+            };
+            if (hl.hit && hr.hit) {
+                // the later one first, so that the nearer one is taken next
+                if (hl.tmin < hr.tmin) {
+                    push(ref + 1u, hr);
+                    push(ref, hl);
+                } else {
+                    push(ref, hl);
+                    push(ref + 1u, hr);
+                }
+            } else if (hl.hit) {
+                push(ref, hl);
+            } else if (hr.hit) {
+                push(ref + 1u, hr);
+            }
+            continue;
+        }
+        const uint32_t n = meta & 0xffffu;
+        for (uint32_t i = ref; i != ref + n; ++i) {
+            const float4* t4 = tris + 3ull * i;
+            const float4 q0 = __ldg(t4), q1 = __ldg(t4 + 1), q2 = __ldg(t4 + 2);
+            const float3 p0 = xform(cm, make_float3(q0.x, q0.y, q0.z), 1.0f);
+            const float3 p1 = xform(cm, make_float3(q1.x, q1.y, q1.z), 1.0f);
+            const float3 p2 = xform(cm, make_float3(q2.x, q2.y, q2.z), 1.0f);
+            float bx = 0.f, by = 0.f, t = 0.f;
+            bool back = false;
+            const bool hit = ray_tri(zero, dir, p0, p1, p2, bx, by, t, back);
+            if (hit && t > 0.f && t < best.dist) {
+                best.hit = true;
+                best.back = back;
+                best.dist = t;
+                best.tri = i;
+                best.bx = bx;
+                best.by = by;
+            }
+        }
+    }
+    return best;
+}
+
+struct Mat3s {
+    float3 c0, c1, c2;
+};
+__device__ __forceinline__ Mat3s cofactor(const Mat4& M) {
+    const float m00 = M.c0.x, m01 = M.c0.y, m02 = M.c0.z;  // m<column><row>
+    const float m10 = M.c1.x, m11 = M.c1.y, m12 = M.c1.z;
+    const float m20 = M.c2.x, m21 = M.c2.y, m22 = M.c2.z;
+    Mat3s R;
+    R.c0 = make_float3(m11 * m22 - m21 * m12, m20 * m12 - m10 * m22, m10 * m21 - m20 * m11);
+    R.c1 = make_float3(m21 * m02 - m01 * m22, m00 * m22 - m20 * m02, m20 * m01 - m00 * m21);
+    R.c2 = make_float3(m01 * m12 - m11 * m02, m10 * m02 - m00 * m12, m00 * m11 - m10 * m01);
+    return R;
+}
+__device__ __forceinline__ float3 mul3s(const Mat3s& N, float3 v) {
+    return make_float3((N.c0.x * v.x + N.c1.x * v.y) + N.c2.x * v.z, (N.c0.y * v.x + N.c1.y * v.y) + N.c2.y * v.z,
+                       (N.c0.z * v.x + N.c1.z * v.y) + N.c2.z * v.z);
+}
+
+__device__ __forceinline__ float3 add3s(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 scale3s(float s, float3 v) { return make_float3(s * v.x, s * v.y, s * v.z); }
+__device__ __forceinline__ float3 neg3(float3 v) { return make_float3(-v.x, -v.y, -v.z); }
+
+struct Side {
+    uint32_t root;      // root record
+    uint32_t tri_base;
+    const float* nrm;   // per-vertex normals [n_tris][9], or null (face normal)
+    Mat4 m;
+};
+
+struct Pass {
+    bool ok;
+    float3 response, normal;
+};
+
+// ShootUncollideRays::HermannPass (ShootUncollideRays.cpp:127-158).
+__device__ Pass hermann(const ShootParams& P, const Side& A, const Side& B, const Mat3s& nb, float3 o, float3 d) {
+    Pass r{false, make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+    const TreeHit p2 = ray_tree(P.recs, P.tris, B.root, B.m, o, d, P.error);
+    if (!(p2.hit && p2.back)) return r;
+    // Ray::MoveOriginEpsilonTowardsDirection(4) (Ray.cpp:13-20)
+    const float big = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+    const float eps = big * FLT_EPSILON;
+    const float3 moved = add3s(o, scale3s(4.f * eps, d));
+    const float eps_dist = length3(sub3(moved, o));
+    const TreeHit p3 = ray_tree(P.recs, P.tris, A.root, A.m, moved, d, P.error);
+    if (p2.dist <= p3.dist + eps_dist) {
+        r.ok = true;
+        r.response = scale3s(p2.dist, d);
+        // TriangleNormal::GetNormal(bary, matrix) (Triangle.cpp:197-204)
+        float3 n0, n1, n2;
+        const uint32_t local = p2.tri - B.tri_base;
+        if (B.nrm) {
+            const float* nn = B.nrm + 9ull * local;
+            n0 = make_float3(nn[0], nn[1], nn[2]);
+            n1 = make_float3(nn[3], nn[4], nn[5]);
+            n2 = make_float3(nn[6], nn[7], nn[8]);
+        } else {
+            const float4* t4 = P.tris + 3ull * p2.tri;
+            const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
+            n0 = n1 = n2 = normalize3(cross3(sub3(make_float3(b.x, b.y, b.z), make_float3(a.x, a.y, a.z)),
+                                             sub3(make_float3(c.x, c.y, c.z), make_float3(a.x, a.y, a.z))));
+        }
+        const float b0 = (1.f - p2.bx) - p2.by;
+        const float3 n = add3s(add3s(scale3s(b0, n0), scale3s(p2.bx, n1)), scale3s(p2.by, n2));
+        r.normal = normalize3(mul3s(nb, n));
+    }
+    return r;
+}
+
+// ShootUncollideRays::CalcForceResponse (ShootUncollideRays.cpp:116-125).
+__device__ __forceinline__ float3 force_response(const Pass& h) {
+    const float3 dir = normalize3(h.response);
+    const float len = length3(h.response);
+    const float c = dot3(h.normal, dir);
+    return scale3s(c * c * len, dir);
+}
+
+__device__ __forceinline__ void put3(float* p, float3 v) {
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+__device__ __forceinline__ float3 get3(const float* p) { return make_float3(p[0], p[1], p[2]); }
+
+__device__ __forceinline__ Mat4 mat_of(const float* m) {
+    return Mat4{make_float4(m[0], m[1], m[2], m[3]), make_float4(m[4], m[5], m[6], m[7]),
+                make_float4(m[8], m[9], m[10], m[11]), make_float4(m[12], m[13], m[14], m[15])};
+}
+
+__global__ void __launch_bounds__(128) shoot_ray_kernel(const ShootParams P) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n_rays) return;
+    const uint32_t tag = P.ray_query[i];
+    const uint32_t qi = tag & 0x7fffffffu;
+    const bool from_second = (tag >> 31) != 0;
+    const ShootQuery& Q = P.q[qi];
+    const DevTree& TA = P.trees[Q.tree_a];
+    const DevTree& TB = P.trees[Q.tree_b];
+    const Mat4 M = mat_of(Q.relative);
+    const Mat4 I = Mat4{make_float4(1.f, 0.f, 0.f, 0.f), make_float4(0.f, 1.f, 0.f, 0.f), make_float4(0.f, 0.f, 1.f, 0.f),
+                        make_float4(0.f, 0.f, 0.f, 1.f)};
+    const Mat3s N = cofactor(M);
+    const Mat3s I3 = Mat3s{make_float3(1.f, 0.f, 0.f), make_float3(0.f, 1.f, 0.f), make_float3(0.f, 0.f, 1.f)};
+    const Side first{TA.rec_base + 1u, TA.tri_base, TA.nrm, I};
+    const Side second{TB.rec_base + 1u, TB.tri_base, TB.nrm, M};
+    const float* ray = P.rays + 6ull * i;
+    const float3 o = get3(ray), d = get3(ray + 3);
+    ShootRayOut out;
+    out.ok1 = out.ok2 = 0u;
+    // first to second: the pass against the second entity (force subtracted,
+    // response negated); second to first: against the first entity
+    auto pass = [&](bool to_first, float3 po, float3 pd, float* f, float* rr) -> Pass {
+        const Pass h = to_first ? hermann(P, second, first, I3, po, pd) : hermann(P, first, second, N, po, pd);
+        if (h.ok) {
+            const float3 fr = force_response(h);
+            put3(f, to_first ? fr : neg3(fr));
+            put3(rr, to_first ? h.response : neg3(h.response));
+        }
+        return h;
+    };
+    const Pass h1 = pass(from_second, o, d, out.f1, out.r1);
+    if (h1.ok) {
+        out.ok1 = 1u;
+        // ShootUncollideRays::ReflectHermannResult (ShootUncollideRays.cpp:100-106)
+        const float3 ro = add3s(o, h1.response), rd = neg3(h1.normal);
+        const Pass h2 = pass(!from_second, ro, rd, out.f2, out.r2);
+        out.ok2 = h2.ok ? 1u : 0u;
+    }
+    P.out[i] = out;
+}
+
+// ShootUncollideRays::SmootherStep (ShootUncollideRays.cpp:175-179).
+__device__ __forceinline__ float smoother_step(float a, float b, float x) {
+    float v = (x - a) / (b - a);
+    v = (v < 0.f) ? 0.f : ((1.f < v) ? 1.f : v);
+    return v * v * v * (v * (v * 6.f - 15.f) + 10.f);
+}
+
+__global__ void shoot_query_kernel(const ShootParams P) {
+    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= P.n_queries) return;
+    const ShootQuery& Q = P.q[qi];
+    const uint32_t r0 = Q.ray_first, r1 = Q.ray_first + Q.n_first + Q.n_second;
+    float3 avg = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t i = r0; i < r1; ++i) {
+        const ShootRayOut& o = P.out[i];
+        if (o.ok1) avg = add3s(avg, get3(o.f1));
+        if (o.ok2) avg = add3s(avg, get3(o.f2));
+    }
+    float3 delta = make_float3(0.f, 0.f, 0.f);
+    if (avg.x != 0.f || avg.y != 0.f || avg.z != 0.f) {
+        const float3 nf = normalize3(avg);
+        float max_len = 0.f;
+        auto one = [&](float3 r) {
+            const float3 nr = normalize3(r);
+            const float dt = dot3(nr, nf);
+            const float len = length3(r);
+            const float need = len / dt;
+            const float x = smoother_step(P.cos_finish, P.cos_start, dt) * need;
+            max_len = (max_len < x) ? x : max_len;
+        };
+        for (uint32_t i = r0; i < r1; ++i) {
+            const ShootRayOut& o = P.out[i];
+            if (o.ok1) one(get3(o.r1));
+            if (o.ok2) one(get3(o.r2));
+        }
+        const float3 local = scale3s(P.bias, scale3s(max_len, nf));
+        delta = xform(mat_of(Q.first_global), local, 0.f);
+    }
+    put3(P.deltas + 3ull * qi, delta);
+}
+
+}  // namespace
+
+cudaError_t launch_shoot(const ShootParams& p, cudaStream_t s) {
+    if (p.n_rays) shoot_ray_kernel<<<(p.n_rays + 127u) / 128u, 128, 0, s>>>(p);
+    if (p.n_queries) shoot_query_kernel<<<(p.n_queries + 127u) / 128u, 128, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace cg

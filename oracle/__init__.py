@@ -69,6 +69,7 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
     f("obb_from_points").argtypes = [_f32p, sz, _f32p]
     f("eig3").argtypes = [_f64p, _f64p, _f64p]
     f("rays").argtypes = [vp, _f32p, _f32p, sz, sz, C.POINTER(sz), _f32p]
+    f("shoot_rays").argtypes = [vp, vp, _f32p, _f32p, _f32p, sz, _f32p, sz, vp, _f32p]
     if prefix == "ref_":
         f("narrow").restype = sz
         f("narrow").argtypes = [vp, _u32p, _f32p, sz, C.POINTER(C.c_uint64)]
@@ -332,6 +333,22 @@ class Impl:
         hits = C.c_uint64()
         tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(hits), C.byref(rays))
         return dict(tests=tests, hits=hits.value, rays=rays.value)
+
+    def shoot_rays(self, ta: "Tree", tb: "Tree", ga, gb, rays_a, rays_b, params=None) -> np.ndarray:
+        """ShootUncollideRays::ExecuteShootUncollideRays for one pair: the
+        first entity's world-space delta. rays_*: (n, 6) origin + direction in
+        the first entity's space; params (start, finish angle in radians,
+        bias) or the engine's settings."""
+        ra = np.ascontiguousarray(np.asarray(rays_a, np.float32).reshape(-1, 6))
+        rb = np.ascontiguousarray(np.asarray(rays_b, np.float32).reshape(-1, 6))
+        out = np.zeros(3, np.float32)
+        pr = None
+        if params is not None:
+            pr = np.ascontiguousarray(params, np.float32)
+        self.fn("shoot_rays")(ta.h, tb.h, _f32(ga), _f32(gb), ra if len(ra) else np.zeros((1, 6), np.float32),
+                              len(ra), rb if len(rb) else np.zeros((1, 6), np.float32), len(rb),
+                              pr.ctypes.data if pr is not None else None, out)
+        return out
 
     def collide_pairs(self, trees_a, trees_b, mats_a, mats_b):
         """(port) all colliding pairs of a batch: (n,3) [query, ia, ib], (n,6) segs, tests, leaf pairs."""

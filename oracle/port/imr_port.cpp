@@ -775,6 +775,238 @@ void run_query(const Tree& A, const Tree& B, const M4& ma, const M4& mb, Query& 
     q.avg_b = xform(inverse(M), avg, 1.0f);
 }
 
+// ------------------------------------------------------ ray shooting ----
+// Ray::IntersectParalgram (Ray.cpp:36-133): Haines' slab test against the
+// box's three face-plane pairs, the ray starting at the origin (the tree is
+// moved so, Ray.cpp:150-157).
+struct Slab {
+    bool hit;
+    float tmin, tmax;
+};
+inline Slab ray_box(const Box& b, V3 dir) {
+    float mn = -std::numeric_limits<float>::infinity();
+    float mx = std::numeric_limits<float>::infinity();
+    const V3 ro = sub(V3{0.f, 0.f, 0.f}, b.c);
+    const V3 fa[3] = {b.v, b.w, b.u}, fb[3] = {b.w, b.u, b.v}, side[3] = {b.u, b.v, b.w};
+    for (int k = 0; k < 3; ++k) {
+        const V3 pd = normalize(cross(fa[k], fb[k]));
+        const float d = -std::fabs(dot(pd, side[k]));
+        const float pc = dot(pd, ro);
+        const float n1 = pc + d;
+        const float n2 = -pc + d;
+        const float vd = dot(pd, dir);
+        if (std::fabs(vd) >= std::numeric_limits<float>::epsilon()) {
+            const float inv = 1.f / vd;
+            float t1 = -n1 * inv;
+            float t2 = n2 * inv;
+            if (t1 > t2) std::swap(t1, t2);
+            mn = (t1 < mn) ? mn : t1;  // std::max(t1, mn)
+            mx = (mx < t2) ? mx : t2;  // std::min(t2, mx)
+            if (mn > mx || mx < 0.f) return Slab{false, 0.f, 0.f};
+        } else if (n1 > 0 || n2 > 0) {
+            return Slab{false, 0.f, 0.f};
+        }
+    }
+    return Slab{true, mn, mx};
+}
+
+// The ray/triangle test the reference calls through its glm fork
+// (Ray.cpp:22-33), as the glm shim states it: Moller-Trumbore, two-sided,
+// reporting a back-face hit (a negative determinant).
+inline bool ray_tri(V3 orig, V3 dir, V3 v0, V3 v1, V3 v2, float& bx, float& by, float& t, bool& back) {
+    const V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    const V3 p = cross(dir, e2);
+    const float det = dot(e1, p);
+    back = det < 0.f;
+    if (std::fabs(det) <= std::numeric_limits<float>::epsilon()) return false;
+    const float inv = 1.f / det;
+    const V3 s0 = sub(orig, v0);
+    const float u = dot(s0, p) * inv;
+    if (u < 0.f || u > 1.f) return false;
+    const V3 q = cross(s0, e1);
+    const float v = dot(dir, q) * inv;
+    if (v < 0.f || u + v > 1.f) return false;
+    const float tt = dot(e2, q) * inv;
+    if (tt < 0.f) return false;
+    bx = u;
+    by = v;
+    t = tt;
+    return true;
+}
+
+// RayOBBtreeIntersectInfo (Ray.h:17-24).
+struct TreeHit {
+    bool hit = false, back = false;
+    float dist = std::numeric_limits<float>::infinity();
+    uint32_t tri = ~0u;
+    float bx = 0.f, by = 0.f;
+};
+
+// Ray::IntersectOBBtreeRecursive (Ray.cpp:161-237): both children's slabs,
+// the nearer entry first (ties: the right child first), a child visited when
+// its entry is before the best hit so far and its exit not behind the ray.
+void ray_tree_rec(const Tree& T, const Traveler& tr, const M4& cm, V3 dir, TreeHit& best) {
+    if (!tr.leaf) {
+        const Traveler L = child(T, tr, 0), R = child(T, tr, 1);
+        const Slab hl = ray_box(xform_box(cm, *L.box), dir);
+        const Slab hr = ray_box(xform_box(cm, *R.box), dir);
+        auto visit = [&](const Traveler& c, const Slab& h) {
+            if (h.tmin < best.dist && h.tmax >= 0.f) ray_tree_rec(T, c, cm, dir, best);
+        };
+        if (hl.hit && hr.hit) {
+            if (hl.tmin < hr.tmin) {
+                visit(L, hl);
+                visit(R, hr);
+            } else {
+                visit(R, hr);
+                visit(L, hl);
+            }
+        } else if (hl.hit) {
+            visit(L, hl);
+        } else if (hr.hit) {
+            visit(R, hr);
+        }
+        return;
+    }
+    for (uint32_t i = tr.off; i != tr.off + tr.cnt; ++i) {
+        V3 p[3];
+        xform_tri(cm, T.tris[i], p);
+        float bx = 0.f, by = 0.f, t = 0.f;
+        bool back = false;
+        const bool hit = ray_tri(V3{0.f, 0.f, 0.f}, dir, p[0], p[1], p[2], bx, by, t, back);
+        if (hit && t > 0.f && t < best.dist) {
+            best.hit = true;
+            best.back = back;
+            best.dist = t;
+            best.tri = i;
+            best.bx = bx;
+            best.by = by;
+        }
+    }
+}
+
+// Ray::IntersectOBBtree (Ray.cpp:135-159): the tree moved so that the ray
+// starts at the origin, then the root's slab.
+TreeHit ray_tree(const Tree& T, const M4& matrix, V3 origin, V3 dir) {
+    M4 cm = matrix;
+    if (!(origin.x == 0.f && origin.y == 0.f && origin.z == 0.f)) {
+        cm.m[12] = matrix.m[12] - origin.x;
+        cm.m[13] = matrix.m[13] - origin.y;
+        cm.m[14] = matrix.m[14] - origin.z;
+        cm.m[15] = matrix.m[15] - 0.f;
+    }
+    TreeHit best;
+    const Traveler root = root_traveler(T);
+    const Slab h = ray_box(xform_box(cm, *root.box), dir);
+    if (h.hit && h.tmax >= 0.f) ray_tree_rec(T, root, cm, dir, best);
+    return best;
+}
+
+inline M4 identity4() {
+    M4 m{};
+    m.m[0] = m.m[5] = m.m[10] = m.m[15] = 1.f;
+    return m;
+}
+inline M3 identity3() {
+    M3 m{};
+    m.m[0] = m.m[4] = m.m[8] = 1.f;
+    return m;
+}
+
+// ShootUncollideRays::HermannPass (ShootUncollideRays.cpp:127-158).
+struct Hermann {
+    bool ok = false;
+    V3 response{}, normal{};
+};
+Hermann hermann_pass(const Tree& A, const Tree& B, const M4& ma, const M4& mb, const M3& nb, const Ray& ray) {
+    Hermann r;
+    const TreeHit p2 = ray_tree(B, mb, ray.o, ray.d);
+    if (!(p2.hit && p2.back)) return r;
+    // Ray::MoveOriginEpsilonTowardsDirection(4) (Ray.cpp:13-20)
+    const float big = std::max({std::fabs(ray.o.x), std::fabs(ray.o.y), std::fabs(ray.o.z)});
+    const float eps = big * std::numeric_limits<float>::epsilon();
+    const V3 moved = add(ray.o, scale(4.f * eps, ray.d));
+    const float eps_dist = length(sub(moved, ray.o));
+    const TreeHit p3 = ray_tree(A, ma, moved, ray.d);
+    if (p2.dist <= p3.dist + eps_dist) {
+        r.ok = true;
+        r.response = scale(p2.dist, ray.d);
+        // TriangleNormal::GetNormal(bary, matrix) (Triangle.cpp:197-204)
+        const Tri& tr = B.tris[p2.tri];
+        const float b0 = (1.f - p2.bx) - p2.by;
+        const V3 n = add(add(scale(b0, tr.n[0]), scale(p2.bx, tr.n[1])), scale(p2.by, tr.n[2]));
+        r.normal = normalize(mul3(nb, n));
+    }
+    return r;
+}
+
+// ShootUncollideRays::CalcForceResponse (ShootUncollideRays.cpp:116-125).
+inline V3 force_response(const Hermann& h) {
+    const V3 dir = normalize(h.response);
+    const float len = length(h.response);
+    const float c = dot(h.normal, dir);
+    return scale(c * c * len, dir);
+}
+
+// ShootUncollideRays::SmootherStep (ShootUncollideRays.cpp:175-179).
+inline float smoother_step(float a, float b, float x) {
+    float v = (x - a) / (b - a);
+    v = (v < 0.f) ? 0.f : ((1.f < v) ? 1.f : v);  // std::clamp(v, 0, 1)
+    return v * v * v * (v * (v * 6 - 15) + 10);
+}
+
+struct ShootParams {
+    float cos_start, cos_finish, bias;
+};
+
+// ShootUncollideRays::ExecuteShootUncollideRays (ShootUncollideRays.cpp:14-98)
+// with FindResponse (:160-173): the world-space delta for the first entity.
+V3 shoot(const Tree& A, const Tree& B, const M4& ga, const M4& gb, const std::vector<Ray>& rays_a,
+         const std::vector<Ray>& rays_b, const ShootParams& P) {
+    const M4 M = relative(ga, gb);
+    const M3 N = cofactor3(M);
+    const M4 I = identity4();
+    const M3 I3 = identity3();
+    V3 avg{0.f, 0.f, 0.f};
+    std::vector<V3> responses;
+    auto reflect = [](const Hermann& h, const Ray& ray) { return Ray{add(ray.o, h.response), neg(h.normal)}; };
+    auto first_to_second = [&](const Ray& ray, Ray& out) {
+        const Hermann h = hermann_pass(A, B, I, M, N, ray);
+        if (!h.ok) return false;
+        avg = sub(avg, force_response(h));
+        responses.push_back(neg(h.response));
+        out = reflect(h, ray);
+        return true;
+    };
+    auto second_to_first = [&](const Ray& ray, Ray& out) {
+        const Hermann h = hermann_pass(B, A, M, I, I3, ray);
+        if (!h.ok) return false;
+        avg = add(avg, force_response(h));
+        responses.push_back(h.response);
+        out = reflect(h, ray);
+        return true;
+    };
+    Ray r1, r2;
+    for (const Ray& ray : rays_a)
+        if (first_to_second(ray, r1)) second_to_first(r1, r2);
+    for (const Ray& ray : rays_b)
+        if (second_to_first(ray, r1)) first_to_second(r1, r2);
+    if (avg.x == 0.f && avg.y == 0.f && avg.z == 0.f) return V3{0.f, 0.f, 0.f};
+    const V3 nf = normalize(avg);
+    float max_len = 0.f;
+    for (const V3& r : responses) {
+        const V3 nr = normalize(r);
+        const float dt = dot(nr, nf);
+        const float len = length(r);
+        const float need = len / dt;
+        const float sm = smoother_step(P.cos_finish, P.cos_start, dt);
+        const float x = sm * need;
+        max_len = (max_len < x) ? x : max_len;  // std::max(max_len, x)
+    }
+    const V3 local = scale(P.bias, scale(max_len, nf));
+    return xform(ga, local, 0.f);
+}
+
 }  // namespace port
 
 // ================================================================ C ABI ====
@@ -1172,6 +1404,28 @@ void port_tree_refit(size_t n_nodes, const uint32_t* node_ref, const uint32_t* n
     }
     const std::pair<uint32_t, uint32_t> root = n_nodes ? rg[0] : std::make_pair(0u, uint32_t(n_tris));
     stbox(fit_range(root.first, root.second), out_root12);
+}
+
+
+// ShootUncollideRays::ExecuteShootUncollideRays for one entity pair with the
+// engine's settings (CollisionDetection.cpp:22-24: 40 and 65 degrees, 1.01)
+// unless params (start angle, finish angle in radians, bias) is given; rays
+// as (origin, direction) sextuples in the first entity's space.
+void port_shoot_rays(void* ta, void* tb, const float* ga16, const float* gb16, const float* rays_a, size_t n_a,
+                     const float* rays_b, size_t n_b, const float* params, float* out3) {
+    auto load = [](const float* r, size_t n) {
+        std::vector<Ray> v(n);
+        for (size_t i = 0; i < n; ++i) v[i] = Ray{ld3(r + 6 * i), ld3(r + 6 * i + 3)};
+        return v;
+    };
+    const float deg = 0.01745329251994329576923690768489f;
+    ShootParams P;
+    P.cos_start = std::cos(params ? params[0] : 40.f * deg);
+    P.cos_finish = std::cos(params ? params[1] : 65.f * deg);
+    P.bias = params ? params[2] : 1.01f;
+    const V3 r = shoot(*static_cast<Tree*>(ta), *static_cast<Tree*>(tb), ldm(ga16), ldm(gb16), load(rays_a, n_a),
+                       load(rays_b, n_b), P);
+    st3(r, out3);
 }
 
 }  // extern "C"

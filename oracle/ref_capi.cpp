@@ -12,6 +12,7 @@
 
 #include "CollisionDetection/CreateUncollideRays.h"
 #include "CollisionDetection/OBBtreesCollision.h"
+#include "CollisionDetection/ShootUncollideRays.h"
 #include "Geometry/OBBtree.h"
 #include "Geometry/Paralgram.h"
 #include "Geometry/Triangle.h"
@@ -335,6 +336,32 @@ uint64_t ref_collide_batch(void* const* trees_a, void* const* trees_b, const flo
     }
     if (n_rays) *n_rays = total_rays;
     return total;
+}
+
+// ShootUncollideRays::ExecuteShootUncollideRays for one entity pair, built
+// with the engine's settings (CollisionDetection.cpp:22-24) or params (start
+// and finish angle in radians, bias); rays as (origin, direction) sextuples.
+void ref_shoot_rays(void* ta, void* tb, const float* ga16, const float* gb16, const float* rays_a, size_t n_a,
+                    const float* rays_b, size_t n_b, const float* params, float* out3) {
+    CDentriesUncollideRays u;
+    u.firstEntry.currentGlobalMatrix = u.firstEntry.previousGlobalMatrix = load_mat(ga16);
+    u.firstEntry.OBBtree_ptr = static_cast<const OBBtree*>(ta);
+    u.firstEntry.shouldCallback = true;
+    u.firstEntry.entity = 0;
+    u.secondEntry.currentGlobalMatrix = u.secondEntry.previousGlobalMatrix = load_mat(gb16);
+    u.secondEntry.OBBtree_ptr = static_cast<const OBBtree*>(tb);
+    u.secondEntry.shouldCallback = true;
+    u.secondEntry.entity = 1;
+    auto load = [](const float* r, size_t n, std::vector<Ray>& out) {
+        for (size_t i = 0; i < n; ++i)
+            out.emplace_back(glm::vec3(r[6 * i], r[6 * i + 1], r[6 * i + 2]),
+                             glm::vec3(r[6 * i + 3], r[6 * i + 4], r[6 * i + 5]));
+    };
+    load(rays_a, n_a, u.rays_from_first_to_second);
+    load(rays_b, n_b, u.rays_from_second_to_first);
+    const ShootUncollideRays shooter = params ? ShootUncollideRays(params[0], params[1], params[2])
+                                              : ShootUncollideRays(glm::radians(40.f), glm::radians(65.f), 1.01f);
+    put_vec(shooter.ExecuteShootUncollideRays(u), out3);
 }
 
 }  // extern "C"

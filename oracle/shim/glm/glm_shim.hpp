@@ -46,7 +46,9 @@ template <class T> struct tvec3 {
     constexpr tvec3(T a, T b, T c) : x(a), y(b), z(c) {}
     template <class U> constexpr tvec3(const tvec3<U>& o)
         : x(static_cast<T>(o.x)), y(static_cast<T>(o.y)), z(static_cast<T>(o.z)) {}
-    template <class U> constexpr explicit tvec3(const tvec4<U>& o)
+    // implicit, as glm's own (no GLM_FORCE_EXPLICIT_CTOR): the reference
+    // returns a vec4 where a vec3 is expected (ShootUncollideRays.cpp:94)
+    template <class U> constexpr tvec3(const tvec4<U>& o)
         : x(static_cast<T>(o.x)), y(static_cast<T>(o.y)), z(static_cast<T>(o.z)) {}
     T& operator[](std::size_t i) { return i == 0 ? x : (i == 1 ? y : z); }
     const T& operator[](std::size_t i) const { return i == 0 ? x : (i == 1 ? y : z); }

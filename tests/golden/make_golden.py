@@ -92,6 +92,23 @@ def box_cases(rng):
     return np.array(A), np.array(B)
 
 
+def shoot_fixture(R):
+    """ShootUncollideRays::ExecuteShootUncollideRays on the rigid_small poses
+    with the reference's own rays of each pose (in its order)."""
+    g = np.load(os.path.join(HERE, "rigid_small.npz"))
+
+    def tree(tag):
+        return R.tree_build(g[f"points_{tag}"], g[f"indices_{tag}"], g[f"normals_{tag}"])
+
+    ta, tb = tree("a"), tree("b")
+    deltas = []
+    for k in range(len(g["mats_a"])):
+        ra = g["rays_a"][g["rays_a"][:, 0] == k, 1:]
+        rb = g["rays_b"][g["rays_b"][:, 0] == k, 1:]
+        deltas.append(R.shoot_rays(ta, tb, g["mats_a"][k], g["mats_b"][k], ra, rb))
+    np.savez_compressed(os.path.join(HERE, "shoot_small.npz"), deltas=np.array(deltas, np.float32))
+
+
 def main():
     R = oracle.ref()
     if R is None:
@@ -167,6 +184,7 @@ def main():
                rays_a=np.concatenate(rays_a), rays_b=np.concatenate(rays_b), avgs=np.array(avgs),
                tests=np.array(tests, np.uint64))
     np.savez_compressed(os.path.join(HERE, "rigid_small.npz"), **out)
+    shoot_fixture(R)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -126,3 +126,17 @@ def test_mid_and_narrow_phase_match_reference(port, rigid):
             key = lambda r: r[np.lexsort(bits(r).T[::-1])]  # noqa: E731
             assert np.array_equal(bits(key(got)), bits(key(want))), k
         np.testing.assert_allclose(avg, rigid["avgs"][k], rtol=1e-5, atol=1e-6)
+
+
+def test_shoot_rays_matches_reference(port):
+    """ShootUncollideRays::ExecuteShootUncollideRays on the rigid_small poses
+    with the reference's rays: the deltas bit for bit."""
+    g = load("rigid_small.npz")
+    want = load("shoot_small.npz")["deltas"]
+    ta = port.tree_build(g["points_a"], g["indices_a"], g["normals_a"])
+    tb = port.tree_build(g["points_b"], g["indices_b"], g["normals_b"])
+    for k in range(len(g["mats_a"])):
+        ra = g["rays_a"][g["rays_a"][:, 0] == k, 1:]
+        rb = g["rays_b"][g["rays_b"][:, 0] == k, 1:]
+        got = port.shoot_rays(ta, tb, g["mats_a"][k], g["mats_b"][k], ra, rb)
+        assert np.array_equal(bits(got), bits(want[k])), k

@@ -65,3 +65,20 @@ def test_batch_counts_match(port, ref):
     r1 = port.collide_batch([tp[i] for i in sc.pairs[:, 0]], [tp[j] for j in sc.pairs[:, 1]], ma, mb, threads=4)
     r2 = ref.collide_batch([tr[i] for i in sc.pairs[:, 0]], [tr[j] for j in sc.pairs[:, 1]], ma, mb, threads=4)
     assert r1["tests"] == r2["tests"] and r1["rays"] == r2["rays"]
+
+
+def test_shoot_rays_full_size(port, ref):
+    """ShootUncollideRays with the engine's settings and with others, on the
+    full rigid pair: port and reference give the same deltas, bit for bit."""
+    rp = scenes.rigid_pair(n_poses=30)
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in (rp.mesh_a, rp.mesh_b)]
+    tr = [ref.tree_build(m.points, m.indices, m.normals) for m in (rp.mesh_a, rp.mesh_b)]
+    moved = 0
+    for k in range(len(rp.mats_a)):
+        ra, rb, _ = port.mid_phase(tp[0], tp[1], rp.mats_a[k], rp.mats_b[k]).rays()
+        for params in (None, np.array([0.3, 1.2, 1.5], np.float32)):
+            a = port.shoot_rays(tp[0], tp[1], rp.mats_a[k], rp.mats_b[k], ra, rb, params)
+            b = ref.shoot_rays(tr[0], tr[1], rp.mats_a[k], rp.mats_b[k], ra, rb, params)
+            assert np.array_equal(bits(a), bits(b)), (k, a, b)
+            moved += int(np.any(a != 0))
+    assert moved > 30
