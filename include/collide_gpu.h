@@ -377,6 +377,24 @@ typedef struct cg_energy_side {
 int cg_energy_backward(cg_ctx* ctx, const double* d_grad_energy, const cg_energy_side* side_a,
                        const cg_energy_side* side_b, void* stream);
 
+/* ---- Broad phase ----
+ *
+ * SweepAndPrune::ExecuteSweepAndPrune (src/CollisionDetection/SweepAndPrune.cpp:
+ * 15-88) for n entities: the pairs whose world root boxes
+ * (global * root OBB) project onto each of the three axes as overlapping
+ * closed intervals, where at least one entity calls back, as (the entity
+ * whose projection starts earlier on U, the other; equal starts: the lower
+ * index first). axes: U, V, W (9 floats) or NULL for the engine's
+ * (CollisionDetection.cpp:9-13). Host arrays; callback may be NULL (all call
+ * back); synchronous. Pairs beyond cap are counted in *n_pairs, not written
+ * (then CG_ERR_OUTPUT_OVERFLOW). */
+typedef struct cg_entity_pair {
+    uint32_t first, second;
+} cg_entity_pair;
+
+int cg_broad_phase(cg_ctx* ctx, const uint32_t* tree_ids, const float* globals, const uint8_t* callback, uint32_t n,
+                   const float* axes, cg_entity_pair* pairs, uint64_t cap, uint64_t* n_pairs);
+
 /* ---- Uncollide-ray shooting ----
  *
  * ShootUncollideRays::ExecuteShootUncollideRays

@@ -31,7 +31,8 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_traversal_time_ms", "cg_narrow_time_ms", "cg_read_trace", "cg_graph_capture", "cg_graph_launch",
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
            "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
-           "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays"]
+           "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays",
+           "cg_broad_phase"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -160,6 +161,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_tree_refit_batch.argtypes = [vp, vp, vp, vp, u32, vp]
     lib.cg_tree_download.argtypes = [vp, u32, vp, vp, u32, vp, u32]
     lib.cg_set_host_outputs.argtypes = [vp, vp, u64, vp, u64, vp, u64]
+    lib.cg_broad_phase.argtypes = [vp, vp, vp, vp, u32, vp, vp, u64, C.POINTER(u64)]
     lib.cg_shoot_params_default.argtypes = [C.POINTER(cg_shoot_params)]
     lib.cg_shoot_params_default.restype = None
     lib.cg_shoot_rays.argtypes = [vp, vp, u32, vp, u64, C.POINTER(cg_shoot_params), vp]
@@ -406,6 +408,23 @@ class Context:
         p, r, v = arg(pairs, TRI_PAIR_DTYPE), arg(rays, RAY_DTYPE), arg(averages, RAY_AVERAGE_DTYPE)
         self._check(self.lib.cg_set_host_outputs(self.h, p[0], p[1], r[0], r[1], v[0], v[1]), "cg_set_host_outputs")
         self._host_outputs = (pairs, rays, averages)
+
+    def broad_phase(self, tree_ids, globals_, callback=None, axes=None, cap: int | None = None) -> np.ndarray:
+        """cg_broad_phase: (k, 2) [first, second] entity indices (the engine's
+        axes unless axes (3, 3))."""
+        ids = np.ascontiguousarray(tree_ids, np.uint32)
+        n = len(ids)
+        g = np.ascontiguousarray(globals_, np.float32).reshape(n, 16)
+        cb = None if callback is None else np.ascontiguousarray(callback, np.uint8)
+        ax = None if axes is None else np.ascontiguousarray(axes, np.float32).reshape(9)
+        cap = n * (n - 1) // 2 if cap is None else cap
+        out = np.zeros((max(cap, 1), 2), np.uint32)
+        cnt = C.c_uint64()
+        rc = self.lib.cg_broad_phase(self.h, ids.ctypes.data if n else None, g.ctypes.data if n else None,
+                                     cb.ctypes.data if cb is not None else None, n,
+                                     ax.ctypes.data if ax is not None else None, out.ctypes.data, cap, C.byref(cnt))
+        self._check(rc, "cg_broad_phase")
+        return out[:cnt.value]
 
     def shoot_rays(self, tree_a, tree_b, first_globals, second_globals, rays_first, rays_second,
                    params: tuple | None = None) -> np.ndarray:

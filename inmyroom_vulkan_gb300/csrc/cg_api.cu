@@ -200,6 +200,8 @@ struct cg_ctx {
     uint64_t vgrad_cap = 0;
     void* shoot = nullptr;                  // cg_shoot_rays: queries, rays, tags, per-ray results, deltas, flag
     size_t shoot_cap = 0;
+    void* broad = nullptr;                  // cg_broad_phase: ids, globals, callbacks, projections, pairs, count
+    size_t broad_cap = 0;
 
     std::string err;
 };
@@ -781,6 +783,7 @@ int cg_destroy(cg_ctx* c) {
     cudaFree(c->pose_scratch);
     cudaFree(c->vgrad);
     cudaFree(c->shoot);
+    cudaFree(c->broad);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
@@ -1450,6 +1453,81 @@ int cg_energy_backward(cg_ctx* c, const double* d_grad_energy, const cg_energy_s
     p.max_targets = max_targets;
     CG_CUDA(launch_energy_backward(p, c->energy_blocks, max_vertices, s), "energy adjoint kernels");
     return CG_OK;
+}
+
+int cg_broad_phase(cg_ctx* c, const uint32_t* tree_ids, const float* globals, const uint8_t* callback, uint32_t n,
+                   const float* axes, cg_entity_pair* pairs, uint64_t cap, uint64_t* n_pairs) {
+    if (!c || !n_pairs || (n && (!tree_ids || !globals)) || (cap && !pairs)) return CG_ERR_INVALID_ARGUMENT;
+    *n_pairs = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        if (tree_ids[i] >= c->trees.size() || !c->trees[tree_ids[i]].live)
+            return fail(c, CG_ERR_NOT_FOUND, "entity %u names tree %u", i, tree_ids[i]);
+    if (n < 2) return CG_OK;
+    // the engine's axes (CollisionDetection.cpp:9-13), glm-convention arithmetic
+    auto norm = [](float x, float y, float z, float* o) {
+        const float inv = 1.0f / std::sqrt((x * x + y * y) + z * z);
+        o[0] = x * inv, o[1] = y * inv, o[2] = z * inv;
+    };
+    auto cross = [](const float* a, const float* b, float* o) {
+        o[0] = a[1] * b[2] - b[1] * a[2];
+        o[1] = a[2] * b[0] - b[2] * a[0];
+        o[2] = a[0] * b[1] - b[0] * a[1];
+    };
+    float ax[9];
+    if (axes) {
+        std::memcpy(ax, axes, sizeof(ax));
+    } else {
+        float t[3];
+        const float down[3] = {0.f, -1.f, 0.f};
+        norm(0.8f, -0.2f, 0.f, ax);
+        cross(ax, down, t);
+        norm(t[0], t[1], t[2], ax + 6);
+        cross(ax + 6, ax, t);
+        norm(t[0], t[1], t[2], ax + 3);
+    }
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
+    const uint64_t pair_cap = std::max<uint64_t>(cap, 1);
+    const size_t b_id = up(sizeof(uint32_t) * n), b_g = up(sizeof(float) * 16 * n), b_cb = up(n),
+                 b_p = up(sizeof(float) * 6 * n), b_out = up(sizeof(uint2) * pair_cap), b_cnt = 256;
+    const size_t need = b_id + b_g + b_cb + b_p + b_out + b_cnt;
+    if (need > c->broad_cap) {
+        CG_CUDA(cudaStreamSynchronize(s), "broad-phase buffers");
+        cudaFree(c->broad);
+        c->broad = nullptr;
+        c->broad_cap = 0;
+        CG_CUDA(cudaMalloc(&c->broad, need), "alloc broad-phase buffers");
+        c->broad_cap = need;
+    }
+    char* base = static_cast<char*>(c->broad);
+    BroadParams p{};
+    uint32_t* d_ids = reinterpret_cast<uint32_t*>(base);
+    float* d_g = reinterpret_cast<float*>(base + b_id);
+    uint8_t* d_cb = reinterpret_cast<uint8_t*>(base + b_id + b_g);
+    p.proj = reinterpret_cast<float*>(base + b_id + b_g + b_cb);
+    p.pairs = reinterpret_cast<uint2*>(base + b_id + b_g + b_cb + b_p);
+    p.count = reinterpret_cast<unsigned long long*>(base + b_id + b_g + b_cb + b_p + b_out);
+    CG_CUDA(cudaMemcpyAsync(d_ids, tree_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s), "upload ids");
+    CG_CUDA(cudaMemcpyAsync(d_g, globals, sizeof(float) * 16 * n, cudaMemcpyHostToDevice, s), "upload matrices");
+    if (callback) CG_CUDA(cudaMemcpyAsync(d_cb, callback, n, cudaMemcpyHostToDevice, s), "upload callbacks");
+    CG_CUDA(cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s), "clear count");
+    p.tree_ids = d_ids;
+    p.trees = c->d_trees;
+    p.recs = c->recs.ptr;
+    p.globals = d_g;
+    p.callback = callback ? d_cb : nullptr;
+    p.n = n;
+    for (int k = 0; k < 3; ++k) p.axes[k] = make_float3(ax[3 * k], ax[3 * k + 1], ax[3 * k + 2]);
+    p.cap = cap;
+    CG_CUDA(launch_broad(p, s), "broad-phase kernels");
+    unsigned long long cnt = 0;
+    CG_CUDA(cudaMemcpyAsync(&cnt, p.count, sizeof(cnt), cudaMemcpyDeviceToHost, s), "read count");
+    CG_CUDA(cudaStreamSynchronize(s), "broad phase");
+    *n_pairs = cnt;
+    const uint64_t m = std::min<uint64_t>(cnt, cap);
+    if (m) CG_CUDA(cudaMemcpy(pairs, p.pairs, sizeof(uint2) * m, cudaMemcpyDeviceToHost), "read pairs");
+    return cnt > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
 }
 
 void cg_shoot_params_default(cg_shoot_params* p) {

@@ -320,6 +320,22 @@ cudaError_t launch_energy(const EnergyParams& p, uint32_t blocks, cudaStream_t s
 cudaError_t launch_energy_backward(const EnergyParams& p, uint32_t blocks, uint32_t max_vertices, cudaStream_t s);
 cudaError_t energy_occupancy(int* blocks_per_sm);
 
+// Broad phase (cg_broad.cu).
+struct BroadParams {
+    const uint32_t* tree_ids;  // per entity
+    const DevTree* trees;
+    const float4* recs;
+    const float* globals;      // [n][16] world matrices
+    const uint8_t* callback;   // per entity, or null: all call back
+    uint32_t n;
+    float3 axes[3];            // U, V, W
+    float* proj;               // [n][6] scratch: min/max on U, V, W
+    uint2* pairs;
+    unsigned long long cap;
+    unsigned long long* count;
+};
+cudaError_t launch_broad(const BroadParams& p, cudaStream_t s);
+
 // Uncollide-ray shooting (cg_shoot.cu).
 struct ShootQuery {
     float relative[16];      // second entity's model space to the first's

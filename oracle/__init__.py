@@ -70,6 +70,8 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
     f("eig3").argtypes = [_f64p, _f64p, _f64p]
     f("rays").argtypes = [vp, _f32p, _f32p, sz, sz, C.POINTER(sz), _f32p]
     f("shoot_rays").argtypes = [vp, vp, _f32p, _f32p, _f32p, sz, _f32p, sz, vp, _f32p]
+    f("sweep_and_prune").restype = sz
+    f("sweep_and_prune").argtypes = [vp, _f32p, vp, sz, vp, vp, sz]
     if prefix == "ref_":
         f("narrow").restype = sz
         f("narrow").argtypes = [vp, _u32p, _f32p, sz, C.POINTER(C.c_uint64)]
@@ -349,6 +351,20 @@ class Impl:
                               len(ra), rb if len(rb) else np.zeros((1, 6), np.float32), len(rb),
                               pr.ctypes.data if pr is not None else None, out)
         return out
+
+    def sweep_and_prune(self, trees, globals_, callback=None, axes=None) -> np.ndarray:
+        """SweepAndPrune::ExecuteSweepAndPrune: (k, 2) [first, second] entity
+        indices in no particular order (the engine's axes unless axes (3, 3))."""
+        n = len(trees)
+        h = (C.c_void_p * n)(*[t.h for t in trees])
+        g = _f32(globals_)
+        cb = np.ascontiguousarray(np.ones(n, np.uint8) if callback is None else callback, np.uint8)
+        ax = None if axes is None else np.ascontiguousarray(axes, np.float32).reshape(9)
+        axp = ax.ctypes.data if ax is not None else None
+        cnt = self.fn("sweep_and_prune")(h, g, cb.ctypes.data, n, axp, None, 0)
+        out = np.zeros((max(cnt, 1), 2), np.uint32)
+        self.fn("sweep_and_prune")(h, g, cb.ctypes.data, n, axp, out.ctypes.data, cnt)
+        return out[:cnt]
 
     def collide_pairs(self, trees_a, trees_b, mats_a, mats_b):
         """(port) all colliding pairs of a batch: (n,3) [query, ia, ib], (n,6) segs, tests, leaf pairs."""

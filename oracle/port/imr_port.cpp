@@ -1007,6 +1007,72 @@ V3 shoot(const Tree& A, const Tree& B, const M4& ga, const M4& gb, const std::ve
     return xform(ga, local, 0.f);
 }
 
+// ------------------------------------------------------- broad phase ----
+// The engine's three skewed axes (CollisionDetection.cpp:9-13).
+inline void engine_axes(V3& U, V3& V, V3& W) {
+    U = normalize(V3{0.8f, -0.2f, 0.f});
+    W = normalize(cross(U, V3{0.f, -1.f, 0.f}));
+    V = normalize(cross(W, U));
+}
+
+// SweepAndPrune::ExecuteSweepAndPrune (SweepAndPrune.cpp:15-88): each
+// entity's world root box projected on U, V, W; per axis sorted by the
+// projection's start and swept with an active list (an entry leaves when its
+// end is before the new start); a pair found on U (at least one entity with a
+// callback) is kept when V and W find it too. Pairs as (the entity earlier on
+// U, the later one).
+std::vector<std::pair<uint32_t, uint32_t>> sweep_and_prune(const std::vector<const Tree*>& trees,
+                                                           const std::vector<M4>& globals,
+                                                           const std::vector<uint8_t>& callback, V3 U, V3 V,
+                                                           V3 W) {
+    struct Entry {
+        float lo, hi;
+        uint32_t index;
+        bool cb;
+    };
+    const size_t n = trees.size();
+    std::vector<Entry> axis_entries[3];
+    const V3 axes[3] = {U, V, W};
+    for (size_t i = 0; i < n; ++i) {
+        const Box b = xform_box(globals[i], trees[i]->root);
+        for (int a = 0; a < 3; ++a) {
+            Entry e{0.f, 0.f, uint32_t(i), callback[i] != 0};
+            project(b, axes[a], e.lo, e.hi);
+            axis_entries[a].push_back(e);
+        }
+    }
+    for (auto& v : axis_entries)
+        std::sort(v.begin(), v.end(), [](const Entry& a, const Entry& b) { return a.lo < b.lo; });
+    struct Found {
+        uint32_t first, second, count;
+    };
+    std::unordered_map<uint64_t, Found> found;  // keyed by the unordered pair
+    auto key = [](uint32_t a, uint32_t b) { return (uint64_t(std::min(a, b)) << 32) | std::max(a, b); };
+    for (int a = 0; a < 3; ++a) {
+        std::vector<Entry> active;
+        for (const Entry& e : axis_entries[a]) {
+            std::vector<Entry> kept;
+            for (const Entry& act : active) {
+                if (act.hi < e.lo) continue;  // leaves the active list
+                kept.push_back(act);
+                if (!(act.cb || e.cb)) continue;
+                if (a == 0) {
+                    found.emplace(key(act.index, e.index), Found{act.index, e.index, 1});
+                } else {
+                    auto it = found.find(key(act.index, e.index));
+                    if (it != found.end()) ++it->second.count;
+                }
+            }
+            kept.push_back(e);
+            active.swap(kept);
+        }
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> out;
+    for (const auto& kv : found)
+        if (kv.second.count == 3) out.emplace_back(kv.second.first, kv.second.second);
+    return out;
+}
+
 }  // namespace port
 
 // ================================================================ C ABI ====
@@ -1426,6 +1492,33 @@ void port_shoot_rays(void* ta, void* tb, const float* ga16, const float* gb16, c
     const V3 r = shoot(*static_cast<Tree*>(ta), *static_cast<Tree*>(tb), ldm(ga16), ldm(gb16), load(rays_a, n_a),
                        load(rays_b, n_b), P);
     st3(r, out3);
+}
+
+// SweepAndPrune::ExecuteSweepAndPrune with the engine's axes or axes9 (U, V,
+// W); the pairs (first, second) in no particular order; returns their count.
+size_t port_sweep_and_prune(void* const* trees, const float* globals, const uint8_t* callback, size_t n,
+                            const float* axes9, uint32_t* out_pairs, size_t cap) {
+    std::vector<const Tree*> ts(n);
+    std::vector<M4> gs(n);
+    std::vector<uint8_t> cb(callback, callback + n);
+    for (size_t i = 0; i < n; ++i) {
+        ts[i] = static_cast<const Tree*>(trees[i]);
+        gs[i] = ldm(globals + 16 * i);
+    }
+    V3 U, V, W;
+    if (axes9) {
+        U = ld3(axes9);
+        V = ld3(axes9 + 3);
+        W = ld3(axes9 + 6);
+    } else {
+        engine_axes(U, V, W);
+    }
+    const auto pairs = sweep_and_prune(ts, gs, cb, U, V, W);
+    for (size_t k = 0; k < pairs.size() && k < cap; ++k) {
+        out_pairs[2 * k] = pairs[k].first;
+        out_pairs[2 * k + 1] = pairs[k].second;
+    }
+    return pairs.size();
 }
 
 }  // extern "C"

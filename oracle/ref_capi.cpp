@@ -13,6 +13,7 @@
 #include "CollisionDetection/CreateUncollideRays.h"
 #include "CollisionDetection/OBBtreesCollision.h"
 #include "CollisionDetection/ShootUncollideRays.h"
+#include "CollisionDetection/SweepAndPrune.h"
 #include "Geometry/OBBtree.h"
 #include "Geometry/Paralgram.h"
 #include "Geometry/Triangle.h"
@@ -362,6 +363,38 @@ void ref_shoot_rays(void* ta, void* tb, const float* ga16, const float* gb16, co
     const ShootUncollideRays shooter = params ? ShootUncollideRays(params[0], params[1], params[2])
                                               : ShootUncollideRays(glm::radians(40.f), glm::radians(65.f), 1.01f);
     put_vec(shooter.ExecuteShootUncollideRays(u), out3);
+}
+
+// SweepAndPrune::ExecuteSweepAndPrune with the engine's axes
+// (CollisionDetection.cpp:9-13) or axes9 (U, V, W): the pairs as
+// (first entity, second entity) in the order produced; returns their count
+// (pairs beyond cap are counted, not written).
+size_t ref_sweep_and_prune(void* const* trees, const float* globals, const uint8_t* callback, size_t n,
+                           const float* axes9, uint32_t* out_pairs, size_t cap) {
+    glm::vec3 U, V, W;
+    if (axes9) {
+        U = glm::vec3(axes9[0], axes9[1], axes9[2]);
+        V = glm::vec3(axes9[3], axes9[4], axes9[5]);
+        W = glm::vec3(axes9[6], axes9[7], axes9[8]);
+    } else {
+        U = glm::normalize(glm::vec3(0.8f, -0.2f, 0.f));
+        W = glm::normalize(glm::cross(U, glm::vec3(0.f, -1.f, 0.f)));
+        V = glm::normalize(glm::cross(W, U));
+    }
+    SweepAndPrune sap(U, V, W);
+    std::vector<CollisionDetectionEntry> entries(n);
+    for (size_t i = 0; i < n; ++i) {
+        entries[i].currentGlobalMatrix = entries[i].previousGlobalMatrix = load_mat(globals + 16 * i);
+        entries[i].OBBtree_ptr = static_cast<const OBBtree*>(trees[i]);
+        entries[i].shouldCallback = callback[i] != 0;
+        entries[i].entity = Entity(i);
+    }
+    const auto pairs = sap.ExecuteSweepAndPrune(entries);
+    for (size_t k = 0; k < pairs.size() && k < cap; ++k) {
+        out_pairs[2 * k] = pairs[k].first.entity;
+        out_pairs[2 * k + 1] = pairs[k].second.entity;
+    }
+    return pairs.size();
 }
 
 }  // extern "C"

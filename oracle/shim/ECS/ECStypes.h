@@ -6,6 +6,12 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <unordered_map>  // the real header's standard includes (ECStypes.h:3-8), which
+#include <vector>         // the reference's translation units rely on
 
 #include "glm/mat4x4.hpp"
 #include "glm/vec3.hpp"

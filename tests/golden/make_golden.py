@@ -109,6 +109,18 @@ def shoot_fixture(R):
     np.savez_compressed(os.path.join(HERE, "shoot_small.npz"), deltas=np.array(deltas, np.float32))
 
 
+def sap_fixture(R):
+    """SweepAndPrune::ExecuteSweepAndPrune on the 256-entity scene (seed 1002)
+    with a seeded 70% of the entities calling back: the pairs as the
+    reference orients them."""
+    sc = scenes.scene()
+    trees = [R.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    cb = (np.random.Generator(np.random.PCG64(7)).random(len(trees)) < 0.7).astype(np.uint8)
+    pairs = R.sweep_and_prune(trees, sc.mats, cb)
+    pairs = pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
+    np.savez_compressed(os.path.join(HERE, "sap_scene.npz"), callback=cb, pairs=pairs)
+
+
 def main():
     R = oracle.ref()
     if R is None:
@@ -185,6 +197,7 @@ def main():
                tests=np.array(tests, np.uint64))
     np.savez_compressed(os.path.join(HERE, "rigid_small.npz"), **out)
     shoot_fixture(R)
+    sap_fixture(R)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -140,3 +140,16 @@ def test_shoot_rays_matches_reference(port):
         rb = g["rays_b"][g["rays_b"][:, 0] == k, 1:]
         got = port.shoot_rays(ta, tb, g["mats_a"][k], g["mats_b"][k], ra, rb)
         assert np.array_equal(bits(got), bits(want[k])), k
+
+
+def test_sweep_and_prune_matches_reference(port):
+    """SweepAndPrune::ExecuteSweepAndPrune on the 256-entity scene: the same
+    pairs, oriented the same way."""
+    from inmyroom_vulkan_gb300 import scenes
+
+    want = load("sap_scene.npz")
+    sc = scenes.scene()
+    trees = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    got = port.sweep_and_prune(trees, sc.mats, want["callback"])
+    got = got[np.lexsort((got[:, 1], got[:, 0]))]
+    assert np.array_equal(got, want["pairs"])

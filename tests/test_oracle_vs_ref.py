@@ -82,3 +82,18 @@ def test_shoot_rays_full_size(port, ref):
             assert np.array_equal(bits(a), bits(b)), (k, a, b)
             moved += int(np.any(a != 0))
     assert moved > 30
+
+
+def test_sweep_and_prune_axes_and_callbacks(port, ref):
+    """SweepAndPrune with the engine's axes and with others, all and some
+    entities calling back: port and reference give the same oriented pairs."""
+    sc = scenes.scene(n_entities=128, seed=1077)
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    tr = [ref.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    rng = np.random.default_rng(3)
+    axes = np.linalg.qr(rng.normal(size=(3, 3)))[0].T.astype(np.float32)
+    for cb in (np.ones(len(tp), np.uint8), (rng.random(len(tp)) < 0.3).astype(np.uint8)):
+        for ax in (None, axes):
+            a = port.sweep_and_prune(tp, sc.mats, cb, ax)
+            b = ref.sweep_and_prune(tr, sc.mats, cb, ax)
+            assert set(map(tuple, a)) == set(map(tuple, b)) and len(a) == len(b)
