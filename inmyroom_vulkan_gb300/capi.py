@@ -14,6 +14,8 @@ import numpy as np
 from . import build as _build
 
 CG_OK = 0
+CG_ERR_INVALID_ARGUMENT, CG_ERR_CUDA, CG_ERR_OUT_OF_MEMORY, CG_ERR_QUEUE_OVERFLOW = -1, -2, -3, -4
+CG_ERR_OUTPUT_OVERFLOW, CG_ERR_TIMEOUT, CG_ERR_BAD_TREE, CG_ERR_NOT_FOUND = -5, -6, -7, -8
 STATUS = {0: "CG_OK", -1: "CG_ERR_INVALID_ARGUMENT", -2: "CG_ERR_CUDA", -3: "CG_ERR_OUT_OF_MEMORY",
           -4: "CG_ERR_QUEUE_OVERFLOW", -5: "CG_ERR_OUTPUT_OVERFLOW", -6: "CG_ERR_TIMEOUT", -7: "CG_ERR_BAD_TREE",
           -8: "CG_ERR_NOT_FOUND"}
