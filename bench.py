@@ -249,6 +249,53 @@ def run_shoot(args, ctx, sc, ids, q, cpu_seconds: float) -> dict:
     return res
 
 
+def run_frame(args, ctx, sc, ids, cpu_seconds: float) -> dict:
+    """One collision frame of the 256-entity scene (cg_collision_frame): the
+    engine's whole per-frame pipeline (broad phase, OBB-tree collide with
+    contacts and rays, shooting for pairs where an entity moved, the delta
+    split) from the entities' current and previous matrices to one record per
+    pair with rays. A third of the entities stand still, the rest moved up to
+    0.05; 70% call back. Host-timed around the synchronous call (entities in,
+    results out); beside it the oracle's frame on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle
+    from inmyroom_vulkan_gb300 import scenes
+    from oracle import frame
+
+    prev, cb = scenes.frame_motion(sc)
+    for _ in range(max(args.warmup, 3)):
+        res = ctx.collision_frame(ids, sc.mats, prev, cb)
+    times = []
+    for _ in range(max(args.steps, 5)):
+        t0 = time.perf_counter()
+        res = ctx.collision_frame(ids, sc.mats, prev, cb)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.median(times))
+    out = {"workload": "one collision frame of the 256-entity scene (SweepAndPrune, OBB trees, uncollide rays, "
+                       "ShootUncollideRays, delta split)",
+           "entities": len(ids), "pairs_with_rays": int(len(res)),
+           "pairs_moved": int((np.abs(res["first_delta"]).sum(1) + np.abs(res["second_delta"]).sum(1) > 0).sum()),
+           "ms_per_frame": ms, "frames_per_s": 1e3 / ms,
+           "timing": "host perf_counter around the synchronous cg_collision_frame (entity upload and result "
+                     "read-back included); median of the steps"}
+    if cpu_seconds > 0:
+        fast = oracle.port(fast=True)
+        trees = [fast.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+        cores = os.cpu_count() or 1
+        pool = ThreadPoolExecutor(cores)
+        runs, t0 = 0, time.perf_counter()
+        while True:
+            frame.collision_frame(fast, trees, sc.mats, prev, cb, map_fn=pool.map)
+            runs += 1
+            if time.perf_counter() - t0 >= cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"ms_per_frame": 1e3 * el / runs, "cores": cores, "kind": "port",
+                               "sample": f"{runs} whole frames, {el:.1f} s, release flags, pairs over a thread pool"}
+    return out
+
+
 def run_sweep(args, local: int, flush, stream, cpu_seconds: float) -> dict:
     """Autotuned batch sweep: 10,000 uneven rigid mesh-pair queries (a pool of
     48 meshes of 256..65,536 triangles, log-uniform; random SO(3) poses with
@@ -651,6 +698,9 @@ def run_gpu(args) -> dict:
     shoot = None
     if rank == 0 and not args.skip_shoot:
         shoot = run_shoot(args, ctx, sc, ids, q, min(args.cpu_seconds, 5.0))
+    frame_line = None
+    if rank == 0 and not args.skip_frame:
+        frame_line = run_frame(args, ctx, sc, ids, min(args.cpu_seconds, 5.0))
     cpu = cpu_baseline(sc, seconds=args.cpu_seconds) if rank == 0 and args.cpu_seconds > 0 else None
     deforming = None
     if rank == 0 and not args.skip_deforming:
@@ -704,6 +754,8 @@ def run_gpu(args) -> dict:
         out["batch_sweep"] = sweep
     if shoot:
         out["shoot"] = shoot
+    if frame_line:
+        out["frame"] = frame_line
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -738,6 +790,7 @@ def main():
     ap.add_argument("--skip-sweep", action="store_true", help="leave out the autotuned batch-sweep line")
     ap.add_argument("--no-tune", action="store_true", help="time the scene step with the default launch settings")
     ap.add_argument("--skip-shoot", action="store_true", help="leave out the uncollide-ray shooting line")
+    ap.add_argument("--skip-frame", action="store_true", help="leave out the collision-frame line")
     ap.add_argument("--only", choices=["deforming", "differentiable", "sweep"],
                     help="run one secondary workload alone and print its object (for profiling)")
     args = ap.parse_args()

@@ -432,6 +432,36 @@ typedef struct cg_shoot_query {
 int cg_shoot_rays(cg_ctx* ctx, const cg_shoot_query* queries, uint32_t n, const float* rays, uint64_t n_rays,
                   const cg_shoot_params* params, float* deltas);
 
+/* ---- A collision frame ----
+ *
+ * CollisionDetection::ExecuteCollisionDetection
+ * (src/CollisionDetection/CollisionDetection.cpp:38-129) for n entities on the
+ * device: broad phase (cg_broad_phase), the collide step of every broad pair
+ * with contacts and uncollide rays, shooting (cg_shoot_rays, for pairs where an
+ * entity moved, :80-82) and the delta split by each entity's movement of its
+ * mean ray origin (:84-103). One result per pair with rays (:62-66), the
+ * pair as the broad phase orients it; the fan-out of each result to the
+ * entities' ancestors (:106-124) needs the engine's entity tree and is the
+ * caller's. The deltas can differ from the reference's in the last bits (the
+ * rays of a pair are summed in the order the contact kernels make them, the
+ * reference's in its unordered_map's order). The broad pairs must fit in
+ * max_queries. Synchronous. */
+typedef struct cg_frame_entity {
+    uint32_t tree;
+    uint32_t should_callback;
+    float current_global[16];
+    float previous_global[16];
+} cg_frame_entity;
+
+typedef struct cg_frame_result {
+    uint32_t first, second;   /* entity indices */
+    float first_delta[3];     /* CollisionCallbackData::deltaVector of the first entity */
+    float second_delta[3];    /* and of the second */
+} cg_frame_result;
+
+int cg_collision_frame(cg_ctx* ctx, const cg_frame_entity* entities, uint32_t n, const cg_shoot_params* params,
+                       cg_frame_result* results, uint64_t cap, uint64_t* n_results);
+
 /* ---- No-allocation collide step (no reference counterpart) ----
  *
  * The collide step of cg_collide_async (same kernels, same colliding pairs)

@@ -34,7 +34,7 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
            "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
            "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays",
-           "cg_broad_phase"]
+           "cg_broad_phase", "cg_collision_frame"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -116,6 +116,11 @@ RAY_AVERAGE_DTYPE = np.dtype([("first", "<f4", (3,)), ("second", "<f4", (3,)), (
 SHOOT_QUERY_DTYPE = np.dtype([("tree_a", "<u4"), ("tree_b", "<u4"), ("first_global", "<f4", (16,)),
                               ("second_global", "<f4", (16,)), ("n_first", "<u4"), ("n_second", "<u4")])
 assert SHOOT_QUERY_DTYPE.itemsize == 144
+FRAME_ENTITY_DTYPE = np.dtype([("tree", "<u4"), ("should_callback", "<u4"), ("current_global", "<f4", (16,)),
+                               ("previous_global", "<f4", (16,))])
+FRAME_RESULT_DTYPE = np.dtype([("first", "<u4"), ("second", "<u4"), ("first_delta", "<f4", (3,)),
+                               ("second_delta", "<f4", (3,))])
+assert FRAME_ENTITY_DTYPE.itemsize == 136 and FRAME_RESULT_DTYPE.itemsize == 32
 assert QUERY_DTYPE.itemsize == 72 and TRI_PAIR_DTYPE.itemsize == 36 and LEAF_PAIR_DTYPE.itemsize == 16
 assert CONTACT_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32 and RAY_AVERAGE_DTYPE.itemsize == 32
 
@@ -165,6 +170,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_set_host_outputs.argtypes = [vp, vp, u64, vp, u64, vp, u64]
     lib.cg_broad_phase.argtypes = [vp, vp, vp, vp, u32, vp, vp, u64, C.POINTER(u64)]
     lib.cg_shoot_params_default.argtypes = [C.POINTER(cg_shoot_params)]
+    lib.cg_collision_frame.argtypes = [vp, vp, u32, C.POINTER(cg_shoot_params), vp, u64, C.POINTER(u64)]
     lib.cg_shoot_params_default.restype = None
     lib.cg_shoot_rays.argtypes = [vp, vp, u32, vp, u64, C.POINTER(cg_shoot_params), vp]
     lib.cg_pose.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, u32, vp, vp]
@@ -426,6 +432,29 @@ class Context:
                                      cb.ctypes.data if cb is not None else None, n,
                                      ax.ctypes.data if ax is not None else None, out.ctypes.data, cap, C.byref(cnt))
         self._check(rc, "cg_broad_phase")
+        return out[:cnt.value]
+
+    def collision_frame(self, tree_ids, current, previous, callback=None, params: tuple | None = None,
+                        cap: int | None = None) -> np.ndarray:
+        """cg_collision_frame: one frame of the engine's collision detection
+        over n entities (tree ids (n,), current and previous world matrices
+        (n, 16), should-callback flags (n,) or all). A FRAME_RESULT_DTYPE array,
+        one record per broad pair with rays, in no fixed order."""
+        ids = np.ascontiguousarray(tree_ids, np.uint32)
+        n = len(ids)
+        ent = np.zeros(n, FRAME_ENTITY_DTYPE)
+        ent["tree"] = ids
+        ent["should_callback"] = 1 if callback is None else np.asarray(callback, np.uint32)
+        ent["current_global"] = np.asarray(current, np.float32).reshape(n, 16)
+        ent["previous_global"] = np.asarray(previous, np.float32).reshape(n, 16)
+        cap = self.config().max_queries if cap is None else cap
+        out = np.zeros(max(cap, 1), FRAME_RESULT_DTYPE)
+        cnt = C.c_uint64()
+        pp = None if params is None else cg_shoot_params(*[float(x) for x in params])
+        rc = self.lib.cg_collision_frame(self.h, ent.ctypes.data if n else None, n,
+                                         C.byref(pp) if pp is not None else None, out.ctypes.data, cap,
+                                         C.byref(cnt))
+        self._check(rc, "cg_collision_frame")
         return out[:cnt.value]
 
     def shoot_rays(self, tree_a, tree_b, first_globals, second_globals, rays_first, rays_second,

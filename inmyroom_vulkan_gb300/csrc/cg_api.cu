@@ -202,6 +202,8 @@ struct cg_ctx {
     size_t shoot_cap = 0;
     void* broad = nullptr;                  // cg_broad_phase: ids, globals, callbacks, projections, pairs, count
     size_t broad_cap = 0;
+    void* frame = nullptr;                  // cg_collision_frame's buffers
+    size_t frame_cap = 0;
 
     std::string err;
 };
@@ -360,6 +362,27 @@ EnergyParams energy_params(cg_ctx* c) {
     p.ctr = c->d_ctr;
     p.pairs_cap = c->cfg.max_tri_pairs;
     return p;
+}
+
+// The engine's broad-phase axes U, V, W (CollisionDetection.cpp:9-13) in
+// glm-convention arithmetic.
+void engine_axes(float* ax) {
+    auto norm = [](float x, float y, float z, float* o) {
+        const float inv = 1.0f / std::sqrt((x * x + y * y) + z * z);
+        o[0] = x * inv, o[1] = y * inv, o[2] = z * inv;
+    };
+    auto cross = [](const float* a, const float* b, float* o) {
+        o[0] = a[1] * b[2] - b[1] * a[2];
+        o[1] = a[2] * b[0] - b[2] * a[0];
+        o[2] = a[0] * b[1] - b[0] * a[1];
+    };
+    float t[3];
+    const float down[3] = {0.f, -1.f, 0.f};
+    norm(0.8f, -0.2f, 0.f, ax);
+    cross(ax, down, t);
+    norm(t[0], t[1], t[2], ax + 6);
+    cross(ax + 6, ax, t);
+    norm(t[0], t[1], t[2], ax + 3);
 }
 
 void drop_graph(cg_ctx* c) {
@@ -784,6 +807,7 @@ int cg_destroy(cg_ctx* c) {
     cudaFree(c->vgrad);
     cudaFree(c->shoot);
     cudaFree(c->broad);
+    cudaFree(c->frame);
     free_buffers(c);
     cudaEventDestroy(c->ev_t0);
     cudaEventDestroy(c->ev_t1);
@@ -1463,28 +1487,11 @@ int cg_broad_phase(cg_ctx* c, const uint32_t* tree_ids, const float* globals, co
         if (tree_ids[i] >= c->trees.size() || !c->trees[tree_ids[i]].live)
             return fail(c, CG_ERR_NOT_FOUND, "entity %u names tree %u", i, tree_ids[i]);
     if (n < 2) return CG_OK;
-    // the engine's axes (CollisionDetection.cpp:9-13), glm-convention arithmetic
-    auto norm = [](float x, float y, float z, float* o) {
-        const float inv = 1.0f / std::sqrt((x * x + y * y) + z * z);
-        o[0] = x * inv, o[1] = y * inv, o[2] = z * inv;
-    };
-    auto cross = [](const float* a, const float* b, float* o) {
-        o[0] = a[1] * b[2] - b[1] * a[2];
-        o[1] = a[2] * b[0] - b[2] * a[0];
-        o[2] = a[0] * b[1] - b[0] * a[1];
-    };
     float ax[9];
-    if (axes) {
+    if (axes)
         std::memcpy(ax, axes, sizeof(ax));
-    } else {
-        float t[3];
-        const float down[3] = {0.f, -1.f, 0.f};
-        norm(0.8f, -0.2f, 0.f, ax);
-        cross(ax, down, t);
-        norm(t[0], t[1], t[2], ax + 6);
-        cross(ax + 6, ax, t);
-        norm(t[0], t[1], t[2], ax + 3);
-    }
+    else
+        engine_axes(ax);
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
     auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
@@ -1530,6 +1537,160 @@ int cg_broad_phase(cg_ctx* c, const uint32_t* tree_ids, const float* globals, co
     return cnt > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
 }
 
+int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, const cg_shoot_params* params,
+                       cg_frame_result* results, uint64_t cap, uint64_t* n_results) {
+    if (!c || !n_results || (n && !entities) || (cap && !results)) return CG_ERR_INVALID_ARGUMENT;
+    *n_results = 0;
+    if (!c->cfg.max_contacts || !c->cfg.max_tri_pairs)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "a collision frame needs max_contacts and max_tri_pairs > 0");
+    for (uint32_t i = 0; i < n; ++i)
+        if (entities[i].tree >= c->trees.size() || !c->trees[entities[i].tree].live)
+            return fail(c, CG_ERR_NOT_FOUND, "entity %u names tree %u", i, entities[i].tree);
+    if (n < 2) return CG_OK;  // CollisionDetection.cpp:40
+    cg_shoot_params pr;
+    cg_shoot_params_default(&pr);
+    if (params) pr = *params;
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    // broad phase, on the device
+    std::vector<uint32_t> ids(n);
+    std::vector<float> globals(16ull * n);
+    std::vector<uint8_t> cbs(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        ids[i] = entities[i].tree;
+        std::memcpy(globals.data() + 16ull * i, entities[i].current_global, 16 * sizeof(float));
+        cbs[i] = entities[i].should_callback ? 1u : 0u;
+    }
+    const uint32_t max_pairs = c->cfg.max_queries;
+    const uint32_t max_rays = c->ct.max_rays;
+    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
+    const size_t b_ent = up(sizeof(cg_frame_entity) * n), b_id = up(sizeof(uint32_t) * n),
+                 b_g = up(sizeof(float) * 16 * n), b_cb = up(n), b_proj = up(sizeof(float) * 6 * n),
+                 b_pairs = up(sizeof(uint2) * max_pairs), b_cnt = 256, b_c3 = up(3 * sizeof(uint32_t) * 2 * max_pairs),
+                 b_grp = up(sizeof(float) * 6 * max_rays), b_tag = up(sizeof(uint32_t) * max_rays),
+                 b_sq = up(sizeof(ShootQuery) * max_pairs), b_so = up(sizeof(ShootRayOut) * max_rays),
+                 b_dl = up(sizeof(float) * 3 * max_pairs), b_res = up(sizeof(cg_frame_result) * max_pairs);
+    const size_t need = b_ent + b_id + b_g + b_cb + b_proj + b_pairs + b_cnt + b_c3 + b_grp + b_tag + b_sq + b_so +
+                        b_dl + b_res + b_cnt;
+    if (need > c->frame_cap) {
+        CG_CUDA(cudaStreamSynchronize(s), "frame buffers");
+        cudaFree(c->frame);
+        c->frame = nullptr;
+        c->frame_cap = 0;
+        CG_CUDA(cudaMalloc(&c->frame, need), "alloc frame buffers");
+        c->frame_cap = need;
+    }
+    char* p0 = static_cast<char*>(c->frame);
+    auto take = [&](size_t b) {
+        char* r = p0;
+        p0 += b;
+        return r;
+    };
+    cg_frame_entity* d_ent = reinterpret_cast<cg_frame_entity*>(take(b_ent));
+    uint32_t* d_ids = reinterpret_cast<uint32_t*>(take(b_id));
+    float* d_g = reinterpret_cast<float*>(take(b_g));
+    uint8_t* d_cb = reinterpret_cast<uint8_t*>(take(b_cb));
+    float* d_proj = reinterpret_cast<float*>(take(b_proj));
+    uint2* d_pairs = reinterpret_cast<uint2*>(take(b_pairs));
+    unsigned long long* d_npairs = reinterpret_cast<unsigned long long*>(take(b_cnt));
+    uint32_t* d_c3 = reinterpret_cast<uint32_t*>(take(b_c3));
+    float* d_grp = reinterpret_cast<float*>(take(b_grp));
+    uint32_t* d_tag = reinterpret_cast<uint32_t*>(take(b_tag));
+    ShootQuery* d_sq = reinterpret_cast<ShootQuery*>(take(b_sq));
+    ShootRayOut* d_so = reinterpret_cast<ShootRayOut*>(take(b_so));
+    float* d_dl = reinterpret_cast<float*>(take(b_dl));
+    cg_frame_result* d_res = reinterpret_cast<cg_frame_result*>(take(b_res));
+    unsigned long long* d_nres = reinterpret_cast<unsigned long long*>(take(b_cnt));
+    CG_CUDA(cudaMemcpyAsync(d_ent, entities, sizeof(cg_frame_entity) * n, cudaMemcpyHostToDevice, s), "upload entities");
+    CG_CUDA(cudaMemcpyAsync(d_ids, ids.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s), "upload ids");
+    CG_CUDA(cudaMemcpyAsync(d_g, globals.data(), sizeof(float) * 16 * n, cudaMemcpyHostToDevice, s), "upload matrices");
+    CG_CUDA(cudaMemcpyAsync(d_cb, cbs.data(), n, cudaMemcpyHostToDevice, s), "upload callbacks");
+    CG_CUDA(cudaMemsetAsync(d_npairs, 0, sizeof(unsigned long long), s), "clear count");
+    BroadParams bp{};
+    bp.tree_ids = d_ids;
+    bp.trees = c->d_trees;
+    bp.recs = c->recs.ptr;
+    bp.globals = d_g;
+    bp.callback = d_cb;
+    bp.n = n;
+    float ax[9];
+    engine_axes(ax);
+    for (int k = 0; k < 3; ++k) bp.axes[k] = make_float3(ax[3 * k], ax[3 * k + 1], ax[3 * k + 2]);
+    bp.proj = d_proj;
+    bp.pairs = d_pairs;
+    bp.cap = max_pairs;
+    bp.count = d_npairs;
+    CG_CUDA(launch_broad(bp, s), "broad-phase kernels");
+    unsigned long long np = 0;
+    CG_CUDA(cudaMemcpyAsync(&np, d_npairs, sizeof(np), cudaMemcpyDeviceToHost, s), "read pair count");
+    CG_CUDA(cudaStreamSynchronize(s), "broad phase");
+    if (np > max_pairs)
+        return fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu broad-phase pairs > max_queries %u", np, max_pairs);
+    if (np == 0) return CG_OK;
+    // collide every broad pair with contacts and rays
+    FrameParams fp{};
+    fp.entities = d_ent;
+    fp.pairs = d_pairs;
+    fp.n_pairs = uint32_t(np);
+    fp.max_rays = max_rays;
+    fp.queries = c->d_queries;
+    fp.rays = c->ct.rays;
+    fp.n_rays = &c->d_ctr->n_rays;
+    fp.counts = d_c3;
+    fp.offsets = d_c3 + 2 * max_pairs;
+    fp.cursor = d_c3 + 4 * max_pairs;
+    fp.grouped = d_grp;
+    fp.tags = d_tag;
+    fp.shoot = d_sq;
+    fp.deltas = d_dl;
+    fp.averages = c->ct.averages;
+    fp.results = d_res;
+    fp.results_cap = max_pairs;
+    fp.n_results = d_nres;
+    CG_CUDA(launch_frame_queries(fp, s), "frame query kernel");
+    c->last_flags = CG_CONTACTS;
+    int rc = enqueue_step(c, c->d_queries, uint32_t(np), CG_CONTACTS, s);
+    if (rc != CG_OK) return rc;
+    // rays per pair, shooting, the delta split
+    CG_CUDA(cudaMemsetAsync(fp.counts, 0, sizeof(uint32_t) * 2 * np, s), "clear ray counts");
+    CG_CUDA(cudaMemsetAsync(d_nres, 0, sizeof(unsigned long long), s), "clear result count");
+    CG_CUDA(launch_frame_rays(fp, uint32_t(4 * c->sm_count), s), "frame ray kernels");
+    ShootParams sp{};
+    sp.q = d_sq;
+    sp.n_queries = uint32_t(np);
+    sp.n_rays = max_rays;
+    sp.n_rays_dev = fp.n_rays;
+    sp.trees = c->d_trees;
+    sp.recs = c->recs.ptr;
+    sp.tris = c->tris.ptr;
+    sp.rays = d_grp;
+    sp.ray_query = d_tag;
+    sp.out = d_so;
+    sp.cos_start = std::cos(pr.smoothstep_start);
+    sp.cos_finish = std::cos(pr.smoothstep_finish);
+    sp.bias = pr.distance_bias;
+    sp.deltas = d_dl;
+    unsigned* d_err = reinterpret_cast<unsigned*>(d_npairs);  // the pair count is read: its word is free now
+    CG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s), "clear flag");
+    sp.error = d_err;
+    CG_CUDA(launch_shoot(sp, s), "shoot kernels");
+    CG_CUDA(launch_frame_split(fp, s), "frame split kernel");
+    unsigned long long nres = 0;
+    unsigned err = 0;
+    CG_CUDA(cudaMemcpyAsync(&nres, d_nres, sizeof(nres), cudaMemcpyDeviceToHost, s), "read result count");
+    CG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(err), cudaMemcpyDeviceToHost, s), "read flag");
+    CG_CUDA(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s), "read counters");
+    CG_CUDA(cudaStreamSynchronize(s), "collision frame");
+    cg_stats st{};
+    rc = stats_from(c, *c->h_ctr, &st);
+    if (rc != CG_OK) return rc;
+    if (err) return fail(c, CG_ERR_QUEUE_OVERFLOW, "a tree is deeper than the ray traversal's stack");
+    *n_results = nres;
+    const uint64_t m = std::min<uint64_t>(nres, cap);
+    if (m) CG_CUDA(cudaMemcpy(results, d_res, sizeof(cg_frame_result) * m, cudaMemcpyDeviceToHost), "read results");
+    return nres > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
 void cg_shoot_params_default(cg_shoot_params* p) {
     if (!p) return;
     const float deg = 0.01745329251994329576923690768489f;  // glm::radians
@@ -1568,6 +1729,8 @@ int cg_shoot_rays(cg_ctx* c, const cg_shoot_query* queries, uint32_t n, const fl
         t.ray_first = uint32_t(next);
         t.n_first = q.n_first;
         t.n_second = q.n_second;
+        t.pad[0] = 1u;
+        t.pad[1] = t.pad[2] = 0u;
         for (uint64_t k = 0; k < cnt; ++k) tags[next + k] = i | (k >= q.n_first ? 0x80000000u : 0u);
         next += cnt;
     }

@@ -89,46 +89,6 @@ __device__ __forceinline__ float3 mul3(const Mat3& N, float3 v) {
                        (N.c0.z * v.x + N.c1.z * v.y) + N.c2.z * v.z);
 }
 
-// glm-convention inverse (Laplace expansion over 2x2 minors), the expression
-// tree of the host's cg_relative_matrix.
-__device__ Mat4 inverse4(const Mat4& M) {
-    const float4 col[4] = {M.c0, M.c1, M.c2, M.c3};
-    auto a = [&](int r, int c) { return r == 0 ? col[c].x : (r == 1 ? col[c].y : (r == 2 ? col[c].z : col[c].w)); };
-    const float s01 = a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1);
-    const float s02 = a(0, 0) * a(1, 2) - a(1, 0) * a(0, 2);
-    const float s03 = a(0, 0) * a(1, 3) - a(1, 0) * a(0, 3);
-    const float s12 = a(0, 1) * a(1, 2) - a(1, 1) * a(0, 2);
-    const float s13 = a(0, 1) * a(1, 3) - a(1, 1) * a(0, 3);
-    const float s23 = a(0, 2) * a(1, 3) - a(1, 2) * a(0, 3);
-    const float q01 = a(2, 0) * a(3, 1) - a(3, 0) * a(2, 1);
-    const float q02 = a(2, 0) * a(3, 2) - a(3, 0) * a(2, 2);
-    const float q03 = a(2, 0) * a(3, 3) - a(3, 0) * a(2, 3);
-    const float q12 = a(2, 1) * a(3, 2) - a(3, 1) * a(2, 2);
-    const float q13 = a(2, 1) * a(3, 3) - a(3, 1) * a(2, 3);
-    const float q23 = a(2, 2) * a(3, 3) - a(3, 2) * a(2, 3);
-    const float det = s01 * q23 - s02 * q13 + s03 * q12 + s12 * q03 - s13 * q02 + s23 * q01;
-    const float inv = 1.0f / det;
-    float b[4][4];
-    b[0][0] = (a(1, 1) * q23 - a(1, 2) * q13 + a(1, 3) * q12) * inv;
-    b[0][1] = (-a(0, 1) * q23 + a(0, 2) * q13 - a(0, 3) * q12) * inv;
-    b[0][2] = (a(3, 1) * s23 - a(3, 2) * s13 + a(3, 3) * s12) * inv;
-    b[0][3] = (-a(2, 1) * s23 + a(2, 2) * s13 - a(2, 3) * s12) * inv;
-    b[1][0] = (-a(1, 0) * q23 + a(1, 2) * q03 - a(1, 3) * q02) * inv;
-    b[1][1] = (a(0, 0) * q23 - a(0, 2) * q03 + a(0, 3) * q02) * inv;
-    b[1][2] = (-a(3, 0) * s23 + a(3, 2) * s03 - a(3, 3) * s02) * inv;
-    b[1][3] = (a(2, 0) * s23 - a(2, 2) * s03 + a(2, 3) * s02) * inv;
-    b[2][0] = (a(1, 0) * q13 - a(1, 1) * q03 + a(1, 3) * q01) * inv;
-    b[2][1] = (-a(0, 0) * q13 + a(0, 1) * q03 - a(0, 3) * q01) * inv;
-    b[2][2] = (a(3, 0) * s13 - a(3, 1) * s03 + a(3, 3) * s01) * inv;
-    b[2][3] = (-a(2, 0) * s13 + a(2, 1) * s03 - a(2, 3) * s01) * inv;
-    b[3][0] = (-a(1, 0) * q12 + a(1, 1) * q02 - a(1, 2) * q01) * inv;
-    b[3][1] = (a(0, 0) * q12 - a(0, 1) * q02 + a(0, 2) * q01) * inv;
-    b[3][2] = (-a(3, 0) * s12 + a(3, 1) * s02 - a(3, 2) * s01) * inv;
-    b[3][3] = (a(2, 0) * s12 - a(2, 1) * s02 + a(2, 2) * s01) * inv;
-    return Mat4{make_float4(b[0][0], b[1][0], b[2][0], b[3][0]), make_float4(b[0][1], b[1][1], b[2][1], b[3][1]),
-                make_float4(b[0][2], b[1][2], b[2][2], b[3][2]), make_float4(b[0][3], b[1][3], b[2][3], b[3][3])};
-}
-
 __device__ __forceinline__ Mat4 query_mat(const PackedQuery* Q) {
     return Mat4{__ldg(&Q->m[0]), __ldg(&Q->m[1]), __ldg(&Q->m[2]), __ldg(&Q->m[3])};
 }

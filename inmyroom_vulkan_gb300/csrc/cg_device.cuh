@@ -51,6 +51,66 @@ __device__ __forceinline__ float3 xform(const Mat4& M, float3 p, float w) {
     return r;
 }
 
+// glm-convention inverse (Laplace expansion over 2x2 minors), the expression
+// tree of the host's cg_relative_matrix.
+__device__ inline Mat4 inverse4(const Mat4& M) {
+    const float4 col[4] = {M.c0, M.c1, M.c2, M.c3};
+    auto a = [&](int r, int c) { return r == 0 ? col[c].x : (r == 1 ? col[c].y : (r == 2 ? col[c].z : col[c].w)); };
+    const float s01 = a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1);
+    const float s02 = a(0, 0) * a(1, 2) - a(1, 0) * a(0, 2);
+    const float s03 = a(0, 0) * a(1, 3) - a(1, 0) * a(0, 3);
+    const float s12 = a(0, 1) * a(1, 2) - a(1, 1) * a(0, 2);
+    const float s13 = a(0, 1) * a(1, 3) - a(1, 1) * a(0, 3);
+    const float s23 = a(0, 2) * a(1, 3) - a(1, 2) * a(0, 3);
+    const float q01 = a(2, 0) * a(3, 1) - a(3, 0) * a(2, 1);
+    const float q02 = a(2, 0) * a(3, 2) - a(3, 0) * a(2, 2);
+    const float q03 = a(2, 0) * a(3, 3) - a(3, 0) * a(2, 3);
+    const float q12 = a(2, 1) * a(3, 2) - a(3, 1) * a(2, 2);
+    const float q13 = a(2, 1) * a(3, 3) - a(3, 1) * a(2, 3);
+    const float q23 = a(2, 2) * a(3, 3) - a(3, 2) * a(2, 3);
+    const float det = s01 * q23 - s02 * q13 + s03 * q12 + s12 * q03 - s13 * q02 + s23 * q01;
+    const float inv = 1.0f / det;
+    float b[4][4];
+    b[0][0] = (a(1, 1) * q23 - a(1, 2) * q13 + a(1, 3) * q12) * inv;
+    b[0][1] = (-a(0, 1) * q23 + a(0, 2) * q13 - a(0, 3) * q12) * inv;
+    b[0][2] = (a(3, 1) * s23 - a(3, 2) * s13 + a(3, 3) * s12) * inv;
+    b[0][3] = (-a(2, 1) * s23 + a(2, 2) * s13 - a(2, 3) * s12) * inv;
+    b[1][0] = (-a(1, 0) * q23 + a(1, 2) * q03 - a(1, 3) * q02) * inv;
+    b[1][1] = (a(0, 0) * q23 - a(0, 2) * q03 + a(0, 3) * q02) * inv;
+    b[1][2] = (-a(3, 0) * s23 + a(3, 2) * s03 - a(3, 3) * s02) * inv;
+    b[1][3] = (a(2, 0) * s23 - a(2, 2) * s03 + a(2, 3) * s02) * inv;
+    b[2][0] = (a(1, 0) * q13 - a(1, 1) * q03 + a(1, 3) * q01) * inv;
+    b[2][1] = (-a(0, 0) * q13 + a(0, 1) * q03 - a(0, 3) * q01) * inv;
+    b[2][2] = (a(3, 0) * s13 - a(3, 1) * s03 + a(3, 3) * s01) * inv;
+    b[2][3] = (-a(2, 0) * s13 + a(2, 1) * s03 - a(2, 3) * s01) * inv;
+    b[3][0] = (-a(1, 0) * q12 + a(1, 1) * q02 - a(1, 2) * q01) * inv;
+    b[3][1] = (a(0, 0) * q12 - a(0, 1) * q02 + a(0, 2) * q01) * inv;
+    b[3][2] = (-a(3, 0) * s12 + a(3, 1) * s02 - a(3, 2) * s01) * inv;
+    b[3][3] = (a(2, 0) * s12 - a(2, 1) * s02 + a(2, 2) * s01) * inv;
+    return Mat4{make_float4(b[0][0], b[1][0], b[2][0], b[3][0]), make_float4(b[0][1], b[1][1], b[2][1], b[3][1]),
+                make_float4(b[0][2], b[1][2], b[2][2], b[3][2]), make_float4(b[0][3], b[1][3], b[2][3], b[3][3])};
+}
+
+// glm-convention product A * B of column-major 4x4s (a left-to-right sum over
+// k), the host's mat_mul.
+__device__ inline Mat4 mul4(const Mat4& A, const Mat4& B) {
+    const float4 a[4] = {A.c0, A.c1, A.c2, A.c3}, b[4] = {B.c0, B.c1, B.c2, B.c3};
+    auto e = [](const float4& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w)); };
+    float4 out[4];
+    for (int j = 0; j < 4; ++j) {
+        float r[4];
+        for (int k = 0; k < 4; ++k) {
+            float acc = e(a[0], k) * e(b[j], 0);
+            acc = acc + e(a[1], k) * e(b[j], 1);
+            acc = acc + e(a[2], k) * e(b[j], 2);
+            acc = acc + e(a[3], k) * e(b[j], 3);
+            r[k] = acc;
+        }
+        out[j] = make_float4(r[0], r[1], r[2], r[3]);
+    }
+    return Mat4{out[0], out[1], out[2], out[3]};
+}
+
 // Paralgram::MultiplyBy4x4Matrix (src/Geometry/Paralgram.cpp:4-15).
 __device__ __forceinline__ Box xform_box(const Mat4& M, const Box& b) {
     return Box{xform(M, b.c, 1.0f), xform(M, b.u, 0.0f), xform(M, b.v, 0.0f), xform(M, b.w, 0.0f)};

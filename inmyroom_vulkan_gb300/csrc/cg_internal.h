@@ -342,7 +342,7 @@ struct ShootQuery {
     float first_global[16];  // the first entity's world matrix (the delta's frame)
     uint32_t tree_a, tree_b;
     uint32_t ray_first, n_first, n_second;  // rays [ray_first, + n_first) from the first, then n_second
-    uint32_t pad[3];
+    uint32_t pad[3];                        // pad[0]: shoot this pair's rays (0: skip them)
 };
 struct ShootRayOut {  // a ray's pass and its reflection's: signed force and ray responses
     float f1[3], r1[3], f2[3], r2[3];
@@ -360,8 +360,34 @@ struct ShootParams {
     float cos_start, cos_finish, bias;
     float* deltas;              // [n_queries][3]
     unsigned* error;            // ERR_QUEUE when a tree is deeper than the traversal stack
+    const unsigned* n_rays_dev; // or null: the rays' count in device memory (at most n_rays)
 };
 cudaError_t launch_shoot(const ShootParams& p, cudaStream_t s);
+
+// A collision frame (cg_frame.cu).
+struct FrameParams {
+    const cg_frame_entity* entities;
+    const uint2* pairs;          // broad-phase pairs (first, second)
+    uint32_t n_pairs;
+    uint32_t max_rays;
+    cg_query* queries;           // [n_pairs] collide queries
+    const cg_ray* rays;          // the collide step's rays
+    const unsigned* n_rays;      // their count (device)
+    uint32_t* counts;            // [2 n_pairs] rays per pair and side, zero before the frame
+    uint32_t* offsets;           // [2 n_pairs]
+    uint32_t* cursor;            // [2 n_pairs]
+    float* grouped;              // [max_rays][6] rays grouped per pair, first entity's then second's
+    uint32_t* tags;              // [max_rays] pair | (from the second entity) << 31
+    ShootQuery* shoot;           // [n_pairs]; pad[0]: an entity moved
+    const float* deltas;         // [n_pairs][3]
+    const cg_ray_average* averages;
+    cg_frame_result* results;
+    unsigned long long results_cap;
+    unsigned long long* n_results;
+};
+cudaError_t launch_frame_queries(const FrameParams& p, cudaStream_t s);
+cudaError_t launch_frame_rays(const FrameParams& p, uint32_t blocks, cudaStream_t s);
+cudaError_t launch_frame_split(const FrameParams& p, cudaStream_t s);
 
 // Kernel launchers (cg_kernels.cu).
 cudaError_t launch_pack(const cg_query* in, uint32_t n, const DevTree* trees, uint32_t n_trees, const float4* recs,

@@ -292,11 +292,22 @@ __device__ __forceinline__ Mat4 mat_of(const float* m) {
 
 __global__ void __launch_bounds__(128) shoot_ray_kernel(const ShootParams P) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n_rays) return;
+    uint32_t nr = P.n_rays;
+    if (P.n_rays_dev) {
+        const uint32_t v = *P.n_rays_dev;
+        nr = v < nr ? v : nr;
+    }
+    if (i >= nr) return;
     const uint32_t tag = P.ray_query[i];
     const uint32_t qi = tag & 0x7fffffffu;
     const bool from_second = (tag >> 31) != 0;
     const ShootQuery& Q = P.q[qi];
+    if (!Q.pad[0]) {  // a pair that is not shot
+        ShootRayOut none;
+        none.ok1 = none.ok2 = 0u;
+        P.out[i] = none;
+        return;
+    }
     const DevTree& TA = P.trees[Q.tree_a];
     const DevTree& TB = P.trees[Q.tree_b];
     const Mat4 M = mat_of(Q.relative);

@@ -222,6 +222,30 @@ def scene(n_entities: int = 256, seed: int = SEED_BASE + 2, tri_lo: int = 500, t
     return Scene(meshes, mats, aabb_pairs(meshes, mats), kinds)
 
 
+def frame_motion(sc: Scene, seed: int = SEED_BASE + 6, still_every: int = 3, step: float = 0.05,
+                 callback_share: float = 0.7) -> tuple[np.ndarray, np.ndarray]:
+    """A previous frame for a scene's current one: every still_every-th entity
+    stands still, the others moved by up to `step` (a translation and a small
+    rotation about their own origin); and should-callback flags for a seeded
+    share of the entities. (previous (n, 16), callback (n,) uint8)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = len(sc.meshes)
+    prev = sc.mats.copy()
+    for i in range(n):
+        if i % still_every == 0:
+            continue
+        M = sc.mats[i].reshape(4, 4).T.astype(np.float64)
+        ax = rng.normal(size=3)
+        ax *= rng.uniform(0.0, step) / np.linalg.norm(ax)
+        R = np.eye(4)
+        R[:3, :3] = axis_angle_matrix(ax)
+        T = np.eye(4)
+        T[:3, 3] = rng.uniform(-step, step, size=3)
+        prev[i] = (T @ M @ R).T.reshape(16).astype(np.float32)
+    callback = (rng.random(n) < callback_share).astype(np.uint8)
+    return prev, callback
+
+
 # ------------------------------------------------------------------ batch sweep
 @dataclass
 class BatchSweep:

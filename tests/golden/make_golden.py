@@ -20,6 +20,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
+from oracle import frame  # noqa: E402
 from inmyroom_vulkan_gb300 import scenes  # noqa: E402
 
 
@@ -121,6 +122,19 @@ def sap_fixture(R):
     np.savez_compressed(os.path.join(HERE, "sap_scene.npz"), callback=cb, pairs=pairs)
 
 
+def frame_fixture(R):
+    """One frame of CollisionDetection::ExecuteCollisionDetection on the
+    256-entity scene (seed 1002) with scenes.frame_motion's previous frame and
+    callback flags: the (first, second) pairs with rays and their deltas, by
+    the reference's own broad phase, mid phase, rays and shooting."""
+    sc = scenes.scene()
+    prev, cb = scenes.frame_motion(sc)
+    trees = [R.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    pairs, deltas = frame.as_arrays(frame.collision_frame(R, trees, sc.mats, prev, cb))
+    np.savez_compressed(os.path.join(HERE, "frame_scene.npz"), previous=prev, callback=cb, pairs=pairs,
+                        deltas=deltas)
+
+
 def main():
     R = oracle.ref()
     if R is None:
@@ -198,6 +212,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "rigid_small.npz"), **out)
     shoot_fixture(R)
     sap_fixture(R)
+    frame_fixture(R)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

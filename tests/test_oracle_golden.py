@@ -153,3 +153,26 @@ def test_sweep_and_prune_matches_reference(port):
     got = port.sweep_and_prune(trees, sc.mats, want["callback"])
     got = got[np.lexsort((got[:, 1], got[:, 0]))]
     assert np.array_equal(got, want["pairs"])
+
+
+def test_collision_frame_matches_reference(port):
+    """One frame of CollisionDetection::ExecuteCollisionDetection on the
+    256-entity scene with a previous frame (a third of the entities still):
+    the same pairs with rays and the same deltas, bit for bit, including the
+    zero deltas of pairs where neither entity moved."""
+    from inmyroom_vulkan_gb300 import scenes
+    from oracle import frame
+
+    want = load("frame_scene.npz")
+    sc = scenes.scene()
+    prev, cb = scenes.frame_motion(sc)
+    assert np.array_equal(prev, want["previous"]) and np.array_equal(cb, want["callback"])
+    trees = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    pairs, deltas = frame.as_arrays(frame.collision_frame(port, trees, sc.mats, prev, cb))
+    assert np.array_equal(pairs, want["pairs"])
+    assert np.array_equal(bits(deltas), bits(want["deltas"]))
+    still = (pairs[:, 0] % 3 == 0) & (pairs[:, 1] % 3 == 0)
+    assert still.any() and not np.abs(deltas[still]).any()
+    assert np.abs(deltas[~still]).sum(1).min() > 0
+    # fewer than two entities: nothing (CollisionDetection.cpp:40)
+    assert frame.collision_frame(port, trees[:1], sc.mats[:1], prev[:1], cb[:1]) == []
