@@ -442,10 +442,14 @@ int cg_shoot_rays(cg_ctx* ctx, const cg_shoot_query* queries, uint32_t n, const 
  * mean ray origin (:84-103). One result per pair with rays (:62-66), the
  * pair as the broad phase orients it; the fan-out of each result to the
  * entities' ancestors (:106-124) needs the engine's entity tree and is the
- * caller's. The deltas can differ from the reference's in the last bits (the
- * rays of a pair are summed in the order the contact kernels make them, the
- * reference's in its unordered_map's order). The broad pairs must fit in
- * max_queries. Synchronous. */
+ * caller's. The pairs are the reference's. The deltas follow the
+ * reference's arithmetic on the step's rays, which match the reference's up to
+ * the last bits of the rays that start at a contact's weighted average point
+ * (summed in another order); a few deltas per frame can differ from the
+ * reference's by up to a percent where such a ray grazes a triangle's edge or
+ * sets the shooting's maximum. After the call, cg_read_rays and
+ * cg_read_ray_averages give the frame's collide step, whose query index is a
+ * result's `query`. The broad pairs must fit in max_queries. Synchronous. */
 typedef struct cg_frame_entity {
     uint32_t tree;
     uint32_t should_callback;
@@ -457,6 +461,8 @@ typedef struct cg_frame_result {
     uint32_t first, second;   /* entity indices */
     float first_delta[3];     /* CollisionCallbackData::deltaVector of the first entity */
     float second_delta[3];    /* and of the second */
+    uint32_t query;           /* the pair's query index in the frame's collide step */
+    uint32_t reserved;
 } cg_frame_result;
 
 int cg_collision_frame(cg_ctx* ctx, const cg_frame_entity* entities, uint32_t n, const cg_shoot_params* params,

@@ -119,8 +119,8 @@ assert SHOOT_QUERY_DTYPE.itemsize == 144
 FRAME_ENTITY_DTYPE = np.dtype([("tree", "<u4"), ("should_callback", "<u4"), ("current_global", "<f4", (16,)),
                                ("previous_global", "<f4", (16,))])
 FRAME_RESULT_DTYPE = np.dtype([("first", "<u4"), ("second", "<u4"), ("first_delta", "<f4", (3,)),
-                               ("second_delta", "<f4", (3,))])
-assert FRAME_ENTITY_DTYPE.itemsize == 136 and FRAME_RESULT_DTYPE.itemsize == 32
+                               ("second_delta", "<f4", (3,)), ("query", "<u4"), ("reserved", "<u4")])
+assert FRAME_ENTITY_DTYPE.itemsize == 136 and FRAME_RESULT_DTYPE.itemsize == 40
 assert QUERY_DTYPE.itemsize == 72 and TRI_PAIR_DTYPE.itemsize == 36 and LEAF_PAIR_DTYPE.itemsize == 16
 assert CONTACT_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32 and RAY_AVERAGE_DTYPE.itemsize == 32
 

@@ -1626,7 +1626,10 @@ int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, c
     CG_CUDA(cudaStreamSynchronize(s), "broad phase");
     if (np > max_pairs)
         return fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu broad-phase pairs > max_queries %u", np, max_pairs);
-    if (np == 0) return CG_OK;
+    if (np == 0) {
+        c->last_flags = 0;  // no collide step in this frame: nothing to read
+        return CG_OK;
+    }
     // collide every broad pair with contacts and rays
     FrameParams fp{};
     fp.entities = d_ent;

@@ -12,8 +12,9 @@
 //   movement of its mean ray origin (:84-97), appended to the results.
 // The rays of a pair come out of the contact kernels in no fixed order (the
 // reference's come out of an unordered_map), so the summed force responses
-// can differ from the reference's in the last bits; every other step is the
-// reference's arithmetic.
+// can differ from the reference's in the last bits, and so can the origins of
+// the rays that start at a contact's weighted average point; every other step
+// is the reference's arithmetic.
 #include <cuda_runtime.h>
 
 #include "cg_device.cuh"
@@ -155,6 +156,8 @@ __global__ void frame_split_kernel(const FrameParams P) {
     }
     r.first_delta[0] = d1.x, r.first_delta[1] = d1.y, r.first_delta[2] = d1.z;
     r.second_delta[0] = d2.x, r.second_delta[1] = d2.y, r.second_delta[2] = d2.z;
+    r.query = k;
+    r.reserved = 0u;
     const unsigned long long o = atomicAdd(P.n_results, 1ull);
     if (o < P.results_cap) P.results[o] = r;
 }

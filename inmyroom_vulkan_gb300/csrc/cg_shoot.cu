@@ -3,12 +3,13 @@
 // pairs, over Ray::IntersectOBBtree closest-hit traversals
 // (src/Geometry/Ray.cpp:36-237).
 //
-//   shoot_ray_kernel    a thread per ray: the Hermann pass of the ray (the
+//   shoot_ray_kernel    four lanes per ray: the Hermann pass of the ray (the
 //                       closest hit on the other tree, a back face, no nearer
-//                       hit on its own tree from the origin moved by 4 ulps),
-//                       and when it succeeds the pass of its reflection back;
-//                       each success as (signed force response, signed ray
-//                       response)
+//                       hit on its own tree from the origin moved by 4 ulps;
+//                       the two traversals side by side, each kept by a lane
+//                       pair), and when it succeeds the pass of its
+//                       reflection back; each success as (signed force
+//                       response, signed ray response)
 //   shoot_query_kernel  a thread per pair: the force responses summed in the
 //                       reference's order (rays from the first entity, each
 //                       followed by its reflection, then those from the
@@ -116,14 +117,20 @@ __device__ __forceinline__ void rec_box(const float4* recs, uint32_t r, Box& b, 
     meta = __float_as_uint(d.y);
 }
 
-// Ray::IntersectOBBtree (Ray.cpp:135-237) on the tree rooted at record root.
+// Ray::IntersectOBBtree (Ray.cpp:135-237) on the tree rooted at record root,
+// by a lane pair (c = 0, 1; pm = the pair's mask) that keeps one traversal in
+// step: both lanes hold the same stack; at an inner node lane c tests child
+// c's box and the pair swaps the results, at a leaf lane c tests every other
+// triangle and the pair keeps the nearer hit (equal distances: the lower
+// triangle, as the one-lane scan keeps the first). A stack entry carries the
+// child's own link word and leaf word, read when its box was tested.
 __device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t root, const Mat4& matrix, float3 origin,
-                            float3 dir, unsigned* error) {
+                            float3 dir, unsigned* error, uint32_t c, unsigned pm) {
     Mat4 cm = matrix;
     if (!(origin.x == 0.f && origin.y == 0.f && origin.z == 0.f))
         cm.c3 = make_float4(matrix.c3.x - origin.x, matrix.c3.y - origin.y, matrix.c3.z - origin.z, matrix.c3.w - 0.f);
     TreeHit best{false, false, __int_as_float(0x7f800000), 0xffffffffu, 0.f, 0.f};
-    uint32_t st_rec[kShootStack];
+    uint32_t st_ref[kShootStack], st_meta[kShootStack];
     float st_min[kShootStack];
     uint32_t sp = 0;
     {
@@ -132,7 +139,8 @@ __device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t roo
         rec_box(recs, root, b, ref, meta);
         const Slab h = ray_box(xform_box(cm, b), dir);
         if (h.hit && h.tmax >= 0.f) {
-            st_rec[0] = root;
+            st_ref[0] = ref;
+            st_meta[0] = meta;
             st_min[0] = -__int_as_float(0x7f800000);  // the root is entered without the distance check
             sp = 1;
         }
@@ -140,23 +148,26 @@ __device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t roo
     const float3 zero = make_float3(0.f, 0.f, 0.f);
     while (sp) {
         --sp;
-        const uint32_t r = st_rec[sp];
+        const uint32_t ref = st_ref[sp], meta = st_meta[sp];
         if (!(st_min[sp] < best.dist)) continue;
-        Box nb;
-        uint32_t ref, meta;
-        rec_box(recs, r, nb, ref, meta);
         if (!(meta & kLeafFlag)) {
-            Box lb, rb;
-            uint32_t lref, lmeta, rref, rmeta;
-            rec_box(recs, ref, lb, lref, lmeta);
-            rec_box(recs, ref + 1u, rb, rref, rmeta);
-            const Slab hl = ray_box(xform_box(cm, lb), dir);
-            const Slab hr = ray_box(xform_box(cm, rb), dir);
-            auto push = [&](uint32_t rec, const Slab& h) {
-                if (h.tmax < 0.f) return;  // the box is behind the ray
+            Box b;
+            uint32_t cref, cmeta;
+            rec_box(recs, ref + c, b, cref, cmeta);
+            const Slab h = ray_box(xform_box(cm, b), dir);
+            const int ohit = __shfl_xor_sync(pm, int(h.hit), 1);
+            const float omin = __shfl_xor_sync(pm, h.tmin, 1), omax = __shfl_xor_sync(pm, h.tmax, 1);
+            const uint32_t oref = __shfl_xor_sync(pm, cref, 1), ometa = __shfl_xor_sync(pm, cmeta, 1);
+            const Slab other{ohit != 0, omin, omax};
+            const Slab hl = c ? other : h, hr = c ? h : other;
+            const uint32_t lref = c ? oref : cref, lmeta = c ? ometa : cmeta;
+            const uint32_t rref = c ? cref : oref, rmeta = c ? cmeta : ometa;
+            auto push = [&](uint32_t r, uint32_t m, const Slab& s) {
+                if (s.tmax < 0.f) return;  // the box is behind the ray
                 if (sp < kShootStack) {
-                    st_rec[sp] = rec;
-                    st_min[sp] = h.tmin;
+                    st_ref[sp] = r;
+                    st_meta[sp] = m;
+                    st_min[sp] = s.tmin;
                     ++sp;
                 } else {
                     atomicOr(error, ERR_QUEUE);
@@ -165,21 +176,22 @@ __device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t roo
             if (hl.hit && hr.hit) {
                 // the later one first, so that the nearer one is taken next
                 if (hl.tmin < hr.tmin) {
-                    push(ref + 1u, hr);
-                    push(ref, hl);
+                    push(rref, rmeta, hr);
+                    push(lref, lmeta, hl);
                 } else {
-                    push(ref, hl);
-                    push(ref + 1u, hr);
+                    push(lref, lmeta, hl);
+                    push(rref, rmeta, hr);
                 }
             } else if (hl.hit) {
-                push(ref, hl);
+                push(lref, lmeta, hl);
             } else if (hr.hit) {
-                push(ref + 1u, hr);
+                push(rref, rmeta, hr);
             }
             continue;
         }
         const uint32_t n = meta & 0xffffu;
-        for (uint32_t i = ref; i != ref + n; ++i) {
+        TreeHit mine = best;
+        for (uint32_t i = ref + c; i < ref + n; i += 2u) {
             const float4* t4 = tris + 3ull * i;
             const float4 q0 = __ldg(t4), q1 = __ldg(t4 + 1), q2 = __ldg(t4 + 2);
             const float3 p0 = xform(cm, make_float3(q0.x, q0.y, q0.z), 1.0f);
@@ -188,15 +200,25 @@ __device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t roo
             float bx = 0.f, by = 0.f, t = 0.f;
             bool back = false;
             const bool hit = ray_tri(zero, dir, p0, p1, p2, bx, by, t, back);
-            if (hit && t > 0.f && t < best.dist) {
-                best.hit = true;
-                best.back = back;
-                best.dist = t;
-                best.tri = i;
-                best.bx = bx;
-                best.by = by;
+            if (hit && t > 0.f && t < mine.dist) {
+                mine.hit = true;
+                mine.back = back;
+                mine.dist = t;
+                mine.tri = i;
+                mine.bx = bx;
+                mine.by = by;
             }
         }
+        TreeHit oth;
+        const int flags = __shfl_xor_sync(pm, int(mine.hit) | (int(mine.back) << 1), 1);
+        oth.hit = (flags & 1) != 0;
+        oth.back = (flags & 2) != 0;
+        oth.dist = __shfl_xor_sync(pm, mine.dist, 1);
+        oth.tri = __shfl_xor_sync(pm, mine.tri, 1);
+        oth.bx = __shfl_xor_sync(pm, mine.bx, 1);
+        oth.by = __shfl_xor_sync(pm, mine.by, 1);
+        const bool take = oth.dist < mine.dist || (!(mine.dist < oth.dist) && oth.tri < mine.tri);
+        best = take ? oth : mine;
     }
     return best;
 }
@@ -235,17 +257,46 @@ struct Pass {
     float3 response, normal;
 };
 
-// ShootUncollideRays::HermannPass (ShootUncollideRays.cpp:127-158).
-__device__ Pass hermann(const ShootParams& P, const Side& A, const Side& B, const Mat3s& nb, float3 o, float3 d) {
+// The lanes of a ray: a quad; lanes 0-1 and 2-3 are the pairs of the two
+// traversals of a pass.
+struct Quad {
+    uint32_t q;     // lane within the quad
+    uint32_t base;  // the quad's first lane in the warp
+    unsigned qm;    // the quad's mask
+    unsigned pm;    // the lane pair's mask
+};
+
+__device__ __forceinline__ TreeHit shfl_hit(const TreeHit& h, uint32_t src, unsigned m) {
+    TreeHit o;
+    const int f = __shfl_sync(m, int(h.hit) | (int(h.back) << 1), src);
+    o.hit = (f & 1) != 0;
+    o.back = (f & 2) != 0;
+    o.dist = __shfl_sync(m, h.dist, src);
+    o.tri = __shfl_sync(m, h.tri, src);
+    o.bx = __shfl_sync(m, h.bx, src);
+    o.by = __shfl_sync(m, h.by, src);
+    return o;
+}
+
+// ShootUncollideRays::HermannPass (ShootUncollideRays.cpp:127-158). Its two
+// traversals (the closest hit on B from the origin, on A from the origin moved
+// by 4 ulps) do not depend on each other: lane pair 0 runs the first, pair 1
+// the second (which the reference skips when the first fails; its result is
+// then unused), and the quad shares both.
+__device__ Pass hermann(const ShootParams& P, const Side& A, const Side& B, const Mat3s& nb, float3 o, float3 d,
+                        const Quad& L) {
     Pass r{false, make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    const TreeHit p2 = ray_tree(P.recs, P.tris, B.root, B.m, o, d, P.error);
-    if (!(p2.hit && p2.back)) return r;
     // Ray::MoveOriginEpsilonTowardsDirection(4) (Ray.cpp:13-20)
     const float big = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
     const float eps = big * FLT_EPSILON;
     const float3 moved = add3s(o, scale3s(4.f * eps, d));
     const float eps_dist = length3(sub3(moved, o));
-    const TreeHit p3 = ray_tree(P.recs, P.tris, A.root, A.m, moved, d, P.error);
+    const bool own = (L.q >> 1) != 0u;
+    const TreeHit h = ray_tree(P.recs, P.tris, own ? A.root : B.root, own ? A.m : B.m, own ? moved : o, d, P.error,
+                               L.q & 1u, L.pm);
+    const TreeHit p2 = shfl_hit(h, L.base, L.qm);
+    const TreeHit p3 = shfl_hit(h, L.base + 2u, L.qm);
+    if (!(p2.hit && p2.back)) return r;
     if (p2.dist <= p3.dist + eps_dist) {
         r.ok = true;
         r.response = scale3s(p2.dist, d);
@@ -290,57 +341,67 @@ __device__ __forceinline__ Mat4 mat_of(const float* m) {
                 make_float4(m[8], m[9], m[10], m[11]), make_float4(m[12], m[13], m[14], m[15])};
 }
 
+// Four lanes per ray (a quad), the rays strided over the grid.
 __global__ void __launch_bounds__(128) shoot_ray_kernel(const ShootParams P) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nr = P.n_rays;
     if (P.n_rays_dev) {
         const uint32_t v = *P.n_rays_dev;
         nr = v < nr ? v : nr;
     }
-    if (i >= nr) return;
-    const uint32_t tag = P.ray_query[i];
-    const uint32_t qi = tag & 0x7fffffffu;
-    const bool from_second = (tag >> 31) != 0;
-    const ShootQuery& Q = P.q[qi];
-    if (!Q.pad[0]) {  // a pair that is not shot
-        ShootRayOut none;
-        none.ok1 = none.ok2 = 0u;
-        P.out[i] = none;
-        return;
-    }
-    const DevTree& TA = P.trees[Q.tree_a];
-    const DevTree& TB = P.trees[Q.tree_b];
-    const Mat4 M = mat_of(Q.relative);
-    const Mat4 I = Mat4{make_float4(1.f, 0.f, 0.f, 0.f), make_float4(0.f, 1.f, 0.f, 0.f), make_float4(0.f, 0.f, 1.f, 0.f),
-                        make_float4(0.f, 0.f, 0.f, 1.f)};
-    const Mat3s N = cofactor(M);
-    const Mat3s I3 = Mat3s{make_float3(1.f, 0.f, 0.f), make_float3(0.f, 1.f, 0.f), make_float3(0.f, 0.f, 1.f)};
-    const Side first{TA.rec_base + 1u, TA.tri_base, TA.nrm, I};
-    const Side second{TB.rec_base + 1u, TB.tri_base, TB.nrm, M};
-    const float* ray = P.rays + 6ull * i;
-    const float3 o = get3(ray), d = get3(ray + 3);
-    ShootRayOut out;
-    out.ok1 = out.ok2 = 0u;
-    // first to second: the pass against the second entity (force subtracted,
-    // response negated); second to first: against the first entity
-    auto pass = [&](bool to_first, float3 po, float3 pd, float* f, float* rr) -> Pass {
-        const Pass h = to_first ? hermann(P, second, first, I3, po, pd) : hermann(P, first, second, N, po, pd);
-        if (h.ok) {
-            const float3 fr = force_response(h);
-            put3(f, to_first ? fr : neg3(fr));
-            put3(rr, to_first ? h.response : neg3(h.response));
+    Quad L;
+    const uint32_t lane = threadIdx.x & 31u;
+    L.q = lane & 3u;
+    L.base = lane & ~3u;
+    L.qm = 0xfu << L.base;
+    L.pm = 0x3u << (lane & ~1u);
+    const uint32_t stride = (gridDim.x * blockDim.x) >> 2;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < nr; i += stride) {
+        const uint32_t tag = P.ray_query[i];
+        const uint32_t qi = tag & 0x7fffffffu;
+        const bool from_second = (tag >> 31) != 0;
+        const ShootQuery& Q = P.q[qi];
+        if (!Q.pad[0]) {  // a pair that is not shot
+            if (L.q == 0u) {
+                ShootRayOut none;
+                none.ok1 = none.ok2 = 0u;
+                P.out[i] = none;
+            }
+            continue;
         }
-        return h;
-    };
-    const Pass h1 = pass(from_second, o, d, out.f1, out.r1);
-    if (h1.ok) {
-        out.ok1 = 1u;
-        // ShootUncollideRays::ReflectHermannResult (ShootUncollideRays.cpp:100-106)
-        const float3 ro = add3s(o, h1.response), rd = neg3(h1.normal);
-        const Pass h2 = pass(!from_second, ro, rd, out.f2, out.r2);
-        out.ok2 = h2.ok ? 1u : 0u;
+        const DevTree& TA = P.trees[Q.tree_a];
+        const DevTree& TB = P.trees[Q.tree_b];
+        const Mat4 M = mat_of(Q.relative);
+        const Mat4 I = Mat4{make_float4(1.f, 0.f, 0.f, 0.f), make_float4(0.f, 1.f, 0.f, 0.f),
+                            make_float4(0.f, 0.f, 1.f, 0.f), make_float4(0.f, 0.f, 0.f, 1.f)};
+        const Mat3s N = cofactor(M);
+        const Mat3s I3 = Mat3s{make_float3(1.f, 0.f, 0.f), make_float3(0.f, 1.f, 0.f), make_float3(0.f, 0.f, 1.f)};
+        const Side first{TA.rec_base + 1u, TA.tri_base, TA.nrm, I};
+        const Side second{TB.rec_base + 1u, TB.tri_base, TB.nrm, M};
+        const float* ray = P.rays + 6ull * i;
+        const float3 o = get3(ray), d = get3(ray + 3);
+        ShootRayOut out;
+        out.ok1 = out.ok2 = 0u;
+        // first to second: the pass against the second entity (force subtracted,
+        // response negated); second to first: against the first entity
+        auto pass = [&](bool to_first, float3 po, float3 pd, float* f, float* rr) -> Pass {
+            const Pass h = to_first ? hermann(P, second, first, I3, po, pd, L) : hermann(P, first, second, N, po, pd, L);
+            if (h.ok) {
+                const float3 fr = force_response(h);
+                put3(f, to_first ? fr : neg3(fr));
+                put3(rr, to_first ? h.response : neg3(h.response));
+            }
+            return h;
+        };
+        const Pass h1 = pass(from_second, o, d, out.f1, out.r1);
+        if (h1.ok) {
+            out.ok1 = 1u;
+            // ShootUncollideRays::ReflectHermannResult (ShootUncollideRays.cpp:100-106)
+            const float3 ro = add3s(o, h1.response), rd = neg3(h1.normal);
+            const Pass h2 = pass(!from_second, ro, rd, out.f2, out.r2);
+            out.ok2 = h2.ok ? 1u : 0u;
+        }
+        if (L.q == 0u) P.out[i] = out;
     }
-    P.out[i] = out;
 }
 
 // ShootUncollideRays::SmootherStep (ShootUncollideRays.cpp:175-179).
@@ -387,7 +448,10 @@ __global__ void shoot_query_kernel(const ShootParams P) {
 }  // namespace
 
 cudaError_t launch_shoot(const ShootParams& p, cudaStream_t s) {
-    if (p.n_rays) shoot_ray_kernel<<<(p.n_rays + 127u) / 128u, 128, 0, s>>>(p);
+    if (p.n_rays) {
+        const uint64_t blocks = (4ull * p.n_rays + 127u) / 128u;  // a quad per ray, strided beyond 8192 blocks
+        shoot_ray_kernel<<<uint32_t(blocks < 8192u ? blocks : 8192u), 128, 0, s>>>(p);
+    }
     if (p.n_queries) shoot_query_kernel<<<(p.n_queries + 127u) / 128u, 128, 0, s>>>(p);
     return cudaGetLastError();
 }
