@@ -124,8 +124,8 @@ __device__ __forceinline__ void rec_box(const float4* recs, uint32_t r, Box& b, 
 // triangle and the pair keeps the nearer hit (equal distances: the lower
 // triangle, as the one-lane scan keeps the first). A stack entry carries the
 // child's own link word and leaf word, read when its box was tested.
-__device__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t root, const Mat4& matrix, float3 origin,
-                            float3 dir, unsigned* error, uint32_t c, unsigned pm) {
+__device__ __noinline__ TreeHit ray_tree(const float4* recs, const float4* tris, uint32_t root, const Mat4& matrix,
+                                         float3 origin, float3 dir, unsigned* error, uint32_t c, unsigned pm) {
     Mat4 cm = matrix;
     if (!(origin.x == 0.f && origin.y == 0.f && origin.z == 0.f))
         cm.c3 = make_float4(matrix.c3.x - origin.x, matrix.c3.y - origin.y, matrix.c3.z - origin.z, matrix.c3.w - 0.f);
@@ -342,7 +342,7 @@ __device__ __forceinline__ Mat4 mat_of(const float* m) {
 }
 
 // Four lanes per ray (a quad), the rays strided over the grid.
-__global__ void __launch_bounds__(128) shoot_ray_kernel(const ShootParams P) {
+__global__ void __launch_bounds__(128, 6) shoot_ray_kernel(const ShootParams P) {
     uint32_t nr = P.n_rays;
     if (P.n_rays_dev) {
         const uint32_t v = *P.n_rays_dev;
@@ -379,28 +379,36 @@ __global__ void __launch_bounds__(128) shoot_ray_kernel(const ShootParams P) {
         const Side second{TB.rec_base + 1u, TB.tri_base, TB.nrm, M};
         const float* ray = P.rays + 6ull * i;
         const float3 o = get3(ray), d = get3(ray + 3);
-        ShootRayOut out;
-        out.ok1 = out.ok2 = 0u;
-        // first to second: the pass against the second entity (force subtracted,
-        // response negated); second to first: against the first entity
-        auto pass = [&](bool to_first, float3 po, float3 pd, float* f, float* rr) -> Pass {
-            const Pass h = to_first ? hermann(P, second, first, I3, po, pd, L) : hermann(P, first, second, N, po, pd, L);
-            if (h.ok) {
-                const float3 fr = force_response(h);
-                put3(f, to_first ? fr : neg3(fr));
-                put3(rr, to_first ? h.response : neg3(h.response));
-            }
-            return h;
-        };
-        const Pass h1 = pass(from_second, o, d, out.f1, out.r1);
-        if (h1.ok) {
-            out.ok1 = 1u;
+        // The ray's pass, then (when it succeeds) its reflection's pass back, in
+        // one loop so that the traversal code exists once. First to second: the
+        // pass against the second entity (force subtracted, response negated);
+        // second to first: against the first entity.
+        float3 res[4];  // f1, r1, f2, r2
+        uint32_t ok = 0;
+        float3 po = o, pd = d;
+        bool to_first = from_second;
+#pragma unroll 1
+        for (uint32_t k = 0; k < 2u; ++k) {
+            const Pass h = hermann(P, to_first ? second : first, to_first ? first : second, to_first ? I3 : N, po, pd,
+                                   L);
+            if (!h.ok) break;
+            const float3 fr = force_response(h);
+            res[2 * k] = to_first ? fr : neg3(fr);
+            res[2 * k + 1] = to_first ? h.response : neg3(h.response);
+            ok = k + 1u;
             // ShootUncollideRays::ReflectHermannResult (ShootUncollideRays.cpp:100-106)
-            const float3 ro = add3s(o, h1.response), rd = neg3(h1.normal);
-            const Pass h2 = pass(!from_second, ro, rd, out.f2, out.r2);
-            out.ok2 = h2.ok ? 1u : 0u;
+            po = add3s(o, h.response);
+            pd = neg3(h.normal);
+            to_first = !to_first;
         }
-        if (L.q == 0u) P.out[i] = out;
+        if (L.q == 0u) {
+            ShootRayOut out;
+            out.ok1 = ok >= 1u ? 1u : 0u;
+            out.ok2 = ok >= 2u ? 1u : 0u;
+            if (ok >= 1u) put3(out.f1, res[0]), put3(out.r1, res[1]);
+            if (ok >= 2u) put3(out.f2, res[2]), put3(out.r2, res[3]);
+            P.out[i] = out;
+        }
     }
 }
 
