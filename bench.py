@@ -118,14 +118,39 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def build_scene(seed: int):
-    import oracle
-    from inmyroom_vulkan_gb300 import scenes
+def run_tree_build(ctx, sc, cpu_seconds: float) -> tuple[np.ndarray, dict]:
+    """OBB trees of the scene's meshes built on the device (cg_tree_build, one
+    call for all 256, trees uploaded); host-timed around the synchronous call,
+    the second of two builds. Beside it the oracle's builder on all host
+    cores. Returns the trees' ids and the line."""
+    ids = ctx.build_trees(sc.meshes)
+    for tid in ids:
+        ctx.free_tree(int(tid))
+    t0 = time.perf_counter()
+    ids = ctx.build_trees(sc.meshes)
+    ms = 1e3 * (time.perf_counter() - t0)
+    tris = int(sum(m.n_tris for m in sc.meshes))
+    line = {"workload": f"OBB trees of the scene's {len(sc.meshes)} meshes ({tris} triangles), one cg_tree_build",
+            "ms": ms, "triangles_per_s": tris / (ms / 1e3),
+            "timing": "host perf_counter around the synchronous call (meshes uploaded, trees uploaded)"}
+    if cpu_seconds > 0:
+        from concurrent.futures import ThreadPoolExecutor
 
-    sc = scenes.scene(seed=seed)
-    port = oracle.port()
-    trees = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
-    return sc, trees
+        import oracle
+
+        fast = oracle.port(fast=True)
+        cores = os.cpu_count() or 1
+        pool = ThreadPoolExecutor(cores)
+        runs, t0 = 0, time.perf_counter()
+        while True:
+            list(pool.map(lambda m: fast.tree_build(m.points, m.indices, m.normals), sc.meshes))
+            runs += 1
+            if time.perf_counter() - t0 >= cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"ms": 1e3 * el / runs, "cores": cores, "kind": "port",
+                                "sample": f"{runs} builds of all the scene's trees, {el:.1f} s, release flags"}
+    return ids, line
 
 
 def cpu_baseline(sc, seconds: float = 10.0) -> dict:
@@ -310,10 +335,8 @@ def run_sweep(args, local: int, flush, stream, cpu_seconds: float) -> dict:
     from inmyroom_vulkan_gb300 import autotune, capi, scenes
 
     bs = scenes.batch_sweep()
-    port = oracle.port(fast=True)
-    trees = [port.tree_build(m.points, m.indices, m.normals) for m in bs.meshes]
     ctx = capi.Context(device=local, max_queries=16384, max_tri_pairs=1 << 23, max_leaf_pairs=1 << 24)
-    ids = np.array([ctx.upload_flat(t.export()) for t in trees], np.uint32)
+    ids = ctx.build_trees(bs.meshes)
     rel = np.stack([capi.relative_matrix(a, b) for a, b in zip(bs.mats_a, bs.mats_b)])
     q = capi.make_queries(ids[bs.qa], ids[bs.qb], rel)
     n = len(q)
@@ -369,6 +392,8 @@ def run_sweep(args, local: int, flush, stream, cpu_seconds: float) -> dict:
            "cache": "L2 flushed (512 MB write) before every timed launch", "launch": "CUDA graph after tuning"}
     ctx.close()
     if cpu_seconds > 0:
+        port = oracle.port(fast=True)
+        trees = [port.tree_build(m.points, m.indices, m.normals) for m in bs.meshes]
         cores = os.cpu_count() or 1
         ta = [trees[i] for i in bs.qa[:P]]
         tb = [trees[i] for i in bs.qb[:P]]
@@ -393,19 +418,16 @@ def run_differentiable(args, ctx_factory, flush, stream, cpu_seconds: float) -> 
     same pair set on the host (torch autograd on the CPU)."""
     import torch
 
-    import oracle
     from inmyroom_vulkan_gb300 import capi, scenes
     from inmyroom_vulkan_gb300.energy import DeformingCollider, penetration_energy
 
     sc = scenes.deforming()
     n = sc.vertices.shape[0]
     parent, offsets = scenes.chain_skeleton(sc)
-    port = oracle.port(fast=True)
-    rest = port.tree_build(sc.mesh.points, sc.mesh.indices, sc.mesh.normals)
-    field = port.tree_build(sc.field.points, sc.field.indices, sc.field.normals)
-    rf, ff = rest.export(), field.export()
     ctx = ctx_factory()
-    fid = ctx.upload_flat(ff)
+    rid, fid = (int(t) for t in ctx.build_trees([sc.mesh, sc.field]))
+    rf, ff = ctx.export_tree(rid), ctx.export_tree(fid)
+    ctx.free_tree(rid)
     eye = np.eye(4, dtype=np.float32).reshape(16)
     rel = np.stack([capi.relative_matrix(m, eye) for m in sc.models])
     col = DeformingCollider(ctx, rf, capi.Skeleton(parent, offsets), sc.vertices, sc.joints, sc.weights,
@@ -476,13 +498,11 @@ def run_deforming(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
     sc = scenes.deforming()
     n = sc.vertices.shape[0]
     V = sc.vertices.shape[1]
-    port = oracle.port(fast=True)
-    rest = port.tree_build(sc.mesh.points, sc.mesh.indices, sc.mesh.normals)
-    field = port.tree_build(sc.field.points, sc.field.indices, sc.field.normals)
-    rest_flat = rest.export()
     ctx = ctx_factory()
-    ids = [ctx.upload_flat(rest_flat) for _ in range(n)]
-    fid = ctx.upload_flat(field.export())
+    rid, fid = (int(t) for t in ctx.build_trees([sc.mesh, sc.field]))
+    rest_arrays = ctx.export_tree(rid)
+    ctx.free_tree(rid)
+    ids = [ctx.upload_flat(rest_arrays) for _ in range(n)]
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
     j, w, ib = dev(sc.joints.view(np.int16)), dev(sc.weights), dev(sc.inverse_bind)
     keep, views, outs = [j, w, ib], [], []
@@ -534,6 +554,9 @@ def run_deforming(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
     if cpu_seconds > 0:
         from concurrent.futures import ThreadPoolExecutor
 
+        port = oracle.port(fast=True)
+        rest_flat = port.tree_build(sc.mesh.points, sc.mesh.indices, sc.mesh.normals).export()
+        field = port.tree_build(sc.field.points, sc.field.indices, sc.field.normals)
         cores = os.cpu_count() or 1
         pool = ThreadPoolExecutor(cores)
 
@@ -572,9 +595,9 @@ def run_gpu(args) -> dict:
     dev = torch.device("cuda", local)
 
     # each rank collides its own scene replica (weak scaling, no data exchange)
-    sc, trees = build_scene(seed=1002 + 1000 * rank)
+    sc = scenes.scene(seed=1002 + 1000 * rank)
     ctx = capi.Context(device=local, max_queries=max(4096, len(sc.pairs)), max_tri_pairs=1 << 22)
-    ids = np.array([ctx.upload_flat(t.export()) for t in trees], np.uint32)
+    ids, tree_build = run_tree_build(ctx, sc, min(args.cpu_seconds, 5.0) if rank == 0 else 0.0)
     qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
     rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
     q = capi.make_queries(ids[qa], ids[qb], rel)
@@ -672,11 +695,7 @@ def run_gpu(args) -> dict:
 
     # plain path: the rigid pair, one query per launch (the reference's unit of work)
     rp = scenes.rigid_pair(n_poses=200)
-    import oracle
-
-    port = oracle.port()
-    pt = [port.tree_build(m.points, m.indices, m.normals) for m in (rp.mesh_a, rp.mesh_b)]
-    pid = [ctx.upload_flat(t.export()) for t in pt]
+    pid = [int(t) for t in ctx.build_trees([rp.mesh_a, rp.mesh_b])]
     prel = np.stack([capi.relative_matrix(a, b) for a, b in zip(rp.mats_a, rp.mats_b)])
     pq = capi.make_queries(np.full(200, pid[0]), np.full(200, pid[1]), prel)
     d_pq = torch.from_numpy(pq.view(np.uint8).copy()).to(dev)
@@ -754,6 +773,8 @@ def run_gpu(args) -> dict:
         out["batch_sweep"] = sweep
     if shoot:
         out["shoot"] = shoot
+    if rank == 0:
+        out["tree_build"] = tree_build
     if frame_line:
         out["frame"] = frame_line
     ctx.close()

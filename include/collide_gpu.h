@@ -109,6 +109,39 @@ typedef struct cg_tree_view {
 int cg_tree_upload(cg_ctx* ctx, const cg_tree_view* view, uint32_t* tree_id);
 int cg_tree_free(cg_ctx* ctx, uint32_t tree_id);
 
+/* An indexed triangle mesh: the vertex and index buffers the engine reads
+ * its collision triangles from (one Triangle per index triple, with the
+ * vertices' positions, normals and indices). */
+typedef struct cg_mesh_view {
+    const float* positions;   /* [n_vertices][3] */
+    const float* normals;     /* [n_vertices][3], or NULL (rays then use the face normal) */
+    const uint32_t* indices;  /* [n_triangles][3], each < n_vertices */
+    uint32_t n_vertices;
+    uint32_t n_triangles;
+} cg_mesh_view;
+
+/* OBBtree::OBBtree(std::vector<Triangle>&&) (src/Geometry/OBBtree.cpp:321-358)
+ * for n meshes on the device: the PCA-fitted boxes (FP64 covariance and eig3,
+ * OBB.cpp:33-166), the centre splits of at most 4 triangles per leaf
+ * (OBBtree.cpp:43-108) and the pre-order layout, bit-identical to the
+ * reference builder's tree; then each tree is uploaded as by cg_tree_upload.
+ * tree_ids[n] out. CG_ERR_BAD_TREE for an index outside its mesh's vertices.
+ * Synchronous. */
+int cg_tree_build(cg_ctx* ctx, const cg_mesh_view* meshes, uint32_t n, uint32_t* tree_ids);
+
+/* A tree's sizes, and its whole flat layout back in the form of
+ * cg_tree_view (the tree cache's content): root box, node_obbs[node_count][2],
+ * node_ref and node_tri_count [node_count][2], triangles_position and
+ * triangles_normal [triangle_count][3][3], triangles_indices [triangle_count][3]
+ * (a tree uploaded without indices gives 3t + k). Any pointer may be NULL;
+ * the arrays must hold the sizes cg_tree_info gives. Normals exist when
+ * has_normals is 1. Waits for the context's stream. */
+int cg_tree_info(cg_ctx* ctx, uint32_t tree_id, uint32_t* node_count, uint32_t* triangle_count,
+                 uint32_t* has_normals);
+int cg_tree_export(cg_ctx* ctx, uint32_t tree_id, cg_obb* root, cg_obb* node_obbs, uint32_t* node_ref,
+                   uint32_t* node_tri_count, float* triangles_position, float* triangles_normal,
+                   uint32_t* triangles_indices);
+
 /* ---- queries ---------------------------------------------------------- */
 
 /* One entity pair, the unit of OBBtreesCollision::ExecuteOBBtreesCollision.

@@ -34,7 +34,7 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
            "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
            "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays",
-           "cg_broad_phase", "cg_collision_frame"]
+           "cg_broad_phase", "cg_collision_frame", "cg_tree_build", "cg_tree_info", "cg_tree_export"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -62,6 +62,32 @@ class cg_tree_view(C.Structure):
                 ("node_ref", C.c_void_p), ("node_tri_count", C.c_void_p), ("triangle_count", C.c_uint32),
                 ("triangles_position", C.c_void_p), ("triangles_normal", C.c_void_p),
                 ("triangles_indices", C.c_void_p)]
+
+
+class cg_mesh_view(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("indices", C.c_void_p),
+                ("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32)]
+
+
+class TreeArrays:
+    """A tree's flat layout (cg_tree_export): the reference's node layout
+    (OBBtree.h:61-75) with its triangles in leaf order."""
+
+    def __init__(self, root, node_obbs, node_ref, node_cnt, tri_pos, tri_nrm, tri_idx):
+        self.root = np.ascontiguousarray(root, np.float32).reshape(12)
+        self.node_obbs = np.ascontiguousarray(node_obbs, np.float32).reshape(-1, 2, 12)
+        self.node_ref = np.ascontiguousarray(node_ref, np.uint32).reshape(-1, 2)
+        self.node_cnt = np.ascontiguousarray(node_cnt, np.uint32).reshape(-1, 2)
+        self.tri_pos = np.ascontiguousarray(tri_pos, np.float32).reshape(-1, 9)
+        self.tri_nrm = None if tri_nrm is None else np.ascontiguousarray(tri_nrm, np.float32).reshape(-1, 9)
+        self.tri_idx = np.ascontiguousarray(tri_idx, np.uint32).reshape(-1, 3)
+
+    def arrays(self) -> dict:
+        d = dict(root=self.root, node_obbs=self.node_obbs, node_ref=self.node_ref, node_cnt=self.node_cnt,
+                 tri_pos=self.tri_pos, tri_idx=self.tri_idx)
+        if self.tri_nrm is not None:
+            d["tri_nrm"] = self.tri_nrm
+        return d
 
 
 class cg_deform_view(C.Structure):
@@ -145,6 +171,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_status_string.restype = C.c_char_p
     lib.cg_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     lib.cg_tree_upload.argtypes = [vp, C.POINTER(cg_tree_view), C.POINTER(u32)]
+    lib.cg_tree_build.argtypes = [vp, vp, u32, vp]
+    lib.cg_tree_info.argtypes = [vp, u32, vp, vp, vp]
+    lib.cg_tree_export.argtypes = [vp, u32, vp, vp, vp, vp, vp, vp, vp]
     lib.cg_tree_free.argtypes = [vp, u32]
     lib.cg_relative_matrix.argtypes = [vp, vp, vp]
     lib.cg_collide.argtypes = [vp, vp, u32, u32, C.POINTER(cg_stats)]
@@ -282,6 +311,45 @@ class Context:
         tid = C.c_uint32()
         self._check(self.lib.cg_tree_upload(self.h, C.byref(v), C.byref(tid)), "cg_tree_upload")
         return tid.value
+
+    def build_trees(self, meshes) -> np.ndarray:
+        """cg_tree_build: one tree per mesh (objects with points (V, 3),
+        indices (T, 3) and normals (V, 3) or None); their ids."""
+        keep, views = [], (cg_mesh_view * max(len(meshes), 1))()
+        for k, m in enumerate(meshes):
+            pts = np.ascontiguousarray(m.points, np.float32).reshape(-1, 3)
+            idx = np.ascontiguousarray(m.indices, np.uint32).reshape(-1, 3)
+            nrm = None if getattr(m, "normals", None) is None else np.ascontiguousarray(m.normals, np.float32)
+            keep += [pts, idx, nrm]
+            views[k].positions = pts.ctypes.data if pts.size else None
+            views[k].normals = None if nrm is None else nrm.ctypes.data
+            views[k].indices = idx.ctypes.data if idx.size else None
+            views[k].n_vertices = len(pts)
+            views[k].n_triangles = len(idx)
+        ids = np.zeros(max(len(meshes), 1), np.uint32)
+        self._check(self.lib.cg_tree_build(self.h, views, len(meshes), ids.ctypes.data), "cg_tree_build")
+        return ids[:len(meshes)]
+
+    def tree_info(self, tid: int) -> tuple[int, int, bool]:
+        n, t, h = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._check(self.lib.cg_tree_info(self.h, tid, C.byref(n), C.byref(t), C.byref(h)), "cg_tree_info")
+        return n.value, t.value, bool(h.value)
+
+    def export_tree(self, tid: int) -> TreeArrays:
+        """cg_tree_export: the tree's whole flat layout."""
+        n, t, has_nrm = self.tree_info(tid)
+        root = np.zeros(12, np.float32)
+        obbs = np.zeros((max(n, 1), 2, 12), np.float32)
+        ref = np.zeros((max(n, 1), 2), np.uint32)
+        cnt = np.zeros((max(n, 1), 2), np.uint32)
+        pos = np.zeros((max(t, 1), 9), np.float32)
+        nrm = np.zeros((max(t, 1), 9), np.float32) if has_nrm else None
+        idx = np.zeros((max(t, 1), 3), np.uint32)
+        self._check(self.lib.cg_tree_export(self.h, tid, root.ctypes.data, obbs.ctypes.data, ref.ctypes.data,
+                                            cnt.ctypes.data, pos.ctypes.data,
+                                            None if nrm is None else nrm.ctypes.data, idx.ctypes.data),
+                    "cg_tree_export")
+        return TreeArrays(root, obbs[:n], ref[:n], cnt[:n], pos[:t], None if nrm is None else nrm[:t], idx[:t])
 
     def upload_flat(self, ft) -> int:
         """Uploads an oracle-style flat tree (attributes root, node_obbs, ...)."""

@@ -1,0 +1,656 @@
+// OBB-tree construction: OBBtree::OBBtree(vector<Triangle>&&)
+// (src/Geometry/OBBtree.cpp:321-358) for a batch of meshes on the device, one
+// tree level per round of launches, every node of every tree of the level at
+// once.
+//
+// A node is a range of a triangle permutation; a split partitions its range
+// in place (stably, as the reference's push_backs keep order), so every node's
+// triangles stay in the reference's order. The box of a node is
+// OBB::CreateOBBfromTriangles / CreateOBBfromPoints / CreateAABBfromPoints
+// (src/Geometry/OBB.cpp:33-166). Its FP64 sums are sequential in the
+// reference (std::accumulate, std::inner_product), so each is one thread's
+// chain here; the FP64 pipe of this part is narrow, so everything around the
+// chains runs a thread per corner on every SM:
+//   build_points  a thread per triangle position: its corners as doubles
+//   build_sums    a thread per node and coordinate: the sum in corner order,
+//                 the mean
+//   build_terms   a thread per triangle position: the six centred products
+//                 of its corners
+//   build_cov     a thread per node and product: the covariance sum in
+//                 corner order
+//   build_fit     a warp per node: fewer than two distinct corners give the
+//                 empty or point box; else eig3 in FP64 (lane 0), the FP64
+//                 min/max projections on the axes over the lanes (equal
+//                 values: the later corner, as the sequential std::min /
+//                 std::max keep) and the box; then, for a node of more than 4
+//                 triangles, OBBtreeSplitBuildNode::SplitOBBandCreateChildren
+//                 (OBBtree.cpp:43-108): axes by half-length, longest first
+//                 (equal lengths keep u, v, w order); left when the mean of a
+//                 triangle's projection interval is <= the centre's
+//                 projection; the first axis leaving both sides non-empty,
+//                 else halves by position; the two children appended to the
+//                 node table for the next level
+// Built with no contraction, IEEE division and square root, the boxes are the
+// reference builder's bits. Then the trees' pre-order layout
+// (OBBtree.cpp:179-233, 385-394), the larger-surface child first
+// (OBBtree.cpp:100-106), goes straight into the context's arenas:
+//   build_inner   bottom-up by level: the inner nodes of each subtree
+//   build_order   top-down by level: each node's pre-order index, first
+//                 triangle, leaf ordinal and record
+//   build_emit    a thread per node: its record (box, links), subtree range,
+//                 parent and leaf-list entry; a thread per triangle: the
+//                 triangle (and its corner normals) at its leaf's place
+// The meshes' triangles are gathered from their vertex and index buffers on
+// the device (build_gather) before the first level.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <vector>
+
+#include "cg_device.cuh"
+#include "cg_eig.cuh"
+#include "cg_internal.h"
+
+namespace cg {
+
+namespace {
+
+constexpr unsigned kAll = 0xffffffffu;
+constexpr uint32_t kLeafMax = 4;  // OBBtree.h:49 maxNumberOfTriangles
+
+__device__ __forceinline__ float3 corner(const float* P, uint32_t t, uint32_t k) {
+    const float* q = P + 9ull * t + 3u * k;
+    return make_float3(q[0], q[1], q[2]);
+}
+
+// An order-preserving integer key of a double for min/max on the integer
+// pipe (this part's FP64 pipe is narrow); both zeros key 0, as they compare
+// equal.
+__device__ __forceinline__ long long dkey(double x) {
+    const long long b = __double_as_longlong(x);
+    return (b & 0x7fffffffffffffffll) == 0 ? 0ll : (b >= 0 ? b : b ^ 0x7fffffffffffffffll);
+}
+
+// One projection extreme: its key, value and corner position.
+struct Ext {
+    long long k;
+    double v;
+    uint32_t j;
+};
+
+// std::min(pr, lo) / std::max(pr, hi) as the sequential scan applies them:
+// an equal value replaces (the later corner is kept).
+__device__ __forceinline__ void take_lo(Ext& e, long long k, double v, uint32_t j) {
+    if (k <= e.k) e = Ext{k, v, j};
+}
+__device__ __forceinline__ void take_hi(Ext& e, long long k, double v, uint32_t j) {
+    if (k >= e.k) e = Ext{k, v, j};
+}
+
+// The warp's extreme: the smaller key (lo) or the larger (hi); of equal keys
+// the later corner.
+__device__ __forceinline__ void warp_extreme(Ext& e, bool lo) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const long long ok = __shfl_xor_sync(kAll, e.k, o);
+        const double ov = __shfl_xor_sync(kAll, e.v, o);
+        const uint32_t oj = __shfl_xor_sync(kAll, e.j, o);
+        if ((lo ? ok < e.k : ok > e.k) || (ok == e.k && oj > e.j)) e = Ext{ok, ov, oj};
+    }
+}
+
+// The corners of the level's triangles as doubles, by coordinate, at their
+// triangle's position: a thread per position (positions of earlier levels'
+// leaves are skipped).
+__global__ void build_points_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < B.T; t += gridDim.x * blockDim.x) {
+        const uint32_t o = B.own[t];
+        if (o < B.lo || o >= B.hi) continue;
+        const float* q = B.P + 9ull * B.perm[t];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) B.D[c * n3 + 3ull * t + k] = double(q[3 * k + c]);
+    }
+}
+
+// A thread per node and coordinate: the coordinate's sum over the node's
+// corners in order (std::accumulate, OBB.cpp:53-55), then the mean.
+__global__ void build_sums_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    const uint32_t total = 3u * (B.hi - B.lo);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t node = B.lo + g / 3u, c = g % 3u;
+        const BuildNode& N = B.nodes[node];
+        const double* d = B.D + c * n3 + 3ull * N.begin;
+        const uint32_t np = 3u * N.count;
+        double s = 0.0;
+        for (uint32_t j = 0; j < np; ++j) s = s + d[j];
+        B.mom[9ull * (node - B.lo) + c] = np ? s / double(np) : 0.0;
+    }
+}
+
+// The centred products of every corner of the level, a thread per position:
+// xx, yy, zz, xy, xz, yz (OBB.cpp:57-74).
+__global__ void build_terms_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < B.T; t += gridDim.x * blockDim.x) {
+        const uint32_t o = B.own[t];
+        if (o < B.lo || o >= B.hi) continue;
+        const double* m = B.mom + 9ull * (o - B.lo);
+        const double mx = m[0], my = m[1], mz = m[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint64_t j = 3ull * t + k;
+            const double dx = B.D[j] - mx, dy = B.D[n3 + j] - my, dz = B.D[2 * n3 + j] - mz;
+            B.Tm[j] = dx * dx;
+            B.Tm[n3 + j] = dy * dy;
+            B.Tm[2 * n3 + j] = dz * dz;
+            B.Tm[3 * n3 + j] = dx * dy;
+            B.Tm[4 * n3 + j] = dx * dz;
+            B.Tm[5 * n3 + j] = dy * dz;
+        }
+    }
+}
+
+// A thread per node and product: the covariance sum over the node's corners
+// in order (std::inner_product, OBB.cpp:57-74).
+__global__ void build_cov_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    const uint32_t total = 6u * (B.hi - B.lo);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t node = B.lo + g / 6u, q = g % 6u;
+        const BuildNode& N = B.nodes[node];
+        const double* d = B.Tm + q * n3 + 3ull * N.begin;
+        const uint32_t np = 3u * N.count;
+        double s = 0.0;
+        for (uint32_t j = 0; j < np; ++j) s = s + d[j];
+        B.mom[9ull * (node - B.lo) + 3u + q] = s;
+    }
+}
+
+// A thread per node of the level: eig3 of its covariance (OBB.cpp:76-86) in
+// FP64; the box axes (the rows of the eigenvector matrix) replace the node's
+// moments.
+__global__ void build_eig_kernel(const BuildParams B) {
+    for (uint32_t node = B.lo + blockIdx.x * blockDim.x + threadIdx.x; node < B.hi; node += gridDim.x * blockDim.x) {
+        double* m = B.mom + 9ull * (node - B.lo);
+        if (B.nodes[node].count == 0u) continue;  // an empty mesh: the empty box, no axes
+        const double dn = double(3u * B.nodes[node].count);
+        const double cxx = m[3], cyy = m[4], czz = m[5], cxy = m[6], cxz = m[7], cyz = m[8];
+        double v[3][3] = {{cxx / dn, cxy / dn, cxz / dn}, {cxy / dn, cyy / dn, cyz / dn}, {cxz / dn, cyz / dn, czz / dn}};
+        double d[3], off[3];
+        tridiagonalize(v, d, off);
+        ql_sort(v, d, off, 2.220446049250313e-16);  // 2^-52
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) m[3 * r + c] = v[r][c];
+    }
+}
+
+__device__ __forceinline__ Box empty_box() {  // OBB::EmptyOBB (OBB.cpp:168-178)
+    const float e = FLT_EPSILON;
+    return Box{make_float3(0.f, 0.f, 0.f), make_float3(e, 0.f, 0.f), make_float3(0.f, e, 0.f),
+               make_float3(0.f, 0.f, e)};
+}
+
+// The projections of corner j (coordinates px, py, pz) on the three axes.
+__device__ __forceinline__ void project3(const double* ax, double px, double py, double pz, uint32_t j, Ext* lo,
+                                         Ext* hi) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double pr = ax[3 * a] * px;
+        pr = pr + ax[3 * a + 1] * py;
+        pr = pr + ax[3 * a + 2] * pz;
+        const long long k = dkey(pr);
+        take_lo(lo[a], k, pr, j);
+        take_hi(hi[a], k, pr, j);
+    }
+}
+
+__device__ __forceinline__ void init_ext(Ext* lo, Ext* hi) {
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = Ext{dkey(inf), inf, 0u};
+        hi[a] = Ext{dkey(-inf), -inf, 0u};
+    }
+}
+
+// OBB::CreateAABBfromPoints (OBB.cpp:105-166) from the extremes.
+__device__ Box box_from(const double* ax, const Ext* lo, const Ext* hi) {
+    const double pad = 2.0 * double(FLT_EPSILON);
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    float3 half[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double delta = (hi[a].v - lo[a].v) + pad;
+        const double mid = (hi[a].v + lo[a].v) / 2.0;
+        cx = cx + mid * ax[3 * a];
+        cy = cy + mid * ax[3 * a + 1];
+        cz = cz + mid * ax[3 * a + 2];
+        const double h = delta / 2.0;
+        half[a] = make_float3(float(h * ax[3 * a]), float(h * ax[3 * a + 1]), float(h * ax[3 * a + 2]));
+    }
+    return Box{make_float3(float(cx), float(cy), float(cz)), half[0], half[1], half[2]};
+}
+
+__device__ __forceinline__ bool same_point(float3 p, float3 q) { return p.x == q.x && p.y == q.y && p.z == q.z; }
+
+// The node's box (OBB::CreateOBBfromPoints, OBB.cpp:33-89) by a warp.
+__device__ Box fit_warp(const BuildParams& B, uint32_t begin, uint32_t n, const double* ax, uint32_t lane) {
+    if (n == 0u) return empty_box();
+    const uint32_t* perm = B.perm + begin;
+    const uint32_t np = 3u * n;
+    const float3 p0 = corner(B.P, perm[0], 0);
+    bool differ = false;
+    for (uint32_t j = lane; j < np; j += 32u) differ |= !same_point(corner(B.P, perm[j / 3u], j % 3u), p0);
+    if (!__any_sync(kAll, differ)) {  // one distinct point
+        Box b = empty_box();
+        b.c = p0;
+        return b;
+    }
+    double a[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = ax[k];
+    Ext lo[3], hi[3];
+    init_ext(lo, hi);
+    const uint64_t n3 = 3ull * B.T;
+    const double* d = B.D + 3ull * begin;
+    for (uint32_t j = lane; j < np; j += 32u) project3(a, d[j], d[n3 + j], d[2 * n3 + j], j, lo, hi);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        warp_extreme(lo[k], true);
+        warp_extreme(hi[k], false);
+    }
+    return box_from(a, lo, hi);
+}
+
+// The same by one thread (a small node).
+__device__ Box fit_thread(const BuildParams& B, uint32_t begin, uint32_t n, const double* ax) {
+    if (n == 0u) return empty_box();
+    const uint32_t* perm = B.perm + begin;
+    const uint32_t np = 3u * n;
+    const float3 p0 = corner(B.P, perm[0], 0);
+    bool differ = false;
+    for (uint32_t j = 1; j < np && !differ; ++j) differ = !same_point(corner(B.P, perm[j / 3u], j % 3u), p0);
+    if (!differ) {
+        Box b = empty_box();
+        b.c = p0;
+        return b;
+    }
+    double a[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = ax[k];
+    Ext lo[3], hi[3];
+    init_ext(lo, hi);
+    const uint64_t n3 = 3ull * B.T;
+    const double* d = B.D + 3ull * begin;
+    for (uint32_t j = 0; j < np; ++j) project3(a, d[j], d[n3 + j], d[2 * n3 + j], j, lo, hi);
+    return box_from(a, lo, hi);
+}
+
+// TrianglePosition::GetMinMaxProjectionToAxis (Triangle.cpp:113-138), then the
+// split test of OBBtree.cpp:70-74.
+__device__ __forceinline__ bool goes_left(const float* P, uint32_t t, float3 axis, float cp) {
+    float lo = __int_as_float(0x7f800000), hi = -lo;
+#pragma unroll
+    for (uint32_t k = 0; k < 3u; ++k) {
+        const float pr = dot3(axis, corner(P, t, k));
+        if (pr < lo) lo = pr;
+        if (pr > hi) hi = pr;
+    }
+    const float mid = (lo + hi) / 2.0f;
+    return mid <= cp;
+}
+
+__device__ __forceinline__ void split_axes(const Box& b, float3* dir, int* ord);
+
+// Splits the node's range (perm, n > kLeafMax) in place and returns the
+// left child's size.
+__device__ uint32_t split_node(const float* P, uint32_t* perm, uint32_t* scratch, uint32_t n, const Box& b,
+                               uint32_t lane) {
+    float3 dir[3];
+    int ord[3];
+    split_axes(b, dir, ord);
+    bool chosen = false;
+    uint32_t nl = n / 2u;
+    float3 axis = dir[ord[0]];
+    float cp = 0.f;
+    for (int k = 0; k < 3 && !chosen; ++k) {
+        const float3 a = dir[ord[k]];
+        const float c = dot3(b.c, a);
+        uint32_t cnt = 0;
+        for (uint32_t base = 0; base < n; base += 32u) {
+            const uint32_t t = base + lane;
+            const bool left = t < n && goes_left(P, perm[t], a, c);
+            cnt += __popc(__ballot_sync(kAll, left));
+        }
+        if (cnt > 0u && cnt < n) {
+            chosen = true;
+            nl = cnt;
+            axis = a;
+            cp = c;
+        }
+    }
+    uint32_t lb = 0, rb = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t base = 0; base < n; base += 32u) {
+        const uint32_t t = base + lane;
+        const bool valid = t < n;
+        uint32_t id = 0;
+        bool left = false;
+        if (valid) {
+            id = perm[t];
+            left = chosen ? goes_left(P, id, axis, cp) : (t < nl);
+        }
+        const unsigned ml = __ballot_sync(kAll, left), mv = __ballot_sync(kAll, valid);
+        if (valid) scratch[left ? lb + __popc(ml & lt) : nl + rb + __popc(mv & ~ml & lt)] = id;
+        lb += __popc(ml);
+        rb += __popc(mv & ~ml);
+    }
+    __syncwarp();
+    for (uint32_t t = lane; t < n; t += 32u) perm[t] = scratch[t];
+    __syncwarp();
+    return nl;
+}
+
+// The split's axes in order (OBBtree.cpp:45-53): by half-length, longest
+// first; equal lengths keep u, v, w order (std::sort of three is an
+// insertion sort).
+__device__ __forceinline__ void split_axes(const Box& b, float3* dir, int* ord) {
+    const float len[3] = {length3(b.u), length3(b.v), length3(b.w)};
+    dir[0] = normalize3(b.u);
+    dir[1] = normalize3(b.v);
+    dir[2] = normalize3(b.w);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int r = 0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            r += (len[j] > len[k]) || (j < k && !(len[j] > len[k]) && !(len[k] > len[j]));
+        ord[r] = k;
+    }
+}
+
+// The same split by one thread (a small node).
+__device__ uint32_t split_thread(const float* P, uint32_t* perm, uint32_t* scratch, uint32_t n, const Box& b) {
+    float3 dir[3];
+    int ord[3];
+    split_axes(b, dir, ord);
+    bool chosen = false;
+    uint32_t nl = n / 2u;
+    float3 axis = dir[ord[0]];
+    float cp = 0.f;
+    for (int k = 0; k < 3 && !chosen; ++k) {
+        const float3 a = dir[ord[k]];
+        const float c = dot3(b.c, a);
+        uint32_t cnt = 0;
+        for (uint32_t t = 0; t < n; ++t) cnt += goes_left(P, perm[t], a, c) ? 1u : 0u;
+        if (cnt > 0u && cnt < n) {
+            chosen = true;
+            nl = cnt;
+            axis = a;
+            cp = c;
+        }
+    }
+    uint32_t lb = 0, rb = nl;
+    for (uint32_t t = 0; t < n; ++t) {
+        const uint32_t id = perm[t];
+        const bool left = chosen ? goes_left(P, id, axis, cp) : (t < nl);
+        scratch[left ? lb++ : rb++] = id;
+    }
+    for (uint32_t t = 0; t < n; ++t) perm[t] = scratch[t];
+    return nl;
+}
+
+__device__ __forceinline__ void store_box(BuildNode& N, const Box& box) {
+    float* o = N.box;
+    o[0] = box.c.x, o[1] = box.c.y, o[2] = box.c.z;
+    o[3] = box.u.x, o[4] = box.u.y, o[5] = box.u.z;
+    o[6] = box.v.x, o[7] = box.v.y, o[8] = box.v.z;
+    o[9] = box.w.x, o[10] = box.w.y, o[11] = box.w.z;
+}
+
+// Appends the two children of a split node (its first nl triangles, the
+// rest) and returns the first's id, or kNoKid when the table is full.
+__device__ __forceinline__ uint32_t add_children(const BuildParams& B, BuildNode& N, uint32_t nl) {
+    const uint32_t k = atomicAdd(B.node_ctr, 2u);
+    if (k + 2u > B.node_cap) {
+        atomicOr(B.error, 1u);
+        return kNoKid;
+    }
+    BuildNode& L = B.nodes[k];
+    BuildNode& R = B.nodes[k + 1u];
+    L.begin = N.begin, L.count = nl, L.kid = kNoKid, L.tree = N.tree;
+    R.begin = N.begin + nl, R.count = N.count - nl, R.kid = kNoKid, R.tree = N.tree;
+    N.kid = k;
+    return k;
+}
+
+constexpr uint32_t kSmall = 16;  // nodes of at most this many triangles: a thread each
+
+// A warp per node of the level with more than kSmall triangles: the box, the
+// split, the children's positions.
+__global__ void __launch_bounds__(128) build_fit_kernel(const BuildParams B) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t id = B.lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); id < B.hi; id += warps) {
+        BuildNode& N = B.nodes[id];
+        const uint32_t begin = N.begin, n = N.count;
+        if (n <= kSmall) continue;
+        const Box box = fit_warp(B, begin, n, B.mom + 9ull * (id - B.lo), lane);
+        const uint32_t nl = split_node(B.P, B.perm + begin, B.scratch + begin, n, box, lane);
+        uint32_t k = 0;
+        if (lane == 0u) {
+            store_box(N, box);
+            N.kid = kNoKid;
+            k = add_children(B, N, nl);
+        }
+        k = __shfl_sync(kAll, k, 0);
+        if (k == kNoKid) continue;
+        for (uint32_t t = lane; t < n; t += 32u) B.own[begin + t] = t < nl ? k : k + 1u;
+    }
+}
+
+// A thread per node of the level with at most kSmall triangles.
+__global__ void __launch_bounds__(128) build_fit_small_kernel(const BuildParams B) {
+    for (uint32_t id = B.lo + blockIdx.x * blockDim.x + threadIdx.x; id < B.hi; id += gridDim.x * blockDim.x) {
+        BuildNode& N = B.nodes[id];
+        const uint32_t begin = N.begin, n = N.count;
+        if (n > kSmall) continue;
+        const Box box = fit_thread(B, begin, n, B.mom + 9ull * (id - B.lo));
+        store_box(N, box);
+        N.kid = kNoKid;
+        if (n <= kLeafMax) continue;
+        const uint32_t nl = split_thread(B.P, B.perm + begin, B.scratch + begin, n, box);
+        const uint32_t k = add_children(B, N, nl);
+        if (k == kNoKid) continue;
+        for (uint32_t t = 0; t < n; ++t) B.own[begin + t] = t < nl ? k : k + 1u;
+    }
+}
+
+// The meshes' triangles from their vertex and index buffers: a thread per
+// triangle (its mesh is its root node, the owner of every position before
+// the first split).
+__global__ void build_gather_kernel(const BuildParams B, const BuildInput I) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < B.T; g += gridDim.x * blockDim.x) {
+        const uint32_t m = B.own[g];
+        const BuildMesh M = I.meshes[m];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t vi = I.indices[3ull * g + k];
+            const float* v = I.vertices + 3ull * (M.vbase + vi);
+            float* o = I.P + 9ull * g + 3 * k;
+            o[0] = v[0], o[1] = v[1], o[2] = v[2];
+            if (M.has_normals) {
+                const float* nv = I.normals + 3ull * (M.vbase + vi);
+                float* on = I.corner_normals + 9ull * g + 3 * k;
+                on[0] = nv[0], on[1] = nv[1], on[2] = nv[2];
+            }
+        }
+        B.perm[g] = g;
+    }
+}
+
+// Bottom-up, a level at a time from the deepest: the inner nodes of each
+// node's subtree.
+__global__ void build_inner_kernel(const BuildParams B, BuildFlat* flat) {
+    for (uint32_t id = B.lo + blockIdx.x * blockDim.x + threadIdx.x; id < B.hi; id += gridDim.x * blockDim.x) {
+        const uint32_t k = B.nodes[id].kid;
+        flat[id].inner = k == kNoKid ? 0u : 1u + flat[k].inner + flat[k + 1u].inner;
+    }
+}
+
+__device__ __forceinline__ float node_surface(const BuildNode& N) {  // Paralgram::GetSurface (Paralgram.cpp:203-210)
+    const float* b = N.box;
+    const float3 u = make_float3(b[3], b[4], b[5]), v = make_float3(b[6], b[7], b[8]), w = make_float3(b[9], b[10], b[11]);
+    const float uv = length3(cross3(u, v)), uw = length3(cross3(u, w)), vw = length3(cross3(v, w));
+    return 2.0f * (uv + uw + vw);
+}
+
+// Top-down, a level at a time from the roots: each node's place in its tree's
+// pre-order layout (OBBtree.cpp:179-233, 385-394): the larger-surface child
+// first (OBBtree.cpp:100-106), inner nodes numbered in pre-order, leaves'
+// triangles appended in pre-order; the children's records follow their
+// parent's index (records 2k + 2 and 2k + 3 of inner node k, the root's 1).
+__global__ void build_order_kernel(const BuildParams B, BuildFlat* flat, uint32_t n_roots) {
+    for (uint32_t id = B.lo + blockIdx.x * blockDim.x + threadIdx.x; id < B.hi; id += gridDim.x * blockDim.x) {
+        BuildFlat X = flat[id];
+        if (id < n_roots) {
+            X.index = 0u, X.tri_off = 0u, X.leaf_off = 0u, X.rec = 1u, X.prec = kNoKid;
+            flat[id] = X;
+        }
+        const BuildNode& N = B.nodes[id];
+        if (N.kid == kNoKid) continue;
+        uint32_t f = N.kid, s = N.kid + 1u;
+        if (node_surface(B.nodes[s]) > node_surface(B.nodes[f])) {
+            const uint32_t t = f;
+            f = s;
+            s = t;
+        }
+        BuildFlat& F = flat[f];
+        BuildFlat& S = flat[s];
+        F.index = X.index + 1u;
+        S.index = X.index + 1u + F.inner;
+        F.tri_off = X.tri_off;
+        S.tri_off = X.tri_off + B.nodes[f].count;
+        F.leaf_off = X.leaf_off;
+        S.leaf_off = X.leaf_off + F.inner + 1u;
+        F.rec = 2u * X.index + 2u;
+        S.rec = 2u * X.index + 3u;
+        F.prec = S.prec = X.rec;
+    }
+}
+
+// A thread per node of the batch: its record in its tree's arena range (box,
+// link word: first child record or first triangle, leaf word), its subtree's
+// triangle range, its parent record and, for a leaf, its place in the leaf
+// list; a root also writes its tree's unused record 0.
+__global__ void build_emit_nodes_kernel(const BuildParams B, const BuildFlat* flat, const BuildEmit* emit,
+                                        float4* recs, uint32_t n_nodes, uint32_t n_roots) {
+    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_nodes; id += gridDim.x * blockDim.x) {
+        const BuildNode& N = B.nodes[id];
+        const BuildFlat& X = flat[id];
+        const BuildEmit& E = emit[N.tree];
+        const bool leaf = N.kid == kNoKid;
+        const uint32_t ref = leaf ? E.tri_base + X.tri_off : E.rec_base + 2u * X.index + 2u;
+        const uint32_t meta = leaf ? (kLeafFlag | (N.count & 0xffffu)) : 0u;
+        const float* b = N.box;
+        float4* r = recs + 4ull * (E.rec_base + X.rec);
+        r[0] = make_float4(b[0], b[1], b[2], b[3]);
+        r[1] = make_float4(b[4], b[5], b[6], b[7]);
+        r[2] = make_float4(b[8], b[9], b[10], b[11]);
+        r[3] = make_float4(__uint_as_float(ref), __uint_as_float(meta), 0.f, 0.f);
+        E.ranges[X.rec] = make_uint2(X.tri_off, N.count);
+        E.topo[X.rec] = X.prec;
+        if (leaf) E.topo[E.n_recs + X.leaf_off] = X.rec;
+        if (id < n_roots) {
+            float4* z = recs + 4ull * E.rec_base;
+            z[0] = z[1] = z[2] = z[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+            E.ranges[0] = make_uint2(0u, ~0u);
+            E.topo[0] = kNoKid;
+        }
+    }
+}
+
+// A thread per triangle position: the triangle into its tree's arena range at
+// its leaf's place (corners, vertex indices in the w words), with its corner
+// normals when the mesh has them.
+__global__ void build_emit_tris_kernel(const BuildParams B, const BuildInput I, const BuildFlat* flat,
+                                       const BuildEmit* emit, float4* tris) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < B.T; p += gridDim.x * blockDim.x) {
+        const uint32_t leaf = B.own[p];
+        const BuildNode& N = B.nodes[leaf];
+        const BuildEmit& E = emit[N.tree];
+        const uint32_t local = flat[leaf].tri_off + (p - N.begin);
+        const uint32_t g = B.perm[p];
+        const float* c = I.P + 9ull * g;
+        float4* o = tris + 3ull * (E.tri_base + local);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) o[k] = make_float4(c[3 * k], c[3 * k + 1], c[3 * k + 2], __uint_as_float(I.indices[3ull * g + k]));
+        if (E.nrm) {
+            const float* n = I.corner_normals + 9ull * g;
+            float* on = E.nrm + 9ull * local;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) on[k] = n[k];
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStream_t s) {
+    if (p.hi <= p.lo) return cudaSuccess;
+    const uint32_t width = p.hi - p.lo;
+    const uint32_t wide = sm_count * 8u;  // blocks of the per-position kernels
+    auto grid = [&](uint64_t threads) {
+        const uint64_t b = (threads + 127u) / 128u;
+        return uint32_t(b < wide ? (b ? b : 1u) : wide);
+    };
+    build_points_kernel<<<grid(p.T), 128, 0, s>>>(p);
+    build_sums_kernel<<<grid(3ull * width), 128, 0, s>>>(p);
+    build_terms_kernel<<<grid(p.T), 128, 0, s>>>(p);
+    build_cov_kernel<<<grid(6ull * width), 128, 0, s>>>(p);
+    build_eig_kernel<<<grid(width), 128, 0, s>>>(p);
+    const uint32_t blocks = (width + 3u) / 4u;
+    build_fit_kernel<<<blocks < 65535u ? blocks : 65535u, 128, 0, s>>>(p);
+    build_fit_small_kernel<<<grid(width), 128, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+namespace {
+uint32_t grid_of(uint64_t threads, uint32_t sm_count) {
+    const uint64_t b = (threads + 127u) / 128u, cap = uint64_t(sm_count) * 8u;
+    return uint32_t(b < cap ? (b ? b : 1u) : cap);
+}
+}  // namespace
+
+cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint32_t sm_count, cudaStream_t s) {
+    if (p.T) build_gather_kernel<<<grid_of(p.T, sm_count), 128, 0, s>>>(p, in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_inner(const BuildParams& p, BuildFlat* flat, uint32_t sm_count, cudaStream_t s) {
+    if (p.hi > p.lo) build_inner_kernel<<<grid_of(p.hi - p.lo, sm_count), 128, 0, s>>>(p, flat);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_order(const BuildParams& p, BuildFlat* flat, uint32_t n_roots, uint32_t sm_count,
+                               cudaStream_t s) {
+    if (p.hi > p.lo) build_order_kernel<<<grid_of(p.hi - p.lo, sm_count), 128, 0, s>>>(p, flat, n_roots);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_emit(const BuildParams& p, const BuildInput& in, const BuildFlat* flat,
+                              const BuildEmit* emit, float4* recs, float4* tris, uint32_t n_nodes, uint32_t n_roots,
+                              uint32_t sm_count, cudaStream_t s) {
+    if (n_nodes) build_emit_nodes_kernel<<<grid_of(n_nodes, sm_count), 128, 0, s>>>(p, flat, emit, recs, n_nodes, n_roots);
+    if (p.T) build_emit_tris_kernel<<<grid_of(p.T, sm_count), 128, 0, s>>>(p, in, flat, emit, tris);
+    return cudaGetLastError();
+}
+
+}  // namespace cg

@@ -27,6 +27,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "collide_gpu.h"
 
@@ -363,6 +364,65 @@ struct ShootParams {
     const unsigned* n_rays_dev; // or null: the rays' count in device memory (at most n_rays)
 };
 cudaError_t launch_shoot(const ShootParams& p, cudaStream_t s);
+
+// OBB-tree construction (cg_build.cu).
+constexpr uint32_t kNoKid = 0xffffffffu;
+struct BuildNode {           // 64 bytes
+    uint32_t begin, count;   // the node's triangles: perm[begin, begin + count)
+    uint32_t kid;            // its children at kid, kid + 1 (as split: left, right), or kNoKid
+    uint32_t tree;
+    float box[12];           // centre, u, v, w
+};
+static_assert(sizeof(BuildNode) == 64, "BuildNode layout");
+struct BuildParams {
+    const float* P;          // [triangles][3][3] corners, the meshes one after another
+    uint32_t* perm;          // [triangles] triangle ids, each node's range partitioned in place
+    uint32_t* scratch;       // [triangles]
+    uint32_t* own;           // [triangles] the node that holds each position (its level's or a leaf's)
+    double* D;               // [3][3 triangles] the corners' coordinates at their position, by coordinate
+    double* Tm;              // [6][3 triangles] the corners' centred products
+    double* mom;             // [level width][9] mean, then the six covariance sums
+    BuildNode* nodes;
+    uint32_t T;              // triangles
+    uint32_t lo, hi;         // this level's nodes
+    uint32_t* node_ctr;      // next free node
+    uint32_t node_cap;
+    unsigned* error;
+};
+cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStream_t s);
+struct BuildMesh {
+    uint32_t vbase;          // first vertex in BuildInput::vertices / normals
+    uint32_t has_normals;
+};
+struct BuildInput {
+    const BuildMesh* meshes;
+    const float* vertices;   // [all meshes' vertices][3]
+    const float* normals;    // [all meshes' vertices][3] (rows of meshes without normals unused)
+    const uint32_t* indices; // [triangles][3] mesh-local vertex indices
+    float* P;                // [triangles][3][3] out: corners
+    float* corner_normals;   // [triangles][3][3] out: corner normals
+};
+struct BuildFlat {           // a node's place in its tree's layout
+    uint32_t inner;          // inner nodes of its subtree
+    uint32_t index;          // pre-order index (inner nodes)
+    uint32_t tri_off;        // first triangle of its subtree
+    uint32_t leaf_off;       // leaves before it in pre-order
+    uint32_t rec;            // its record (tree-local)
+    uint32_t prec;           // its parent's record
+};
+struct BuildEmit {           // a built tree's arena places
+    uint32_t rec_base, tri_base, n_recs, pad;
+    float* nrm;              // [triangles][9] or null
+    uint2* ranges;           // [n_recs]
+    uint32_t* topo;          // [n_recs] parents, then the leaf records
+};
+cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint32_t sm_count, cudaStream_t s);
+cudaError_t launch_build_inner(const BuildParams& p, BuildFlat* flat, uint32_t sm_count, cudaStream_t s);
+cudaError_t launch_build_order(const BuildParams& p, BuildFlat* flat, uint32_t n_roots, uint32_t sm_count,
+                               cudaStream_t s);
+cudaError_t launch_build_emit(const BuildParams& p, const BuildInput& in, const BuildFlat* flat,
+                              const BuildEmit* emit, float4* recs, float4* tris, uint32_t n_nodes, uint32_t n_roots,
+                              uint32_t sm_count, cudaStream_t s);
 
 // A collision frame (cg_frame.cu).
 struct FrameParams {
