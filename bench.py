@@ -793,6 +793,19 @@ def run_only(args) -> dict:
     torch.cuda.set_stream(stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     factory = lambda: capi.Context(max_queries=4096, max_tri_pairs=1 << 22)  # noqa: E731
+    if args.only in ("shoot", "frame", "build"):
+        from inmyroom_vulkan_gb300 import scenes
+
+        sc = scenes.scene(seed=1002)
+        ctx = capi.Context(max_queries=max(4096, len(sc.pairs)), max_tri_pairs=1 << 22)
+        ids, line = run_tree_build(ctx, sc, 0.0)
+        if args.only == "build":
+            return line
+        if args.only == "frame":
+            return run_frame(args, ctx, sc, ids, 0.0)
+        qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+        rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
+        return run_shoot(args, ctx, sc, ids, capi.make_queries(ids[qa], ids[qb], rel), 0.0)
     if args.only == "deforming":
         return run_deforming(args, factory, flush, stream, 0.0)
     if args.only == "differentiable":
@@ -812,7 +825,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="time the scene step with the default launch settings")
     ap.add_argument("--skip-shoot", action="store_true", help="leave out the uncollide-ray shooting line")
     ap.add_argument("--skip-frame", action="store_true", help="leave out the collision-frame line")
-    ap.add_argument("--only", choices=["deforming", "differentiable", "sweep"],
+    ap.add_argument("--only", choices=["deforming", "differentiable", "sweep", "shoot", "frame", "build"],
                     help="run one secondary workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -10,11 +10,11 @@
 //                       pair), and when it succeeds the pass of its
 //                       reflection back; each success as (signed force
 //                       response, signed ray response)
-//   shoot_query_kernel  a thread per pair: the force responses summed in the
+//   shoot_query_kernel  a warp per pair: the force responses summed in the
 //                       reference's order (rays from the first entity, each
 //                       followed by its reflection, then those from the
-//                       second), FindResponse over the ray responses, the
-//                       delta in world space
+//                       second), FindResponse's maximum over the ray
+//                       responses (order-free), the delta in world space
 // Every step rounds where the reference rounds (built without contraction,
 // IEEE division and square root), so the deltas are the reference's bits for
 // the same rays in the same order. The ray/triangle test is the one the glm
@@ -419,38 +419,52 @@ __device__ __forceinline__ float smoother_step(float a, float b, float x) {
     return v * v * v * (v * (v * 6.f - 15.f) + 10.f);
 }
 
-__global__ void shoot_query_kernel(const ShootParams P) {
-    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= P.n_queries) return;
-    const ShootQuery& Q = P.q[qi];
-    const uint32_t r0 = Q.ray_first, r1 = Q.ray_first + Q.n_first + Q.n_second;
-    float3 avg = make_float3(0.f, 0.f, 0.f);
-    for (uint32_t i = r0; i < r1; ++i) {
-        const ShootRayOut& o = P.out[i];
-        if (o.ok1) avg = add3s(avg, get3(o.f1));
-        if (o.ok2) avg = add3s(avg, get3(o.f2));
-    }
-    float3 delta = make_float3(0.f, 0.f, 0.f);
-    if (avg.x != 0.f || avg.y != 0.f || avg.z != 0.f) {
-        const float3 nf = normalize3(avg);
-        float max_len = 0.f;
-        auto one = [&](float3 r) {
-            const float3 nr = normalize3(r);
-            const float dt = dot3(nr, nf);
-            const float len = length3(r);
-            const float need = len / dt;
-            const float x = smoother_step(P.cos_finish, P.cos_start, dt) * need;
-            max_len = (max_len < x) ? x : max_len;
-        };
-        for (uint32_t i = r0; i < r1; ++i) {
-            const ShootRayOut& o = P.out[i];
-            if (o.ok1) one(get3(o.r1));
-            if (o.ok2) one(get3(o.r2));
+// A warp per pair: the force responses summed in the reference's order by
+// lane 0 (a float sum is order-dependent), FindResponse's maximum over the
+// ray responses by all lanes (a maximum is not), then the delta.
+__global__ void __launch_bounds__(128) shoot_query_kernel(const ShootParams P) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < P.n_queries; qi += warps) {
+        const ShootQuery& Q = P.q[qi];
+        const uint32_t r0 = Q.ray_first, r1 = Q.ray_first + Q.n_first + Q.n_second;
+        float3 avg = make_float3(0.f, 0.f, 0.f);
+        if (lane == 0u) {
+            for (uint32_t i = r0; i < r1; ++i) {
+                const ShootRayOut& o = P.out[i];
+                if (o.ok1) avg = add3s(avg, get3(o.f1));
+                if (o.ok2) avg = add3s(avg, get3(o.f2));
+            }
         }
-        const float3 local = scale3s(P.bias, scale3s(max_len, nf));
-        delta = xform(mat_of(Q.first_global), local, 0.f);
+        avg = make_float3(__shfl_sync(0xffffffffu, avg.x, 0), __shfl_sync(0xffffffffu, avg.y, 0),
+                          __shfl_sync(0xffffffffu, avg.z, 0));
+        float3 delta = make_float3(0.f, 0.f, 0.f);
+        if (avg.x != 0.f || avg.y != 0.f || avg.z != 0.f) {
+            const float3 nf = normalize3(avg);
+            float max_len = 0.f;
+            auto one = [&](float3 r) {
+                const float3 nr = normalize3(r);
+                const float dt = dot3(nr, nf);
+                const float len = length3(r);
+                const float need = len / dt;
+                const float x = smoother_step(P.cos_finish, P.cos_start, dt) * need;
+                max_len = (max_len < x) ? x : max_len;
+            };
+            for (uint32_t i = r0 + lane; i < r1; i += 32u) {
+                const ShootRayOut& o = P.out[i];
+                if (o.ok1) one(get3(o.r1));
+                if (o.ok2) one(get3(o.r2));
+            }
+#pragma unroll
+            for (int w = 16; w; w >>= 1) {
+                const float x = __shfl_xor_sync(0xffffffffu, max_len, w);
+                max_len = (max_len < x) ? x : max_len;
+            }
+            const float3 local = scale3s(P.bias, scale3s(max_len, nf));
+            delta = xform(mat_of(Q.first_global), local, 0.f);
+        }
+        if (lane == 0u) put3(P.deltas + 3ull * qi, delta);
     }
-    put3(P.deltas + 3ull * qi, delta);
 }
 
 }  // namespace
@@ -460,7 +474,10 @@ cudaError_t launch_shoot(const ShootParams& p, cudaStream_t s) {
         const uint64_t blocks = (4ull * p.n_rays + 127u) / 128u;  // a quad per ray, strided beyond 8192 blocks
         shoot_ray_kernel<<<uint32_t(blocks < 8192u ? blocks : 8192u), 128, 0, s>>>(p);
     }
-    if (p.n_queries) shoot_query_kernel<<<(p.n_queries + 127u) / 128u, 128, 0, s>>>(p);
+    if (p.n_queries) {
+        const uint32_t blocks = (p.n_queries + 3u) / 4u;  // a warp per pair
+        shoot_query_kernel<<<blocks < 65535u ? blocks : 65535u, 128, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
