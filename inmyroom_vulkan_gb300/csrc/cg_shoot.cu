@@ -419,25 +419,39 @@ __device__ __forceinline__ float smoother_step(float a, float b, float x) {
     return v * v * v * (v * (v * 6.f - 15.f) + 10.f);
 }
 
-// A warp per pair: the force responses summed in the reference's order by
-// lane 0 (a float sum is order-dependent), FindResponse's maximum over the
-// ray responses by all lanes (a maximum is not), then the delta.
+// A warp per pair: the force responses summed in the reference's order (a
+// float sum is order-dependent), FindResponse's maximum over the ray
+// responses split over the lanes (a maximum is not), then the delta.
 __global__ void __launch_bounds__(128) shoot_query_kernel(const ShootParams P) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < P.n_queries; qi += warps) {
         const ShootQuery& Q = P.q[qi];
         const uint32_t r0 = Q.ray_first, r1 = Q.ray_first + Q.n_first + Q.n_second;
+        // the lanes load 32 rays' responses at a time; every lane then adds
+        // them in ray order from the shuffles (the same sum on all lanes)
         float3 avg = make_float3(0.f, 0.f, 0.f);
-        if (lane == 0u) {
-            for (uint32_t i = r0; i < r1; ++i) {
+        for (uint32_t base = r0; base < r1; base += 32u) {
+            const uint32_t i = base + lane;
+            uint32_t ok = 0u;
+            float3 f1 = make_float3(0.f, 0.f, 0.f), f2 = f1;
+            if (i < r1) {
                 const ShootRayOut& o = P.out[i];
-                if (o.ok1) avg = add3s(avg, get3(o.f1));
-                if (o.ok2) avg = add3s(avg, get3(o.f2));
+                ok = (o.ok1 ? 1u : 0u) | (o.ok2 ? 2u : 0u);
+                if (ok & 1u) f1 = get3(o.f1);
+                if (ok & 2u) f2 = get3(o.f2);
+            }
+            const uint32_t m = (r1 - base) < 32u ? (r1 - base) : 32u;
+            for (uint32_t j = 0; j < m; ++j) {
+                const uint32_t k = __shfl_sync(0xffffffffu, ok, j);
+                const float3 a = make_float3(__shfl_sync(0xffffffffu, f1.x, j), __shfl_sync(0xffffffffu, f1.y, j),
+                                             __shfl_sync(0xffffffffu, f1.z, j));
+                const float3 b = make_float3(__shfl_sync(0xffffffffu, f2.x, j), __shfl_sync(0xffffffffu, f2.y, j),
+                                             __shfl_sync(0xffffffffu, f2.z, j));
+                if (k & 1u) avg = add3s(avg, a);
+                if (k & 2u) avg = add3s(avg, b);
             }
         }
-        avg = make_float3(__shfl_sync(0xffffffffu, avg.x, 0), __shfl_sync(0xffffffffu, avg.y, 0),
-                          __shfl_sync(0xffffffffu, avg.z, 0));
         float3 delta = make_float3(0.f, 0.f, 0.f);
         if (avg.x != 0.f || avg.y != 0.f || avg.z != 0.f) {
             const float3 nf = normalize3(avg);
