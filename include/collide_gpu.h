@@ -501,6 +501,28 @@ typedef struct cg_frame_result {
 int cg_collision_frame(cg_ctx* ctx, const cg_frame_entity* entities, uint32_t n, const cg_shoot_params* params,
                        cg_frame_result* results, uint64_t cap, uint64_t* n_results);
 
+/* The fan-out of a frame's results to the entities' ancestors
+ * (CollisionDetection.cpp:104-124, host only, no device): result k gives
+ * CollisionCallbackData{first, second, first_delta} to every ancestor of
+ * `first` (the root, entity 0, down to `first` itself,
+ * EntitiesHandler::GetEntityAncestors) that is not the second's ancestor at
+ * the same depth, and {second, first, second_delta} likewise. entity_ids maps
+ * the frame's entity indices to the engine's entities; parent[e] is entity
+ * e's parent (parent of the root unused). The callbacks come grouped by
+ * receiver, each receiver's in result order (the reference's map of vectors,
+ * flattened). CG_ERR_OUTPUT_OVERFLOW with the exact count when cap is short;
+ * CG_ERR_INVALID_ARGUMENT for an id out of range or a parent cycle. */
+typedef struct cg_frame_callback {
+    uint32_t receiver;       /* the entity whose components get the callback */
+    uint32_t family_entity;  /* CollisionCallbackData::familyEntity */
+    uint32_t collide_with;   /* CollisionCallbackData::collideWithEntity */
+    float delta[3];          /* CollisionCallbackData::deltaVector */
+} cg_frame_callback;
+
+int cg_frame_callbacks(const cg_frame_result* results, uint64_t n_results, const uint32_t* entity_ids,
+                       uint32_t n_entities, const uint32_t* parent, uint32_t n_ids, cg_frame_callback* out,
+                       uint64_t cap, uint64_t* n_out);
+
 /* ---- No-allocation collide step (no reference counterpart) ----
  *
  * The collide step of cg_collide_async (same kernels, same colliding pairs)

@@ -34,7 +34,8 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_collide_static", "cg_deform", "cg_deform_batch", "cg_tree_refit", "cg_tree_refit_batch",
            "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
            "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays",
-           "cg_broad_phase", "cg_collision_frame", "cg_tree_build", "cg_tree_info", "cg_tree_export"]
+           "cg_broad_phase", "cg_collision_frame", "cg_tree_build", "cg_tree_info", "cg_tree_export",
+           "cg_frame_callbacks"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -146,7 +147,10 @@ FRAME_ENTITY_DTYPE = np.dtype([("tree", "<u4"), ("should_callback", "<u4"), ("cu
                                ("previous_global", "<f4", (16,))])
 FRAME_RESULT_DTYPE = np.dtype([("first", "<u4"), ("second", "<u4"), ("first_delta", "<f4", (3,)),
                                ("second_delta", "<f4", (3,)), ("query", "<u4"), ("reserved", "<u4")])
+FRAME_CALLBACK_DTYPE = np.dtype([("receiver", "<u4"), ("family_entity", "<u4"), ("collide_with", "<u4"),
+                                 ("delta", "<f4", (3,))])
 assert FRAME_ENTITY_DTYPE.itemsize == 136 and FRAME_RESULT_DTYPE.itemsize == 40
+assert FRAME_CALLBACK_DTYPE.itemsize == 24
 assert QUERY_DTYPE.itemsize == 72 and TRI_PAIR_DTYPE.itemsize == 36 and LEAF_PAIR_DTYPE.itemsize == 16
 assert CONTACT_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32 and RAY_AVERAGE_DTYPE.itemsize == 32
 
@@ -200,6 +204,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_broad_phase.argtypes = [vp, vp, vp, vp, u32, vp, vp, u64, C.POINTER(u64)]
     lib.cg_shoot_params_default.argtypes = [C.POINTER(cg_shoot_params)]
     lib.cg_collision_frame.argtypes = [vp, vp, u32, C.POINTER(cg_shoot_params), vp, u64, C.POINTER(u64)]
+    lib.cg_frame_callbacks.argtypes = [vp, u64, vp, u32, vp, u32, vp, u64, C.POINTER(u64)]
     lib.cg_shoot_params_default.restype = None
     lib.cg_shoot_rays.argtypes = [vp, vp, u32, vp, u64, C.POINTER(cg_shoot_params), vp]
     lib.cg_pose.argtypes = [vp, C.POINTER(cg_skeleton_view), vp, u32, vp, vp]
@@ -226,6 +231,27 @@ def relative_matrix(a16, b16) -> np.ndarray:
     if rc != CG_OK:
         raise CgError(rc, "cg_relative_matrix")
     return out
+
+
+def frame_callbacks(results: np.ndarray, entity_ids, parent) -> np.ndarray:
+    """cg_frame_callbacks (host only): a frame's FRAME_RESULT_DTYPE records
+    fanned out to the entities' ancestors; FRAME_CALLBACK_DTYPE, grouped by
+    receiver."""
+    lib = load_library()
+    res = np.ascontiguousarray(results, FRAME_RESULT_DTYPE)
+    ids = np.ascontiguousarray(entity_ids, np.uint32)
+    par = np.ascontiguousarray(parent, np.uint32)
+    cnt = C.c_uint64()
+    args = (res.ctypes.data if len(res) else None, len(res), ids.ctypes.data if len(ids) else None, len(ids),
+            par.ctypes.data if len(par) else None, len(par))
+    rc = lib.cg_frame_callbacks(*args, None, 0, C.byref(cnt))
+    if rc not in (0, CG_ERR_OUTPUT_OVERFLOW):
+        raise CgError(rc, "cg_frame_callbacks")
+    out = np.zeros(max(cnt.value, 1), FRAME_CALLBACK_DTYPE)
+    rc = lib.cg_frame_callbacks(*args, out.ctypes.data, len(out), C.byref(cnt))
+    if rc != 0:
+        raise CgError(rc, "cg_frame_callbacks")
+    return out[:cnt.value]
 
 
 def make_queries(tree_a, tree_b, relative) -> np.ndarray:

@@ -1997,6 +1997,48 @@ int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, c
     return nres > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
 }
 
+int cg_frame_callbacks(const cg_frame_result* results, uint64_t n_results, const uint32_t* entity_ids,
+                       uint32_t n_entities, const uint32_t* parent, uint32_t n_ids, cg_frame_callback* out,
+                       uint64_t cap, uint64_t* n_out) {
+    if (!n_out || (n_results && (!results || !entity_ids || !parent)) || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
+    *n_out = 0;
+    // EntitiesHandler::GetEntityAncestors (EntitiesHandler.cpp:186-204): the
+    // chain up to the root (entity 0), reversed
+    auto ancestors = [&](uint32_t e, std::vector<uint32_t>& a) {
+        a.clear();
+        for (;;) {
+            if (e >= n_ids || a.size() > n_ids) return false;  // out of range, or a cycle
+            a.push_back(e);
+            if (e == 0) break;
+            e = parent[e];
+        }
+        std::reverse(a.begin(), a.end());
+        return true;
+    };
+    std::vector<cg_frame_callback> cb;
+    std::vector<uint32_t> fa, sa;
+    for (uint64_t k = 0; k < n_results; ++k) {
+        const cg_frame_result& r = results[k];
+        if (r.first >= n_entities || r.second >= n_entities) return CG_ERR_INVALID_ARGUMENT;
+        const uint32_t f = entity_ids[r.first], s = entity_ids[r.second];
+        if (!ancestors(f, fa) || !ancestors(s, sa)) return CG_ERR_INVALID_ARGUMENT;
+        auto emit = [&](const std::vector<uint32_t>& mine, const std::vector<uint32_t>& other, uint32_t fam,
+                        uint32_t with, const float* d) {
+            for (size_t i = 0; i < mine.size(); ++i)
+                if (i >= other.size() || mine[i] != other[i])
+                    cb.push_back(cg_frame_callback{mine[i], fam, with, {d[0], d[1], d[2]}});
+        };
+        emit(fa, sa, f, s, r.first_delta);   // CollisionDetection.cpp:109-116
+        emit(sa, fa, s, f, r.second_delta);  // :118-124
+    }
+    std::stable_sort(cb.begin(), cb.end(),
+                     [](const cg_frame_callback& a, const cg_frame_callback& b) { return a.receiver < b.receiver; });
+    *n_out = cb.size();
+    const uint64_t m = std::min<uint64_t>(cb.size(), cap);
+    if (m) std::memcpy(out, cb.data(), sizeof(cg_frame_callback) * m);
+    return cb.size() > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+}
+
 void cg_shoot_params_default(cg_shoot_params* p) {
     if (!p) return;
     const float deg = 0.01745329251994329576923690768489f;  // glm::radians

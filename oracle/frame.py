@@ -71,3 +71,28 @@ def as_arrays(records):
     d = np.array([np.concatenate([r[2], r[3]]) for r in records], f32)
     o = np.lexsort((p[:, 1], p[:, 0]))
     return p[o], d[o]
+
+
+def ancestors(entity: int, parent) -> list:
+    """EntitiesHandler::GetEntityAncestors (src/ECS/EntitiesHandler.cpp:186-204):
+    the root (entity 0) down to the entity."""
+    out = [entity]
+    while entity != 0:
+        entity = int(parent[entity])
+        out.append(entity)
+    return out[::-1]
+
+
+def fan_out(records, entity_ids, parent) -> dict:
+    """CollisionDetection.cpp:104-124: receiver -> [(family, collide_with,
+    delta)] in record order, for records (first, second, first_delta,
+    second_delta) over frame entity indices."""
+    calls: dict = {}
+    for a, b, d1, d2 in records:
+        fa, fb = int(entity_ids[a]), int(entity_ids[b])
+        A, B = ancestors(fa, parent), ancestors(fb, parent)
+        for mine, other, fam, with_, d in ((A, B, fa, fb, d1), (B, A, fb, fa, d2)):
+            for i, e in enumerate(mine):
+                if i >= len(other) or other[i] != e:
+                    calls.setdefault(e, []).append((fam, with_, tuple(np.asarray(d, f32).tolist())))
+    return calls
