@@ -142,6 +142,15 @@ int cg_tree_export(cg_ctx* ctx, uint32_t tree_id, cg_obb* root, cg_obb* node_obb
                    uint32_t* node_tri_count, float* triangles_position, float* triangles_normal,
                    uint32_t* triangles_indices);
 
+/* The tree cache: a tree's flat layout in a file, loaded again without a
+ * build. Little-endian: "CGTREE01", uint32 node_count, triangle_count, flags
+ * (1: normals), then the root box, node_obbs, node_ref, node_tri_count,
+ * triangles_position, triangles_normal (if flagged), triangles_indices, and a
+ * 64-bit FNV-1a of everything before it. cg_tree_load checks the sizes and
+ * the checksum (CG_ERR_BAD_TREE) and uploads as cg_tree_upload. */
+int cg_tree_save(cg_ctx* ctx, uint32_t tree_id, const char* path);
+int cg_tree_load(cg_ctx* ctx, const char* path, uint32_t* tree_id);
+
 /* ---- queries ---------------------------------------------------------- */
 
 /* One entity pair, the unit of OBBtreesCollision::ExecuteOBBtreesCollision.

@@ -35,7 +35,7 @@ EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg
            "cg_tree_download", "cg_pose", "cg_pose_backward", "cg_energy", "cg_energy_backward",
            "cg_set_host_outputs", "cg_shoot_params_default", "cg_shoot_rays",
            "cg_broad_phase", "cg_collision_frame", "cg_tree_build", "cg_tree_info", "cg_tree_export",
-           "cg_frame_callbacks"]
+           "cg_frame_callbacks", "cg_tree_save", "cg_tree_load"]
 CG_STATIC_MAX_QUERIES = 1024
 CG_STATIC_MAX_LEAF_PAIRS = 131072
 
@@ -178,6 +178,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.cg_tree_build.argtypes = [vp, vp, u32, vp]
     lib.cg_tree_info.argtypes = [vp, u32, vp, vp, vp]
     lib.cg_tree_export.argtypes = [vp, u32, vp, vp, vp, vp, vp, vp, vp]
+    lib.cg_tree_save.argtypes = [vp, u32, C.c_char_p]
+    lib.cg_tree_load.argtypes = [vp, C.c_char_p, C.POINTER(u32)]
     lib.cg_tree_free.argtypes = [vp, u32]
     lib.cg_relative_matrix.argtypes = [vp, vp, vp]
     lib.cg_collide.argtypes = [vp, vp, u32, u32, C.POINTER(cg_stats)]
@@ -376,6 +378,16 @@ class Context:
                                             None if nrm is None else nrm.ctypes.data, idx.ctypes.data),
                     "cg_tree_export")
         return TreeArrays(root, obbs[:n], ref[:n], cnt[:n], pos[:t], None if nrm is None else nrm[:t], idx[:t])
+
+    def save_tree(self, tid: int, path: str):
+        """cg_tree_save: the tree cache file."""
+        self._check(self.lib.cg_tree_save(self.h, tid, os.fsencode(path)), "cg_tree_save")
+
+    def load_tree(self, path: str) -> int:
+        """cg_tree_load: a tree from its cache file; its id."""
+        tid = C.c_uint32()
+        self._check(self.lib.cg_tree_load(self.h, os.fsencode(path), C.byref(tid)), "cg_tree_load")
+        return tid.value
 
     def upload_flat(self, ft) -> int:
         """Uploads an oracle-style flat tree (attributes root, node_obbs, ...)."""

@@ -1582,6 +1582,107 @@ int cg_tree_download(cg_ctx* c, uint32_t id, cg_obb* root, cg_obb* node_obbs, ui
     return CG_OK;
 }
 
+namespace {
+constexpr char kCacheMagic[8] = {'C', 'G', 'T', 'R', 'E', 'E', '0', '1'};
+
+uint64_t fnv1a(const unsigned char* p, size_t n, uint64_t h = 1469598103934665603ull) {
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+}  // namespace
+
+int cg_tree_save(cg_ctx* c, uint32_t id, const char* path) {
+    if (!c || !path) return CG_ERR_INVALID_ARGUMENT;
+    uint32_t N = 0, T = 0, has_nrm = 0;
+    int rc = cg_tree_info(c, id, &N, &T, &has_nrm);
+    if (rc != CG_OK) return rc;
+    cg_obb root;
+    std::vector<cg_obb> obbs(2ull * N);
+    std::vector<uint32_t> ref(2ull * N), cnt(2ull * N), idx(3ull * T);
+    std::vector<float> pos(9ull * T), nrm(has_nrm ? 9ull * T : 0);
+    rc = cg_tree_export(c, id, &root, obbs.data(), ref.data(), cnt.data(), pos.data(), has_nrm ? nrm.data() : nullptr,
+                        idx.data());
+    if (rc != CG_OK) return rc;
+    std::vector<unsigned char> buf;
+    auto put = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        buf.insert(buf.end(), b, b + n);
+    };
+    const uint32_t head[3] = {N, T, has_nrm ? 1u : 0u};
+    put(kCacheMagic, 8);
+    put(head, sizeof(head));
+    put(&root, sizeof(root));
+    put(obbs.data(), sizeof(cg_obb) * obbs.size());
+    put(ref.data(), 4 * ref.size());
+    put(cnt.data(), 4 * cnt.size());
+    put(pos.data(), 4 * pos.size());
+    put(nrm.data(), 4 * nrm.size());
+    put(idx.data(), 4 * idx.size());
+    const uint64_t h = fnv1a(buf.data(), buf.size());
+    put(&h, 8);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(c, CG_ERR_INVALID_ARGUMENT, "cannot write %s", path);
+    const size_t w = std::fwrite(buf.data(), 1, buf.size(), f);
+    const int closed = std::fclose(f);
+    if (w != buf.size() || closed != 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "short write to %s", path);
+    return CG_OK;
+}
+
+int cg_tree_load(cg_ctx* c, const char* path, uint32_t* tree_id) {
+    if (!c || !path || !tree_id) return CG_ERR_INVALID_ARGUMENT;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(c, CG_ERR_NOT_FOUND, "cannot read %s", path);
+    std::vector<unsigned char> buf;
+    unsigned char chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+    std::fclose(f);
+    const size_t fixed = 8 + 12 + sizeof(cg_obb) + 8;
+    if (buf.size() < fixed || std::memcmp(buf.data(), kCacheMagic, 8) != 0)
+        return fail(c, CG_ERR_BAD_TREE, "%s is not a tree cache file", path);
+    uint32_t head[3];
+    std::memcpy(head, buf.data() + 8, sizeof(head));
+    const uint64_t N = head[0], T = head[1];
+    const bool has_nrm = (head[2] & 1u) != 0;
+    const uint64_t need = fixed + N * (2 * sizeof(cg_obb) + 16) + T * (36 + (has_nrm ? 36 : 0) + 12);
+    if (buf.size() != need) return fail(c, CG_ERR_BAD_TREE, "%s: %zu bytes, its header says %llu", path, buf.size(),
+                                        (unsigned long long)need);
+    uint64_t h;
+    std::memcpy(&h, buf.data() + need - 8, 8);
+    if (h != fnv1a(buf.data(), need - 8)) return fail(c, CG_ERR_BAD_TREE, "%s: checksum mismatch", path);
+    const unsigned char* p = buf.data() + 20;
+    cg_obb root;
+    std::memcpy(&root, p, sizeof(root));
+    p += sizeof(root);
+    std::vector<cg_obb> obbs(2 * N);
+    std::vector<uint32_t> ref(2 * N), cnt(2 * N), idx(3 * T);
+    std::vector<float> pos(9 * T), nrm(has_nrm ? 9 * T : 0);
+    auto get = [&](void* d, size_t n) {
+        if (n) std::memcpy(d, p, n);
+        p += n;
+    };
+    get(obbs.data(), sizeof(cg_obb) * obbs.size());
+    get(ref.data(), 4 * ref.size());
+    get(cnt.data(), 4 * cnt.size());
+    get(pos.data(), 4 * pos.size());
+    get(nrm.data(), 4 * nrm.size());
+    get(idx.data(), 4 * idx.size());
+    cg_tree_view v{};
+    v.root_obb = root;
+    v.node_count = uint32_t(N);
+    v.node_obbs = obbs.data();
+    v.node_ref = ref.data();
+    v.node_tri_count = cnt.data();
+    v.triangle_count = uint32_t(T);
+    v.triangles_position = pos.data();
+    v.triangles_normal = has_nrm ? nrm.data() : nullptr;
+    v.triangles_indices = idx.data();
+    return cg_tree_upload(c, &v, tree_id);
+}
+
 int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const* positions,
                         const uint32_t* n_positions, uint32_t n, void* stream) {
     if (!c || (n && (!tree_ids || !positions || !n_positions))) return CG_ERR_INVALID_ARGUMENT;

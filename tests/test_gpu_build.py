@@ -132,3 +132,35 @@ def test_built_tree_refits_like_uploaded(gpu_ctx, port):
     assert not np.array_equal(a.root, port.tree_build(m.points, m.indices, m.normals).export().root)
     gpu_ctx.free_tree(built)
     gpu_ctx.free_tree(uploaded)
+
+
+def test_tree_cache_round_trip(gpu_ctx, tmp_path):
+    """cg_tree_save / cg_tree_load: the same flat tree back; a damaged or
+    truncated file is refused."""
+    sc = scenes.scene()
+    meshes = [sc.meshes[3], M(sc.meshes[4].points, sc.meshes[4].indices)]  # with and without normals
+    ids = gpu_ctx.build_trees(meshes)
+    for k, tid in enumerate(ids):
+        path = str(tmp_path / f"tree{k}.cgtree")
+        gpu_ctx.save_tree(int(tid), path)
+        back = gpu_ctx.load_tree(path)
+        a, b = gpu_ctx.export_tree(int(tid)).arrays(), gpu_ctx.export_tree(back).arrays()
+        assert a.keys() == b.keys()
+        for key in a:
+            assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), key
+        gpu_ctx.free_tree(back)
+        raw = bytearray(open(path, "rb").read())
+        raw[100] ^= 1
+        open(path, "wb").write(bytes(raw))
+        with pytest.raises(capi.CgError) as e:
+            gpu_ctx.load_tree(path)
+        assert e.value.code == capi.CG_ERR_BAD_TREE
+        open(path, "wb").write(bytes(raw[:-9]))
+        with pytest.raises(capi.CgError) as e:
+            gpu_ctx.load_tree(path)
+        assert e.value.code == capi.CG_ERR_BAD_TREE
+    with pytest.raises(capi.CgError) as e:
+        gpu_ctx.load_tree(str(tmp_path / "missing.cgtree"))
+    assert e.value.code == capi.CG_ERR_NOT_FOUND
+    for tid in ids:
+        gpu_ctx.free_tree(int(tid))
