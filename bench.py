@@ -581,7 +581,7 @@ def run_deforming(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
 def run_gpu(args) -> dict:
     import torch
 
-    from inmyroom_vulkan_gb300 import capi, scenes
+    from inmyroom_vulkan_gb300 import capi, scenes, shard
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -627,9 +627,8 @@ def run_gpu(args) -> dict:
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     trav_ms, narrow_ms = [], []
-    if dist:
-        dist.barrier()
     torch.cuda.synchronize()
+    shard.barrier(dist)
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
             flush.fill_(k & 0xff)
@@ -639,6 +638,7 @@ def run_gpu(args) -> dict:
             trav_ms.append(ctx.traversal_ms())
             narrow_ms.append(ctx.narrow_ms())
         torch.cuda.synchronize()
+        shard.barrier(dist)
         step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
         st = ctx.sync_stats()
         assert st["tri_tests"] == tests_per_step and st["status"] == 0 and st["rays"] == rays_per_step
@@ -666,13 +666,10 @@ def run_gpu(args) -> dict:
             e2e_times.append(time.perf_counter() - t0)
         assert len(pairs) == pairs_per_step and len(rays) == rays_per_step and len(avgs) == n
         assert np.array_equal(pairs.view(np.uint8), ctx.tri_pairs().view(np.uint8))
-    total_ms = float(np.sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    # the slowest rank's times (every rank does a replica's fixed work)
+    total_ms = shard.max_over_ranks(float(np.sum(step_ms)), dist, dev)
     value = world * tests_per_step * args.steps / (total_ms / 1e3)
-    e2e_s = float(np.sum(e2e_times))
+    e2e_s = shard.max_over_ranks(float(np.sum(e2e_times)), dist, dev)
     e2e_value = world * tests_per_step * args.steps / e2e_s
 
     peaks = measured_peaks()
