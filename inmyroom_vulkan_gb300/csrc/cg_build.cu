@@ -18,12 +18,17 @@
 //                 of its corners
 //   build_cov     a thread per node and product: the covariance sum in
 //                 corner order
-//   build_fit     a warp per node: fewer than two distinct corners give the
-//                 empty or point box; else eig3 in FP64 (lane 0), the FP64
-//                 min/max projections on the axes over the lanes (equal
-//                 values: the later corner, as the sequential std::min /
-//                 std::max keep) and the box; then, for a node of more than 4
-//                 triangles, OBBtreeSplitBuildNode::SplitOBBandCreateChildren
+//   build_eig     a thread per node: eig3 of the covariance in FP64; the
+//                 box axes are the rows of the eigenvector matrix
+//   build_proj    a thread per triangle position: its corners' FP64
+//                 projections on its node's axes
+//   build_fit     a warp per node of more than 16 triangles (build_fit_small:
+//                 a thread per smaller node): fewer than two distinct corners
+//                 give the empty or point box; else the min/max projections
+//                 (integer keys of the doubles; equal values: the later
+//                 corner, as the sequential std::min / std::max keep) and the
+//                 box; then, for a node of more than 4 triangles,
+//                 OBBtreeSplitBuildNode::SplitOBBandCreateChildren
 //                 (OBBtree.cpp:43-108): axes by half-length, longest first
 //                 (equal lengths keep u, v, w order); left when the mean of a
 //                 triangle's projection interval is <= the centre's
@@ -191,23 +196,48 @@ __global__ void build_eig_kernel(const BuildParams B) {
     }
 }
 
+// The projections of every corner of the level on its node's three axes
+// (the dot products of OBB.cpp:117, 136, 155), a thread per triangle
+// position, into the products' buffer (free once the covariances are
+// summed): [axis][corner].
+__global__ void build_proj_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < B.T; t += gridDim.x * blockDim.x) {
+        const uint32_t o = B.own[t];
+        if (o < B.lo || o >= B.hi) continue;
+        const double* ax = B.mom + 9ull * (o - B.lo);
+        double a[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = ax[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint64_t j = 3ull * t + k;
+            const double px = B.D[j], py = B.D[n3 + j], pz = B.D[2 * n3 + j];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                double pr = a[3 * r] * px;
+                pr = pr + a[3 * r + 1] * py;
+                pr = pr + a[3 * r + 2] * pz;
+                B.Tm[r * n3 + j] = pr;
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ Box empty_box() {  // OBB::EmptyOBB (OBB.cpp:168-178)
     const float e = FLT_EPSILON;
     return Box{make_float3(0.f, 0.f, 0.f), make_float3(e, 0.f, 0.f), make_float3(0.f, e, 0.f),
                make_float3(0.f, 0.f, e)};
 }
 
-// The projections of corner j (coordinates px, py, pz) on the three axes.
-__device__ __forceinline__ void project3(const double* ax, double px, double py, double pz, uint32_t j, Ext* lo,
-                                         Ext* hi) {
+// Corner j's projections (from build_proj) into the extremes.
+__device__ __forceinline__ void extend3(const double* pr, uint64_t n3, uint32_t j, Ext* lo, Ext* hi) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double pr = ax[3 * a] * px;
-        pr = pr + ax[3 * a + 1] * py;
-        pr = pr + ax[3 * a + 2] * pz;
-        const long long k = dkey(pr);
-        take_lo(lo[a], k, pr, j);
-        take_hi(hi[a], k, pr, j);
+        const double v = pr[a * n3 + j];
+        const long long k = dkey(v);
+        take_lo(lo[a], k, v, j);
+        take_hi(hi[a], k, v, j);
     }
 }
 
@@ -259,8 +289,8 @@ __device__ Box fit_warp(const BuildParams& B, uint32_t begin, uint32_t n, const 
     Ext lo[3], hi[3];
     init_ext(lo, hi);
     const uint64_t n3 = 3ull * B.T;
-    const double* d = B.D + 3ull * begin;
-    for (uint32_t j = lane; j < np; j += 32u) project3(a, d[j], d[n3 + j], d[2 * n3 + j], j, lo, hi);
+    const double* pr = B.Tm + 3ull * begin;
+    for (uint32_t j = lane; j < np; j += 32u) extend3(pr, n3, j, lo, hi);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         warp_extreme(lo[k], true);
@@ -288,8 +318,8 @@ __device__ Box fit_thread(const BuildParams& B, uint32_t begin, uint32_t n, cons
     Ext lo[3], hi[3];
     init_ext(lo, hi);
     const uint64_t n3 = 3ull * B.T;
-    const double* d = B.D + 3ull * begin;
-    for (uint32_t j = 0; j < np; ++j) project3(a, d[j], d[n3 + j], d[2 * n3 + j], j, lo, hi);
+    const double* pr = B.Tm + 3ull * begin;
+    for (uint32_t j = 0; j < np; ++j) extend3(pr, n3, j, lo, hi);
     return box_from(a, lo, hi);
 }
 
@@ -616,6 +646,7 @@ cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStre
     build_terms_kernel<<<grid(p.T), 128, 0, s>>>(p);
     build_cov_kernel<<<grid(6ull * width), 128, 0, s>>>(p);
     build_eig_kernel<<<grid(width), 128, 0, s>>>(p);
+    build_proj_kernel<<<grid(p.T), 128, 0, s>>>(p);
     const uint32_t blocks = (width + 3u) / 4u;
     build_fit_kernel<<<blocks < 65535u ? blocks : 65535u, 128, 0, s>>>(p);
     build_fit_small_kernel<<<grid(width), 128, 0, s>>>(p);
