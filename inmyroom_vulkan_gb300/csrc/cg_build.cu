@@ -121,6 +121,30 @@ __global__ void build_points_kernel(const BuildParams B) {
     }
 }
 
+// s + x[0] + x[1] + ... + x[n-1], left to right in FP64. The adds are one
+// dependent chain; the loads are not, so they go in blocks of kChainBlock,
+// the next block in flight while the current one is added.
+constexpr uint32_t kChainBlock = 16;
+__device__ __forceinline__ double chain_sum(const double* x, uint32_t n) {
+    double s = 0.0;
+    double cur[kChainBlock], nxt[kChainBlock];
+#pragma unroll
+    for (uint32_t k = 0; k < kChainBlock; ++k) cur[k] = k < n ? x[k] : 0.0;
+    for (uint32_t j = 0; j < n; j += kChainBlock) {
+#pragma unroll
+        for (uint32_t k = 0; k < kChainBlock; ++k) {
+            const uint32_t i = j + kChainBlock + k;
+            nxt[k] = i < n ? x[i] : 0.0;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kChainBlock; ++k)
+            if (j + k < n) s = s + cur[k];  // only the reference's terms: adding a 0 could flip a -0
+#pragma unroll
+        for (uint32_t k = 0; k < kChainBlock; ++k) cur[k] = nxt[k];
+    }
+    return s;
+}
+
 // A thread per node and coordinate: the coordinate's sum over the node's
 // corners in order (std::accumulate, OBB.cpp:53-55), then the mean.
 __global__ void build_sums_kernel(const BuildParams B) {
@@ -129,10 +153,8 @@ __global__ void build_sums_kernel(const BuildParams B) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         const uint32_t node = B.lo + g / 3u, c = g % 3u;
         const BuildNode& N = B.nodes[node];
-        const double* d = B.D + c * n3 + 3ull * N.begin;
         const uint32_t np = 3u * N.count;
-        double s = 0.0;
-        for (uint32_t j = 0; j < np; ++j) s = s + d[j];
+        const double s = chain_sum(B.D + c * n3 + 3ull * N.begin, np);
         B.mom[9ull * (node - B.lo) + c] = np ? s / double(np) : 0.0;
     }
 }
@@ -168,11 +190,7 @@ __global__ void build_cov_kernel(const BuildParams B) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         const uint32_t node = B.lo + g / 6u, q = g % 6u;
         const BuildNode& N = B.nodes[node];
-        const double* d = B.Tm + q * n3 + 3ull * N.begin;
-        const uint32_t np = 3u * N.count;
-        double s = 0.0;
-        for (uint32_t j = 0; j < np; ++j) s = s + d[j];
-        B.mom[9ull * (node - B.lo) + 3u + q] = s;
+        B.mom[9ull * (node - B.lo) + 3u + q] = chain_sum(B.Tm + q * n3 + 3ull * N.begin, 3u * N.count);
     }
 }
 
