@@ -1039,7 +1039,8 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
         off += up(bytes);
         return o;
     };
-    const size_t oP = take(sizeof(float) * 9 * T), oCN = take(any_normals ? sizeof(float) * 9 * T : 0);
+    const size_t oP = take(sizeof(float) * 9 * T), oPp = take(sizeof(float) * 9 * T);
+    const size_t oCN = take(any_normals ? sizeof(float) * 9 * T : 0);
     const size_t oPerm = take(4 * T), oScr = take(4 * T), oOwn = take(4 * T);
     const size_t oD = take(sizeof(double) * 9 * T), oTm = take(sizeof(double) * 18 * T);
     const size_t oMom = take(sizeof(double) * 9 * std::max<uint64_t>(T, n));  // a level: one node per triangle, or the roots
@@ -1064,6 +1065,7 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     in.P = reinterpret_cast<float*>(mem + oP);
     in.corner_normals = any_normals ? reinterpret_cast<float*>(mem + oCN) : nullptr;
     bp.P = in.P;
+    bp.Pp = reinterpret_cast<float*>(mem + oPp);
     bp.perm = reinterpret_cast<uint32_t*>(mem + oPerm);
     bp.scratch = reinterpret_cast<uint32_t*>(mem + oScr);
     bp.own = reinterpret_cast<uint32_t*>(mem + oOwn);

@@ -105,8 +105,9 @@ __device__ __forceinline__ void warp_extreme(Ext& e, bool lo) {
     }
 }
 
-// The corners of the level's triangles as doubles, by coordinate, at their
-// triangle's position: a thread per position (positions of earlier levels'
+// The corners of the level's triangles at their triangle's position: as
+// doubles by coordinate, and as floats by position (so that a node reads its
+// corners contiguously); a thread per position (positions of earlier levels'
 // leaves are skipped).
 __global__ void build_points_kernel(const BuildParams B) {
     const uint64_t n3 = 3ull * B.T;
@@ -114,10 +115,14 @@ __global__ void build_points_kernel(const BuildParams B) {
         const uint32_t o = B.own[t];
         if (o < B.lo || o >= B.hi) continue;
         const float* q = B.P + 9ull * B.perm[t];
+        float* pp = B.Pp + 9ull * t;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) B.D[c * n3 + 3ull * t + k] = double(q[3 * k + c]);
+            for (int c = 0; c < 3; ++c) {
+                B.D[c * n3 + 3ull * t + k] = double(q[3 * k + c]);
+                pp[3 * k + c] = q[3 * k + c];
+            }
     }
 }
 
@@ -291,11 +296,11 @@ __device__ __forceinline__ bool same_point(float3 p, float3 q) { return p.x == q
 // The node's box (OBB::CreateOBBfromPoints, OBB.cpp:33-89) by a warp.
 __device__ Box fit_warp(const BuildParams& B, uint32_t begin, uint32_t n, const double* ax, uint32_t lane) {
     if (n == 0u) return empty_box();
-    const uint32_t* perm = B.perm + begin;
+    const float* pn = B.Pp + 9ull * begin;
     const uint32_t np = 3u * n;
-    const float3 p0 = corner(B.P, perm[0], 0);
+    const float3 p0 = corner(pn, 0, 0);
     bool differ = false;
-    for (uint32_t j = lane; j < np; j += 32u) differ |= !same_point(corner(B.P, perm[j / 3u], j % 3u), p0);
+    for (uint32_t j = lane; j < np; j += 32u) differ |= !same_point(corner(pn, j / 3u, j % 3u), p0);
     if (!__any_sync(kAll, differ)) {  // one distinct point
         Box b = empty_box();
         b.c = p0;
@@ -320,11 +325,11 @@ __device__ Box fit_warp(const BuildParams& B, uint32_t begin, uint32_t n, const 
 // The same by one thread (a small node).
 __device__ Box fit_thread(const BuildParams& B, uint32_t begin, uint32_t n, const double* ax) {
     if (n == 0u) return empty_box();
-    const uint32_t* perm = B.perm + begin;
+    const float* pn = B.Pp + 9ull * begin;
     const uint32_t np = 3u * n;
-    const float3 p0 = corner(B.P, perm[0], 0);
+    const float3 p0 = corner(pn, 0, 0);
     bool differ = false;
-    for (uint32_t j = 1; j < np && !differ; ++j) differ = !same_point(corner(B.P, perm[j / 3u], j % 3u), p0);
+    for (uint32_t j = 1; j < np && !differ; ++j) differ = !same_point(corner(pn, j / 3u, j % 3u), p0);
     if (!differ) {
         Box b = empty_box();
         b.c = p0;
@@ -357,8 +362,8 @@ __device__ __forceinline__ bool goes_left(const float* P, uint32_t t, float3 axi
 
 __device__ __forceinline__ void split_axes(const Box& b, float3* dir, int* ord);
 
-// Splits the node's range (perm, n > kLeafMax) in place and returns the
-// left child's size.
+// Splits the node's range (perm, n > kLeafMax; P its corners by position) in
+// place and returns the left child's size.
 __device__ uint32_t split_node(const float* P, uint32_t* perm, uint32_t* scratch, uint32_t n, const Box& b,
                                uint32_t lane) {
     float3 dir[3];
@@ -374,7 +379,7 @@ __device__ uint32_t split_node(const float* P, uint32_t* perm, uint32_t* scratch
         uint32_t cnt = 0;
         for (uint32_t base = 0; base < n; base += 32u) {
             const uint32_t t = base + lane;
-            const bool left = t < n && goes_left(P, perm[t], a, c);
+            const bool left = t < n && goes_left(P, t, a, c);
             cnt += __popc(__ballot_sync(kAll, left));
         }
         if (cnt > 0u && cnt < n) {
@@ -393,7 +398,7 @@ __device__ uint32_t split_node(const float* P, uint32_t* perm, uint32_t* scratch
         bool left = false;
         if (valid) {
             id = perm[t];
-            left = chosen ? goes_left(P, id, axis, cp) : (t < nl);
+            left = chosen ? goes_left(P, t, axis, cp) : (t < nl);
         }
         const unsigned ml = __ballot_sync(kAll, left), mv = __ballot_sync(kAll, valid);
         if (valid) scratch[left ? lb + __popc(ml & lt) : nl + rb + __popc(mv & ~ml & lt)] = id;
@@ -437,7 +442,7 @@ __device__ uint32_t split_thread(const float* P, uint32_t* perm, uint32_t* scrat
         const float3 a = dir[ord[k]];
         const float c = dot3(b.c, a);
         uint32_t cnt = 0;
-        for (uint32_t t = 0; t < n; ++t) cnt += goes_left(P, perm[t], a, c) ? 1u : 0u;
+        for (uint32_t t = 0; t < n; ++t) cnt += goes_left(P, t, a, c) ? 1u : 0u;
         if (cnt > 0u && cnt < n) {
             chosen = true;
             nl = cnt;
@@ -448,7 +453,7 @@ __device__ uint32_t split_thread(const float* P, uint32_t* perm, uint32_t* scrat
     uint32_t lb = 0, rb = nl;
     for (uint32_t t = 0; t < n; ++t) {
         const uint32_t id = perm[t];
-        const bool left = chosen ? goes_left(P, id, axis, cp) : (t < nl);
+        const bool left = chosen ? goes_left(P, t, axis, cp) : (t < nl);
         scratch[left ? lb++ : rb++] = id;
     }
     for (uint32_t t = 0; t < n; ++t) perm[t] = scratch[t];
@@ -491,7 +496,7 @@ __global__ void __launch_bounds__(128) build_fit_kernel(const BuildParams B) {
         const uint32_t begin = N.begin, n = N.count;
         if (n <= kSmall) continue;
         const Box box = fit_warp(B, begin, n, B.mom + 9ull * (id - B.lo), lane);
-        const uint32_t nl = split_node(B.P, B.perm + begin, B.scratch + begin, n, box, lane);
+        const uint32_t nl = split_node(B.Pp + 9ull * begin, B.perm + begin, B.scratch + begin, n, box, lane);
         uint32_t k = 0;
         if (lane == 0u) {
             store_box(N, box);
@@ -514,7 +519,7 @@ __global__ void __launch_bounds__(128) build_fit_small_kernel(const BuildParams 
         store_box(N, box);
         N.kid = kNoKid;
         if (n <= kLeafMax) continue;
-        const uint32_t nl = split_thread(B.P, B.perm + begin, B.scratch + begin, n, box);
+        const uint32_t nl = split_thread(B.Pp + 9ull * begin, B.perm + begin, B.scratch + begin, n, box);
         const uint32_t k = add_children(B, N, nl);
         if (k == kNoKid) continue;
         for (uint32_t t = 0; t < n; ++t) B.own[begin + t] = t < nl ? k : k + 1u;

@@ -376,6 +376,7 @@ struct BuildNode {           // 64 bytes
 static_assert(sizeof(BuildNode) == 64, "BuildNode layout");
 struct BuildParams {
     const float* P;          // [triangles][3][3] corners, the meshes one after another
+    float* Pp;               // [triangles][3][3] the same at each triangle's position in the permutation
     uint32_t* perm;          // [triangles] triangle ids, each node's range partitioned in place
     uint32_t* scratch;       // [triangles]
     uint32_t* own;           // [triangles] the node that holds each position (its level's or a leaf's)
