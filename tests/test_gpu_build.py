@@ -164,3 +164,19 @@ def test_tree_cache_round_trip(gpu_ctx, tmp_path):
     assert e.value.code == capi.CG_ERR_NOT_FOUND
     for tid in ids:
         gpu_ctx.free_tree(int(tid))
+
+
+def test_trees_from_gltf(gpu_ctx, port, tmp_path):
+    """Meshes through a glTF file (inmyroom_vulkan_gb300.gltf) built on the
+    device: the oracle's trees of the same triangles, bit for bit; the
+    instances' matrices come back exactly."""
+    from inmyroom_vulkan_gb300 import gltf
+
+    sc = scenes.scene(n_entities=12)
+    meshes = [gltf.Mesh(f"m{k}", m.points, m.normals if k % 3 else None, np.asarray(m.indices).reshape(-1, 3))
+              for k, m in enumerate(sc.meshes)]
+    path = str(tmp_path / "scene.gltf")
+    gltf.save(path, gltf.Scene(meshes, [gltf.Instance(k, sc.mats[k]) for k in range(12)]))
+    back = gltf.load(path)
+    assert all(np.array_equal(a.matrix, sc.mats[a.mesh]) for a in back.instances)
+    build_and_check(gpu_ctx, port, [M(m.points, m.indices, m.normals) for m in back.meshes])
