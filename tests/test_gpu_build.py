@@ -80,6 +80,14 @@ def test_degenerate_meshes(gpu_ctx, port):
         M(np.round(pts * 4) / 4, rng.integers(0, 40, (200, 3))),   # equal projections, signed zeros
     ]
     build_and_check(gpu_ctx, port, cases)
+    # an empty mesh between two others in one batch
+    mixed = gpu_ctx.build_trees([cases[2], M(np.zeros((0, 3)), np.zeros((0, 3))), cases[6]])
+    for tid, m in zip((mixed[0], mixed[2]), (cases[2], cases[6])):
+        same(gpu_ctx.export_tree(int(tid)), port.tree_build(m.points, m.indices, m.normals).export(),
+             normals=m.normals is not None)
+    assert gpu_ctx.tree_info(int(mixed[1]))[:2] == (0, 0)
+    for tid in mixed:
+        gpu_ctx.free_tree(int(tid))
     # an empty mesh: the empty box and no triangles
     tid = int(gpu_ctx.build_trees([M(np.zeros((0, 3)), np.zeros((0, 3)))])[0])
     t = gpu_ctx.export_tree(tid)

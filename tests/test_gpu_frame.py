@@ -129,6 +129,12 @@ def test_frame_edge_cases(gpu_ctx, scene_trees):
     with pytest.raises(capi.CgError) as e:
         gpu_ctx.collision_frame(ids, sc.mats, sc.mats, cap=10)
     assert e.value.code == capi.CG_ERR_OUTPUT_OVERFLOW
+    # more broad pairs than the context's max_queries: refused with the count
+    with capi.Context(max_queries=32) as small:  # the first 40 entities make 47 broad pairs
+        sids = small.build_trees(sc.meshes[:40])
+        with pytest.raises(capi.CgError) as e:
+            small.collision_frame(sids, sc.mats[:40], sc.mats[:40])
+        assert e.value.code == capi.CG_ERR_OUTPUT_OVERFLOW
     # an unknown tree id
     bad = ids.copy()
     bad[3] = 0xFFFFFF
