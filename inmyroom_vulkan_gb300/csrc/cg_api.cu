@@ -1207,11 +1207,15 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
                           p.nrm == ~0ull ? nullptr : reinterpret_cast<float*>(ab + p.nrm),
                           reinterpret_cast<uint2*>(ab + p.ranges), reinterpret_cast<uint32_t*>(ab + p.topo)};
     }
-    CG_CUDA(cudaMemcpyAsync(d_emit, em.data(), sizeof(BuildEmit) * n, cudaMemcpyHostToDevice, s), "upload places");
-    CG_CUDA(launch_build_emit(bp, in, flat, d_emit, c->recs.ptr, c->tris.ptr, n_nodes, n, sms, s), "emit kernels");
-    for (uint32_t i = 0; i < n; ++i)
-        CG_CUDA(launch_surfaces(c->recs.ptr, em[i].rec_base, em[i].n_recs, s), "surface kernel");
-    CG_CUDA(cudaStreamSynchronize(s), "tree build");
+    // from here on a failure gives the arena places back
+    cudaError_t e = cudaMemcpyAsync(d_emit, em.data(), sizeof(BuildEmit) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_build_emit(bp, in, flat, d_emit, c->recs.ptr, c->tris.ptr, n_nodes, n, sms, s);
+    for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) e = launch_surfaces(c->recs.ptr, em[i].rec_base, em[i].n_recs, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        undo();
+        return cuda_fail(c, e, "tree layout kernels");
+    }
     for (uint32_t i = 0; i < n; ++i) {
         cg_ctx::Slot slot;
         slot.rec_base = em[i].rec_base;
