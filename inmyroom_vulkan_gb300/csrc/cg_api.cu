@@ -1,6 +1,8 @@
 // Host side of the C ABI declared in include/collide_gpu.h: context and
-// buffers, tree arenas with upload validation, launches, result read-back and
-// the CUDA graph of one collide step.
+// buffers, tree arenas with upload validation, launches, result read-back,
+// the CUDA graph of one collide step, deformation, refit and the
+// differentiable energy. Tree build and the tree cache are in cg_api_tree.cu,
+// the broad phase, shooting and the collision frame in cg_api_frame.cu.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -14,205 +16,9 @@
 #include <utility>
 #include <vector>
 
-#include "cg_internal.h"
-#include "collide_gpu.h"
+#include "cg_ctx.h"
 
-using namespace cg;
-
-namespace {
-
-// A growable device array of fixed-size units (a unit is `width` float4s)
-// with first-fit reuse of released ranges. Growth copies the contents to a
-// larger allocation at the same offsets, so indices stay valid; the base
-// pointer changes and `gen` counts those changes.
-struct Arena {
-    float4* ptr = nullptr;
-    uint32_t width = 1;
-    uint64_t cap = 0;
-    uint64_t used = 0;
-    uint64_t gen = 0;
-    std::vector<std::pair<uint64_t, uint64_t>> free_list;  // (offset, units), sorted by offset
-
-    cudaError_t alloc(uint64_t n, uint64_t* off, cudaStream_t s) {
-        for (size_t i = 0; i < free_list.size(); ++i) {
-            if (free_list[i].second >= n) {
-                *off = free_list[i].first;
-                free_list[i].first += n;
-                free_list[i].second -= n;
-                if (free_list[i].second == 0) free_list.erase(free_list.begin() + long(i));
-                return cudaSuccess;
-            }
-        }
-        if (used + n > cap) {
-            uint64_t ncap = std::max<uint64_t>(std::max<uint64_t>(cap * 2, used + n), 1u << 14);
-            float4* np = nullptr;
-            cudaError_t e = cudaMalloc(&np, sizeof(float4) * width * ncap);
-            if (e != cudaSuccess) return e;
-            if (used) {
-                e = cudaStreamSynchronize(s);
-                if (e == cudaSuccess)
-                    e = cudaMemcpy(np, ptr, sizeof(float4) * width * used, cudaMemcpyDeviceToDevice);
-                if (e != cudaSuccess) {
-                    cudaFree(np);
-                    return e;
-                }
-            }
-            cudaFree(ptr);
-            ptr = np;
-            cap = ncap;
-            ++gen;
-        }
-        *off = used;
-        used += n;
-        return cudaSuccess;
-    }
-
-    void release(uint64_t off, uint64_t n) {
-        if (n == 0) return;
-        auto it = std::lower_bound(free_list.begin(), free_list.end(), std::make_pair(off, uint64_t(0)));
-        it = free_list.insert(it, {off, n});
-        size_t i = size_t(it - free_list.begin());
-        if (i + 1 < free_list.size() && free_list[i].first + free_list[i].second == free_list[i + 1].first) {
-            free_list[i].second += free_list[i + 1].second;
-            free_list.erase(free_list.begin() + long(i + 1));
-        }
-        if (i > 0 && free_list[i - 1].first + free_list[i - 1].second == free_list[i].first) {
-            free_list[i - 1].second += free_list[i].second;
-            free_list.erase(free_list.begin() + long(i));
-            --i;
-        }
-        if (free_list[i].first + free_list[i].second == used) {
-            used = free_list[i].first;
-            free_list.erase(free_list.begin() + long(i));
-        }
-    }
-
-    void destroy() {
-        cudaFree(ptr);
-        ptr = nullptr;
-        cap = used = 0;
-        free_list.clear();
-    }
-};
-
-}  // namespace
-
-struct cg_ctx {
-    cg_config cfg{};
-    int device = 0;
-    int sm_count = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t blocks = 0;         // persistent traversal grid
-    uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
-    uint32_t accumulate_blocks = 0, emit_blocks = 0;  // contact kernels: one resident wave
-    uint32_t energy_blocks = 0;                        // energy kernels: one resident wave
-
-    // trees
-    struct Slot {
-        uint64_t rec_base = 0, n_recs = 0, tri_base = 0, n_tris = 0;
-        uint32_t n_tri_used = 0;  // the tree's triangle count (n_tris is at least 1)
-        float* nrm = nullptr;
-        uint2* ranges = nullptr;  // per record: first triangle and count of its subtree (refit)
-        uint32_t* topo = nullptr;  // refit: parent per record, then the leaf records
-        uint32_t n_leaves = 0;
-        std::shared_ptr<void> pool;  // the block that holds nrm, ranges and topo when the tree was built here
-        bool live = false;
-    };
-    std::vector<Slot> trees;
-    Arena recs, tris;
-    DevTree* d_trees = nullptr;
-    uint32_t d_trees_cap = 0;
-    uint64_t table_gen = 0;         // reallocations of d_trees
-
-    // per-launch buffers
-    cg_query* d_queries = nullptr;  // staging for host queries
-    PackedQuery* d_packed = nullptr;
-    Counters* d_ctr = nullptr;
-    uint4* d_pool = nullptr;        // donated node-pair entries
-    unsigned int* d_ready = nullptr;
-    uint32_t slot_cap = 0;          // chunk slots donors may reserve
-    uint32_t slot_alloc = 0;        // allocated, with slack for concurrent reservations and waiters
-    uint4* d_leaf_list = nullptr;   // candidate leaf pairs between the two kernels
-    cg_tri_pair* d_pairs = nullptr;
-    cg_leaf_pair* d_leafs = nullptr;
-    unsigned int* d_trace = nullptr;
-    uint32_t trace_ns = 0;
-
-    // contacts and rays (CG_CONTACTS), allocated when max_contacts > 0
-    struct Contacts {
-        uint4* pair_aux = nullptr;
-        ContactSlot* table = nullptr;
-        uint32_t table_slots = 0;
-        uint32_t* occupied = nullptr;
-        unsigned long long* vkeys = nullptr;
-        uint32_t vslots = 0;
-        uint32_t* vocc = nullptr;
-        cg_contact* contacts = nullptr;
-        cg_ray* rays = nullptr;
-        uint32_t max_rays = 0;
-        double* sums = nullptr;
-        cg_ray_average* averages = nullptr;
-    } ct;
-
-    cg_query* h_queries = nullptr;  // pinned
-    Counters* h_ctr = nullptr;      // pinned
-
-    uint32_t last_flags = 0;
-    uint32_t last_n = 0;            // queries of the last collide step enqueued
-
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
-    uint64_t graph_gen = 0;         // arena generations the graph was captured with
-    uint32_t graph_n = 0, graph_flags = 0;
-    struct HostGraph {              // cg_collide's own graph of a whole step
-        cudaGraphExec_t exec = nullptr;
-        uint32_t n = 0, flags = 0;
-        uint64_t gen = 0, out_gen = 0;
-    } host_graph;
-    bool capturing = false;
-    // cg_set_host_outputs: page-locked host destinations of cg_collide's
-    // results (device aliases), written by the step graph itself
-    struct HostOut {
-        cg_tri_pair* pairs = nullptr;
-        uint64_t pairs_cap = 0;
-        cg_ray* rays = nullptr;
-        uint64_t rays_cap = 0;
-        cg_ray_average* averages = nullptr;
-        uint64_t averages_cap = 0;
-        uint64_t gen = 0;  // settings changes (the step graph is captured again)
-    } host_out;
-    uint32_t copy_blocks = 0;
-    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_t2 = nullptr;  // traversal start, end; narrow end
-    cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
-    cudaStream_t side = nullptr;    // a branch of cg_collide's step graph (host copy of the pairs)
-    cudaEvent_t ev_fork = nullptr, ev_joined = nullptr;
-
-    // batch tables of cg_deform_batch / cg_tree_refit_batch in device memory,
-    // uploaded when their contents change
-    struct Table {
-        std::vector<char> host;
-        void* dev = nullptr;
-        size_t cap = 0;
-    } deform_table, refit_table, skeleton_table, energy_table;
-    void* refit_scratch = nullptr;          // RefitBufs for this many records of a refit batch
-    uint32_t refit_scratch_cap = 0;
-    float* pose_scratch = nullptr;          // pose adjoint: dE/dG accumulated per bone
-    uint64_t pose_scratch_cap = 0;
-    float* vgrad = nullptr;                 // energy adjoint: per-vertex gradient, zero between calls
-    uint64_t vgrad_cap = 0;
-    void* shoot = nullptr;                  // cg_shoot_rays: queries, rays, tags, per-ray results, deltas, flag
-    size_t shoot_cap = 0;
-    void* broad = nullptr;                  // cg_broad_phase: ids, globals, callbacks, projections, pairs, count
-    size_t broad_cap = 0;
-    void* frame = nullptr;                  // cg_collision_frame's buffers
-    size_t frame_cap = 0;
-    void* build = nullptr;                  // cg_tree_build's scratch
-    size_t build_cap = 0;
-
-    std::string err;
-};
-
-namespace {
+namespace cg_host {
 
 int fail(cg_ctx* c, int code, const char* fmt, ...) {
     if (c) {
@@ -231,11 +37,6 @@ int cuda_fail(cg_ctx* c, cudaError_t e, const char* what) {
     return fail(c, code, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CG_CUDA(call, what)                                   \
-    do {                                                      \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
-    } while (0)
 
 bool pow2(uint32_t x) { return x && !(x & (x - 1)); }
 
@@ -516,7 +317,7 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
 // pairs_copy: with the step's colliding pairs final (after the narrow phase),
 // copy them out on a branch that runs beside the contact kernels.
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s,
-                 const CopyOutParams* pairs_copy = nullptr) {
+                 const CopyOutParams* pairs_copy) {
     c->last_n = n;
     unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
     const uint32_t trace_ns = c->trace_ns ? c->trace_ns : 1000u;
@@ -699,7 +500,9 @@ void mat_inverse(const float* M, float* R) {
         for (int r = 0; r < 4; ++r) R[4 * col + r] = b[r][col];
 }
 
-}  // namespace
+}  // namespace cg_host
+
+using namespace cg_host;
 
 extern "C" {
 
@@ -1001,305 +804,6 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
     return CG_OK;
 }
 
-namespace {
-inline uint32_t bits_of(float f) {
-    uint32_t u;
-    std::memcpy(&u, &f, 4);
-    return u;
-}
-}  // namespace
-
-int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* tree_ids) {
-    if (!c || (n && (!meshes || !tree_ids))) return CG_ERR_INVALID_ARGUMENT;
-    if (n == 0) return CG_OK;
-    std::vector<uint64_t> base(n + 1, 0), vbase(n + 1, 0);
-    bool any_normals = false;
-    for (uint32_t i = 0; i < n; ++i) {
-        const cg_mesh_view& m = meshes[i];
-        if (m.n_triangles && (!m.positions || !m.indices))
-            return fail(c, CG_ERR_INVALID_ARGUMENT, "mesh %u has null positions or indices", i);
-        for (uint64_t k = 0; k < 3ull * m.n_triangles; ++k)
-            if (m.indices[k] >= m.n_vertices)
-                return fail(c, CG_ERR_BAD_TREE, "mesh %u index %llu is vertex %u of %u", i, (unsigned long long)k,
-                            m.indices[k], m.n_vertices);
-        any_normals |= m.normals != nullptr && m.n_triangles;
-        base[i + 1] = base[i] + m.n_triangles;
-        vbase[i + 1] = vbase[i] + (m.n_triangles ? m.n_vertices : 0u);
-    }
-    const uint64_t total = base[n], nv = vbase[n];
-    if (total > 0x3fffffffull || nv > 0xffffffffull)
-        return fail(c, CG_ERR_INVALID_ARGUMENT, "%llu triangles in one build", (unsigned long long)total);
-    const uint64_t T = std::max<uint64_t>(total, 1);
-    const uint32_t cap = uint32_t(2 * total + n);
-    // the scratch: carved in 256-byte steps
-    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
-    size_t off = 0;
-    auto take = [&](size_t bytes) {
-        const size_t o = off;
-        off += up(bytes);
-        return o;
-    };
-    const size_t oP = take(sizeof(float) * 9 * T), oPp = take(sizeof(float) * 9 * T);
-    const size_t oCN = take(any_normals ? sizeof(float) * 9 * T : 0);
-    const size_t oPerm = take(4 * T), oScr = take(4 * T), oOwn = take(4 * T);
-    const size_t oD = take(sizeof(double) * 9 * T), oTm = take(sizeof(double) * 18 * T);
-    const size_t oMom = take(sizeof(double) * 9 * std::max<uint64_t>(T, n));  // a level: one node per triangle, or the roots
-    const size_t oNodes = take(sizeof(BuildNode) * cap), oFlat = take(sizeof(BuildFlat) * cap), oCtr = take(8);
-    const size_t oV = take(sizeof(float) * 3 * std::max<uint64_t>(nv, 1));
-    const size_t oNV = take(any_normals ? sizeof(float) * 3 * std::max<uint64_t>(nv, 1) : 0);
-    const size_t oIdx = take(sizeof(uint32_t) * 3 * T), oMesh = take(sizeof(BuildMesh) * n);
-    const size_t oEmit = take(sizeof(BuildEmit) * n);
-    cudaSetDevice(c->device);
-    cudaStream_t s = c->stream;
-    if (off > c->build_cap) {
-        CG_CUDA(cudaStreamSynchronize(s), "build scratch");
-        cudaFree(c->build);
-        c->build = nullptr;
-        c->build_cap = 0;
-        CG_CUDA(cudaMalloc(&c->build, off), "alloc build scratch");
-        c->build_cap = off;
-    }
-    char* mem = static_cast<char*>(c->build);
-    BuildParams bp{};
-    BuildInput in{};
-    in.P = reinterpret_cast<float*>(mem + oP);
-    in.corner_normals = any_normals ? reinterpret_cast<float*>(mem + oCN) : nullptr;
-    bp.P = in.P;
-    bp.Pp = reinterpret_cast<float*>(mem + oPp);
-    bp.perm = reinterpret_cast<uint32_t*>(mem + oPerm);
-    bp.scratch = reinterpret_cast<uint32_t*>(mem + oScr);
-    bp.own = reinterpret_cast<uint32_t*>(mem + oOwn);
-    bp.D = reinterpret_cast<double*>(mem + oD);
-    bp.Tm = reinterpret_cast<double*>(mem + oTm);
-    bp.mom = reinterpret_cast<double*>(mem + oMom);
-    bp.nodes = reinterpret_cast<BuildNode*>(mem + oNodes);
-    BuildFlat* flat = reinterpret_cast<BuildFlat*>(mem + oFlat);
-    bp.node_ctr = reinterpret_cast<uint32_t*>(mem + oCtr);
-    bp.error = bp.node_ctr + 1;
-    bp.node_cap = cap;
-    bp.T = uint32_t(total);
-    float* d_V = reinterpret_cast<float*>(mem + oV);
-    float* d_NV = any_normals ? reinterpret_cast<float*>(mem + oNV) : nullptr;
-    uint32_t* d_idx = reinterpret_cast<uint32_t*>(mem + oIdx);
-    BuildMesh* d_mesh = reinterpret_cast<BuildMesh*>(mem + oMesh);
-    BuildEmit* d_emit = reinterpret_cast<BuildEmit*>(mem + oEmit);
-    in.meshes = d_mesh;
-    in.vertices = d_V;
-    in.normals = d_NV;
-    in.indices = d_idx;
-    // the meshes' buffers, one after another
-    std::vector<BuildMesh> mt(n);
-    std::vector<BuildNode> roots(n);
-    std::vector<uint32_t> own(T, 0u);
-    for (uint32_t i = 0; i < n; ++i) {
-        const cg_mesh_view& m = meshes[i];
-        mt[i] = BuildMesh{uint32_t(vbase[i]), (m.normals && m.n_triangles) ? 1u : 0u};
-        roots[i] = BuildNode{};
-        roots[i].begin = uint32_t(base[i]);
-        roots[i].count = m.n_triangles;
-        roots[i].kid = kNoKid;
-        roots[i].tree = i;
-        std::fill(own.begin() + long(base[i]), own.begin() + long(base[i + 1]), i);
-        if (!m.n_triangles) continue;
-        CG_CUDA(cudaMemcpyAsync(d_V + 3 * vbase[i], m.positions, sizeof(float) * 3 * m.n_vertices,
-                                cudaMemcpyHostToDevice, s),
-                "upload vertices");
-        if (m.normals)
-            CG_CUDA(cudaMemcpyAsync(d_NV + 3 * vbase[i], m.normals, sizeof(float) * 3 * m.n_vertices,
-                                    cudaMemcpyHostToDevice, s),
-                    "upload normals");
-        CG_CUDA(cudaMemcpyAsync(d_idx + 3 * base[i], m.indices, sizeof(uint32_t) * 3 * m.n_triangles,
-                                cudaMemcpyHostToDevice, s),
-                "upload indices");
-    }
-    const uint32_t ctr0[2] = {n, 0u};
-    CG_CUDA(cudaMemcpyAsync(d_mesh, mt.data(), sizeof(BuildMesh) * n, cudaMemcpyHostToDevice, s), "upload meshes");
-    CG_CUDA(cudaMemcpyAsync(bp.own, own.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, s), "upload owners");
-    CG_CUDA(cudaMemcpyAsync(bp.nodes, roots.data(), sizeof(BuildNode) * n, cudaMemcpyHostToDevice, s), "upload roots");
-    CG_CUDA(cudaMemcpyAsync(bp.node_ctr, ctr0, sizeof(ctr0), cudaMemcpyHostToDevice, s), "upload counter");
-    const uint32_t sms = uint32_t(c->sm_count);
-    CG_CUDA(launch_build_gather(bp, in, sms, s), "gather kernel");
-    // one level per round of launches; the splits' children are the next level
-    std::vector<std::pair<uint32_t, uint32_t>> levels;
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        bp.lo = lo;
-        bp.hi = hi;
-        levels.emplace_back(lo, hi);
-        CG_CUDA(launch_build_level(bp, sms, s), "build level kernels");
-        uint32_t ctr[2];
-        CG_CUDA(cudaMemcpyAsync(ctr, bp.node_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read node count");
-        CG_CUDA(cudaStreamSynchronize(s), "build level");
-        if (ctr[1]) return fail(c, CG_ERR_OUT_OF_MEMORY, "tree build ran out of node slots");
-        lo = hi;
-        hi = std::min(ctr[0], cap);
-    }
-    const uint32_t n_nodes = hi;
-    // the pre-order layout: subtree sizes bottom-up, places top-down
-    for (size_t l = levels.size(); l-- > 0;) {
-        bp.lo = levels[l].first;
-        bp.hi = levels[l].second;
-        CG_CUDA(launch_build_inner(bp, flat, sms, s), "layout kernel");
-    }
-    for (const auto& lv : levels) {
-        bp.lo = lv.first;
-        bp.hi = lv.second;
-        CG_CUDA(launch_build_order(bp, flat, n, sms, s), "layout kernel");
-    }
-    std::vector<BuildFlat> rootflat(n);
-    CG_CUDA(cudaMemcpyAsync(rootflat.data(), flat, sizeof(BuildFlat) * n, cudaMemcpyDeviceToHost, s), "read layout");
-    CG_CUDA(cudaStreamSynchronize(s), "tree layout");
-    // arena places and the trees' side arrays (one block for the batch)
-    struct Place {
-        uint64_t rpair, n_recs, tb, n_tris, nrm, ranges, topo;
-        uint32_t n_leaves;
-    };
-    std::vector<Place> pl(n);
-    size_t aux = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        const uint64_t N = rootflat[i].inner, Ti = meshes[i].n_triangles;
-        Place& p = pl[i];
-        p.n_recs = 2 * N + 2;
-        p.n_tris = std::max<uint64_t>(Ti, 1);
-        p.n_leaves = uint32_t(N + 1);
-        p.nrm = mt[i].has_normals ? aux : ~0ull;
-        if (mt[i].has_normals) aux += up(sizeof(float) * 9 * Ti);
-        p.ranges = aux;
-        aux += up(sizeof(uint2) * p.n_recs);
-        p.topo = aux;
-        aux += up(sizeof(uint32_t) * (p.n_recs + p.n_leaves));
-    }
-    void* block = nullptr;
-    CG_CUDA(cudaMalloc(&block, aux), "alloc tree side arrays");
-    std::shared_ptr<void> pool(block, [](void* q) { cudaFree(q); });
-    uint32_t done = 0;
-    auto undo = [&]() {
-        for (uint32_t j = 0; j < done; ++j) {
-            c->recs.release(pl[j].rpair, pl[j].n_recs / 2);
-            c->tris.release(pl[j].tb, pl[j].n_tris);
-        }
-    };
-    for (; done < n; ++done) {
-        Place& p = pl[done];
-        cudaError_t e = c->recs.alloc(p.n_recs / 2, &p.rpair, s);
-        if (e != cudaSuccess) {
-            undo();
-            return cuda_fail(c, e, "record arena");
-        }
-        e = c->tris.alloc(p.n_tris, &p.tb, s);
-        if (e != cudaSuccess) {
-            c->recs.release(p.rpair, p.n_recs / 2);
-            undo();
-            return cuda_fail(c, e, "triangle arena");
-        }
-        if (2 * p.rpair + p.n_recs > 0xffffffffull || p.tb + p.n_tris > 0x7fffffffull) {
-            c->recs.release(p.rpair, p.n_recs / 2);
-            c->tris.release(p.tb, p.n_tris);
-            undo();
-            return fail(c, CG_ERR_OUT_OF_MEMORY, "arena index space exhausted");
-        }
-    }
-    char* ab = static_cast<char*>(block);
-    std::vector<BuildEmit> em(n);
-    for (uint32_t i = 0; i < n; ++i) {
-        const Place& p = pl[i];
-        em[i] = BuildEmit{uint32_t(2 * p.rpair), uint32_t(p.tb), uint32_t(p.n_recs), 0u,
-                          p.nrm == ~0ull ? nullptr : reinterpret_cast<float*>(ab + p.nrm),
-                          reinterpret_cast<uint2*>(ab + p.ranges), reinterpret_cast<uint32_t*>(ab + p.topo)};
-    }
-    // from here on a failure gives the arena places back
-    cudaError_t e = cudaMemcpyAsync(d_emit, em.data(), sizeof(BuildEmit) * n, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = launch_build_emit(bp, in, flat, d_emit, c->recs.ptr, c->tris.ptr, n_nodes, n, sms, s);
-    for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) e = launch_surfaces(c->recs.ptr, em[i].rec_base, em[i].n_recs, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        undo();
-        return cuda_fail(c, e, "tree layout kernels");
-    }
-    for (uint32_t i = 0; i < n; ++i) {
-        cg_ctx::Slot slot;
-        slot.rec_base = em[i].rec_base;
-        slot.n_recs = pl[i].n_recs;
-        slot.tri_base = pl[i].tb;
-        slot.n_tris = pl[i].n_tris;
-        slot.n_tri_used = meshes[i].n_triangles;
-        slot.nrm = em[i].nrm;
-        slot.ranges = em[i].ranges;
-        slot.topo = em[i].topo;
-        slot.n_leaves = pl[i].n_leaves;
-        slot.pool = pool;
-        slot.live = true;
-        uint32_t id = uint32_t(c->trees.size());
-        for (uint32_t k = 0; k < c->trees.size(); ++k)
-            if (!c->trees[k].live) {
-                id = k;
-                break;
-            }
-        if (id == c->trees.size())
-            c->trees.push_back(slot);
-        else
-            c->trees[id] = slot;
-        tree_ids[i] = id;
-    }
-    return sync_tree_table(c);
-}
-
-int cg_tree_info(cg_ctx* c, uint32_t id, uint32_t* node_count, uint32_t* triangle_count, uint32_t* has_normals) {
-    if (!c) return CG_ERR_INVALID_ARGUMENT;
-    if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
-    const auto& t = c->trees[id];
-    if (node_count) *node_count = uint32_t((t.n_recs - 2) / 2);
-    if (triangle_count) *triangle_count = t.n_tri_used;
-    if (has_normals) *has_normals = t.nrm ? 1u : 0u;
-    return CG_OK;
-}
-
-int cg_tree_export(cg_ctx* c, uint32_t id, cg_obb* root, cg_obb* node_obbs, uint32_t* node_ref,
-                   uint32_t* node_tri_count, float* triangles_position, float* triangles_normal,
-                   uint32_t* triangles_indices) {
-    if (!c) return CG_ERR_INVALID_ARGUMENT;
-    if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
-    const auto& t = c->trees[id];
-    const uint32_t N = uint32_t((t.n_recs - 2) / 2), T = t.n_tri_used;
-    cudaSetDevice(c->device);
-    CG_CUDA(cudaStreamSynchronize(c->stream), "export tree");
-    std::vector<float4> recs(4ull * t.n_recs);
-    CG_CUDA(cudaMemcpy(recs.data(), c->recs.ptr + 4 * t.rec_base, sizeof(float4) * recs.size(), cudaMemcpyDeviceToHost),
-            "read records");
-    auto unbox = [](const float4* r, cg_obb* b) {
-        b->center[0] = r[0].x, b->center[1] = r[0].y, b->center[2] = r[0].z;
-        b->u[0] = r[0].w, b->u[1] = r[1].x, b->u[2] = r[1].y;
-        b->v[0] = r[1].z, b->v[1] = r[1].w, b->v[2] = r[2].x;
-        b->w[0] = r[2].y, b->w[1] = r[2].z, b->w[2] = r[2].w;
-    };
-    if (root) unbox(&recs[4], root);
-    for (uint32_t r = 2; r < t.n_recs; ++r) {
-        const float4* q = &recs[4ull * r];
-        if (node_obbs) unbox(q, node_obbs + (r - 2));
-        const uint32_t ref = bits_of(q[3].x), meta = bits_of(q[3].y);
-        const bool leaf = (meta & kLeafFlag) != 0u;
-        if (node_ref) node_ref[r - 2] = leaf ? uint32_t(ref - t.tri_base) : uint32_t((ref - t.rec_base - 2) / 2);
-        if (node_tri_count) node_tri_count[r - 2] = leaf ? (meta & 0xffffu) : 0u;
-    }
-    if (T && (triangles_position || triangles_indices)) {
-        std::vector<float4> tris(3ull * T);
-        CG_CUDA(cudaMemcpy(tris.data(), c->tris.ptr + 3 * t.tri_base, sizeof(float4) * tris.size(),
-                           cudaMemcpyDeviceToHost),
-                "read triangles");
-        for (size_t k = 0; k < tris.size(); ++k) {
-            if (triangles_position) {
-                triangles_position[3 * k] = tris[k].x;
-                triangles_position[3 * k + 1] = tris[k].y;
-                triangles_position[3 * k + 2] = tris[k].z;
-            }
-            if (triangles_indices) triangles_indices[k] = bits_of(tris[k].w);
-        }
-    }
-    if (T && triangles_normal && t.nrm)
-        CG_CUDA(cudaMemcpy(triangles_normal, t.nrm, sizeof(float) * 9ull * T, cudaMemcpyDeviceToHost), "read normals");
-    return CG_OK;
-}
-
 int cg_tree_free(cg_ctx* c, uint32_t id) {
     if (!c) return CG_ERR_INVALID_ARGUMENT;
     if (id >= c->trees.size() || !c->trees[id].live) return fail(c, CG_ERR_NOT_FOUND, "tree %u", id);
@@ -1588,107 +1092,6 @@ int cg_tree_download(cg_ctx* c, uint32_t id, cg_obb* root, cg_obb* node_obbs, ui
     return CG_OK;
 }
 
-namespace {
-constexpr char kCacheMagic[8] = {'C', 'G', 'T', 'R', 'E', 'E', '0', '1'};
-
-uint64_t fnv1a(const unsigned char* p, size_t n, uint64_t h = 1469598103934665603ull) {
-    for (size_t i = 0; i < n; ++i) {
-        h ^= p[i];
-        h *= 1099511628211ull;
-    }
-    return h;
-}
-}  // namespace
-
-int cg_tree_save(cg_ctx* c, uint32_t id, const char* path) {
-    if (!c || !path) return CG_ERR_INVALID_ARGUMENT;
-    uint32_t N = 0, T = 0, has_nrm = 0;
-    int rc = cg_tree_info(c, id, &N, &T, &has_nrm);
-    if (rc != CG_OK) return rc;
-    cg_obb root;
-    std::vector<cg_obb> obbs(2ull * N);
-    std::vector<uint32_t> ref(2ull * N), cnt(2ull * N), idx(3ull * T);
-    std::vector<float> pos(9ull * T), nrm(has_nrm ? 9ull * T : 0);
-    rc = cg_tree_export(c, id, &root, obbs.data(), ref.data(), cnt.data(), pos.data(), has_nrm ? nrm.data() : nullptr,
-                        idx.data());
-    if (rc != CG_OK) return rc;
-    std::vector<unsigned char> buf;
-    auto put = [&](const void* p, size_t n) {
-        const unsigned char* b = static_cast<const unsigned char*>(p);
-        buf.insert(buf.end(), b, b + n);
-    };
-    const uint32_t head[3] = {N, T, has_nrm ? 1u : 0u};
-    put(kCacheMagic, 8);
-    put(head, sizeof(head));
-    put(&root, sizeof(root));
-    put(obbs.data(), sizeof(cg_obb) * obbs.size());
-    put(ref.data(), 4 * ref.size());
-    put(cnt.data(), 4 * cnt.size());
-    put(pos.data(), 4 * pos.size());
-    put(nrm.data(), 4 * nrm.size());
-    put(idx.data(), 4 * idx.size());
-    const uint64_t h = fnv1a(buf.data(), buf.size());
-    put(&h, 8);
-    FILE* f = std::fopen(path, "wb");
-    if (!f) return fail(c, CG_ERR_INVALID_ARGUMENT, "cannot write %s", path);
-    const size_t w = std::fwrite(buf.data(), 1, buf.size(), f);
-    const int closed = std::fclose(f);
-    if (w != buf.size() || closed != 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "short write to %s", path);
-    return CG_OK;
-}
-
-int cg_tree_load(cg_ctx* c, const char* path, uint32_t* tree_id) {
-    if (!c || !path || !tree_id) return CG_ERR_INVALID_ARGUMENT;
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return fail(c, CG_ERR_NOT_FOUND, "cannot read %s", path);
-    std::vector<unsigned char> buf;
-    unsigned char chunk[1 << 16];
-    size_t got;
-    while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
-    std::fclose(f);
-    const size_t fixed = 8 + 12 + sizeof(cg_obb) + 8;
-    if (buf.size() < fixed || std::memcmp(buf.data(), kCacheMagic, 8) != 0)
-        return fail(c, CG_ERR_BAD_TREE, "%s is not a tree cache file", path);
-    uint32_t head[3];
-    std::memcpy(head, buf.data() + 8, sizeof(head));
-    const uint64_t N = head[0], T = head[1];
-    const bool has_nrm = (head[2] & 1u) != 0;
-    const uint64_t need = fixed + N * (2 * sizeof(cg_obb) + 16) + T * (36 + (has_nrm ? 36 : 0) + 12);
-    if (buf.size() != need) return fail(c, CG_ERR_BAD_TREE, "%s: %zu bytes, its header says %llu", path, buf.size(),
-                                        (unsigned long long)need);
-    uint64_t h;
-    std::memcpy(&h, buf.data() + need - 8, 8);
-    if (h != fnv1a(buf.data(), need - 8)) return fail(c, CG_ERR_BAD_TREE, "%s: checksum mismatch", path);
-    const unsigned char* p = buf.data() + 20;
-    cg_obb root;
-    std::memcpy(&root, p, sizeof(root));
-    p += sizeof(root);
-    std::vector<cg_obb> obbs(2 * N);
-    std::vector<uint32_t> ref(2 * N), cnt(2 * N), idx(3 * T);
-    std::vector<float> pos(9 * T), nrm(has_nrm ? 9 * T : 0);
-    auto get = [&](void* d, size_t n) {
-        if (n) std::memcpy(d, p, n);
-        p += n;
-    };
-    get(obbs.data(), sizeof(cg_obb) * obbs.size());
-    get(ref.data(), 4 * ref.size());
-    get(cnt.data(), 4 * cnt.size());
-    get(pos.data(), 4 * pos.size());
-    get(nrm.data(), 4 * nrm.size());
-    get(idx.data(), 4 * idx.size());
-    cg_tree_view v{};
-    v.root_obb = root;
-    v.node_count = uint32_t(N);
-    v.node_obbs = obbs.data();
-    v.node_ref = ref.data();
-    v.node_tri_count = cnt.data();
-    v.triangle_count = uint32_t(T);
-    v.triangles_position = pos.data();
-    v.triangles_normal = has_nrm ? nrm.data() : nullptr;
-    v.triangles_indices = idx.data();
-    return cg_tree_upload(c, &v, tree_id);
-}
-
 int cg_tree_refit_batch(cg_ctx* c, const uint32_t* tree_ids, const float* const* positions,
                         const uint32_t* n_positions, uint32_t n, void* stream) {
     if (!c || (n && (!tree_ids || !positions || !n_positions))) return CG_ERR_INVALID_ARGUMENT;
@@ -1886,362 +1289,6 @@ int cg_energy_backward(cg_ctx* c, const double* d_grad_energy, const cg_energy_s
     p.max_joints = max_joints;
     p.max_targets = max_targets;
     CG_CUDA(launch_energy_backward(p, c->energy_blocks, max_vertices, s), "energy adjoint kernels");
-    return CG_OK;
-}
-
-int cg_broad_phase(cg_ctx* c, const uint32_t* tree_ids, const float* globals, const uint8_t* callback, uint32_t n,
-                   const float* axes, cg_entity_pair* pairs, uint64_t cap, uint64_t* n_pairs) {
-    if (!c || !n_pairs || (n && (!tree_ids || !globals)) || (cap && !pairs)) return CG_ERR_INVALID_ARGUMENT;
-    *n_pairs = 0;
-    for (uint32_t i = 0; i < n; ++i)
-        if (tree_ids[i] >= c->trees.size() || !c->trees[tree_ids[i]].live)
-            return fail(c, CG_ERR_NOT_FOUND, "entity %u names tree %u", i, tree_ids[i]);
-    if (n < 2) return CG_OK;
-    float ax[9];
-    if (axes)
-        std::memcpy(ax, axes, sizeof(ax));
-    else
-        engine_axes(ax);
-    cudaSetDevice(c->device);
-    cudaStream_t s = c->stream;
-    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
-    const uint64_t pair_cap = std::max<uint64_t>(cap, 1);
-    const size_t b_id = up(sizeof(uint32_t) * n), b_g = up(sizeof(float) * 16 * n), b_cb = up(n),
-                 b_p = up(sizeof(float) * 6 * n), b_out = up(sizeof(uint2) * pair_cap), b_cnt = 256;
-    const size_t need = b_id + b_g + b_cb + b_p + b_out + b_cnt;
-    if (need > c->broad_cap) {
-        CG_CUDA(cudaStreamSynchronize(s), "broad-phase buffers");
-        cudaFree(c->broad);
-        c->broad = nullptr;
-        c->broad_cap = 0;
-        CG_CUDA(cudaMalloc(&c->broad, need), "alloc broad-phase buffers");
-        c->broad_cap = need;
-    }
-    char* base = static_cast<char*>(c->broad);
-    BroadParams p{};
-    uint32_t* d_ids = reinterpret_cast<uint32_t*>(base);
-    float* d_g = reinterpret_cast<float*>(base + b_id);
-    uint8_t* d_cb = reinterpret_cast<uint8_t*>(base + b_id + b_g);
-    p.proj = reinterpret_cast<float*>(base + b_id + b_g + b_cb);
-    p.pairs = reinterpret_cast<uint2*>(base + b_id + b_g + b_cb + b_p);
-    p.count = reinterpret_cast<unsigned long long*>(base + b_id + b_g + b_cb + b_p + b_out);
-    CG_CUDA(cudaMemcpyAsync(d_ids, tree_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s), "upload ids");
-    CG_CUDA(cudaMemcpyAsync(d_g, globals, sizeof(float) * 16 * n, cudaMemcpyHostToDevice, s), "upload matrices");
-    if (callback) CG_CUDA(cudaMemcpyAsync(d_cb, callback, n, cudaMemcpyHostToDevice, s), "upload callbacks");
-    CG_CUDA(cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s), "clear count");
-    p.tree_ids = d_ids;
-    p.trees = c->d_trees;
-    p.recs = c->recs.ptr;
-    p.globals = d_g;
-    p.callback = callback ? d_cb : nullptr;
-    p.n = n;
-    for (int k = 0; k < 3; ++k) p.axes[k] = make_float3(ax[3 * k], ax[3 * k + 1], ax[3 * k + 2]);
-    p.cap = cap;
-    CG_CUDA(launch_broad(p, s), "broad-phase kernels");
-    unsigned long long cnt = 0;
-    CG_CUDA(cudaMemcpyAsync(&cnt, p.count, sizeof(cnt), cudaMemcpyDeviceToHost, s), "read count");
-    CG_CUDA(cudaStreamSynchronize(s), "broad phase");
-    *n_pairs = cnt;
-    const uint64_t m = std::min<uint64_t>(cnt, cap);
-    if (m) CG_CUDA(cudaMemcpy(pairs, p.pairs, sizeof(uint2) * m, cudaMemcpyDeviceToHost), "read pairs");
-    return cnt > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
-}
-
-int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, const cg_shoot_params* params,
-                       cg_frame_result* results, uint64_t cap, uint64_t* n_results) {
-    if (!c || !n_results || (n && !entities) || (cap && !results)) return CG_ERR_INVALID_ARGUMENT;
-    *n_results = 0;
-    if (!c->cfg.max_contacts || !c->cfg.max_tri_pairs)
-        return fail(c, CG_ERR_INVALID_ARGUMENT, "a collision frame needs max_contacts and max_tri_pairs > 0");
-    for (uint32_t i = 0; i < n; ++i)
-        if (entities[i].tree >= c->trees.size() || !c->trees[entities[i].tree].live)
-            return fail(c, CG_ERR_NOT_FOUND, "entity %u names tree %u", i, entities[i].tree);
-    if (n < 2) return CG_OK;  // CollisionDetection.cpp:40
-    cg_shoot_params pr;
-    cg_shoot_params_default(&pr);
-    if (params) pr = *params;
-    cudaSetDevice(c->device);
-    cudaStream_t s = c->stream;
-    // broad phase, on the device
-    std::vector<uint32_t> ids(n);
-    std::vector<float> globals(16ull * n);
-    std::vector<uint8_t> cbs(n);
-    for (uint32_t i = 0; i < n; ++i) {
-        ids[i] = entities[i].tree;
-        std::memcpy(globals.data() + 16ull * i, entities[i].current_global, 16 * sizeof(float));
-        cbs[i] = entities[i].should_callback ? 1u : 0u;
-    }
-    const uint32_t max_pairs = c->cfg.max_queries;
-    const uint32_t max_rays = c->ct.max_rays;
-    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
-    const size_t b_ent = up(sizeof(cg_frame_entity) * n), b_id = up(sizeof(uint32_t) * n),
-                 b_g = up(sizeof(float) * 16 * n), b_cb = up(n), b_proj = up(sizeof(float) * 6 * n),
-                 b_pairs = up(sizeof(uint2) * max_pairs), b_cnt = 256, b_c3 = up(3 * sizeof(uint32_t) * 2 * max_pairs),
-                 b_grp = up(sizeof(float) * 6 * max_rays), b_tag = up(sizeof(uint32_t) * max_rays),
-                 b_sq = up(sizeof(ShootQuery) * max_pairs), b_so = up(sizeof(ShootRayOut) * max_rays),
-                 b_dl = up(sizeof(float) * 3 * max_pairs), b_res = up(sizeof(cg_frame_result) * max_pairs);
-    const size_t need = b_ent + b_id + b_g + b_cb + b_proj + b_pairs + b_cnt + b_c3 + b_grp + b_tag + b_sq + b_so +
-                        b_dl + b_res + b_cnt;
-    if (need > c->frame_cap) {
-        CG_CUDA(cudaStreamSynchronize(s), "frame buffers");
-        cudaFree(c->frame);
-        c->frame = nullptr;
-        c->frame_cap = 0;
-        CG_CUDA(cudaMalloc(&c->frame, need), "alloc frame buffers");
-        c->frame_cap = need;
-    }
-    char* p0 = static_cast<char*>(c->frame);
-    auto take = [&](size_t b) {
-        char* r = p0;
-        p0 += b;
-        return r;
-    };
-    cg_frame_entity* d_ent = reinterpret_cast<cg_frame_entity*>(take(b_ent));
-    uint32_t* d_ids = reinterpret_cast<uint32_t*>(take(b_id));
-    float* d_g = reinterpret_cast<float*>(take(b_g));
-    uint8_t* d_cb = reinterpret_cast<uint8_t*>(take(b_cb));
-    float* d_proj = reinterpret_cast<float*>(take(b_proj));
-    uint2* d_pairs = reinterpret_cast<uint2*>(take(b_pairs));
-    unsigned long long* d_npairs = reinterpret_cast<unsigned long long*>(take(b_cnt));
-    uint32_t* d_c3 = reinterpret_cast<uint32_t*>(take(b_c3));
-    float* d_grp = reinterpret_cast<float*>(take(b_grp));
-    uint32_t* d_tag = reinterpret_cast<uint32_t*>(take(b_tag));
-    ShootQuery* d_sq = reinterpret_cast<ShootQuery*>(take(b_sq));
-    ShootRayOut* d_so = reinterpret_cast<ShootRayOut*>(take(b_so));
-    float* d_dl = reinterpret_cast<float*>(take(b_dl));
-    cg_frame_result* d_res = reinterpret_cast<cg_frame_result*>(take(b_res));
-    unsigned long long* d_nres = reinterpret_cast<unsigned long long*>(take(b_cnt));
-    CG_CUDA(cudaMemcpyAsync(d_ent, entities, sizeof(cg_frame_entity) * n, cudaMemcpyHostToDevice, s), "upload entities");
-    CG_CUDA(cudaMemcpyAsync(d_ids, ids.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s), "upload ids");
-    CG_CUDA(cudaMemcpyAsync(d_g, globals.data(), sizeof(float) * 16 * n, cudaMemcpyHostToDevice, s), "upload matrices");
-    CG_CUDA(cudaMemcpyAsync(d_cb, cbs.data(), n, cudaMemcpyHostToDevice, s), "upload callbacks");
-    CG_CUDA(cudaMemsetAsync(d_npairs, 0, sizeof(unsigned long long), s), "clear count");
-    BroadParams bp{};
-    bp.tree_ids = d_ids;
-    bp.trees = c->d_trees;
-    bp.recs = c->recs.ptr;
-    bp.globals = d_g;
-    bp.callback = d_cb;
-    bp.n = n;
-    float ax[9];
-    engine_axes(ax);
-    for (int k = 0; k < 3; ++k) bp.axes[k] = make_float3(ax[3 * k], ax[3 * k + 1], ax[3 * k + 2]);
-    bp.proj = d_proj;
-    bp.pairs = d_pairs;
-    bp.cap = max_pairs;
-    bp.count = d_npairs;
-    CG_CUDA(launch_broad(bp, s), "broad-phase kernels");
-    unsigned long long np = 0;
-    CG_CUDA(cudaMemcpyAsync(&np, d_npairs, sizeof(np), cudaMemcpyDeviceToHost, s), "read pair count");
-    CG_CUDA(cudaStreamSynchronize(s), "broad phase");
-    if (np > max_pairs)
-        return fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu broad-phase pairs > max_queries %u", np, max_pairs);
-    if (np == 0) {
-        c->last_flags = 0;  // no collide step in this frame: nothing to read
-        return CG_OK;
-    }
-    // collide every broad pair with contacts and rays
-    FrameParams fp{};
-    fp.entities = d_ent;
-    fp.pairs = d_pairs;
-    fp.n_pairs = uint32_t(np);
-    fp.max_rays = max_rays;
-    fp.queries = c->d_queries;
-    fp.rays = c->ct.rays;
-    fp.n_rays = &c->d_ctr->n_rays;
-    fp.counts = d_c3;
-    fp.offsets = d_c3 + 2 * max_pairs;
-    fp.cursor = d_c3 + 4 * max_pairs;
-    fp.grouped = d_grp;
-    fp.tags = d_tag;
-    fp.shoot = d_sq;
-    fp.deltas = d_dl;
-    fp.averages = c->ct.averages;
-    fp.results = d_res;
-    fp.results_cap = max_pairs;
-    fp.n_results = d_nres;
-    CG_CUDA(launch_frame_queries(fp, s), "frame query kernel");
-    c->last_flags = CG_CONTACTS;
-    int rc = enqueue_step(c, c->d_queries, uint32_t(np), CG_CONTACTS, s);
-    if (rc != CG_OK) return rc;
-    // rays per pair, shooting, the delta split
-    CG_CUDA(cudaMemsetAsync(fp.counts, 0, sizeof(uint32_t) * 2 * np, s), "clear ray counts");
-    CG_CUDA(cudaMemsetAsync(d_nres, 0, sizeof(unsigned long long), s), "clear result count");
-    CG_CUDA(launch_frame_rays(fp, uint32_t(4 * c->sm_count), s), "frame ray kernels");
-    ShootParams sp{};
-    sp.q = d_sq;
-    sp.n_queries = uint32_t(np);
-    sp.n_rays = max_rays;
-    sp.n_rays_dev = fp.n_rays;
-    sp.trees = c->d_trees;
-    sp.recs = c->recs.ptr;
-    sp.tris = c->tris.ptr;
-    sp.rays = d_grp;
-    sp.ray_query = d_tag;
-    sp.out = d_so;
-    sp.cos_start = std::cos(pr.smoothstep_start);
-    sp.cos_finish = std::cos(pr.smoothstep_finish);
-    sp.bias = pr.distance_bias;
-    sp.deltas = d_dl;
-    unsigned* d_err = reinterpret_cast<unsigned*>(d_npairs);  // the pair count is read: its word is free now
-    CG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s), "clear flag");
-    sp.error = d_err;
-    CG_CUDA(launch_shoot(sp, s), "shoot kernels");
-    CG_CUDA(launch_frame_split(fp, s), "frame split kernel");
-    unsigned long long nres = 0;
-    unsigned err = 0;
-    CG_CUDA(cudaMemcpyAsync(&nres, d_nres, sizeof(nres), cudaMemcpyDeviceToHost, s), "read result count");
-    CG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(err), cudaMemcpyDeviceToHost, s), "read flag");
-    CG_CUDA(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s), "read counters");
-    CG_CUDA(cudaStreamSynchronize(s), "collision frame");
-    cg_stats st{};
-    rc = stats_from(c, *c->h_ctr, &st);
-    if (rc != CG_OK) return rc;
-    if (err) return fail(c, CG_ERR_QUEUE_OVERFLOW, "a tree is deeper than the ray traversal's stack");
-    *n_results = nres;
-    const uint64_t m = std::min<uint64_t>(nres, cap);
-    if (m) CG_CUDA(cudaMemcpy(results, d_res, sizeof(cg_frame_result) * m, cudaMemcpyDeviceToHost), "read results");
-    return nres > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
-}
-
-int cg_frame_callbacks(const cg_frame_result* results, uint64_t n_results, const uint32_t* entity_ids,
-                       uint32_t n_entities, const uint32_t* parent, uint32_t n_ids, cg_frame_callback* out,
-                       uint64_t cap, uint64_t* n_out) {
-    if (!n_out || (n_results && (!results || !entity_ids || !parent)) || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
-    *n_out = 0;
-    // EntitiesHandler::GetEntityAncestors (EntitiesHandler.cpp:186-204): the
-    // chain up to the root (entity 0), reversed
-    auto ancestors = [&](uint32_t e, std::vector<uint32_t>& a) {
-        a.clear();
-        for (;;) {
-            if (e >= n_ids || a.size() > n_ids) return false;  // out of range, or a cycle
-            a.push_back(e);
-            if (e == 0) break;
-            e = parent[e];
-        }
-        std::reverse(a.begin(), a.end());
-        return true;
-    };
-    std::vector<cg_frame_callback> cb;
-    std::vector<uint32_t> fa, sa;
-    for (uint64_t k = 0; k < n_results; ++k) {
-        const cg_frame_result& r = results[k];
-        if (r.first >= n_entities || r.second >= n_entities) return CG_ERR_INVALID_ARGUMENT;
-        const uint32_t f = entity_ids[r.first], s = entity_ids[r.second];
-        if (!ancestors(f, fa) || !ancestors(s, sa)) return CG_ERR_INVALID_ARGUMENT;
-        auto emit = [&](const std::vector<uint32_t>& mine, const std::vector<uint32_t>& other, uint32_t fam,
-                        uint32_t with, const float* d) {
-            for (size_t i = 0; i < mine.size(); ++i)
-                if (i >= other.size() || mine[i] != other[i])
-                    cb.push_back(cg_frame_callback{mine[i], fam, with, {d[0], d[1], d[2]}});
-        };
-        emit(fa, sa, f, s, r.first_delta);   // CollisionDetection.cpp:109-116
-        emit(sa, fa, s, f, r.second_delta);  // :118-124
-    }
-    std::stable_sort(cb.begin(), cb.end(),
-                     [](const cg_frame_callback& a, const cg_frame_callback& b) { return a.receiver < b.receiver; });
-    *n_out = cb.size();
-    const uint64_t m = std::min<uint64_t>(cb.size(), cap);
-    if (m) std::memcpy(out, cb.data(), sizeof(cg_frame_callback) * m);
-    return cb.size() > cap ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
-}
-
-void cg_shoot_params_default(cg_shoot_params* p) {
-    if (!p) return;
-    const float deg = 0.01745329251994329576923690768489f;  // glm::radians
-    p->smoothstep_start = 40.f * deg;
-    p->smoothstep_finish = 65.f * deg;
-    p->distance_bias = 1.01f;
-}
-
-int cg_shoot_rays(cg_ctx* c, const cg_shoot_query* queries, uint32_t n, const float* rays, uint64_t n_rays,
-                  const cg_shoot_params* params, float* deltas) {
-    if (!c || (n && (!queries || !deltas)) || (n_rays && !rays)) return CG_ERR_INVALID_ARGUMENT;
-    if (n_rays > 0x7fffffffull) return fail(c, CG_ERR_INVALID_ARGUMENT, "more than 2^31 rays");
-    if (n > 0x7fffffffu) return fail(c, CG_ERR_INVALID_ARGUMENT, "more than 2^31 queries");
-    cg_shoot_params pr;
-    cg_shoot_params_default(&pr);
-    if (params) pr = *params;
-    std::vector<ShootQuery> table(n);
-    std::vector<uint32_t> tags(n_rays);
-    uint64_t next = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        const cg_shoot_query& q = queries[i];
-        if (q.tree_a >= c->trees.size() || !c->trees[q.tree_a].live || q.tree_b >= c->trees.size() ||
-            !c->trees[q.tree_b].live)
-            return fail(c, CG_ERR_NOT_FOUND, "shoot query %u names tree %u / %u", i, q.tree_a, q.tree_b);
-        const uint64_t cnt = uint64_t(q.n_first) + q.n_second;
-        if (next + cnt > n_rays)
-            return fail(c, CG_ERR_INVALID_ARGUMENT, "the queries' ray counts exceed n_rays (%llu)",
-                        (unsigned long long)n_rays);
-        ShootQuery& t = table[i];
-        float inv[16];
-        mat_inverse(q.first_global, inv);
-        mat_mul(inv, q.second_global, t.relative);  // OBBtreesCollision.cpp:15 / ShootUncollideRays.cpp:16-17
-        std::memcpy(t.first_global, q.first_global, sizeof(t.first_global));
-        t.tree_a = q.tree_a;
-        t.tree_b = q.tree_b;
-        t.ray_first = uint32_t(next);
-        t.n_first = q.n_first;
-        t.n_second = q.n_second;
-        t.pad[0] = 1u;
-        t.pad[1] = t.pad[2] = 0u;
-        for (uint64_t k = 0; k < cnt; ++k) tags[next + k] = i | (k >= q.n_first ? 0x80000000u : 0u);
-        next += cnt;
-    }
-    if (next != n_rays)
-        return fail(c, CG_ERR_INVALID_ARGUMENT, "the queries' ray counts (%llu) differ from n_rays (%llu)",
-                    (unsigned long long)next, (unsigned long long)n_rays);
-    if (n == 0) return CG_OK;
-    cudaSetDevice(c->device);
-    cudaStream_t s = c->stream;
-    auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
-    const size_t b_q = up(sizeof(ShootQuery) * n), b_r = up(sizeof(float) * 6 * n_rays), b_t = up(sizeof(uint32_t) * n_rays),
-                 b_o = up(sizeof(ShootRayOut) * n_rays), b_d = up(sizeof(float) * 3 * n), b_e = 256;
-    const size_t need = b_q + b_r + b_t + b_o + b_d + b_e;
-    if (need > c->shoot_cap) {
-        CG_CUDA(cudaStreamSynchronize(s), "shoot buffers");
-        cudaFree(c->shoot);
-        c->shoot = nullptr;
-        c->shoot_cap = 0;
-        CG_CUDA(cudaMalloc(&c->shoot, need), "alloc shoot buffers");
-        c->shoot_cap = need;
-    }
-    char* base = static_cast<char*>(c->shoot);
-    ShootQuery* d_q = reinterpret_cast<ShootQuery*>(base);
-    float* d_rays = reinterpret_cast<float*>(base + b_q);
-    uint32_t* d_tags = reinterpret_cast<uint32_t*>(base + b_q + b_r);
-    ShootRayOut* d_out = reinterpret_cast<ShootRayOut*>(base + b_q + b_r + b_t);
-    float* d_deltas = reinterpret_cast<float*>(base + b_q + b_r + b_t + b_o);
-    unsigned* d_err = reinterpret_cast<unsigned*>(base + b_q + b_r + b_t + b_o + b_d);
-    CG_CUDA(cudaMemcpyAsync(d_q, table.data(), sizeof(ShootQuery) * n, cudaMemcpyHostToDevice, s), "upload queries");
-    if (n_rays) {
-        CG_CUDA(cudaMemcpyAsync(d_rays, rays, sizeof(float) * 6 * n_rays, cudaMemcpyHostToDevice, s), "upload rays");
-        CG_CUDA(cudaMemcpyAsync(d_tags, tags.data(), sizeof(uint32_t) * n_rays, cudaMemcpyHostToDevice, s),
-                "upload ray tags");
-    }
-    CG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s), "clear flag");
-    ShootParams p{};
-    p.q = d_q;
-    p.n_queries = n;
-    p.n_rays = uint32_t(n_rays);
-    p.trees = c->d_trees;
-    p.recs = c->recs.ptr;
-    p.tris = c->tris.ptr;
-    p.rays = d_rays;
-    p.ray_query = d_tags;
-    p.out = d_out;
-    p.cos_start = std::cos(pr.smoothstep_start);  // the constructor's cosines (ShootUncollideRays.cpp:4-11)
-    p.cos_finish = std::cos(pr.smoothstep_finish);
-    p.bias = pr.distance_bias;
-    p.deltas = d_deltas;
-    p.error = d_err;
-    CG_CUDA(launch_shoot(p, s), "shoot kernels");
-    unsigned err = 0;
-    CG_CUDA(cudaMemcpyAsync(deltas, d_deltas, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s), "read deltas");
-    CG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read flag");
-    CG_CUDA(cudaStreamSynchronize(s), "shoot");
-    if (err) return fail(c, CG_ERR_QUEUE_OVERFLOW, "a tree is deeper than the ray traversal's stack");
     return CG_OK;
 }
 
