@@ -89,10 +89,15 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # sampling is live before the timed region starts
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.005)
+            self.rows.clear()
         except Exception:
             self.proc = None
         return self
