@@ -129,7 +129,7 @@ __global__ void build_points_kernel(const BuildParams B) {
 // s + x[0] + x[1] + ... + x[n-1], left to right in FP64. The adds are one
 // dependent chain; the loads are not, so they go in blocks of kChainBlock,
 // the next block in flight while the current one is added.
-constexpr uint32_t kChainBlock = 16;
+constexpr uint32_t kChainBlock = 48;
 __device__ __forceinline__ double chain_sum(const double* x, uint32_t n) {
     double s = 0.0;
     double cur[kChainBlock], nxt[kChainBlock];
