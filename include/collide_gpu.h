@@ -200,6 +200,8 @@ typedef struct cg_stats {
     uint64_t rays;        /* uncollide rays (CG_CONTACTS) */
     int32_t status;       /* CG_OK or the error the launch raised */
     int32_t pad;
+    uint64_t rechecked;      /* plane distances recomputed in FP64 (CG_RECHECK / CG_ROBUST) */
+    uint64_t disagreements;  /* triangle-pair tests where a recomputed distance changed class */
 } cg_stats;
 
 #define CG_KEEP_LEAF_PAIRS 1u /* also write the candidate leaf pairs */
@@ -207,6 +209,22 @@ typedef struct cg_stats {
 #define CG_TRACE 4u           /* record a utilisation timeline (see cg_read_trace) */
 #define CG_MID_ONLY 8u        /* mid phase only: candidate leaf pairs, no triangle tests */
 #define CG_CONTACTS 16u       /* also per-triangle contacts, uncollide rays and their averages */
+/* FP64 recheck of the triangle tests' orientation determinants. The Moller
+ * test (Triangle.cpp:866-1003) classifies the six plane distances
+ * d = n . p + d0 of each pair (FP32, as the reference computes them) as zero
+ * (|d| < 1e-6), positive or negative. A distance whose FP32 magnitude lies
+ * within the filter bound B = 32 u C |e1|_1 |e2|_1 of 0 or of 1e-6 (u = 2^-24;
+ * e1, e2 the plane's triangle edges; C the largest coordinate magnitude of
+ * its first corner and the three tested corners; twice the forward error of
+ * the FP32 value against the exact determinant) is recomputed in FP64 as
+ * det[e1, e2, p - a0] and classified again.
+ * CG_RECHECK: the verdicts stay the reference's; cg_stats.rechecked counts
+ * the recomputed distances and cg_stats.disagreements the tests in which one
+ * changed class. CG_ROBUST: the same, and the test goes on with the FP64
+ * classes (and the FP64 values, rounded to FP32, of the nonzero ones): a
+ * robust verdict that can differ from the reference's on those tests. */
+#define CG_RECHECK 32u
+#define CG_ROBUST 64u
 
 /* Per-triangle contact record, the TriangleCandidateRays of
  * CreateUncollideRays.cpp:14-58 after the merge: bit k of mask set = vertex k
@@ -256,8 +274,14 @@ int cg_read_leaf_pairs(cg_ctx* ctx, cg_leaf_pair* out, uint64_t cap, uint64_t* n
 /* Device pointers to the last launch's results (valid until the next launch). */
 int cg_device_results(cg_ctx* ctx, const cg_tri_pair** pairs, const unsigned long long** pair_count);
 
-/* Results of a launch made with CG_CONTACTS (record order is unspecified;
- * read the averages with cap >= the launch's query count). */
+/* Results of a launch made with CG_CONTACTS. Contacts and rays come grouped by
+ * query, then side (first tree, second tree); within a group in the order the
+ * reference makes them: the iteration order of its per-triangle
+ * std::unordered_map<uint32_t, ...> (CreateUncollideRays.cpp:70-71, 138) as
+ * GCC's libstdc++ lays it out, reproduced from the library's own growth
+ * sizes read on the host. So rays_from_first_to_second of query q is the run
+ * of rays with (query q, side 0), bit for bit and in order. Read the averages
+ * with cap >= the launch's query count. */
 int cg_read_contacts(cg_ctx* ctx, cg_contact* out, uint64_t cap, uint64_t* n);
 int cg_read_rays(cg_ctx* ctx, cg_ray* out, uint64_t cap, uint64_t* n);
 int cg_read_ray_averages(cg_ctx* ctx, cg_ray_average* out, uint64_t cap, uint64_t* n);

@@ -24,6 +24,8 @@ CG_NO_TRI_PAIRS = 2
 CG_TRACE = 4
 CG_MID_ONLY = 8
 CG_CONTACTS = 16
+CG_RECHECK = 32
+CG_ROBUST = 64
 
 # Every function the header declares (checked by the CPU tests).
 EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",
@@ -124,7 +126,8 @@ class cg_static_counts(C.Structure):
 class cg_stats(C.Structure):
     _fields_ = [("node_pairs", C.c_uint64), ("leaf_pairs", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("tri_pairs", C.c_uint64), ("fragile", C.c_uint64), ("donations", C.c_uint64), ("warp_steps", C.c_uint64),
-                ("contacts", C.c_uint64), ("rays", C.c_uint64), ("status", C.c_int32), ("pad", C.c_int32)]
+                ("contacts", C.c_uint64), ("rays", C.c_uint64), ("status", C.c_int32), ("pad", C.c_int32),
+                ("rechecked", C.c_uint64), ("disagreements", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
@@ -453,11 +456,14 @@ class Context:
         return out[:n.value]
 
     def contacts(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
-        """Per-triangle contacts of the last CG_CONTACTS launch (CONTACT_DTYPE, unordered)."""
+        """Per-triangle contacts of the last CG_CONTACTS launch (CONTACT_DTYPE):
+        grouped by query, then side, each group in the order of the
+        reference's per-triangle map."""
         return self._read("cg_read_contacts", CONTACT_DTYPE, out, count)
 
     def rays(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:
-        """Uncollide rays of the last CG_CONTACTS launch (RAY_DTYPE, unordered)."""
+        """Uncollide rays of the last CG_CONTACTS launch (RAY_DTYPE): grouped by
+        query, then side, each group in the reference's order."""
         return self._read("cg_read_rays", RAY_DTYPE, out, count)
 
     def ray_averages(self, out: np.ndarray | None = None, count: int | None = None) -> np.ndarray:

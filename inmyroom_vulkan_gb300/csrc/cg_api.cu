@@ -13,6 +13,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -54,15 +55,11 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_leafs);
     cudaFree(c->d_trace);
     auto& t = c->ct;
-    cudaFree(t.pair_aux);
-    cudaFree(t.table);
-    cudaFree(t.occupied);
-    cudaFree(t.vkeys);
-    cudaFree(t.vocc);
-    cudaFree(t.contacts);
-    cudaFree(t.rays);
-    cudaFree(t.sums);
-    cudaFree(t.averages);
+    for (void* p : {(void*)t.pair_aux, (void*)t.table, (void*)t.occupied, (void*)t.pg_geom, (void*)t.pg_link,
+                    (void*)t.pg_mask, (void*)t.contrib, (void*)t.maps, (void*)t.elems, (void*)t.work, (void*)t.vkeys,
+                    (void*)t.vval, (void*)t.vocc, (void*)t.ctmp, (void*)t.rtmp, (void*)t.contacts, (void*)t.rays,
+                    (void*)t.averages})
+        cudaFree(p);
     t = cg_ctx::Contacts{};
     cudaFreeHost(c->h_queries);
     cudaFreeHost(c->h_ctr);
@@ -211,10 +208,46 @@ int check_config(cg_ctx* c, const cg_config* cfg) {
     if (cfg->queue_capacity < 1024) return fail(c, CG_ERR_INVALID_ARGUMENT, "queue_capacity must be >= 1024");
     if (cfg->wait_limit_ms == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "wait_limit_ms must be > 0");
     if (cfg->max_leaf_pairs >= (1ull << 31)) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_leaf_pairs must be < 2^31");
-    if (cfg->max_contacts > (1ull << 28)) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_contacts must be <= 2^28");
-    if (cfg->max_contacts && (cfg->max_tri_pairs == 0 || cfg->max_tri_pairs >= (1ull << 32)))
-        return fail(c, CG_ERR_INVALID_ARGUMENT, "contacts need 0 < max_tri_pairs < 2^32");
+    if (cfg->max_contacts > (1ull << 22)) return fail(c, CG_ERR_INVALID_ARGUMENT, "max_contacts must be <= 2^22");
+    if (cfg->max_contacts && (cfg->max_tri_pairs == 0 || cfg->max_tri_pairs >= (1ull << 31)))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "contacts need 0 < max_tri_pairs < 2^31");
     return CG_OK;
+}
+
+// The sizes at which std::unordered_map<uint32_t, T> grows, read from the
+// host's own library (the one the engine links): keys are inserted one at a
+// time and every change of bucket_count() is recorded, as (insertion index,
+// new bucket count). The reference's per-triangle maps list their keys in an
+// order that follows from these sizes (cg_contacts.cu). Computed once per
+// process up to the largest size asked for.
+bool growth_schedule(uint32_t max_elems, uint32_t* start, uint32_t* buckets, uint32_t* n) {
+    static std::mutex mu;
+    static std::vector<std::pair<uint32_t, uint32_t>> sched;
+    static uint64_t covered = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (covered <= max_elems) {
+        sched.clear();
+        std::unordered_map<uint32_t, char> m;
+        size_t prev = m.bucket_count();
+        // one growth past max_elems, so that the last entry covers every size up to it
+        uint64_t i = 0;
+        for (;; ++i) {
+            m.emplace(uint32_t(i), 0);
+            if (m.bucket_count() != prev) {
+                prev = m.bucket_count();
+                sched.emplace_back(uint32_t(i), uint32_t(prev));
+                if (i > max_elems) break;
+            }
+        }
+        covered = i;
+    }
+    if (sched.size() > kMaxSchedule) return false;
+    *n = uint32_t(sched.size());
+    for (size_t k = 0; k < sched.size(); ++k) {
+        start[k] = sched[k].first;
+        buckets[k] = sched[k].second;
+    }
+    return true;
 }
 
 int alloc_buffers(cg_ctx* c) {
@@ -232,10 +265,7 @@ int alloc_buffers(cg_ctx* c) {
     int nocc = 0;
     CG_CUDA(narrow_occupancy(8, &nocc), "occupancy");
     c->narrow_blocks = uint32_t(std::max(nocc, 1) * c->sm_count);
-    int aocc = 0, eocc = 0;
-    CG_CUDA(contacts_occupancy(&aocc, &eocc), "occupancy");
-    c->accumulate_blocks = uint32_t(std::max(aocc, 1) * c->sm_count);
-    c->emit_blocks = uint32_t(std::max(eocc, 1) * c->sm_count);
+    c->contact_blocks = uint32_t(8 * c->sm_count);  // 2048 threads per SM of 256-thread blocks
     CG_CUDA(deform_smem_limit(), "deform kernel shared memory");
     c->copy_blocks = uint32_t(4 * c->sm_count);
     int gocc = 0;
@@ -254,28 +284,43 @@ int alloc_buffers(cg_ctx* c) {
     if (g.max_leaf_pairs)
         CG_CUDA(cudaMalloc(&c->d_leafs, sizeof(cg_leaf_pair) * g.max_leaf_pairs), "alloc leaf-pair output");
     if (g.max_contacts) {
-        // Hash tables at most half full: contacts, vertices with a ray (3 per
-        // contact at most).
+        // Hash tables at most half full: contact slots, vertices with a ray
+        // (3 per contact at most).
         auto pow2_at_least = [](uint64_t x) {
             uint64_t p = 1024;
             while (p < x) p <<= 1;
             return uint32_t(p);
         };
         auto& t = c->ct;
-        t.table_slots = pow2_at_least(2 * g.max_contacts);
-        t.vslots = pow2_at_least(6 * g.max_contacts);
-        t.max_rays = uint32_t(3 * g.max_contacts);
-        CG_CUDA(cudaMalloc(&t.pair_aux, sizeof(uint4) * g.max_tri_pairs), "alloc pair side records");
+        const uint64_t mc = g.max_contacts, mp = g.max_tri_pairs, mq = g.max_queries;
+        t.table_slots = pow2_at_least(2 * mc);
+        t.vslots = pow2_at_least(6 * mc);
+        t.max_rays = uint32_t(3 * mc);
+        CG_CUDA(cudaMalloc(&t.pair_aux, sizeof(uint4) * mp), "alloc pair side records");
         CG_CUDA(cudaMalloc(&t.table, sizeof(ContactSlot) * t.table_slots), "alloc contact table");
         CG_CUDA(cudaMalloc(&t.occupied, sizeof(uint32_t) * t.table_slots), "alloc contact list");
+        CG_CUDA(cudaMalloc(&t.pg_geom, sizeof(float4) * mp), "alloc pair geometry");
+        CG_CUDA(cudaMalloc(&t.pg_link, sizeof(uint4) * mp), "alloc pair links");
+        CG_CUDA(cudaMalloc(&t.pg_mask, sizeof(uint32_t) * mp), "alloc pair masks");
+        CG_CUDA(cudaMalloc(&t.contrib, sizeof(unsigned long long) * 2 * mp), "alloc contributions");
+        CG_CUDA(cudaMalloc(&t.maps, sizeof(uint32_t) * 6 * 2 * mq), "alloc contact maps");
+        CG_CUDA(cudaMemset(t.maps, 0, sizeof(uint32_t) * 6 * 2 * mq), "zero contact maps");
+        CG_CUDA(cudaMalloc(&t.elems, sizeof(ContactElem) * mc), "alloc contact elements");
+        CG_CUDA(cudaMalloc(&t.work, sizeof(uint32_t) * kOrderWords * mc), "alloc contact order memory");
         CG_CUDA(cudaMalloc(&t.vkeys, sizeof(unsigned long long) * t.vslots), "alloc vertex set");
+        CG_CUDA(cudaMalloc(&t.vval, sizeof(uint32_t) * t.vslots), "alloc vertex set");
         CG_CUDA(cudaMalloc(&t.vocc, sizeof(uint32_t) * t.vslots), "alloc vertex list");
-        CG_CUDA(cudaMalloc(&t.contacts, sizeof(cg_contact) * g.max_contacts), "alloc contacts");
+        CG_CUDA(cudaMalloc(&t.ctmp, sizeof(cg_contact) * mc), "alloc contact staging");
+        CG_CUDA(cudaMalloc(&t.rtmp, sizeof(cg_ray) * t.max_rays), "alloc ray staging");
+        CG_CUDA(cudaMalloc(&t.contacts, sizeof(cg_contact) * mc), "alloc contacts");
         CG_CUDA(cudaMalloc(&t.rays, sizeof(cg_ray) * t.max_rays), "alloc rays");
-        CG_CUDA(cudaMalloc(&t.sums, sizeof(double) * 8 * g.max_queries), "alloc ray sums");
-        CG_CUDA(cudaMalloc(&t.averages, sizeof(cg_ray_average) * g.max_queries), "alloc ray averages");
-        CG_CUDA(init_contact_tables(t.table, t.table_slots, t.vkeys, t.vslots, c->stream), "init contact tables");
+        CG_CUDA(cudaMalloc(&t.averages, sizeof(cg_ray_average) * mq), "alloc ray averages");
+        CG_CUDA(init_contact_tables(t.table, t.table_slots, t.vkeys, t.vval, t.vslots, c->stream),
+                "init contact tables");
         CG_CUDA(cudaStreamSynchronize(c->stream), "init contact tables");
+        if (!growth_schedule(uint32_t(mc), c->sched_start, c->sched_buckets, &c->n_sched))
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "the host's unordered_map grows more than %u times up to %llu "
+                        "elements", kMaxSchedule, (unsigned long long)mc);
     }
     CG_CUDA(cudaMallocHost(&c->h_queries, sizeof(cg_query) * g.max_queries), "alloc pinned queries");
     CG_CUDA(cudaMallocHost(&c->h_ctr, sizeof(Counters)), "alloc pinned counters");
@@ -297,7 +342,7 @@ int sync_tree_table(cg_ctx* c) {
     for (uint32_t i = 0; i < n; ++i) {
         const auto& s = c->trees[i];
         host[i] = DevTree{uint32_t(s.rec_base), uint32_t(s.tri_base), uint32_t(s.n_recs), uint32_t(s.n_tris),
-                          s.live ? 1u : 0u, 0u, s.nrm};
+                          s.live ? 1u : 0u, 0u, s.nrm, s.ranges};
     }
     if (n) CG_CUDA(cudaMemcpy(c->d_trees, host.data(), sizeof(DevTree) * n, cudaMemcpyHostToDevice), "upload tree table");
     return CG_OK;
@@ -374,7 +419,9 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         ContactParams cp{};
         cp.q = c->d_packed;
         cp.n_queries = n;
+        cp.n_sched = c->n_sched;
         cp.tris = c->tris.ptr;
+        cp.recs = c->recs.ptr;
         cp.trees = c->d_trees;
         cp.pairs = c->d_pairs;
         cp.pair_aux = t.pair_aux;
@@ -382,18 +429,37 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.pairs_cap = c->cfg.max_tri_pairs;
         cp.table = t.table;
         cp.table_mask = t.table_slots - 1u;
+        cp.max_contacts = uint32_t(c->cfg.max_contacts);
         cp.occupied = t.occupied;
+        cp.pg_geom = t.pg_geom;
+        cp.pg_link = t.pg_link;
+        cp.pg_mask = t.pg_mask;
+        cp.contrib = t.contrib;
+        const size_t mq2 = 2ull * c->cfg.max_queries;
+        cp.map_cnt = t.maps;
+        cp.map_off = t.maps + mq2;
+        cp.map_fill = t.maps + 2 * mq2;
+        cp.map_nr = t.maps + 3 * mq2;
+        cp.map_coff = t.maps + 4 * mq2;
+        cp.map_roff = t.maps + 5 * mq2;
+        cp.elems = t.elems;
+        cp.work = t.work;
         cp.vkeys = t.vkeys;
+        cp.vval = t.vval;
         cp.vtable_mask = t.vslots - 1u;
         cp.vocc = t.vocc;
-        cp.max_contacts = uint32_t(c->cfg.max_contacts);
+        cp.ctmp = t.ctmp;
+        cp.rtmp = t.rtmp;
         cp.contacts = t.contacts;
         cp.rays = t.rays;
         cp.max_rays = t.max_rays;
-        cp.sums = t.sums;
         cp.averages = t.averages;
         cp.ctr = c->d_ctr;
-        CG_CUDA(launch_contacts(cp, c->accumulate_blocks, c->emit_blocks, s), "contact kernels");
+        for (uint32_t k = 0; k < c->n_sched; ++k) {
+            cp.sched_start[k] = c->sched_start[k];
+            cp.sched_buckets[k] = c->sched_buckets[k];
+        }
+        CG_CUDA(launch_contacts(cp, c->contact_blocks, s), "contact kernels");
     }
     if (pairs_copy) CG_CUDA(cudaStreamWaitEvent(s, c->ev_joined, 0), "join");
     return CG_OK;
@@ -408,8 +474,10 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
     s.fragile = k.fragile;
     s.donations = k.donations;
     s.warp_steps = k.warp_steps;
-    s.contacts = k.n_contacts;
+    s.contacts = k.n_elems;
     s.rays = k.n_rays;
+    s.rechecked = k.rechecked;
+    s.disagreements = k.disagreements;
     int status = CG_OK;
     if (k.error & ERR_TIMEOUT)
         status = fail(c, CG_ERR_TIMEOUT, "a device-side wait exceeded %u ms", c->cfg.wait_limit_ms);
@@ -427,9 +495,15 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
         status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu leaf pairs, capacity %llu", (unsigned long long)k.n_leafs,
                       (unsigned long long)c->cfg.max_leaf_pairs);
     else if ((c->last_flags & CG_CONTACTS) &&
-             (k.c_overflow || k.n_contacts > c->cfg.max_contacts || k.n_rays > c->ct.max_rays))
-        status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%u contacts, %u rays (max_contacts %llu, flags %u): raise max_contacts",
-                      k.n_contacts, k.n_rays, (unsigned long long)c->cfg.max_contacts, k.c_overflow);
+             (k.c_overflow || k.n_contacts > c->cfg.max_contacts || k.n_rays > c->ct.max_rays)) {
+        if (k.c_overflow & CONTACT_ORDER)
+            status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "contact order: a leaf pair deeper than 127 splits of the "
+                          "simultaneous descent");
+        else
+            status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%u triangles with colliding pairs, %u rays (max_contacts %llu, "
+                          "flags %u): raise max_contacts", k.n_contacts, k.n_rays,
+                          (unsigned long long)c->cfg.max_contacts, k.c_overflow);
+    }
     s.status = status;
     if (st) *st = s;
     return status;
@@ -987,12 +1061,12 @@ int cg_read_contacts(cg_ctx* c, cg_contact* out, uint64_t cap, uint64_t* n) {
     if (!c || !n || (cap && !out)) return CG_ERR_INVALID_ARGUMENT;
     int rc = contact_counters(c);
     if (rc != CG_OK) return rc;
-    const uint64_t total = c->h_ctr->n_contacts;
+    const uint64_t total = c->h_ctr->n_elems;
     const uint64_t avail = std::min<uint64_t>(total, c->cfg.max_contacts);
     *n = total;
     const uint64_t m = std::min(avail, cap);
     if (m) CG_CUDA(cudaMemcpy(out, c->ct.contacts, sizeof(cg_contact) * m, cudaMemcpyDeviceToHost), "read contacts");
-    return (total > avail || (c->h_ctr->c_overflow & CONTACT_TABLE)) ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
+    return (total > avail || c->h_ctr->c_overflow) ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
 }
 
 int cg_read_rays(cg_ctx* c, cg_ray* out, uint64_t cap, uint64_t* n) {

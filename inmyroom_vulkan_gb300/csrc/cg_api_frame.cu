@@ -102,11 +102,11 @@ int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, c
     auto up = [](size_t x) { return (x + 255u) & ~size_t(255); };
     const size_t b_ent = up(sizeof(cg_frame_entity) * n), b_id = up(sizeof(uint32_t) * n),
                  b_g = up(sizeof(float) * 16 * n), b_cb = up(n), b_proj = up(sizeof(float) * 6 * n),
-                 b_pairs = up(sizeof(uint2) * max_pairs), b_cnt = 256, b_c3 = up(3 * sizeof(uint32_t) * 2 * max_pairs),
+                 b_pairs = up(sizeof(uint2) * max_pairs), b_cnt = 256,
                  b_grp = up(sizeof(float) * 6 * max_rays), b_tag = up(sizeof(uint32_t) * max_rays),
                  b_sq = up(sizeof(ShootQuery) * max_pairs), b_so = up(sizeof(ShootRayOut) * max_rays),
                  b_dl = up(sizeof(float) * 3 * max_pairs), b_res = up(sizeof(cg_frame_result) * max_pairs);
-    const size_t need = b_ent + b_id + b_g + b_cb + b_proj + b_pairs + b_cnt + b_c3 + b_grp + b_tag + b_sq + b_so +
+    const size_t need = b_ent + b_id + b_g + b_cb + b_proj + b_pairs + b_cnt + b_grp + b_tag + b_sq + b_so +
                         b_dl + b_res + b_cnt;
     if (need > c->frame_cap) {
         CG_CUDA(cudaStreamSynchronize(s), "frame buffers");
@@ -129,7 +129,6 @@ int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, c
     float* d_proj = reinterpret_cast<float*>(take(b_proj));
     uint2* d_pairs = reinterpret_cast<uint2*>(take(b_pairs));
     unsigned long long* d_npairs = reinterpret_cast<unsigned long long*>(take(b_cnt));
-    uint32_t* d_c3 = reinterpret_cast<uint32_t*>(take(b_c3));
     float* d_grp = reinterpret_cast<float*>(take(b_grp));
     uint32_t* d_tag = reinterpret_cast<uint32_t*>(take(b_tag));
     ShootQuery* d_sq = reinterpret_cast<ShootQuery*>(take(b_sq));
@@ -175,9 +174,8 @@ int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, c
     fp.queries = c->d_queries;
     fp.rays = c->ct.rays;
     fp.n_rays = &c->d_ctr->n_rays;
-    fp.counts = d_c3;
-    fp.offsets = d_c3 + 2 * max_pairs;
-    fp.cursor = d_c3 + 4 * max_pairs;
+    fp.counts = c->ct.maps + 3 * 2ull * c->cfg.max_queries;   // the contact step's rays per map
+    fp.offsets = c->ct.maps + 5 * 2ull * c->cfg.max_queries;  // and their first ray
     fp.grouped = d_grp;
     fp.tags = d_tag;
     fp.shoot = d_sq;
@@ -191,7 +189,6 @@ int cg_collision_frame(cg_ctx* c, const cg_frame_entity* entities, uint32_t n, c
     int rc = enqueue_step(c, c->d_queries, uint32_t(np), CG_CONTACTS, s);
     if (rc != CG_OK) return rc;
     // rays per pair, shooting, the delta split
-    CG_CUDA(cudaMemsetAsync(fp.counts, 0, sizeof(uint32_t) * 2 * np, s), "clear ray counts");
     CG_CUDA(cudaMemsetAsync(d_nres, 0, sizeof(unsigned long long), s), "clear result count");
     CG_CUDA(launch_frame_rays(fp, uint32_t(4 * c->sm_count), s), "frame ray kernels");
     ShootParams sp{};

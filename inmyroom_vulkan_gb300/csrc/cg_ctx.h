@@ -105,7 +105,7 @@ struct cg_ctx {
     cudaStream_t stream = nullptr;
     uint32_t blocks = 0;         // persistent traversal grid
     uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
-    uint32_t accumulate_blocks = 0, emit_blocks = 0;  // contact kernels: one resident wave
+    uint32_t contact_blocks = 0;                       // contact kernels: one resident wave
     uint32_t energy_blocks = 0;                        // energy kernels: one resident wave
 
     // trees
@@ -145,15 +145,29 @@ struct cg_ctx {
         ContactSlot* table = nullptr;
         uint32_t table_slots = 0;
         uint32_t* occupied = nullptr;
+        float4* pg_geom = nullptr;
+        uint4* pg_link = nullptr;
+        uint32_t* pg_mask = nullptr;
+        unsigned long long* contrib = nullptr;
+        uint32_t* maps = nullptr;  // 6 arrays of 2 max_queries: count, offset, fill, rays, record and ray offsets
+        ContactElem* elems = nullptr;
+        uint32_t* work = nullptr;
         unsigned long long* vkeys = nullptr;
+        uint32_t* vval = nullptr;
         uint32_t vslots = 0;
         uint32_t* vocc = nullptr;
+        cg_contact* ctmp = nullptr;
+        cg_ray* rtmp = nullptr;
         cg_contact* contacts = nullptr;
         cg_ray* rays = nullptr;
         uint32_t max_rays = 0;
-        double* sums = nullptr;
         cg_ray_average* averages = nullptr;
     } ct;
+    // growth sizes of the host's std::unordered_map<uint32_t, T> (the
+    // reference's per-triangle maps), up to max_contacts elements
+    uint32_t n_sched = 0;
+    uint32_t sched_start[kMaxSchedule] = {};
+    uint32_t sched_buckets[kMaxSchedule] = {};
 
     cg_query* h_queries = nullptr;  // pinned
     Counters* h_ctr = nullptr;      // pinned
@@ -230,6 +244,7 @@ void engine_axes(float* ax);
 void drop_graph(cg_ctx* c);
 int check_config(cg_ctx* c, const cg_config* cfg);
 int alloc_buffers(cg_ctx* c);
+bool growth_schedule(uint32_t max_elems, uint32_t* start, uint32_t* buckets, uint32_t* n);
 int sync_tree_table(cg_ctx* c);
 void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta);
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s,

@@ -206,23 +206,103 @@ __device__ __forceinline__ bool interval(float3 x0, float3 x1, float3 x2, float 
 // Outcome of one triangle-pair test.
 enum : int { TT_MISS = 0, TT_HIT = 1, TT_COPLANAR = 2, TT_FRAGILE = 3 };
 
+// ---- FP64 recheck of the orientation determinants ----
+//
+// The six plane distances of the test (du_k of the second triangle's corners
+// to the first's plane, dv_k the other way) are the orientation determinants
+// det[a1 - a0, a2 - a0, p - a0] as the reference computes them in FP32:
+// d = (n . p) + (-(n . a0)) with n = (a1 - a0) x (a2 - a0). The test only
+// looks at each one's class: zero when |d| < 1e-6 (Triangle.cpp:898-915),
+// else its sign. The FP32 value's error against the exact determinant is at
+// most 16 u C |a1 - a0|_1 |a2 - a0|_1 (u = 2^-24, C the largest coordinate
+// magnitude of a0 and the three tested corners: the edges and the cross
+// product round at 4u relative, the two dot products at 3u, the last sum at
+// u). The filter bound is twice that,
+//   B = 32 u C |a1 - a0|_1 |a2 - a0|_1,
+// and a distance whose FP32 magnitude lies within B of 0 or of 1e-6 is
+// uncertain: it is recomputed in FP64 from the same corners (det form, with
+// differences of floats, exact in FP64 for the meshes' coordinate ranges)
+// and classified again. Outside the band the FP32 class is the exact one.
+constexpr float kRecheckU32 = 32.0f * 0x1p-24f;
+
+__device__ __forceinline__ float amax3(float3 p) { return fmaxf(fmaxf(fabsf(p.x), fabsf(p.y)), fabsf(p.z)); }
+__device__ __forceinline__ float norm1(float3 p) { return (fabsf(p.x) + fabsf(p.y)) + fabsf(p.z); }
+
+__device__ __forceinline__ float filter_bound(float3 a0, float3 e1, float3 e2, float3 p0, float3 p1, float3 p2) {
+    const float C = fmaxf(fmaxf(amax3(a0), amax3(p0)), fmaxf(amax3(p1), amax3(p2)));
+    return kRecheckU32 * C * norm1(e1) * norm1(e2);
+}
+__device__ __forceinline__ bool uncertain(float d, float bound) {
+    const float a = fabsf(d);
+    return a < bound || fabsf(a - 1e-6f) < bound;
+}
+__device__ __forceinline__ int class32(float d) { return tiny(d) ? 0 : (d > 0.0f ? 1 : -1); }
+__device__ __forceinline__ int class64(double d) { return fabs(d) < 1e-6 ? 0 : (d > 0.0 ? 1 : -1); }
+__device__ __noinline__ double orient64(float3 a0, float3 a1, float3 a2, float3 p) {
+    const double e1x = double(a1.x) - double(a0.x), e1y = double(a1.y) - double(a0.y), e1z = double(a1.z) - double(a0.z);
+    const double e2x = double(a2.x) - double(a0.x), e2y = double(a2.y) - double(a0.y), e2z = double(a2.z) - double(a0.z);
+    const double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+    return (nx * (double(p.x) - double(a0.x)) + ny * (double(p.y) - double(a0.y))) + nz * (double(p.z) - double(a0.z));
+}
+
+// Recheck state of one test: distances recomputed in FP64, and whether any
+// of them changed class.
+struct Recheck {
+    uint32_t checked = 0;
+    bool disagree = false;
+};
+
+// The zero snap of three distances of one plane (a0, a1, a2 the plane's
+// triangle, p the other's corners, d their FP32 distances). kMode 0: the
+// reference's snap; 1: the same values, uncertain ones rechecked and counted;
+// 2: uncertain ones replaced by the FP64 class (0, or the FP64 value in FP32).
+template <int kMode>
+__device__ __forceinline__ void snap3(float3 a0, float3 a1, float3 a2, float3 e1, float3 e2, const float3 p[3],
+                                      float d[3], Recheck& rc) {
+    bool unc[3] = {false, false, false};
+    if (kMode != 0) {
+        const float B = filter_bound(a0, e1, e2, p[0], p[1], p[2]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) unc[k] = uncertain(d[k], B);
+        if (unc[0] | unc[1] | unc[2]) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (!unc[k]) continue;
+                const double x = orient64(a0, a1, a2, p[k]);
+                const int c = class64(x);
+                ++rc.checked;
+                if (c != class32(d[k])) rc.disagree = true;
+                if (kMode == 2) d[k] = c == 0 ? 0.0f : float(x);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (!(kMode == 2 && unc[k]) && tiny(d[k])) d[k] = 0.0f;
+}
+
 // tri_tri_intersect_with_isectline (Triangle.cpp:866-1003). TT_HIT means
 // doIntersept && !areCoplanar (the pairs CreateUncollideRays.cpp:88 keeps);
 // TT_COPLANAR covers every coplanar outcome (never kept); TT_FRAGILE is the
 // case where the second interval degenerates (U's distances all zero while V's
 // are not), in which the reference reads uninitialised values: it is defined
-// here, as in the oracle, as "not colliding" and counted.
-__device__ __forceinline__ int tri_tri(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float3& src,
-                                       float3& tgt) {
+// here, as in the oracle, as "not colliding" and counted. kMode: the FP64
+// recheck of the plane distances (snap3: 0 off, 1 counted, 2 FP64 verdict).
+template <int kMode>
+__device__ __forceinline__ int tri_tri_mode(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2,
+                                            float3& src, float3& tgt, Recheck& rc) {
     float3 e1 = sub3(V1, V0), e2 = sub3(V2, V0);
     const float3 n1 = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
     const float d1 = -((n1.x * V0.x + n1.y * V0.y) + n1.z * V0.z);
-    float du0 = ((n1.x * U0.x + n1.y * U0.y) + n1.z * U0.z) + d1;
-    float du1 = ((n1.x * U1.x + n1.y * U1.y) + n1.z * U1.z) + d1;
-    float du2 = ((n1.x * U2.x + n1.y * U2.y) + n1.z * U2.z) + d1;
-    if (tiny(du0)) du0 = 0.0f;
-    if (tiny(du1)) du1 = 0.0f;
-    if (tiny(du2)) du2 = 0.0f;
+    float du[3];
+    du[0] = ((n1.x * U0.x + n1.y * U0.y) + n1.z * U0.z) + d1;
+    du[1] = ((n1.x * U1.x + n1.y * U1.y) + n1.z * U1.z) + d1;
+    du[2] = ((n1.x * U2.x + n1.y * U2.y) + n1.z * U2.z) + d1;
+    {
+        const float3 U[3] = {U0, U1, U2};
+        snap3<kMode>(V0, V1, V2, e1, e2, U, du, rc);
+    }
+    const float du0 = du[0], du1 = du[1], du2 = du[2];
     const float du0du1 = du0 * du1;
     const float du0du2 = du0 * du2;
     if (du0du1 > 0.0f && du0du2 > 0.0f) return TT_MISS;
@@ -231,12 +311,15 @@ __device__ __forceinline__ int tri_tri(float3 V0, float3 V1, float3 V2, float3 U
     e2 = sub3(U2, U0);
     const float3 n2 = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
     const float d2 = -((n2.x * U0.x + n2.y * U0.y) + n2.z * U0.z);
-    float dv0 = ((n2.x * V0.x + n2.y * V0.y) + n2.z * V0.z) + d2;
-    float dv1 = ((n2.x * V1.x + n2.y * V1.y) + n2.z * V1.z) + d2;
-    float dv2 = ((n2.x * V2.x + n2.y * V2.y) + n2.z * V2.z) + d2;
-    if (tiny(dv0)) dv0 = 0.0f;
-    if (tiny(dv1)) dv1 = 0.0f;
-    if (tiny(dv2)) dv2 = 0.0f;
+    float dv[3];
+    dv[0] = ((n2.x * V0.x + n2.y * V0.y) + n2.z * V0.z) + d2;
+    dv[1] = ((n2.x * V1.x + n2.y * V1.y) + n2.z * V1.z) + d2;
+    dv[2] = ((n2.x * V2.x + n2.y * V2.y) + n2.z * V2.z) + d2;
+    {
+        const float3 V[3] = {V0, V1, V2};
+        snap3<kMode>(U0, U1, U2, e1, e2, V, dv, rc);
+    }
+    const float dv0 = dv[0], dv1 = dv[1], dv2 = dv[2];
     const float dv0dv1 = dv0 * dv1;
     const float dv0dv2 = dv0 * dv2;
     if (dv0dv1 > 0.0f && dv0dv2 > 0.0f) return TT_MISS;
@@ -292,6 +375,12 @@ __device__ __forceinline__ int tri_tri(float3 V0, float3 V1, float3 V2, float3 U
             tgt = smallest2 == 0 ? pb2 : pb1;
     }
     return TT_HIT;
+}
+
+__device__ __forceinline__ int tri_tri(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float3& src,
+                                       float3& tgt) {
+    Recheck rc;
+    return tri_tri_mode<0>(V0, V1, V2, U0, U1, U2, src, tgt, rc);
 }
 
 }  // namespace cg

@@ -5,16 +5,14 @@
 //   broad phase (cg_broad.cu) -> frame_queries_kernel: one collide query per
 //   broad pair, relative = inverse(first current) * second current
 //   (OBBtreesCollision.cpp:15) -> the collide step with contacts and rays ->
-//   ray_count / ray_offsets / ray_scatter: the rays grouped per pair, first
-//   entity's then second's -> frame_shoot_kernel: the shooting table (pairs
-//   where an entity moved, :80-82) -> the shooting kernels (cg_shoot.cu) ->
+//   ray_pack: the step's rays, which come grouped per pair and side in the
+//   reference's order (its unordered_map's iteration order), into the
+//   shooting's layout -> frame_shoot_kernel: the shooting table (pairs where
+//   an entity moved, :80-82) -> the shooting kernels (cg_shoot.cu) ->
 //   frame_split_kernel: per pair with rays, the delta split by each entity's
 //   movement of its mean ray origin (:84-97), appended to the results.
-// The rays of a pair come out of the contact kernels in no fixed order (the
-// reference's come out of an unordered_map), so the summed force responses
-// can differ from the reference's in the last bits, and so can the origins of
-// the rays that start at a contact's weighted average point; every other step
-// is the reference's arithmetic.
+// Every step is the reference's arithmetic on the reference's rays in the
+// reference's order.
 #include <cuda_runtime.h>
 
 #include "cg_device.cuh"
@@ -60,48 +58,16 @@ __device__ __forceinline__ uint32_t stored_rays(const FrameParams& P) {
     return n < P.max_rays ? n : P.max_rays;
 }
 
-__global__ void ray_count_kernel(const FrameParams P) {
+// The rays, grouped per pair and side by the contact step, as origin +
+// direction and a tag (pair | from the second entity << 31), in place.
+__global__ void ray_pack_kernel(const FrameParams P) {
     const uint32_t n = stored_rays(P);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const cg_ray& r = P.rays[i];
-        atomicAdd(P.counts + 2u * r.query + r.side, 1u);
-    }
-}
-
-// Exclusive prefix sum of the 2 n counts (one block), into offsets and the
-// scatter cursors.
-__global__ void __launch_bounds__(1024) ray_offsets_kernel(const FrameParams P) {
-    __shared__ uint32_t part[1024];
-    const uint32_t m = 2u * P.n_pairs;
-    const uint32_t per = (m + blockDim.x - 1u) / blockDim.x;
-    const uint32_t b0 = threadIdx.x * per, b1 = min(m, b0 + per);
-    uint32_t sum = 0;
-    for (uint32_t i = b0; i < b1; ++i) sum += P.counts[i];
-    part[threadIdx.x] = sum;
-    __syncthreads();
-    for (uint32_t o = 1; o < blockDim.x; o <<= 1) {  // inclusive scan of the parts
-        const uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[threadIdx.x] - sum;
-    for (uint32_t i = b0; i < b1; ++i) {
-        P.offsets[i] = run;
-        P.cursor[i] = run;
-        run += P.counts[i];
-    }
-}
-
-__global__ void ray_scatter_kernel(const FrameParams P) {
-    const uint32_t n = stored_rays(P);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const cg_ray& r = P.rays[i];
-        const uint32_t slot = atomicAdd(P.cursor + 2u * r.query + r.side, 1u);
-        float* o = P.grouped + 6ull * slot;
+        float* o = P.grouped + 6ull * i;
         o[0] = r.origin[0], o[1] = r.origin[1], o[2] = r.origin[2];
         o[3] = r.direction[0], o[4] = r.direction[1], o[5] = r.direction[2];
-        P.tags[slot] = r.query | (r.side ? 0x80000000u : 0u);
+        P.tags[i] = r.query | (r.side ? 0x80000000u : 0u);
     }
 }
 
@@ -171,9 +137,7 @@ cudaError_t launch_frame_queries(const FrameParams& p, cudaStream_t s) {
 
 cudaError_t launch_frame_rays(const FrameParams& p, uint32_t blocks, cudaStream_t s) {
     if (!p.n_pairs) return cudaSuccess;
-    ray_count_kernel<<<blocks, 256, 0, s>>>(p);
-    ray_offsets_kernel<<<1, 1024, 0, s>>>(p);
-    ray_scatter_kernel<<<blocks, 256, 0, s>>>(p);
+    ray_pack_kernel<<<blocks, 256, 0, s>>>(p);
     frame_shoot_kernel<<<(p.n_pairs + 127u) / 128u, 128, 0, s>>>(p);
     return cudaGetLastError();
 }

@@ -46,6 +46,7 @@ struct DevTree {
     uint32_t live;
     uint32_t pad;
     const float* nrm;
+    const uint2* ranges;  // per record (tree-local): first triangle and triangle count of its subtree
 };
 
 // A query as the kernels read it: relative matrix columns, the first
@@ -78,42 +79,62 @@ struct Counters {
     unsigned long long node_pairs;
     unsigned long long tri_tests;
     unsigned long long fragile;
+    unsigned long long rechecked;      // plane distances recomputed in FP64 (CG_RECHECK, CG_ROBUST)
+    unsigned long long disagreements;  // triangle-pair tests where one changed class
     unsigned long long donations;  // node pairs handed to other warps
     unsigned long long warp_steps; // traversal steps (node_pairs / warp_steps = lanes busy per step)
     unsigned long long t_start;    // globaltimer at the first warp's start (trace only)
     // contacts (CG_CONTACTS)
-    unsigned int n_vertices;  // vertex-set slots taken  } one 64-bit word: the emit kernel
-    unsigned int n_rays;      // rays                    } appends to both with one atomic
-    unsigned int n_contacts;  // contact slots taken
+    unsigned int n_vertices;     // vertex-set slots taken by this launch (emptied by the next contacts launch)
+    unsigned int n_rays;         // uncollide rays
+    unsigned int n_contacts;     // contact slots taken: (side, query, triangle) with a colliding pair
     unsigned int c_overflow;     // CONTACT_* bits
-    unsigned int emit_done;      // blocks of the emit kernel that finished
+    unsigned int n_elems;        // triangles with contacts (non-zero weight): the contact records
     unsigned int prev_vertices;  // vertex-set slots earlier launches took and no launch emptied yet
 };
 
-static_assert(offsetof(Counters, n_vertices) % 8 == 0 && offsetof(Counters, n_rays) == offsetof(Counters, n_vertices) + 4,
-              "n_vertices and n_rays form one 64-bit word");
-
-enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u };
+enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ORDER = 8u };
 
 enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
 
-// Contacts and rays (cg_contacts.cu). A contact slot holds one triangle's
-// merged TriangleCandidateRays: the sums are kept in double and rounded to
-// float once, so the order in which threads add changes them by at most the
-// last bit of the double.
+// Contacts and rays (cg_contacts.cu). A slot of the contact table names one
+// triangle of one side of one query that has colliding pairs; its pairs'
+// contributions are listed together and folded in the reference's order.
 constexpr unsigned long long kEmptyKey = ~0ull;
 
 struct ContactSlot {
     unsigned long long key;  // side << 63 | query << 32 | tree-local triangle, or kEmptyKey
-    double sx, sy, sz, sw;   // sums of weight * midpoint and of weight
-    unsigned int mask;       // AND of the "vertex not outside" bits
-    unsigned int pad;
+    uint32_t count;          // colliding pairs of the triangle
+    uint32_t offset;         // first entry of its contributions in the contribution list
 };
+
+// A triangle with contacts (the merged TriangleCandidateRays of a non-zero
+// weight), the element of its (query, side) map. key: the path of the
+// simultaneous descent to the first leaf pair that gave it weight, one bit per
+// split (left 0, right 1), left-aligned in 128 bits; in the engine's
+// unordered_map it was inserted in that leaf pair's turn.
+struct alignas(16) ContactElem {
+    unsigned long long key_hi, key_lo;
+    float sx, sy, sz, w;  // weighted midpoint sum and weight: the reference's float folds
+    uint32_t tri, mask, depth, pad;
+};
+
+// std::unordered_map<uint32_t, T> grows at fixed sizes: the elements with
+// insertion index in [start[e], start[e + 1]) are inserted with bucket count
+// buckets[e] (the whole table is rehashed into it when start[e] is inserted).
+constexpr uint32_t kMaxSchedule = 40;
+
+// Order kernel working memory: maps of up to kOrderSmem triangles are ordered
+// in shared memory, larger ones in global memory (kOrderWords words per slot).
+constexpr uint32_t kOrderSmem = 1024;
+constexpr uint32_t kOrderWords = 18;
 
 struct ContactParams {
     const PackedQuery* q;
     uint32_t n_queries;
+    uint32_t n_sched;           // entries of the growth schedule
     const float4* tris;
+    const float4* recs;
     const DevTree* trees;
     const cg_tri_pair* pairs;
     const uint4* pair_aux;      // per pair: (first triangle, second triangle, leaf-list index, query), arena indices
@@ -121,20 +142,36 @@ struct ContactParams {
     unsigned long long pairs_cap;
     ContactSlot* table;
     uint32_t table_mask;
-    uint32_t* occupied;         // slots taken this launch
-    unsigned long long* vkeys;  // set of (side, query, vertex index) that already have a ray
+    uint32_t max_contacts;      // contact slots (and records) a launch can hold
+    uint32_t* occupied;         // slots taken this launch, in the order they were taken
+    float4* pg_geom;            // per pair: weight * midpoint, weight
+    uint4* pg_link;             // per pair: both triangles' slots and places in their slots' lists
+    uint32_t* pg_mask;          // per pair: "not outside" bits of the first triangle | the second's << 3
+    unsigned long long* contrib;// contributions: (other triangle << 32) | (pair << 1) | side
+    uint32_t* map_cnt;          // per map (2 query + side): slots; then per map element offsets
+    uint32_t* map_off;
+    uint32_t* map_fill;         // elements (triangles with contacts)
+    uint32_t* map_nr;           // rays
+    uint32_t* map_coff;         // first contact record and first ray of each map in the outputs
+    uint32_t* map_roff;
+    ContactElem* elems;         // per map from map_off
+    uint32_t* work;             // order kernel: global working memory of large maps
+    unsigned long long* vkeys;  // set of (side, query, vertex index) with their first corner in map order
+    uint32_t* vval;
     uint32_t vtable_mask;
     uint32_t* vocc;             // vertex-set slots taken, in order
-    uint32_t max_contacts;
+    cg_contact* ctmp;           // per map from map_off: the map's records in iteration order
+    cg_ray* rtmp;               // per map from 3 map_off: its rays in order
     cg_contact* contacts;
     cg_ray* rays;
     uint32_t max_rays;
-    double* sums;               // per query: 2 sides x (x, y, z, count)
     cg_ray_average* averages;
     Counters* ctr;
+    uint32_t sched_start[kMaxSchedule];
+    uint32_t sched_buckets[kMaxSchedule];
 };
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t accumulate_grid, uint32_t emit_grid, cudaStream_t s);
+cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s);
 
 // Results of a step written to host buffers (cg_set_host_outputs).
 struct CopyOutParams {
@@ -152,9 +189,8 @@ struct CopyOutParams {
     unsigned long long host_averages_cap;
 };
 cudaError_t launch_copy_out(const CopyOutParams& p, uint32_t blocks, cudaStream_t s);
-cudaError_t contacts_occupancy(int* accumulate_blocks_per_sm, int* emit_blocks_per_sm);
-cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t n_vslots,
-                                cudaStream_t s);
+cudaError_t init_contact_tables(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t* vval,
+                                uint32_t n_vslots, cudaStream_t s);
 
 struct NarrowParams {
     const PackedQuery* q;
@@ -434,10 +470,9 @@ struct FrameParams {
     cg_query* queries;           // [n_pairs] collide queries
     const cg_ray* rays;          // the collide step's rays
     const unsigned* n_rays;      // their count (device)
-    uint32_t* counts;            // [2 n_pairs] rays per pair and side, zero before the frame
-    uint32_t* offsets;           // [2 n_pairs]
-    uint32_t* cursor;            // [2 n_pairs]
-    float* grouped;              // [max_rays][6] rays grouped per pair, first entity's then second's
+    const uint32_t* counts;      // [2 n_pairs] rays per pair and side (the contact step's)
+    const uint32_t* offsets;     // [2 n_pairs] first ray of each pair and side
+    float* grouped;              // [max_rays][6] the rays as origin, direction
     uint32_t* tags;              // [max_rays] pair | (from the second entity) << 31
     ShootQuery* shoot;           // [n_pairs]; pad[0]: an entity moved
     const float* deltas;         // [n_pairs][3]

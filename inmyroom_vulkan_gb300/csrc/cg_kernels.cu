@@ -320,8 +320,10 @@ __device__ __forceinline__ unsigned long long trace_base(Counters* ctr) {
 // The narrow phase of leaf pairs [first, first + nl) of the list (nl <= 32),
 // staged in `stage` (kNarrowWarpWords words); all 32 lanes call it. The
 // entries must be visible to the calling warp.
+template <int kMode>
 __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* stage, uint32_t first, uint32_t nl,
                                              int lane, unsigned long long& tests, unsigned long long& fragile,
+                                             unsigned long long& rechecked, unsigned long long& disagree,
                                              unsigned long long t_base) {
     uint32_t* lq = stage;
     uint32_t* loa = lq + 32;
@@ -381,6 +383,7 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
         int res = TT_MISS;
         uint32_t q = 0, ia = 0, ib = 0, leaf_i = 0;
         float3 src = make_float3(0.f, 0.f, 0.f), tgt = src;
+        Recheck rck;
         if (t < total) {
             if (!counted) {
                 int l = 0, h = int(nl) - 1;
@@ -410,10 +413,18 @@ __device__ __forceinline__ void narrow_block(const NarrowParams& P, uint32_t* st
             b0 = xform(M, b0, 1.0f);
             b1 = xform(M, b1, 1.0f);
             b2 = xform(M, b2, 1.0f);
-            res = tri_tri(a0, a1, a2, b0, b1, b2, src, tgt);
+            res = tri_tri_mode<kMode>(a0, a1, a2, b0, b1, b2, src, tgt, rck);
         }
         const unsigned hitmask = __ballot_sync(kFull, res == TT_HIT);
         const unsigned fragmask = __ballot_sync(kFull, res == TT_FRAGILE);
+        if (kMode != 0) {
+            const unsigned nchk = __reduce_add_sync(kFull, rck.checked);
+            const unsigned ndis = __popc(__ballot_sync(kFull, rck.disagree));
+            if (lane == 0) {
+                rechecked += nchk;
+                disagree += ndis;
+            }
+        }
         if (hitmask) {
             unsigned long long obase = 0;
             if (lane == 0) obase = atomicAdd(&P.ctr->n_pairs, (unsigned long long)__popc(hitmask));
@@ -704,6 +715,7 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
 // one triangle pair per lane, in the order of the reference's pair loop per
 // leaf pair (CreateUncollideRays.cpp:78-86): B's triangle is moved into A's
 // space with TrianglePosition::MultiplyBy4x4Matrix arithmetic, then tested.
+template <int kMode>
 __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
     __shared__ uint32_t sm[8 * kNarrowWarpWords];
     const int lane = threadIdx.x & 31;
@@ -712,7 +724,7 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
 
     const unsigned long long n_all = *reinterpret_cast<volatile unsigned long long*>(&P.ctr->n_leafs);
     const uint32_t n = uint32_t(n_all < P.leaf_cap ? n_all : P.leaf_cap);
-    unsigned long long tests = 0, fragile = 0;
+    unsigned long long tests = 0, fragile = 0, rechecked = 0, disagree = 0;
     unsigned long long t_base = 0;
     if (P.trace && lane == 0) t_base = trace_base(P.ctr);
 
@@ -722,11 +734,15 @@ __global__ void __launch_bounds__(256) narrow_kernel(const NarrowParams P) {
         first = __shfl_sync(kFull, first, 0);
         if (first >= n) break;
         const uint32_t nl = min(32u, n - first);
-        narrow_block(P, stage, first, nl, lane, tests, fragile, t_base);
+        narrow_block<kMode>(P, stage, first, nl, lane, tests, fragile, rechecked, disagree, t_base);
     }
     if (lane == 0) {
         atomicAdd(&P.ctr->tri_tests, tests);
         atomicAdd(&P.ctr->fragile, fragile);
+        if (kMode != 0) {
+            atomicAdd(&P.ctr->rechecked, rechecked);
+            atomicAdd(&P.ctr->disagreements, disagree);
+        }
     }
 }
 
@@ -852,7 +868,7 @@ cudaError_t traverse_occupancy(uint32_t warps_per_block, uint32_t stack_cap, int
 }
 
 cudaError_t narrow_occupancy(uint32_t warps_per_block, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, narrow_kernel, int(32 * warps_per_block), 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, narrow_kernel<0>, int(32 * warps_per_block), 0);
 }
 
 cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s) {
@@ -862,7 +878,12 @@ cudaError_t launch_traverse(const TraverseParams& p, uint32_t blocks, uint32_t w
 }
 
 cudaError_t launch_narrow(const NarrowParams& p, uint32_t blocks, uint32_t warps_per_block, cudaStream_t s) {
-    narrow_kernel<<<blocks, 32 * warps_per_block, 0, s>>>(p);
+    if (p.flags & CG_ROBUST)
+        narrow_kernel<2><<<blocks, 32 * warps_per_block, 0, s>>>(p);
+    else if (p.flags & CG_RECHECK)
+        narrow_kernel<1><<<blocks, 32 * warps_per_block, 0, s>>>(p);
+    else
+        narrow_kernel<0><<<blocks, 32 * warps_per_block, 0, s>>>(p);
     return cudaGetLastError();
 }
 

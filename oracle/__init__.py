@@ -86,6 +86,8 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
         f("tri_tri_ex").argtypes = [_f32p, _f32p, C.POINTER(C.c_int), C.POINTER(C.c_int), _f32p, _f32p]
         f("contacts").restype = sz
         f("contacts").argtypes = [vp, C.c_int, _u32p, _u32p, _f32p, sz]
+        f("contacts_iter").restype = sz
+        f("contacts_iter").argtypes = [vp, C.c_int, _u32p, _u32p, _f32p, sz]
         f("collide_batch").restype = C.c_uint64
         f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int,
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
@@ -94,6 +96,13 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
         f("collide_pairs").restype = sz
         f("collide_pairs").argtypes = [vp, vp, _f32p, _f32p, sz, _u32p, _f32p, sz,
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        f("collide_pairs_mode").restype = sz
+        f("collide_pairs_mode").argtypes = [vp, vp, _f32p, _f32p, sz, _u32p, _f32p, sz,
+                                            C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int,
+                                            np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
+        f("tri_tri_recheck").restype = C.c_int
+        f("tri_tri_recheck").argtypes = [_f32p, _f32p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _u32p,
+                                         _f32p, _f32p]
 
 
 class FlatTree:
@@ -200,15 +209,18 @@ class Mid:
         self.impl.fn("rays")(self.h, ra, rb, na, nb, counts, avg)
         return ra[:na], rb[:nb], avg
 
-    def contacts(self, side: int):
-        """(port only) per-triangle (index, mask, wsum xyz + weight), sorted by index."""
+    def contacts(self, side: int, iteration_order: bool = False):
+        """(port only) per-triangle (index, mask, wsum xyz + weight), sorted by
+        index, or in the per-triangle map's iteration order (the order its rays
+        are made in)."""
+        fn = self.impl.fn("contacts_iter" if iteration_order else "contacts")
         z32 = np.zeros(1, np.uint32)
         zf = np.zeros((1, 4), np.float32)
-        n = self.impl.fn("contacts")(self.h, side, z32, z32, zf, 0)
+        n = fn(self.h, side, z32, z32, zf, 0)
         idx = np.zeros(max(n, 1), np.uint32)
         mask = np.zeros(max(n, 1), np.uint32)
         f = np.zeros((max(n, 1), 4), np.float32)
-        self.impl.fn("contacts")(self.h, side, idx, mask, f, n)
+        fn(self.h, side, idx, mask, f, n)
         return idx[:n], mask[:n], f[:n]
 
 
@@ -366,8 +378,9 @@ class Impl:
         self.fn("sweep_and_prune")(h, g, cb.ctypes.data, n, axp, out.ctypes.data, cnt)
         return out[:cnt]
 
-    def collide_pairs(self, trees_a, trees_b, mats_a, mats_b):
-        """(port) all colliding pairs of a batch: (n,3) [query, ia, ib], (n,6) segs, tests, leaf pairs."""
+    def collide_pairs(self, trees_a, trees_b, mats_a, mats_b, recheck_mode=None):
+        """(port) all colliding pairs of a batch: (n,3) [query, ia, ib], (n,6) segs, tests, leaf pairs.
+        With recheck_mode (0 off, 1 counted, 2 FP64 verdict) also (rechecked, disagreements)."""
         n = len(trees_a)
         ha = (C.c_void_p * n)(*[t.h for t in trees_a])
         hb = (C.c_void_p * n)(*[t.h for t in trees_b])
@@ -377,11 +390,27 @@ class Impl:
         lp = C.c_uint64()
         z = np.zeros((1, 3), np.uint32)
         zs = np.zeros((1, 6), np.float32)
-        cnt = self.fn("collide_pairs")(ha, hb, ma, mb, n, z, zs, 0, C.byref(t), C.byref(lp))
+        rk = np.zeros(2, np.uint64)
+        if recheck_mode is None:
+            fn = lambda *a: self.fn("collide_pairs")(*a)  # noqa: E731
+        else:
+            fn = lambda *a: self.fn("collide_pairs_mode")(*a, int(recheck_mode), rk)  # noqa: E731
+        cnt = fn(ha, hb, ma, mb, n, z, zs, 0, C.byref(t), C.byref(lp))
         pairs = np.zeros((max(cnt, 1), 3), np.uint32)
         segs = np.zeros((max(cnt, 1), 6), np.float32)
-        self.fn("collide_pairs")(ha, hb, ma, mb, n, pairs, segs, cnt, C.byref(t), C.byref(lp))
-        return pairs[:cnt], segs[:cnt], t.value, lp.value
+        fn(ha, hb, ma, mb, n, pairs, segs, cnt, C.byref(t), C.byref(lp))
+        if recheck_mode is None:
+            return pairs[:cnt], segs[:cnt], t.value, lp.value
+        return pairs[:cnt], segs[:cnt], t.value, lp.value, (int(rk[0]), int(rk[1]))
+
+    def tri_tri_recheck(self, a, b, mode):
+        """(port) one test with the FP64 recheck: hit, coplanar, fragile, rechecked, disagreed, src, tgt."""
+        cop, fr = C.c_int(), C.c_int()
+        chk = np.zeros(2, np.uint32)
+        s = np.zeros(3, np.float32)
+        t = np.zeros(3, np.float32)
+        hit = self.fn("tri_tri_recheck")(_f32(a, 9), _f32(b, 9), int(mode), C.byref(cop), C.byref(fr), chk, s, t)
+        return hit, cop.value, fr.value, int(chk[0]), int(chk[1]), s, t
 
 
 _cache: dict = {}

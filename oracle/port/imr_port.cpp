@@ -486,11 +486,61 @@ struct Result {
     float src[3], tgt[3];
 };
 
+// FP64 recheck of the six plane distances: the GPU library's CG_RECHECK /
+// CG_ROBUST, which the reference does not have, restated here as its checker.
+// A distance d (FP32, the reference's arithmetic) is uncertain when |d| lies
+// within B = 32 u C |e1|_1 |e2|_1 of 0 or of 1e-6 (u = 2^-24, e1, e2 the
+// plane triangle's edges, C the largest coordinate magnitude of its first
+// corner and the three tested corners); then det[e1, e2, p - a0] is computed
+// in FP64 and classified (zero below 1e-6, else by sign). mode 1 counts,
+// mode 2 also goes on with the FP64 classes (nonzero ones as the FP64 value
+// rounded to FP32).
+struct Recheck {
+    uint64_t checked = 0;
+    int disagree = 0;
+};
+inline float amax3(const float* p) { return std::fmax(std::fmax(std::fabs(p[0]), std::fabs(p[1])), std::fabs(p[2])); }
+inline float norm1(const float* p) { return (std::fabs(p[0]) + std::fabs(p[1])) + std::fabs(p[2]); }
+inline int class32(float d) { return tiny(d) ? 0 : (d > 0.0f ? 1 : -1); }
+inline int class64(double d) { return std::fabs(d) < 1e-6 ? 0 : (d > 0.0 ? 1 : -1); }
+inline double orient64(const float* a0, const float* a1, const float* a2, const float* p) {
+    const double e1x = double(a1[0]) - double(a0[0]), e1y = double(a1[1]) - double(a0[1]), e1z = double(a1[2]) - double(a0[2]);
+    const double e2x = double(a2[0]) - double(a0[0]), e2y = double(a2[1]) - double(a0[1]), e2z = double(a2[2]) - double(a0[2]);
+    const double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+    return (nx * (double(p[0]) - double(a0[0])) + ny * (double(p[1]) - double(a0[1]))) +
+           nz * (double(p[2]) - double(a0[2]));
+}
+// The snap of three distances (Triangle.cpp:898-915) with the recheck.
+inline void snap3(int mode, const float* a0, const float* a1, const float* a2, const float* e1, const float* e2,
+                  const float* const p[3], float d[3], Recheck* rc) {
+    bool unc[3] = {false, false, false};
+    if (mode != 0) {
+        const float C = std::fmax(std::fmax(amax3(a0), amax3(p[0])), std::fmax(amax3(p[1]), amax3(p[2])));
+        const float B = (32.0f * 0x1p-24f) * C * norm1(e1) * norm1(e2);
+        for (int k = 0; k < 3; ++k) {
+            const float a = std::fabs(d[k]);
+            unc[k] = a < B || std::fabs(a - 1e-6f) < B;
+        }
+        for (int k = 0; k < 3; ++k) {
+            if (!unc[k]) continue;
+            const double x = orient64(a0, a1, a2, p[k]);
+            const int c = class64(x);
+            ++rc->checked;
+            if (c != class32(d[k])) rc->disagree = 1;
+            if (mode == 2) d[k] = c == 0 ? 0.0f : float(x);
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        if (!(mode == 2 && unc[k]) && tiny(d[k])) d[k] = 0.0f;
+}
+
 // tri_tri_intersect_with_isectline (Triangle.cpp:866-1003) as called through
 // TrianglePosition::IntersectTriangles (Triangle.cpp:85-110).
 inline Result test(const float* V0, const float* V1, const float* V2, const float* U0, const float* U1,
-                   const float* U2) {
+                   const float* U2, int mode = 0, Recheck* rc = nullptr) {
     Result r{};
+    Recheck scratch;
+    if (!rc) rc = &scratch;
     float e1[3], e2[3], n1[3], n2[3], dd[3];
     for (int k = 0; k < 3; ++k) {
         e1[k] = V1[k] - V0[k];
@@ -500,12 +550,15 @@ inline Result test(const float* V0, const float* V1, const float* V2, const floa
     n1[1] = e1[2] * e2[0] - e1[0] * e2[2];
     n1[2] = e1[0] * e2[1] - e1[1] * e2[0];
     const float d1 = -(n1[0] * V0[0] + n1[1] * V0[1] + n1[2] * V0[2]);
-    float du0 = (n1[0] * U0[0] + n1[1] * U0[1] + n1[2] * U0[2]) + d1;
-    float du1 = (n1[0] * U1[0] + n1[1] * U1[1] + n1[2] * U1[2]) + d1;
-    float du2 = (n1[0] * U2[0] + n1[1] * U2[1] + n1[2] * U2[2]) + d1;
-    if (tiny(du0)) du0 = 0.0f;
-    if (tiny(du1)) du1 = 0.0f;
-    if (tiny(du2)) du2 = 0.0f;
+    float du[3];
+    du[0] = (n1[0] * U0[0] + n1[1] * U0[1] + n1[2] * U0[2]) + d1;
+    du[1] = (n1[0] * U1[0] + n1[1] * U1[1] + n1[2] * U1[2]) + d1;
+    du[2] = (n1[0] * U2[0] + n1[1] * U2[1] + n1[2] * U2[2]) + d1;
+    {
+        const float* const Up[3] = {U0, U1, U2};
+        snap3(mode, V0, V1, V2, e1, e2, Up, du, rc);
+    }
+    const float du0 = du[0], du1 = du[1], du2 = du[2];
     const float du0du1 = du0 * du1;
     const float du0du2 = du0 * du2;
     if (du0du1 > 0.0f && du0du2 > 0.0f) return r;
@@ -518,12 +571,15 @@ inline Result test(const float* V0, const float* V1, const float* V2, const floa
     n2[1] = e1[2] * e2[0] - e1[0] * e2[2];
     n2[2] = e1[0] * e2[1] - e1[1] * e2[0];
     const float d2 = -(n2[0] * U0[0] + n2[1] * U0[1] + n2[2] * U0[2]);
-    float dv0 = (n2[0] * V0[0] + n2[1] * V0[1] + n2[2] * V0[2]) + d2;
-    float dv1 = (n2[0] * V1[0] + n2[1] * V1[1] + n2[2] * V1[2]) + d2;
-    float dv2 = (n2[0] * V2[0] + n2[1] * V2[1] + n2[2] * V2[2]) + d2;
-    if (tiny(dv0)) dv0 = 0.0f;
-    if (tiny(dv1)) dv1 = 0.0f;
-    if (tiny(dv2)) dv2 = 0.0f;
+    float dv[3];
+    dv[0] = (n2[0] * V0[0] + n2[1] * V0[1] + n2[2] * V0[2]) + d2;
+    dv[1] = (n2[0] * V1[0] + n2[1] * V1[1] + n2[2] * V1[2]) + d2;
+    dv[2] = (n2[0] * V2[0] + n2[1] * V2[1] + n2[2] * V2[2]) + d2;
+    {
+        const float* const Vp[3] = {V0, V1, V2};
+        snap3(mode, U0, U1, U2, e1, e2, Vp, dv, rc);
+    }
+    const float dv0 = dv[0], dv1 = dv[1], dv2 = dv[2];
     const float dv0dv1 = dv0 * dv1;
     const float dv0dv2 = dv0 * dv2;
     if (dv0dv1 > 0.0f && dv0dv2 > 0.0f) return r;
@@ -633,6 +689,9 @@ struct Narrow {
     uint64_t tests = 0;
     std::unordered_map<uint32_t, Contact> ca, cb;
     uint64_t fragile = 0;
+    int recheck_mode = 0;         // moller::snap3's mode for every test
+    uint64_t rechecked = 0;       // distances recomputed in FP64
+    uint64_t disagreements = 0;   // tests where one changed class
 };
 
 // The pair loop of CreateUncollideRays::ExecuteCreateUncollideRays
@@ -649,9 +708,13 @@ void narrow(const Tree& A, const Tree& B, const M4& M, const std::vector<LeafPai
                 const Tri& ta = A.tris[lp.off_a + i];
                 V3 pb[3];
                 xform_tri(M, B.tris[lp.off_b + j], pb);
-                moller::Result r = moller::test(&ta.p[0].x, &ta.p[1].x, &ta.p[2].x, &pb[0].x, &pb[1].x, &pb[2].x);
+                moller::Recheck rc;
+                moller::Result r = moller::test(&ta.p[0].x, &ta.p[1].x, &ta.p[2].x, &pb[0].x, &pb[1].x, &pb[2].x,
+                                                out.recheck_mode, &rc);
                 ++out.tests;
                 out.fragile += uint64_t(r.fragile);
+                out.rechecked += rc.checked;
+                out.disagreements += uint64_t(rc.disagree);
                 if (!(r.hit && !r.coplanar)) continue;
                 if (keep_hits) {
                     Hit h;
@@ -760,8 +823,10 @@ struct Query {
 
 inline M4 relative(const M4& a, const M4& b) { return mul(inverse(a), b); }
 
-void run_query(const Tree& A, const Tree& B, const M4& ma, const M4& mb, Query& q, bool keep_hits, bool rays) {
+void run_query(const Tree& A, const Tree& B, const M4& ma, const M4& mb, Query& q, bool keep_hits, bool rays,
+               int recheck_mode = 0) {
     const M4 M = relative(ma, mb);
+    q.nr.recheck_mode = recheck_mode;
     q.lps.clear();
     traverse(A, B, root_traveler(A), root_traveler(B), M, q.lps);
     if (q.lps.empty()) return;
@@ -1248,6 +1313,28 @@ size_t port_contacts(void* r, int side, uint32_t* out_idx, uint32_t* out_mask, f
     return keys.size();
 }
 
+// The same records in the map's own iteration order (the order of the rays
+// that find_rays_lambda makes from it, CreateUncollideRays.cpp:138).
+size_t port_contacts_iter(void* r, int side, uint32_t* out_idx, uint32_t* out_mask, float* out_f, size_t cap) {
+    auto* h = as_mid(r);
+    Narrow nr;
+    narrow(*h->A, *h->B, h->M, h->q.lps, nr, false, true);
+    const auto& m = side == 0 ? nr.ca : nr.cb;
+    size_t k = 0;
+    for (const auto& kv : m) {
+        if (k < cap) {
+            out_idx[k] = kv.first;
+            out_mask[k] = kv.second.mask;
+            out_f[4 * k + 0] = kv.second.wsum.x;
+            out_f[4 * k + 1] = kv.second.wsum.y;
+            out_f[4 * k + 2] = kv.second.wsum.z;
+            out_f[4 * k + 3] = kv.second.weight;
+        }
+        ++k;
+    }
+    return m.size();
+}
+
 void port_rays(void* r, float* rays_a, float* rays_b, size_t cap_a, size_t cap_b, size_t* counts, float* avg) {
     auto* h = as_mid(r);
     const Tree& A = *h->A;
@@ -1287,6 +1374,23 @@ int port_tri_tri(const float* a9, const float* b9, int* coplanar, float* src3, f
 }
 
 // Same as port_tri_tri, also reporting the "fragile" flag.
+// One test with the FP64 recheck (mode 1 counted, 2 FP64 verdict); checks[0]
+// distances recomputed, checks[1] 1 when one of them changed class.
+int port_tri_tri_recheck(const float* a9, const float* b9, int mode, int* coplanar, int* fragile, uint32_t* checks,
+                         float* src3, float* tgt3) {
+    moller::Recheck rc;
+    moller::Result r = moller::test(a9, a9 + 3, a9 + 6, b9, b9 + 3, b9 + 6, mode, &rc);
+    *coplanar = r.coplanar;
+    *fragile = r.fragile;
+    checks[0] = uint32_t(rc.checked);
+    checks[1] = uint32_t(rc.disagree);
+    if (r.hit && !r.coplanar) {
+        std::memcpy(src3, r.src, sizeof(r.src));
+        std::memcpy(tgt3, r.tgt, sizeof(r.tgt));
+    }
+    return r.hit;
+}
+
 int port_tri_tri_ex(const float* a9, const float* b9, int* coplanar, int* fragile, float* src3, float* tgt3) {
     moller::Result r = moller::test(a9, a9 + 3, a9 + 6, b9, b9 + 3, b9 + 6);
     *coplanar = r.coplanar;
@@ -1362,17 +1466,21 @@ uint64_t port_collide_batch(void* const* trees_a, void* const* trees_b, const fl
 // Colliding pairs of a batch of queries: for query q, pairs are written to
 // pair_out[...] as (query, ia, ib) with segments; returns total count (writes
 // at most cap). Used as the parity oracle for batched GPU runs.
-size_t port_collide_pairs(void* const* trees_a, void* const* trees_b, const float* mats_a, const float* mats_b,
-                          size_t n, uint32_t* pair_out, float* seg_out, size_t cap, uint64_t* tests_out,
-                          uint64_t* leafpairs_out) {
+// The colliding pairs of a batch with the FP64 recheck in mode `mode` (0 off,
+// 1 counted, 2 FP64 verdict; moller::snap3), its counts in recheck[2].
+size_t port_collide_pairs_mode(void* const* trees_a, void* const* trees_b, const float* mats_a, const float* mats_b,
+                               size_t n, uint32_t* pair_out, float* seg_out, size_t cap, uint64_t* tests_out,
+                               uint64_t* leafpairs_out, int mode, uint64_t* recheck) {
     size_t total = 0;
-    uint64_t tests = 0, lpairs = 0;
+    uint64_t tests = 0, lpairs = 0, checked = 0, disagree = 0;
     for (size_t q = 0; q < n; ++q) {
         Query qr;
         run_query(*static_cast<const Tree*>(trees_a[q]), *static_cast<const Tree*>(trees_b[q]),
-                  ldm(mats_a + 16 * q), ldm(mats_b + 16 * q), qr, true, false);
+                  ldm(mats_a + 16 * q), ldm(mats_b + 16 * q), qr, true, false, mode);
         tests += qr.nr.tests;
         lpairs += qr.lps.size();
+        checked += qr.nr.rechecked;
+        disagree += qr.nr.disagreements;
         for (const Hit& h : qr.nr.hits) {
             if (total < cap) {
                 pair_out[3 * total + 0] = uint32_t(q);
@@ -1386,7 +1494,18 @@ size_t port_collide_pairs(void* const* trees_a, void* const* trees_b, const floa
     }
     if (tests_out) *tests_out = tests;
     if (leafpairs_out) *leafpairs_out = lpairs;
+    if (recheck) {
+        recheck[0] = checked;
+        recheck[1] = disagree;
+    }
     return total;
+}
+
+size_t port_collide_pairs(void* const* trees_a, void* const* trees_b, const float* mats_a, const float* mats_b,
+                          size_t n, uint32_t* pair_out, float* seg_out, size_t cap, uint64_t* tests_out,
+                          uint64_t* leafpairs_out) {
+    return port_collide_pairs_mode(trees_a, trees_b, mats_a, mats_b, n, pair_out, seg_out, cap, tests_out,
+                                   leafpairs_out, 0, nullptr);
 }
 
 // Morph targets, then linear-blend skinning, of dynamicMeshShader_glsl.comp

@@ -67,6 +67,51 @@ def tri_cases(rng):
     return np.array(A, np.float32).reshape(-1, 9), np.array(B, np.float32).reshape(-1, 9)
 
 
+def near_epsilon_cases(rng):
+    """Pairs whose plane distances lie near the Moller test's 1e-6 threshold
+    (or near 0) while the FP32 arithmetic that computes them carries errors of
+    that size: tilted triangles far from the origin (coordinates up to 1e3,
+    so the two dot products of d = n . p - n . a0 cancel), one corner of the
+    other triangle placed at a distance within a few 1e-6 of the plane, the
+    other two on both sides of it. Half the pairs have the roles swapped."""
+    A, B = [], []
+    for _ in range(400):
+        off = rng.uniform(-1, 1, 3) * 10.0 ** rng.uniform(0, 3)
+        edge = 10.0 ** rng.uniform(-2, 0.5)
+        R = scenes.random_rotation(rng)
+        a = off + (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]]) @ R.T) * edge
+        a = a.astype(np.float32).astype(np.float64)
+        e1, e2 = a[1] - a[0], a[2] - a[0]
+        n = np.cross(e1, e2)
+        target = rng.uniform(-3e-6, 3e-6) if rng.random() < 0.8 else rng.choice([-1e-6, 0.0, 1e-6])
+        inplane = a[0] + e1 * rng.uniform(0.1, 0.4) + e2 * rng.uniform(0.1, 0.4)
+        p0 = inplane + n * (target / (n @ n))
+        u = R[:, 2] * edge * rng.uniform(0.3, 1.0)
+        v = (R[:, 0] - R[:, 1]) * edge * rng.uniform(0.2, 0.8)
+        b = np.stack([p0, p0 + u + v, p0 - u + v]).astype(np.float32)
+        if rng.random() < 0.5:
+            A.append(a.astype(np.float32)); B.append(b)
+        else:
+            A.append(b); B.append(a.astype(np.float32))
+    return np.array(A, np.float32).reshape(-1, 9), np.array(B, np.float32).reshape(-1, 9)
+
+
+def near_epsilon_fixture(R, rng):
+    """The reference's verdicts on near_epsilon_cases (the FP32 verdict that
+    the GPU library keeps by default; the FP64 recheck is checked against
+    exact arithmetic by the tests)."""
+    a, b = near_epsilon_cases(rng)
+    n = len(a)
+    hit = np.zeros(n, np.int32); cop = np.zeros(n, np.int32)
+    src = np.zeros((n, 3), np.float32); tgt = np.zeros((n, 3), np.float32)
+    for i in range(n):
+        h, c, s, t = R.tri_tri(a[i], b[i])
+        hit[i], cop[i] = h, c
+        if h and not c:
+            src[i], tgt[i] = s, t
+    np.savez_compressed(os.path.join(HERE, "tritri_near.npz"), a=a, b=b, hit=hit, coplanar=cop, src=src, tgt=tgt)
+
+
 def box_cases(rng):
     A, B = [], []
     for _ in range(600):
@@ -213,6 +258,7 @@ def main():
     shoot_fixture(R)
     sap_fixture(R)
     frame_fixture(R)
+    near_epsilon_fixture(R, np.random.Generator(np.random.PCG64(4243)))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -5,18 +5,17 @@ pairs and deltas on the 256-entity scene, the oracle's frame with other
 motions, the composition of the frame from its own collide step's rays, and
 the edge cases.
 
-The pairs with rays are exact. The deltas are the reference's arithmetic on
-the frame's own rays, which match the reference's up to the last bits of the
-rays that start at a contact's weighted average point (summed in another
-order). Hence two bars:
-* composition: every delta within 1e-4 relative of the oracle's shooting and
-  split run on the frame's own rays and ray averages (only the order in which
-  a pair's force responses are summed differs);
-* reference: at least 95% of the pairs within 2e-4 relative of the
-  reference's deltas, every pair within 2% of its delta's length (a ray that
-  grazes a triangle's edge, or that sets the shooting's maximum, can move a
-  delta by up to a percent).
-Pairs where neither entity moved have exactly zero deltas on both sides."""
+Bit for bit: the pairs with rays, and every delta, against the oracle's
+frame (the frame's rays are the reference's rays in the reference's order, so
+the shooting's sums and the split are the reference's arithmetic on the same
+operands), and against the reference's golden frame on every pair whose
+triangle tests the reference defines: a pair with a fragile test (the
+second interval degenerates, Triangle.cpp:960-966, where the reference reads
+uninitialised values; the oracle and the GPU define it as no intersection)
+has no defined reference delta (two runs of the same reference build gave
+different deltas for the golden frame's one such pair), so the golden
+comparison leaves it out. Pairs where neither entity moved have exactly zero
+deltas on both sides."""
 import os
 
 import numpy as np
@@ -28,9 +27,21 @@ from oracle import frame
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-RTOL, ATOL = 2e-4, 1e-5     # against the reference: most pairs
-ROW_TOL = 2e-2              # against the reference: every pair, relative to the delta's length
-COMPOSE_RTOL = 1e-4         # against the oracle on the frame's own rays
+
+
+def bits(x):
+    return np.ascontiguousarray(x, np.float32).view(np.uint32)
+
+
+def same_bits(got, want, what=""):
+    got = np.ascontiguousarray(got, np.float32)
+    want = np.ascontiguousarray(want, np.float32)
+    assert got.shape == want.shape, what
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan), what
+    bad = np.argwhere(bits(got) != bits(want))
+    bad = bad[~nan[tuple(bad.T)]] if len(bad) else bad
+    assert not len(bad), (what, bad[:5], got[tuple(bad[:5].T)], want[tuple(bad[:5].T)])
 
 
 def as_arrays(res):
@@ -40,13 +51,21 @@ def as_arrays(res):
     return p[o], d[o]
 
 
-def check_against_reference(p, d, wp, wd):
+def check_against_reference(p, d, wp, wd, defined=None):
     assert np.array_equal(p, wp)
-    tight = np.isclose(d, wd, rtol=RTOL, atol=ATOL).all(1)
-    assert tight.mean() >= 0.95, (tight.sum(), len(tight))
-    for half in (slice(0, 3), slice(3, 6)):
-        err = np.linalg.norm(d[:, half] - wd[:, half], axis=1)
-        assert (err <= ROW_TOL * np.linalg.norm(wd[:, half], axis=1) + ATOL).all()
+    if defined is None:
+        defined = np.ones(len(p), bool)
+    same_bits(d[defined], wd[defined], "deltas")
+
+
+def reference_defined(port, trees, mats, pairs):
+    """Rows whose pair has no fragile triangle test (the reference's result
+    is defined there)."""
+    ok = []
+    for a, b in pairs:
+        _, _, _, fragile = port.mid_phase(trees[a], trees[b], mats[a], mats[b]).narrow()
+        ok.append(fragile == 0)
+    return np.array(ok, bool)
 
 
 @pytest.fixture(scope="module")
@@ -59,12 +78,14 @@ def scene_trees(gpu_ctx, port):
         gpu_ctx.free_tree(int(i))
 
 
-def test_golden_frame(gpu_ctx, scene_trees):
-    sc, _, ids = scene_trees
+def test_golden_frame(gpu_ctx, port, scene_trees):
+    sc, trees, ids = scene_trees
     want = np.load(os.path.join(GOLD, "frame_scene.npz"))
+    defined = reference_defined(port, trees, sc.mats, want["pairs"])
+    assert defined.sum() >= len(defined) - 2
     for _ in range(2):  # the second frame reuses the buffers
         p, d = as_arrays(gpu_ctx.collision_frame(ids, sc.mats, want["previous"], want["callback"]))
-        check_against_reference(p, d, want["pairs"], want["deltas"])
+        check_against_reference(p, d, want["pairs"], want["deltas"], defined)
         still = ~np.abs(want["deltas"]).any(1)
         assert still.any() and not np.abs(d[still]).any()
 
@@ -96,9 +117,8 @@ def test_frame_composition(gpu_ctx, port, scene_trees):
             total = np.float32(m1 + m2)
             d1 = -delta * np.float32(m1 / total)
             d2 = delta * np.float32(m2 / total)
-        scale = float(np.linalg.norm(delta)) + 1e-6
-        np.testing.assert_allclose(r["first_delta"], d1, rtol=COMPOSE_RTOL, atol=COMPOSE_RTOL * scale)
-        np.testing.assert_allclose(r["second_delta"], d2, rtol=COMPOSE_RTOL, atol=COMPOSE_RTOL * scale)
+        same_bits(r["first_delta"], d1, (a, b, "first delta"))
+        same_bits(r["second_delta"], d2, (a, b, "second delta"))
     assert moved_rows > 150
 
 

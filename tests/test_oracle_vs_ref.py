@@ -97,3 +97,37 @@ def test_sweep_and_prune_axes_and_callbacks(port, ref):
             a = port.sweep_and_prune(tp, sc.mats, cb, ax)
             b = ref.sweep_and_prune(tr, sc.mats, cb, ax)
             assert set(map(tuple, a)) == set(map(tuple, b)) and len(a) == len(b)
+
+
+def _same_bits(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    nan = np.isnan(b)
+    return a.shape == b.shape and np.array_equal(np.isnan(a), nan) and np.array_equal(bits(a)[~nan], bits(b)[~nan])
+
+
+def test_scene256_full_size(port, ref):
+    """The full 256-entity scene: every tree of the port's builder equals the
+    reference builder's, and for every AABB-overlap query the leaf pairs (in
+    the descent's order), the colliding pairs and segments, the uncollide rays
+    (in the order of the reference's unordered_map) and the mean origins are
+    the reference's, bit for bit."""
+    sc = scenes.scene()
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    tr = [ref.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    for k, (a, b) in enumerate(zip(tp, tr)):
+        assert a.export().equal(b.export()), k
+    n_rays = 0
+    for i, j in sc.pairs:
+        mp = port.mid_phase(tp[i], tp[j], sc.mats[i], sc.mats[j])
+        mr = ref.mid_phase(tr[i], tr[j], sc.mats[i], sc.mats[j])
+        assert np.array_equal(mp.leaf_pairs(), mr.leaf_pairs()), (i, j)
+        p1, s1, t1, _ = mp.narrow()
+        p2, s2, t2, _ = mr.narrow()
+        assert np.array_equal(p1, p2) and np.array_equal(bits(s1), bits(s2)) and t1 == t2, (i, j)
+        ra1, rb1, avg1 = mp.rays()
+        ra2, rb2, avg2 = mr.rays()
+        assert _same_bits(ra1, ra2) and _same_bits(rb1, rb2), (i, j)
+        assert _same_bits(avg1, avg2), (i, j, avg1, avg2)
+        n_rays += len(ra1) + len(rb1)
+    assert n_rays > 20000
