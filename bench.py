@@ -1,8 +1,9 @@
 """Benchmark of the GB300 collision path on the 256-entity scene.
 
 One step = one batched collide launch (CUDA graph: counter reset, query
-packing, persistent traversal, persistent triangle-pair narrow phase, then
-per-triangle contacts, uncollide rays and their mean origins) over every
+packing, persistent traversal, persistent triangle-pair narrow phase with the
+FP64 recheck of near-threshold plane distances, then per-triangle contacts,
+uncollide rays and their mean origins in the reference's order) over every
 entity pair of the scene whose world AABBs overlap, the work the reference's
 mid phase + CreateUncollideRays does per pair. The metric is triangle-pair
 tests per second (Moller calls on candidate leaf pairs), with collision
@@ -46,8 +47,18 @@ NODE_PAIR_BYTES = 2 * 48   # two boxes
 TRI_TEST_BYTES = 2 * 36    # two triangles
 NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
 TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
-COUNTERS_BYTES = 112       # the launch counters, read back by cg_collide and by each result read
-STEP_KERNELS = 6           # init, pack, traverse, narrow, contacts_accumulate, contacts_emit
+COUNTERS_BYTES = 128       # the launch counters, read back by cg_collide and by each result read
+# init, pack, traverse, narrow; contacts: pairs, scan, scatter, fold, order, offsets, emit
+STEP_KERNELS = 11
+STEP_FLAGS_DOC = ("CUDA graph: init + pack + persistent traversal + persistent narrow phase (FP64 recheck counted) "
+                  "+ contacts (pairs, scan, scatter, fold, order, offsets, emit)")
+CACHE_DOC = "L2 flushed (512 MB write) between timed GPU steps"
+
+
+def scene_config(n_queries: int, n_tris: int, tests: int, rays: int) -> dict:
+    """The workload's description, the same keys and values in both arms."""
+    return {"workload": WORKLOAD, "queries_per_step": int(n_queries), "triangles": int(n_tris),
+            "tri_tests_per_step": int(tests), "rays_per_step": int(rays), "cache": CACHE_DOC}
 
 
 def measured_peaks() -> dict:
@@ -123,21 +134,28 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def run_tree_build(ctx, sc, cpu_seconds: float) -> tuple[np.ndarray, dict]:
+def run_tree_build(ctx, sc, cpu_seconds: float, reps: int = 10, device: int = 0) -> tuple[np.ndarray, dict]:
     """OBB trees of the scene's meshes built on the device (cg_tree_build, one
     call for all 256, trees uploaded); host-timed around the synchronous call,
-    the second of two builds. Beside it the oracle's builder on all host
-    cores. Returns the trees' ids and the line."""
+    the median of `reps` builds after one untimed build, with the SM clocks
+    sampled meanwhile. Beside it the oracle's builder on all host cores.
+    Returns the trees' ids and the line."""
     ids = ctx.build_trees(sc.meshes)
-    for tid in ids:
-        ctx.free_tree(int(tid))
-    t0 = time.perf_counter()
-    ids = ctx.build_trees(sc.meshes)
-    ms = 1e3 * (time.perf_counter() - t0)
+    times = []
+    with ClockSampler(device) as clocks:
+        for _ in range(reps):
+            for tid in ids:
+                ctx.free_tree(int(tid))
+            t0 = time.perf_counter()
+            ids = ctx.build_trees(sc.meshes)
+            times.append(1e3 * (time.perf_counter() - t0))
+    ms = float(np.median(times))
     tris = int(sum(m.n_tris for m in sc.meshes))
     line = {"workload": f"OBB trees of the scene's {len(sc.meshes)} meshes ({tris} triangles), one cg_tree_build",
-            "ms": ms, "triangles_per_s": tris / (ms / 1e3),
-            "timing": "host perf_counter around the synchronous call (meshes uploaded, trees uploaded)"}
+            "ms": ms, "ms_min": float(np.min(times)), "ms_max": float(np.max(times)), "builds": reps,
+            "triangles_per_s": tris / (ms / 1e3), "clocks": clocks.summary(),
+            "timing": "host perf_counter around the synchronous call (meshes uploaded, trees uploaded); median of "
+                      f"{reps} builds"}
     if cpu_seconds > 0:
         from concurrent.futures import ThreadPoolExecutor
 
@@ -180,9 +198,11 @@ def cpu_baseline(sc, seconds: float = 10.0) -> dict:
     t1 = time.perf_counter()
     r1 = fast.collide_batch(ta, tb, ma, mb, threads=1)
     single = time.perf_counter() - t1
+    v1 = r1["tests"] / single
     return {"value": tests / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{steps} whole scene steps ({len(qa)} queries each), {el:.1f} s, release flags",
-            "single_thread_value": r1["tests"] / single, "steps": steps}
+            "sample": f"{steps} whole scene steps ({len(qa)} queries each), {el:.1f} s, release flags, queries "
+                      "largest first from a shared counter",
+            "single_thread_value": v1, "efficiency": tests / el / v1 / cores, "steps": steps}
 
 
 def run_reference(args) -> dict:
@@ -201,20 +221,24 @@ def run_reference(args) -> dict:
     ta, tb = [trees[i] for i in qa], [trees[j] for j in qb]
     ma, mb = sc.mats[qa], sc.mats[qb]
     cores = os.cpu_count() or 1
+    first = None
     for _ in range(args.warmup):
-        impl.collide_batch(ta, tb, ma, mb, threads=cores)
+        first = impl.collide_batch(ta, tb, ma, mb, threads=cores)
     tests, t0 = 0, time.perf_counter()
     for _ in range(args.steps):
-        tests += impl.collide_batch(ta, tb, ma, mb, threads=cores)["tests"]
+        r = impl.collide_batch(ta, tb, ma, mb, threads=cores)
+        tests += r["tests"]
     el = time.perf_counter() - t0
     v = tests / el
+    r = first or r
     return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PCG64, seed 1002)",
-            "config": {"workload": WORKLOAD, "queries": int(len(qa)), "cache": "n/a (CPU)"},
+            "config": scene_config(len(qa), sum(m.n_tris for m in sc.meshes), r["tests"], r["rays"]),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
-                             "sample": f"{args.steps} whole scene steps, release flags"},
+                             "sample": f"{args.steps} whole scene steps, release flags, queries largest first from a "
+                                       "shared counter"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -602,7 +626,7 @@ def run_gpu(args) -> dict:
     # each rank collides its own scene replica (weak scaling, no data exchange)
     sc = scenes.scene(seed=1002 + 1000 * rank)
     ctx = capi.Context(device=local, max_queries=max(4096, len(sc.pairs)), max_tri_pairs=1 << 22)
-    ids, tree_build = run_tree_build(ctx, sc, min(args.cpu_seconds, 5.0) if rank == 0 else 0.0)
+    ids, tree_build = run_tree_build(ctx, sc, min(args.cpu_seconds, 5.0) if rank == 0 else 0.0, device=local)
     qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
     rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
     q = capi.make_queries(ids[qa], ids[qb], rel)
@@ -610,7 +634,9 @@ def run_gpu(args) -> dict:
 
     d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
     torch.cuda.synchronize()
-    flags = capi.CG_CONTACTS
+    # the scene with the FP64 determinant filter: near-threshold plane
+    # distances rechecked in FP64 and counted, the reference's verdicts kept
+    flags = capi.CG_CONTACTS | capi.CG_RECHECK
     # a dedicated stream: its handle is never 0, which the C ABI reads as
     # "the context's own stream"
     stream = torch.cuda.Stream(dev)
@@ -671,6 +697,27 @@ def run_gpu(args) -> dict:
             e2e_times.append(time.perf_counter() - t0)
         assert len(pairs) == pairs_per_step and len(rays) == rays_per_step and len(avgs) == n
         assert np.array_equal(pairs.view(np.uint8), ctx.tri_pairs().view(np.uint8))
+    ctx.set_host_outputs()
+
+    # the recheck's cost: the same step without it, event-timed the same way
+    recheck = {"rechecked_per_step": int(st["rechecked"]), "disagreements_per_step": int(st["disagreements"]),
+               "ms_per_step_with": float(np.mean(step_ms))}
+    ctx.graph_capture(d_q.data_ptr(), n, capi.CG_CONTACTS)
+    for _ in range(3):
+        ctx.graph_launch(stream.cuda_stream)
+    plain_steps = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        ctx.graph_launch(stream.cuda_stream)
+        s1.record(stream)
+        s1.synchronize()
+        plain_steps.append(s0.elapsed_time(s1))
+    st_plain = ctx.sync_stats()
+    assert st_plain["tri_pairs"] == pairs_per_step and st_plain["rays"] == rays_per_step
+    recheck["ms_per_step_without"] = float(np.mean(plain_steps))
+    recheck["cost_ms"] = recheck["ms_per_step_with"] - recheck["ms_per_step_without"]
     # the slowest rank's times (every rank does a replica's fixed work)
     total_ms = shard.max_over_ranks(float(np.sum(step_ms)), dist, dev)
     value = world * tests_per_step * args.steps / (total_ms / 1e3)
@@ -741,14 +788,11 @@ def run_gpu(args) -> dict:
         "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded PCG64, seed 1002 + 1000*rank)",
-        "config": {"workload": WORKLOAD, "queries_per_step": n, "triangles": int(sum(m.n_tris for m in sc.meshes)),
-                   "tri_tests_per_step": int(tests_per_step), "colliding_pairs_per_step": int(pairs_per_step),
-                   "contacts_per_step": int(st["contacts"]), "rays_per_step": int(rays_per_step),
-                   "node_pairs_per_step": int(st["node_pairs"]), "cache": "L2 flushed (512 MB write) between steps",
-                   "launch": "CUDA graph: init + pack + persistent traversal + persistent narrow phase + "
-                             "contact accumulate + contact/ray emit",
-                   "lanes_per_step": st["node_pairs"] / max(1, st["warp_steps"]),
-                   "autotune": tune},
+        "config": scene_config(n, sum(m.n_tris for m in sc.meshes), tests_per_step, rays_per_step),
+        "step": {"launch": STEP_FLAGS_DOC, "colliding_pairs": int(pairs_per_step), "contacts": int(st["contacts"]),
+                 "node_pairs": int(st["node_pairs"]), "lanes_per_traversal_step": st["node_pairs"] / max(1, st["warp_steps"]),
+                 "autotune": tune},
+        "recheck": recheck,
         "queries_per_s": world * n * args.steps / (total_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(n * capi.QUERY_DTYPE.itemsize),
                 "d2h_bytes_per_step": int(COUNTERS_BYTES + pairs_per_step * capi.TRI_PAIR_DTYPE.itemsize

@@ -575,15 +575,24 @@ int cg_frame_callbacks(const cg_frame_result* results, uint64_t n_results, const
  * so calls whose work overlaps on the device (any context, any stream) race:
  * order them on one stream or wait for one before launching the next.
  *
+ * The set-up is per process and device: a cudaDeviceReset, which ends every
+ * context of this library anyway, also ends it, and the entry point is not
+ * usable in that process afterwards.
+ *
  * Limits: n <= CG_STATIC_MAX_QUERIES (else CG_ERR_INVALID_ARGUMENT, nothing
  * launched); at most CG_STATIC_MAX_LEAF_PAIRS candidate leaf pairs per call
- * (else counts->status = CG_ERR_OUTPUT_OVERFLOW). Enqueued on `stream` (NULL =
- * the context's stream), no host synchronisation: *d_counts (device memory)
- * is valid once the stream reaches that point. Pairs beyond pairs_cap are
- * counted, not written. */
+ * (else counts->status = CG_ERR_OUTPUT_OVERFLOW); a work queue of at least
+ * 32,768 donated chunks of node pairs, as many as cg_collide's default
+ * queue_capacity (the traversal grid is narrowed when the context's would
+ * leave fewer), else counts->status = CG_ERR_QUEUE_OVERFLOW. Enqueued on
+ * `stream` (NULL = the context's stream), no host synchronisation: *d_counts
+ * (device memory) is valid once the stream reaches that point. Pairs beyond
+ * pairs_cap are counted, not written, and make the status
+ * CG_ERR_OUTPUT_OVERFLOW; a count-only call (d_pairs NULL, pairs_cap 0)
+ * reports the count with CG_OK. */
 #define CG_STATIC_MAX_QUERIES 1024u
 #define CG_STATIC_MAX_LEAF_PAIRS 131072u
-#define CG_STATIC_SCRATCH_BYTES 10649856u /* about 10.2 MiB */
+#define CG_STATIC_SCRATCH_BYTES 36012288u /* about 34.3 MiB */
 
 typedef struct cg_static_counts {
     uint64_t tri_pairs;  /* colliding triangle pairs found */

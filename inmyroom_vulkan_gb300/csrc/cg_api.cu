@@ -1415,8 +1415,8 @@ int cg_graph_launch(cg_ctx* c, void* stream) {
 // static device array (no allocation on the call's path).
 namespace {
 
-constexpr uint32_t kStaticSlots = 16384;     // work-queue chunk slots (ready flags + pool)
-constexpr uint32_t kStaticMinChunks = 1024;  // donated chunks a launch may always reserve
+constexpr uint32_t kStaticSlots = 65536;      // work-queue chunk slots (ready flags + pool)
+constexpr uint32_t kStaticMinChunks = 32768;  // donated chunks a launch may always reserve: cg_collide's default
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kOffReady = align256(sizeof(Counters));
 constexpr size_t kOffPool = kOffReady + align256(sizeof(unsigned int) * kStaticSlots);
@@ -1461,8 +1461,8 @@ __global__ void static_counts_kernel(const Counters* k, uint64_t pairs_cap, cg_s
         r.status = CG_ERR_QUEUE_OVERFLOW;
     else if (k->error & ERR_BAD_QUERY)
         r.status = CG_ERR_INVALID_ARGUMENT;
-    else if (k->n_leafs > CG_STATIC_MAX_LEAF_PAIRS || k->n_pairs > pairs_cap)
-        r.status = CG_ERR_OUTPUT_OVERFLOW;
+    else if (k->n_leafs > CG_STATIC_MAX_LEAF_PAIRS || (pairs_cap && k->n_pairs > pairs_cap))
+        r.status = CG_ERR_OUTPUT_OVERFLOW;  // a count-only call (no pair buffer) is not an overflow
     else
         r.status = CG_OK;
     *out = r;
@@ -1487,7 +1487,8 @@ extern "C" int cg_collide_static(cg_ctx* c, const cg_query* d_queries, uint32_t 
     auto* packed = reinterpret_cast<PackedQuery*>(base + kOffPacked);
 
     // The traversal grid is the context's, made smaller if its waiting warps
-    // would leave fewer than kStaticMinChunks slots for donations.
+    // would leave fewer than kStaticMinChunks slots for donations (the
+    // default grids leave more).
     const uint32_t wpb = c->cfg.warps_per_block;
     const uint32_t max_blocks = (kStaticSlots - kStaticMinChunks - 64u) / (9u * wpb);
     const uint32_t blocks = std::min(c->blocks, max_blocks);

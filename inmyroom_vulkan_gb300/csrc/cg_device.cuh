@@ -238,7 +238,7 @@ __device__ __forceinline__ bool uncertain(float d, float bound) {
 }
 __device__ __forceinline__ int class32(float d) { return tiny(d) ? 0 : (d > 0.0f ? 1 : -1); }
 __device__ __forceinline__ int class64(double d) { return fabs(d) < 1e-6 ? 0 : (d > 0.0 ? 1 : -1); }
-__device__ __noinline__ double orient64(float3 a0, float3 a1, float3 a2, float3 p) {
+static __device__ __noinline__ double orient64(float3 a0, float3 a1, float3 a2, float3 p) {
     const double e1x = double(a1.x) - double(a0.x), e1y = double(a1.y) - double(a0.y), e1z = double(a1.z) - double(a0.z);
     const double e2x = double(a2.x) - double(a0.x), e2y = double(a2.y) - double(a0.y), e2z = double(a2.z) - double(a0.z);
     const double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;

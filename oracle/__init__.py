@@ -28,6 +28,7 @@ REF_ROOT_DEFAULT = "/root/reference"
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
 
 
 def build_port() -> None:
@@ -76,7 +77,7 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
         f("narrow").restype = sz
         f("narrow").argtypes = [vp, _u32p, _f32p, sz, C.POINTER(C.c_uint64)]
         f("collide_batch").restype = C.c_uint64
-        f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int, C.POINTER(C.c_uint64)]
+        f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int, C.POINTER(C.c_uint64), _u64p]
     else:
         f("narrow").restype = sz
         f("narrow").argtypes = [vp, _u32p, _f32p, sz, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
@@ -90,7 +91,7 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
         f("contacts_iter").argtypes = [vp, C.c_int, _u32p, _u32p, _f32p, sz]
         f("collide_batch").restype = C.c_uint64
         f("collide_batch").argtypes = [vp, vp, _f32p, _f32p, sz, C.c_int,
-                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _u64p]
         f("deform").argtypes = [sz, sz, sz, sz, _f32p, _f32p, vp, _f32p, _f32p, _f32p, _f32p]
         f("tree_refit").argtypes = [sz, _u32p, _u32p, sz, _u32p, _f32p, sz, _f32p, _f32p, _f32p]
         f("collide_pairs").restype = sz
@@ -150,9 +151,11 @@ class Tree:
             pass
 
     def sizes(self):
-        n, t = C.c_size_t(), C.c_size_t()
-        self.impl.fn("tree_sizes")(self.h, C.byref(n), C.byref(t))
-        return n.value, t.value
+        if getattr(self, "_sizes", None) is None:
+            n, t = C.c_size_t(), C.c_size_t()
+            self.impl.fn("tree_sizes")(self.h, C.byref(n), C.byref(t))
+            self._sizes = (n.value, t.value)
+        return self._sizes
 
     def export(self) -> FlatTree:
         n, t = self.sizes()
@@ -335,17 +338,23 @@ class Impl:
         return v.reshape(3, 3), d
 
     def collide_batch(self, trees_a, trees_b, mats_a, mats_b, threads=1):
+        """The whole per-pair path (mid phase, triangle tests, contacts, rays)
+        of a batch on `threads` host threads, which take the queries largest
+        first (by the product of the trees' triangle counts) from a shared
+        counter."""
         n = len(trees_a)
         ha = (C.c_void_p * n)(*[t.h for t in trees_a])
         hb = (C.c_void_p * n)(*[t.h for t in trees_b])
         ma = _f32(mats_a)
         mb = _f32(mats_b)
+        cost = np.array([float(a.sizes()[1]) * float(b.sizes()[1]) for a, b in zip(trees_a, trees_b)])
+        order = np.ascontiguousarray(np.argsort(-cost, kind="stable"), np.uint64)
         rays = C.c_uint64()
         if self.prefix == "ref_":
-            tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(rays))
+            tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(rays), order)
             return dict(tests=tests, rays=rays.value)
         hits = C.c_uint64()
-        tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(hits), C.byref(rays))
+        tests = self.fn("collide_batch")(ha, hb, ma, mb, n, threads, C.byref(hits), C.byref(rays), order)
         return dict(tests=tests, hits=hits.value, rays=rays.value)
 
     def shoot_rays(self, ta: "Tree", tb: "Tree", ga, gb, rays_a, rays_b, params=None) -> np.ndarray:

@@ -8,6 +8,7 @@
 // triangle pairs and segments are bit-identical to the reference compiled
 // against the same glm-convention shim. The C ABI mirrors oracle/ref_capi.cpp
 // with a port_ prefix.
+#include <atomic>
 #include <algorithm>
 #include <array>
 #include <cstring>
@@ -1435,11 +1436,16 @@ void port_eig3(const double* a9, double* v9, double* d3) {
 // triangle-pair tests; *n_hits receives the number of colliding pairs and
 // *n_rays the number of uncollide rays.
 uint64_t port_collide_batch(void* const* trees_a, void* const* trees_b, const float* mats_a, const float* mats_b,
-                            size_t n, int threads, uint64_t* n_hits, uint64_t* n_rays) {
+                            size_t n, int threads, uint64_t* n_hits, uint64_t* n_rays, const uint64_t* order) {
     threads = std::max(1, threads);
     std::vector<uint64_t> tests(threads, 0), hits(threads, 0), rays(threads, 0);
+    // Each thread takes the next query of `order` (the caller's: largest
+    // first) from a shared counter (costs differ by orders of magnitude: a
+    // fixed split leaves threads idle).
+    std::atomic<size_t> next{0};
     auto work = [&](int tid) {
-        for (size_t q = size_t(tid); q < n; q += size_t(threads)) {
+        for (size_t k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+            const size_t q = order ? size_t(order[k]) : k;
             Query qr;
             run_query(*static_cast<const Tree*>(trees_a[q]), *static_cast<const Tree*>(trees_b[q]),
                       ldm(mats_a + 16 * q), ldm(mats_b + 16 * q), qr, true, true);

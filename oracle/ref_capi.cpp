@@ -4,6 +4,7 @@
 // eig3/eig3.cpp) against the glm shim. Tests use it to pin the C++ restatement
 // in oracle/port and to make golden fixtures; it only exists where the
 // reference sources are present.
+#include <atomic>
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -302,13 +303,19 @@ void ref_eig3(const double* a9, double* v9, double* d3) {
 // number of triangle-pair tests the narrow phase ran (sum of leaf-pair count
 // products); *n_rays receives the total number of uncollide rays.
 uint64_t ref_collide_batch(void* const* trees_a, void* const* trees_b, const float* mats_a, const float* mats_b,
-                           size_t n, int threads, uint64_t* n_rays) {
+                           size_t n, int threads, uint64_t* n_rays, const uint64_t* order) {
     threads = std::max(1, threads);
     std::vector<uint64_t> tests(threads, 0), rays(threads, 0);
+    // Each thread takes the next query of `order` (the caller's: largest
+    // first) from a shared counter: the cost of a query varies by orders of
+    // magnitude, so a fixed split of the list leaves threads idle while one
+    // finishes its share.
+    std::atomic<size_t> next{0};
     auto work = [&](int tid) {
         OBBtreesCollision mid;
         CreateUncollideRays narrow;
-        for (size_t q = size_t(tid); q < n; q += size_t(threads)) {
+        for (size_t k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+            const size_t q = order ? size_t(order[k]) : k;
             std::pair<CollisionDetectionEntry, CollisionDetectionEntry> p;
             p.first.currentGlobalMatrix = p.first.previousGlobalMatrix = load_mat(mats_a + 16 * q);
             p.first.OBBtree_ptr = static_cast<const OBBtree*>(trees_a[q]);
