@@ -225,6 +225,14 @@ typedef struct cg_stats {
  * robust verdict that can differ from the reference's on those tests. */
 #define CG_RECHECK 32u
 #define CG_ROBUST 64u
+/* With CG_KEEP_LEAF_PAIRS: cg_read_leaf_pairs returns the candidate leaf pairs
+ * grouped by query and, within a query, in the order the reference's
+ * recursion emits them (OBBtree::IntersectOBBtreesRecursive,
+ * src/Geometry/OBBtree.cpp:414-476: the order of their paths from the root
+ * pair, left before right), the exact vector ExecuteOBBtreesCollision
+ * returns. Each leaf pair's path is found on the device; a path of 128 or
+ * more splits makes the launch CG_ERR_OUTPUT_OVERFLOW. */
+#define CG_DFS_ORDER 128u
 
 /* Per-triangle contact record, the TriangleCandidateRays of
  * CreateUncollideRays.cpp:14-58 after the merge: bit k of mask set = vertex k
@@ -270,6 +278,8 @@ int cg_collide_async(cg_ctx* ctx, const cg_query* d_queries, uint32_t n, uint32_
 /* Waits for the last launch and reads its statistics. */
 int cg_sync_stats(cg_ctx* ctx, cg_stats* stats);
 int cg_read_tri_pairs(cg_ctx* ctx, cg_tri_pair* out, uint64_t cap, uint64_t* n);
+/* Candidate leaf pairs of the last launch made with CG_KEEP_LEAF_PAIRS: in no
+ * fixed order, or in the reference's order with CG_DFS_ORDER. */
 int cg_read_leaf_pairs(cg_ctx* ctx, cg_leaf_pair* out, uint64_t cap, uint64_t* n);
 /* Device pointers to the last launch's results (valid until the next launch). */
 int cg_device_results(cg_ctx* ctx, const cg_tri_pair** pairs, const unsigned long long** pair_count);

@@ -1,87 +1,70 @@
-// Drop-in GPU mid phase for the inMyRoom_vulkan engine, header-only C++ over
-// the C ABI of include/collide_gpu.h. It is compiled inside the engine (it
-// uses the engine's OBBtree, CollisionDetectionEntry and glm types) and sits
-// beside OBBtreesCollision (include/CollisionDetection/OBBtreesCollision.h):
+// Drop-in GPU mid and narrow phase for the inMyRoom_vulkan engine, header-only
+// C++ over the C ABI of include/collide_gpu.h (through cg_session.h). It is
+// compiled inside the engine (it uses the engine's OBBtree,
+// CollisionDetectionEntry, Ray and glm types) and sits beside the CPU classes
+// that CollisionDetection owns (include/CollisionDetection/CollisionDetection.h:
+// 29-32):
 //
-//   OBBtreesCollision::ExecuteOBBtreesCollision(pair)      (CPU, one pair)
-//   GpuOBBtreesCollision::ExecuteOBBtreesCollision(pair)   (GPU, same result)
-//   GpuOBBtreesCollision::ExecuteOBBtreesCollisionBatch(pairs)
-//                                   (GPU, every pair of a frame in one launch)
+//   OBBtreesCollision::ExecuteOBBtreesCollision(pair)           (CPU, one pair)
+//   GpuOBBtreesCollision::ExecuteOBBtreesCollision(pair)        (GPU, same result)
+//   GpuOBBtreesCollision::ExecuteOBBtreesCollisionBatch(pairs)  (GPU, one launch)
 //
-// The candidate leaf pairs are the same set as the CPU call returns; within a
-// pair's vector they are sorted by (first offset, second offset) instead of
-// the CPU recursion order. Trees are uploaded on first use, keyed by the
-// OBBtree pointer; call ForgetTree when an OBBtree is destroyed.
+//   CreateUncollideRays::ExecuteCreateUncollideRays(pair_tris)        (CPU)
+//   GpuCreateUncollideRays::ExecuteCreateUncollideRays(pair_tris)     (GPU, same result)
+//   GpuCreateUncollideRays::ExecuteCreateUncollideRaysBatch(...)      (GPU, one launch)
+//
+// Results are the CPU calls' bit for bit and in their order: the candidate
+// leaf pairs in the recursion's order, the rays in the order the CPU's
+// per-triangle unordered_map gives them (GCC's libstdc++), the mean origins.
+// The GPU narrow phase runs the mid phase of the pair again in the same
+// launch (it does not read the CDentriesPairTrianglesPairs' leaf pairs), so
+// its result is the CPU's for the leaf pairs the engine passes: those of the
+// pair's own mid phase in their order (CollisionDetection.cpp:49-67).
+//
+// Both adapters can share one GpuCollisionContext (its trees are uploaded on
+// first use, keyed by the OBBtree pointer; call ForgetTree when an OBBtree is
+// destroyed).
 #pragma once
 
 #include <algorithm>
-#include <stdexcept>
-#include <string>
+#include <memory>
 #include <unordered_map>
 #include <utility>
 #include <vector>
 
+#include "CollisionDetection/CreateUncollideRays.h"
 #include "CollisionDetection/OBBtreesCollision.h"
 #include "Geometry/OBBtree.h"
+#include "Geometry/Ray.h"
+#include "cg_session.h"
 #include "collide_gpu.h"
 #include "glm/gtc/type_ptr.hpp"
 
-class GpuOBBtreesCollision {
+class GpuCollisionContext {
 public:
-    explicit GpuOBBtreesCollision(const cg_config* cfg = nullptr) {
-        const int rc = cg_create(cfg, &ctx_);
-        if (rc != CG_OK) throw std::runtime_error(std::string("cg_create: ") + cg_status_string(rc));
-    }
-    ~GpuOBBtreesCollision() { cg_destroy(ctx_); }
-    GpuOBBtreesCollision(const GpuOBBtreesCollision&) = delete;
-    GpuOBBtreesCollision& operator=(const GpuOBBtreesCollision&) = delete;
+    explicit GpuCollisionContext(const cg_config* cfg = nullptr) : session_(cfg) {}
 
-    // Same signature and result as OBBtreesCollision::ExecuteOBBtreesCollision.
-    CDentriesPairTrianglesPairs ExecuteOBBtreesCollision(
-        const std::pair<CollisionDetectionEntry, CollisionDetectionEntry>& entries) const {
-        return ExecuteOBBtreesCollisionBatch({entries}).front();
-    }
+    const cg_adapter::Session& Session() const { return session_; }
 
-    std::vector<CDentriesPairTrianglesPairs> ExecuteOBBtreesCollisionBatch(
-        const std::vector<std::pair<CollisionDetectionEntry, CollisionDetectionEntry>>& pairs) const {
-        std::vector<cg_query> queries(pairs.size());
-        for (size_t i = 0; i < pairs.size(); ++i) {
-            queries[i].tree_a = TreeId(pairs[i].first.OBBtree_ptr);
-            queries[i].tree_b = TreeId(pairs[i].second.OBBtree_ptr);
-            // the relative matrix of OBBtreesCollision.cpp:15, with the engine's glm
-            const glm::mat4 rel =
-                glm::inverse(pairs[i].first.currentGlobalMatrix) * pairs[i].second.currentGlobalMatrix;
-            std::copy(glm::value_ptr(rel), glm::value_ptr(rel) + 16, queries[i].relative);
-        }
-        cg_stats st;
-        Check(cg_collide(ctx_, queries.data(), uint32_t(queries.size()), CG_KEEP_LEAF_PAIRS | CG_MID_ONLY, &st));
-        std::vector<cg_leaf_pair> leafs(st.leaf_pairs);
-        uint64_t n = 0;
-        Check(cg_read_leaf_pairs(ctx_, leafs.data(), leafs.size(), &n));
-        std::sort(leafs.begin(), leafs.end(), [](const cg_leaf_pair& a, const cg_leaf_pair& b) {
-            return a.query != b.query ? a.query < b.query
-                                      : (a.offset_a != b.offset_a ? a.offset_a < b.offset_a : a.offset_b < b.offset_b);
-        });
-        std::vector<CDentriesPairTrianglesPairs> out(pairs.size());
-        for (size_t i = 0; i < pairs.size(); ++i) {
-            out[i].firstEntry = pairs[i].first;
-            out[i].secondEntry = pairs[i].second;
-        }
-        for (const cg_leaf_pair& lp : leafs)
-            out[lp.query].OBBtreesIntersectInfoObj.candidateTriangleRangeCombinations.push_back(
-                {size_t(lp.offset_a), size_t(lp.count_a), size_t(lp.offset_b), size_t(lp.count_b)});
-        return out;
+    // The query of an entity pair: both trees' ids and the relative matrix of
+    // OBBtreesCollision.cpp:15 / CreateUncollideRays.cpp:62-63, with the
+    // engine's glm.
+    cg_query Query(const CollisionDetectionEntry& first, const CollisionDetectionEntry& second) const {
+        cg_query q;
+        q.tree_a = TreeId(first.OBBtree_ptr);
+        q.tree_b = TreeId(second.OBBtree_ptr);
+        const glm::mat4 rel = glm::inverse(first.currentGlobalMatrix) * second.currentGlobalMatrix;
+        std::copy(glm::value_ptr(rel), glm::value_ptr(rel) + 16, q.relative);
+        return q;
     }
 
     void ForgetTree(const OBBtree* tree) {
         auto it = ids_.find(tree);
         if (it != ids_.end()) {
-            cg_tree_free(ctx_, it->second);
+            session_.Free(it->second);
             ids_.erase(it);
         }
     }
-
-    cg_ctx* Context() const { return ctx_; }
 
     // Uploads `tree` (once) and returns its id. The flat view is exported
     // through the public OBBtreeTraveler walk: inner nodes in pre-order get
@@ -121,8 +104,7 @@ public:
         view.triangles_position = pos.data();
         view.triangles_normal = nrm.data();
         view.triangles_indices = idx.data();
-        uint32_t id = 0;
-        Check(cg_tree_upload(ctx_, &view, &id));
+        const uint32_t id = session_.Upload(view);
         ids_.emplace(tree, id);
         return id;
     }
@@ -162,14 +144,78 @@ private:
         }
     }
 
-    void Check(int rc) const {
-        if (rc != CG_OK) {
-            char buf[512];
-            cg_last_error(ctx_, buf, sizeof(buf));
-            throw std::runtime_error(std::string(cg_status_string(rc)) + ": " + buf);
-        }
+    cg_adapter::Session session_;
+    mutable std::unordered_map<const OBBtree*, uint32_t> ids_;
+};
+
+class GpuOBBtreesCollision {
+public:
+    explicit GpuOBBtreesCollision(const cg_config* cfg = nullptr)
+        : ctx_(std::make_shared<GpuCollisionContext>(cfg)) {}
+    explicit GpuOBBtreesCollision(std::shared_ptr<GpuCollisionContext> ctx) : ctx_(std::move(ctx)) {}
+
+    // Same signature and result as OBBtreesCollision::ExecuteOBBtreesCollision.
+    CDentriesPairTrianglesPairs ExecuteOBBtreesCollision(
+        const std::pair<CollisionDetectionEntry, CollisionDetectionEntry>& entries) const {
+        return ExecuteOBBtreesCollisionBatch({entries}).front();
     }
 
-    cg_ctx* ctx_ = nullptr;
-    mutable std::unordered_map<const OBBtree*, uint32_t> ids_;
+    std::vector<CDentriesPairTrianglesPairs> ExecuteOBBtreesCollisionBatch(
+        const std::vector<std::pair<CollisionDetectionEntry, CollisionDetectionEntry>>& pairs) const {
+        std::vector<cg_query> queries(pairs.size());
+        for (size_t i = 0; i < pairs.size(); ++i) queries[i] = ctx_->Query(pairs[i].first, pairs[i].second);
+        const std::vector<std::vector<cg_leaf_pair>> leafs = ctx_->Session().MidPhase(queries);
+        std::vector<CDentriesPairTrianglesPairs> out(pairs.size());
+        for (size_t i = 0; i < pairs.size(); ++i) {
+            out[i].firstEntry = pairs[i].first;
+            out[i].secondEntry = pairs[i].second;
+            auto& v = out[i].OBBtreesIntersectInfoObj.candidateTriangleRangeCombinations;
+            for (const cg_leaf_pair& lp : leafs[i])
+                v.push_back({size_t(lp.offset_a), size_t(lp.count_a), size_t(lp.offset_b), size_t(lp.count_b)});
+        }
+        return out;
+    }
+
+    void ForgetTree(const OBBtree* tree) { ctx_->ForgetTree(tree); }
+    cg_ctx* Context() const { return ctx_->Session().Context(); }
+    const std::shared_ptr<GpuCollisionContext>& Shared() const { return ctx_; }
+
+private:
+    std::shared_ptr<GpuCollisionContext> ctx_;
+};
+
+class GpuCreateUncollideRays {
+public:
+    explicit GpuCreateUncollideRays(const cg_config* cfg = nullptr)
+        : ctx_(std::make_shared<GpuCollisionContext>(cfg)) {}
+    explicit GpuCreateUncollideRays(std::shared_ptr<GpuCollisionContext> ctx) : ctx_(std::move(ctx)) {}
+
+    // Same signature and result as CreateUncollideRays::ExecuteCreateUncollideRays.
+    CDentriesUncollideRays ExecuteCreateUncollideRays(const CDentriesPairTrianglesPairs& pair_tris) const {
+        return ExecuteCreateUncollideRaysBatch({pair_tris}).front();
+    }
+
+    std::vector<CDentriesUncollideRays> ExecuteCreateUncollideRaysBatch(
+        const std::vector<CDentriesPairTrianglesPairs>& batch) const {
+        std::vector<cg_query> queries(batch.size());
+        for (size_t i = 0; i < batch.size(); ++i) queries[i] = ctx_->Query(batch[i].firstEntry, batch[i].secondEntry);
+        const std::vector<cg_adapter::QueryRays> rays = ctx_->Session().UncollideRays(queries);
+        std::vector<CDentriesUncollideRays> out(batch.size());
+        auto vec = [](const float* p) { return glm::vec3(p[0], p[1], p[2]); };
+        for (size_t i = 0; i < batch.size(); ++i) {
+            out[i].firstEntry = batch[i].firstEntry;
+            out[i].secondEntry = batch[i].secondEntry;
+            for (const cg_ray& r : rays[i].first) out[i].rays_from_first_to_second.emplace_back(vec(r.origin), vec(r.direction));
+            for (const cg_ray& r : rays[i].second) out[i].rays_from_second_to_first.emplace_back(vec(r.origin), vec(r.direction));
+            out[i].average_point_first_modelspace = vec(rays[i].average_first);
+            out[i].average_point_second_modelspace = vec(rays[i].average_second);
+        }
+        return out;
+    }
+
+    void ForgetTree(const OBBtree* tree) { ctx_->ForgetTree(tree); }
+    const std::shared_ptr<GpuCollisionContext>& Shared() const { return ctx_; }
+
+private:
+    std::shared_ptr<GpuCollisionContext> ctx_;
 };

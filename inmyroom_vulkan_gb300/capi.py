@@ -26,6 +26,7 @@ CG_MID_ONLY = 8
 CG_CONTACTS = 16
 CG_RECHECK = 32
 CG_ROBUST = 64
+CG_DFS_ORDER = 128
 
 # Every function the header declares (checked by the CPU tests).
 EXPORTS = ["cg_config_default", "cg_create", "cg_destroy", "cg_reconfigure", "cg_get_config", "cg_status_string",

@@ -53,6 +53,8 @@ void free_buffers(cg_ctx* c) {
     cudaFree(c->d_ready);
     cudaFree(c->d_pairs);
     cudaFree(c->d_leafs);
+    cudaFree(c->d_leaf_keys);
+    c->d_leaf_keys = nullptr;
     cudaFree(c->d_trace);
     auto& t = c->ct;
     for (void* p : {(void*)t.pair_aux, (void*)t.table, (void*)t.occupied, (void*)t.pg_geom, (void*)t.pg_link,
@@ -408,6 +410,18 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t1, s, rec_flags), "timing event");
     if (n) CG_CUDA(launch_narrow(np, c->narrow_blocks, 8, s), "narrow-phase kernel");
     CG_CUDA(cudaEventRecordWithFlags(c->ev_t2, s, rec_flags), "timing event");
+    if ((flags & CG_DFS_ORDER) && n) {
+        LeafKeyParams kp{};
+        kp.q = c->d_packed;
+        kp.trees = c->d_trees;
+        kp.recs = c->recs.ptr;
+        kp.leaf_list = c->d_leaf_list;
+        kp.n_leafs = &c->d_ctr->n_leafs;
+        kp.leaf_cap = p.leaf_cap;
+        kp.error = &c->d_ctr->error;
+        kp.keys = c->d_leaf_keys;
+        CG_CUDA(launch_leaf_keys(kp, c->contact_blocks, s), "leaf-pair key kernel");
+    }
     if (pairs_copy) {
         CG_CUDA(cudaEventRecord(c->ev_fork, s), "fork event");
         CG_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
@@ -485,6 +499,9 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
         status = fail(c, CG_ERR_QUEUE_OVERFLOW, "node-pair queue full (queue_capacity %u)", c->cfg.queue_capacity);
     else if (k.error & ERR_BAD_QUERY)
         status = fail(c, CG_ERR_INVALID_ARGUMENT, "a query names an unknown tree");
+    else if (k.error & ERR_DEEP)
+        status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "CG_DFS_ORDER: a leaf pair deeper than 127 splits of the "
+                      "simultaneous descent");
     else if (k.n_leafs > c->cfg.max_leaf_pairs)
         status = fail(c, CG_ERR_OUTPUT_OVERFLOW, "%llu candidate leaf pairs, max_leaf_pairs %llu: triangle tests "
                       "incomplete", (unsigned long long)k.n_leafs, (unsigned long long)c->cfg.max_leaf_pairs);
@@ -510,6 +527,13 @@ int stats_from(cg_ctx* c, const Counters& k, cg_stats* st) {
 }
 
 int check_flags(cg_ctx* c, uint32_t flags) {
+    if (flags & CG_DFS_ORDER) {
+        if (!(flags & CG_KEEP_LEAF_PAIRS) || !c->d_leafs)
+            return fail(c, CG_ERR_INVALID_ARGUMENT, "CG_DFS_ORDER orders the kept leaf pairs: it needs "
+                        "CG_KEEP_LEAF_PAIRS and max_leaf_pairs > 0");
+        if (!c->d_leaf_keys)
+            CG_CUDA(cudaMalloc(&c->d_leaf_keys, sizeof(ulonglong2) * c->cfg.max_leaf_pairs), "alloc leaf-pair keys");
+    }
     if (!(flags & CG_CONTACTS)) return CG_OK;
     if (!c->cfg.max_contacts) return fail(c, CG_ERR_INVALID_ARGUMENT, "CG_CONTACTS needs max_contacts > 0");
     if (flags & (CG_NO_TRI_PAIRS | CG_MID_ONLY))
@@ -1042,7 +1066,25 @@ int cg_read_leaf_pairs(cg_ctx* c, cg_leaf_pair* out, uint64_t cap, uint64_t* n) 
     const uint64_t avail = std::min<uint64_t>(c->h_ctr->n_leafs, c->d_leafs ? c->cfg.max_leaf_pairs : 0);
     *n = c->h_ctr->n_leafs;
     const uint64_t m = std::min(avail, cap);
-    if (m) CG_CUDA(cudaMemcpy(out, c->d_leafs, sizeof(cg_leaf_pair) * m, cudaMemcpyDeviceToHost), "read leaf pairs");
+    if (m && (c->last_flags & CG_DFS_ORDER)) {
+        // grouped by query, each query's in the order of its descent path
+        std::vector<cg_leaf_pair> all(avail);
+        std::vector<ulonglong2> keys(avail);
+        CG_CUDA(cudaMemcpy(all.data(), c->d_leafs, sizeof(cg_leaf_pair) * avail, cudaMemcpyDeviceToHost),
+                "read leaf pairs");
+        CG_CUDA(cudaMemcpy(keys.data(), c->d_leaf_keys, sizeof(ulonglong2) * avail, cudaMemcpyDeviceToHost),
+                "read leaf-pair keys");
+        std::vector<uint32_t> order(avail);
+        for (uint32_t i = 0; i < avail; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+            if (all[x].query != all[y].query) return all[x].query < all[y].query;
+            if (keys[x].x != keys[y].x) return keys[x].x < keys[y].x;
+            return keys[x].y < keys[y].y;
+        });
+        for (uint64_t i = 0; i < m; ++i) out[i] = all[order[i]];
+    } else if (m) {
+        CG_CUDA(cudaMemcpy(out, c->d_leafs, sizeof(cg_leaf_pair) * m, cudaMemcpyDeviceToHost), "read leaf pairs");
+    }
     return c->h_ctr->n_leafs > avail ? CG_ERR_OUTPUT_OVERFLOW : CG_OK;
 }
 

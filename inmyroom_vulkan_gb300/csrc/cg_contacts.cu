@@ -295,19 +295,19 @@ __device__ __forceinline__ WalkRec walk_rec(const float4* recs, uint32_t r) {
 // boxes: the first tree's when its surface is at least the second's as
 // transformed; else the inner one), then the child whose subtree holds the
 // leaf (bit 0 left, 1 right). Left-aligned in 128 bits; *depth = splits.
-__device__ void descent_path(const ContactParams& P, uint32_t leaf_i, unsigned long long& hi, unsigned long long& lo,
-                             uint32_t& depth) {
-    const uint4 lp = P.leaf_list[leaf_i];  // (query, first triangle a, first triangle b, counts)
-    const PackedQuery* Q = P.q + lp.x;
-    const DevTree* TA = P.trees + __ldg(&Q->tree_a);
-    const DevTree* TB = P.trees + __ldg(&Q->tree_b);
+__device__ void descent_path(const PackedQuery* queries, const DevTree* trees, const float4* recs, uint4 lp,
+                             unsigned long long& hi, unsigned long long& lo, uint32_t& depth) {
+    // lp: (query, first triangle a, first triangle b, counts), arena indices
+    const PackedQuery* Q = queries + lp.x;
+    const DevTree* TA = trees + __ldg(&Q->tree_a);
+    const DevTree* TB = trees + __ldg(&Q->tree_b);
     const uint32_t base_a = TA->rec_base, base_b = TB->rec_base;
     const uint2* rg_a = TA->ranges;
     const uint2* rg_b = TB->ranges;
     const uint32_t ta = lp.y - TA->tri_base, tb = lp.z - TB->tri_base;
     const Mat4 M = query_mat(Q);
-    WalkRec A = walk_rec(P.recs, base_a + 1u);
-    WalkRec B = walk_rec(P.recs, base_b + 1u);
+    WalkRec A = walk_rec(recs, base_a + 1u);
+    WalkRec B = walk_rec(recs, base_b + 1u);
     float sb = surface(xform_box(M, B.box));
     hi = lo = 0ull;
     depth = 0;
@@ -323,9 +323,9 @@ __device__ void descent_path(const ContactParams& P, uint32_t leaf_i, unsigned l
         lo = (lo << 1) | bit;
         ++depth;
         if (split_a) {
-            A = walk_rec(P.recs, left + bit);
+            A = walk_rec(recs, left + bit);
         } else {
-            B = walk_rec(P.recs, left + bit);
+            B = walk_rec(recs, left + bit);
             sb = surface(xform_box(M, B.box));
         }
     }
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(256) contacts_fold_kernel(const ContactParams 
         if (cur != ~0u) close();
         if (!have) continue;  // only pairs of zero length: no record (IsNull)
         ContactElem E;
-        descent_path(P, first_leaf, E.key_hi, E.key_lo, E.depth);
+        descent_path(P.q, P.trees, P.recs, P.leaf_list[first_leaf], E.key_hi, E.key_lo, E.depth);
         if (E.depth >= 128u) atomicOr(&P.ctr->c_overflow, CONTACT_ORDER);
         E.sx = ax;
         E.sy = ay;
@@ -905,6 +905,27 @@ __global__ void __launch_bounds__(256) copy_out_kernel(const CopyOutParams P) {
 
 cudaError_t launch_copy_out(const CopyOutParams& p, uint32_t blocks, cudaStream_t s) {
     copy_out_kernel<<<blocks, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// The descent path of every stored candidate leaf pair (CG_DFS_ORDER), for
+// reading them back in the reference's depth-first order: keys[i] = (path
+// high 64 bits, path low 64 bits) of leaf pair i; ERR_DEEP in *error when a
+// path has 128 or more splits.
+__global__ void __launch_bounds__(256) leaf_keys_kernel(const LeafKeyParams P) {
+    const unsigned long long n_all = *reinterpret_cast<const volatile unsigned long long*>(P.n_leafs);
+    const uint32_t n = uint32_t(n_all < P.leaf_cap ? n_all : P.leaf_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned long long hi, lo;
+        uint32_t depth;
+        descent_path(P.q, P.trees, P.recs, P.leaf_list[i], hi, lo, depth);
+        if (depth >= 128u) atomicOr(P.error, ERR_DEEP);
+        P.keys[i] = make_ulonglong2(hi, lo);
+    }
+}
+
+cudaError_t launch_leaf_keys(const LeafKeyParams& p, uint32_t grid, cudaStream_t s) {
+    leaf_keys_kernel<<<grid, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -136,6 +136,7 @@ struct cg_ctx {
     uint4* d_leaf_list = nullptr;   // candidate leaf pairs between the two kernels
     cg_tri_pair* d_pairs = nullptr;
     cg_leaf_pair* d_leafs = nullptr;
+    ulonglong2* d_leaf_keys = nullptr;  // CG_DFS_ORDER: each leaf pair's descent path (allocated on first use)
     unsigned int* d_trace = nullptr;
     uint32_t trace_ns = 0;
 

@@ -95,7 +95,7 @@ struct Counters {
 
 enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ORDER = 8u };
 
-enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u };
+enum : unsigned int { ERR_TIMEOUT = 1u, ERR_QUEUE = 2u, ERR_BAD_QUERY = 4u, ERR_DEEP = 8u };
 
 // Contacts and rays (cg_contacts.cu). A slot of the contact table names one
 // triangle of one side of one query that has colliding pairs; its pairs'
@@ -172,6 +172,19 @@ struct ContactParams {
 };
 
 cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s);
+
+// Descent paths of the stored candidate leaf pairs (CG_DFS_ORDER).
+struct LeafKeyParams {
+    const PackedQuery* q;
+    const DevTree* trees;
+    const float4* recs;
+    const uint4* leaf_list;
+    const unsigned long long* n_leafs;  // the launch's count (device)
+    uint32_t leaf_cap;
+    unsigned* error;                    // ERR_DEEP when a path is too deep for 128 bits
+    ulonglong2* keys;                   // per leaf pair: path high, low
+};
+cudaError_t launch_leaf_keys(const LeafKeyParams& p, uint32_t grid, cudaStream_t s);
 
 // Results of a step written to host buffers (cg_set_host_outputs).
 struct CopyOutParams {

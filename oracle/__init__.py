@@ -23,7 +23,10 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT_DEFAULT = "/root/reference"
+# The reference checkout: $INMYROOM_REFERENCE, else its usual place in this
+# build's container. Absent on machines without it (the compiled reference and
+# the tests that read its sources are then skipped).
+REF_ROOT_DEFAULT = os.environ.get("INMYROOM_REFERENCE", "/root/reference")
 
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")

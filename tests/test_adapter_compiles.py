@@ -9,7 +9,7 @@ import pytest
 
 from inmyroom_vulkan_gb300 import build
 
-REF = "/root/reference"
+from oracle import REF_ROOT_DEFAULT as REF
 IMR = os.path.join(REF, "inMyRoom_vulkan")
 ROOT = build.ROOT
 
@@ -23,9 +23,12 @@ def test_adapter_builds_against_reference_headers(tmp_path):
         "int main(int argc, char**) {\n"
         "    if (argc < 0) {  // never runs: this program only has to build and link\n"
         "        GpuOBBtreesCollision gpu;\n"
+        "        GpuCreateUncollideRays rays(gpu.Shared());\n"
         "        std::pair<CollisionDetectionEntry, CollisionDetectionEntry> p{};\n"
         "        CDentriesPairTrianglesPairs r = gpu.ExecuteOBBtreesCollision(p);\n"
-        "        return int(r.OBBtreesIntersectInfoObj.candidateTriangleRangeCombinations.size());\n"
+        "        CDentriesUncollideRays u = rays.ExecuteCreateUncollideRays(r);\n"
+        "        return int(r.OBBtreesIntersectInfoObj.candidateTriangleRangeCombinations.size() +\n"
+        "                   u.rays_from_first_to_second.size());\n"
         "    }\n"
         "    return 0;\n"
         "}\n")

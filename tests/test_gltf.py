@@ -9,8 +9,9 @@ import numpy as np
 import pytest
 
 from inmyroom_vulkan_gb300 import gltf, scenes
+from oracle import REF_ROOT_DEFAULT
 
-SNAKE = "/root/reference/inMyRoom_vulkan/testGames/SnakeGame"
+SNAKE = os.path.join(REF_ROOT_DEFAULT, "inMyRoom_vulkan", "testGames", "SnakeGame")
 
 
 def test_triplets_by_mode():

@@ -243,3 +243,28 @@ def test_large_leaves_bit_exact(gpu_ctx, port):
     assert np.array_equal(gpu_pair_table(gpu_ctx.tri_pairs()), pair_table(pairs[:, 0], pairs[:, 1], pairs[:, 2], segs))
     for i in ids:
         gpu_ctx.free_tree(i)
+
+
+def test_leaf_pairs_in_the_reference_order(gpu_ctx, port):
+    """CG_DFS_ORDER: every query's candidate leaf pairs in the order the
+    reference's recursion emits them (OBBtree.cpp:414-476), on the scene."""
+    sc = scenes.scene()
+    tp = [port.tree_build(m.points, m.indices, m.normals) for m in sc.meshes]
+    ids = np.array([gpu_ctx.upload_flat(t.export()) for t in tp], np.uint32)
+    qa, qb = sc.pairs[:, 0], sc.pairs[:, 1]
+    rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
+    q = capi.make_queries(ids[qa], ids[qb], rel)
+    with pytest.raises(capi.CgError):  # the order applies to kept leaf pairs
+        gpu_ctx.collide(q, flags=capi.CG_DFS_ORDER)
+    st = gpu_ctx.collide(q, flags=capi.CG_KEEP_LEAF_PAIRS | capi.CG_DFS_ORDER | capi.CG_MID_ONLY)
+    assert st["status"] == 0
+    lp = gpu_ctx.leaf_pairs()
+    assert len(lp) == st["leaf_pairs"] and np.all(np.diff(lp["query"].astype(np.int64)) >= 0)
+    starts = np.searchsorted(lp["query"], np.arange(len(q) + 1))
+    for k in range(len(q)):
+        want = port.mid_phase(tp[qa[k]], tp[qb[k]], sc.mats[qa[k]], sc.mats[qb[k]]).leaf_pairs()
+        g = lp[starts[k]:starts[k + 1]]
+        got = np.stack([g["offset_a"], g["count_a"], g["offset_b"], g["count_b"]], 1).astype(np.uint32)
+        assert np.array_equal(got, want.astype(np.uint32)), k
+    for i in ids:
+        gpu_ctx.free_tree(int(i))
