@@ -47,7 +47,7 @@ NODE_PAIR_BYTES = 2 * 48   # two boxes
 TRI_TEST_BYTES = 2 * 36    # two triangles
 NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
 TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
-COUNTERS_BYTES = 128       # the launch counters, read back by cg_collide and by each result read
+COUNTERS_BYTES = 144       # the launch counters, read back by cg_collide and by each result read
 # init, pack, traverse, narrow; contacts: pairs, scan, scatter, fold, order, offsets, emit
 STEP_KERNELS = 11
 STEP_FLAGS_DOC = ("CUDA graph: init + pack + persistent traversal + persistent narrow phase (FP64 recheck counted) "

@@ -20,9 +20,20 @@ candidate is timed with CUDA events over `reps` launches after `warmup`
 launches; a candidate that fails (queue overflow, a launch that does not fit)
 or whose triangle-test, leaf-pair and colliding-pair counts differ from the
 starting settings' is dropped, so a tuned launch computes the same sets.
+
+Cache: with `cache` (a JSON file path), results are kept per shape signature
+(the device's name and SM count, the batch's query count and flags, and a
+workload tag the caller gives, e.g. the scene's name). A later tuning of the
+same signature takes the stored settings after one check launch (its counts
+must equal the starting settings' and it must not fail) instead of
+searching; a missing, unreadable or mismatching entry is searched and written
+again.
 """
 from __future__ import annotations
 
+import json
+import os
+import tempfile
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -51,9 +62,61 @@ class Result:
     start_ms: float
     trials: list = field(default_factory=list)
 
+    cached: bool = False
+
     def as_dict(self) -> dict:
         return {"best": self.best, "best_ms": self.best_ms, "start_ms": self.start_ms,
-                "trials": len(self.trials), "dropped": sum(t.ms is None for t in self.trials)}
+                "trials": len(self.trials), "dropped": sum(t.ms is None for t in self.trials), "cached": self.cached}
+
+
+def load_cache(path: str) -> dict:
+    """The cache's entries, or {} when the file is missing or unreadable."""
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d if isinstance(d, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def store_cache(path: str, signature: str, res: Result, space: dict) -> None:
+    """Writes (atomically: a temporary file renamed over the old one) the
+    entry of `signature`, keeping the others."""
+    entries = load_cache(path)
+    entries[signature] = {"best": res.best, "best_ms": res.best_ms, "start_ms": res.start_ms,
+                          "space": sorted(space)}
+    folder = os.path.dirname(os.path.abspath(path))
+    os.makedirs(folder, exist_ok=True)
+    fd, tmp = tempfile.mkstemp(dir=folder, suffix=".tmp")
+    with os.fdopen(fd, "w") as f:
+        json.dump(entries, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def cached_descent(measure, start: dict, space: dict, signature: str, cache: str | None, **kw) -> Result:
+    """coordinate_descent, or the cache's settings for `signature` when they
+    cover the same settings and one measurement of them succeeds."""
+    if cache:
+        e = load_cache(cache).get(signature)
+        if isinstance(e, dict) and e.get("space") == sorted(space) and isinstance(e.get("best"), dict) and \
+                set(e["best"]) == set(space):
+            try:
+                ms = float(measure(dict(e["best"])))
+                return Result(dict(e["best"]), ms, float(e.get("start_ms", ms)), [], cached=True)
+            except Exception:  # noqa: BLE001 - a stale entry is searched again
+                pass
+    res = coordinate_descent(measure, start, space, **kw)
+    if cache:
+        store_cache(cache, signature, res, space)
+    return res
+
+
+def shape_signature(n: int, flags: int, workload: str = "") -> str:
+    """Device name, SM count, query count, flags and the caller's workload tag."""
+    import torch
+
+    p = torch.cuda.get_device_properties(torch.cuda.current_device())
+    return f"{p.name}|sm{p.multi_processor_count}|queries{n}|flags{flags}|{workload}"
 
 
 def coordinate_descent(measure, start: dict, space: dict, passes: int = 2, tol: float = 0.01) -> Result:
@@ -88,10 +151,13 @@ def coordinate_descent(measure, start: dict, space: dict, passes: int = 2, tol: 
 
 
 def tune_collide(ctx, d_queries: int, n: int, flags: int = 0, space: dict | None = None, reps: int = 5,
-                 warmup: int = 2, passes: int = 2, flush=None) -> Result:
+                 warmup: int = 2, passes: int = 2, flush=None, cache: str | None = None,
+                 workload: str = "") -> Result:
     """Tunes ctx (a capi.Context) for the batch at device pointer d_queries
     (n queries) and leaves it configured with the best settings. `flush`, a
-    CUDA tensor larger than L2, is rewritten before every timed launch."""
+    CUDA tensor larger than L2, is rewritten before every timed launch.
+    `cache`: a JSON file of earlier results by shape signature (`workload`
+    names the batch's scene in it)."""
     import torch
 
     space = dict(SPACE if space is None else space)
@@ -124,6 +190,13 @@ def tune_collide(ctx, d_queries: int, n: int, flags: int = 0, space: dict | None
             ctx.sync_stats()
         return float(np.median(times))
 
-    res = coordinate_descent(measure, start, space, passes=passes)
+    if cache:
+        # the starting settings' counts, which a cached setting must reproduce
+        ctx.reconfigure(**start)
+        with torch.cuda.stream(stream):
+            ctx.collide_async(d_queries, n, flags, stream.cuda_stream)
+            st = ctx.sync_stats()
+        want.append((st["tri_tests"], st["leaf_pairs"], st["tri_pairs"]))
+    res = cached_descent(measure, start, space, shape_signature(n, flags, workload), cache, passes=passes)
     ctx.reconfigure(**res.best)
     return res

@@ -57,8 +57,9 @@ void free_buffers(cg_ctx* c) {
     c->d_leaf_keys = nullptr;
     cudaFree(c->d_trace);
     auto& t = c->ct;
-    for (void* p : {(void*)t.pair_aux, (void*)t.table, (void*)t.occupied, (void*)t.pg_geom, (void*)t.pg_link,
-                    (void*)t.pg_mask, (void*)t.contrib, (void*)t.maps, (void*)t.elems, (void*)t.work, (void*)t.vkeys,
+    for (void* p : {(void*)t.pair_aux, (void*)t.table, (void*)t.occupied, (void*)t.slot_info, (void*)t.pg_geom, (void*)t.pg_link,
+                    (void*)t.pg_mask, (void*)t.contrib, (void*)t.leaf_mark, (void*)t.kleaf, (void*)t.kpath,
+                    (void*)t.maps, (void*)t.elems, (void*)t.work, (void*)t.vkeys,
                     (void*)t.vval, (void*)t.vocc, (void*)t.ctmp, (void*)t.rtmp, (void*)t.contacts, (void*)t.rays,
                     (void*)t.averages})
         cudaFree(p);
@@ -268,6 +269,9 @@ int alloc_buffers(cg_ctx* c) {
     CG_CUDA(narrow_occupancy(8, &nocc), "occupancy");
     c->narrow_blocks = uint32_t(std::max(nocc, 1) * c->sm_count);
     c->contact_blocks = uint32_t(8 * c->sm_count);  // 2048 threads per SM of 256-thread blocks
+    int oocc = 0;
+    CG_CUDA(contacts_order_occupancy(&oocc), "occupancy");
+    c->order_blocks = uint32_t(std::max(oocc, 1) * c->sm_count);
     CG_CUDA(deform_smem_limit(), "deform kernel shared memory");
     c->copy_blocks = uint32_t(4 * c->sm_count);
     int gocc = 0;
@@ -301,12 +305,19 @@ int alloc_buffers(cg_ctx* c) {
         CG_CUDA(cudaMalloc(&t.pair_aux, sizeof(uint4) * mp), "alloc pair side records");
         CG_CUDA(cudaMalloc(&t.table, sizeof(ContactSlot) * t.table_slots), "alloc contact table");
         CG_CUDA(cudaMalloc(&t.occupied, sizeof(uint32_t) * t.table_slots), "alloc contact list");
+        CG_CUDA(cudaMalloc(&t.slot_info, sizeof(uint4) * t.table_slots), "alloc contact slot list");
         CG_CUDA(cudaMalloc(&t.pg_geom, sizeof(float4) * mp), "alloc pair geometry");
         CG_CUDA(cudaMalloc(&t.pg_link, sizeof(uint4) * mp), "alloc pair links");
         CG_CUDA(cudaMalloc(&t.pg_mask, sizeof(uint32_t) * mp), "alloc pair masks");
         CG_CUDA(cudaMalloc(&t.contrib, sizeof(unsigned long long) * 2 * mp), "alloc contributions");
-        CG_CUDA(cudaMalloc(&t.maps, sizeof(uint32_t) * 6 * 2 * mq), "alloc contact maps");
-        CG_CUDA(cudaMemset(t.maps, 0, sizeof(uint32_t) * 6 * 2 * mq), "zero contact maps");
+        CG_CUDA(cudaMalloc(&t.maps, sizeof(uint32_t) * 7 * 2 * mq), "alloc contact maps");
+        CG_CUDA(cudaMemset(t.maps, 0, sizeof(uint32_t) * 7 * 2 * mq), "zero contact maps");
+        const uint64_t ml = std::max<uint64_t>(g.max_leaf_pairs, 1);
+        CG_CUDA(cudaMalloc(&t.leaf_mark, sizeof(uint32_t) * ml), "alloc leaf-pair marks");
+        CG_CUDA(cudaMemset(t.leaf_mark, 0, sizeof(uint32_t) * ml), "zero leaf-pair marks");
+        t.kleaf_cap = t.table_slots;
+        CG_CUDA(cudaMalloc(&t.kleaf, sizeof(uint32_t) * t.kleaf_cap), "alloc contact leaf pairs");
+        CG_CUDA(cudaMalloc(&t.kpath, sizeof(ulonglong2) * t.kleaf_cap), "alloc contact leaf-pair paths");
         CG_CUDA(cudaMalloc(&t.elems, sizeof(ContactElem) * mc), "alloc contact elements");
         CG_CUDA(cudaMalloc(&t.work, sizeof(uint32_t) * kOrderWords * mc), "alloc contact order memory");
         CG_CUDA(cudaMalloc(&t.vkeys, sizeof(unsigned long long) * t.vslots), "alloc vertex set");
@@ -344,20 +355,21 @@ int sync_tree_table(cg_ctx* c) {
     for (uint32_t i = 0; i < n; ++i) {
         const auto& s = c->trees[i];
         host[i] = DevTree{uint32_t(s.rec_base), uint32_t(s.tri_base), uint32_t(s.n_recs), uint32_t(s.n_tris),
-                          s.live ? 1u : 0u, 0u, s.nrm, s.ranges};
+                          s.live ? 1u : 0u, 0u, s.nrm};
     }
     if (n) CG_CUDA(cudaMemcpy(c->d_trees, host.data(), sizeof(DevTree) * n, cudaMemcpyHostToDevice), "upload tree table");
     return CG_OK;
 }
 
-void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta) {
+void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta, uint32_t split) {
     rec[0] = make_float4(b.center[0], b.center[1], b.center[2], b.u[0]);
     rec[1] = make_float4(b.u[1], b.u[2], b.v[0], b.v[1]);
     rec[2] = make_float4(b.v[2], b.w[0], b.w[1], b.w[2]);
-    float r, m;
+    float r, m, sp;
     std::memcpy(&r, &ref, 4);
     std::memcpy(&m, &meta, 4);
-    rec[3] = make_float4(r, m, 0.f, 0.f);
+    std::memcpy(&sp, &split, 4);
+    rec[3] = make_float4(r, m, 0.f, sp);
 }
 
 // Enqueues counter reset, packing, the traversal and the narrow phase on `s`.
@@ -445,6 +457,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.table_mask = t.table_slots - 1u;
         cp.max_contacts = uint32_t(c->cfg.max_contacts);
         cp.occupied = t.occupied;
+        cp.slot_info = t.slot_info;
         cp.pg_geom = t.pg_geom;
         cp.pg_link = t.pg_link;
         cp.pg_mask = t.pg_mask;
@@ -456,6 +469,11 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.map_nr = t.maps + 3 * mq2;
         cp.map_coff = t.maps + 4 * mq2;
         cp.map_roff = t.maps + 5 * mq2;
+        cp.map_order = t.maps + 6 * mq2;
+        cp.leaf_mark = t.leaf_mark;
+        cp.kleaf = t.kleaf;
+        cp.kpath = t.kpath;
+        cp.kleaf_cap = t.kleaf_cap;
         cp.elems = t.elems;
         cp.work = t.work;
         cp.vkeys = t.vkeys;
@@ -473,7 +491,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
             cp.sched_start[k] = c->sched_start[k];
             cp.sched_buckets[k] = c->sched_buckets[k];
         }
-        CG_CUDA(launch_contacts(cp, c->contact_blocks, s), "contact kernels");
+        CG_CUDA(launch_contacts(cp, c->contact_blocks, c->order_blocks, s), "contact kernels");
     }
     if (pairs_copy) CG_CUDA(cudaStreamWaitEvent(s, c->ev_joined, 0), "join");
     return CG_OK;
@@ -796,15 +814,38 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
         return fail(c, CG_ERR_OUT_OF_MEMORY, "arena index space exhausted");
     }
 
+    // subtree triangle range of every record (the root, then both children of
+    // each node; children come after their parent, so a backward pass over
+    // the nodes sees each inner child's range before its parent needs it)
+    std::vector<uint2> rg(n_recs, make_uint2(0u, ~0u));
+    std::vector<uint2> node_rg(N);
+    for (uint32_t k = N; k-- > 0;) {
+        uint32_t lo = 0xffffffffu, hi = 0;
+        for (int s2 = 0; s2 < 2; ++s2) {
+            const uint32_t ref = v->node_ref[2 * k + s2], cnt = v->node_tri_count[2 * k + s2];
+            const uint2 crg = cnt ? make_uint2(ref, cnt) : node_rg[ref];
+            rg[2ull * k + 2 + s2] = crg;
+            if (crg.y) {
+                lo = std::min(lo, crg.x);
+                hi = std::max(hi, crg.x + crg.y);
+            }
+        }
+        node_rg[k] = lo <= hi ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
+    }
+    rg[1] = N ? node_rg[0] : make_uint2(0u, T);
+    // an inner box's split word: the first triangle of node k's right child
+    auto split_of = [&](uint32_t k) { return uint32_t(tb + rg[2ull * k + 3].x); };
+
     std::vector<float4> recs(4ull * n_recs, make_float4(0, 0, 0, 0));
-    put_box(&recs[4], v->root_obb, N ? uint32_t(rb + 2) : uint32_t(tb), N ? 0u : (kLeafFlag | T));
+    put_box(&recs[4], v->root_obb, N ? uint32_t(rb + 2) : uint32_t(tb), N ? 0u : (kLeafFlag | T), N ? split_of(0) : 0u);
     for (uint32_t k = 0; k < N; ++k)
         for (int s = 0; s < 2; ++s) {
             const uint64_t r = 2ull * k + 2 + s;
             const uint32_t ref = v->node_ref[2 * k + s];
             const uint32_t cnt = v->node_tri_count[2 * k + s];
             const uint32_t abs_ref = cnt ? uint32_t(tb + ref) : uint32_t(rb + 2ull * ref + 2);
-            put_box(&recs[4 * r], v->node_obbs[2 * k + s], abs_ref, cnt ? (kLeafFlag | cnt) : 0u);
+            put_box(&recs[4 * r], v->node_obbs[2 * k + s], abs_ref, cnt ? (kLeafFlag | cnt) : 0u,
+                    cnt ? 0u : split_of(ref));
         }
     std::vector<float4> tris(3ull * n_tris, make_float4(0, 0, 0, 0));
     for (uint32_t t = 0; t < T; ++t)
@@ -833,26 +874,7 @@ int cg_tree_upload(cg_ctx* c, const cg_tree_view* v, uint32_t* tree_id) {
                                 c->stream),
                 "upload normals");
     }
-    // subtree triangle range of every record (the root, then both children of
-    // each node; children come after their parent, so a backward pass over
-    // the nodes sees each inner child's range before its parent needs it)
     {
-        std::vector<uint2> rg(n_recs, make_uint2(0u, ~0u));
-        std::vector<uint2> node_rg(N);
-        for (uint32_t k = N; k-- > 0;) {
-            uint32_t lo = 0xffffffffu, hi = 0;
-            for (int s2 = 0; s2 < 2; ++s2) {
-                const uint32_t ref = v->node_ref[2 * k + s2], cnt = v->node_tri_count[2 * k + s2];
-                const uint2 crg = cnt ? make_uint2(ref, cnt) : node_rg[ref];
-                rg[2ull * k + 2 + s2] = crg;
-                if (crg.y) {
-                    lo = std::min(lo, crg.x);
-                    hi = std::max(hi, crg.x + crg.y);
-                }
-            }
-            node_rg[k] = lo <= hi ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
-        }
-        rg[1] = N ? node_rg[0] : make_uint2(0u, T);
         CG_CUDA(cudaMalloc(&slot.ranges, sizeof(uint2) * n_recs), "alloc record ranges");
         CG_CUDA(cudaMemcpyAsync(slot.ranges, rg.data(), sizeof(uint2) * n_recs, cudaMemcpyHostToDevice, c->stream),
                 "upload record ranges");

@@ -587,6 +587,7 @@ __global__ void build_order_kernel(const BuildParams B, BuildFlat* flat, uint32_
         }
         BuildFlat& F = flat[f];
         BuildFlat& S = flat[s];
+        flat[id].split_off = X.tri_off + B.nodes[f].count;
         F.index = X.index + 1u;
         S.index = X.index + 1u + F.inner;
         F.tri_off = X.tri_off;
@@ -617,7 +618,8 @@ __global__ void build_emit_nodes_kernel(const BuildParams B, const BuildFlat* fl
         r[0] = make_float4(b[0], b[1], b[2], b[3]);
         r[1] = make_float4(b[4], b[5], b[6], b[7]);
         r[2] = make_float4(b[8], b[9], b[10], b[11]);
-        r[3] = make_float4(__uint_as_float(ref), __uint_as_float(meta), 0.f, 0.f);
+        r[3] = make_float4(__uint_as_float(ref), __uint_as_float(meta), 0.f,
+                           __uint_as_float(leaf ? 0u : E.tri_base + X.split_off));
         E.ranges[X.rec] = make_uint2(X.tri_off, N.count);
         E.topo[X.rec] = X.prec;
         if (leaf) E.topo[E.n_recs + X.leaf_off] = X.rec;

@@ -35,21 +35,27 @@
 //   contacts_pairs    thread per colliding pair: planes (Plane.cpp:5-28),
 //                     weight, weighted midpoint, vertex bits; the two
 //                     triangles' slots in the contact table, a place in each
-//                     slot's list; empties the previous launch's vertex set
-//   contacts_scan     one block: the slots' list offsets, the maps' offsets
+//                     slot's list; its leaf pair listed once; empties the
+//                     previous launch's vertex set
+//   contacts_alloc    each slot's place in the contribution list (one atomic
+//                     per 32 slots); the first block: the maps' offsets
 //   contacts_scatter  thread per pair: both contributions into their lists
-//   contacts_fold     thread per slot: the list sorted by the other triangle,
+//   contacts_paths    thread per listed leaf pair: its descent path
+//   contacts_fold     warp per slot: the list sorted by the other triangle,
 //                     the reference's two folds, the path of the first leaf
 //                     pair of non-zero weight; the triangle into its map
-//   contacts_order    block per map (query, side): the insertion order (sort
-//                     by path, triangle), the iteration order (one reordering
-//                     per growth), the rays (find_rays_lambda,
-//                     CreateUncollideRays.cpp:131-178: one per vertex index,
-//                     at its first corner in iteration order, else from the
-//                     weighted average), the mean origin in ray order
+//   contacts_rank     one block: the maps largest first
+//   contacts_order    persistent, a block per map in that order: the
+//                     insertion order (sort by path, triangle), the iteration
+//                     order (counting passes per growth), the rays
+//                     (find_rays_lambda, CreateUncollideRays.cpp:131-178: one
+//                     per vertex index, at its first corner in iteration
+//                     order, else from the weighted average), the mean origin
+//                     in ray order
 //   contacts_offsets  one block: each map's first record and ray
 //   contacts_emit     block per map: records and rays to their places;
-//                     empties the table slots and map counters it used
+//                     empties the table slots, leaf-pair marks and map
+//                     counters it used
 // Geometry uses the reference's arithmetic (no contraction, IEEE division and
 // square root).
 #include <cuda_runtime.h>
@@ -240,39 +246,75 @@ __device__ __forceinline__ uint32_t n_slots(const ContactParams& P) {
     return n < P.table_mask + 1u ? n : P.table_mask + 1u;
 }
 
-// Exclusive scan of get(0..n-1) by one block (blockDim.x <= 1024): each
-// thread takes a contiguous run, the runs' sums are scanned in shared memory,
-// put(i, prefix) is called in order within each run. Returns the total.
+// Exclusive scans by one block (blockDim.x a multiple of 32, at most 1024) of
+// get1(0..n1-1) and get2(0..n2-1) side by side: each thread takes a
+// contiguous run of each, the runs' sums are scanned with warp shuffles, every
+// warp adds up the partial sums of the warps before it, put(i, prefix) is
+// called in order within each run. Two barriers; the totals go to every
+// thread. `part` holds 64 words. get must return the same value twice.
+template <class Get1, class Put1, class Get2, class Put2>
+__device__ void block_scan2(uint32_t n1, uint32_t n2, uint32_t* part, Get1 get1, Put1 put1, Get2 get2, Put2 put2,
+                            uint32_t& total1, uint32_t& total2) {
+    const uint32_t T = blockDim.x, t = threadIdx.x, lane = t & 31u, warp = t >> 5, nw = T >> 5;
+    const uint32_t per1 = (n1 + T - 1u) / T, a0 = min(n1, t * per1), a1 = min(n1, a0 + per1);
+    const uint32_t per2 = (n2 + T - 1u) / T, c0 = min(n2, t * per2), c1 = min(n2, c0 + per2);
+    uint32_t s1 = 0, s2 = 0;
+    for (uint32_t i = a0; i < a1; ++i) s1 += get1(i);
+    for (uint32_t i = c0; i < c1; ++i) s2 += get2(i);
+    uint32_t i1 = s1, i2 = s2;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v1 = __shfl_up_sync(kFullMask, i1, o);
+        const uint32_t v2 = __shfl_up_sync(kFullMask, i2, o);
+        if (lane >= uint32_t(o)) {
+            i1 += v1;
+            i2 += v2;
+        }
+    }
+    if (lane == 31u) {
+        part[warp] = i1;
+        part[32u + warp] = i2;
+    }
+    __syncthreads();
+    uint32_t b1 = 0, b2 = 0, t1 = 0, t2 = 0;
+    for (uint32_t w = 0; w < nw; ++w) {
+        const uint32_t p1 = part[w], p2 = part[32u + w];
+        if (w < warp) {
+            b1 += p1;
+            b2 += p2;
+        }
+        t1 += p1;
+        t2 += p2;
+    }
+    uint32_t r1 = b1 + i1 - s1, r2 = b2 + i2 - s2;
+    for (uint32_t i = a0; i < a1; ++i) {
+        const uint32_t v = get1(i);
+        put1(i, r1);
+        r1 += v;
+    }
+    for (uint32_t i = c0; i < c1; ++i) {
+        const uint32_t v = get2(i);
+        put2(i, r2);
+        r2 += v;
+    }
+    __syncthreads();
+    total1 = t1;
+    total2 = t2;
+}
+
+// One exclusive scan of get(0..n-1) (block_scan2 with an empty second).
+// Returns the total.
 template <class Get, class Put>
 __device__ uint32_t block_scan(uint32_t n, uint32_t* part, Get get, Put put) {
-    const uint32_t T = blockDim.x, t = threadIdx.x;
-    const uint32_t per = (n + T - 1u) / T;
-    const uint32_t b0 = min(n, t * per), b1 = min(n, b0 + per);
-    uint32_t sum = 0;
-    for (uint32_t i = b0; i < b1; ++i) sum += get(i);
-    part[t] = sum;
-    __syncthreads();
-    for (uint32_t o = 1; o < T; o <<= 1) {
-        const uint32_t v = t >= o ? part[t - o] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - sum;
-    const uint32_t total = part[T - 1u];
-    for (uint32_t i = b0; i < b1; ++i) {
-        const uint32_t v = get(i);
-        put(i, run);
-        run += v;
-    }
-    __syncthreads();
+    uint32_t total = 0, none = 0;
+    block_scan2(
+        n, 0u, part, get, put, [](uint32_t) { return 0u; }, [](uint32_t, uint32_t) {}, total, none);
     return total;
 }
 
 struct WalkRec {
     Box box;
-    uint32_t ref, meta;
-    float surf;
+    uint32_t ref, meta, split;
 };
 
 __device__ __forceinline__ WalkRec walk_rec(const float4* recs, uint32_t r) {
@@ -285,49 +327,60 @@ __device__ __forceinline__ WalkRec walk_rec(const float4* recs, uint32_t r) {
     R.box.w = make_float3(c.y, c.z, c.w);
     R.ref = __float_as_uint(d.x);
     R.meta = __float_as_uint(d.y);
-    R.surf = d.z;
+    R.split = __float_as_uint(d.w);
     return R;
 }
 
 // The path of the simultaneous descent (OBBtree::IntersectOBBtreesRecursive,
-// src/Geometry/OBBtree.cpp:414-476) from the root pair to leaf pair `leaf_i`
-// of the list: at every node pair the reference's split decision (two inner
-// boxes: the first tree's when its surface is at least the second's as
-// transformed; else the inner one), then the child whose subtree holds the
-// leaf (bit 0 left, 1 right). Left-aligned in 128 bits; *depth = splits.
+// src/Geometry/OBBtree.cpp:414-476) from the root pair to leaf pair lp
+// (query, first triangle a, first triangle b, counts; arena indices): at every
+// node pair the reference's split decision (two inner boxes: the first tree's
+// when its surface is at least the second's as transformed; else the inner
+// one), then the child whose subtree holds the leaf's first triangle (bit 0
+// left, 1 right, from the record's split word). A step on the first tree
+// reads the child's link word only; one on the second tree reads the child's
+// box to transform it. The way down each tree is fixed by the leaf alone, so
+// each tree's next node is loaded one step ahead: a split of the other tree
+// finds it there. Left-aligned in 128 bits; *depth = splits.
 __device__ void descent_path(const PackedQuery* queries, const DevTree* trees, const float4* recs, uint4 lp,
                              unsigned long long& hi, unsigned long long& lo, uint32_t& depth) {
-    // lp: (query, first triangle a, first triangle b, counts), arena indices
     const PackedQuery* Q = queries + lp.x;
-    const DevTree* TA = trees + __ldg(&Q->tree_a);
-    const DevTree* TB = trees + __ldg(&Q->tree_b);
-    const uint32_t base_a = TA->rec_base, base_b = TB->rec_base;
-    const uint2* rg_a = TA->ranges;
-    const uint2* rg_b = TB->ranges;
-    const uint32_t ta = lp.y - TA->tri_base, tb = lp.z - TB->tri_base;
+    const uint32_t base_a = trees[__ldg(&Q->tree_a)].rec_base;
+    const uint32_t base_b = trees[__ldg(&Q->tree_b)].rec_base;
     const Mat4 M = query_mat(Q);
-    WalkRec A = walk_rec(recs, base_a + 1u);
+    // (ref, meta, surface, split) of the first tree's node
+    auto a_leaf = [](float4 a) { return (__float_as_uint(a.y) & kLeafFlag) != 0u; };
+    auto a_next = [&](float4 a) {
+        return a_leaf(a) ? a : __ldg(recs + 4ull * (__float_as_uint(a.x) + (lp.y >= __float_as_uint(a.w))) + 3);
+    };
+    auto b_next = [&](const WalkRec& b) {
+        return (b.meta & kLeafFlag) != 0u ? b : walk_rec(recs, b.ref + (lp.z >= b.split ? 1u : 0u));
+    };
+    float4 A = __ldg(recs + 4ull * (base_a + 1u) + 3);
     WalkRec B = walk_rec(recs, base_b + 1u);
+    float4 An = a_next(A);
+    WalkRec Bn = b_next(B);
     float sb = surface(xform_box(M, B.box));
     hi = lo = 0ull;
     depth = 0;
     for (;;) {
-        const bool la = (A.meta & kLeafFlag) != 0u, lb = (B.meta & kLeafFlag) != 0u;
+        const bool la = a_leaf(A), lb = (B.meta & kLeafFlag) != 0u;
         if ((la && lb) || depth > 128u) break;
-        const bool split_a = (!la && !lb) ? (A.surf >= sb) : !la;
-        const uint32_t left = split_a ? A.ref : B.ref;
-        const uint2 rg = split_a ? __ldg(rg_a + (left - base_a)) : __ldg(rg_b + (left - base_b));
-        const uint32_t target = split_a ? ta : tb;
-        const uint32_t bit = target >= rg.x + rg.y ? 1u : 0u;
+        const bool split_a = (!la && !lb) ? (A.z >= sb) : !la;
+        uint32_t bit;
+        if (split_a) {
+            bit = lp.y >= __float_as_uint(A.w) ? 1u : 0u;
+            A = An;
+            An = a_next(A);
+        } else {
+            bit = lp.z >= B.split ? 1u : 0u;
+            B = Bn;
+            Bn = b_next(B);
+            sb = surface(xform_box(M, B.box));
+        }
         hi = (hi << 1) | (lo >> 63);
         lo = (lo << 1) | bit;
         ++depth;
-        if (split_a) {
-            A = walk_rec(recs, left + bit);
-        } else {
-            B = walk_rec(recs, left + bit);
-            sb = surface(xform_box(M, B.box));
-        }
     }
     if (depth == 0u || depth >= 128u) return;
     const uint32_t s = 128u - depth;
@@ -360,10 +413,181 @@ __device__ void bitonic(K* a, uint32_t n2, Less less) {
         }
 }
 
+// Ascending bitonic sort of the warp's 32 values, one per lane.
+__device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (uint32_t k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(kFullMask, v, j);
+            const bool lower = (lane & j) == 0u;
+            const bool up = (lane & k) == 0u;
+            v = (lower == up) ? (v < o ? v : o) : (v > o ? v : o);
+        }
+    return v;
+}
+
+// Ascending bitonic sort of n2 (a power of two) values in shared memory by
+// one warp.
+__device__ void warp_sort_smem(unsigned long long* a, uint32_t n2) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t k = 2; k <= n2; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = lane; i < n2; i += 32u) {
+                const uint32_t l = i ^ j;
+                if (l > i) {
+                    const unsigned long long x = a[i], y = a[l];
+                    if ((i & k) == 0u ? y < x : x < y) {
+                        a[i] = y;
+                        a[l] = x;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+}
+
 struct SortKey {
     unsigned long long hi, lo;
     uint32_t tri, idx;
 };
+
+// Insertion-order keys held in registers, each the narrowest exact form of
+// (first leaf pair's path, triangle) with the element index as payload: K1
+// when every path of the map has at most 32 splits (path's top 32 bits <<
+// 32 | triangle), K2 at most 64 (path's high word, triangle << 32 |
+// element), K3 any (high word, low word, triangle << 32 | element).
+struct K1 {
+    unsigned long long k;
+    uint32_t idx;
+    __device__ __forceinline__ static bool less(const K1& a, const K1& b) { return a.k < b.k; }
+    __device__ __forceinline__ K1 xor_lane(uint32_t j) const {
+        return K1{__shfl_xor_sync(kFullMask, k, j), __shfl_xor_sync(kFullMask, idx, j)};
+    }
+    __device__ __forceinline__ static K1 make(unsigned long long hi, unsigned long long, uint32_t tri, uint32_t i) {
+        return K1{(hi & 0xffffffff00000000ull) | tri, i};
+    }
+    __device__ __forceinline__ static K1 pad() { return K1{~0ull, ~0u}; }
+    __device__ __forceinline__ uint32_t tri() const { return uint32_t(k); }
+    __device__ __forceinline__ uint32_t elem() const { return idx; }
+};
+struct K2 {
+    unsigned long long hi, ti;
+    __device__ __forceinline__ static bool less(const K2& a, const K2& b) {
+        return a.hi != b.hi ? a.hi < b.hi : a.ti < b.ti;
+    }
+    __device__ __forceinline__ K2 xor_lane(uint32_t j) const {
+        return K2{__shfl_xor_sync(kFullMask, hi, j), __shfl_xor_sync(kFullMask, ti, j)};
+    }
+    __device__ __forceinline__ static K2 make(unsigned long long hi, unsigned long long, uint32_t tri, uint32_t i) {
+        return K2{hi, (unsigned long long)tri << 32 | i};
+    }
+    __device__ __forceinline__ static K2 pad() { return K2{~0ull, ~0ull}; }
+    __device__ __forceinline__ uint32_t tri() const { return uint32_t(ti >> 32); }
+    __device__ __forceinline__ uint32_t elem() const { return uint32_t(ti); }
+};
+struct K3 {
+    unsigned long long hi, lo, ti;
+    __device__ __forceinline__ static bool less(const K3& a, const K3& b) {
+        return a.hi != b.hi ? a.hi < b.hi : (a.lo != b.lo ? a.lo < b.lo : a.ti < b.ti);
+    }
+    __device__ __forceinline__ K3 xor_lane(uint32_t j) const {
+        return K3{__shfl_xor_sync(kFullMask, hi, j), __shfl_xor_sync(kFullMask, lo, j),
+                  __shfl_xor_sync(kFullMask, ti, j)};
+    }
+    __device__ __forceinline__ static K3 make(unsigned long long hi, unsigned long long lo, uint32_t tri, uint32_t i) {
+        return K3{hi, lo, (unsigned long long)tri << 32 | i};
+    }
+    __device__ __forceinline__ static K3 pad() { return K3{~0ull, ~0ull, ~0ull}; }
+    __device__ __forceinline__ uint32_t tri() const { return uint32_t(ti >> 32); }
+    __device__ __forceinline__ uint32_t elem() const { return uint32_t(ti); }
+};
+
+// x becomes the smaller (keep_min) or the larger of x and y (keys are
+// distinct but for the padding, whose order does not matter).
+template <class K>
+__device__ __forceinline__ void k_keep(K& x, const K& y, bool keep_min) {
+    if (K::less(y, x) == keep_min) x = y;
+}
+
+constexpr uint32_t kSortThreads = 256;               // the order kernel's block
+constexpr uint32_t kRegSortMax = 4u * kSortThreads;  // keys the block sorts in registers
+
+// Ascending bitonic sort by the block (kSortThreads threads) of n2 keys (a
+// power of two, 32 <= n2 <= E * kSortThreads, E = 1, 2 or 4); thread t holds
+// keys t + 256 e: exchanges within a warp by shuffles, across warps through
+// xchg (n2 keys of shared memory, two barriers), between a thread's own keys
+// in registers.
+template <class K, int E>
+__device__ __forceinline__ void block_sort_regs(K (&x)[E], uint32_t n2, K* xchg) {
+    const uint32_t t = threadIdx.x;
+    const bool active = t < n2;  // warp-uniform: n2 is a multiple of 32
+    for (uint32_t k = 2; k <= n2; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= kSortThreads) {
+                // a thread's own keys e and e ^ (j / 256); the lower one keeps
+                // the minimum when ascending
+                const uint32_t jj = j / kSortThreads;
+#pragma unroll
+                for (int e = 0; e < E; ++e)
+#pragma unroll
+                    for (int f = e + 1; f < E; ++f)
+                        if (uint32_t(e ^ f) == jj) {
+                            const bool asc = ((t + kSortThreads * uint32_t(e)) & k) == 0u;
+                            const K lo = x[e], hi = x[f];
+                            const bool sw = K::less(hi, lo) == asc;
+                            x[e] = sw ? hi : lo;
+                            x[f] = sw ? lo : hi;
+                        }
+            } else if (j >= 32u) {
+                if (active) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) xchg[t + kSortThreads * e] = x[e];
+                }
+                __syncthreads();
+                if (active) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                        const uint32_t i = t + kSortThreads * e;
+                        k_keep(x[e], xchg[i ^ j], ((i & j) == 0u) == ((i & k) == 0u));
+                    }
+                }
+                __syncthreads();
+            } else if (active) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const uint32_t i = t + kSortThreads * e;
+                    k_keep(x[e], x[e].xor_lane(j), ((i & j) == 0u) == ((i & k) == 0u));
+                }
+            }
+        }
+    }
+}
+
+// The insertion order of the map's n elements El (n2 = pow2 >= max(n, 32),
+// n2 <= E * kSortThreads): keys from the elements' paths and triangles,
+// sorted, then per insertion index its triangle and element.
+template <class K, int E>
+__device__ __forceinline__ void insertion_order(const ContactElem* El, uint32_t n, uint32_t n2, void* xchg,
+                                                uint32_t* ins_tri, uint32_t* ins_elem) {
+    const uint32_t t = threadIdx.x;
+    K x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t i = t + kSortThreads * e;
+        x[e] = i < n ? K::make(El[i].key_hi, El[i].key_lo, El[i].tri, i) : K::pad();
+    }
+    block_sort_regs<K, E>(x, n2, reinterpret_cast<K*>(xchg));
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t i = t + kSortThreads * e;
+        if (i < n) {
+            ins_tri[i] = x[e].tri();
+            ins_elem[i] = x[e].elem();
+        }
+    }
+}
 
 __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
     uint32_t p = 1;
@@ -378,20 +602,24 @@ __device__ __forceinline__ uint32_t buckets_at(const ContactParams& P, uint32_t 
     return b;
 }
 
-// Working memory of the order kernel for a map of n triangles (words):
-// insertion order (triangle, element), then the sort keys, or the iteration
-// order, the growth step's sort keys, their values and the buckets' first
-// places; later the rays' counts and places.
+// Working memory of the order kernel for a map of n triangles (words): per
+// insertion index its triangle and element, per element its corner mask;
+// then either the insertion sort's keys, or for the growth steps two orders
+// (the table's, the next), each place's bucket, its place in the bucket's
+// member list, the run starts, the member lists, and per bucket its first
+// place and count (two sets: this step's and the next's) and member offset;
+// the ray phase keeps the order and reuses the rest.
 struct OrderLayout {
-    uint32_t nr, n2, words;
+    uint32_t nr, n2, nb, words;
 };
 __device__ __forceinline__ OrderLayout order_layout(const ContactParams& P, uint32_t n) {
     OrderLayout L;
     L.nr = (n + 1u) & ~1u;
-    L.n2 = pow2_ceil(n);
+    L.n2 = pow2_ceil(n > 32u ? n : 32u);
+    L.nb = buckets_at(P, n);
     const uint32_t sort_w = 6u * L.n2;
-    const uint32_t epoch_w = 2u * L.nr + 2u * L.n2 + buckets_at(P, n);
-    L.words = 2u * L.nr + (sort_w > epoch_w ? sort_w : epoch_w);
+    const uint32_t epoch_w = 6u * L.nr + 5u * (L.nb + 1u);
+    L.words = 3u * L.nr + (sort_w > epoch_w ? sort_w : epoch_w);
     return L;
 }
 
@@ -412,7 +640,8 @@ __global__ void __launch_bounds__(256) contacts_pairs_kernel(const ContactParams
     for (unsigned long long base = warp0; base < n; base += stride) {
         const unsigned long long i = base + (threadIdx.x & 31u);
         int ra = -2, rb = -2;  // -2: no slot wanted, else the insert's result
-        uint32_t sa = 0, sb = 0;
+        uint32_t sa = 0, sb = 0, leaf = 0;
+        bool new_leaf = false;
         if (i < n) {
             const PairGeom g = pair_geom(P, i);
             const Probe T = contact_table(P);
@@ -429,9 +658,11 @@ __global__ void __launch_bounds__(256) contacts_pairs_kernel(const ContactParams
             if (ra < 0 || rb < 0) {
                 atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
             } else {
-                const uint32_t xa = atomicAdd(&P.table[sa].count, 1u);
-                const uint32_t xb = atomicAdd(&P.table[sb].count, 1u);
-                link = make_uint4(sa, sb, xa, xb);
+                // a place in each slot's contribution list
+                link = make_uint4(sa, sb, atomicAdd(&P.table[sa].count, 1u), atomicAdd(&P.table[sb].count, 1u));
+                // the leaf pair has colliding pairs: its descent path is needed
+                leaf = __ldg(&P.pair_aux[i].z);
+                new_leaf = atomicCAS(P.leaf_mark + leaf, 0u, 1u) == 0u;
             }
             P.pg_geom[i] = make_float4(g.mid.x, g.mid.y, g.mid.z, g.w);
             P.pg_link[i] = link;
@@ -442,20 +673,42 @@ __global__ void __launch_bounds__(256) contacts_pairs_kernel(const ContactParams
         const unsigned o = warp_append(&P.ctr->n_contacts, new_a + new_b);
         if (new_a) P.occupied[o] = sa;  // one entry per slot: the list never outgrows the table
         if (new_b) P.occupied[o + new_a] = sb;
+        const unsigned k = warp_append(&P.ctr->n_kleaf, new_leaf ? 1u : 0u);
+        if (new_leaf) {
+            if (k < P.kleaf_cap) {
+                P.kleaf[k] = leaf;
+                P.leaf_mark[leaf] = 1u + k;
+            } else {
+                atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
+            }
+        }
     }
 }
 
-__global__ void __launch_bounds__(1024) contacts_scan_kernel(const ContactParams P) {
-    __shared__ uint32_t part[1024];
+// Each slot's place in the contribution list (one atomic per warp of 32
+// slots), and, in the first block, the maps' element offsets.
+__global__ void __launch_bounds__(256) contacts_alloc_kernel(const ContactParams P) {
+    __shared__ uint32_t part[64];
     const uint32_t ns = n_slots(P);
-    if (threadIdx.x == 0 && ns > P.max_contacts) atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
-    block_scan(
-        ns, part, [&](uint32_t i) { return P.table[P.occupied[i]].count; },
-        [&](uint32_t i, uint32_t v) { P.table[P.occupied[i]].offset = v; });
-    block_scan(
-        2u * P.n_queries, part, [&](uint32_t i) { return P.map_cnt[i]; }, [&](uint32_t i, uint32_t v) { P.map_off[i] = v; });
+    if (blockIdx.x == 0 && threadIdx.x == 0 && ns > P.max_contacts) atomicOr(&P.ctr->c_overflow, CONTACT_TABLE);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t j0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; j0 < ns; j0 += stride) {
+        const uint32_t j = j0 + (threadIdx.x & 31u);
+        ContactSlot* sl = j < ns ? P.table + P.occupied[j] : nullptr;
+        const ContactSlot v = sl ? *sl : ContactSlot{kEmptyKey, 0u, 0u};
+        const uint32_t off = warp_append(&P.ctr->contrib_used, v.count);
+        if (sl) {
+            sl->offset = off;
+            P.slot_info[j] = make_uint4(uint32_t(v.key), uint32_t(v.key >> 32), off, v.count);
+        }
+    }
+    if (blockIdx.x == 0)
+        block_scan(
+            2u * P.n_queries, part, [&](uint32_t i) { return P.map_cnt[i]; },
+            [&](uint32_t i, uint32_t v) { P.map_off[i] = v; });
 }
 
+// Both contributions of every pair into their slots' lists.
 __global__ void __launch_bounds__(256) contacts_scatter_kernel(const ContactParams P) {
     const unsigned long long n = n_written_pairs(P);
     for (unsigned long long i = blockIdx.x * 1ull * blockDim.x + threadIdx.x; i < n;
@@ -463,84 +716,221 @@ __global__ void __launch_bounds__(256) contacts_scatter_kernel(const ContactPara
         const uint4 link = P.pg_link[i];
         if (link.x == ~0u) continue;
         const uint4 aux = P.pair_aux[i];
-        const unsigned long long pid = (unsigned long long)i << 1;
-        P.contrib[P.table[link.x].offset + link.z] = ((unsigned long long)aux.y << 32) | pid;
-        P.contrib[P.table[link.y].offset + link.w] = ((unsigned long long)aux.x << 32) | pid | 1ull;
+        const unsigned long long c = (unsigned long long)i << 1;
+        P.contrib[P.table[link.x].offset + link.z] = ((unsigned long long)aux.y << 32) | c;
+        P.contrib[P.table[link.y].offset + link.w] = ((unsigned long long)aux.x << 32) | c | 1ull;
     }
 }
 
-__global__ void __launch_bounds__(256) contacts_fold_kernel(const ContactParams P) {
-    const uint32_t ns = n_slots(P);
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += gridDim.x * blockDim.x) {
-        const ContactSlot sl = P.table[P.occupied[j]];
-        const uint32_t side = uint32_t(sl.key >> 63);
-        const uint32_t q = uint32_t(sl.key >> 32) & 0x7fffffffu;
-        const uint32_t c = sl.count;
-        unsigned long long* L = P.contrib + sl.offset;
-        // the triangle's colliding pairs by the other triangle (a handful)
-        for (uint32_t a = 1; a < c; ++a) {
-            const unsigned long long x = L[a];
-            uint32_t b = a;
-            while (b > 0u && L[b - 1u] > x) {
-                L[b] = L[b - 1u];
-                --b;
-            }
-            L[b] = x;
+// The descent path of every listed leaf pair (those with colliding pairs).
+__global__ void __launch_bounds__(256) contacts_paths_kernel(const ContactParams P) {
+    const uint32_t nk = min(*reinterpret_cast<const volatile unsigned*>(&P.ctr->n_kleaf), P.kleaf_cap);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nk; j += gridDim.x * blockDim.x) {
+        unsigned long long hi, lo;
+        uint32_t depth;
+        descent_path(P.q, P.trees, P.recs, P.leaf_list[P.kleaf[j]], hi, lo, depth);
+        if (depth >= 128u) atomicOr(&P.ctr->c_overflow, CONTACT_ORDER);
+        P.kpath[j] = make_ulonglong2(hi, lo);
+    }
+}
+
+// The reference's two folds over one triangle's colliding pairs in the
+// order of the other triangle (CreateUncollideRays.cpp:79-100, 117-127): a
+// fold per leaf pair from zero, merged in leaf-pair order when its weight is
+// not zero; the first leaf pair merged is kept for the insertion order.
+struct TriFold {
+    bool have = false;
+    float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+    unsigned am = 7u;
+    uint32_t first_leaf = 0u, cur = ~0u;
+    float px = 0.f, py = 0.f, pz = 0.f, pw = 0.f;
+    unsigned pm = 7u;
+    __device__ __forceinline__ void close() {
+        if (pw == 0.0f) return;
+        if (!have) {
+            have = true;
+            first_leaf = cur;
+            ax = px, ay = py, az = pz, aw = pw;
+            am = pm;
+        } else {
+            am &= pm;
+            ax = ax + px;
+            ay = ay + py;
+            az = az + pz;
+            aw = aw + pw;
         }
-        // CreateUncollideRays.cpp:96-100, 117-127: a fold per leaf pair from
-        // zero, merged in leaf-pair order when its weight is not zero
-        bool have = false;
-        float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
-        unsigned am = 7u;
-        uint32_t first_leaf = 0u, cur = ~0u;
-        float px = 0.f, py = 0.f, pz = 0.f, pw = 0.f;
-        unsigned pm = 7u;
-        auto close = [&]() {
-            if (pw == 0.0f) return;
-            if (!have) {
-                have = true;
-                first_leaf = cur;
-                ax = px, ay = py, az = pz, aw = pw;
-                am = pm;
-            } else {
-                am &= pm;
-                ax = ax + px;
-                ay = ay + py;
-                az = az + pz;
-                aw = aw + pw;
-            }
-        };
-        for (uint32_t a = 0; a < c; ++a) {
-            const uint32_t pid = uint32_t(L[a]) >> 1;
-            const uint32_t leaf = __ldg(&P.pair_aux[pid].z);
-            if (leaf != cur) {
-                if (cur != ~0u) close();
-                cur = leaf;
-                px = py = pz = pw = 0.0f;
-                pm = 7u;
-            }
-            const float4 g = P.pg_geom[pid];
-            px = px + g.x;
-            py = py + g.y;
-            pz = pz + g.z;
-            pw = pw + g.w;
-            pm &= (P.pg_mask[pid] >> (3u * side)) & 7u;
+    }
+    __device__ __forceinline__ void add(uint32_t leaf, float4 g, unsigned mk) {
+        if (leaf != cur) {
+            if (cur != ~0u) close();
+            cur = leaf;
+            px = py = pz = pw = 0.0f;
+            pm = 7u;
         }
+        px = px + g.x;
+        py = py + g.y;
+        pz = pz + g.z;
+        pw = pw + g.w;
+        pm &= mk;
+    }
+    __device__ __forceinline__ void finish() {
         if (cur != ~0u) close();
-        if (!have) continue;  // only pairs of zero length: no record (IsNull)
-        ContactElem E;
-        descent_path(P.q, P.trees, P.recs, P.leaf_list[first_leaf], E.key_hi, E.key_lo, E.depth);
-        if (E.depth >= 128u) atomicOr(&P.ctr->c_overflow, CONTACT_ORDER);
-        E.sx = ax;
-        E.sy = ay;
-        E.sz = az;
-        E.w = aw;
-        E.tri = uint32_t(sl.key);
-        E.mask = am;
-        E.pad = 0u;
-        const uint32_t map = 2u * q + side;
-        const uint32_t idx = P.map_off[map] + atomicAdd(P.map_fill + map, 1u);
-        if (idx < P.max_contacts) P.elems[idx] = E;
+    }
+};
+
+// The triangle of slot key `key` into its map, with the path of its first
+// leaf pair of non-zero weight; nothing when every pair had zero length
+// (IsNull).
+__device__ __forceinline__ void put_elem(const ContactParams& P, unsigned long long key, const TriFold& F) {
+    if (!F.have) return;
+    const uint32_t side = uint32_t(key >> 63);
+    const uint32_t q = uint32_t(key >> 32) & 0x7fffffffu;
+    const uint32_t mark = P.leaf_mark[F.first_leaf];
+    const ulonglong2 path =
+        mark > 0u && mark - 1u < P.kleaf_cap ? P.kpath[mark - 1u] : make_ulonglong2(~0ull, ~0ull);
+    ContactElem E;
+    E.key_hi = path.x;
+    E.key_lo = path.y;
+    E.depth = 0u;
+    E.sx = F.ax;
+    E.sy = F.ay;
+    E.sz = F.az;
+    E.w = F.aw;
+    E.tri = uint32_t(key);
+    E.mask = F.am;
+    E.pad = 0u;
+    const uint32_t map = 2u * q + side;
+    const uint32_t idx = P.map_off[map] + atomicAdd(P.map_fill + map, 1u);
+    if (idx < P.max_contacts) P.elems[idx] = E;
+}
+
+// One slot of at most kFoldThread contributions by its own thread: the
+// contributions sorted in registers, their pairs' data loaded together, the
+// folds.
+__device__ __forceinline__ void fold_thread(const ContactParams& P, unsigned long long key, uint32_t off, uint32_t c,
+                                            TriFold& F) {
+    const uint32_t side = uint32_t(key >> 63);
+    unsigned long long v[kFoldThread];
+#pragma unroll
+    for (uint32_t a = 0; a < kFoldThread; ++a) v[a] = a < c ? P.contrib[off + a] : ~0ull;
+    if (c > 1u) {
+        // odd-even transposition sort: kFoldThread rounds sort kFoldThread values
+#pragma unroll
+        for (uint32_t r = 0; r < kFoldThread; ++r)
+#pragma unroll
+            for (uint32_t a = r & 1u; a + 1u < kFoldThread; a += 2u) {
+                const unsigned long long x = v[a], y = v[a + 1u];
+                v[a] = x < y ? x : y;
+                v[a + 1u] = x < y ? y : x;
+            }
+    }
+    uint32_t leaf[kFoldThread];
+    float4 g[kFoldThread];
+    unsigned mk[kFoldThread];
+#pragma unroll
+    for (uint32_t a = 0; a < kFoldThread; ++a) {
+        if (a < c) {
+            const uint32_t pid = uint32_t(v[a]) >> 1;
+            leaf[a] = __ldg(&P.pair_aux[pid].z);
+            g[a] = __ldg(P.pg_geom + pid);
+            mk[a] = (__ldg(P.pg_mask + pid) >> (3u * side)) & 7u;
+        }
+    }
+#pragma unroll
+    for (uint32_t a = 0; a < kFoldThread; ++a)
+        if (a < c) F.add(leaf[a], g[a], mk[a]);
+    F.finish();
+}
+
+// One slot of more than kFoldThread contributions by the whole warp (all
+// lanes call it): sorted in registers (<= 32), in the warp's shared buffer
+// (<= kFoldSmem) or in place; then every lane folds them in order.
+__device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32_t off, uint32_t c,
+                          unsigned long long* buf, TriFold& F) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t side = uint32_t(key >> 63);
+    unsigned long long mine = ~0ull;
+    const unsigned long long* S = nullptr;
+    if (c <= 32u) {
+        mine = warp_sort32(lane < c ? P.contrib[off + lane] : ~0ull);
+    } else if (c <= kFoldSmem) {
+        uint32_t n2 = 64;
+        while (n2 < c) n2 <<= 1;
+        for (uint32_t i = lane; i < n2; i += 32u) buf[i] = i < c ? P.contrib[off + i] : ~0ull;
+        __syncwarp();
+        warp_sort_smem(buf, n2);
+        S = buf;
+    } else {
+        unsigned long long* G = P.contrib + off;  // rare: insertion sort in place by lane 0
+        if (lane == 0)
+            for (uint32_t a = 1; a < c; ++a) {
+                const unsigned long long x = G[a];
+                uint32_t b = a;
+                while (b > 0u && G[b - 1u] > x) {
+                    G[b] = G[b - 1u];
+                    --b;
+                }
+                G[b] = x;
+            }
+        __syncwarp();
+        S = G;
+    }
+    // 32 contributions at a time: each lane loads one's data, every lane
+    // folds them in order
+    for (uint32_t a0 = 0; a0 < c; a0 += 32u) {
+        const uint32_t a = a0 + lane;
+        uint32_t leaf = 0;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        unsigned mk = 7u;
+        if (a < c) {
+            const uint32_t pid = uint32_t(S ? S[a] : mine) >> 1;
+            leaf = __ldg(&P.pair_aux[pid].z);
+            g = __ldg(P.pg_geom + pid);
+            mk = (__ldg(P.pg_mask + pid) >> (3u * side)) & 7u;
+        }
+        const uint32_t m = c - a0 < 32u ? c - a0 : 32u;
+        for (uint32_t k = 0; k < m; ++k) {
+            const uint32_t lk = __shfl_sync(kFullMask, leaf, k);
+            const float4 gk = make_float4(__shfl_sync(kFullMask, g.x, k), __shfl_sync(kFullMask, g.y, k),
+                                          __shfl_sync(kFullMask, g.z, k), __shfl_sync(kFullMask, g.w, k));
+            F.add(lk, gk, __shfl_sync(kFullMask, mk, k));
+        }
+    }
+    F.finish();
+    __syncwarp();
+}
+
+// A thread per slot: the triangle's contributions sorted by the other
+// triangle (a triangle's pairs within a leaf pair come in the other
+// triangle's order, and its leaf pairs in the order of the other leaf's first
+// triangle), the reference's folds in that order, the path of the first leaf
+// pair of non-zero weight; the triangle into its map. A slot of more than
+// kFoldThread contributions is folded by its warp afterwards.
+constexpr uint32_t kFoldWarps = 8;
+
+__global__ void __launch_bounds__(256) contacts_fold_kernel(const ContactParams P) {
+    __shared__ unsigned long long buf[kFoldWarps][kFoldSmem];
+    const uint32_t ns = n_slots(P);
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t j0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; j0 < ns; j0 += stride) {
+        const uint32_t j = j0 + lane;
+        const uint4 si = j < ns ? P.slot_info[j] : make_uint4(0u, 0u, 0u, 0u);
+        const unsigned long long key = (unsigned long long)si.y << 32 | si.x;
+        if (si.w <= kFoldThread) {
+            TriFold F;
+            fold_thread(P, key, si.z, si.w, F);
+            put_elem(P, key, F);
+        }
+        unsigned big = __ballot_sync(kFullMask, si.w > kFoldThread);
+        while (big) {
+            const uint32_t l = uint32_t(__ffs(big)) - 1u;
+            big &= big - 1u;
+            const unsigned long long k = __shfl_sync(kFullMask, key, l);
+            TriFold F;
+            fold_warp(P, k, __shfl_sync(kFullMask, si.z, l), __shfl_sync(kFullMask, si.w, l), buf[wib], F);
+            if (lane == 0) put_elem(P, k, F);
+        }
     }
 }
 
@@ -601,50 +991,119 @@ __device__ cg_ray contact_ray(const ContactParams& P, uint32_t q, uint32_t side,
     return r;
 }
 
-// The corners of element E whose vertex ray this map makes (bit k), given
-// each corner's place code (pos * 4 + k) in the vertex set: a corner whose
-// bit is set makes the ray of its vertex index when it is that index's first
-// corner in iteration order (CreateUncollideRays.cpp:148-161, the
-// emplaced_point_indices set). insert_codes: record this element's codes
-// first.
-__device__ unsigned vertex_corners(const ContactParams& P, uint32_t q, uint32_t side, const ContactElem& E,
-                                   uint32_t pos, bool insert_codes) {
-    const PackedQuery* Q = P.q + q;
-    const float4* t = P.tris + 3ull * ((side ? __ldg(&Q->tri_base_b) : __ldg(&Q->tri_base_a)) + E.tri);
-    uint32_t vi[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) vi[k] = __float_as_uint(__ldg(&t[k].w));
-    const Probe V{P.vkeys, 1u, P.vtable_mask};
+// The vertex set of one map (CreateUncollideRays.cpp:148-161, the
+// emplaced_point_indices set): each vertex index of a corner that may make a
+// ray, with the place code (place * 4 + corner) of its first such corner in
+// iteration order. In shared memory (keys: vertex indices, ~0u empty; `mask`
+// + 1 slots, a power of two, hashed by the top bits of a multiplicative
+// hash) when `keys` is set, else the launch's global set keyed by (side,
+// query, vertex index).
+struct VSet {
+    uint32_t* keys;
+    uint32_t* vals;
+    uint32_t mask, shift;
+};
+
+__device__ __forceinline__ int smem_insert(const VSet& V, uint32_t key, uint32_t* slot) {
+    uint32_t s = (key * 0x9E3779B1u) >> V.shift;
+    for (uint32_t probe = 0; probe <= V.mask; ++probe) {
+        const uint32_t cur = atomicCAS(V.keys + s, ~0u, key);
+        if (cur == ~0u || cur == key) {
+            *slot = s;
+            return cur == ~0u ? 1 : 0;
+        }
+        s = (s + 1u) & V.mask;
+    }
+    return -1;
+}
+
+// The corners of a contact element (mask bits, vertex indices vi) whose
+// vertex ray this map makes (bit k): a corner whose bit is set makes the ray
+// of its vertex index when it is that index's first corner in iteration
+// order; an earlier corner of the same triangle with the same index makes it
+// instead. kRecord: record this element's codes first (place `pos`).
+template <bool kRecord>
+__device__ unsigned vertex_corners(const ContactParams& P, const VSet& V, uint32_t q, uint32_t side, uint32_t mask,
+                                   const uint32_t vi[3], uint32_t pos) {
     unsigned out = 0u;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        if (!((E.mask >> k) & 1u)) continue;
-        bool dup = false;  // an earlier corner of the same triangle with the same vertex index
+        if (!((mask >> k) & 1u)) continue;
+        bool dup = false;
 #pragma unroll
-        for (int j = 0; j < k; ++j) dup |= ((E.mask >> j) & 1u) && vi[j] == vi[k];
+        for (int j = 0; j < k; ++j) dup |= ((mask >> j) & 1u) && vi[j] == vi[k];
         if (dup) continue;
         uint32_t slot = 0;
-        const int r = insert(V, make_key(side, q, vi[k]), &slot);
+        uint32_t* val;
+        int r;
+        if (V.keys) {
+            r = smem_insert(V, vi[k], &slot);
+            val = V.vals + slot;
+        } else {
+            r = insert(Probe{P.vkeys, 1u, P.vtable_mask}, make_key(side, q, vi[k]), &slot);
+            val = P.vval + slot;
+            if (kRecord && r == 1) P.vocc[atomicAdd(&P.ctr->n_vertices, 1u)] = slot;
+        }
         if (r < 0) {
             atomicOr(&P.ctr->c_overflow, CONTACT_VERTICES);
             continue;
         }
         const uint32_t code = pos * 4u + uint32_t(k);
-        if (insert_codes) {
-            if (r == 1) P.vocc[atomicAdd(&P.ctr->n_vertices, 1u)] = slot;
-            atomicMin(P.vval + slot, code);
-        } else if (atomicOr(P.vval + slot, 0u) == code) {
+        if (kRecord)
+            atomicMin(val, code);
+        else if ((V.keys ? *val : atomicOr(val, 0u)) == code)
             out |= 1u << k;
-        }
     }
     return out;
 }
 
-__global__ void __launch_bounds__(256) contacts_order_kernel(const ContactParams P) {
-    extern __shared__ __align__(16) uint32_t smem_order[];
-    __shared__ uint32_t part[256];
-    __shared__ float fold[3];
-    const uint32_t map = blockIdx.x;
+// Keys in the table at the end of growth step e of a map of n keys.
+__device__ __forceinline__ uint32_t step_end(const ContactParams& P, uint32_t e, uint32_t n) {
+    return (e + 1u < P.n_sched && P.sched_start[e + 1u] < n) ? P.sched_start[e + 1u] : n;
+}
+
+// The growth steps of a map of n keys that end with at most 32 keys.
+__device__ __forceinline__ uint32_t warp_step_count(const ContactParams& P, uint32_t n) {
+    uint32_t e = 0;
+    while (e < P.n_sched && P.sched_start[e] < n && step_end(P, e, n) <= 32u) ++e;
+    return e;
+}
+
+// Growth steps 0..steps-1 (at most 32 keys each) by one warp, a key per
+// lane: a bucket's keys are the lanes that match its index, its first place
+// the lowest of them; a key goes after the keys of the buckets whose first
+// place is later and after the later keys of its own bucket.
+__device__ void warp_steps(const ContactParams& P, uint32_t n, uint32_t steps, const uint32_t* ins_tri,
+                           uint32_t* ord) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t e = 0; e < steps; ++e) {
+        const uint32_t st = P.sched_start[e];
+        const uint32_t m = step_end(P, e, n);
+        const uint32_t nb = P.sched_buckets[e];
+        const uint32_t x = lane < m ? (lane < st ? ord[lane] : lane) : ~0u;
+        const uint32_t b = lane < m ? ins_tri[x] % nb : ~0u;
+        const unsigned same = __match_any_sync(kFullMask, b);
+        const uint32_t first = uint32_t(__ffs(same)) - 1u;
+        const uint32_t c = lane < m && lane == first ? uint32_t(__popc(same)) : 0u;
+        uint32_t after = c;  // keys of the buckets first placed at this lane or later
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_down_sync(kFullMask, after, o);
+            if (lane + uint32_t(o) < 32u) after += v;
+        }
+        after -= c;
+        const uint32_t before_bucket = __shfl_sync(kFullMask, after, first);
+        const uint32_t later = lane < 31u ? uint32_t(__popc(same >> (lane + 1u))) : 0u;
+        __syncwarp();
+        if (lane < m) ord[before_bucket + later] = x;
+        __syncwarp();
+    }
+}
+
+// One map (query, side) by the whole block: its triangles in the reference's
+// iteration order, their contact records and rays in that order, and the
+// map's mean ray origin.
+__device__ void order_map(const ContactParams& P, uint32_t map, uint32_t* smem, uint32_t* part, float* fold) {
     const uint32_t q = map >> 1, side = map & 1u;
     const uint32_t n = P.map_fill[map];
     const uint32_t base = P.map_off[map];
@@ -652,113 +1111,231 @@ __global__ void __launch_bounds__(256) contacts_order_kernel(const ContactParams
     uint32_t n_rays = 0;
     bool ok = n > 0u && base + n <= P.max_contacts;
     OrderLayout L{};
-    uint32_t* W = smem_order;
+    uint32_t* W = smem;
+    VSet V{nullptr, nullptr, 0u, 0u};
     if (ok) {
         L = order_layout(P, n);
-        if (L.words > kOrderSmem * 8u) {
+        // the vertex set: at most 3 n keys, at most three quarters full
+        const uint32_t hs = pow2_ceil(4u * n);
+        uint32_t used = L.words;
+        if (L.words + 2u * hs > kOrderSmemWords) {
             // this map's part of the global working memory: kOrderWords per
             // element from its first element (base + n <= max_contacts)
             W = P.work + size_t(kOrderWords) * base;
             ok = L.words <= kOrderWords * n;
             if (!ok && t == 0u) atomicOr(&P.ctr->c_overflow, CONTACT_ORDER);
+            used = 0u;
+        }
+        if (used + 2u * hs <= kOrderSmemWords) {
+            V.keys = smem + used;
+            V.vals = V.keys + hs;
+            V.mask = hs - 1u;
+            V.shift = 33u - uint32_t(__ffs(hs));
+            for (uint32_t i = t; i < hs; i += T) {
+                V.keys[i] = ~0u;
+                V.vals[i] = ~0u;
+            }
         }
     }
+    cg_ray* R = P.rtmp + 3ull * base;
     if (ok) {
         const ContactElem* El = P.elems + base;
+        const PackedQuery* Q = P.q + q;
+        const uint32_t tri_base = side ? __ldg(&Q->tri_base_b) : __ldg(&Q->tri_base_a);
         uint32_t* ins_tri = W;
         uint32_t* ins_elem = W + L.nr;
-        uint32_t* B0 = W + 2u * L.nr;
+        uint32_t* mask_of = W + 2u * L.nr;
+        uint32_t* B0 = W + 3u * L.nr;
         // 1. insertion order: the first leaf pair's path, then the triangle
-        SortKey* sk = reinterpret_cast<SortKey*>(B0);
-        for (uint32_t i = t; i < L.n2; i += T) {
-            SortKey k;
-            if (i < n) {
+        if (L.n2 <= kRegSortMax) {
+            bool wide = false, mid = false;  // a path with low-word bits; with bits in the high word's low half
+            for (uint32_t i = t; i < n; i += T) {
                 const ContactElem& E = El[i];
-                k.hi = E.key_hi;
-                k.lo = E.key_lo;
-                k.tri = E.tri;
-                k.idx = i;
-            } else {
-                k.hi = k.lo = ~0ull;
-                k.tri = k.idx = ~0u;
+                mask_of[i] = E.mask;
+                wide |= E.key_lo != 0ull;
+                mid |= (E.key_hi & 0xffffffffull) != 0ull;
             }
-            sk[i] = k;
-        }
-        __syncthreads();
-        bitonic(sk, L.n2, [](const SortKey& a, const SortKey& b) {
-            return a.hi != b.hi ? a.hi < b.hi : (a.lo != b.lo ? a.lo < b.lo : a.tri < b.tri);
-        });
-        for (uint32_t i = t; i < n; i += T) {
-            ins_tri[i] = sk[i].tri;
-            ins_elem[i] = sk[i].idx;
-        }
-        __syncthreads();
-        // 2. iteration order after each growth of the table: its buckets most
-        // recently started first, each bucket's keys most recently placed
-        // first; `ord` is the table's order (insertion indices)
-        uint32_t* ord = B0;
-        unsigned long long* k64 = reinterpret_cast<unsigned long long*>(B0 + L.nr);
-        uint32_t* val = B0 + L.nr + 2u * L.n2;
-        uint32_t* first = val + L.nr;
-        for (uint32_t e = 0; e < P.n_sched && P.sched_start[e] < n; ++e) {
-            const uint32_t st = P.sched_start[e];  // keys in the table when it grows
-            const uint32_t m = (e + 1u < P.n_sched && P.sched_start[e + 1u] < n) ? P.sched_start[e + 1u] : n;
-            const uint32_t nb = P.sched_buckets[e];
-            const uint32_t m2 = pow2_ceil(m);
-            for (uint32_t b = t; b < nb; b += T) first[b] = ~0u;
+            wide = __syncthreads_or(wide) != 0;
+            mid = __syncthreads_or(mid) != 0;
+            const uint32_t E = L.n2 <= kSortThreads ? 1u : (L.n2 <= 2u * kSortThreads ? 2u : 4u);
+            if (!wide && !mid) {
+                if (E == 1u) insertion_order<K1, 1>(El, n, L.n2, B0, ins_tri, ins_elem);
+                else if (E == 2u) insertion_order<K1, 2>(El, n, L.n2, B0, ins_tri, ins_elem);
+                else insertion_order<K1, 4>(El, n, L.n2, B0, ins_tri, ins_elem);
+            } else if (!wide) {
+                if (E == 1u) insertion_order<K2, 1>(El, n, L.n2, B0, ins_tri, ins_elem);
+                else if (E == 2u) insertion_order<K2, 2>(El, n, L.n2, B0, ins_tri, ins_elem);
+                else insertion_order<K2, 4>(El, n, L.n2, B0, ins_tri, ins_elem);
+            } else {
+                if (E == 1u) insertion_order<K3, 1>(El, n, L.n2, B0, ins_tri, ins_elem);
+                else if (E == 2u) insertion_order<K3, 2>(El, n, L.n2, B0, ins_tri, ins_elem);
+                else insertion_order<K3, 4>(El, n, L.n2, B0, ins_tri, ins_elem);
+            }
+        } else {
+            SortKey* sk = reinterpret_cast<SortKey*>(B0);
+            for (uint32_t i = t; i < L.n2; i += T) {
+                SortKey k;
+                if (i < n) {
+                    const ContactElem& E = El[i];
+                    k.hi = E.key_hi;
+                    k.lo = E.key_lo;
+                    k.tri = E.tri;
+                    k.idx = i;
+                    mask_of[i] = E.mask;
+                } else {
+                    k.hi = k.lo = ~0ull;
+                    k.tri = k.idx = ~0u;
+                }
+                sk[i] = k;
+            }
             __syncthreads();
-            // place s: the key the growth re-places s-th (the table's order),
-            // then the keys inserted before the next growth
+            bitonic(sk, L.n2, [](const SortKey& a, const SortKey& b) {
+                return a.hi != b.hi ? a.hi < b.hi : (a.lo != b.lo ? a.lo < b.lo : a.tri < b.tri);
+            });
+            for (uint32_t i = t; i < n; i += T) {
+                ins_tri[i] = sk[i].tri;
+                ins_elem[i] = sk[i].idx;
+            }
+        }
+        __syncthreads();
+        // 2. the table's order (insertion indices) after each growth: its
+        // buckets in the order of their first place, latest first, each
+        // bucket's keys latest first, where a growth places the table's keys
+        // in the order it held them and then the new keys in insertion order
+        uint32_t* ord = B0;
+        uint32_t* nord = B0 + L.nr;
+        uint32_t* bs = B0 + 2u * L.nr;    // per place: its bucket
+        uint32_t* kb = B0 + 3u * L.nr;    // per place: its place in the bucket's member list
+        uint32_t* run = B0 + 4u * L.nr;   // per place: keys of the buckets first placed later
+        uint32_t* mem = B0 + 5u * L.nr;   // the buckets' member lists (places)
+        uint32_t* first = B0 + 6u * L.nr;
+        uint32_t* cnt = first + L.nb + 1u;
+        uint32_t* first2 = cnt + L.nb + 1u;
+        uint32_t* cnt2 = first2 + L.nb + 1u;
+        uint32_t* boff = cnt2 + L.nb + 1u;
+        // the steps of up to 32 keys by warp 0, meanwhile the first larger
+        // step's buckets start empty
+        uint32_t e = warp_step_count(P, n);
+        if (t < 32u && e > 0u) warp_steps(P, n, e, ins_tri, ord);
+        const uint32_t nb0 = e < P.n_sched && P.sched_start[e] < n ? P.sched_buckets[e] : 0u;
+        for (uint32_t b = t; b < nb0; b += T) {
+            first[b] = ~0u;
+            cnt[b] = 0u;
+        }
+        __syncthreads();
+        for (; e < P.n_sched && P.sched_start[e] < n; ++e) {
+            const uint32_t st = P.sched_start[e];  // keys in the table when it grows
+            const uint32_t m = step_end(P, e, n);
+            const uint32_t nb = P.sched_buckets[e];
             for (uint32_t s = t; s < m; s += T) {
                 const uint32_t x = s < st ? ord[s] : s;
-                atomicMin(first + ins_tri[x] % nb, s);
+                const uint32_t b = ins_tri[x] % nb;
+                bs[s] = b;
+                kb[s] = atomicAdd(cnt + b, 1u);
+                atomicMin(first + b, s);
             }
             __syncthreads();
-            for (uint32_t s = t; s < m2; s += T) {
-                unsigned long long k = ~0ull;
-                if (s < m) {
-                    const uint32_t x = s < st ? ord[s] : s;
-                    k = ((unsigned long long)(~first[ins_tri[x] % nb]) << 32) | (~s);
-                }
-                k64[s] = k;
+            // the member lists' offsets, and the run starts (the keys of the
+            // buckets whose first place is later)
+            uint32_t total = 0, none = 0;
+            block_scan2(
+                nb, m, part, [&](uint32_t b) { return cnt[b]; }, [&](uint32_t b, uint32_t v) { boff[b] = v; },
+                [&](uint32_t i) {
+                    const uint32_t s = m - 1u - i, b = bs[s];
+                    return first[b] == s ? cnt[b] : 0u;
+                },
+                [&](uint32_t i, uint32_t v) { run[m - 1u - i] = v; }, total, none);
+            for (uint32_t s = t; s < m; s += T) mem[boff[bs[s]] + kb[s]] = s;
+            if (t == 0u) boff[nb] = total;
+            __syncthreads();
+            // the next step's buckets start empty
+            const bool more = e + 1u < P.n_sched && P.sched_start[e + 1u] < n;
+            const uint32_t nb2 = more ? P.sched_buckets[e + 1u] : 0u;
+            for (uint32_t b = t; b < nb2; b += T) {
+                first2[b] = ~0u;
+                cnt2[b] = 0u;
+            }
+            for (uint32_t s = t; s < m; s += T) {
+                const uint32_t b = bs[s];
+                uint32_t later = 0;
+                for (uint32_t k = boff[b]; k < boff[b + 1u]; ++k) later += mem[k] > s ? 1u : 0u;
+                nord[run[first[b]] + later] = s < st ? ord[s] : s;
             }
             __syncthreads();
-            bitonic(k64, m2, [](unsigned long long a, unsigned long long b) { return a < b; });
-            for (uint32_t p = t; p < m; p += T) {
-                const uint32_t s = ~uint32_t(k64[p]);
-                val[p] = s < st ? ord[s] : s;
-            }
-            __syncthreads();
-            for (uint32_t p = t; p < m; p += T) ord[p] = val[p];
-            __syncthreads();
+            uint32_t* sw = ord;
+            ord = nord;
+            nord = sw;
+            sw = first;
+            first = first2;
+            first2 = sw;
+            sw = cnt;
+            cnt = cnt2;
+            cnt2 = sw;
         }
-        // 3. rays: the vertex set keeps each vertex index's first corner
-        uint32_t* rc = B0 + L.nr;  // per place: rays
-        uint32_t* rb = val;        // per place: vertex corners that make a ray
+        // 3. rays: the vertex set keeps each vertex index's first corner. Per
+        // place: mask then vertex-ray corners (rb), rays (rc), its corners'
+        // vertex indices (vi0..2); the order stays where the last step left it
+        uint32_t* rb = B0 + 2u * L.nr;
+        uint32_t* rc = B0 + 3u * L.nr;
+        uint32_t* vi0 = B0 + 4u * L.nr;
+        uint32_t* vi1 = B0 + 5u * L.nr;
+        uint32_t* vi2 = B0 + 6u * L.nr;
         for (uint32_t p = t; p < n; p += T) {
-            const ContactElem& E = El[ins_elem[ord[p]]];
-            if (E.mask) vertex_corners(P, q, side, E, p, true);
+            const uint32_t x = ord[p];
+            const uint32_t mask = mask_of[ins_elem[x]];
+            uint32_t vi[3] = {0u, 0u, 0u};
+            if (mask) {
+                const float4* tv = P.tris + 3ull * (tri_base + ins_tri[x]);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) vi[k] = __float_as_uint(__ldg(&tv[k].w));
+                vertex_corners<true>(P, V, q, side, mask, vi, p);
+            }
+            rb[p] = mask;
+            vi0[p] = vi[0];
+            vi1[p] = vi[1];
+            vi2[p] = vi[2];
         }
         __syncthreads();
         for (uint32_t p = t; p < n; p += T) {
-            const ContactElem& E = El[ins_elem[ord[p]]];
-            const unsigned bits = E.mask ? vertex_corners(P, q, side, E, p, false) : 0u;
+            const uint32_t mask = rb[p];
+            const uint32_t vi[3] = {vi0[p], vi1[p], vi2[p]};
+            const unsigned bits = mask ? vertex_corners<false>(P, V, q, side, mask, vi, p) : 0u;
             rb[p] = bits;
-            rc[p] = E.mask ? __popc(bits) : 1u;
+            rc[p] = mask ? __popc(bits) : 1u;
         }
         __syncthreads();
         n_rays = block_scan(
             n, part, [&](uint32_t i) { return rc[i]; }, [&](uint32_t i, uint32_t v) { rc[i] = v; });
-        cg_ray* R = P.rtmp + 3ull * base;
+        // a thread per ray: its place is the last one whose first ray is at
+        // or before it (a place without rays shares its first ray with the
+        // next place)
+        for (uint32_t r = t; r < n_rays; r += T) {
+            uint32_t a = 0, b = n - 1u;
+            while (a < b) {
+                const uint32_t mid = (a + b + 1u) >> 1;
+                if (rc[mid] <= r)
+                    a = mid;
+                else
+                    b = mid - 1u;
+            }
+            const ContactElem& E = El[ins_elem[ord[a]]];
+            int corner = -1;
+            if (E.mask) {
+                uint32_t left = r - rc[a];  // the ray's rank among the place's vertex rays
+                const uint32_t bits = rb[a];
+                for (int k = 0; k < 3; ++k)
+                    if ((bits >> k) & 1u) {
+                        if (left == 0u) {
+                            corner = k;
+                            break;
+                        }
+                        --left;
+                    }
+            }
+            R[r] = contact_ray(P, q, side, E, corner);
+        }
         for (uint32_t p = t; p < n; p += T) {
             const ContactElem& E = El[ins_elem[ord[p]]];
-            uint32_t o = rc[p];
-            if (E.mask) {
-                for (int k = 0; k < 3; ++k)
-                    if ((rb[p] >> k) & 1u) R[o++] = contact_ray(P, q, side, E, k);
-            } else {
-                R[o] = contact_ray(P, q, side, E, -1);
-            }
             cg_contact c;
             c.query = q;
             c.side = side;
@@ -772,22 +1349,31 @@ __global__ void __launch_bounds__(256) contacts_order_kernel(const ContactParams
             P.ctmp[base + p] = c;
         }
         __syncthreads();
-        // the mean origin: std::accumulate over the rays in order, one
-        // coordinate per lane
-        if (t < 3u) {
-            float s = 0.0f;
-            for (uint32_t r = 0; r < n_rays; ++r) s = s + R[r].origin[t];
-            fold[t] = s;
+    }
+    // the mean origin: std::accumulate over the rays in order, one coordinate
+    // per lane, from shared memory a chunk of rays at a time
+    {
+        constexpr uint32_t kStageRays = kOrderSmemWords / 3u;
+        float* stage = reinterpret_cast<float*>(smem);
+        float acc = 0.0f;
+        for (uint32_t r0 = 0; r0 < n_rays; r0 += kStageRays) {
+            const uint32_t m = n_rays - r0 < kStageRays ? n_rays - r0 : kStageRays;
+            for (uint32_t i = t; i < 3u * m; i += T) stage[i] = R[r0 + i / 3u].origin[i % 3u];
+            __syncthreads();
+            if (t < 3u) {
+#pragma unroll 8
+                for (uint32_t r = 0; r < m; ++r) acc = acc + stage[3u * r + t];
+            }
+            __syncthreads();
         }
-    } else if (t < 3u) {
-        fold[t] = 0.0f;
+        if (t < 3u) fold[t] = acc;
     }
     __syncthreads();
     if (t == 0u) {
         // CreateUncollideRays.cpp:185-198: the sum over the count (0 / 0 for
         // a side without rays), the second side's moved back to its space
-        const float cnt = float(n_rays);
-        float3 avg = divs3(make_float3(fold[0], fold[1], fold[2]), cnt);
+        const float cnt_f = float(n_rays);
+        float3 avg = divs3(make_float3(fold[0], fold[1], fold[2]), cnt_f);
         cg_ray_average* A = P.averages + q;
         if (side) {
             avg = xform(inverse4(query_mat(P.q + q)), avg, 1.0f);
@@ -806,8 +1392,54 @@ __global__ void __launch_bounds__(256) contacts_order_kernel(const ContactParams
     }
 }
 
+// The maps, largest first (by size class: the bit length of the triangle
+// count), for the order kernel's blocks to take in that order.
+__global__ void __launch_bounds__(1024) contacts_rank_kernel(const ContactParams P) {
+    __shared__ uint32_t count[33], start[33];
+    const uint32_t m = 2u * P.n_queries;
+    if (threadIdx.x < 33u) count[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const uint32_t n = P.map_fill[i];
+        atomicAdd(count + (n ? 32u - __clz(n) : 0u), 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t off = 0;
+        for (int c = 32; c >= 0; --c) {
+            start[c] = off;
+            off += count[c];
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const uint32_t n = P.map_fill[i];
+        P.map_order[atomicAdd(start + (n ? 32u - __clz(n) : 0u), 1u)] = i;
+    }
+}
+
+// Persistent: each block takes the next map of the largest-first list.
+__global__ void __launch_bounds__(256, 2) contacts_order_kernel(const ContactParams P) {
+    extern __shared__ __align__(16) uint32_t smem_order[];
+    __shared__ uint32_t part[64];
+    __shared__ float fold[3];
+    __shared__ uint32_t next_map;
+    const uint32_t n_maps = 2u * P.n_queries;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t i = atomicAdd(&P.ctr->order_ticket, 1u);
+            next_map = i < n_maps ? P.map_order[i] : ~0u;
+        }
+        __syncthreads();
+        const uint32_t map = next_map;
+        if (map == ~0u) break;
+        order_map(P, map, smem_order, part, fold);
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(1024) contacts_offsets_kernel(const ContactParams P) {
-    __shared__ uint32_t part[1024];
+    __shared__ uint32_t part[64];
     const uint32_t m = 2u * P.n_queries;
     const uint32_t nc = block_scan(
         m, part, [&](uint32_t i) { return P.map_fill[i]; }, [&](uint32_t i, uint32_t v) { P.map_coff[i] = v; });
@@ -835,7 +1467,7 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
             P.map_fill[map] = 0u;
         }
     }
-    // the table slots this launch took
+    // the table slots and leaf-pair marks this launch took
     const uint32_t ns = n_slots(P);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += gridDim.x * blockDim.x) {
         ContactSlot e;
@@ -844,6 +1476,9 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
         e.offset = 0u;
         P.table[P.occupied[j]] = e;
     }
+    const uint32_t nk = min(P.ctr->n_kleaf, P.kleaf_cap);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nk; j += gridDim.x * blockDim.x)
+        P.leaf_mark[P.kleaf[j]] = 0u;
 }
 
 __global__ void init_tables_kernel(ContactSlot* table, uint32_t n_slots, unsigned long long* vkeys, uint32_t* vval,
@@ -929,14 +1564,23 @@ cudaError_t launch_leaf_keys(const LeafKeyParams& p, uint32_t grid, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s) {
+cudaError_t contacts_order_occupancy(int* blocks_per_sm) {
+    const int smem = int(kOrderSmemWords * sizeof(uint32_t));
+    cudaError_t e = cudaFuncSetAttribute(contacts_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, contacts_order_kernel, 256, smem);
+}
+
+cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t order_grid, cudaStream_t s) {
     if (!p.n_queries) return cudaSuccess;
     const uint32_t maps = 2u * p.n_queries;
     contacts_pairs_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_scan_kernel<<<1, 1024, 0, s>>>(p);
+    contacts_alloc_kernel<<<grid, 256, 0, s>>>(p);
     contacts_scatter_kernel<<<grid, 256, 0, s>>>(p);
+    contacts_paths_kernel<<<grid, 256, 0, s>>>(p);
     contacts_fold_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_order_kernel<<<maps, 256, kOrderSmem * 8u * sizeof(uint32_t), s>>>(p);
+    contacts_rank_kernel<<<1, 1024, 0, s>>>(p);
+    contacts_order_kernel<<<maps < order_grid ? maps : order_grid, 256, kOrderSmemWords * sizeof(uint32_t), s>>>(p);
     contacts_offsets_kernel<<<1, 1024, 0, s>>>(p);
     contacts_emit_kernel<<<maps < grid ? maps : grid, 256, 0, s>>>(p);
     return cudaGetLastError();

@@ -106,6 +106,7 @@ struct cg_ctx {
     uint32_t blocks = 0;         // persistent traversal grid
     uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
     uint32_t contact_blocks = 0;                       // contact kernels: one resident wave
+    uint32_t order_blocks = 0;                         // the persistent contact order kernel
     uint32_t energy_blocks = 0;                        // energy kernels: one resident wave
 
     // trees
@@ -146,11 +147,17 @@ struct cg_ctx {
         ContactSlot* table = nullptr;
         uint32_t table_slots = 0;
         uint32_t* occupied = nullptr;
+        uint4* slot_info = nullptr;
         float4* pg_geom = nullptr;
         uint4* pg_link = nullptr;
         uint32_t* pg_mask = nullptr;
         unsigned long long* contrib = nullptr;
-        uint32_t* maps = nullptr;  // 6 arrays of 2 max_queries: count, offset, fill, rays, record and ray offsets
+        uint32_t* leaf_mark = nullptr;  // per leaf-list entry, zero between launches
+        uint32_t* kleaf = nullptr;
+        ulonglong2* kpath = nullptr;
+        uint32_t kleaf_cap = 0;
+        uint32_t* maps = nullptr;  // 7 arrays of 2 max_queries: count, offset, fill, rays, record and ray
+                                   // offsets, the largest-first order
         ContactElem* elems = nullptr;
         uint32_t* work = nullptr;
         unsigned long long* vkeys = nullptr;
@@ -247,7 +254,7 @@ int check_config(cg_ctx* c, const cg_config* cfg);
 int alloc_buffers(cg_ctx* c);
 bool growth_schedule(uint32_t max_elems, uint32_t* start, uint32_t* buckets, uint32_t* n);
 int sync_tree_table(cg_ctx* c);
-void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta);
+void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta, uint32_t split);
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s,
                  const CopyOutParams* pairs_copy = nullptr);
 int stats_from(cg_ctx* c, const Counters& k, cg_stats* st);

@@ -8,11 +8,14 @@
 //              k are records rec_base + 2k + 2 (left) and + 2k + 3 (right), so
 //              one node's children share a 128-byte line.
 //              q0 = (c.x, c.y, c.z, u.x)  q1 = (u.y, u.z, v.x, v.y)
-//              q2 = (v.z, w.x, w.y, w.z)  q3 = (ref, meta, surface, 0)
+//              q2 = (v.z, w.x, w.y, w.z)  q3 = (ref, meta, surface, split)
 //              ref  = absolute record index of the left child (inner box), or
 //                     absolute index of the leaf's first triangle
 //              meta = triangle count | 0x80000000 for a leaf
 //              surface = Paralgram::GetSurface of the box, precomputed
+//              split = absolute index of the right child's first triangle
+//                      (inner box; 0 for a leaf): a triangle t of the subtree
+//                      lies under the right child when t >= split
 //   triangles: float4[3 * n], 48 bytes per triangle in leaf (DFS) order,
 //              (p_k.xyz, vertex index k as bits) for k = 0, 1, 2; a tree's
 //              triangles start at tri_base.
@@ -46,7 +49,6 @@ struct DevTree {
     uint32_t live;
     uint32_t pad;
     const float* nrm;
-    const uint2* ranges;  // per record (tree-local): first triangle and triangle count of its subtree
 };
 
 // A query as the kernels read it: relative matrix columns, the first
@@ -91,6 +93,10 @@ struct Counters {
     unsigned int c_overflow;     // CONTACT_* bits
     unsigned int n_elems;        // triangles with contacts (non-zero weight): the contact records
     unsigned int prev_vertices;  // vertex-set slots earlier launches took and no launch emptied yet
+    unsigned int n_kleaf;        // leaf pairs with colliding pairs (listed for their descent paths)
+    unsigned int contrib_used;   // contribution-list entries given to slots
+    unsigned int order_ticket;   // maps taken by the order kernel's blocks
+    unsigned int pad_c;
 };
 
 enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ORDER = 8u };
@@ -124,10 +130,14 @@ struct alignas(16) ContactElem {
 // buckets[e] (the whole table is rehashed into it when start[e] is inserted).
 constexpr uint32_t kMaxSchedule = 40;
 
-// Order kernel working memory: maps of up to kOrderSmem triangles are ordered
-// in shared memory, larger ones in global memory (kOrderWords words per slot).
-constexpr uint32_t kOrderSmem = 1024;
-constexpr uint32_t kOrderWords = 18;
+// Order kernel working memory: a map whose working set and vertex set fit
+// kOrderSmemWords words (every map of up to 1,024 triangles) is ordered in
+// shared memory, larger ones in global memory (kOrderWords words per
+// element).
+constexpr uint32_t kOrderSmemWords = 24576;
+constexpr uint32_t kOrderWords = 24;
+constexpr uint32_t kFoldThread = 8;  // contributions a slot's own thread folds (more: its warp)
+constexpr uint32_t kFoldSmem = 256;  // contributions a fold warp sorts in shared memory (more: in place)
 
 struct ContactParams {
     const PackedQuery* q;
@@ -144,10 +154,16 @@ struct ContactParams {
     uint32_t table_mask;
     uint32_t max_contacts;      // contact slots (and records) a launch can hold
     uint32_t* occupied;         // slots taken this launch, in the order they were taken
+    uint4* slot_info;           // per entry of occupied: its key (low, high word), first contribution, count
     float4* pg_geom;            // per pair: weight * midpoint, weight
     uint4* pg_link;             // per pair: both triangles' slots and places in their slots' lists
     uint32_t* pg_mask;          // per pair: "not outside" bits of the first triangle | the second's << 3
-    unsigned long long* contrib;// contributions: (other triangle << 32) | (pair << 1) | side
+    unsigned long long* contrib;// contributions by slot: (other triangle << 32) | (pair << 1) | side
+    uint32_t* leaf_mark;        // per leaf pair of the list: 0, or 1 + its place in kleaf once listed
+    uint32_t* kleaf;            // leaf pairs with colliding pairs, listed once each
+    ulonglong2* kpath;          // their descent paths (high, low)
+    uint32_t kleaf_cap;
+    uint32_t* map_order;        // the maps, largest first
     uint32_t* map_cnt;          // per map (2 query + side): slots; then per map element offsets
     uint32_t* map_off;
     uint32_t* map_fill;         // elements (triangles with contacts)
@@ -171,7 +187,8 @@ struct ContactParams {
     uint32_t sched_buckets[kMaxSchedule];
 };
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, cudaStream_t s);
+cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t order_grid, cudaStream_t s);
+cudaError_t contacts_order_occupancy(int* blocks_per_sm);
 
 // Descent paths of the stored candidate leaf pairs (CG_DFS_ORDER).
 struct LeafKeyParams {
@@ -459,6 +476,7 @@ struct BuildFlat {           // a node's place in its tree's layout
     uint32_t leaf_off;       // leaves before it in pre-order
     uint32_t rec;            // its record (tree-local)
     uint32_t prec;           // its parent's record
+    uint32_t split_off;      // first triangle of its second (right) child's subtree (inner nodes)
 };
 struct BuildEmit {           // a built tree's arena places
     uint32_t rec_base, tri_base, n_recs, pad;
