@@ -57,7 +57,7 @@ void free_buffers(cg_ctx* c) {
     c->d_leaf_keys = nullptr;
     cudaFree(c->d_trace);
     auto& t = c->ct;
-    for (void* p : {(void*)t.pair_aux, (void*)t.table, (void*)t.occupied, (void*)t.slot_info, (void*)t.pg_geom, (void*)t.pg_link,
+    for (void* p : {(void*)t.pair_aux, (void*)t.table, (void*)t.occupied, (void*)t.slot_info, (void*)t.big_slots, (void*)t.pg_geom, (void*)t.pg_link,
                     (void*)t.pg_mask, (void*)t.contrib, (void*)t.leaf_mark, (void*)t.kleaf, (void*)t.kpath,
                     (void*)t.maps, (void*)t.elems, (void*)t.work, (void*)t.vkeys,
                     (void*)t.vval, (void*)t.vocc, (void*)t.ctmp, (void*)t.rtmp, (void*)t.contacts, (void*)t.rays,
@@ -272,6 +272,9 @@ int alloc_buffers(cg_ctx* c) {
     int oocc = 0;
     CG_CUDA(contacts_order_occupancy(&oocc), "occupancy");
     c->order_blocks = uint32_t(std::max(oocc, 1) * c->sm_count);
+    int focc = 0;
+    CG_CUDA(contacts_fold_occupancy(&focc), "occupancy");
+    c->fold_blocks = uint32_t(std::max(focc, 1) * c->sm_count);
     CG_CUDA(deform_smem_limit(), "deform kernel shared memory");
     c->copy_blocks = uint32_t(4 * c->sm_count);
     int gocc = 0;
@@ -306,6 +309,7 @@ int alloc_buffers(cg_ctx* c) {
         CG_CUDA(cudaMalloc(&t.table, sizeof(ContactSlot) * t.table_slots), "alloc contact table");
         CG_CUDA(cudaMalloc(&t.occupied, sizeof(uint32_t) * t.table_slots), "alloc contact list");
         CG_CUDA(cudaMalloc(&t.slot_info, sizeof(uint4) * t.table_slots), "alloc contact slot list");
+        CG_CUDA(cudaMalloc(&t.big_slots, sizeof(uint32_t) * t.table_slots), "alloc contact slot list");
         CG_CUDA(cudaMalloc(&t.pg_geom, sizeof(float4) * mp), "alloc pair geometry");
         CG_CUDA(cudaMalloc(&t.pg_link, sizeof(uint4) * mp), "alloc pair links");
         CG_CUDA(cudaMalloc(&t.pg_mask, sizeof(uint32_t) * mp), "alloc pair masks");
@@ -458,6 +462,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.max_contacts = uint32_t(c->cfg.max_contacts);
         cp.occupied = t.occupied;
         cp.slot_info = t.slot_info;
+        cp.big_slots = t.big_slots;
         cp.pg_geom = t.pg_geom;
         cp.pg_link = t.pg_link;
         cp.pg_mask = t.pg_mask;
@@ -491,7 +496,7 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
             cp.sched_start[k] = c->sched_start[k];
             cp.sched_buckets[k] = c->sched_buckets[k];
         }
-        CG_CUDA(launch_contacts(cp, c->contact_blocks, c->order_blocks, s), "contact kernels");
+        CG_CUDA(launch_contacts(cp, c->contact_blocks, c->fold_blocks, c->order_blocks, s), "contact kernels");
     }
     if (pairs_copy) CG_CUDA(cudaStreamWaitEvent(s, c->ev_joined, 0), "join");
     return CG_OK;

@@ -315,6 +315,7 @@ __device__ uint32_t block_scan(uint32_t n, uint32_t* part, Get get, Put put) {
 struct WalkRec {
     Box box;
     uint32_t ref, meta, split;
+    float surf;
 };
 
 __device__ __forceinline__ WalkRec walk_rec(const float4* recs, uint32_t r) {
@@ -327,8 +328,23 @@ __device__ __forceinline__ WalkRec walk_rec(const float4* recs, uint32_t r) {
     R.box.w = make_float3(c.y, c.z, c.w);
     R.ref = __float_as_uint(d.x);
     R.meta = __float_as_uint(d.y);
+    R.surf = d.z;
     R.split = __float_as_uint(d.w);
     return R;
+}
+
+// A path of `depth` splits (1 <= depth < 128) held in the low bits of
+// (hi, lo), moved to the top (left-aligned in 128 bits).
+__device__ __forceinline__ void align_path(unsigned long long& hi, unsigned long long& lo, uint32_t depth) {
+    if (depth == 0u || depth >= 128u) return;
+    const uint32_t s = 128u - depth;
+    if (s >= 64u) {
+        hi = lo << (s - 64u);
+        lo = 0ull;
+    } else {
+        hi = (hi << s) | (lo >> (64u - s));
+        lo <<= s;
+    }
 }
 
 // The path of the simultaneous descent (OBBtree::IntersectOBBtreesRecursive,
@@ -382,15 +398,78 @@ __device__ void descent_path(const PackedQuery* queries, const DevTree* trees, c
         lo = (lo << 1) | bit;
         ++depth;
     }
-    if (depth == 0u || depth >= 128u) return;
-    const uint32_t s = 128u - depth;
-    if (s >= 64u) {
-        hi = lo << (s - 64u);
-        lo = 0ull;
-    } else {
-        hi = (hi << s) | (lo >> (64u - s));
-        lo <<= s;
+    align_path(hi, lo, depth);
+}
+
+constexpr uint32_t kWayLevels = 64;  // levels of one tree's way a lane stages (deeper: descent_path)
+constexpr uint32_t kPathWarps = 4;   // warps of a paths block
+
+// descent_path for 16 leaf pairs per warp (all lanes call it; `valid`: this
+// lane pair has leaf pair lp), with the two trees' ways down walked side by
+// side: the way to a leaf is fixed by the leaf alone, so lane 2i follows the
+// first tree to the pair's first leaf and lane 2i + 1 the second tree to its
+// second leaf, both chains of dependent loads in flight together; each lane
+// stages per level its node's surface (the second tree's box as transformed)
+// in its row of `way` and keeps the child taken in `bits`. Lane 2i then
+// merges the two ways by the reference's split rule into the path (its hi,
+// lo, depth; the other lanes' are zero). A way of more than kWayLevels
+// levels falls back to descent_path.
+__device__ void paired_path(const PackedQuery* queries, const DevTree* trees, const float4* recs, uint4 lp, bool valid,
+                            float (*way)[kWayLevels + 1], unsigned long long& hi, unsigned long long& lo,
+                            uint32_t& depth) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool second = (lane & 1u) != 0u;
+    uint32_t d = 0;
+    unsigned long long bits = 0ull;
+    bool deep = false;
+    if (valid) {
+        const PackedQuery* Q = queries + lp.x;
+        const uint32_t base = trees[second ? __ldg(&Q->tree_b) : __ldg(&Q->tree_a)].rec_base;
+        const uint32_t target = second ? lp.z : lp.y;
+        const Mat4 M = query_mat(Q);
+        float* row = way[lane];
+        uint32_t node = base + 1u;
+        for (;;) {
+            const WalkRec R = walk_rec(recs, node);
+            if (R.meta & kLeafFlag) break;
+            if (d == kWayLevels) {
+                deep = true;
+                break;
+            }
+            row[d] = second ? surface(xform_box(M, R.box)) : R.surf;
+            const uint32_t bit = target >= R.split ? 1u : 0u;
+            bits |= (unsigned long long)bit << d;
+            node = R.ref + bit;
+            ++d;
+        }
     }
+    __syncwarp();
+    const uint32_t d2 = __shfl_down_sync(kFullMask, d, 1);
+    const unsigned long long bits2 = __shfl_down_sync(kFullMask, bits, 1);
+    const bool deep2 = __shfl_down_sync(kFullMask, deep ? 1u : 0u, 1) != 0u;
+    hi = lo = 0ull;
+    depth = 0u;
+    if (second || !valid) return;
+    if (deep || deep2) {
+        descent_path(queries, trees, recs, lp, hi, lo, depth);
+        return;
+    }
+    const float* SA = way[lane];
+    const float* SB = way[lane + 1u];
+    uint32_t i = 0, j = 0;
+    while (i < d || j < d2) {
+        const bool la = i == d, lb = j == d2;
+        const bool split_a = (!la && !lb) ? (SA[i] >= SB[j]) : !la;
+        const uint32_t bit = split_a ? uint32_t(bits >> i) & 1u : uint32_t(bits2 >> j) & 1u;
+        hi = (hi << 1) | (lo >> 63);
+        lo = (lo << 1) | bit;
+        if (split_a)
+            ++i;
+        else
+            ++j;
+        ++depth;
+    }
+    align_path(hi, lo, depth);
 }
 
 // Ascending bitonic sort of n2 (a power of two) entries by the whole block.
@@ -410,41 +489,6 @@ __device__ void bitonic(K* a, uint32_t n2, Less less) {
                 }
             }
             __syncthreads();
-        }
-}
-
-// Ascending bitonic sort of the warp's 32 values, one per lane.
-__device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v) {
-    const uint32_t lane = threadIdx.x & 31u;
-#pragma unroll
-    for (uint32_t k = 2; k <= 32; k <<= 1)
-#pragma unroll
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            const unsigned long long o = __shfl_xor_sync(kFullMask, v, j);
-            const bool lower = (lane & j) == 0u;
-            const bool up = (lane & k) == 0u;
-            v = (lower == up) ? (v < o ? v : o) : (v > o ? v : o);
-        }
-    return v;
-}
-
-// Ascending bitonic sort of n2 (a power of two) values in shared memory by
-// one warp.
-__device__ void warp_sort_smem(unsigned long long* a, uint32_t n2) {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t k = 2; k <= n2; k <<= 1)
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = lane; i < n2; i += 32u) {
-                const uint32_t l = i ^ j;
-                if (l > i) {
-                    const unsigned long long x = a[i], y = a[l];
-                    if ((i & k) == 0u ? y < x : x < y) {
-                        a[i] = y;
-                        a[l] = x;
-                    }
-                }
-            }
-            __syncwarp();
         }
 }
 
@@ -686,7 +730,8 @@ __global__ void __launch_bounds__(256) contacts_pairs_kernel(const ContactParams
 }
 
 // Each slot's place in the contribution list (one atomic per warp of 32
-// slots), and, in the first block, the maps' element offsets.
+// slots), the list of slots for the fold's warps, and, in the first block,
+// the maps' element offsets.
 __global__ void __launch_bounds__(256) contacts_alloc_kernel(const ContactParams P) {
     __shared__ uint32_t part[64];
     const uint32_t ns = n_slots(P);
@@ -697,10 +742,13 @@ __global__ void __launch_bounds__(256) contacts_alloc_kernel(const ContactParams
         ContactSlot* sl = j < ns ? P.table + P.occupied[j] : nullptr;
         const ContactSlot v = sl ? *sl : ContactSlot{kEmptyKey, 0u, 0u};
         const uint32_t off = warp_append(&P.ctr->contrib_used, v.count);
+        const unsigned big = v.count > kFoldThread ? 1u : 0u;
+        const uint32_t bi = warp_append(&P.ctr->n_big, big);
         if (sl) {
             sl->offset = off;
             P.slot_info[j] = make_uint4(uint32_t(v.key), uint32_t(v.key >> 32), off, v.count);
         }
+        if (big) P.big_slots[bi] = j;  // at most one entry per slot: the list never outgrows the table
     }
     if (blockIdx.x == 0)
         block_scan(
@@ -723,14 +771,22 @@ __global__ void __launch_bounds__(256) contacts_scatter_kernel(const ContactPara
 }
 
 // The descent path of every listed leaf pair (those with colliding pairs).
-__global__ void __launch_bounds__(256) contacts_paths_kernel(const ContactParams P) {
+__global__ void __launch_bounds__(kPathWarps * 32) contacts_paths_kernel(const ContactParams P) {
+    __shared__ float way[kPathWarps][32][kWayLevels + 1];
     const uint32_t nk = min(*reinterpret_cast<const volatile unsigned*>(&P.ctr->n_kleaf), P.kleaf_cap);
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nk; j += gridDim.x * blockDim.x) {
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    for (uint32_t b = (blockIdx.x * kPathWarps + wib) * 16u; b < nk; b += gridDim.x * kPathWarps * 16u) {
+        const uint32_t j = b + (lane >> 1);
+        const bool valid = j < nk;
+        const uint4 lp = valid ? P.leaf_list[P.kleaf[j]] : make_uint4(0u, 0u, 0u, 0u);
         unsigned long long hi, lo;
         uint32_t depth;
-        descent_path(P.q, P.trees, P.recs, P.leaf_list[P.kleaf[j]], hi, lo, depth);
-        if (depth >= 128u) atomicOr(&P.ctr->c_overflow, CONTACT_ORDER);
-        P.kpath[j] = make_ulonglong2(hi, lo);
+        paired_path(P.q, P.trees, P.recs, lp, valid, way[wib], hi, lo, depth);
+        if (!(lane & 1u) && valid) {
+            if (depth >= 128u) atomicOr(&P.ctr->c_overflow, CONTACT_ORDER);
+            P.kpath[j] = make_ulonglong2(hi, lo);
+        }
+        __syncwarp();  // the rows are the next round's
     }
 }
 
@@ -842,26 +898,68 @@ __device__ __forceinline__ void fold_thread(const ContactParams& P, unsigned lon
     F.finish();
 }
 
+// A contribution's pair data staged for the folding lane.
+struct FoldItem {
+    float4 g;
+    uint32_t leaf, mk;
+};
+
+// Ascending bitonic sort by one warp of n2 (32, 64 or 128) values, four per
+// lane (value i = lane + 32 r in v[r]): between a lane's own values in
+// registers, within a row by shuffles.
+__device__ __forceinline__ void warp_sort128(unsigned long long (&v)[4], uint32_t n2) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t k = 2; k <= n2; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32u) {
+                const uint32_t jj = j >> 5;
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int f = r + 1; f < 4; ++f)
+                        if (uint32_t(r ^ f) == jj) {
+                            const bool asc = ((lane + 32u * uint32_t(r)) & k) == 0u;
+                            const unsigned long long lo = v[r], hi = v[f];
+                            const bool sw = (hi < lo) == asc;
+                            v[r] = sw ? hi : lo;
+                            v[f] = sw ? lo : hi;
+                        }
+            } else {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    if (32u * uint32_t(r) < n2) {
+                        const uint32_t i = lane + 32u * uint32_t(r);
+                        const unsigned long long o = __shfl_xor_sync(kFullMask, v[r], j);
+                        const bool keep_min = ((i & j) == 0u) == ((i & k) == 0u);
+                        v[r] = keep_min ? (o < v[r] ? o : v[r]) : (o > v[r] ? o : v[r]);
+                    }
+                }
+            }
+        }
+}
+
+constexpr uint32_t kFoldStage = 128;  // contributions a fold warp sorts in registers and stages at once
+
 // One slot of more than kFoldThread contributions by the whole warp (all
-// lanes call it): sorted in registers (<= 32), in the warp's shared buffer
-// (<= kFoldSmem) or in place; then every lane folds them in order.
+// lanes call it): sorted in registers (<= kFoldStage) or, rarely, in place by
+// lane 0; kFoldStage at a time, every lane stages its contributions' pair
+// data in `stage` (all loads in flight together) and lane 0 folds them in
+// order (F is lane 0's).
 __device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32_t off, uint32_t c,
-                          unsigned long long* buf, TriFold& F) {
+                          FoldItem* stage, TriFold& F) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t side = uint32_t(key >> 63);
-    unsigned long long mine = ~0ull;
+    unsigned long long v[4];
     const unsigned long long* S = nullptr;
-    if (c <= 32u) {
-        mine = warp_sort32(lane < c ? P.contrib[off + lane] : ~0ull);
-    } else if (c <= kFoldSmem) {
-        uint32_t n2 = 64;
-        while (n2 < c) n2 <<= 1;
-        for (uint32_t i = lane; i < n2; i += 32u) buf[i] = i < c ? P.contrib[off + i] : ~0ull;
-        __syncwarp();
-        warp_sort_smem(buf, n2);
-        S = buf;
+    if (c <= kFoldStage) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t i = lane + 32u * uint32_t(r);
+            v[r] = i < c ? P.contrib[off + i] : ~0ull;
+        }
+        warp_sort128(v, c <= 32u ? 32u : (c <= 64u ? 64u : 128u));
     } else {
-        unsigned long long* G = P.contrib + off;  // rare: insertion sort in place by lane 0
+        unsigned long long* G = P.contrib + off;
         if (lane == 0)
             for (uint32_t a = 1; a < c; ++a) {
                 const unsigned long long x = G[a];
@@ -875,29 +973,28 @@ __device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32
         __syncwarp();
         S = G;
     }
-    // 32 contributions at a time: each lane loads one's data, every lane
-    // folds them in order
-    for (uint32_t a0 = 0; a0 < c; a0 += 32u) {
-        const uint32_t a = a0 + lane;
-        uint32_t leaf = 0;
-        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-        unsigned mk = 7u;
-        if (a < c) {
-            const uint32_t pid = uint32_t(S ? S[a] : mine) >> 1;
-            leaf = __ldg(&P.pair_aux[pid].z);
-            g = __ldg(P.pg_geom + pid);
-            mk = (__ldg(P.pg_mask + pid) >> (3u * side)) & 7u;
+    for (uint32_t a0 = 0; a0 < c; a0 += kFoldStage) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t a = a0 + lane + 32u * uint32_t(r);
+            if (a < c) {
+                const unsigned long long x = S ? S[a] : v[r];
+                const uint32_t pid = uint32_t(x) >> 1;
+                FoldItem it;
+                it.leaf = __ldg(&P.pair_aux[pid].z);
+                it.g = __ldg(P.pg_geom + pid);
+                it.mk = (__ldg(P.pg_mask + pid) >> (3u * side)) & 7u;
+                stage[a - a0] = it;
+            }
         }
-        const uint32_t m = c - a0 < 32u ? c - a0 : 32u;
-        for (uint32_t k = 0; k < m; ++k) {
-            const uint32_t lk = __shfl_sync(kFullMask, leaf, k);
-            const float4 gk = make_float4(__shfl_sync(kFullMask, g.x, k), __shfl_sync(kFullMask, g.y, k),
-                                          __shfl_sync(kFullMask, g.z, k), __shfl_sync(kFullMask, g.w, k));
-            F.add(lk, gk, __shfl_sync(kFullMask, mk, k));
+        __syncwarp();
+        if (lane == 0) {
+            const uint32_t m = c - a0 < kFoldStage ? c - a0 : kFoldStage;
+            for (uint32_t k = 0; k < m; ++k) F.add(stage[k].leaf, stage[k].g, stage[k].mk);
         }
+        __syncwarp();
     }
-    F.finish();
-    __syncwarp();
+    if (lane == 0) F.finish();
 }
 
 // A thread per slot: the triangle's contributions sorted by the other
@@ -905,11 +1002,13 @@ __device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32
 // triangle's order, and its leaf pairs in the order of the other leaf's first
 // triangle), the reference's folds in that order, the path of the first leaf
 // pair of non-zero weight; the triangle into its map. A slot of more than
-// kFoldThread contributions is folded by its warp afterwards.
+// kFoldThread contributions is folded by a warp of its own, the listed slots
+// taken from the grid's last warp down (one resident wave: those warps have
+// few or no slots of their own).
 constexpr uint32_t kFoldWarps = 8;
 
-__global__ void __launch_bounds__(256) contacts_fold_kernel(const ContactParams P) {
-    __shared__ unsigned long long buf[kFoldWarps][kFoldSmem];
+__global__ void __launch_bounds__(256, 3) contacts_fold_kernel(const ContactParams P) {
+    __shared__ FoldItem stage[kFoldWarps][kFoldStage];
     const uint32_t ns = n_slots(P);
     const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -922,15 +1021,16 @@ __global__ void __launch_bounds__(256) contacts_fold_kernel(const ContactParams 
             fold_thread(P, key, si.z, si.w, F);
             put_elem(P, key, F);
         }
-        unsigned big = __ballot_sync(kFullMask, si.w > kFoldThread);
-        while (big) {
-            const uint32_t l = uint32_t(__ffs(big)) - 1u;
-            big &= big - 1u;
-            const unsigned long long k = __shfl_sync(kFullMask, key, l);
-            TriFold F;
-            fold_warp(P, k, __shfl_sync(kFullMask, si.z, l), __shfl_sync(kFullMask, si.w, l), buf[wib], F);
-            if (lane == 0) put_elem(P, k, F);
-        }
+    }
+    const uint32_t n_warps = gridDim.x * kFoldWarps;
+    const uint32_t gw = blockIdx.x * kFoldWarps + wib;
+    const uint32_t nb = *reinterpret_cast<const volatile unsigned*>(&P.ctr->n_big);
+    for (uint32_t b = n_warps - 1u - gw; b < nb; b += n_warps) {
+        const uint4 si = P.slot_info[P.big_slots[b]];
+        const unsigned long long key = (unsigned long long)si.y << 32 | si.x;
+        TriFold F;
+        fold_warp(P, key, si.z, si.w, stage[wib], F);
+        if (lane == 0) put_elem(P, key, F);
     }
 }
 
@@ -1547,20 +1647,28 @@ cudaError_t launch_copy_out(const CopyOutParams& p, uint32_t blocks, cudaStream_
 // reading them back in the reference's depth-first order: keys[i] = (path
 // high 64 bits, path low 64 bits) of leaf pair i; ERR_DEEP in *error when a
 // path has 128 or more splits.
-__global__ void __launch_bounds__(256) leaf_keys_kernel(const LeafKeyParams P) {
+__global__ void __launch_bounds__(kPathWarps * 32) leaf_keys_kernel(const LeafKeyParams P) {
+    __shared__ float way[kPathWarps][32][kWayLevels + 1];
     const unsigned long long n_all = *reinterpret_cast<const volatile unsigned long long*>(P.n_leafs);
     const uint32_t n = uint32_t(n_all < P.leaf_cap ? n_all : P.leaf_cap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    for (uint32_t b = (blockIdx.x * kPathWarps + wib) * 16u; b < n; b += gridDim.x * kPathWarps * 16u) {
+        const uint32_t i = b + (lane >> 1);
+        const bool valid = i < n;
+        const uint4 lp = valid ? P.leaf_list[i] : make_uint4(0u, 0u, 0u, 0u);
         unsigned long long hi, lo;
         uint32_t depth;
-        descent_path(P.q, P.trees, P.recs, P.leaf_list[i], hi, lo, depth);
-        if (depth >= 128u) atomicOr(P.error, ERR_DEEP);
-        P.keys[i] = make_ulonglong2(hi, lo);
+        paired_path(P.q, P.trees, P.recs, lp, valid, way[wib], hi, lo, depth);
+        if (!(lane & 1u) && valid) {
+            if (depth >= 128u) atomicOr(P.error, ERR_DEEP);
+            P.keys[i] = make_ulonglong2(hi, lo);
+        }
+        __syncwarp();
     }
 }
 
 cudaError_t launch_leaf_keys(const LeafKeyParams& p, uint32_t grid, cudaStream_t s) {
-    leaf_keys_kernel<<<grid, 256, 0, s>>>(p);
+    leaf_keys_kernel<<<2u * grid, kPathWarps * 32, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -1571,14 +1679,19 @@ cudaError_t contacts_order_occupancy(int* blocks_per_sm) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, contacts_order_kernel, 256, smem);
 }
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t order_grid, cudaStream_t s) {
+cudaError_t contacts_fold_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, contacts_fold_kernel, 256, 0);
+}
+
+cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t fold_grid, uint32_t order_grid,
+                            cudaStream_t s) {
     if (!p.n_queries) return cudaSuccess;
     const uint32_t maps = 2u * p.n_queries;
     contacts_pairs_kernel<<<grid, 256, 0, s>>>(p);
     contacts_alloc_kernel<<<grid, 256, 0, s>>>(p);
     contacts_scatter_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_paths_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_fold_kernel<<<grid, 256, 0, s>>>(p);
+    contacts_paths_kernel<<<2u * grid, kPathWarps * 32, 0, s>>>(p);
+    contacts_fold_kernel<<<fold_grid, 256, 0, s>>>(p);
     contacts_rank_kernel<<<1, 1024, 0, s>>>(p);
     contacts_order_kernel<<<maps < order_grid ? maps : order_grid, 256, kOrderSmemWords * sizeof(uint32_t), s>>>(p);
     contacts_offsets_kernel<<<1, 1024, 0, s>>>(p);

@@ -106,6 +106,7 @@ struct cg_ctx {
     uint32_t blocks = 0;         // persistent traversal grid
     uint32_t narrow_blocks = 0;  // persistent narrow-phase grid
     uint32_t contact_blocks = 0;                       // contact kernels: one resident wave
+    uint32_t fold_blocks = 0;                          // the contact fold kernel: one resident wave
     uint32_t order_blocks = 0;                         // the persistent contact order kernel
     uint32_t energy_blocks = 0;                        // energy kernels: one resident wave
 
@@ -148,6 +149,7 @@ struct cg_ctx {
         uint32_t table_slots = 0;
         uint32_t* occupied = nullptr;
         uint4* slot_info = nullptr;
+        uint32_t* big_slots = nullptr;
         float4* pg_geom = nullptr;
         uint4* pg_link = nullptr;
         uint32_t* pg_mask = nullptr;

@@ -96,7 +96,7 @@ struct Counters {
     unsigned int n_kleaf;        // leaf pairs with colliding pairs (listed for their descent paths)
     unsigned int contrib_used;   // contribution-list entries given to slots
     unsigned int order_ticket;   // maps taken by the order kernel's blocks
-    unsigned int pad_c;
+    unsigned int n_big;          // contact slots of more than kFoldThread contributions (listed for the fold)
 };
 
 enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ORDER = 8u };
@@ -137,7 +137,6 @@ constexpr uint32_t kMaxSchedule = 40;
 constexpr uint32_t kOrderSmemWords = 24576;
 constexpr uint32_t kOrderWords = 24;
 constexpr uint32_t kFoldThread = 8;  // contributions a slot's own thread folds (more: its warp)
-constexpr uint32_t kFoldSmem = 256;  // contributions a fold warp sorts in shared memory (more: in place)
 
 struct ContactParams {
     const PackedQuery* q;
@@ -155,6 +154,7 @@ struct ContactParams {
     uint32_t max_contacts;      // contact slots (and records) a launch can hold
     uint32_t* occupied;         // slots taken this launch, in the order they were taken
     uint4* slot_info;           // per entry of occupied: its key (low, high word), first contribution, count
+    uint32_t* big_slots;        // entries of occupied with more than kFoldThread contributions
     float4* pg_geom;            // per pair: weight * midpoint, weight
     uint4* pg_link;             // per pair: both triangles' slots and places in their slots' lists
     uint32_t* pg_mask;          // per pair: "not outside" bits of the first triangle | the second's << 3
@@ -187,8 +187,10 @@ struct ContactParams {
     uint32_t sched_buckets[kMaxSchedule];
 };
 
-cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t order_grid, cudaStream_t s);
+cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t fold_grid, uint32_t order_grid,
+                            cudaStream_t s);
 cudaError_t contacts_order_occupancy(int* blocks_per_sm);
+cudaError_t contacts_fold_occupancy(int* blocks_per_sm);
 
 // Descent paths of the stored candidate leaf pairs (CG_DFS_ORDER).
 struct LeafKeyParams {
