@@ -49,9 +49,10 @@ NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
 TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
 COUNTERS_BYTES = 144       # the launch counters, read back by cg_collide and by each result read
 # init, pack, traverse, narrow; contacts: pairs, scan, scatter, fold, order, offsets, emit
-STEP_KERNELS = 11
+STEP_KERNELS = 13
 STEP_FLAGS_DOC = ("CUDA graph: init + pack + persistent traversal + persistent narrow phase (FP64 recheck counted) "
-                  "+ contacts (pairs, scan, scatter, fold, order, offsets, emit)")
+                  "+ contacts in the reference's order (pairs, alloc, scatter, descent paths, fold, rank, order, "
+                  "offsets, emit)")
 CACHE_DOC = "L2 flushed (512 MB write) between timed GPU steps"
 
 
@@ -607,6 +608,65 @@ def run_deforming(args, ctx_factory, flush, stream, cpu_seconds: float) -> dict:
     return res
 
 
+def run_sharded(args, dist, rank, world, local, dev, stream, flush) -> dict:
+    """Strong scaling: the one 256-entity frame (seed 1002) split over the
+    ranks by cost (LPT, every rank computing the same partition); each rank
+    builds the trees its queries use and collides its share, event-timed; the
+    frame's time is the slowest rank's. The colliding pairs are then gathered
+    to every rank (fixed-width rows, all_gather_into_tensor), outside the
+    timed steps and timed on their own."""
+    import torch
+
+    from inmyroom_vulkan_gb300 import capi, scenes, shard
+
+    sc = scenes.scene(seed=1002)
+    pa, pb = sc.pairs[:, 0], sc.pairs[:, 1]
+    costs = shard.query_costs([sc.meshes[i].n_tris for i in pa], [sc.meshes[j].n_tris for j in pb])
+    parts = shard.lpt_partition(costs, world)
+    mine = parts[rank]
+    used = np.unique(sc.pairs[mine])
+    ctx = capi.Context(device=local, max_queries=max(4096, len(mine)), max_tri_pairs=1 << 22)
+    ids = np.zeros(len(sc.meshes), np.uint32)
+    ids[used] = ctx.build_trees([sc.meshes[i] for i in used])
+    qa, qb = pa[mine], pb[mine]
+    rel = np.stack([capi.relative_matrix(sc.mats[i], sc.mats[j]) for i, j in zip(qa, qb)])
+    q = capi.make_queries(ids[qa], ids[qb], rel)
+    d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
+    flags = capi.CG_CONTACTS | capi.CG_RECHECK
+    ctx.graph_capture(d_q.data_ptr(), len(q), flags)
+    for _ in range(max(args.warmup, 3)):
+        ctx.graph_launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    shard.barrier(dist)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        ev[k][0].record(stream)
+        ctx.graph_launch(stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+    st = ctx.sync_stats()
+    frame_ms = shard.max_over_ranks(ms, dist, dev) / args.steps
+    mine_tests = torch.tensor([float(st["tri_tests"])], dtype=torch.float64, device=dev)
+    dist.all_reduce(mine_tests)
+    tests = float(mine_tests.item())
+    rows = ctx.tri_pairs()
+    out_rows = np.zeros(len(rows), shard.PAIR_ROW_DTYPE)
+    out_rows["query"], out_rows["tri_a"], out_rows["tri_b"] = rows["query"], rows["tri_a"], rows["tri_b"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gathered = shard.gather_rows(out_rows, mine, dist, device=dev)
+    gather_ms = 1e3 * (time.perf_counter() - t0)
+    ctx.close()
+    loads = np.array([costs[p].sum() for p in parts])
+    return {"workload": "the scene of 256 rigid entities (seed 1002) split over the ranks by cost (LPT)",
+            "scaling": "strong", "value": tests / (frame_ms / 1e3), "unit": UNIT, "ms_per_frame": frame_ms,
+            "queries_per_rank": [int(len(p)) for p in parts], "load_spread": float(loads.max() / loads.min()),
+            "gathered_pairs": int(len(gathered)), "gather_ms": gather_ms,
+            "note": "unmeasured on hardware until a several-GPU run exists"}
+
+
 def run_gpu(args) -> dict:
     import torch
 
@@ -782,6 +842,7 @@ def run_gpu(args) -> dict:
     sweep = None
     if rank == 0 and not args.skip_sweep:
         sweep = run_sweep(args, local, flush, stream, min(args.cpu_seconds, 5.0))
+    sharded = run_sharded(args, dist, rank, world, local, dev, stream, flush) if world > 1 else None
     clk = clocks.summary()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -823,6 +884,8 @@ def run_gpu(args) -> dict:
         out["tree_build"] = tree_build
     if frame_line:
         out["frame"] = frame_line
+    if sharded:
+        out["sharded"] = sharded
     ctx.close()
     if dist:
         dist.destroy_process_group()

@@ -126,27 +126,65 @@ __global__ void build_points_kernel(const BuildParams B) {
     }
 }
 
-// s + x[0] + x[1] + ... + x[n-1], left to right in FP64. The adds are one
-// dependent chain; the loads are not, so they go in blocks of kChainBlock,
-// the next block in flight while the current one is added.
-constexpr uint32_t kChainBlock = 48;
+// Sum of x[0..n-1] in order, in FP64: the reference's std::accumulate. The
+// adds are one dependent chain, and on this part each FP64 instruction holds
+// the sub-partition's FP64 pipe for about 64 cycles, so the chain's pace is
+// one add per FP64 instruction time if its terms are at hand: they are loaded
+// 16 bytes (two terms) at a time, in blocks of kChainBlock, the next block in
+// flight while the current one is added (a chain that starts off a 16-byte
+// boundary takes its first term alone); then the tail, in order. Only the
+// reference's terms are added (adding a 0 could turn a -0 into +0).
+constexpr uint32_t kChainBlock = 64;
 __device__ __forceinline__ double chain_sum(const double* x, uint32_t n) {
     double s = 0.0;
-    double cur[kChainBlock], nxt[kChainBlock];
+    if (n && (reinterpret_cast<uintptr_t>(x) & 15u)) {
+        s = s + x[0];
+        ++x;
+        --n;
+    }
+    constexpr uint32_t H = kChainBlock / 2;
+    const double2* x2 = reinterpret_cast<const double2*>(x);
+    const uint32_t nb = n / kChainBlock;  // full blocks
+    double2 a[H], b[H];
+    if (nb > 0) {
 #pragma unroll
-    for (uint32_t k = 0; k < kChainBlock; ++k) cur[k] = k < n ? x[k] : 0.0;
-    for (uint32_t j = 0; j < n; j += kChainBlock) {
+        for (uint32_t k = 0; k < H; ++k) a[k] = __ldg(x2 + k);
+    }
+    uint32_t blk = 0;
+    for (; blk + 2u <= nb; blk += 2u) {
+        const double2* xb = x2 + size_t(blk) * H;
+        // blocks four and five ahead into L2 (four 128-byte lines each): the
+        // terms come from DRAM when a level's arrays outgrow L2
+        if (blk + 6u <= nb) {
 #pragma unroll
-        for (uint32_t k = 0; k < kChainBlock; ++k) {
-            const uint32_t i = j + kChainBlock + k;
-            nxt[k] = i < n ? x[i] : 0.0;
+            for (uint32_t k = 0; k < 8u; ++k) asm volatile("prefetch.global.L2 [%0];" ::"l"(xb + 4u * H + 8u * k));
         }
 #pragma unroll
-        for (uint32_t k = 0; k < kChainBlock; ++k)
-            if (j + k < n) s = s + cur[k];  // only the reference's terms: adding a 0 could flip a -0
+        for (uint32_t k = 0; k < H; ++k) b[k] = __ldg(xb + H + k);
 #pragma unroll
-        for (uint32_t k = 0; k < kChainBlock; ++k) cur[k] = nxt[k];
+        for (uint32_t k = 0; k < H; ++k) {
+            s = s + a[k].x;
+            s = s + a[k].y;
+        }
+        if (blk + 2u < nb) {
+#pragma unroll
+            for (uint32_t k = 0; k < H; ++k) a[k] = __ldg(xb + 2u * H + k);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < H; ++k) {
+            s = s + b[k].x;
+            s = s + b[k].y;
+        }
     }
+    if (blk < nb) {
+#pragma unroll
+        for (uint32_t k = 0; k < H; ++k) {
+            s = s + a[k].x;
+            s = s + a[k].y;
+        }
+        ++blk;
+    }
+    for (uint32_t j = blk * kChainBlock; j < n; ++j) s = s + x[j];
     return s;
 }
 

@@ -7,7 +7,9 @@
   inputs, so no message is needed to agree on it.
 * `gather_rows`: the ranks' result rows (colliding pairs, rays) to every rank
   once per frame, in rank order, with the query indices mapped back to the
-  frame's numbering.
+  frame's numbering: fixed-width rows as bytes through
+  all_gather_into_tensor (the counts first, then the rows padded to the
+  largest count).
 * `max_over_ranks` / `barrier`: the timing rule of the bench (the slowest
   rank's time).
 
@@ -41,19 +43,33 @@ def lpt_partition(costs, world: int) -> list[np.ndarray]:
     return [np.array(sorted(p), np.int64) for p in parts]
 
 
-def gather_rows(rows: np.ndarray, shard: np.ndarray, dist, query_field: str = "query") -> np.ndarray:
-    """All ranks' structured result rows, rank by rank; each rank's
-    `query_field` (an index into its shard) becomes the frame's query
-    index."""
-    rows = rows.copy()
+PAIR_ROW_DTYPE = np.dtype([("query", "<i8"), ("tri_a", "<u4"), ("tri_b", "<u4")])
+
+
+def gather_rows(rows: np.ndarray, shard: np.ndarray, dist, query_field: str = "query", device=None) -> np.ndarray:
+    """All ranks' structured result rows (one fixed dtype), rank by rank; each
+    rank's `query_field` (an index into its shard) becomes the frame's query
+    index. `device`: where the collective's tensors live (the rank's GPU for
+    NCCL, None for gloo)."""
+    import torch
+
+    rows = np.ascontiguousarray(rows).copy()
     if len(rows):
         rows[query_field] = shard[rows[query_field]]
     if dist is None:
         return rows
     world = dist.get_world_size()
-    got = [None] * world
-    dist.all_gather_object(got, rows)
-    return np.concatenate(got) if got else rows
+    width = rows.dtype.itemsize
+    counts = torch.empty(world, dtype=torch.int64, device=device)
+    dist.all_gather_into_tensor(counts, torch.tensor([len(rows)], dtype=torch.int64, device=device))
+    counts = counts.cpu().numpy()
+    cap = max(int(counts.max()), 1)
+    buf = np.zeros(cap * width, np.uint8)
+    buf[:len(rows) * width] = rows.view(np.uint8).reshape(-1)
+    out = torch.empty(world * cap * width, dtype=torch.uint8, device=device)
+    dist.all_gather_into_tensor(out, torch.from_numpy(buf).to(device))
+    out = out.cpu().numpy().reshape(world, cap * width)
+    return np.concatenate([out[r, :int(counts[r]) * width].view(rows.dtype) for r in range(world)])
 
 
 def max_over_ranks(x: float, dist, device=None) -> float:
