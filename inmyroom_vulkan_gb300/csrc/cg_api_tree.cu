@@ -44,10 +44,16 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
         const cg_mesh_view& m = meshes[i];
         if (m.n_triangles && (!m.positions || !m.indices))
             return fail(c, CG_ERR_INVALID_ARGUMENT, "mesh %u has null positions or indices", i);
-        for (uint64_t k = 0; k < 3ull * m.n_triangles; ++k)
-            if (m.indices[k] >= m.n_vertices)
-                return fail(c, CG_ERR_BAD_TREE, "mesh %u index %llu is vertex %u of %u", i, (unsigned long long)k,
-                            m.indices[k], m.n_vertices);
+        // the largest index first (a loop the compiler vectorises), the
+        // offending place only when there is one
+        uint32_t mx = 0;
+        const uint64_t k3 = 3ull * m.n_triangles;
+        for (uint64_t k = 0; k < k3; ++k) mx = std::max(mx, m.indices[k]);
+        if (k3 && mx >= m.n_vertices)
+            for (uint64_t k = 0; k < k3; ++k)
+                if (m.indices[k] >= m.n_vertices)
+                    return fail(c, CG_ERR_BAD_TREE, "mesh %u index %llu is vertex %u of %u", i, (unsigned long long)k,
+                                m.indices[k], m.n_vertices);
         any_normals |= m.normals != nullptr && m.n_triangles;
         base[i + 1] = base[i] + m.n_triangles;
         vbase[i + 1] = vbase[i] + (m.n_triangles ? m.n_vertices : 0u);
@@ -116,16 +122,14 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     // the meshes' buffers, one after another
     std::vector<BuildMesh> mt(n);
     std::vector<BuildNode> roots(n);
-    std::vector<uint32_t> own(T, 0u);
     for (uint32_t i = 0; i < n; ++i) {
         const cg_mesh_view& m = meshes[i];
-        mt[i] = BuildMesh{uint32_t(vbase[i]), (m.normals && m.n_triangles) ? 1u : 0u};
+        mt[i] = BuildMesh{uint32_t(vbase[i]), (m.normals && m.n_triangles) ? 1u : 0u, uint32_t(base[i]), 0u};
         roots[i] = BuildNode{};
         roots[i].begin = uint32_t(base[i]);
         roots[i].count = m.n_triangles;
         roots[i].kid = kNoKid;
         roots[i].tree = i;
-        std::fill(own.begin() + long(base[i]), own.begin() + long(base[i + 1]), i);
         if (!m.n_triangles) continue;
         CG_CUDA(cudaMemcpyAsync(d_V + 3 * vbase[i], m.positions, sizeof(float) * 3 * m.n_vertices,
                                 cudaMemcpyHostToDevice, s),
@@ -140,11 +144,10 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     }
     const uint32_t ctr0[2] = {n, 0u};
     CG_CUDA(cudaMemcpyAsync(d_mesh, mt.data(), sizeof(BuildMesh) * n, cudaMemcpyHostToDevice, s), "upload meshes");
-    CG_CUDA(cudaMemcpyAsync(bp.own, own.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, s), "upload owners");
     CG_CUDA(cudaMemcpyAsync(bp.nodes, roots.data(), sizeof(BuildNode) * n, cudaMemcpyHostToDevice, s), "upload roots");
     CG_CUDA(cudaMemcpyAsync(bp.node_ctr, ctr0, sizeof(ctr0), cudaMemcpyHostToDevice, s), "upload counter");
     const uint32_t sms = uint32_t(c->sm_count);
-    CG_CUDA(launch_build_gather(bp, in, sms, s), "gather kernel");
+    CG_CUDA(launch_build_gather(bp, in, n, sms, s), "gather kernel");
     // one level per round of launches; the splits' children are the next level
     std::vector<std::pair<uint32_t, uint32_t>> levels;
     uint32_t lo = 0, hi = n;
@@ -236,7 +239,6 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     // from here on a failure gives the arena places back
     cudaError_t e = cudaMemcpyAsync(d_emit, em.data(), sizeof(BuildEmit) * n, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = launch_build_emit(bp, in, flat, d_emit, c->recs.ptr, c->tris.ptr, n_nodes, n, sms, s);
-    for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) e = launch_surfaces(c->recs.ptr, em[i].rec_base, em[i].n_recs, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         undo();

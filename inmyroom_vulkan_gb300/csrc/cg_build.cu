@@ -567,6 +567,22 @@ __global__ void __launch_bounds__(128) build_fit_small_kernel(const BuildParams 
 // The meshes' triangles from their vertex and index buffers: a thread per
 // triangle (its mesh is its root node, the owner of every position before
 // the first split).
+// A thread per triangle position: its mesh (the last mesh whose first
+// triangle is at or before it; empty meshes share the next one's start).
+__global__ void build_owner_kernel(const BuildParams B, const BuildInput I, uint32_t n_meshes) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < B.T; t += gridDim.x * blockDim.x) {
+        uint32_t a = 0, b = n_meshes - 1u;
+        while (a < b) {
+            const uint32_t m = (a + b + 1u) >> 1;
+            if (I.meshes[m].tbase <= t)
+                a = m;
+            else
+                b = m - 1u;
+        }
+        B.own[t] = a;
+    }
+}
+
 __global__ void build_gather_kernel(const BuildParams B, const BuildInput I) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < B.T; g += gridDim.x * blockDim.x) {
         const uint32_t m = B.own[g];
@@ -656,7 +672,7 @@ __global__ void build_emit_nodes_kernel(const BuildParams B, const BuildFlat* fl
         r[0] = make_float4(b[0], b[1], b[2], b[3]);
         r[1] = make_float4(b[4], b[5], b[6], b[7]);
         r[2] = make_float4(b[8], b[9], b[10], b[11]);
-        r[3] = make_float4(__uint_as_float(ref), __uint_as_float(meta), 0.f,
+        r[3] = make_float4(__uint_as_float(ref), __uint_as_float(meta), node_surface(N),
                            __uint_as_float(leaf ? 0u : E.tri_base + X.split_off));
         E.ranges[X.rec] = make_uint2(X.tri_off, N.count);
         E.topo[X.rec] = X.prec;
@@ -723,7 +739,9 @@ uint32_t grid_of(uint64_t threads, uint32_t sm_count) {
 }
 }  // namespace
 
-cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint32_t sm_count, cudaStream_t s) {
+cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint32_t n_meshes, uint32_t sm_count,
+                                cudaStream_t s) {
+    if (p.T && n_meshes) build_owner_kernel<<<grid_of(p.T, sm_count), 128, 0, s>>>(p, in, n_meshes);
     if (p.T) build_gather_kernel<<<grid_of(p.T, sm_count), 128, 0, s>>>(p, in);
     return cudaGetLastError();
 }

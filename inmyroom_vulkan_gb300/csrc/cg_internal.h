@@ -462,6 +462,8 @@ cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStre
 struct BuildMesh {
     uint32_t vbase;          // first vertex in BuildInput::vertices / normals
     uint32_t has_normals;
+    uint32_t tbase;          // first triangle position
+    uint32_t pad;
 };
 struct BuildInput {
     const BuildMesh* meshes;
@@ -486,7 +488,8 @@ struct BuildEmit {           // a built tree's arena places
     uint2* ranges;           // [n_recs]
     uint32_t* topo;          // [n_recs] parents, then the leaf records
 };
-cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint32_t sm_count, cudaStream_t s);
+cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint32_t n_meshes, uint32_t sm_count,
+                                cudaStream_t s);
 cudaError_t launch_build_inner(const BuildParams& p, BuildFlat* flat, uint32_t sm_count, cudaStream_t s);
 cudaError_t launch_build_order(const BuildParams& p, BuildFlat* flat, uint32_t n_roots, uint32_t sm_count,
                                cudaStream_t s);
