@@ -705,9 +705,9 @@ __global__ void __launch_bounds__(256, 2) traverse_kernel(const TraverseParams P
     // remaining buffered leaf pairs
     if (nl) flush_leafs(P, lq, loa, lob, lcn, nl, lane);
     if (lane == 0) {
-        atomicAdd(&P.ctr->node_pairs, st_nodes);
-        atomicAdd(&P.ctr->donations, st_don);
-        atomicAdd(&P.ctr->warp_steps, st_steps);
+        if (st_nodes) atomicAdd(&P.ctr->node_pairs, st_nodes);
+        if (st_don) atomicAdd(&P.ctr->donations, st_don);
+        if (st_steps) atomicAdd(&P.ctr->warp_steps, st_steps);
     }
 }
 
@@ -728,20 +728,24 @@ __global__ void __launch_bounds__(256, 3) narrow_kernel(const NarrowParams P) {
     unsigned long long t_base = 0;
     if (P.trace && lane == 0) t_base = trace_base(P.ctr);
 
-    for (;;) {
-        uint32_t first = 0;
-        if (lane == 0) first = atomicAdd(&P.ctr->narrow_lp, 32u);
-        first = __shfl_sync(kFull, first, 0);
-        if (first >= n) break;
+    // Each warp's first 32 leaf pairs are fixed by its index; later ones
+    // come from the shared counter, past all first rounds. A small list
+    // costs no atomic to the warps it does not reach.
+    const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    uint32_t first = 32u * (blockIdx.x * (blockDim.x >> 5) + uint32_t(warp));
+    while (first < n) {
         const uint32_t nl = min(32u, n - first);
         narrow_block<kMode>(P, stage, first, nl, lane, tests, fragile, rechecked, disagree, t_base);
+        uint32_t next = 0;
+        if (lane == 0) next = 32u * n_warps + atomicAdd(&P.ctr->narrow_lp, 32u);
+        first = __shfl_sync(kFull, next, 0);
     }
     if (lane == 0) {
-        atomicAdd(&P.ctr->tri_tests, tests);
-        atomicAdd(&P.ctr->fragile, fragile);
+        if (tests) atomicAdd(&P.ctr->tri_tests, tests);
+        if (fragile) atomicAdd(&P.ctr->fragile, fragile);
         if (kMode != 0) {
-            atomicAdd(&P.ctr->rechecked, rechecked);
-            atomicAdd(&P.ctr->disagreements, disagree);
+            if (rechecked) atomicAdd(&P.ctr->rechecked, rechecked);
+            if (disagree) atomicAdd(&P.ctr->disagreements, disagree);
         }
     }
 }
