@@ -939,12 +939,51 @@ __device__ __forceinline__ void warp_sort128(unsigned long long (&v)[4], uint32_
 }
 
 constexpr uint32_t kFoldStage = 128;  // contributions a fold warp sorts in registers and stages at once
+constexpr uint32_t kFoldSort = kFoldStage * sizeof(FoldItem) / sizeof(unsigned long long);  // ... sorts in its staging buffer
+
+// Ascending sort of a[0..c-1] by one warp (all lanes call it): a bitonic
+// network whose comparators all put the smaller value first (the first step
+// of each merge compares mirrored places), so that the places past c, the
+// network's padding, are +infinity that never moves: a comparison with a
+// place past c is skipped. __syncwarp orders the lanes' accesses between
+// steps (shared or global memory).
+__device__ void warp_sort_any(unsigned long long* a, uint32_t c) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t n2 = 1;
+    while (n2 < c) n2 <<= 1;
+    auto cmpx = [&](uint32_t i, uint32_t l) {
+        if (l < c) {
+            const unsigned long long x = a[i], y = a[l];
+            if (y < x) {
+                a[i] = y;
+                a[l] = x;
+            }
+        }
+    };
+    for (uint32_t k = 2; k <= n2; k <<= 1) {
+        const uint32_t h = k >> 1;
+#pragma unroll 4
+        for (uint32_t t = lane; t < (n2 >> 1); t += 32u) {
+            const uint32_t base = (t / h) * k, off = t % h;
+            cmpx(base + off, base + k - 1u - off);
+        }
+        __syncwarp();
+        for (uint32_t j = k >> 2; j > 0; j >>= 1) {
+#pragma unroll 4
+            for (uint32_t t = lane; t < (n2 >> 1); t += 32u) {
+                const uint32_t i = (t / j) * 2u * j + t % j;
+                cmpx(i, i + j);
+            }
+            __syncwarp();
+        }
+    }
+}
 
 // One slot of more than kFoldThread contributions by the whole warp (all
-// lanes call it): sorted in registers (<= kFoldStage) or, rarely, in place by
-// lane 0; kFoldStage at a time, every lane stages its contributions' pair
-// data in `stage` (all loads in flight together) and lane 0 folds them in
-// order (F is lane 0's).
+// lanes call it): sorted in registers (<= kFoldStage), in the warp's staging
+// buffer (<= kFoldSort) or in place in global memory; kFoldStage at a time,
+// every lane stages its contributions' pair data in `stage` (all loads in
+// flight together) and lane 0 folds them in order (F is lane 0's).
 __device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32_t off, uint32_t c,
                           FoldItem* stage, TriFold& F) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -960,16 +999,15 @@ __device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32
         warp_sort128(v, c <= 32u ? 32u : (c <= 64u ? 64u : 128u));
     } else {
         unsigned long long* G = P.contrib + off;
-        if (lane == 0)
-            for (uint32_t a = 1; a < c; ++a) {
-                const unsigned long long x = G[a];
-                uint32_t b = a;
-                while (b > 0u && G[b - 1u] > x) {
-                    G[b] = G[b - 1u];
-                    --b;
-                }
-                G[b] = x;
-            }
+        if (c <= kFoldSort) {
+            unsigned long long* sh = reinterpret_cast<unsigned long long*>(stage);
+            for (uint32_t i = lane; i < c; i += 32u) sh[i] = G[i];
+            __syncwarp();
+            warp_sort_any(sh, c);
+            for (uint32_t i = lane; i < c; i += 32u) G[i] = sh[i];
+        } else {
+            warp_sort_any(G, c);
+        }
         __syncwarp();
         S = G;
     }

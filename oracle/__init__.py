@@ -174,8 +174,12 @@ class Tree:
 
 
 class Mid:
-    def __init__(self, impl: "Impl", handle: int):
+    """A mid + narrow phase result. It reads its trees when asked for
+    contacts and rays, so it keeps them alive."""
+
+    def __init__(self, impl: "Impl", handle: int, trees=()):
         self.impl, self.h = impl, handle
+        self._trees = tuple(trees)
 
     def __del__(self):
         try:
@@ -272,7 +276,7 @@ class Impl:
         return out
 
     def mid_phase(self, ta: Tree, tb: Tree, ma, mb) -> Mid:
-        return Mid(self, self.fn("mid_phase")(ta.h, tb.h, _f32(ma, 16), _f32(mb, 16)))
+        return Mid(self, self.fn("mid_phase")(ta.h, tb.h, _f32(ma, 16), _f32(mb, 16)), (ta, tb))
 
     # --- primitives
     def tri_tri(self, a, b):
