@@ -36,22 +36,28 @@
 //                     weight, weighted midpoint, vertex bits; the two
 //                     triangles' slots in the contact table, a place in each
 //                     slot's list; its leaf pair listed once; empties the
-//                     previous launch's vertex set
+//                     previous launch's global vertex set
 //   contacts_alloc    each slot's place in the contribution list (one atomic
-//                     per 32 slots); the first block: the maps' offsets
+//                     per 32 slots), the slots of more than kFoldThread
+//                     contributions listed; the first block: the maps'
+//                     offsets
 //   contacts_scatter  thread per pair: both contributions into their lists
-//   contacts_paths    thread per listed leaf pair: its descent path
-//   contacts_fold     warp per slot: the list sorted by the other triangle,
-//                     the reference's two folds, the path of the first leaf
-//                     pair of non-zero weight; the triangle into its map
+//   contacts_paths    lane pair per listed leaf pair: the two trees' ways
+//                     down walked side by side, merged into its descent path
+//   contacts_fold     thread per slot (a warp per listed large slot): the
+//                     list sorted by the other triangle, the reference's two
+//                     folds, the path of the first leaf pair of non-zero
+//                     weight; the triangle into its map
 //   contacts_rank     one block: the maps largest first
 //   contacts_order    persistent, a block per map in that order: the
-//                     insertion order (sort by path, triangle), the iteration
-//                     order (counting passes per growth), the rays
-//                     (find_rays_lambda, CreateUncollideRays.cpp:131-178: one
-//                     per vertex index, at its first corner in iteration
-//                     order, else from the weighted average), the mean origin
-//                     in ray order
+//                     insertion order (sort by path, triangle, in registers
+//                     on the narrowest exact key), the iteration order (the
+//                     growth steps: by one warp up to 32 keys, else counting
+//                     passes), the rays (find_rays_lambda,
+//                     CreateUncollideRays.cpp:131-178: one per vertex index,
+//                     at its first corner in iteration order, else from the
+//                     weighted average; the vertex set in shared memory when
+//                     it fits), the mean origin in ray order
 //   contacts_offsets  one block: each map's first record and ray
 //   contacts_emit     block per map: records and rays to their places;
 //                     empties the table slots, leaf-pair marks and map
