@@ -496,7 +496,8 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
             cp.sched_start[k] = c->sched_start[k];
             cp.sched_buckets[k] = c->sched_buckets[k];
         }
-        CG_CUDA(launch_contacts(cp, c->contact_blocks, c->fold_blocks, c->order_blocks, s), "contact kernels");
+        CG_CUDA(launch_contacts(cp, c->contact_blocks, c->fold_blocks, c->order_blocks, s, c->branch,
+                                c->ev_branch, c->ev_branched), "contact kernels");
     }
     if (pairs_copy) CG_CUDA(cudaStreamWaitEvent(s, c->ev_joined, 0), "join");
     return CG_OK;
@@ -698,6 +699,9 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_joined, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->branch, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_branch, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_branched, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&c->d_trace, sizeof(unsigned int) * 4 * kTraceBuckets) != cudaSuccess) {
         delete c;
         return CG_ERR_CUDA;
@@ -748,6 +752,9 @@ int cg_destroy(cg_ctx* c) {
     cudaEventDestroy(c->ev_fork);
     cudaEventDestroy(c->ev_joined);
     cudaStreamDestroy(c->side);
+    cudaEventDestroy(c->ev_branch);
+    cudaEventDestroy(c->ev_branched);
+    cudaStreamDestroy(c->branch);
     cudaStreamDestroy(c->stream);
     delete c;
     return CG_OK;

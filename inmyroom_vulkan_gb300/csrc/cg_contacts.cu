@@ -42,13 +42,14 @@
 //                     contributions listed; the first block: the maps'
 //                     offsets
 //   contacts_scatter  thread per pair: both contributions into their lists
-//   contacts_paths    lane pair per listed leaf pair: the two trees' ways
-//                     down walked side by side, merged into its descent path
+//   contacts_paths    (on a branch beside alloc and scatter) lane pair per
+//                     listed leaf pair: the two trees' ways down walked side
+//                     by side, merged into its descent path
 //   contacts_fold     thread per slot (a warp per listed large slot): the
 //                     list sorted by the other triangle, the reference's two
 //                     folds, the path of the first leaf pair of non-zero
-//                     weight; the triangle into its map
-//   contacts_rank     one block: the maps largest first
+//                     weight; the triangle into its map. Its last block
+//                     ranks the maps, largest first
 //   contacts_order    persistent, a block per map in that order: the
 //                     insertion order (sort by path, triangle, in registers
 //                     on the narrowest exact key), the iteration order (the
@@ -57,8 +58,8 @@
 //                     CreateUncollideRays.cpp:131-178: one per vertex index,
 //                     at its first corner in iteration order, else from the
 //                     weighted average; the vertex set in shared memory when
-//                     it fits), the mean origin in ray order
-//   contacts_offsets  one block: each map's first record and ray
+//                     it fits), the mean origin in ray order. Its last block
+//                     places each map's first record and ray
 //   contacts_emit     block per map: records and rays to their places;
 //                     empties the table slots, leaf-pair marks and map
 //                     counters it used
@@ -1041,6 +1042,60 @@ __device__ void fold_warp(const ContactParams& P, unsigned long long key, uint32
     if (lane == 0) F.finish();
 }
 
+// The maps, largest first (by size class: the bit length of the triangle
+// count), for the order kernel's blocks to take in that order; by one block.
+__device__ void rank_maps(const ContactParams& P) {
+    __shared__ uint32_t count[33], start[33];
+    const uint32_t m = 2u * P.n_queries;
+    if (threadIdx.x < 33u) count[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const uint32_t n = P.map_fill[i];
+        atomicAdd(count + (n ? 32u - __clz(n) : 0u), 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t off = 0;
+        for (int c = 32; c >= 0; --c) {
+            start[c] = off;
+            off += count[c];
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const uint32_t n = P.map_fill[i];
+        P.map_order[atomicAdd(start + (n ? 32u - __clz(n) : 0u), 1u)] = i;
+    }
+}
+
+// Each map's first record and ray in the outputs, the counts; by one block.
+__device__ void place_maps(const ContactParams& P, uint32_t* part) {
+    const uint32_t m = 2u * P.n_queries;
+    const uint32_t nc = block_scan(
+        m, part, [&](uint32_t i) { return P.map_fill[i]; }, [&](uint32_t i, uint32_t v) { P.map_coff[i] = v; });
+    const uint32_t nr = block_scan(
+        m, part, [&](uint32_t i) { return P.map_nr[i]; }, [&](uint32_t i, uint32_t v) { P.map_roff[i] = v; });
+    if (threadIdx.x == 0) {
+        P.ctr->n_elems = nc;
+        P.ctr->n_rays = nr;
+        P.ctr->prev_vertices = 0u;  // the pairs kernel emptied them
+    }
+}
+
+// True in the block that finishes last of the grid (counted on `done`); its
+// threads then see every other block's writes.
+__device__ bool last_block(unsigned* done) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1u;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
 // A thread per slot: the triangle's contributions sorted by the other
 // triangle (a triangle's pairs within a leaf pair come in the other
 // triangle's order, and its leaf pairs in the order of the other leaf's first
@@ -1076,6 +1131,7 @@ __global__ void __launch_bounds__(256, 3) contacts_fold_kernel(const ContactPara
         fold_warp(P, key, si.z, si.w, stage[wib], F);
         if (lane == 0) put_elem(P, key, F);
     }
+    if (last_block(&P.ctr->fold_done)) rank_maps(P);
 }
 
 // A ray of find_rays_lambda (CreateUncollideRays.cpp:140-173) for contact
@@ -1536,32 +1592,6 @@ __device__ void order_map(const ContactParams& P, uint32_t map, uint32_t* smem, 
     }
 }
 
-// The maps, largest first (by size class: the bit length of the triangle
-// count), for the order kernel's blocks to take in that order.
-__global__ void __launch_bounds__(1024) contacts_rank_kernel(const ContactParams P) {
-    __shared__ uint32_t count[33], start[33];
-    const uint32_t m = 2u * P.n_queries;
-    if (threadIdx.x < 33u) count[threadIdx.x] = 0u;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-        const uint32_t n = P.map_fill[i];
-        atomicAdd(count + (n ? 32u - __clz(n) : 0u), 1u);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t off = 0;
-        for (int c = 32; c >= 0; --c) {
-            start[c] = off;
-            off += count[c];
-        }
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-        const uint32_t n = P.map_fill[i];
-        P.map_order[atomicAdd(start + (n ? 32u - __clz(n) : 0u), 1u)] = i;
-    }
-}
-
 // Persistent: each block takes the next map of the largest-first list.
 __global__ void __launch_bounds__(256, 2) contacts_order_kernel(const ContactParams P) {
     extern __shared__ __align__(16) uint32_t smem_order[];
@@ -1580,20 +1610,7 @@ __global__ void __launch_bounds__(256, 2) contacts_order_kernel(const ContactPar
         order_map(P, map, smem_order, part, fold);
         __syncthreads();
     }
-}
-
-__global__ void __launch_bounds__(1024) contacts_offsets_kernel(const ContactParams P) {
-    __shared__ uint32_t part[64];
-    const uint32_t m = 2u * P.n_queries;
-    const uint32_t nc = block_scan(
-        m, part, [&](uint32_t i) { return P.map_fill[i]; }, [&](uint32_t i, uint32_t v) { P.map_coff[i] = v; });
-    const uint32_t nr = block_scan(
-        m, part, [&](uint32_t i) { return P.map_nr[i]; }, [&](uint32_t i, uint32_t v) { P.map_roff[i] = v; });
-    if (threadIdx.x == 0) {
-        P.ctr->n_elems = nc;
-        P.ctr->n_rays = nr;
-        P.ctr->prev_vertices = 0u;  // the pairs kernel emptied them
-    }
+    if (last_block(&P.ctr->order_done)) place_maps(P, part);
 }
 
 __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams P) {
@@ -1728,17 +1745,24 @@ cudaError_t contacts_fold_occupancy(int* blocks_per_sm) {
 }
 
 cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t fold_grid, uint32_t order_grid,
-                            cudaStream_t s) {
+                            cudaStream_t s, cudaStream_t branch, cudaEvent_t ev_fork, cudaEvent_t ev_join) {
     if (!p.n_queries) return cudaSuccess;
     const uint32_t maps = 2u * p.n_queries;
     contacts_pairs_kernel<<<grid, 256, 0, s>>>(p);
+    // the descent paths need only the listed leaf pairs: a branch beside the
+    // contribution lists, joined before the fold
+    cudaError_t e = cudaEventRecord(ev_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(branch, ev_fork, 0);
+    if (e != cudaSuccess) return e;
+    contacts_paths_kernel<<<2u * grid, kPathWarps * 32, 0, branch>>>(p);
+    e = cudaEventRecord(ev_join, branch);
+    if (e != cudaSuccess) return e;
     contacts_alloc_kernel<<<grid, 256, 0, s>>>(p);
     contacts_scatter_kernel<<<grid, 256, 0, s>>>(p);
-    contacts_paths_kernel<<<2u * grid, kPathWarps * 32, 0, s>>>(p);
+    e = cudaStreamWaitEvent(s, ev_join, 0);
+    if (e != cudaSuccess) return e;
     contacts_fold_kernel<<<fold_grid, 256, 0, s>>>(p);
-    contacts_rank_kernel<<<1, 1024, 0, s>>>(p);
     contacts_order_kernel<<<maps < order_grid ? maps : order_grid, 256, kOrderSmemWords * sizeof(uint32_t), s>>>(p);
-    contacts_offsets_kernel<<<1, 1024, 0, s>>>(p);
     contacts_emit_kernel<<<maps < grid ? maps : grid, 256, 0, s>>>(p);
     return cudaGetLastError();
 }

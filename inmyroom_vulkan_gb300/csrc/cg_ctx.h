@@ -211,6 +211,8 @@ struct cg_ctx {
     cudaEvent_t ev_join = nullptr;  // joins an external launch stream to the context stream
     cudaStream_t side = nullptr;    // a branch of cg_collide's step graph (host copy of the pairs)
     cudaEvent_t ev_fork = nullptr, ev_joined = nullptr;
+    cudaStream_t branch = nullptr;  // a branch of the contact kernels (the descent paths)
+    cudaEvent_t ev_branch = nullptr, ev_branched = nullptr;
 
     // batch tables of cg_deform_batch / cg_tree_refit_batch in device memory,
     // uploaded when their contents change

@@ -97,6 +97,8 @@ struct Counters {
     unsigned int contrib_used;   // contribution-list entries given to slots
     unsigned int order_ticket;   // maps taken by the order kernel's blocks
     unsigned int n_big;          // contact slots of more than kFoldThread contributions (listed for the fold)
+    unsigned int fold_done;      // fold blocks finished (the last one ranks the maps)
+    unsigned int order_done;     // order blocks finished (the last one places the maps' records and rays)
 };
 
 enum : unsigned int { CONTACT_TABLE = 1u, CONTACT_VERTICES = 2u, CONTACT_RAYS = 4u, CONTACT_ORDER = 8u };
@@ -188,7 +190,7 @@ struct ContactParams {
 };
 
 cudaError_t launch_contacts(const ContactParams& p, uint32_t grid, uint32_t fold_grid, uint32_t order_grid,
-                            cudaStream_t s);
+                            cudaStream_t s, cudaStream_t branch, cudaEvent_t ev_fork, cudaEvent_t ev_join);
 cudaError_t contacts_order_occupancy(int* blocks_per_sm);
 cudaError_t contacts_fold_occupancy(int* blocks_per_sm);
 
