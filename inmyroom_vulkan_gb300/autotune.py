@@ -40,7 +40,7 @@ import numpy as np
 
 SPACE: dict[str, tuple] = {
     "warps_per_block": (2, 4, 8),
-    "blocks_per_sm": (1, 2),
+    "blocks_per_sm": (1, 2, 3),
     "stack_entries": (256, 512, 1024),
     "donate_min": (8, 16, 32, 64),
     "leaf_flush": (8, 16, 32),
