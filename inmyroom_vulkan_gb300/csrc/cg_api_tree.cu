@@ -76,7 +76,11 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     const size_t oPerm = take(4 * T), oScr = take(4 * T), oOwn = take(4 * T);
     const size_t oD = take(sizeof(double) * 9 * T), oTm = take(sizeof(double) * 18 * T);
     const size_t oMom = take(sizeof(double) * 9 * std::max<uint64_t>(T, n));  // a level: one node per triangle, or the roots
-    const size_t oNodes = take(sizeof(BuildNode) * cap), oFlat = take(sizeof(BuildFlat) * cap), oCtr = take(8);
+    const size_t oNodes = take(sizeof(BuildNode) * cap), oFlat = take(sizeof(BuildFlat) * cap), oCtr = take(16);
+    // a level's nodes of more than kBuildBig triangles: the roots, or disjoint
+    // ranges of more than kBuildBig triangles each
+    const uint64_t big_cap = n + T / (kBuildBig + 1) + 1;
+    const size_t oBig = take(sizeof(uint32_t) * 2 * big_cap);
     const size_t oV = take(sizeof(float) * 3 * std::max<uint64_t>(nv, 1));
     const size_t oNV = take(any_normals ? sizeof(float) * 3 * std::max<uint64_t>(nv, 1) : 0);
     const size_t oIdx = take(sizeof(uint32_t) * 3 * T), oMesh = take(sizeof(BuildMesh) * n);
@@ -110,6 +114,7 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     bp.error = bp.node_ctr + 1;
     bp.node_cap = cap;
     bp.T = uint32_t(total);
+    uint32_t* big_list[2] = {reinterpret_cast<uint32_t*>(mem + oBig), reinterpret_cast<uint32_t*>(mem + oBig) + big_cap};
     float* d_V = reinterpret_cast<float*>(mem + oV);
     float* d_NV = any_normals ? reinterpret_cast<float*>(mem + oNV) : nullptr;
     uint32_t* d_idx = reinterpret_cast<uint32_t*>(mem + oIdx);
@@ -142,26 +147,40 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
                                 cudaMemcpyHostToDevice, s),
                 "upload indices");
     }
-    const uint32_t ctr0[2] = {n, 0u};
+    const uint32_t ctr0[4] = {n, 0u, 0u, 0u};
+    std::vector<uint32_t> big_roots;
+    for (uint32_t i = 0; i < n; ++i)
+        if (roots[i].count > kBuildBig) big_roots.push_back(i);
     CG_CUDA(cudaMemcpyAsync(d_mesh, mt.data(), sizeof(BuildMesh) * n, cudaMemcpyHostToDevice, s), "upload meshes");
     CG_CUDA(cudaMemcpyAsync(bp.nodes, roots.data(), sizeof(BuildNode) * n, cudaMemcpyHostToDevice, s), "upload roots");
     CG_CUDA(cudaMemcpyAsync(bp.node_ctr, ctr0, sizeof(ctr0), cudaMemcpyHostToDevice, s), "upload counter");
+    if (!big_roots.empty())
+        CG_CUDA(cudaMemcpyAsync(big_list[0], big_roots.data(), sizeof(uint32_t) * big_roots.size(),
+                                cudaMemcpyHostToDevice, s),
+                "upload large roots");
     const uint32_t sms = uint32_t(c->sm_count);
     CG_CUDA(launch_build_gather(bp, in, n, sms, s), "gather kernel");
     // one level per round of launches; the splits' children are the next level
     std::vector<std::pair<uint32_t, uint32_t>> levels;
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
+    uint32_t lo = 0, hi = n, n_big = uint32_t(big_roots.size());
+    for (uint32_t level = 0; lo < hi; ++level) {
+        const uint32_t in = level & 1u, out = in ^ 1u;
         bp.lo = lo;
         bp.hi = hi;
+        bp.big = big_list[in];
+        bp.n_big = n_big;
+        bp.big_out = big_list[out];
+        bp.n_big_out = bp.node_ctr + 2 + out;
         levels.emplace_back(lo, hi);
+        CG_CUDA(cudaMemsetAsync(bp.n_big_out, 0, sizeof(uint32_t), s), "clear large node count");
         CG_CUDA(launch_build_level(bp, sms, s), "build level kernels");
-        uint32_t ctr[2];
+        uint32_t ctr[4];
         CG_CUDA(cudaMemcpyAsync(ctr, bp.node_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read node count");
         CG_CUDA(cudaStreamSynchronize(s), "build level");
         if (ctr[1]) return fail(c, CG_ERR_OUT_OF_MEMORY, "tree build ran out of node slots");
         lo = hi;
         hi = std::min(ctr[0], cap);
+        n_big = ctr[2 + out];
     }
     const uint32_t n_nodes = hi;
     // the pre-order layout: subtree sizes bottom-up, places top-down

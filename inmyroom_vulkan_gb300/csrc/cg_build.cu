@@ -23,7 +23,8 @@
 //   build_proj    a thread per triangle position: its corners' FP64
 //                 projections on its node's axes
 //   build_fit     a warp per node of more than 16 triangles (build_fit_small:
-//                 a thread per smaller node): fewer than two distinct corners
+//                 a thread per smaller node; build_fit_big: a block per node
+//                 of more than kBuildBig): fewer than two distinct corners
 //                 give the empty or point box; else the min/max projections
 //                 (integer keys of the doubles; equal values: the later
 //                 corner, as the sequential std::min / std::max keep) and the
@@ -50,6 +51,7 @@
 #include <cuda_runtime.h>
 
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -63,6 +65,7 @@ namespace {
 
 constexpr unsigned kAll = 0xffffffffu;
 constexpr uint32_t kLeafMax = 4;  // OBBtree.h:49 maxNumberOfTriangles
+constexpr uint32_t kBigWarps = 16;  // warps of the block that handles one node of more than kBuildBig triangles
 
 __device__ __forceinline__ float3 corner(const float* P, uint32_t t, uint32_t k) {
     const float* q = P + 9ull * t + 3u * k;
@@ -196,9 +199,172 @@ __global__ void build_sums_kernel(const BuildParams B) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         const uint32_t node = B.lo + g / 3u, c = g % 3u;
         const BuildNode& N = B.nodes[node];
+        if (N.count > kBuildBig) continue;  // build_sums_big
         const uint32_t np = 3u * N.count;
         const double s = chain_sum(B.D + c * n3 + 3ull * N.begin, np);
         B.mom[9ull * (node - B.lo) + c] = np ? s / double(np) : 0.0;
+    }
+}
+
+// The corner's coordinate (a float as a double, finite) as an integer count of
+// 2^q, q at most its float ulp's exponent: exact (the shifted-out bits are
+// zero) while the count fits 64 bits.
+__device__ __forceinline__ long long units_of(double x, int q) {
+    const long long b = __double_as_longlong(x);
+    if ((b & 0x7fffffffffffffffll) == 0) return 0;
+    const int sh = int((b >> 52) & 0x7ff) - 1023 - 52 - q;
+    const long long m = (b & 0xfffffffffffffll) | (1ll << 52);
+    const long long v = sh >= 0 ? (m << sh) : (m >> -sh);
+    return b < 0 ? -v : v;
+}
+
+// Block-wide sum of a 64-bit value per thread; every thread gets the total,
+// and `before` the sum over the threads before it.
+template <uint32_t kWarps>
+__device__ __forceinline__ long long block_scan_ll(long long v, long long* sh, long long& before) {
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(kAll, inc, o);
+        if (lane >= uint32_t(o)) inc += t;
+    }
+    if (lane == 31u) sh[w] = inc;
+    __syncthreads();
+    long long wb = 0, total = 0;
+    for (uint32_t k = 0; k < kWarps; ++k) {
+        const long long t = sh[k];
+        if (k < w) wb += t;
+        total += t;
+    }
+    __syncthreads();
+    before = wb + inc - v;
+    return total;
+}
+
+// A NaN payload that no sum produces: the mean is left to a chain.
+constexpr long long kChainDue = 0x7ff4c4a1d0e00000ll;
+
+// A block per node of the level's list of nodes of more than kBuildBig
+// triangles: the coordinate sums of build_sums_kernel without the chain where
+// the chain makes no rounding. Its terms are floats, integer multiples of
+// 2^q (q the smallest exponent of their ulps); when the exact running sums,
+// counted in units of 2^q, all stay below 2^53 (checked with an exact 64-bit
+// prefix sum, whose terms are bounded so that it cannot overflow), every add
+// of the sequential sum is exact, and the sum is the exact total, whatever the
+// order of its adds. A coordinate that fails the check (or holds a non-finite
+// value) is marked due (kChainDue) and summed by build_sums_due's chain.
+__global__ void __launch_bounds__(kBigWarps * 32) build_sums_big_kernel(const BuildParams B) {
+    constexpr uint32_t NT = kBigWarps * 32u;
+    __shared__ int s_q[kBigWarps][3], s_e[kBigWarps][3];
+    __shared__ long long s_sc[kBigWarps];
+    __shared__ unsigned long long s_mx[kBigWarps][3];
+    __shared__ long long s_tot[3];
+    __shared__ int s_ok[3];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
+    const uint64_t n3 = 3ull * B.T;
+    for (uint32_t i = blockIdx.x; i < B.n_big; i += gridDim.x) {
+        const uint32_t id = B.big[i];
+        const BuildNode& N = B.nodes[id];
+        const uint32_t np = 3u * N.count;
+        const double* x0 = B.D + 3ull * N.begin;
+        // this thread's consecutive corners [j0, j1)
+        const uint32_t L = (np + NT - 1u) / NT;
+        const uint32_t j0 = min(np, tid * L), j1 = min(np, j0 + L);
+        // the smallest ulp exponent and the largest exponent of the non-zero terms
+        int q[3], e[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) q[c] = INT_MAX, e[c] = INT_MIN;
+        for (uint32_t j = j0; j < j1; ++j)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long b = __double_as_longlong(x0[c * n3 + j]);
+                if ((b & 0x7fffffffffffffffll) == 0) continue;
+                const int E = int((b >> 52) & 0x7ff) - 1023;
+                q[c] = min(q[c], max(E, -126) - 23);
+                e[c] = max(e[c], E);
+            }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                q[c] = min(q[c], __shfl_xor_sync(kAll, q[c], o));
+                e[c] = max(e[c], __shfl_xor_sync(kAll, e[c], o));
+            }
+        if (lane == 0u)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) s_q[w][c] = q[c], s_e[w][c] = e[c];
+        __syncthreads();
+        bool use[3];  // the terms' counts cannot overflow 64 bits in any running sum
+        const int lg = 32 - __clz(np - 1u);  // ceil(log2(np)), np > 1
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            for (uint32_t k = 0; k < kBigWarps; ++k) q[c] = min(q[c], s_q[k][c]), e[c] = max(e[c], s_e[k][c]);
+            // |term| < 2^(e + 1), so |count| < 2^(e + 1 - q); np of them < 2^63
+            use[c] = e[c] == INT_MIN || (e[c] < 1024 && lg + e[c] + 1 - q[c] <= 63);
+        }
+        // the counts' sums: the thread's, then the running sums from the
+        // threads before it, and their largest magnitude
+        long long loc[3] = {0, 0, 0};
+        for (uint32_t j = j0; j < j1; ++j)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (use[c] && e[c] != INT_MIN) loc[c] += units_of(x0[c * n3 + j], q[c]);
+        long long run[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const long long tot = block_scan_ll<kBigWarps>(loc[c], s_sc, run[c]);
+            if (tid == 0u) s_tot[c] = tot;
+        }
+        unsigned long long mx[3] = {0, 0, 0};
+        for (uint32_t j = j0; j < j1; ++j)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (use[c] && e[c] != INT_MIN) {
+                    run[c] += units_of(x0[c * n3 + j], q[c]);
+                    mx[c] = max(mx[c], (unsigned long long)(run[c] < 0 ? -run[c] : run[c]));
+                }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int o = 16; o; o >>= 1) mx[c] = max(mx[c], __shfl_xor_sync(kAll, mx[c], o));
+        if (lane == 0u)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) s_mx[w][c] = mx[c];
+        __syncthreads();
+        if (tid < 3u) {
+            const int c = int(tid);
+            unsigned long long m = 0;
+            for (uint32_t k = 0; k < kBigWarps; ++k) m = max(m, s_mx[k][c]);
+            s_ok[c] = use[c] && m < (1ull << 53);
+        }
+        __syncthreads();
+        if (tid < 3u) {
+            const int c = int(tid);
+            double m = __longlong_as_double(kChainDue);
+            if (s_ok[c]) {
+                double s = 0.0;  // every term a zero: +0, as the chain from +0 gives
+                if (e[c] != INT_MIN)  // |total| < 2^53 counts of 2^q, q >= -149: exact
+                    s = __ll2double_rn(s_tot[c]) * __longlong_as_double((long long)(q[c] + 1023) << 52);
+                m = s / double(np);
+            }
+            B.mom[9ull * (id - B.lo) + c] = m;
+        }
+        __syncthreads();  // shared memory is reused by the next node
+    }
+}
+
+// A thread per coordinate of the list's nodes: the chain of each sum that
+// build_sums_big left due.
+__global__ void build_sums_due_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < 3u * B.n_big; g += gridDim.x * blockDim.x) {
+        const uint32_t id = B.big[g / 3u], c = g % 3u;
+        double* m = B.mom + 9ull * (id - B.lo) + c;
+        if (__double_as_longlong(*m) != kChainDue) continue;
+        const BuildNode& N = B.nodes[id];
+        const uint32_t np = 3u * N.count;
+        *m = chain_sum(B.D + c * n3 + 3ull * N.begin, np) / double(np);
     }
 }
 
@@ -524,15 +690,15 @@ __device__ __forceinline__ uint32_t add_children(const BuildParams& B, BuildNode
 
 constexpr uint32_t kSmall = 16;  // nodes of at most this many triangles: a thread each
 
-// A warp per node of the level with more than kSmall triangles: the box, the
-// split, the children's positions.
+// A warp per node of the level with more than kSmall and at most kBuildBig
+// triangles: the box, the split, the children's positions.
 __global__ void __launch_bounds__(128) build_fit_kernel(const BuildParams B) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t id = B.lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); id < B.hi; id += warps) {
         BuildNode& N = B.nodes[id];
         const uint32_t begin = N.begin, n = N.count;
-        if (n <= kSmall) continue;
+        if (n <= kSmall || n > kBuildBig) continue;
         const Box box = fit_warp(B, begin, n, B.mom + 9ull * (id - B.lo), lane);
         const uint32_t nl = split_node(B.Pp + 9ull * begin, B.perm + begin, B.scratch + begin, n, box, lane);
         uint32_t k = 0;
@@ -544,6 +710,158 @@ __global__ void __launch_bounds__(128) build_fit_kernel(const BuildParams B) {
         k = __shfl_sync(kAll, k, 0);
         if (k == kNoKid) continue;
         for (uint32_t t = lane; t < n; t += 32u) B.own[begin + t] = t < nl ? k : k + 1u;
+    }
+}
+
+// Of two extremes with keys k (smaller wins for lo, larger for hi), the one
+// the sequential scan keeps: on equal keys the later corner.
+__device__ __forceinline__ void merge_ext(Ext& e, const Ext& o, bool lo) {
+    if ((lo ? o.k < e.k : o.k > e.k) || (o.k == e.k && o.j > e.j)) e = o;
+}
+
+// A block per node of the level's list of nodes of more than kBuildBig
+// triangles (the top levels of the large meshes, where one warp's walk of the
+// range set the level's time): the box and split of build_fit_kernel, the
+// corners shared out by thread, the split's counts and partition by warp over
+// consecutive segments of the range (each warp's lefts and rights go after
+// those of the segments before it, so the partition stays stable). Children
+// of more than kBuildBig triangles go to the next level's list.
+__global__ void __launch_bounds__(kBigWarps * 32) build_fit_big_kernel(const BuildParams B) {
+    constexpr uint32_t NT = kBigWarps * 32u;
+    __shared__ Ext s_lo[kBigWarps][3], s_hi[kBigWarps][3];
+    __shared__ uint32_t s_cnt[kBigWarps], s_sel[kBigWarps];
+    __shared__ Box s_box;
+    __shared__ uint32_t s_kid;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t i = blockIdx.x; i < B.n_big; i += gridDim.x) {
+        const uint32_t id = B.big[i];
+        BuildNode& N = B.nodes[id];
+        const uint32_t begin = N.begin, n = N.count;
+        const float* pn = B.Pp + 9ull * begin;
+        const uint32_t np = 3u * n;
+        const float3 p0 = corner(pn, 0, 0);
+        bool differ = false;
+        for (uint32_t j = tid; j < np; j += NT) differ |= !same_point(corner(pn, j / 3u, j % 3u), p0);
+        const bool distinct = __syncthreads_or(differ) != 0;
+        if (distinct) {
+            Ext lo[3], hi[3];
+            init_ext(lo, hi);
+            const uint64_t n3 = 3ull * B.T;
+            const double* pr = B.Tm + 3ull * begin;
+            for (uint32_t j = tid; j < np; j += NT) extend3(pr, n3, j, lo, hi);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                warp_extreme(lo[k], true);
+                warp_extreme(hi[k], false);
+            }
+            if (lane == 0u)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    s_lo[w][k] = lo[k];
+                    s_hi[w][k] = hi[k];
+                }
+        }
+        __syncthreads();
+        if (tid == 0u) {
+            Box box;
+            if (distinct) {
+                Ext lo[3], hi[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = s_lo[0][k];
+                    hi[k] = s_hi[0][k];
+                }
+                for (uint32_t v = 1; v < kBigWarps; ++v)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        merge_ext(lo[k], s_lo[v][k], true);
+                        merge_ext(hi[k], s_hi[v][k], false);
+                    }
+                double a[9];
+                const double* ax = B.mom + 9ull * (id - B.lo);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) a[k] = ax[k];
+                box = box_from(a, lo, hi);
+            } else {  // one distinct point
+                box = empty_box();
+                box.c = p0;
+            }
+            s_box = box;
+        }
+        __syncthreads();
+        const Box box = s_box;
+
+        // the split (split_node's rule), this warp over positions [sb, se)
+        float3 dir[3];
+        int ord[3];
+        split_axes(box, dir, ord);
+        const uint32_t seg = (n + kBigWarps - 1u) / kBigWarps;
+        const uint32_t sb = min(n, w * seg), se = min(n, sb + seg);
+        bool chosen = false;
+        uint32_t nl = n / 2u;
+        float3 axis = dir[ord[0]];
+        float cp = 0.f;
+        for (int k = 0; k < 3 && !chosen; ++k) {
+            const float3 a = dir[ord[k]];
+            const float c = dot3(box.c, a);
+            uint32_t cnt = 0;
+            for (uint32_t base = sb; base < se; base += 32u) {
+                const uint32_t t = base + lane;
+                cnt += __popc(__ballot_sync(kAll, t < se && goes_left(pn, t, a, c)));
+            }
+            if (lane == 0u) s_cnt[w] = cnt;
+            __syncthreads();
+            uint32_t total = 0;
+            for (uint32_t v = 0; v < kBigWarps; ++v) total += s_cnt[v];
+            if (total > 0u && total < n) {
+                chosen = true;
+                nl = total;
+                axis = a;
+                cp = c;
+                if (tid < kBigWarps) s_sel[tid] = s_cnt[tid];
+            }
+            __syncthreads();
+        }
+        uint32_t lb = 0;  // left positions before this warp's segment
+        if (chosen)
+            for (uint32_t v = 0; v < w; ++v) lb += s_sel[v];
+        else
+            lb = min(sb, nl);
+        uint32_t rb = sb - lb;
+        uint32_t* perm = B.perm + begin;
+        uint32_t* scr = B.scratch + begin;
+        for (uint32_t base = sb; base < se; base += 32u) {
+            const uint32_t t = base + lane;
+            const bool valid = t < se;
+            uint32_t tri = 0;
+            bool left = false;
+            if (valid) {
+                tri = perm[t];
+                left = chosen ? goes_left(pn, t, axis, cp) : (t < nl);
+            }
+            const unsigned ml = __ballot_sync(kAll, left), mv = __ballot_sync(kAll, valid);
+            if (valid) scr[left ? lb + __popc(ml & lt) : nl + rb + __popc(mv & ~ml & lt)] = tri;
+            lb += __popc(ml);
+            rb += __popc(mv & ~ml);
+        }
+        __syncthreads();
+        for (uint32_t t = tid; t < n; t += NT) perm[t] = scr[t];
+        if (tid == 0u) {
+            store_box(N, box);
+            N.kid = kNoKid;
+            const uint32_t k = add_children(B, N, nl);
+            if (k != kNoKid) {
+                if (nl > kBuildBig) B.big_out[atomicAdd(B.n_big_out, 1u)] = k;
+                if (n - nl > kBuildBig) B.big_out[atomicAdd(B.n_big_out, 1u)] = k + 1u;
+            }
+            s_kid = k;
+        }
+        __syncthreads();
+        const uint32_t k = s_kid;
+        if (k != kNoKid)
+            for (uint32_t t = tid; t < n; t += NT) B.own[begin + t] = t < nl ? k : k + 1u;
+        __syncthreads();  // shared memory is reused by the next node
     }
 }
 
@@ -722,10 +1040,15 @@ cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStre
     };
     build_points_kernel<<<grid(p.T), 128, 0, s>>>(p);
     build_sums_kernel<<<grid(3ull * width), 128, 0, s>>>(p);
+    if (p.n_big) {
+        build_sums_big_kernel<<<p.n_big < 65535u ? p.n_big : 65535u, kBigWarps * 32u, 0, s>>>(p);
+        build_sums_due_kernel<<<grid(3ull * p.n_big), 128, 0, s>>>(p);
+    }
     build_terms_kernel<<<grid(p.T), 128, 0, s>>>(p);
     build_cov_kernel<<<grid(6ull * width), 128, 0, s>>>(p);
     build_eig_kernel<<<grid(width), 128, 0, s>>>(p);
     build_proj_kernel<<<grid(p.T), 128, 0, s>>>(p);
+    if (p.n_big) build_fit_big_kernel<<<p.n_big < 65535u ? p.n_big : 65535u, kBigWarps * 32u, 0, s>>>(p);
     const uint32_t blocks = (width + 3u) / 4u;
     build_fit_kernel<<<blocks < 65535u ? blocks : 65535u, 128, 0, s>>>(p);
     build_fit_small_kernel<<<grid(width), 128, 0, s>>>(p);

@@ -456,10 +456,15 @@ struct BuildParams {
     BuildNode* nodes;
     uint32_t T;              // triangles
     uint32_t lo, hi;         // this level's nodes
-    uint32_t* node_ctr;      // next free node
+    uint32_t* node_ctr;      // [0] next free node, [1] error, [2 + parity] nodes in big_out
     uint32_t node_cap;
     unsigned* error;
+    const uint32_t* big;     // this level's nodes of more than kBuildBig triangles (a block fits each)
+    uint32_t n_big;
+    uint32_t* big_out;       // the next level's, appended by the splits of this level's
+    uint32_t* n_big_out;
 };
+constexpr uint32_t kBuildBig = 256;  // nodes of more than this many triangles are fitted by a block
 cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStream_t s);
 struct BuildMesh {
     uint32_t vbase;          // first vertex in BuildInput::vertices / normals

@@ -97,6 +97,24 @@ def test_degenerate_meshes(gpu_ctx, port):
     gpu_ctx.free_tree(tid)
 
 
+def test_large_node_sums(gpu_ctx, port):
+    """Nodes of more than 256 triangles take their coordinate sums without the
+    chain when no add of it rounds: meshes whose sums round, one coordinate or
+    all, or hold only zeros, against the oracle's sequential sums."""
+    rng = np.random.default_rng(11)
+    n_pts = 1500
+    base = rng.normal(size=(n_pts, 3)).astype(np.float32)
+    wide = base * (10.0 ** rng.uniform(-30, 3, (n_pts, 1))).astype(np.float32)  # exponents too far apart
+    grow = base.copy()                                                               # x's running sum too long
+    grow[:, 0] = 1.0 + rng.random(n_pts, dtype=np.float32)
+    grow[::97, 0] = 2.0 ** -20
+    flat = base.copy()                                                               # z all zeros, signed
+    flat[:, 2] = np.where(rng.random(n_pts) < 0.5, 0.0, -0.0)
+    idx = rng.integers(0, n_pts, (2400, 3))
+    meshes = [M(base, idx), M(wide, idx), M(grow, idx), M(flat, idx)]
+    build_and_check(gpu_ctx, port, meshes)
+
+
 def test_bad_index(gpu_ctx):
     with pytest.raises(capi.CgError) as e:
         gpu_ctx.build_trees([M(np.zeros((3, 3)), [[0, 1, 3]])])
