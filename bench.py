@@ -155,7 +155,7 @@ def run_tree_build(ctx, sc, cpu_seconds: float, reps: int = 10, device: int = 0)
     line = {"workload": f"OBB trees of the scene's {len(sc.meshes)} meshes ({tris} triangles), one cg_tree_build",
             "ms": ms, "ms_min": float(np.min(times)), "ms_max": float(np.max(times)), "builds": reps,
             "triangles_per_s": tris / (ms / 1e3), "clocks": clocks.summary(),
-            "timing": "host perf_counter around the synchronous call (meshes uploaded, trees uploaded); median of "
+            "timing": "host perf_counter around the synchronous call (meshes read from host memory, trees written to the arenas); median of "
                       f"{reps} builds"}
     if cpu_seconds > 0:
         from concurrent.futures import ThreadPoolExecutor

@@ -125,8 +125,12 @@ typedef struct cg_mesh_view {
  * OBB.cpp:33-166), the centre splits of at most 4 triangles per leaf
  * (OBBtree.cpp:43-108) and the pre-order layout, bit-identical to the
  * reference builder's tree; then each tree is uploaded as by cg_tree_upload.
- * tree_ids[n] out. CG_ERR_BAD_TREE for an index outside its mesh's vertices.
- * Synchronous. */
+ * tree_ids[n] out. CG_ERR_BAD_TREE for an index outside its mesh's vertices
+ * (the first by mesh, then index position; checked on the device). Where the
+ * device reads pageable host memory (Grace), it reads the meshes' arrays
+ * itself (which must be 4-byte aligned host memory); else they are copied.
+ * The environment variable CG_PAGEABLE_ACCESS=0, read when a context is
+ * created, makes the context copy them. Synchronous. */
 int cg_tree_build(cg_ctx* ctx, const cg_mesh_view* meshes, uint32_t n, uint32_t* tree_ids);
 
 /* A tree's sizes, and its whole flat layout back in the form of

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -706,6 +707,12 @@ int cg_create(const cg_config* cfg_in, cg_ctx** out) {
         delete c;
         return CG_ERR_CUDA;
     }
+    // where the device reads pageable host memory (Grace), the tree build
+    // pulls the meshes itself; CG_PAGEABLE_ACCESS=0 keeps the copies
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device) != cudaSuccess) pageable = 0;
+    const char* pa = std::getenv("CG_PAGEABLE_ACCESS");
+    c->pageable_access = pageable && !(pa && pa[0] == '0');
     rc = alloc_buffers(c);
     if (rc != CG_OK) {
         free_buffers(c);

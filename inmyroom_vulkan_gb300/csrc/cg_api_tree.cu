@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -44,16 +45,7 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
         const cg_mesh_view& m = meshes[i];
         if (m.n_triangles && (!m.positions || !m.indices))
             return fail(c, CG_ERR_INVALID_ARGUMENT, "mesh %u has null positions or indices", i);
-        // the largest index first (a loop the compiler vectorises), the
-        // offending place only when there is one
-        uint32_t mx = 0;
-        const uint64_t k3 = 3ull * m.n_triangles;
-        for (uint64_t k = 0; k < k3; ++k) mx = std::max(mx, m.indices[k]);
-        if (k3 && mx >= m.n_vertices)
-            for (uint64_t k = 0; k < k3; ++k)
-                if (m.indices[k] >= m.n_vertices)
-                    return fail(c, CG_ERR_BAD_TREE, "mesh %u index %llu is vertex %u of %u", i, (unsigned long long)k,
-                                m.indices[k], m.n_vertices);
+        // vertex indices are checked on the device, as the triangles are gathered
         any_normals |= m.normals != nullptr && m.n_triangles;
         base[i + 1] = base[i] + m.n_triangles;
         vbase[i + 1] = vbase[i] + (m.n_triangles ? m.n_vertices : 0u);
@@ -76,7 +68,14 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     const size_t oPerm = take(4 * T), oScr = take(4 * T), oOwn = take(4 * T);
     const size_t oD = take(sizeof(double) * 9 * T), oTm = take(sizeof(double) * 18 * T);
     const size_t oMom = take(sizeof(double) * 9 * std::max<uint64_t>(T, n));  // a level: one node per triangle, or the roots
-    const size_t oNodes = take(sizeof(BuildNode) * cap), oFlat = take(sizeof(BuildFlat) * cap), oCtr = take(16);
+    // counters: next node, error, large nodes by level parity; then the first bad vertex index
+    struct LevelState {
+        uint32_t ctr[4];
+        unsigned long long bad;
+    };
+    const size_t oNodes = take(sizeof(BuildNode) * cap), oFlat = take(sizeof(BuildFlat) * cap),
+                 oCtr = take(sizeof(LevelState));
+    const size_t oSegs = take(sizeof(PullSeg) * 3 * n);
     // a level's nodes of more than kBuildBig triangles: the roots, or disjoint
     // ranges of more than kBuildBig triangles each
     const uint64_t big_cap = n + T / (kBuildBig + 1) + 1;
@@ -112,6 +111,7 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     BuildFlat* flat = reinterpret_cast<BuildFlat*>(mem + oFlat);
     bp.node_ctr = reinterpret_cast<uint32_t*>(mem + oCtr);
     bp.error = bp.node_ctr + 1;
+    in.bad = reinterpret_cast<unsigned long long*>(mem + oCtr + offsetof(LevelState, bad));
     bp.node_cap = cap;
     bp.T = uint32_t(total);
     uint32_t* big_list[2] = {reinterpret_cast<uint32_t*>(mem + oBig), reinterpret_cast<uint32_t*>(mem + oBig) + big_cap};
@@ -124,18 +124,32 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
     in.vertices = d_V;
     in.normals = d_NV;
     in.indices = d_idx;
-    // the meshes' buffers, one after another
+    // the meshes' buffers, one after another: pulled by the device from the
+    // caller's arrays where it reads pageable host memory, else copied
     std::vector<BuildMesh> mt(n);
     std::vector<BuildNode> roots(n);
+    std::vector<PullSeg> segs;
+    uint64_t seg_max = 0;
+    auto pull = [&](const void* src, void* dst, uint64_t words) {
+        segs.push_back(PullSeg{static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst), words});
+        seg_max = std::max(seg_max, words);
+    };
     for (uint32_t i = 0; i < n; ++i) {
         const cg_mesh_view& m = meshes[i];
-        mt[i] = BuildMesh{uint32_t(vbase[i]), (m.normals && m.n_triangles) ? 1u : 0u, uint32_t(base[i]), 0u};
+        mt[i] = BuildMesh{uint32_t(vbase[i]), (m.normals && m.n_triangles) ? 1u : 0u, uint32_t(base[i]),
+                          m.n_triangles ? m.n_vertices : 0u};
         roots[i] = BuildNode{};
         roots[i].begin = uint32_t(base[i]);
         roots[i].count = m.n_triangles;
         roots[i].kid = kNoKid;
         roots[i].tree = i;
         if (!m.n_triangles) continue;
+        if (c->pageable_access) {
+            if (m.n_vertices) pull(m.positions, d_V + 3 * vbase[i], 3ull * m.n_vertices);
+            if (m.normals && m.n_vertices) pull(m.normals, d_NV + 3 * vbase[i], 3ull * m.n_vertices);
+            pull(m.indices, d_idx + 3 * base[i], 3ull * m.n_triangles);
+            continue;
+        }
         CG_CUDA(cudaMemcpyAsync(d_V + 3 * vbase[i], m.positions, sizeof(float) * 3 * m.n_vertices,
                                 cudaMemcpyHostToDevice, s),
                 "upload vertices");
@@ -147,13 +161,19 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
                                 cudaMemcpyHostToDevice, s),
                 "upload indices");
     }
-    const uint32_t ctr0[4] = {n, 0u, 0u, 0u};
+    if (!segs.empty()) {
+        PullSeg* d_segs = reinterpret_cast<PullSeg*>(mem + oSegs);
+        CG_CUDA(cudaMemcpyAsync(d_segs, segs.data(), sizeof(PullSeg) * segs.size(), cudaMemcpyHostToDevice, s),
+                "upload mesh table");
+        CG_CUDA(launch_build_pull(d_segs, uint32_t(segs.size()), seg_max, s), "pull meshes");
+    }
+    const LevelState st0{{n, 0u, 0u, 0u}, ~0ull};
     std::vector<uint32_t> big_roots;
     for (uint32_t i = 0; i < n; ++i)
         if (roots[i].count > kBuildBig) big_roots.push_back(i);
     CG_CUDA(cudaMemcpyAsync(d_mesh, mt.data(), sizeof(BuildMesh) * n, cudaMemcpyHostToDevice, s), "upload meshes");
     CG_CUDA(cudaMemcpyAsync(bp.nodes, roots.data(), sizeof(BuildNode) * n, cudaMemcpyHostToDevice, s), "upload roots");
-    CG_CUDA(cudaMemcpyAsync(bp.node_ctr, ctr0, sizeof(ctr0), cudaMemcpyHostToDevice, s), "upload counter");
+    CG_CUDA(cudaMemcpyAsync(bp.node_ctr, &st0, sizeof(st0), cudaMemcpyHostToDevice, s), "upload counter");
     if (!big_roots.empty())
         CG_CUDA(cudaMemcpyAsync(big_list[0], big_roots.data(), sizeof(uint32_t) * big_roots.size(),
                                 cudaMemcpyHostToDevice, s),
@@ -174,13 +194,19 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
         levels.emplace_back(lo, hi);
         CG_CUDA(cudaMemsetAsync(bp.n_big_out, 0, sizeof(uint32_t), s), "clear large node count");
         CG_CUDA(launch_build_level(bp, sms, s), "build level kernels");
-        uint32_t ctr[4];
-        CG_CUDA(cudaMemcpyAsync(ctr, bp.node_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read node count");
+        LevelState st;
+        CG_CUDA(cudaMemcpyAsync(&st, bp.node_ctr, sizeof(st), cudaMemcpyDeviceToHost, s), "read node count");
         CG_CUDA(cudaStreamSynchronize(s), "build level");
-        if (ctr[1]) return fail(c, CG_ERR_OUT_OF_MEMORY, "tree build ran out of node slots");
+        if (st.bad != ~0ull) {
+            const uint32_t i = uint32_t(st.bad >> 32);
+            const uint64_t k = st.bad & 0xffffffffull;
+            return fail(c, CG_ERR_BAD_TREE, "mesh %u index %llu is vertex %u of %u", i, (unsigned long long)k,
+                        meshes[i].indices[k], meshes[i].n_vertices);
+        }
+        if (st.ctr[1]) return fail(c, CG_ERR_OUT_OF_MEMORY, "tree build ran out of node slots");
         lo = hi;
-        hi = std::min(ctr[0], cap);
-        n_big = ctr[2 + out];
+        hi = std::min(st.ctr[0], cap);
+        n_big = st.ctr[2 + out];
     }
     const uint32_t n_nodes = hi;
     // the pre-order layout: subtree sizes bottom-up, places top-down

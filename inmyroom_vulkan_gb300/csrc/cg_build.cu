@@ -901,23 +901,57 @@ __global__ void build_owner_kernel(const BuildParams B, const BuildInput I, uint
     }
 }
 
+// A vertex index out of its mesh's range is recorded (the smallest mesh, then
+// index position, in I.bad) and its corner read as vertex 0, or as zeros for
+// a mesh without vertices; the host then fails the build.
 __global__ void build_gather_kernel(const BuildParams B, const BuildInput I) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < B.T; g += gridDim.x * blockDim.x) {
         const uint32_t m = B.own[g];
         const BuildMesh M = I.meshes[m];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const uint32_t vi = I.indices[3ull * g + k];
-            const float* v = I.vertices + 3ull * (M.vbase + vi);
+            uint32_t vi = I.indices[3ull * g + k];
+            if (vi >= M.n_vertices) {
+                atomicMin(I.bad, (unsigned long long)m << 32 | (3ull * (g - M.tbase) + k));
+                vi = 0;
+            }
             float* o = I.P + 9ull * g + 3 * k;
+            float* on = M.has_normals ? I.corner_normals + 9ull * g + 3 * k : nullptr;
+            if (M.n_vertices == 0u) {
+                o[0] = o[1] = o[2] = 0.f;
+                if (on) on[0] = on[1] = on[2] = 0.f;
+                continue;
+            }
+            const float* v = I.vertices + 3ull * (M.vbase + vi);
             o[0] = v[0], o[1] = v[1], o[2] = v[2];
-            if (M.has_normals) {
+            if (on) {
                 const float* nv = I.normals + 3ull * (M.vbase + vi);
-                float* on = I.corner_normals + 9ull * g + 3 * k;
                 on[0] = nv[0], on[1] = nv[1], on[2] = nv[2];
             }
         }
         B.perm[g] = g;
+    }
+}
+
+// The meshes' host arrays into the build's input buffers, read by the device
+// (pageable host memory, where the device reads it): block (x, y) copies
+// words [x kPullWords, (x + 1) kPullWords) of segment y, each thread's loads
+// issued before its stores.
+constexpr uint32_t kPullThreads = 256, kPullPer = 16, kPullWords = kPullThreads * kPullPer;
+__global__ void __launch_bounds__(kPullThreads) build_pull_kernel(const PullSeg* segs) {
+    const PullSeg S = segs[blockIdx.y];
+    const uint64_t base = uint64_t(blockIdx.x) * kPullWords;
+    if (base >= S.n) return;
+    uint32_t v[kPullPer];
+#pragma unroll
+    for (uint32_t k = 0; k < kPullPer; ++k) {
+        const uint64_t w = base + k * kPullThreads + threadIdx.x;
+        if (w < S.n) v[k] = S.src[w];
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kPullPer; ++k) {
+        const uint64_t w = base + k * kPullThreads + threadIdx.x;
+        if (w < S.n) S.dst[w] = v[k];
     }
 }
 
@@ -1066,6 +1100,17 @@ cudaError_t launch_build_gather(const BuildParams& p, const BuildInput& in, uint
                                 cudaStream_t s) {
     if (p.T && n_meshes) build_owner_kernel<<<grid_of(p.T, sm_count), 128, 0, s>>>(p, in, n_meshes);
     if (p.T) build_gather_kernel<<<grid_of(p.T, sm_count), 128, 0, s>>>(p, in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_pull(const PullSeg* segs, uint32_t n_segs, uint64_t max_words, cudaStream_t s) {
+    if (!n_segs || !max_words) return cudaSuccess;
+    const uint64_t gx = (max_words + kPullWords - 1u) / kPullWords;
+    if (gx > 0x7fffffffull) return cudaErrorInvalidValue;
+    for (uint32_t first = 0; first < n_segs; first += 65535u) {  // the grid's y extent
+        const uint32_t ny = n_segs - first < 65535u ? n_segs - first : 65535u;
+        build_pull_kernel<<<dim3(uint32_t(gx), ny), kPullThreads, 0, s>>>(segs + first);
+    }
     return cudaGetLastError();
 }
 

@@ -102,6 +102,7 @@ struct cg_ctx {
     cg_config cfg{};
     int device = 0;
     int sm_count = 0;
+    int pageable_access = 0;     // the device reads pageable host memory (cudaDevAttrPageableMemoryAccess)
     cudaStream_t stream = nullptr;
     uint32_t blocks = 0;         // persistent traversal grid
     uint32_t narrow_blocks = 0;  // persistent narrow-phase grid

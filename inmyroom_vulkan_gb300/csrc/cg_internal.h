@@ -470,7 +470,7 @@ struct BuildMesh {
     uint32_t vbase;          // first vertex in BuildInput::vertices / normals
     uint32_t has_normals;
     uint32_t tbase;          // first triangle position
-    uint32_t pad;
+    uint32_t n_vertices;
 };
 struct BuildInput {
     const BuildMesh* meshes;
@@ -479,7 +479,16 @@ struct BuildInput {
     const uint32_t* indices; // [triangles][3] mesh-local vertex indices
     float* P;                // [triangles][3][3] out: corners
     float* corner_normals;   // [triangles][3][3] out: corner normals
+    unsigned long long* bad; // out: the smallest (mesh << 32 | index position) whose vertex index is out of range
 };
+// One host array copied into the build's input buffers by the device itself
+// (where it reads pageable host memory): n 4-byte words from src to dst.
+struct PullSeg {
+    const uint32_t* src;
+    uint32_t* dst;
+    uint64_t n;
+};
+cudaError_t launch_build_pull(const PullSeg* segs, uint32_t n_segs, uint64_t max_words, cudaStream_t s);
 struct BuildFlat {           // a node's place in its tree's layout
     uint32_t inner;          // inner nodes of its subtree
     uint32_t index;          // pre-order index (inner nodes)

@@ -121,6 +121,30 @@ def test_bad_index(gpu_ctx):
     assert e.value.code == capi.CG_ERR_BAD_TREE
 
 
+@pytest.mark.parametrize("pageable", ["1", "0"])
+def test_mesh_input_paths(port, monkeypatch, pageable):
+    """The meshes read by the device from the caller's arrays (where it reads
+    pageable host memory) or copied (CG_PAGEABLE_ACCESS=0): the same trees;
+    the first bad vertex index by mesh, then position, is the one reported,
+    and the context builds again afterwards."""
+    monkeypatch.setenv("CG_PAGEABLE_ACCESS", pageable)
+    rng = np.random.default_rng(5)
+    pts = rng.normal(size=(300, 3)).astype(np.float32)
+    good = [M(pts, rng.integers(0, 300, (700, 3)), pts), M(pts[:40], rng.integers(0, 40, (60, 3)))]
+    with capi.Context() as ctx:
+        build_and_check(ctx, port, good)
+        bad_a = np.array(good[1].indices)
+        bad_a[17, 2] = 40
+        bad_a[30, 0] = 99
+        bad_b = np.array(good[0].indices)
+        bad_b[3, 1] = 300
+        with pytest.raises(capi.CgError) as e:
+            ctx.build_trees([good[0], M(pts[:40], bad_a), M(pts, bad_b)])
+        assert e.value.code == capi.CG_ERR_BAD_TREE
+        assert "mesh 1 index 53 is vertex 40 of 40" in str(e.value)
+        build_and_check(ctx, port, good)
+
+
 def test_built_trees_collide_like_uploaded(gpu_ctx, port):
     """The scene step on GPU-built trees: the same colliding pairs as on the
     oracle's uploaded trees."""
