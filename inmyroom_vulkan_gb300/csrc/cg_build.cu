@@ -245,22 +245,48 @@ __device__ __forceinline__ long long block_scan_ll(long long v, long long* sh, l
 // A NaN payload that no sum produces: the mean is left to a chain.
 constexpr long long kChainDue = 0x7ff4c4a1d0e00000ll;
 
+// Whether count * 2^q is a double: its significant bits span at most 53.
+__device__ __forceinline__ bool fits_double(long long count) {
+    if (count == 0) return true;
+    const unsigned long long m = count < 0 ? 0ull - (unsigned long long)count : (unsigned long long)count;
+    return (64 - __clzll((long long)m)) - (__ffsll((long long)m) - 1) <= 53;
+}
+
+// count rounded to a double's 53 significant bits, to nearest, ties to even
+// (the sequential sum's add; count * 2^q stays in the normal range).
+__device__ __forceinline__ long long round_double(long long count) {
+    if (fits_double(count)) return count;
+    const bool neg = count < 0;
+    const unsigned long long m = neg ? 0ull - (unsigned long long)count : (unsigned long long)count;
+    const int d = (64 - __clzll((long long)m)) - 53;
+    unsigned long long k = m >> d;
+    const unsigned long long rem = m & ((1ull << d) - 1ull), half = 1ull << (d - 1);
+    if (rem > half || (rem == half && (k & 1ull))) ++k;
+    const long long r = (long long)(k << d);
+    return neg ? -r : r;
+}
+
+constexpr uint32_t kSumChunk = 32;   // consecutive terms a thread adds up at a time
+constexpr uint32_t kSumRounds = 64;  // roundings replayed before a sum is left to the chain
+
 // A block per node of the level's list of nodes of more than kBuildBig
-// triangles: the coordinate sums of build_sums_kernel without the chain where
-// the chain makes no rounding. Its terms are floats, integer multiples of
-// 2^q (q the smallest exponent of their ulps); when the exact running sums,
-// counted in units of 2^q, all stay below 2^53 (checked with an exact 64-bit
-// prefix sum, whose terms are bounded so that it cannot overflow), every add
-// of the sequential sum is exact, and the sum is the exact total, whatever the
-// order of its adds. A coordinate that fails the check (or holds a non-finite
-// value) is marked due (kChainDue) and summed by build_sums_due's chain.
+// triangles: the coordinate sums of build_sums_kernel without the chain. The
+// terms are floats, integer multiples of 2^q (q the smallest exponent of
+// their ulps), so the sequential sum is replayed exactly in 64-bit integer
+// counts of 2^q (the terms are bounded so that no running sum can overflow):
+// the running sums from a start are computed in parallel, a tile of 32-term
+// chunks at a time (chunk sums, their exclusive scan in shared memory, then
+// each chunk's running sums term by term), up to the first one that is not a
+// double. That add is the first that rounds; its rounded value is the next
+// start. A sum that rounds more than kSumRounds times, or holds a non-finite
+// term, is marked due (kChainDue) and summed by build_sums_due's chain.
 __global__ void __launch_bounds__(kBigWarps * 32) build_sums_big_kernel(const BuildParams B) {
     constexpr uint32_t NT = kBigWarps * 32u;
     __shared__ int s_q[kBigWarps][3], s_e[kBigWarps][3];
     __shared__ long long s_sc[kBigWarps];
-    __shared__ unsigned long long s_mx[kBigWarps][3];
-    __shared__ long long s_tot[3];
-    __shared__ int s_ok[3];
+    __shared__ long long s_chunk[NT];
+    __shared__ unsigned s_hit;
+    __shared__ long long s_start;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     const uint64_t n3 = 3ull * B.T;
     for (uint32_t i = blockIdx.x; i < B.n_big; i += gridDim.x) {
@@ -268,14 +294,11 @@ __global__ void __launch_bounds__(kBigWarps * 32) build_sums_big_kernel(const Bu
         const BuildNode& N = B.nodes[id];
         const uint32_t np = 3u * N.count;
         const double* x0 = B.D + 3ull * N.begin;
-        // this thread's consecutive corners [j0, j1)
-        const uint32_t L = (np + NT - 1u) / NT;
-        const uint32_t j0 = min(np, tid * L), j1 = min(np, j0 + L);
         // the smallest ulp exponent and the largest exponent of the non-zero terms
         int q[3], e[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) q[c] = INT_MAX, e[c] = INT_MIN;
-        for (uint32_t j = j0; j < j1; ++j)
+        for (uint32_t j = tid; j < np; j += NT)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const long long b = __double_as_longlong(x0[c * n3 + j]);
@@ -295,62 +318,83 @@ __global__ void __launch_bounds__(kBigWarps * 32) build_sums_big_kernel(const Bu
 #pragma unroll
             for (int c = 0; c < 3; ++c) s_q[w][c] = q[c], s_e[w][c] = e[c];
         __syncthreads();
-        bool use[3];  // the terms' counts cannot overflow 64 bits in any running sum
         const int lg = 32 - __clz(np - 1u);  // ceil(log2(np)), np > 1
-#pragma unroll
+        const uint32_t n_chunks = (np + kSumChunk - 1u) / kSumChunk;
         for (int c = 0; c < 3; ++c) {
-            for (uint32_t k = 0; k < kBigWarps; ++k) q[c] = min(q[c], s_q[k][c]), e[c] = max(e[c], s_e[k][c]);
-            // |term| < 2^(e + 1), so |count| < 2^(e + 1 - q); np of them < 2^63
-            use[c] = e[c] == INT_MIN || (e[c] < 1024 && lg + e[c] + 1 - q[c] <= 63);
-        }
-        // the counts' sums: the thread's, then the running sums from the
-        // threads before it, and their largest magnitude
-        long long loc[3] = {0, 0, 0};
-        for (uint32_t j = j0; j < j1; ++j)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                if (use[c] && e[c] != INT_MIN) loc[c] += units_of(x0[c * n3 + j], q[c]);
-        long long run[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const long long tot = block_scan_ll<kBigWarps>(loc[c], s_sc, run[c]);
-            if (tid == 0u) s_tot[c] = tot;
-        }
-        unsigned long long mx[3] = {0, 0, 0};
-        for (uint32_t j = j0; j < j1; ++j)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                if (use[c] && e[c] != INT_MIN) {
-                    run[c] += units_of(x0[c * n3 + j], q[c]);
-                    mx[c] = max(mx[c], (unsigned long long)(run[c] < 0 ? -run[c] : run[c]));
+            int qc = INT_MAX, ec = INT_MIN;
+            for (uint32_t k = 0; k < kBigWarps; ++k) qc = min(qc, s_q[k][c]), ec = max(ec, s_e[k][c]);
+            double m = 0.0;  // every term a zero: +0, as the chain from +0 gives
+            // |term| < 2^(e + 1), so |count| < 2^(e + 1 - q); np of them, and
+            // the drift of the replayed roundings, < 2^63
+            if (ec != INT_MIN && !(ec < 1024 && lg + ec + 1 - qc <= 62)) {
+                m = __longlong_as_double(kChainDue);
+            } else if (ec != INT_MIN) {
+                const double* x = x0 + c * n3;
+                long long start = 0;  // the sequential sum before term k0, in counts of 2^q
+                uint32_t k0 = 0, rounds = 0;
+                bool due = false;
+                while (k0 < np) {
+                    // running sums from (k0, start), a tile of chunks at a time,
+                    // up to the first that is not a double
+                    uint32_t c0 = k0 / kSumChunk, hit = 0xffffffffu;
+                    long long carry = start;
+                    for (;;) {
+                        const uint32_t ch = c0 + tid;
+                        const uint32_t j0 = max(k0, ch * kSumChunk), j1 = min(np, ch * kSumChunk + kSumChunk);
+                        long long sum = 0;
+                        if (ch < n_chunks) {
+#pragma unroll 8
+                            for (uint32_t j = j0; j < j1; ++j) sum += units_of(x[j], qc);
+                        }
+                        long long before;
+                        const long long tile = block_scan_ll<kBigWarps>(sum, s_sc, before);
+                        if (tid == 0u) s_hit = 0xffffffffu;
+                        __syncthreads();
+                        if (ch < n_chunks) {
+                            long long r = carry + before;
+#pragma unroll 8
+                            for (uint32_t j = j0; j < j1; ++j) {
+                                r += units_of(x[j], qc);
+                                if (!fits_double(r)) {
+                                    atomicMin(&s_hit, j);
+                                    break;
+                                }
+                            }
+                            s_chunk[tid] = carry + before;
+                        }
+                        __syncthreads();
+                        hit = s_hit;
+                        if (hit != 0xffffffffu || c0 + NT >= n_chunks) {
+                            if (hit == 0xffffffffu) start = carry + tile;
+                            break;
+                        }
+                        carry += tile;
+                        c0 += NT;
+                        __syncthreads();  // s_hit and s_chunk are rewritten by the next tile
+                    }
+                    if (hit == 0xffffffffu) break;  // no add rounds from k0 on: start is the sum
+                    if (tid == 0u) {  // the add of term hit rounds: the sum so far, rounded
+                        const uint32_t ch = hit / kSumChunk;
+                        long long r = s_chunk[ch - c0];
+                        for (uint32_t j = max(k0, ch * kSumChunk); j <= hit; ++j) r += units_of(x[j], qc);
+                        s_start = round_double(r);
+                    }
+                    __syncthreads();
+                    start = s_start;
+                    k0 = hit + 1u;
+                    __syncthreads();  // s_start, s_hit and s_chunk are rewritten by the next round
+                    if (++rounds > kSumRounds) {
+                        due = true;
+                        break;
+                    }
                 }
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int o = 16; o; o >>= 1) mx[c] = max(mx[c], __shfl_xor_sync(kAll, mx[c], o));
-        if (lane == 0u)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) s_mx[w][c] = mx[c];
-        __syncthreads();
-        if (tid < 3u) {
-            const int c = int(tid);
-            unsigned long long m = 0;
-            for (uint32_t k = 0; k < kBigWarps; ++k) m = max(m, s_mx[k][c]);
-            s_ok[c] = use[c] && m < (1ull << 53);
-        }
-        __syncthreads();
-        if (tid < 3u) {
-            const int c = int(tid);
-            double m = __longlong_as_double(kChainDue);
-            if (s_ok[c]) {
-                double s = 0.0;  // every term a zero: +0, as the chain from +0 gives
-                if (e[c] != INT_MIN)  // |total| < 2^53 counts of 2^q, q >= -149: exact
-                    s = __ll2double_rn(s_tot[c]) * __longlong_as_double((long long)(q[c] + 1023) << 52);
-                m = s / double(np);
+                // exact: start * 2^q, q >= -149
+                m = due ? __longlong_as_double(kChainDue)
+                        : __ll2double_rn(start) * __longlong_as_double((long long)(qc + 1023) << 52) / double(np);
             }
-            B.mom[9ull * (id - B.lo) + c] = m;
+            if (tid == 0u) B.mom[9ull * (id - B.lo) + c] = m;
+            __syncthreads();  // shared memory is reused by the next coordinate
         }
-        __syncthreads();  // shared memory is reused by the next node
     }
 }
 

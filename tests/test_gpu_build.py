@@ -99,8 +99,9 @@ def test_degenerate_meshes(gpu_ctx, port):
 
 def test_large_node_sums(gpu_ctx, port):
     """Nodes of more than 256 triangles take their coordinate sums without the
-    chain when no add of it rounds: meshes whose sums round, one coordinate or
-    all, or hold only zeros, against the oracle's sequential sums."""
+    chain, replaying its roundings: meshes whose sums cannot be replayed (one
+    coordinate or all), round a few times or too often, or hold only zeros,
+    against the oracle's sequential sums."""
     rng = np.random.default_rng(11)
     n_pts = 1500
     base = rng.normal(size=(n_pts, 3)).astype(np.float32)
@@ -112,6 +113,15 @@ def test_large_node_sums(gpu_ctx, port):
     flat[:, 2] = np.where(rng.random(n_pts) < 0.5, 0.0, -0.0)
     idx = rng.integers(0, n_pts, (2400, 3))
     meshes = [M(base, idx), M(wide, idx), M(grow, idx), M(flat, idx)]
+    # y near 20 with a few values near 2^-20: the sequential y sum rounds 33
+    # times (replayed), or 65 and more (more than the replay takes: the chain)
+    for frac in (0.005, 0.05):
+        t = base.copy()
+        r2 = np.random.default_rng(12)
+        sel = r2.random(n_pts) < frac
+        t[:, 1] += np.float32(20.0)
+        t[sel, 1] = ((1.0 + r2.random(sel.sum())) * 2.0 ** -20).astype(np.float32)
+        meshes.append(M(t, idx))
     build_and_check(gpu_ctx, port, meshes)
 
 
