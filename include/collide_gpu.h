@@ -310,7 +310,8 @@ int cg_read_ray_averages(cg_ctx* ctx, cg_ray_average* out, uint64_t cap, uint64_
  * the device can write: page-locked (cudaHostAlloc, cudaHostRegister), or any
  * host memory where the device accesses pageable memory (Grace); 16-byte
  * aligned; valid until replaced. The pairs are copied while the contact
- * kernels run. A NULL pointer
+ * kernels run; the rays and averages are written by the contact kernels that
+ * make them. A NULL pointer
  * or zero capacity leaves that result on the device only. Results are still
  * readable with the cg_read_* calls. Does not apply to cg_collide_async and
  * cg_graph_launch. */

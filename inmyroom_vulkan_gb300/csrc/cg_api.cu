@@ -381,7 +381,7 @@ void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta, uint32_t
 // pairs_copy: with the step's colliding pairs final (after the narrow phase),
 // copy them out on a branch that runs beside the contact kernels.
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s,
-                 const CopyOutParams* pairs_copy) {
+                 const CopyOutParams* pairs_copy, const CopyOutParams* results_copy) {
     c->last_n = n;
     unsigned int* trace = (flags & CG_TRACE) ? c->d_trace : nullptr;
     const uint32_t trace_ns = c->trace_ns ? c->trace_ns : 1000u;
@@ -492,6 +492,12 @@ int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flag
         cp.rays = t.rays;
         cp.max_rays = t.max_rays;
         cp.averages = t.averages;
+        if (results_copy) {  // a null buffer takes nothing
+            cp.host_rays = results_copy->host_rays;
+            cp.host_rays_cap = cp.host_rays ? results_copy->host_rays_cap : 0;
+            cp.host_averages = results_copy->host_averages;
+            cp.host_averages_cap = cp.host_averages ? results_copy->host_averages_cap : 0;
+        }
         cp.ctr = c->d_ctr;
         for (uint32_t k = 0; k < c->n_sched; ++k) {
             cp.sched_start[k] = c->sched_start[k];
@@ -998,9 +1004,10 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
     if (n) std::memcpy(c->h_queries, queries, sizeof(cg_query) * n);
     c->last_flags = flags;
     c->last_n = n;
-    // The whole step (query upload from the pinned staging buffer, kernels,
-    // counter read-back) is one CUDA graph, captured once per (n, flags) and
-    // tree-storage generation and replayed.
+    // The whole step (kernels, counter read-back) is one CUDA graph, captured
+    // once per (n, flags) and tree-storage generation and replayed; the pack
+    // kernel reads the queries from the pinned staging buffer through the
+    // device's mapping of it.
     auto& G = c->host_graph;
     if (!G.exec || G.n != n || G.flags != flags || G.gen != arena_gen(c) ||
         G.out_gen != c->host_out.gen) {
@@ -1009,11 +1016,11 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
         CG_CUDA(cudaStreamSynchronize(c->stream), "sync before capture");
         CG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         c->capturing = true;
-        cudaError_t e = cudaSuccess;
-        if (n)
-            e = cudaMemcpyAsync(c->d_queries, c->h_queries, sizeof(cg_query) * n, cudaMemcpyHostToDevice, c->stream);
+        void* q_dev = nullptr;
+        cudaError_t e = cudaHostGetDevicePointer(&q_dev, c->h_queries, 0);
         // results to the host buffers: the pairs on a branch beside the
-        // contact kernels, the rays and averages after them
+        // contact kernels, the rays and averages by the contact kernels that
+        // make them
         CopyOutParams pc{}, rc2{};
         pc.ctr = rc2.ctr = c->d_ctr;
         pc.pairs = c->d_pairs;
@@ -1028,9 +1035,9 @@ int cg_collide(cg_ctx* c, const cg_query* queries, uint32_t n, uint32_t flags, c
         rc2.averages = c->ct.averages;
         rc2.host_averages = contacts ? c->host_out.averages : nullptr;
         rc2.host_averages_cap = c->host_out.averages_cap;
-        int rc = e == cudaSuccess ? enqueue_step(c, c->d_queries, n, flags, c->stream, pc.host_pairs ? &pc : nullptr)
+        int rc = e == cudaSuccess ? enqueue_step(c, static_cast<const cg_query*>(q_dev), n, flags, c->stream,
+                                                 pc.host_pairs ? &pc : nullptr, &rc2)
                                   : CG_ERR_CUDA;
-        if (rc == CG_OK && (rc2.host_rays || rc2.host_averages)) e = launch_copy_out(rc2, c->copy_blocks, c->stream);
         if (rc == CG_OK && e == cudaSuccess)
             e = cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream);
         c->capturing = false;

@@ -1574,18 +1574,21 @@ __device__ void order_map(const ContactParams& P, uint32_t map, uint32_t* smem, 
         // a side without rays), the second side's moved back to its space
         const float cnt_f = float(n_rays);
         float3 avg = divs3(make_float3(fold[0], fold[1], fold[2]), cnt_f);
-        cg_ray_average* A = P.averages + q;
-        if (side) {
-            avg = xform(inverse4(query_mat(P.q + q)), avg, 1.0f);
-            A->second[0] = avg.x;
-            A->second[1] = avg.y;
-            A->second[2] = avg.z;
-            A->rays_second = n_rays;
-        } else {
-            A->first[0] = avg.x;
-            A->first[1] = avg.y;
-            A->first[2] = avg.z;
-            A->rays_first = n_rays;
+        if (side) avg = xform(inverse4(query_mat(P.q + q)), avg, 1.0f);
+        for (int copy = 0; copy < 2; ++copy) {  // the device's averages, then the host buffer's
+            cg_ray_average* A = copy ? (q < P.host_averages_cap ? P.host_averages + q : nullptr) : P.averages + q;
+            if (!A) break;
+            if (side) {
+                A->second[0] = avg.x;
+                A->second[1] = avg.y;
+                A->second[2] = avg.z;
+                A->rays_second = n_rays;
+            } else {
+                A->first[0] = avg.x;
+                A->first[1] = avg.y;
+                A->first[2] = avg.z;
+                A->rays_first = n_rays;
+            }
         }
         P.map_nr[map] = n_rays;
         if (!ok) P.map_fill[map] = 0u;  // a map that did not fit makes no records
@@ -1621,7 +1624,11 @@ __global__ void __launch_bounds__(256) contacts_emit_kernel(const ContactParams 
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
             if (co + i < P.max_contacts) P.contacts[co + i] = P.ctmp[base + i];
         for (uint32_t r = threadIdx.x; r < nr; r += blockDim.x)
-            if (ro + r < P.max_rays) P.rays[ro + r] = P.rtmp[3ull * base + r];
+            if (ro + r < P.max_rays) {
+                const cg_ray ray = P.rtmp[3ull * base + r];
+                P.rays[ro + r] = ray;
+                if (ro + r < P.host_rays_cap) P.host_rays[ro + r] = ray;
+            }
         __syncthreads();
         if (threadIdx.x == 0) {
             P.map_cnt[map] = 0u;

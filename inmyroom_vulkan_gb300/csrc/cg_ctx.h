@@ -261,7 +261,7 @@ bool growth_schedule(uint32_t max_elems, uint32_t* start, uint32_t* buckets, uin
 int sync_tree_table(cg_ctx* c);
 void put_box(float4* rec, const cg_obb& b, uint32_t ref, uint32_t meta, uint32_t split);
 int enqueue_step(cg_ctx* c, const cg_query* d_queries, uint32_t n, uint32_t flags, cudaStream_t s,
-                 const CopyOutParams* pairs_copy = nullptr);
+                 const CopyOutParams* pairs_copy = nullptr, const CopyOutParams* results_copy = nullptr);
 int stats_from(cg_ctx* c, const Counters& k, cg_stats* st);
 int check_flags(cg_ctx* c, uint32_t flags);
 int join_stream(cg_ctx* c, cudaStream_t s);

@@ -184,6 +184,10 @@ struct ContactParams {
     cg_ray* rays;
     uint32_t max_rays;
     cg_ray_average* averages;
+    cg_ray* host_rays;                  // device alias of the caller's host buffers, or null: the
+    unsigned long long host_rays_cap;   // rays and averages written there too, as the kernels
+    cg_ray_average* host_averages;      // write them
+    unsigned long long host_averages_cap;
     Counters* ctr;
     uint32_t sched_start[kMaxSchedule];
     uint32_t sched_buckets[kMaxSchedule];

@@ -158,7 +158,7 @@ def test_contacts_flag_combinations_and_overflow(port):
 def test_host_outputs_match_the_read_calls(port):
     """cg_set_host_outputs: one cg_collide writes the pairs, rays and
     averages into page-locked host arrays; they equal what the read calls
-    return. A smaller pair capacity takes the first records."""
+    return. A smaller capacity takes the first records."""
     import torch
 
     sc = scenes.scene()
@@ -188,6 +188,13 @@ def test_host_outputs_match_the_read_calls(port):
         ctx.set_host_outputs(small)
         ctx.collide(q)
         assert np.array_equal(small.view(np.uint8), ctx.tri_pairs()[:100].view(np.uint8))
+        # smaller ray and average buffers take the first ones
+        small_r, small_a = pinned(100, capi.RAY_DTYPE), pinned(3, capi.RAY_AVERAGE_DTYPE)
+        ctx.set_host_outputs(None, small_r, small_a)
+        st3 = ctx.collide(q, flags=capi.CG_CONTACTS)
+        assert st3["rays"] == n_r
+        assert np.array_equal(small_r.view(np.uint8), ctx.rays()[:100].view(np.uint8))
+        assert np.array_equal(small_a.view(np.uint8), ctx.ray_averages()[:3].view(np.uint8))
         # pageable memory: refused, unless the device writes pageable host
         # memory directly (as on Grace), and then the results land there too
         pageable = np.zeros(100, capi.TRI_PAIR_DTYPE)
