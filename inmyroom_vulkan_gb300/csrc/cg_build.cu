@@ -17,7 +17,8 @@
 //   build_terms   a thread per triangle position: the six centred products
 //                 of its corners
 //   build_cov     a thread per node and product: the covariance sum in
-//                 corner order
+//                 corner order (build_cov_big: a warp per node of more
+//                 than kBuildBig triangles)
 //   build_eig     a thread per node: eig3 of the covariance in FP64; the
 //                 box axes are the rows of the eigenvector matrix
 //   build_proj    a thread per triangle position: its corners' FP64
@@ -443,7 +444,22 @@ __global__ void build_cov_kernel(const BuildParams B) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         const uint32_t node = B.lo + g / 6u, q = g % 6u;
         const BuildNode& N = B.nodes[node];
+        if (N.count > kBuildBig) continue;  // build_cov_big
         B.mom[9ull * (node - B.lo) + 3u + q] = chain_sum(B.Tm + q * n3 + 3ull * N.begin, 3u * N.count);
+    }
+}
+
+// The same for the list's nodes of more than kBuildBig triangles, a
+// one-warp block each (lanes 0-5 its six chains): a large node's chains
+// share their warp's FP64 instructions and loads with no other node's.
+__global__ void __launch_bounds__(32) build_cov_big_kernel(const BuildParams B) {
+    const uint64_t n3 = 3ull * B.T;
+    const uint32_t q = threadIdx.x;
+    if (q >= 6u) return;
+    for (uint32_t i = blockIdx.x; i < B.n_big; i += gridDim.x) {
+        const uint32_t id = B.big[i];
+        const BuildNode& N = B.nodes[id];
+        B.mom[9ull * (id - B.lo) + 3u + q] = chain_sum(B.Tm + q * n3 + 3ull * N.begin, 3u * N.count);
     }
 }
 
@@ -1124,6 +1140,7 @@ cudaError_t launch_build_level(const BuildParams& p, uint32_t sm_count, cudaStre
     }
     build_terms_kernel<<<grid(p.T), 128, 0, s>>>(p);
     build_cov_kernel<<<grid(6ull * width), 128, 0, s>>>(p);
+    if (p.n_big) build_cov_big_kernel<<<p.n_big < 65535u ? p.n_big : 65535u, 32, 0, s>>>(p);
     build_eig_kernel<<<grid(width), 128, 0, s>>>(p);
     build_proj_kernel<<<grid(p.T), 128, 0, s>>>(p);
     if (p.n_big) build_fit_big_kernel<<<p.n_big < 65535u ? p.n_big : 65535u, kBigWarps * 32u, 0, s>>>(p);
