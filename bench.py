@@ -48,7 +48,7 @@ TRI_TEST_BYTES = 2 * 36    # two triangles
 NODE_PAIR_FLOPS = 714      # SAT worst case ~650 + B-box transform 64
 TRI_TEST_FLOPS = 147       # full non-coplanar Moller path
 COUNTERS_BYTES = 152       # the launch counters, read back by cg_collide and by each result read
-# init, pack, traverse, narrow; contacts: pairs, scan, scatter, fold, order, offsets, emit
+# init, pack, traverse, narrow; contacts: pairs, paths, alloc, scatter, fold, order, emit
 STEP_KERNELS = 11
 STEP_FLAGS_DOC = ("CUDA graph: init + pack + persistent traversal + persistent narrow phase (FP64 recheck counted) "
                   "+ contacts in the reference's order (pairs; alloc, scatter beside the descent paths; fold and "
