@@ -728,16 +728,18 @@ __global__ void __launch_bounds__(256, 3) narrow_kernel(const NarrowParams P) {
     unsigned long long t_base = 0;
     if (P.trace && lane == 0) t_base = trace_base(P.ctr);
 
-    // Each warp's first 32 leaf pairs are fixed by its index; later ones
+    // Each warp's first `per` leaf pairs are fixed by its index; later ones
     // come from the shared counter, past all first rounds. A small list
-    // costs no atomic to the warps it does not reach.
+    // costs no atomic to the warps it does not reach, and is spread over all
+    // warps (per < 32 leaf pairs each) so that its rounds run side by side.
     const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
-    uint32_t first = 32u * (blockIdx.x * (blockDim.x >> 5) + uint32_t(warp));
+    const uint32_t per = n >= 32u * n_warps ? 32u : max(1u, (n + n_warps - 1u) / n_warps);
+    uint32_t first = per * (blockIdx.x * (blockDim.x >> 5) + uint32_t(warp));
     while (first < n) {
-        const uint32_t nl = min(32u, n - first);
+        const uint32_t nl = min(per, n - first);
         narrow_block<kMode>(P, stage, first, nl, lane, tests, fragile, rechecked, disagree, t_base);
         uint32_t next = 0;
-        if (lane == 0) next = 32u * n_warps + atomicAdd(&P.ctr->narrow_lp, 32u);
+        if (lane == 0) next = per * n_warps + atomicAdd(&P.ctr->narrow_lp, per);
         first = __shfl_sync(kFull, next, 0);
     }
     if (lane == 0) {
