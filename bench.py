@@ -813,6 +813,14 @@ def run_gpu(args) -> dict:
     pq = capi.make_queries(np.full(200, pid[0]), np.full(200, pid[1]), prel)
     d_pq = torch.from_numpy(pq.view(np.uint8).copy()).to(dev)
     qsz = capi.QUERY_DTYPE.itemsize
+    # one-query launches get settings of their own from the autotuner (the
+    # scene's are put back afterwards)
+    plain_tune = None
+    if not args.no_tune:
+        from inmyroom_vulkan_gb300 import autotune
+
+        scene_settings = {k: int(getattr(ctx.config(), k)) for k in autotune.SPACE}
+        plain_tune = autotune.tune_collide(ctx, d_pq.data_ptr(), 1, flags, flush=flush).as_dict()
     for i in range(5):
         ctx.collide_async(d_pq.data_ptr() + i * qsz, 1, flags, stream.cuda_stream)
     torch.cuda.synchronize()
@@ -826,6 +834,8 @@ def run_gpu(args) -> dict:
     plain_ms = s0.elapsed_time(s1)
     ctx.collide(pq, flags=flags)
     ptests = ctx.sync_stats()["tri_tests"]
+    if plain_tune:
+        ctx.reconfigure(**scene_settings)
 
     shoot = None
     if rank == 0 and not args.skip_shoot:
@@ -871,7 +881,7 @@ def run_gpu(args) -> dict:
         "roofline_narrow": roof_narrow,
         "plain": {"workload": "rigid pair, 2x2048 tris, 200 poses, one query per launch (with contacts and rays)",
                   "queries_per_s": 200 / (plain_ms / 1e3), "tri_tests_per_s": ptests / (plain_ms / 1e3),
-                  "ms_per_query": plain_ms / 200},
+                  "ms_per_query": plain_ms / 200, "autotune": plain_tune},
         "gpu_launches": STEP_KERNELS * args.steps,
         "clocks": clk,
     }
