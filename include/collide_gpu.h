@@ -128,7 +128,8 @@ typedef struct cg_mesh_view {
  * tree_ids[n] out. CG_ERR_BAD_TREE for an index outside its mesh's vertices
  * (the first by mesh, then index position; checked on the device). Where the
  * device reads pageable host memory (Grace), it reads the meshes' arrays
- * itself (which must be 4-byte aligned host memory); else they are copied.
+ * itself (a mesh whose arrays are not 4-byte aligned is copied); else they
+ * are copied.
  * The environment variable CG_PAGEABLE_ACCESS=0, read when a context is
  * created, makes the context copy them. Synchronous. */
 int cg_tree_build(cg_ctx* ctx, const cg_mesh_view* meshes, uint32_t n, uint32_t* tree_ids);

@@ -144,7 +144,9 @@ int cg_tree_build(cg_ctx* c, const cg_mesh_view* meshes, uint32_t n, uint32_t* t
         roots[i].kid = kNoKid;
         roots[i].tree = i;
         if (!m.n_triangles) continue;
-        if (c->pageable_access) {
+        // the device's 4-byte loads need 4-byte aligned arrays; others are copied
+        auto word_aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) == 0; };
+        if (c->pageable_access && word_aligned(m.positions) && word_aligned(m.normals) && word_aligned(m.indices)) {
             if (m.n_vertices) pull(m.positions, d_V + 3 * vbase[i], 3ull * m.n_vertices);
             if (m.normals && m.n_vertices) pull(m.normals, d_NV + 3 * vbase[i], 3ull * m.n_vertices);
             pull(m.indices, d_idx + 3 * base[i], 3ull * m.n_triangles);

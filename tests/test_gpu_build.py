@@ -155,6 +155,23 @@ def test_mesh_input_paths(port, monkeypatch, pageable):
         build_and_check(ctx, port, good)
 
 
+def test_misaligned_mesh_arrays(gpu_ctx, port):
+    """Mesh arrays 2 bytes off a 4-byte boundary are copied rather than read
+    by the device's 4-byte loads: the same trees."""
+    rng = np.random.default_rng(9)
+    pts = rng.normal(size=(300, 3)).astype(np.float32)
+    idx = rng.integers(0, 300, (500, 3)).astype(np.uint32)
+
+    def shifted(a):
+        buf = np.zeros(a.nbytes + 2, np.uint8)
+        v = buf[2:2 + a.nbytes].view(a.dtype).reshape(a.shape)
+        v[...] = a
+        assert not v.flags.aligned
+        return v
+
+    build_and_check(gpu_ctx, port, [M(shifted(pts), shifted(idx), shifted(pts)), M(pts, shifted(idx))])
+
+
 def test_built_trees_collide_like_uploaded(gpu_ctx, port):
     """The scene step on GPU-built trees: the same colliding pairs as on the
     oracle's uploaded trees."""
