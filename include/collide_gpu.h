@@ -129,7 +129,8 @@ typedef struct cg_mesh_view {
  * (the first by mesh, then index position; checked on the device). Where the
  * device reads pageable host memory (Grace), it reads the meshes' arrays
  * itself (a mesh whose arrays are not 4-byte aligned is copied); else they
- * are copied.
+ * are copied. Either way each array must hold what its counts say
+ * (n_vertices x 3 floats, n_triangles x 3 indices).
  * The environment variable CG_PAGEABLE_ACCESS=0, read when a context is
  * created, makes the context copy them. Synchronous. */
 int cg_tree_build(cg_ctx* ctx, const cg_mesh_view* meshes, uint32_t n, uint32_t* tree_ids);
